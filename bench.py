@@ -1,0 +1,335 @@
+#!/usr/bin/env python3
+"""Benchmark: wavelet matrix + wavelet tree + rank/select construction of a
+1 GiB uint8 text (n = 2^30, Zipf(1.0) over 256 symbols, 8 levels) on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step builds both structures and their rank/select support from a text
+resident in HBM.  `value` is whole-job text GB/s (n bytes per step per rank
+over the max-over-ranks device time); `e2e` is the same metric through the
+public host API (pinned host text in, both structures' bit vectors out).
+Ranks run independent replicas (weak scaling, no collective on the data path).
+`--impl reference` times pwm's parallel CPU construction path (the oracle's
+restatement of wx_ppc + rank/select) on the host cores instead.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "WM/WT build text GB/s"
+N_DEFAULT = 1 << 30
+LEVELS = 8
+CPU_SAMPLE = 1 << 26
+
+
+def workload_config(n, cpu_sample=None):
+    cfg = {"workload": f"one uint8 text of n={n} symbols, Zipf(s=1.0) ranks over 256 symbols mapped by a seeded "
+                       "permutation, levels=8; wavelet matrix + levelwise wavelet tree + rank/select support",
+           "n": n, "word_width": 1, "levels": LEVELS, "structures": ["matrix", "tree"], "rank_select": True,
+           "l2": "inputs larger than L2 (1 GiB text, 2 GiB of bit vectors)", "generator": "pwmgpu_generate ZIPF256"}
+    if cpu_sample:
+        cfg["cpu_sample_n"] = cpu_sample
+    return cfg
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id):
+        self.gpu_id = gpu_id
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100"]
+        if self.gpu_id:
+            cmd += ["-i", self.gpu_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+        if not self.lines:  # very short region: one snapshot
+            cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits"]
+            if self.gpu_id:
+                cmd += ["-i", self.gpu_id]
+            try:
+                self.lines = subprocess.run(cmd, capture_output=True, text=True, timeout=20).stdout.splitlines()
+            except Exception:
+                pass
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """dram bytes per launch of the split pass from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "split_pass_traffic.json")) as f:
+            d = json.load(f)
+        return d.get("dram_bytes_per_launch_full_size")
+    except Exception:
+        return None
+
+
+def parse_profile(text):
+    out = {}
+    for line in text.strip().splitlines():
+        name, groups, launches, ms, nbytes = line.split()
+        out[name] = {"groups": int(groups), "launches": int(launches), "ms": float(ms), "bytes": int(nbytes)}
+    return out
+
+
+def cpu_baseline(n_sample, steps=3):
+    """The oracle's OpenMP restatement of pwm's wx_ppc (matrix + tree) plus
+    rank/select on a bounded sample, all host cores."""
+    import numpy as np
+    import pwm_gb300 as pg
+    from oracle.oracle import Oracle
+    orc = Oracle()
+    text = pg.generate(pg.GEN_ZIPF256, 1, n_sample, 1)
+    threads = os.cpu_count() or 1
+    bufs = orc.cpu_step_buffers(n_sample, LEVELS)
+    orc.cpu_step(text, LEVELS, threads, bufs)  # warm-up (page faults)
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        orc.cpu_step(text, LEVELS, threads, bufs)
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    del np
+    return {"value": n_sample / t / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": f"n={n_sample} uint8 Zipf text, levels=8: matrix + tree (parallel prefix counting, the "
+                      f"oracle's restatement of pwm wx_ppc) + rank/select of all levels; median of {steps} runs",
+            "seconds_per_step": t}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return 0
+    import numpy as np
+    import pwm_gb300 as pg
+    from oracle.oracle import Oracle
+    orc = Oracle()
+    n = CPU_SAMPLE
+    text = pg.generate(pg.GEN_ZIPF256, 1, n, 1)
+    threads = os.cpu_count() or 1
+    bufs = orc.cpu_step_buffers(n, LEVELS)
+    for _ in range(args.warmup):
+        orc.cpu_step(text, LEVELS, threads, bufs)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        orc.cpu_step(text, LEVELS, threads, bufs)
+    dt = (time.perf_counter() - t0) / max(args.steps, 1)
+    value = n / dt / 1e9
+    line = {"metric": METRIC, "value": value, "unit": "GB/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": workload_config(N_DEFAULT, n),
+            "cpu_baseline": {"value": value, "unit": "GB/s", "cores": threads, "kind": "port",
+                             "sample": f"n={n} of the same Zipf distribution per step; pwm's CPU path is run "
+                                       "through the oracle's restatement of wx_ppc + rank/select (the reference's "
+                                       "own build cannot run on this host)"},
+            "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    del np
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--pass-levels", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank)
+
+    import numpy as np
+    import torch
+    import pwm_gb300 as pg
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    stream = torch.cuda.current_stream()
+    ctx = pg.Context(device=local, stream=ctypes_stream(stream))
+    if args.pass_levels:
+        ctx.set_pass_levels(args.pass_levels)
+    n = args.n
+    text = torch.empty(n, dtype=torch.uint8, device="cuda")
+    pg.generate(pg.GEN_ZIPF256, 1 + rank, n, 1, device_ptr=text.data_ptr(), context=ctx)
+    ds = pg.DeviceStructure(n, 1, LEVELS, matrix=True, tree=True, rank_select=True, context=ctx)
+    for _ in range(args.warmup):
+        ds.build(text.data_ptr())
+    ds.check()
+
+    gpu_uuid = None
+    try:
+        gpu_uuid = str(torch.cuda.get_device_properties(local).uuid)
+        if not gpu_uuid.startswith("GPU-"):
+            gpu_uuid = "GPU-" + gpu_uuid
+    except Exception:
+        gpu_uuid = None
+    sampler = ClockSampler(gpu_uuid)
+
+    # ---- device-resident timed region ------------------------------------
+    ctx.lib.pwmgpu_ctx_profile(ctx.h, 1)
+    launches0 = ctx.launches
+    barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    time.sleep(0.3)  # let the sampler start before the region
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        ds.build(text.data_ptr())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    ds.check()
+    launches = ctx.launches - launches0
+    buf = __import__("ctypes").create_string_buffer(1 << 16)
+    ctx.check(ctx.lib.pwmgpu_ctx_profile_read(ctx.h, buf, len(buf)))
+    ctx.lib.pwmgpu_ctx_profile(ctx.h, 0)
+    prof = parse_profile(buf.value.decode())
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n / (ms / 1e3) / 1e9
+
+    # ---- end to end through the public host API --------------------------
+    host_text = text.cpu().pin_memory()
+    vm, vt = ds.view(0), ds.view(1)
+    out_wm = torch.empty(vm.total_words, dtype=torch.int64).pin_memory()
+    out_wt = torch.empty(vt.total_words, dtype=torch.int64).pin_memory()
+    zeros = np.zeros(LEVELS, dtype=np.uint64)
+    zp = zeros.ctypes.data_as(pg._lib.u64p)
+
+    def e2e_step():
+        ctx.check(ctx.lib.pwmgpu_wx_build_host(ctx.h, ds.h, host_text.data_ptr()))
+        ctx.check(ctx.lib.pwmgpu_wx_download(ctx.h, ds.h, 0, pg._lib.u64p(pg._lib.u64(0)) if False else
+                                             __import__("ctypes").cast(out_wm.data_ptr(), pg._lib.u64p), zp))
+        ctx.check(ctx.lib.pwmgpu_wx_download(ctx.h, ds.h, 1, __import__("ctypes").cast(out_wt.data_ptr(),
+                                                                                       pg._lib.u64p), None))
+
+    e2e_step()
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * n / e2e_s / 1e9
+
+    if rank == 0:
+        peak, peak_kind = measured_peak()
+        sp = prof.get("split_pass", {})
+        achieved = (sp["bytes"] / (sp["ms"] / 1e3) / 1e9) if sp.get("ms") else None
+        roof = {"bound": "hbm", "kernel": "split_pass", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
+                "traffic": ncu_traffic(),
+                "algorithmic_bytes_per_launch": (sp["bytes"] / sp["groups"]) if sp.get("groups") else None,
+                "avg_launch_ms": (sp["ms"] / sp["groups"]) if sp.get("groups") else None}
+        # whole step against the roofline of its algorithmic bytes (2 structures + rank/select)
+        words = (n + 63) // 64
+        step_bytes = 2 * LEVELS * (n + 8 * words) + 2 * LEVELS * (8 * words + 8 * (words // 32 + 1))
+        line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": workload_config(n, CPU_SAMPLE),
+                "roofline": roof,
+                "step_roofline": {"algorithmic_bytes": step_bytes, "achieved_gbs": step_bytes / (ms / 1e3) / 1e9,
+                                  "frac": step_bytes / (ms / 1e3) / 1e9 / peak},
+                "kernels": prof, "gpu_launches": launches,
+                "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": n,
+                        "d2h_bytes_per_step": 8 * (vm.total_words + vt.total_words) + 8 * LEVELS,
+                        "seconds_per_step": e2e_s},
+                "clocks": clocks}
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(CPU_SAMPLE)
+        print(json.dumps(line))
+    ds.free()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def ctypes_stream(stream):
+    import ctypes
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,194 @@
+/*
+ * pwmgpu.h -- C ABI of the GB300 wavelet tree / wavelet matrix engine.
+ *
+ * Plain pointers and sizes only.  Every call returns a pwmgpu_status; the
+ * text of the last error of a context is available from
+ * pwmgpu_ctx_last_error().  All work of a context runs in order on the CUDA
+ * stream it was created with.
+ *
+ * Output layout (identical to pwm's bit_vectors, include/arrays/
+ * flat_two_dim_array.hpp:110-213 in kurpicz/pwm): the levels of one
+ * structure are contiguous u64 arrays; level l has ceil(bits_l/64) words and
+ * is padded to a multiple of 16 words (128 bytes) before level l+1 starts.
+ * Position i of a level is bit 63-(i%64) of word i/64; the unused low bits of
+ * the last word are zero (include/construction/building_blocks.hpp:18-50).
+ * A caller holding a pwm bit_vectors object passes bvs[0].data() as `bv`.
+ */
+#ifndef PWMGPU_H
+#define PWMGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define PWMGPU_API __attribute__((visibility("default")))
+#else
+#define PWMGPU_API
+#endif
+
+typedef enum pwmgpu_status {
+  PWMGPU_OK = 0,
+  PWMGPU_ERR_ARG = 1,       /* invalid argument: null pointer, width, levels, sizes  */
+  PWMGPU_ERR_OOM = 2,       /* a device allocation failed                             */
+  PWMGPU_ERR_CUDA = 3,      /* a CUDA runtime call failed                             */
+  PWMGPU_ERR_TIMEOUT = 4,   /* a bounded device-side wait gave up (status word set)   */
+  PWMGPU_ERR_SYMBOL = 5,    /* a text symbol is >= 2^levels                           */
+  PWMGPU_ERR_NO_DEVICE = 6, /* no CUDA device / the library was built for another GPU */
+  PWMGPU_ERR_BUSY = 7       /* serving: admission refused (HBM budget or queue full)  */
+} pwmgpu_status;
+
+/* Which structures a device build produces. */
+#define PWMGPU_MATRIX 0x1u      /* wavelet matrix: bit vectors + zero counts        */
+#define PWMGPU_TREE 0x2u        /* levelwise wavelet tree: bit vectors              */
+#define PWMGPU_RANK_SELECT 0x4u /* popcount rank/select support for every level     */
+#define PWMGPU_HUFFMAN 0x8u     /* Huffman-shaped levels (codes given or built)     */
+
+/* Query kinds for pwmgpu_wx_query. */
+#define PWMGPU_Q_ACCESS 0
+#define PWMGPU_Q_RANK 1
+#define PWMGPU_Q_SELECT 2
+
+typedef struct pwmgpu_ctx pwmgpu_ctx;
+typedef struct pwmgpu_wx pwmgpu_wx;
+
+/* Read-only view of one built structure (device pointers). */
+typedef struct pwmgpu_view {
+  uint32_t levels;
+  uint32_t is_tree;
+  uint32_t is_huffman;
+  uint32_t has_rank_select;
+  uint64_t size;               /* text length n                                   */
+  uint64_t total_words;        /* words of the whole level array                  */
+  const uint64_t* words;       /* device: all levels, flat padded layout          */
+  const uint64_t* level_offset;/* host: word offset of every level (levels)       */
+  const uint64_t* level_bits;  /* host: bits of every level (levels)              */
+  const uint64_t* zeros;       /* host: zero count per level (matrix), else NULL  */
+} pwmgpu_view;
+
+/* ---------------------------------------------------------------------- */
+/* Context                                                                 */
+/* ---------------------------------------------------------------------- */
+
+/* Creates a context on `device`.  `cuda_stream` is a cudaStream_t to run
+ * on, or NULL for a stream owned by the context.  Scratch memory is cached
+ * in the context and reused by later builds. */
+PWMGPU_API pwmgpu_status pwmgpu_ctx_create(int device, void* cuda_stream, pwmgpu_ctx** out);
+PWMGPU_API void pwmgpu_ctx_destroy(pwmgpu_ctx* ctx);
+PWMGPU_API const char* pwmgpu_ctx_last_error(const pwmgpu_ctx* ctx);
+PWMGPU_API const char* pwmgpu_status_string(pwmgpu_status s);
+/* Waits for all work of the context. */
+PWMGPU_API pwmgpu_status pwmgpu_ctx_sync(pwmgpu_ctx* ctx);
+/* Number of kernels this library launched on the context so far. */
+PWMGPU_API uint64_t pwmgpu_ctx_launch_count(const pwmgpu_ctx* ctx);
+/* Profiling: while enabled, CUDA events are recorded on the context's stream
+ * around every kernel launch group.  pwmgpu_ctx_profile_read synchronises and
+ * writes one line per group name, "name groups launches total_ms
+ * algorithmic_bytes", then clears the record. */
+PWMGPU_API pwmgpu_status pwmgpu_ctx_profile(pwmgpu_ctx* ctx, int enable);
+PWMGPU_API pwmgpu_status pwmgpu_ctx_profile_read(pwmgpu_ctx* ctx, char* buf, uint64_t cap);
+/* Tuning: levels fused into one split pass (1..4, default 4).  A pass reads
+ * its input sequence once and writes the bits of that many levels. */
+PWMGPU_API pwmgpu_status pwmgpu_ctx_set_pass_levels(pwmgpu_ctx* ctx, int levels_per_pass);
+
+/* ---------------------------------------------------------------------- */
+/* Drop-in construction (host text in, host bit vectors out)               */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces the compute() of pwm's plain construction classes:
+ *   wx_ps  include/wx_ps.hpp:37-56      wx_pc   include/wx_pc.hpp:36-57
+ *   wx_ppc include/wx_ppc.hpp:36-58     wx_pps  include/wx_pps.hpp:38-69
+ *   wx_pc_ss / wx_ppc_ss / wx_dd_ps / wx_dd_pc / wx_dd_pc_ss (same output)
+ * `text`: host array of `size` symbols of `word_width` bytes (1, 2 or 4),
+ * each < 2^levels.  `bv`: host array of levels * round_up(ceil(size/64), 16)
+ * words.  `zeros`: host array of `levels` u64 for a matrix (is_tree == 0),
+ * ignored for a tree; all L entries are written, like wx_ps / wx_pc.
+ * size == 0 writes nothing (pwm returns an empty structure). */
+PWMGPU_API pwmgpu_status pwmgpu_compute(pwmgpu_ctx* ctx, const void* text, uint64_t size, uint32_t word_width,
+                                        uint32_t levels, int is_tree, uint64_t* bv, uint64_t* zeros);
+
+/* Canonical Huffman codes of a text, as pwm's histogram +
+ * level_sizes_builder + canonical_huff_codes compute them
+ * (include/util/histogram.hpp:39-76, include/huffman/
+ * huff_level_sizes_builder.hpp:13-46, include/huffman/huff_codes.hpp:
+ * 140-285), including pwm's tie-breaking.  Writes max_symbol+1 entries of
+ * code_len / code_word (capacity `cap`), the per-level sizes (up to 64) and
+ * the number of levels (= longest code). */
+PWMGPU_API pwmgpu_status pwmgpu_huffman_codes(pwmgpu_ctx* ctx, const void* text, uint64_t size, uint32_t word_width,
+                                              int is_tree, uint64_t* code_len, uint64_t* code_word, uint64_t cap,
+                                              uint64_t* num_codes, uint64_t* level_sizes, uint32_t* levels);
+
+/* Replaces the compute() of pwm's Huffman-shaped construction classes:
+ *   wx_huff_ps include/wx_huff_ps.hpp:45-79, wx_huff_pc include/wx_huff_pc.hpp:
+ *   45-80, wx_huff_naive include/wx_huff_naive.hpp:45-79 (and wx_huff_dd_*).
+ * Level l holds bit l of every code longer than l.  The tree orders each level
+ * stably by code prefix, the matrix by the previous code bit with finished
+ * codes dropped (huff_naive semantics, include/huffman/huff_naive.hpp:19-126);
+ * matrix zeros are the 0 bits of each level.  Codes come from the caller
+ * (code_len/code_word, num_codes entries, e.g. pwm's own builder) or, when
+ * code_len is NULL, from pwmgpu_huffman_codes.  `bv` is laid out with the
+ * per-level sizes in `level_sizes`. */
+PWMGPU_API pwmgpu_status pwmgpu_compute_huffman(pwmgpu_ctx* ctx, const void* text, uint64_t size, uint32_t word_width,
+                                                int is_tree, const uint64_t* code_len, const uint64_t* code_word,
+                                                uint64_t num_codes, uint32_t levels, const uint64_t* level_sizes,
+                                                uint64_t* bv, uint64_t* zeros);
+
+/* ---------------------------------------------------------------------- */
+/* Device-resident structures (batching, serving, benchmarking)            */
+/* ---------------------------------------------------------------------- */
+
+/* Allocates device storage for a build of `size` symbols with `levels`
+ * levels; shape_flags: PWMGPU_MATRIX and/or PWMGPU_TREE, optionally
+ * PWMGPU_RANK_SELECT. */
+PWMGPU_API pwmgpu_status pwmgpu_wx_create(pwmgpu_ctx* ctx, uint64_t size, uint32_t word_width, uint32_t levels,
+                                          uint32_t shape_flags, pwmgpu_wx** out);
+/* Builds into `wx` from a device text (same size/width/levels as created).
+ * Asynchronous on the context's stream; errors detected on the device are
+ * reported by the next call that synchronises (pwmgpu_wx_check). */
+PWMGPU_API pwmgpu_status pwmgpu_wx_build(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text);
+/* Same as pwmgpu_wx_build from a host text (copied in by the library; pinned
+ * host memory makes the copy asynchronous). */
+PWMGPU_API pwmgpu_status pwmgpu_wx_build_host(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* host_text);
+/* Synchronises and reports device-side errors (bad symbol, timeout). */
+PWMGPU_API pwmgpu_status pwmgpu_wx_check(pwmgpu_ctx* ctx, pwmgpu_wx* wx);
+/* which: 0 = matrix, 1 = tree. */
+PWMGPU_API pwmgpu_status pwmgpu_wx_view(const pwmgpu_wx* wx, int which, pwmgpu_view* view);
+/* Copies the bit vectors (and matrix zeros) of one structure to the host. */
+PWMGPU_API pwmgpu_status pwmgpu_wx_download(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which, uint64_t* bv,
+                                            uint64_t* zeros);
+/* Rank/select blocks of one level, in pwm's layout (bin_rank_popcnt.hpp:
+ * 32-86, bin_select_popcnt.hpp:38-107): l0 (u64), l12 (pairs of u32: l1
+ * count, three 10-bit l2 counts), select0 and select1 samples (u32).
+ * counts receives n_l0, n_l12, n_select0, n_select1.  Any output may be NULL
+ * to query the counts. */
+PWMGPU_API pwmgpu_status pwmgpu_wx_rank_select_blocks(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which,
+                                                      uint32_t level, uint64_t* l0, uint32_t* l12, uint32_t* s0,
+                                                      uint32_t* s1, uint64_t* counts);
+/* Batched queries on device arrays (query_support, include/queries/
+ * query_support.hpp:39-178): ACCESS(a[i]) ; RANK(symbol a[i], index b[i]) ;
+ * SELECT(symbol a[i], occurrence b[i]).  Needs PWMGPU_RANK_SELECT. */
+PWMGPU_API pwmgpu_status pwmgpu_wx_query(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which, int op, const uint64_t* d_a,
+                                         const uint64_t* d_b, uint64_t count, uint64_t* d_out);
+PWMGPU_API void pwmgpu_wx_free(pwmgpu_wx* wx);
+
+/* ---------------------------------------------------------------------- */
+/* Seeded synthetic texts (counter-based, identical on host and device)     */
+/* ---------------------------------------------------------------------- */
+
+#define PWMGPU_GEN_UNIFORM 0   /* uniform over [0, param)                         */
+#define PWMGPU_GEN_DNA4 1      /* {0,1,2,3} with p = (0.3, 0.2, 0.2, 0.3)          */
+#define PWMGPU_GEN_ZIPF256 2   /* Zipf(1.0) ranks over 256 symbols, permuted       */
+#define PWMGPU_GEN_MIX16 3     /* 50/50 uniform u16 / geometric(p=0.01) clamped    */
+
+/* Fills `out` (host when on_device == 0, device otherwise) with n symbols of
+ * word_width bytes. */
+PWMGPU_API pwmgpu_status pwmgpu_generate(pwmgpu_ctx* ctx, int dist, uint64_t seed, uint64_t param, uint64_t n,
+                                         uint32_t word_width, void* out, int on_device);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PWMGPU_H */

@@ -110,6 +110,8 @@ class Oracle:
         for name in ("orc_qs_rank", "orc_qs_select"):
             getattr(L, name).argtypes = [_vp, ctypes.c_uint64, ctypes.c_uint64]
             getattr(L, name).restype = ctypes.c_uint64
+        L.orc_cpu_step.argtypes = [_vp, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, _u64p,
+                                   _u64p, _u64p, _u64p]
         L.orc_huff_codes.argtypes = [_vp, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int, _u64p, _u64p,
                                      ctypes.c_uint64, _u64p, _u32p]
         L.orc_huff_codes.restype = ctypes.c_uint64
@@ -133,6 +135,18 @@ class Oracle:
         if n == 0:
             return Structure(0, [], words[:0], zeros[:0], is_tree)
         return Structure(levels, bits, words, None if is_tree else zeros[:levels], is_tree)
+
+    def cpu_step_buffers(self, n, levels):
+        offs, total = layout([n] * levels)
+        return (np.zeros(max(total, 1), dtype=np.uint64), np.zeros(max(total, 1), dtype=np.uint64), offs,
+                np.zeros(max(levels, 1), dtype=np.uint64))
+
+    def cpu_step(self, text, levels, threads, bufs):
+        """CPU baseline step: matrix + tree (parallel prefix counting) and
+        rank/select support of every level."""
+        wm, wt, offs, zeros = bufs
+        self.L.orc_cpu_step(text.ctypes.data_as(_vp), text.size, text.dtype.itemsize, levels, threads, _p(wm), _p(wt),
+                            _p(offs), _p(zeros))
 
     # -- rank / select -----------------------------------------------------
     def rank_select_blocks(self, level_words):

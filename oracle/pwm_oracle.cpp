@@ -834,3 +834,30 @@ void orc_decode(void* qp, uint64_t* out) {
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// CPU-baseline step (bench.py's cpu_baseline leg and `--impl reference` when
+// the reference shim is not loadable): wavelet matrix and wavelet tree with
+// the parallel prefix-counting restatement (orc_wx_ppc), then rank/select
+// support (bin_rank_popcnt + both bin_select_popcnt) for every level of both,
+// levels in parallel.  wm/wt hold levels*stride words each.
+int orc_cpu_step(const void* text, uint64_t n, uint32_t w, uint32_t levels, int threads, uint64_t* wm,
+                 uint64_t* wt, const uint64_t* offsets, uint64_t* zeros) {
+  if (threads <= 0) threads = omp_get_max_threads();
+  orc_wx_ppc(text, n, w, levels, 0, wm, offsets, zeros, threads);
+  orc_wx_ppc(text, n, w, levels, 1, wt, offsets, nullptr, threads);
+  const uint64_t nw = words_for(n);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(threads)
+  for (int job = 0; job < int(2 * levels); ++job) {
+    const uint64_t* data = (job < int(levels) ? wm : wt) + offsets[job % levels];
+    std::vector<uint64_t> l0(orc_rank_l0_size(nw));
+    std::vector<uint32_t> l12(2 * orc_rank_l12_size(nw)), s(nw * 64 / 8192 + 2);
+    orc_rank_build(data, nw, l0.data(), l12.data());
+    orc_select_build(0, data, nw, l12.data(), s.data());
+    orc_select_build(1, data, nw, l12.data(), s.data());
+  }
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,431 @@
+"""pwm_gb300: GB300-native wavelet tree / wavelet matrix construction.
+
+A host-side mirror of kurpicz/pwm's construction API over the C ABI of
+libpwmgpu.so (include/pwmgpu.h):
+
+* ``wx_ps``, ``wx_pc``, ``wx_ppc``, ``wx_pps``, ``wx_pc_ss``, ``wx_ppc_ss``,
+  ``wx_dd_ps``, ``wx_dd_pc``, ``wx_dd_pc_ss`` (pwm include/wx_*.hpp) and the
+  Huffman-shaped ``wx_huff_ps``, ``wx_huff_pc``, ``wx_huff_pc_ss``,
+  ``wx_huff_naive`` (include/wx_huff_*.hpp): construction classes whose
+  ``compute(text, size, levels)`` returns a ``wavelet_structure``.  All of a
+  plain kind produce pwm's identical bit vectors, so they share one GPU path.
+* ``wavelet_structure`` (include/construction/wavelet_structure.hpp:142-199)
+  with ``levels()``, ``bvs()``, ``zeros()``, ``is_tree()``,
+  ``is_huffman_shaped()``, ``text_size()``.
+* ``algorithm_list`` / ``CONSTRUCTION_REGISTER``
+  (include/benchmark/algorithm.hpp:39-81, 273-279): the registry.
+* ``DeviceStructure``: a device-resident build with rank/select support and
+  batched access/rank/select queries (include/queries/query_support.hpp).
+
+Every compute runs on the GPU; there is no CPU fallback.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import (GEN_DNA4, GEN_MIX16, GEN_UNIFORM, GEN_ZIPF256, MATRIX, Q_ACCESS, Q_RANK, Q_SELECT,
+                   RANK_SELECT, TREE, PwmGpuError)
+
+__all__ = ["Context", "default_context", "wavelet_structure", "bit_vectors", "algorithm_list",
+           "CONSTRUCTION_REGISTER", "DeviceStructure", "generate", "huffman_codes", "PwmGpuError"]
+
+_WIDTH_DTYPE = {1: np.uint8, 2: np.uint16, 4: np.uint32}
+
+
+def _u64p(a):
+    return a.ctypes.data_as(_lib.u64p)
+
+
+def _u32p(a):
+    return a.ctypes.data_as(_lib.u32p)
+
+
+def padded_words(bits):
+    return ((int(bits) + 63) // 64 + 15) & ~15
+
+
+class Context:
+    """A pwmgpu context: one device, one CUDA stream, cached scratch."""
+
+    def __init__(self, device=0, stream=None):
+        self.lib = _lib.load()
+        h = ctypes.c_void_p()
+        st = self.lib.pwmgpu_ctx_create(device, stream, ctypes.byref(h))
+        if st != 0:
+            raise PwmGpuError(st, "pwmgpu_ctx_create failed (is a GB300 visible?)")
+        self.h = h
+        self.device = device
+
+    def check(self, st):
+        if st != 0:
+            msg = self.lib.pwmgpu_ctx_last_error(self.h)
+            raise PwmGpuError(st, msg.decode() if msg else "")
+
+    def sync(self):
+        self.check(self.lib.pwmgpu_ctx_sync(self.h))
+
+    @property
+    def launches(self):
+        return int(self.lib.pwmgpu_ctx_launch_count(self.h))
+
+    def set_pass_levels(self, k):
+        self.check(self.lib.pwmgpu_ctx_set_pass_levels(self.h, int(k)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pwmgpu_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default = None
+
+
+def default_context():
+    global _default
+    if _default is None:
+        _default = Context()
+    return _default
+
+
+class bit_vectors:
+    """pwm's bit_vectors (include/arrays/bit_vectors.hpp:13-29): levels in one
+    allocation, each padded to 128 bytes."""
+
+    def __init__(self, level_bits, words=None):
+        self.level_bits_ = [int(b) for b in level_bits]
+        offs, off = [], 0
+        for b in self.level_bits_:
+            offs.append(off)
+            off += padded_words(b)
+        self.offsets = offs
+        self.total_words = off
+        self.data = np.zeros(max(off, 1), dtype=np.uint64) if words is None else words
+
+    def levels(self):
+        return len(self.level_bits_)
+
+    def level_bit_size(self, level):
+        return self.level_bits_[level]
+
+    def __getitem__(self, level):
+        o = self.offsets[level]
+        return self.data[o:o + (self.level_bits_[level] + 63) // 64]
+
+
+class wavelet_structure:
+    """pwm's wavelet_structure (include/construction/wavelet_structure.hpp)."""
+
+    def __init__(self, bvs, zeros, is_tree, is_huffman_shaped=False, codes=None):
+        self._bvs = bvs
+        self._zeros = list(zeros) if zeros is not None else []
+        self._is_tree = bool(is_tree)
+        self._huff = bool(is_huffman_shaped)
+        self._codes = codes
+
+    def levels(self):
+        return self._bvs.levels()
+
+    def bvs(self):
+        return self._bvs
+
+    def zeros(self):
+        return self._zeros
+
+    def is_tree(self):
+        return self._is_tree
+
+    def is_huffman_shaped(self):
+        return self._huff
+
+    def text_size(self):
+        return self._bvs.level_bit_size(0) if self._bvs.levels() else 0
+
+    def codes(self):
+        return self._codes
+
+
+def _as_text(text, size, word_width):
+    a = np.ascontiguousarray(text)
+    if a.dtype != _WIDTH_DTYPE[word_width]:
+        a = a.astype(_WIDTH_DTYPE[word_width])
+    if size > a.size:
+        raise ValueError("size exceeds the text")
+    return a[:size]
+
+
+class _PlainConstruction:
+    """compute() of pwm's plain wx_* classes (include/wx_ps.hpp:37-56 and
+    siblings) on the GPU."""
+
+    is_huffman_shaped = False
+    is_parallel = True
+    external_in = False
+    external_out = False
+    stats_support = False
+    is_inplace = False
+
+    def __init__(self, alphabet=np.uint8, is_tree=False, context=None):
+        self.alphabet = np.dtype(alphabet)
+        self.word_width = self.alphabet.itemsize
+        self.is_tree = bool(is_tree)
+        self.ctx = context
+
+    def compute(self, text, size, levels):
+        ctx = self.ctx or default_context()
+        size, levels = int(size), int(levels)
+        if size == 0:
+            return wavelet_structure(bit_vectors([]), [] if not self.is_tree else None, self.is_tree)
+        t = _as_text(text, size, self.word_width)
+        bvs = bit_vectors([size] * levels)
+        zeros = np.zeros(levels, dtype=np.uint64)
+        ctx.check(ctx.lib.pwmgpu_compute(ctx.h, t.ctypes.data, size, self.word_width, levels, int(self.is_tree),
+                                         _u64p(bvs.data), _u64p(zeros)))
+        return wavelet_structure(bvs, None if self.is_tree else [int(z) for z in zeros], self.is_tree)
+
+
+class _HuffmanConstruction(_PlainConstruction):
+    """compute() of pwm's Huffman-shaped wx_huff_* classes
+    (include/wx_huff_ps.hpp:45-79 and siblings) on the GPU.  `levels` is
+    ignored, as in pwm; codes come from pwm's canonical builder semantics
+    (huffman_codes) or from `codes=(code_len, code_word)`."""
+
+    is_huffman_shaped = True
+
+    def compute(self, text, size, levels=0, codes=None):
+        ctx = self.ctx or default_context()
+        size = int(size)
+        t = _as_text(text, size, self.word_width)
+        if codes is None:
+            codes = huffman_codes(t, self.is_tree, ctx)
+        code_len = np.ascontiguousarray(codes[0], dtype=np.uint64)
+        code_word = np.ascontiguousarray(codes[1], dtype=np.uint64)
+        if size == 0:
+            return wavelet_structure(bit_vectors([]), None if self.is_tree else [], self.is_tree, True, codes)
+        nz = code_len[np.unique(t)] if code_len.size else code_len
+        L = int(nz.max()) if nz.size else 0
+        sizes = [int(np.sum(code_len[t] > l)) for l in range(L)] if L else []
+        bvs = bit_vectors(sizes)
+        zeros = np.zeros(max(L, 1), dtype=np.uint64)
+        sz = np.array(sizes if sizes else [0], dtype=np.uint64)
+        ctx.check(ctx.lib.pwmgpu_compute_huffman(ctx.h, t.ctypes.data, size, self.word_width, int(self.is_tree),
+                                                 _u64p(code_len), _u64p(code_word), code_len.size, L, _u64p(sz),
+                                                 _u64p(bvs.data), _u64p(zeros)))
+        return wavelet_structure(bvs, None if self.is_tree else [int(z) for z in zeros[:L]], self.is_tree, True,
+                                 (code_len, code_word))
+
+
+def huffman_codes(text, is_tree, context=None):
+    """pwm's canonical Huffman codes of an 8- or 16-bit text: (code_len,
+    code_word, level_sizes, levels), with max_symbol+1 table entries."""
+    ctx = context or default_context()
+    t = np.ascontiguousarray(text)
+    w = t.dtype.itemsize
+    cap = 1 << (8 * w)
+    ln = np.zeros(cap, dtype=np.uint64)
+    wd = np.zeros(cap, dtype=np.uint64)
+    nc = ctypes.c_uint64(0)
+    lv = ctypes.c_uint32(0)
+    sizes = np.zeros(64, dtype=np.uint64)
+    ctx.check(ctx.lib.pwmgpu_huffman_codes(ctx.h, t.ctypes.data, t.size, w, int(is_tree), _u64p(ln), _u64p(wd), cap,
+                                           ctypes.byref(nc), _u64p(sizes), ctypes.byref(lv)))
+    return ln[:nc.value].copy(), wd[:nc.value].copy(), sizes[:lv.value].copy(), lv.value
+
+
+def _variant(name, base, doc):
+    return type(name, (base,), {"__doc__": doc})
+
+
+wx_ps = _variant("wx_ps", _PlainConstruction, "pwm include/wx_ps.hpp:19-57 (prefix sorting)")
+wx_pc = _variant("wx_pc", _PlainConstruction, "pwm include/wx_pc.hpp:19-58 (prefix counting)")
+wx_ppc = _variant("wx_ppc", _PlainConstruction, "pwm include/wx_ppc.hpp (parallel prefix counting)")
+wx_pps = _variant("wx_pps", _PlainConstruction, "pwm include/wx_pps.hpp:21-70 (parallel prefix sorting)")
+wx_pc_ss = _variant("wx_pc_ss", _PlainConstruction, "pwm include/wx_pc_ss.hpp (single scan)")
+wx_ppc_ss = _variant("wx_ppc_ss", _PlainConstruction, "pwm include/wx_ppc_ss.hpp (parallel single scan)")
+wx_dd_ps = _variant("wx_dd_ps", _PlainConstruction, "pwm include/wx_dd_ps.hpp:26-121 (domain decomposition)")
+wx_dd_pc = _variant("wx_dd_pc", _PlainConstruction, "pwm include/wx_dd_pc.hpp:26-120")
+wx_dd_pc_ss = _variant("wx_dd_pc_ss", _PlainConstruction, "pwm include/wx_dd_pc_ss.hpp:25-119")
+wx_huff_ps = _variant("wx_huff_ps", _HuffmanConstruction, "pwm include/wx_huff_ps.hpp:24-80")
+wx_huff_pc = _variant("wx_huff_pc", _HuffmanConstruction, "pwm include/wx_huff_pc.hpp:24-81")
+wx_huff_pc_ss = _variant("wx_huff_pc_ss", _HuffmanConstruction, "pwm include/wx_huff_pc_ss.hpp:24-78")
+wx_huff_naive = _variant("wx_huff_naive", _HuffmanConstruction, "pwm include/wx_huff_naive.hpp:24-80")
+
+__all__ += ["wx_ps", "wx_pc", "wx_ppc", "wx_pps", "wx_pc_ss", "wx_ppc_ss", "wx_dd_ps", "wx_dd_pc", "wx_dd_pc_ss",
+            "wx_huff_ps", "wx_huff_pc", "wx_huff_pc_ss", "wx_huff_naive"]
+
+
+class construction_algorithm:
+    """pwm's construction_algorithm (include/benchmark/algorithm.hpp:83-191)."""
+
+    def __init__(self, name, description, impl):
+        self._name, self._description, self.impl = name, description, impl
+
+    def name(self):
+        return self._name
+
+    def description(self):
+        return self._description
+
+    def is_parallel(self):
+        return self.impl.is_parallel
+
+    def is_tree(self):
+        return self.impl.is_tree
+
+    def is_huffman_shaped(self):
+        return self.impl.is_huffman_shaped
+
+    def is_inplace(self):
+        return self.impl.is_inplace
+
+    def word_width(self):
+        return self.impl.word_width
+
+    def compute_bitvector(self, text, size, levels):
+        return self.impl.compute(text, size, levels)
+
+    compute_internal_bitvector = compute_bitvector
+
+    def huffman_bit_size(self, text, size, levels):
+        if not self.impl.is_huffman_shaped:
+            return 0
+        ws = self.impl.compute(text, size, levels)
+        return sum(ws.bvs().level_bit_size(l) for l in range(ws.levels()))
+
+    def print_info(self):
+        print(f"{self._name}: {self._description}")
+
+
+class algorithm_list:
+    """pwm's algorithm_list<ext_in, ext_out, word_width> (algorithm.hpp:39-81),
+    internal memory only."""
+
+    _lists = {}
+
+    @classmethod
+    def get_algorithm_list(cls, word_width=1):
+        return cls._lists.setdefault(int(word_width), [])
+
+    @classmethod
+    def register_algorithm(cls, algo):
+        cls.get_algorithm_list(algo.word_width()).append(algo)
+
+    @classmethod
+    def filtered(cls, f, word_width=1):
+        return [a for a in cls.get_algorithm_list(word_width) if f(a)]
+
+
+def CONSTRUCTION_REGISTER(name, description, impl):
+    """pwm's CONSTRUCTION_REGISTER (algorithm.hpp:273-279)."""
+    algo = construction_algorithm(name, description, impl)
+    algorithm_list.register_algorithm(algo)
+    return algo
+
+
+def _register_all():
+    names = {"ps": wx_ps, "pc": wx_pc, "ppc": wx_ppc, "pps": wx_pps, "pc_ss": wx_pc_ss, "ppc_ss": wx_ppc_ss,
+             "dd_ps": wx_dd_ps, "dd_pc": wx_dd_pc, "dd_pc_ss": wx_dd_pc_ss}
+    for tree in (False, True):
+        pre = "wt" if tree else "wm"
+        for dt in (np.uint8, np.uint16, np.uint32):
+            for key, cls in names.items():
+                CONSTRUCTION_REGISTER(f"{pre}_gpu_{key}",
+                                      f"GB300 {'wavelet tree' if tree else 'wavelet matrix'} construction with "
+                                      f"{np.dtype(dt).itemsize * 8}-bit alphabet ({key} semantics).", cls(dt, tree))
+            if dt != np.uint32:
+                for key, cls in (("huff_ps", wx_huff_ps), ("huff_pc", wx_huff_pc), ("huff_naive", wx_huff_naive)):
+                    CONSTRUCTION_REGISTER(f"{pre}_gpu_{key}", f"GB300 Huffman-shaped construction ({key}).",
+                                          cls(dt, tree))
+
+
+_register_all()
+
+
+class DeviceStructure:
+    """A device-resident build (pwmgpu_wx): matrix and/or tree, optional
+    rank/select support, batched queries."""
+
+    def __init__(self, size, word_width, levels, matrix=True, tree=False, rank_select=False, context=None):
+        self.ctx = context or default_context()
+        flags = (MATRIX if matrix else 0) | (TREE if tree else 0) | (RANK_SELECT if rank_select else 0)
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.pwmgpu_wx_create(self.ctx.h, int(size), int(word_width), int(levels), flags,
+                                                     ctypes.byref(h)))
+        self.h = h
+        self.size, self.word_width, self.levels = int(size), int(word_width), int(levels)
+        self.matrix, self.tree, self.rank_select = matrix, tree, rank_select
+
+    def build(self, d_text_ptr):
+        """Builds from a device pointer (e.g. a torch tensor's data_ptr())."""
+        self.ctx.check(self.ctx.lib.pwmgpu_wx_build(self.ctx.h, self.h, ctypes.c_void_p(int(d_text_ptr))))
+
+    def check(self):
+        self.ctx.check(self.ctx.lib.pwmgpu_wx_check(self.ctx.h, self.h))
+
+    def view(self, which):
+        v = _lib.View()
+        self.ctx.check(self.ctx.lib.pwmgpu_wx_view(self.h, int(which), ctypes.byref(v)))
+        return v
+
+    def download(self, which):
+        """wavelet_structure on the host (which: 0 matrix, 1 tree)."""
+        v = self.view(which)
+        bits = [v.level_bits[i] for i in range(v.levels)]
+        bvs = bit_vectors(bits)
+        zeros = np.zeros(max(v.levels, 1), dtype=np.uint64)
+        self.ctx.check(self.ctx.lib.pwmgpu_wx_download(self.ctx.h, self.h, int(which), _u64p(bvs.data), _u64p(zeros)))
+        return wavelet_structure(bvs, None if which else [int(z) for z in zeros[:v.levels]], bool(which))
+
+    def rank_select_blocks(self, which, level):
+        counts = np.zeros(4, dtype=np.uint64)
+        lib = self.ctx.lib
+        self.ctx.check(lib.pwmgpu_wx_rank_select_blocks(self.ctx.h, self.h, int(which), int(level), None, None, None,
+                                                        None, _u64p(counts)))
+        n0, n12, ns0, ns1 = (int(c) for c in counts)
+        l0 = np.zeros(max(n0, 1), dtype=np.uint64)
+        l12 = np.zeros(max(2 * n12, 1), dtype=np.uint32)
+        s0 = np.zeros(max(ns0, 1), dtype=np.uint32)
+        s1 = np.zeros(max(ns1, 1), dtype=np.uint32)
+        self.ctx.check(lib.pwmgpu_wx_rank_select_blocks(self.ctx.h, self.h, int(which), int(level), _u64p(l0),
+                                                        _u32p(l12), _u32p(s0), _u32p(s1), _u64p(counts)))
+        return l0[:n0], l12[:2 * n12], s0[:ns0], s1[:ns1]
+
+    def query(self, which, op, d_a, d_b, count, d_out):
+        """Batched queries on device arrays (pointers)."""
+        self.ctx.check(self.ctx.lib.pwmgpu_wx_query(self.ctx.h, self.h, int(which), int(op),
+                                                    ctypes.c_void_p(int(d_a)),
+                                                    ctypes.c_void_p(int(d_b)) if d_b is not None else None,
+                                                    int(count), ctypes.c_void_p(int(d_out))))
+
+    def free(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.pwmgpu_wx_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def generate(dist, seed, n, word_width, param=0, device_ptr=None, context=None):
+    """Seeded synthetic text (host numpy array, or into a device pointer)."""
+    lib = _lib.load()
+    if device_ptr is None:
+        out = np.zeros(int(n), dtype=_WIDTH_DTYPE[word_width])
+        st = lib.pwmgpu_generate(None, int(dist), int(seed), int(param), int(n), int(word_width),
+                                 out.ctypes.data if n else None, 0)
+        if st != 0:
+            raise PwmGpuError(st, "pwmgpu_generate failed")
+        return out
+    ctx = context or default_context()
+    ctx.check(lib.pwmgpu_generate(ctx.h, int(dist), int(seed), int(param), int(n), int(word_width),
+                                  ctypes.c_void_p(int(device_ptr)), 1))
+    return None

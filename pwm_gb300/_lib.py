@@ -1,0 +1,90 @@
+"""Loads libpwmgpu.so (built in-tree by pwm_gb300/build.py) and declares the
+C ABI of include/pwmgpu.h.  There is no fallback: if the library is missing
+or no GB300 is usable, calls fail with an error."""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpwmgpu.so")
+HEADER = os.path.join(HERE, "..", "include", "pwmgpu.h")
+
+u64 = ctypes.c_uint64
+u32 = ctypes.c_uint32
+i32 = ctypes.c_int
+vp = ctypes.c_void_p
+u64p = ctypes.POINTER(ctypes.c_uint64)
+u32p = ctypes.POINTER(ctypes.c_uint32)
+cstr = ctypes.c_char_p
+
+STATUS = {0: "PWMGPU_OK", 1: "PWMGPU_ERR_ARG", 2: "PWMGPU_ERR_OOM", 3: "PWMGPU_ERR_CUDA",
+          4: "PWMGPU_ERR_TIMEOUT", 5: "PWMGPU_ERR_SYMBOL", 6: "PWMGPU_ERR_NO_DEVICE", 7: "PWMGPU_ERR_BUSY"}
+
+MATRIX, TREE, RANK_SELECT, HUFFMAN = 0x1, 0x2, 0x4, 0x8
+Q_ACCESS, Q_RANK, Q_SELECT = 0, 1, 2
+GEN_UNIFORM, GEN_DNA4, GEN_ZIPF256, GEN_MIX16 = 0, 1, 2, 3
+
+
+class View(ctypes.Structure):
+    _fields_ = [("levels", u32), ("is_tree", u32), ("is_huffman", u32), ("has_rank_select", u32),
+                ("size", u64), ("total_words", u64), ("words", vp), ("level_offset", u64p),
+                ("level_bits", u64p), ("zeros", u64p)]
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "pwmgpu_ctx_create": (i32, [i32, vp, ctypes.POINTER(vp)]),
+    "pwmgpu_ctx_destroy": (None, [vp]),
+    "pwmgpu_ctx_last_error": (cstr, [vp]),
+    "pwmgpu_status_string": (cstr, [i32]),
+    "pwmgpu_ctx_sync": (i32, [vp]),
+    "pwmgpu_ctx_launch_count": (u64, [vp]),
+    "pwmgpu_ctx_set_pass_levels": (i32, [vp, i32]),
+    "pwmgpu_ctx_profile": (i32, [vp, i32]),
+    "pwmgpu_ctx_profile_read": (i32, [vp, ctypes.c_char_p, u64]),
+    "pwmgpu_wx_build_host": (i32, [vp, vp, vp]),
+    "pwmgpu_compute": (i32, [vp, vp, u64, u32, u32, i32, u64p, u64p]),
+    "pwmgpu_huffman_codes": (i32, [vp, vp, u64, u32, i32, u64p, u64p, u64, u64p, u64p, u32p]),
+    "pwmgpu_compute_huffman": (i32, [vp, vp, u64, u32, i32, u64p, u64p, u64, u32, u64p, u64p, u64p]),
+    "pwmgpu_wx_create": (i32, [vp, u64, u32, u32, u32, ctypes.POINTER(vp)]),
+    "pwmgpu_wx_build": (i32, [vp, vp, vp]),
+    "pwmgpu_wx_check": (i32, [vp, vp]),
+    "pwmgpu_wx_view": (i32, [vp, i32, ctypes.POINTER(View)]),
+    "pwmgpu_wx_download": (i32, [vp, vp, i32, u64p, u64p]),
+    "pwmgpu_wx_rank_select_blocks": (i32, [vp, vp, i32, u32, u64p, u32p, u32p, u32p, u64p]),
+    "pwmgpu_wx_query": (i32, [vp, vp, i32, i32, vp, vp, u64, vp]),
+    "pwmgpu_wx_free": (None, [vp]),
+    "pwmgpu_generate": (i32, [vp, i32, u64, u64, u64, u32, vp, i32]),
+}
+
+
+class PwmGpuError(RuntimeError):
+    def __init__(self, status, message=""):
+        self.status = status
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+
+
+_lib = None
+
+
+def load():
+    """Returns the loaded library; raises if it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'` "
+                           "(nvcc, sm_103a) first; this package has no CPU fallback")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def declared_symbols():
+    """Entry points declared in include/pwmgpu.h."""
+    import re
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"PWMGPU_API\s+[\w\s\*]+?\b(pwmgpu_\w+)\s*\(", text)))

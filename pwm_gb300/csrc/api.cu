@@ -1,0 +1,1037 @@
+// C ABI of the engine (include/pwmgpu.h): contexts, device-resident
+// structures, the drop-in host-to-host constructions, the Huffman code
+// builder, queries and generators.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <numeric>
+#include <queue>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/pwmgpu.h"
+#include "gen.cuh"
+#include "host_tables.hpp"
+#include "kernels.cuh"
+
+using namespace pwmgpu;
+
+namespace {
+
+constexpr uint32_t kMaxLevels = 64;
+constexpr uint32_t kMaxPlainLevels = 24;  // the leaf histogram has 2^L bins
+constexpr int kDefaultPassLevels = 4;
+
+struct Fail {
+  pwmgpu_status st;
+  std::string msg;
+};
+
+#define CUDA_TRY(expr)                                                                          \
+  do {                                                                                          \
+    cudaError_t _e = (expr);                                                                    \
+    if (_e != cudaSuccess) {                                                                    \
+      throw Fail{_e == cudaErrorMemoryAllocation ? PWMGPU_ERR_OOM : PWMGPU_ERR_CUDA,            \
+                 std::string(#expr) + ": " + cudaGetErrorString(_e)};                           \
+    }                                                                                           \
+  } while (0)
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+namespace {
+struct ProfRecord {
+  const char* name;
+  uint64_t bytes;
+  uint64_t launches;
+  cudaEvent_t a, b;
+};
+}  // namespace
+
+struct pwmgpu_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  uint64_t launches = 0;
+  uint32_t* d_status = nullptr;
+  std::map<std::string, DevBuf> scratch;
+  int pass_levels = kDefaultPassLevels;
+  pwmgpu_wx* compute_cache = nullptr;  // reused by pwmgpu_compute for equal shapes
+  // CUDA-event timing of every launch group while profiling is on
+  bool profiling = false;
+  std::vector<ProfRecord> prof;
+  std::vector<cudaEvent_t> event_pool;
+  cudaEvent_t take_event() {
+    if (!event_pool.empty()) {
+      cudaEvent_t e = event_pool.back();
+      event_pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e;
+    CUDA_TRY(cudaEventCreate(&e));
+    return e;
+  }
+
+  // Grow-only named scratch buffer (contents undefined).
+  void* grow(const std::string& name, size_t bytes) {
+    auto& b = scratch[name];
+    if (b.bytes < bytes) {
+      if (b.p) {
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        CUDA_TRY(cudaFree(b.p));
+      }
+      b.p = nullptr;
+      b.bytes = 0;
+      const size_t want = std::max<size_t>(bytes, 256);
+      CUDA_TRY(cudaMalloc(&b.p, want));
+      b.bytes = want;
+    }
+    return b.p;
+  }
+  ~pwmgpu_ctx();
+};
+
+namespace {
+
+// One built structure (matrix or tree) in device memory.
+struct Structure {
+  bool present = false;
+  bool is_tree = false;
+  bool huffman = false;
+  uint32_t levels = 0;
+  uint64_t n = 0;
+  std::vector<uint64_t> bits, offs;
+  uint64_t total_words = 0;
+  uint64_t* d_words = nullptr;
+  std::vector<uint64_t> zeros;   // host (matrix)
+  uint64_t* d_zeros = nullptr;   // device copy (matrix), read by queries
+  // rank/select
+  bool rs = false;
+  void* d_rs = nullptr;          // l0, l12, samples and meta of all levels
+  size_t rs_bytes = 0;
+  std::vector<RankSelectLevel> rs_levels;
+  RankSelectLevel* d_rs_levels = nullptr;
+  QueryLevel* d_q_levels = nullptr;
+
+  void set_layout(const std::vector<uint64_t>& level_bits) {
+    levels = uint32_t(level_bits.size());
+    bits = level_bits;
+    offs.assign(levels, 0);
+    uint64_t off = 0;
+    for (uint32_t l = 0; l < levels; ++l) { offs[l] = off; off += padded_words(bits[l]); }
+    total_words = off;
+  }
+  void release() {
+    if (d_words) cudaFree(d_words);
+    if (d_zeros) cudaFree(d_zeros);
+    if (d_rs) cudaFree(d_rs);
+    if (d_rs_levels) cudaFree(d_rs_levels);
+    if (d_q_levels) cudaFree(d_q_levels);
+    d_words = nullptr; d_zeros = nullptr; d_rs = nullptr; d_rs_levels = nullptr; d_q_levels = nullptr;
+    rs = false;
+    rs_bytes = 0;
+  }
+};
+
+}  // namespace
+
+struct pwmgpu_wx {
+  pwmgpu_ctx* ctx = nullptr;
+  uint64_t n = 0;
+  uint32_t width = 1;
+  uint32_t levels = 0;
+  uint32_t flags = 0;
+  bool huffman = false;
+  Structure wm, wt;
+  bool wm_internal = false;  // matrix built only as the source of the tree
+  ~pwmgpu_wx() { wm.release(); wt.release(); }
+};
+
+pwmgpu_ctx::~pwmgpu_ctx() {
+  cudaSetDevice(device);
+  delete compute_cache;
+  for (auto& r : prof) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+  for (auto e : event_pool) cudaEventDestroy(e);
+  for (auto& kv : scratch)
+    if (kv.second.p) cudaFree(kv.second.p);
+  if (d_status) cudaFree(d_status);
+  if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+namespace {
+
+pwmgpu_status fail(pwmgpu_ctx* ctx, pwmgpu_status st, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return st;
+}
+
+template <typename F>
+pwmgpu_status guarded(pwmgpu_ctx* ctx, F&& f) {
+  try {
+    if (ctx) CUDA_TRY(cudaSetDevice(ctx->device));
+    return f();
+  } catch (const Fail& e) {
+    return fail(ctx, e.st, e.msg);
+  } catch (const std::bad_alloc&) {
+    return fail(ctx, PWMGPU_ERR_OOM, "host allocation failed");
+  }
+}
+
+bool valid_width(uint32_t w) { return w == 1 || w == 2 || w == 4; }
+
+// Records CUDA events on the context's stream around one launch group when
+// profiling is on; `bytes` is the algorithmic traffic of the group.
+struct ProfScope {
+  pwmgpu_ctx* ctx;
+  ProfRecord rec{};
+  uint64_t launches_before = 0;
+  ProfScope(pwmgpu_ctx* c, const char* name, uint64_t bytes) : ctx(c) {
+    if (!ctx->profiling) return;
+    rec.name = name;
+    rec.bytes = bytes;
+    rec.a = ctx->take_event();
+    rec.b = ctx->take_event();
+    launches_before = ctx->launches;
+    CUDA_TRY(cudaEventRecord(rec.a, ctx->stream));
+  }
+  ~ProfScope() {
+    if (!ctx->profiling || !rec.a) return;
+    cudaEventRecord(rec.b, ctx->stream);
+    rec.launches = ctx->launches - launches_before;
+    ctx->prof.push_back(rec);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Rank/select storage of a structure
+// ---------------------------------------------------------------------------
+uint64_t rs_n0(uint64_t nwords) { return nwords / (4294967295ull / 64) + 1; }
+uint64_t rs_n12(uint64_t nwords) { return nwords / 32 + 1; }
+uint64_t rs_ns(uint64_t nwords) { return nwords * 64 / 8192 + 2; }
+
+void alloc_rank_select(Structure& s) {
+  size_t bytes = 0;
+  std::vector<size_t> off0(s.levels), off12(s.levels), offs0(s.levels), offs1(s.levels), offm(s.levels);
+  auto take = [&](size_t b) {
+    size_t o = bytes;
+    bytes += (b + 255) & ~size_t(255);
+    return o;
+  };
+  for (uint32_t l = 0; l < s.levels; ++l) {
+    const uint64_t nw = words_for(s.bits[l]);
+    off0[l] = take(rs_n0(nw) * 8);
+    off12[l] = take(rs_n12(nw) * 8);
+    offs0[l] = take(rs_ns(nw) * 4);
+    offs1[l] = take(rs_ns(nw) * 4);
+    offm[l] = take(3 * 8);
+  }
+  s.rs_bytes = std::max<size_t>(bytes, 256);
+  CUDA_TRY(cudaMalloc(&s.d_rs, s.rs_bytes));
+  char* base = static_cast<char*>(s.d_rs);
+  s.rs_levels.resize(s.levels);
+  std::vector<QueryLevel> q(s.levels);
+  for (uint32_t l = 0; l < s.levels; ++l) {
+    auto& r = s.rs_levels[l];
+    r.data = s.d_words + s.offs[l];
+    r.nwords = words_for(s.bits[l]);
+    r.l0 = reinterpret_cast<uint64_t*>(base + off0[l]);
+    r.l12 = reinterpret_cast<uint32_t*>(base + off12[l]);
+    r.s0 = reinterpret_cast<uint32_t*>(base + offs0[l]);
+    r.s1 = reinterpret_cast<uint32_t*>(base + offs1[l]);
+    r.meta = reinterpret_cast<unsigned long long*>(base + offm[l]);
+    q[l] = QueryLevel{r.data, r.nwords, r.l0, rs_n0(r.nwords), r.l12, r.s0, r.s1, r.meta};
+  }
+  const size_t nl = std::max<uint32_t>(s.levels, 1);
+  CUDA_TRY(cudaMalloc(&s.d_rs_levels, sizeof(RankSelectLevel) * nl));
+  CUDA_TRY(cudaMalloc(&s.d_q_levels, sizeof(QueryLevel) * nl));
+  if (s.levels) {
+    CUDA_TRY(cudaMemcpy(s.d_rs_levels, s.rs_levels.data(), sizeof(RankSelectLevel) * s.levels,
+                        cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(s.d_q_levels, q.data(), sizeof(QueryLevel) * s.levels, cudaMemcpyHostToDevice));
+  }
+  s.rs = true;
+}
+
+void alloc_structure(Structure& s, const std::vector<uint64_t>& level_bits, uint64_t n, bool tree, bool huff,
+                     bool rank_select) {
+  s.release();
+  s.present = true;
+  s.is_tree = tree;
+  s.huffman = huff;
+  s.n = n;
+  s.set_layout(level_bits);
+  CUDA_TRY(cudaMalloc(&s.d_words, std::max<uint64_t>(s.total_words, 16) * 8));
+  CUDA_TRY(cudaMalloc(&s.d_zeros, std::max<uint32_t>(s.levels, 1) * 8));
+  if (rank_select) alloc_rank_select(s);
+}
+
+// Rank/select blocks of every level of a structure (asynchronous).
+void build_rank_select(pwmgpu_ctx* ctx, Structure& s) {
+  if (!s.rs || s.levels == 0) return;
+  CUDA_TRY(cudaMemsetAsync(s.d_rs, 0, s.rs_bytes, ctx->stream));
+  uint64_t max_real = 0;
+  for (auto& r : s.rs_levels) max_real = std::max<uint64_t>(max_real, (r.nwords + 31) / 32);
+  const uint64_t stride = max_real + (max_real + 255) / 256 + 1;
+  uint32_t* tmp = static_cast<uint32_t*>(ctx->grow("rs_tmp", std::max<uint64_t>(stride * s.levels * 4, 256)));
+  uint64_t bytes = 0;
+  for (auto& r : s.rs_levels) bytes += r.nwords * 8 + (r.nwords / 32 + 1) * 8;
+  ProfScope ps(ctx, "rank_select", bytes);
+  launch_rank_select(s.rs_levels.data(), s.levels, s.d_rs_levels, tmp, stride, ctx->stream, &ctx->launches);
+}
+
+uint32_t read_status(pwmgpu_ctx* ctx) {
+  uint32_t st = 0;
+  CUDA_TRY(cudaMemcpyAsync(&st, ctx->d_status, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return st;
+}
+
+void check_device_status(pwmgpu_ctx* ctx) {
+  const uint32_t st = read_status(ctx);
+  if (st & kErrSymbol) throw Fail{PWMGPU_ERR_SYMBOL, "a text symbol is >= 2^levels (or has no Huffman code)"};
+  if (st & kErrTimeout) throw Fail{PWMGPU_ERR_TIMEOUT, "a device-side look-back wait gave up"};
+  if (st & kErrBounds) throw Fail{PWMGPU_ERR_CUDA, "a device-side bounds check tripped"};
+}
+
+// ---------------------------------------------------------------------------
+// The matrix passes and the tree regroup, shared by plain and Huffman builds
+// ---------------------------------------------------------------------------
+// keys: the level-0 sequence (text or Huffman keys) of `key_bytes` per
+// element.  Builds the matrix levels into `wm` and, if wanted, the tree
+// levels into `wt`.
+void run_passes(pwmgpu_ctx* ctx, const void* keys, uint32_t key_bytes, uint32_t text_bytes, bool huff, uint32_t L,
+                const std::vector<PassPlan>& plan, const LevelTables& tabs, Structure& wm, Structure* wt) {
+  cudaStream_t s = ctx->stream;
+  // Device copies of the per-pass run starts.
+  size_t start_words = 0;
+  for (auto& st : tabs.starts) start_words += st.size();
+  std::vector<uint64_t> flat_starts;
+  flat_starts.reserve(start_words);
+  for (auto& st : tabs.starts) flat_starts.insert(flat_starts.end(), st.begin(), st.end());
+  uint64_t* d_starts = static_cast<uint64_t*>(ctx->grow("starts", std::max<size_t>(start_words, 1) * 8));
+  CUDA_TRY(cudaMemcpyAsync(d_starts, flat_starts.data(), start_words * 8, cudaMemcpyHostToDevice, s));
+
+  // Inner levels of a pass are written with OR at run edges: zero them.
+  for (const auto& p : plan)
+    for (int j = 1; j < p.K; ++j) {
+      const uint32_t m = p.level + uint32_t(j);
+      CUDA_TRY(cudaMemsetAsync(wm.d_words + wm.offs[m], 0, words_for(wm.bits[m]) * 8, s));
+    }
+
+  const uint64_t n0 = tabs.level_bits.empty() ? 0 : tabs.level_bits[0];
+  const uint32_t T = split_tile_elems(key_bytes);
+  void* ping = ctx->grow("keys_a", std::max<uint64_t>(n0, 1) * key_bytes);
+  void* pong = ctx->grow("keys_b", std::max<uint64_t>(n0, 1) * key_bytes);
+  const void* in = keys;
+  size_t start_off = 0;
+  for (size_t pi = 0; pi < plan.size(); ++pi) {
+    const auto& p = plan[pi];
+    const uint64_t m = tabs.level_bits[p.level];
+    const uint32_t tiles = uint32_t((m + T - 1) / T);
+    const int nlb = huff ? (2 << p.K) - 2 : (1 << p.K);
+    auto* lb = static_cast<unsigned long long*>(ctx->grow("lookback", std::max<uint64_t>(tiles, 1) * nlb * 8 + 64));
+    uint32_t* counter = reinterpret_cast<uint32_t*>(lb + uint64_t(std::max<uint32_t>(tiles, 1)) * nlb);
+    CUDA_TRY(cudaMemsetAsync(lb, 0, uint64_t(std::max<uint32_t>(tiles, 1)) * nlb * 8 + 64, s));
+    SplitArgs a{};
+    a.in = in;
+    a.out = p.has_out ? (in == ping ? pong : ping) : nullptr;
+    a.m = m;
+    a.level = p.level;
+    a.levels_here = uint32_t(p.K);
+    for (int j = 0; j < p.K; ++j) a.bv[j] = wm.d_words + wm.offs[p.level + j];
+    a.tree_level0 = (wt && p.level == 0) ? wt->d_words : nullptr;
+    a.starts = d_starts + start_off;
+    a.lookback = lb;
+    a.tile_counter = counter;
+    a.status = ctx->d_status;
+    a.tiles = tiles;
+    for (int j = 0; j <= p.K; ++j)
+      a.level_size[j] = p.level + j < L ? tabs.level_bits[p.level + j] : 0;
+    {
+      uint64_t bytes = 0;
+      for (int j = 0; j < p.K; ++j) {
+        const uint64_t mj = tabs.level_bits[p.level + j];
+        bytes += mj * text_bytes + words_for(mj) * 8;
+      }
+      ProfScope ps(ctx, "split_pass", bytes);
+      launch_split_pass(key_bytes, huff, p.K, a, L, s, &ctx->launches);
+    }
+    CUDA_TRY(cudaGetLastError());
+    start_off += tabs.starts[pi].size();
+    if (p.has_out) in = a.out;
+  }
+
+  if (wt) {
+    // Tree levels 1..L-1: the matrix level with its prefix groups reordered.
+    size_t seg_words = 0;
+    for (uint32_t m = 1; m < L; ++m) seg_words += 2 * tabs.seg_tree[m].size();
+    std::vector<uint64_t> segs;
+    segs.reserve(seg_words);
+    for (uint32_t m = 1; m < L; ++m) {
+      segs.insert(segs.end(), tabs.seg_tree[m].begin(), tabs.seg_tree[m].end());
+      segs.insert(segs.end(), tabs.seg_matrix[m].begin(), tabs.seg_matrix[m].end());
+    }
+    uint64_t* d_segs = static_cast<uint64_t*>(ctx->grow("segs", std::max<size_t>(seg_words, 1) * 8));
+    if (seg_words) CUDA_TRY(cudaMemcpyAsync(d_segs, segs.data(), seg_words * 8, cudaMemcpyHostToDevice, s));
+    size_t off = 0;
+    for (uint32_t m = 1; m < L; ++m) {
+      const uint64_t ns = tabs.seg_tree[m].size();
+      ProfScope ps(ctx, "regroup", 2 * words_for(wm.bits[m]) * 8);
+      launch_regroup(wm.d_words + wm.offs[m], wt->d_words + wt->offs[m], wm.bits[m], d_segs + off, d_segs + off + ns,
+                     ns, ctx->d_status, s, &ctx->launches);
+      off += 2 * ns;
+    }
+    CUDA_TRY(cudaGetLastError());
+  }
+  // host segment vectors must outlive the async copies
+  CUDA_TRY(cudaStreamSynchronize(s));
+}
+
+void validate_plain(uint64_t n, uint32_t width, uint32_t levels) {
+  if (!valid_width(width)) throw Fail{PWMGPU_ERR_ARG, "word_width must be 1, 2 or 4"};
+  if (levels == 0 || levels > kMaxPlainLevels)
+    throw Fail{PWMGPU_ERR_ARG, "levels must be in 1..24 (the leaf histogram has 2^levels bins)"};
+  if (n >= (uint64_t(1) << 62)) throw Fail{PWMGPU_ERR_ARG, "size too large"};
+}
+
+// Plain build of a wx from a device text.
+void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text) {
+  cudaStream_t s = ctx->stream;
+  const uint32_t L = wx->levels;
+  const uint64_t n = wx->n;
+  if (n == 0) return;
+  CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, 4, s));
+  const uint64_t bins = uint64_t(1) << L;
+  auto* d_hist = static_cast<unsigned long long*>(ctx->grow("hist", bins * 8));
+  CUDA_TRY(cudaMemsetAsync(d_hist, 0, bins * 8, s));
+  {
+    ProfScope ps(ctx, "leaf_histogram", n * wx->width);
+    launch_leaf_histogram(d_text, n, wx->width, L, d_hist, ctx->d_status, s, &ctx->launches);
+  }
+  CUDA_TRY(cudaGetLastError());
+  std::vector<uint64_t> hist(bins);
+  CUDA_TRY(cudaMemcpyAsync(hist.data(), d_hist, bins * 8, cudaMemcpyDeviceToHost, s));
+  check_device_status(ctx);  // synchronises
+  const auto plan = plan_passes(L, ctx->pass_levels);
+  const bool want_tree = wx->wt.present;
+  const LevelTables tabs = build_tables_plain(hist, L, plan, want_tree);
+  wx->wm.zeros = tabs.zeros;
+  CUDA_TRY(cudaMemcpyAsync(wx->wm.d_zeros, wx->wm.zeros.data(), L * 8, cudaMemcpyHostToDevice, s));
+  run_passes(ctx, d_text, wx->width, wx->width, false, L, plan, tabs, wx->wm, want_tree ? &wx->wt : nullptr);
+  if (wx->wm.rs && !wx->wm_internal) build_rank_select(ctx, wx->wm);
+  if (want_tree && wx->wt.rs) build_rank_select(ctx, wx->wt);
+  CUDA_TRY(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------
+// Huffman codes: pwm's canonical_huff_codes (include/huffman/huff_codes.hpp:
+// 140-285) with the same standard containers, so that priority-queue and
+// sort ties break the same way.
+// ---------------------------------------------------------------------------
+struct HuffCodes {
+  std::vector<uint64_t> len, word, level_sizes;
+  uint32_t levels = 0;
+};
+
+// entries: (symbol, frequency) in pwm's histogram order.
+HuffCodes build_huffman_codes(const std::vector<std::pair<uint64_t, uint64_t>>& entries, uint64_t max_symbol,
+                              bool is_tree) {
+  HuffCodes h;
+  if (entries.empty()) return h;
+  const uint64_t nsym = max_symbol + 1;
+  std::vector<uint64_t> freq(nsym, 0);
+  for (const auto& e : entries) freq[e.first] = e.second;
+  struct Item {
+    uint64_t occ;
+    std::vector<uint64_t> syms;
+    bool operator>(const Item& o) const { return occ > o.occ; }
+  };
+  std::priority_queue<Item, std::vector<Item>, std::greater<Item>> pq;
+  h.len.assign(nsym, 0);
+  h.word.assign(nsym, 0);
+  for (const auto& e : entries) pq.emplace(Item{e.second, std::vector<uint64_t>{e.first}});
+  if (pq.size() == 1) ++h.len[pq.top().syms.front()];
+  while (pq.size() > 1) {
+    Item a = pq.top();
+    pq.pop();
+    Item b = pq.top();
+    pq.pop();
+    std::move(b.syms.begin(), b.syms.end(), std::back_inserter(a.syms));
+    for (uint64_t c : a.syms) ++h.len[c];
+    pq.emplace(Item{a.occ + b.occ, a.syms});
+  }
+  std::vector<uint64_t> order(nsym);
+  std::iota(order.begin(), order.end(), uint64_t(0));
+  std::sort(order.begin(), order.end(), [&](uint64_t a, uint64_t b) { return h.len[a] < h.len[b]; });
+  h.levels = uint32_t(h.len[order.back()]);
+  std::vector<uint64_t> sizes(h.levels, 0);
+  uint64_t k = 0;
+  while (k < nsym && h.len[order[k]] == 0) ++k;
+  if (!is_tree) {
+    uint64_t cur = 1;
+    std::vector<uint64_t> words{0, 1};
+    while (k < nsym) {
+      if (h.len[order[k]] > cur) {
+        for (uint64_t i = cur; i < h.len[order[k]]; ++i) {
+          std::vector<uint64_t> nw;
+          nw.reserve(words.size() * 2);
+          for (uint64_t cw : words) nw.push_back(cw << 1);
+          for (uint64_t cw : words) nw.push_back((cw << 1) + 1);
+          words = std::move(nw);
+        }
+        cur = h.len[order[k]];
+      }
+      while (k < nsym && h.len[order[k]] == cur) {
+        const uint64_t sy = order[k++];
+        h.word[sy] = words.back();
+        words.pop_back();
+        sizes[h.len[sy] - 1] += freq[sy];
+      }
+    }
+  } else {
+    uint64_t cw = 0;
+    auto gen = [&]() {
+      const uint64_t sy = order[k];
+      h.word[sy] = (~cw) & ((uint64_t(1) << h.len[sy]) - 1);
+      sizes[h.len[sy] - 1] += freq[sy];
+    };
+    gen();
+    for (++k; k < nsym; ++k) {
+      cw = (cw + 1) << (h.len[order[k]] - h.len[order[k - 1]]);
+      gen();
+    }
+  }
+  for (uint64_t i = h.levels - 1; i > 0; --i) sizes[i - 1] += sizes[i];
+  h.level_sizes = sizes;
+  return h;
+}
+
+// pwm's histogram order (include/util/histogram.hpp:39-76): ascending symbols
+// for 8-bit texts; for wider texts the iteration order of a
+// std::unordered_map filled in order of first occurrence.
+template <typename A>
+std::vector<std::pair<uint64_t, uint64_t>> histogram_order(const std::vector<uint64_t>& count,
+                                                           const std::vector<uint64_t>& first, uint32_t width) {
+  std::vector<std::pair<uint64_t, uint64_t>> out;
+  if (width == 1) {
+    for (uint64_t c = 0; c < count.size(); ++c)
+      if (count[c]) out.emplace_back(c, count[c]);
+    return out;
+  }
+  std::vector<uint64_t> syms;
+  for (uint64_t c = 0; c < count.size(); ++c)
+    if (count[c]) syms.push_back(c);
+  std::sort(syms.begin(), syms.end(), [&](uint64_t a, uint64_t b) { return first[a] < first[b]; });
+  std::unordered_map<A, uint64_t> m;
+  for (uint64_t c : syms) m.emplace(A(c), count[c]);
+  for (const auto& e : m) out.emplace_back(uint64_t(e.first), e.second);
+  return out;
+}
+
+// Symbol histogram + first occurrences of a device text on the GPU, then the
+// code builder on the host.
+HuffCodes huffman_codes_device(pwmgpu_ctx* ctx, const void* d_text, uint64_t n, uint32_t width, bool is_tree,
+                               uint64_t* max_symbol_out) {
+  cudaStream_t s = ctx->stream;
+  uint64_t nsym = width == 1 ? 256 : (width == 2 ? 65536 : 0);
+  if (width == 4) {
+    // bound the alphabet by the largest symbol (one histogram bin per value)
+    throw Fail{PWMGPU_ERR_ARG, "Huffman codes for 32-bit texts: pass a code table"};
+  }
+  auto* d_hist = static_cast<unsigned long long*>(ctx->grow("sym_hist", nsym * 8));
+  auto* d_first = static_cast<unsigned long long*>(ctx->grow("sym_first", nsym * 8));
+  CUDA_TRY(cudaMemsetAsync(d_hist, 0, nsym * 8, s));
+  CUDA_TRY(cudaMemsetAsync(d_first, 0xFF, nsym * 8, s));
+  launch_symbol_histogram(d_text, n, width, nsym, d_hist, width == 1 ? nullptr : d_first, s, &ctx->launches);
+  std::vector<uint64_t> count(nsym), first(nsym);
+  CUDA_TRY(cudaMemcpyAsync(count.data(), d_hist, nsym * 8, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaMemcpyAsync(first.data(), d_first, nsym * 8, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  uint64_t max_symbol = 0;
+  for (uint64_t c = 0; c < nsym; ++c)
+    if (count[c]) max_symbol = c;
+  *max_symbol_out = max_symbol;
+  auto entries = width == 1 ? histogram_order<uint8_t>(count, first, 1) : histogram_order<uint16_t>(count, first, 2);
+  return build_huffman_codes(entries, max_symbol, is_tree);
+}
+
+// Huffman build of one structure (matrix, or tree through the matrix).
+// Returns the level sizes.
+void build_huffman(pwmgpu_ctx* ctx, const void* d_text, uint64_t n, uint32_t width, bool is_tree,
+                   const std::vector<uint64_t>& code_len, const std::vector<uint64_t>& code_word, uint32_t levels,
+                   Structure& wm, Structure* wt, bool rank_select) {
+  cudaStream_t s = ctx->stream;
+  const uint64_t ncodes = code_len.size();
+  // symbol histogram for the weighted codes
+  const uint64_t nsym = ncodes;
+  auto* d_hist = static_cast<unsigned long long*>(ctx->grow("sym_hist", std::max<uint64_t>(nsym, 1) * 8));
+  CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, 4, s));
+  CUDA_TRY(cudaMemsetAsync(d_hist, 0, std::max<uint64_t>(nsym, 1) * 8, s));
+  launch_symbol_histogram(d_text, n, width, nsym, d_hist, nullptr, s, &ctx->launches);
+  std::vector<uint64_t> count(nsym);
+  CUDA_TRY(cudaMemcpyAsync(count.data(), d_hist, nsym * 8, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  uint64_t counted = 0;
+  std::vector<WeightedCode> wc;
+  for (uint64_t c = 0; c < nsym; ++c) {
+    counted += count[c];
+    if (count[c]) {
+      if (code_len[c] == 0 || code_len[c] > 56) throw Fail{PWMGPU_ERR_ARG, "a text symbol has no usable code"};
+      wc.push_back({code_word[c], uint32_t(code_len[c]), count[c]});
+    }
+  }
+  if (counted != n) throw Fail{PWMGPU_ERR_SYMBOL, "a text symbol is outside the code table"};
+  uint32_t maxlen = 0;
+  for (auto& c : wc) maxlen = std::max(maxlen, c.len);
+  if (maxlen != levels) throw Fail{PWMGPU_ERR_ARG, "levels must equal the longest code length"};
+  const uint32_t key_bytes = maxlen <= 24 ? 4 : 8;
+  const auto plan = plan_passes(levels, ctx->pass_levels);
+  const LevelTables tabs = build_tables(wc, levels, plan, wt != nullptr);
+  // layouts
+  alloc_structure(wm, tabs.level_bits, n, false, true, rank_select && !is_tree);
+  wm.zeros = tabs.zeros;
+  CUDA_TRY(cudaMemcpyAsync(wm.d_zeros, wm.zeros.data(), levels * 8, cudaMemcpyHostToDevice, s));
+  if (wt) alloc_structure(*wt, tabs.level_bits, n, true, true, rank_select);
+  // code keys
+  uint64_t* d_len = static_cast<uint64_t*>(ctx->grow("code_len", std::max<uint64_t>(ncodes, 1) * 8));
+  uint64_t* d_word = static_cast<uint64_t*>(ctx->grow("code_word", std::max<uint64_t>(ncodes, 1) * 8));
+  CUDA_TRY(cudaMemcpyAsync(d_len, code_len.data(), ncodes * 8, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(d_word, code_word.data(), ncodes * 8, cudaMemcpyHostToDevice, s));
+  void* keys = ctx->grow("huff_keys", std::max<uint64_t>(n, 1) * key_bytes);
+  launch_huffman_keys(d_text, n, width, d_len, d_word, ncodes, key_bytes, keys, ctx->d_status, s, &ctx->launches);
+  run_passes(ctx, keys, key_bytes, width, true, levels, plan, tabs, wm, wt);
+  check_device_status(ctx);
+  if (!is_tree && wm.rs) build_rank_select(ctx, wm);
+  if (wt && wt->rs) build_rank_select(ctx, *wt);
+}
+
+// Host thresholds / permutation of a generator distribution.
+struct GenTables {
+  std::vector<uint64_t> thr;
+  std::vector<uint32_t> perm;
+};
+
+std::vector<uint64_t> thresholds_from_weights(const std::vector<double>& w) {
+  double total = 0;
+  for (double x : w) total += x;
+  std::vector<uint64_t> thr(w.size());
+  double cum = 0;
+  const double scale = 9007199254740992.0;  // 2^53
+  for (size_t i = 0; i < w.size(); ++i) {
+    cum += w[i];
+    double v = (cum / total) * scale;
+    thr[i] = v >= scale ? (uint64_t(1) << 53) : uint64_t(v);
+  }
+  thr.back() = uint64_t(1) << 53;
+  return thr;
+}
+
+GenTables gen_tables(int dist, uint64_t seed) {
+  GenTables g;
+  if (dist == PWMGPU_GEN_DNA4) {
+    g.thr = thresholds_from_weights({0.3, 0.2, 0.2, 0.3});
+  } else if (dist == PWMGPU_GEN_ZIPF256) {
+    std::vector<double> w(256);
+    for (int r = 1; r <= 256; ++r) w[size_t(r - 1)] = 1.0 / double(r);
+    g.thr = thresholds_from_weights(w);
+    g.perm.resize(256);
+    std::iota(g.perm.begin(), g.perm.end(), 0u);
+    const uint64_t pkey = mix64(seed ^ 0x5bd1e9955bd1e995ull);
+    for (uint32_t j = 255; j > 0; --j) {
+      const uint32_t k = uint32_t(mix64(pkey + j) % (j + 1));
+      std::swap(g.perm[j], g.perm[k]);
+    }
+  } else if (dist == PWMGPU_GEN_MIX16) {
+    // geometric(p = 0.01) on {0, 1, ...} clamped to 65535: cumulative
+    // 1 - q^(k+1) with q^(k+1) by repeated multiplication.
+    const double q = 0.99;
+    std::vector<uint64_t> thr(65536);
+    double qk = 1.0;
+    const double scale = 9007199254740992.0;
+    for (uint32_t k = 0; k < 65536; ++k) {
+      qk *= q;
+      double v = (1.0 - qk) * scale;
+      thr[k] = v >= scale ? (uint64_t(1) << 53) : uint64_t(v);
+    }
+    thr.back() = uint64_t(1) << 53;
+    g.thr = std::move(thr);
+  }
+  if (g.thr.empty()) g.thr.push_back(uint64_t(1) << 53);
+  if (g.perm.empty()) g.perm.push_back(0);
+  return g;
+}
+
+}  // namespace
+
+// ===========================================================================
+// extern "C"
+// ===========================================================================
+extern "C" {
+
+const char* pwmgpu_status_string(pwmgpu_status s) {
+  switch (s) {
+    case PWMGPU_OK: return "ok";
+    case PWMGPU_ERR_ARG: return "invalid argument";
+    case PWMGPU_ERR_OOM: return "out of device memory";
+    case PWMGPU_ERR_CUDA: return "CUDA error";
+    case PWMGPU_ERR_TIMEOUT: return "device-side wait timed out";
+    case PWMGPU_ERR_SYMBOL: return "symbol out of range";
+    case PWMGPU_ERR_NO_DEVICE: return "no usable CUDA device";
+    case PWMGPU_ERR_BUSY: return "admission refused";
+  }
+  return "unknown status";
+}
+
+pwmgpu_status pwmgpu_ctx_create(int device, void* cuda_stream, pwmgpu_ctx** out) {
+  if (!out) return PWMGPU_ERR_ARG;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0 || device < 0 || device >= count) {
+    cudaGetLastError();
+    return PWMGPU_ERR_NO_DEVICE;
+  }
+  auto* ctx = new pwmgpu_ctx;
+  ctx->device = device;
+  pwmgpu_status st = guarded(ctx, [&]() {
+    if (cuda_stream) {
+      ctx->stream = static_cast<cudaStream_t>(cuda_stream);
+    } else {
+      CUDA_TRY(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+      ctx->own_stream = true;
+    }
+    CUDA_TRY(cudaMalloc(&ctx->d_status, 64));
+    CUDA_TRY(cudaMemset(ctx->d_status, 0, 64));
+    // a kernel of this library must be loadable on this device
+    cudaFuncAttributes attr;
+    cudaError_t e = cudaFuncGetAttributes(&attr, reinterpret_cast<const void*>(&pwmgpu_ctx_create));
+    (void)e;
+    cudaGetLastError();
+    return PWMGPU_OK;
+  });
+  if (st != PWMGPU_OK) {
+    delete ctx;
+    return st;
+  }
+  *out = ctx;
+  return PWMGPU_OK;
+}
+
+void pwmgpu_ctx_destroy(pwmgpu_ctx* ctx) { delete ctx; }
+
+const char* pwmgpu_ctx_last_error(const pwmgpu_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+pwmgpu_status pwmgpu_ctx_sync(pwmgpu_ctx* ctx) {
+  if (!ctx) return PWMGPU_ERR_ARG;
+  return guarded(ctx, [&]() {
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return PWMGPU_OK;
+  });
+}
+
+uint64_t pwmgpu_ctx_launch_count(const pwmgpu_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+pwmgpu_status pwmgpu_ctx_set_pass_levels(pwmgpu_ctx* ctx, int k) {
+  if (!ctx || k < 1 || k > kMaxPassLevels) return PWMGPU_ERR_ARG;
+  ctx->pass_levels = k;
+  return PWMGPU_OK;
+}
+
+pwmgpu_status pwmgpu_ctx_profile(pwmgpu_ctx* ctx, int enable) {
+  if (!ctx) return PWMGPU_ERR_ARG;
+  ctx->profiling = enable != 0;
+  return PWMGPU_OK;
+}
+
+pwmgpu_status pwmgpu_ctx_profile_read(pwmgpu_ctx* ctx, char* buf, uint64_t cap) {
+  if (!ctx || !buf || cap == 0) return PWMGPU_ERR_ARG;
+  return guarded(ctx, [&]() {
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    struct Agg { uint64_t groups = 0, launches = 0, bytes = 0; double ms = 0; };
+    std::map<std::string, Agg> agg;
+    for (auto& r : ctx->prof) {
+      float ms = 0;
+      CUDA_TRY(cudaEventElapsedTime(&ms, r.a, r.b));
+      auto& g = agg[r.name];
+      g.groups += 1;
+      g.launches += r.launches;
+      g.bytes += r.bytes;
+      g.ms += ms;
+      ctx->event_pool.push_back(r.a);
+      ctx->event_pool.push_back(r.b);
+    }
+    ctx->prof.clear();
+    std::string out;
+    char line[256];
+    for (auto& kv : agg) {
+      std::snprintf(line, sizeof(line), "%s %llu %llu %.6f %llu\n", kv.first.c_str(),
+                    (unsigned long long)kv.second.groups, (unsigned long long)kv.second.launches, kv.second.ms,
+                    (unsigned long long)kv.second.bytes);
+      out += line;
+    }
+    if (out.size() + 1 > cap) throw Fail{PWMGPU_ERR_ARG, "profile buffer too small"};
+    std::memcpy(buf, out.c_str(), out.size() + 1);
+    return PWMGPU_OK;
+  });
+}
+
+// ---- device-resident structures --------------------------------------------
+pwmgpu_status pwmgpu_wx_create(pwmgpu_ctx* ctx, uint64_t size, uint32_t word_width, uint32_t levels,
+                               uint32_t shape_flags, pwmgpu_wx** out) {
+  if (!ctx || !out) return PWMGPU_ERR_ARG;
+  *out = nullptr;
+  return guarded(ctx, [&]() {
+    validate_plain(size, word_width, levels);
+    if (!(shape_flags & (PWMGPU_MATRIX | PWMGPU_TREE))) throw Fail{PWMGPU_ERR_ARG, "need PWMGPU_MATRIX or PWMGPU_TREE"};
+    if ((shape_flags & PWMGPU_RANK_SELECT) && size >= 4294967295ull - 64)
+      throw Fail{PWMGPU_ERR_ARG, "rank/select support needs levels below 2^32-1 bits"};
+    auto wx = std::make_unique<pwmgpu_wx>();
+    wx->ctx = ctx;
+    wx->n = size;
+    wx->width = word_width;
+    wx->levels = levels;
+    wx->flags = shape_flags;
+    const bool rs = shape_flags & PWMGPU_RANK_SELECT;
+    std::vector<uint64_t> bits(levels, size);
+    alloc_structure(wx->wm, bits, size, false, false, rs && (shape_flags & PWMGPU_MATRIX));
+    wx->wm_internal = !(shape_flags & PWMGPU_MATRIX);
+    if (shape_flags & PWMGPU_TREE) alloc_structure(wx->wt, bits, size, true, false, rs);
+    *out = wx.release();
+    return PWMGPU_OK;
+  });
+}
+
+pwmgpu_status pwmgpu_wx_build(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text) {
+  if (!ctx || !wx || (!d_text && wx->n)) return PWMGPU_ERR_ARG;
+  return guarded(ctx, [&]() {
+    build_plain(ctx, wx, d_text);
+    return PWMGPU_OK;
+  });
+}
+
+pwmgpu_status pwmgpu_wx_build_host(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* host_text) {
+  if (!ctx || !wx || (!host_text && wx->n)) return PWMGPU_ERR_ARG;
+  return guarded(ctx, [&]() {
+    void* d_text = ctx->grow("host_text", std::max<uint64_t>(wx->n * wx->width, 1));
+    if (wx->n)
+      CUDA_TRY(cudaMemcpyAsync(d_text, host_text, wx->n * wx->width, cudaMemcpyHostToDevice, ctx->stream));
+    build_plain(ctx, wx, d_text);
+    return PWMGPU_OK;
+  });
+}
+
+pwmgpu_status pwmgpu_wx_check(pwmgpu_ctx* ctx, pwmgpu_wx* wx) {
+  if (!ctx || !wx) return PWMGPU_ERR_ARG;
+  return guarded(ctx, [&]() {
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    CUDA_TRY(cudaGetLastError());
+    check_device_status(ctx);
+    return PWMGPU_OK;
+  });
+}
+
+pwmgpu_status pwmgpu_wx_view(const pwmgpu_wx* wx, int which, pwmgpu_view* v) {
+  if (!wx || !v) return PWMGPU_ERR_ARG;
+  const Structure& s = which ? wx->wt : wx->wm;
+  if (!s.present || (which == 0 && wx->wm_internal)) return PWMGPU_ERR_ARG;
+  v->levels = s.levels;
+  v->is_tree = s.is_tree;
+  v->is_huffman = s.huffman;
+  v->has_rank_select = s.rs;
+  v->size = s.n;
+  v->total_words = s.total_words;
+  v->words = s.d_words;
+  v->level_offset = s.offs.data();
+  v->level_bits = s.bits.data();
+  v->zeros = s.is_tree ? nullptr : s.zeros.data();
+  return PWMGPU_OK;
+}
+
+pwmgpu_status pwmgpu_wx_download(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which, uint64_t* bv, uint64_t* zeros) {
+  if (!ctx || !wx || !bv) return PWMGPU_ERR_ARG;
+  const Structure& s = which ? wx->wt : wx->wm;
+  if (!s.present) return PWMGPU_ERR_ARG;
+  return guarded(ctx, [&]() {
+    if (s.total_words)
+      CUDA_TRY(cudaMemcpyAsync(bv, s.d_words, s.total_words * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    if (zeros && !s.is_tree) std::memcpy(zeros, s.zeros.data(), s.levels * 8);
+    return PWMGPU_OK;
+  });
+}
+
+pwmgpu_status pwmgpu_wx_rank_select_blocks(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which, uint32_t level,
+                                           uint64_t* l0, uint32_t* l12, uint32_t* s0, uint32_t* s1, uint64_t* counts) {
+  if (!ctx || !wx || !counts) return PWMGPU_ERR_ARG;
+  const Structure& s = which ? wx->wt : wx->wm;
+  if (!s.present || !s.rs || level >= s.levels) return PWMGPU_ERR_ARG;
+  return guarded(ctx, [&]() {
+    const RankSelectLevel& r = s.rs_levels[level];
+    uint64_t meta[3];
+    CUDA_TRY(cudaMemcpyAsync(meta, r.meta, 24, cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    counts[0] = rs_n0(r.nwords);
+    counts[1] = rs_n12(r.nwords);
+    counts[2] = meta[0];
+    counts[3] = meta[1];
+    if (l0) CUDA_TRY(cudaMemcpyAsync(l0, r.l0, counts[0] * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if (l12) CUDA_TRY(cudaMemcpyAsync(l12, r.l12, counts[1] * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if (s0 && counts[2]) CUDA_TRY(cudaMemcpyAsync(s0, r.s0, counts[2] * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (s1 && counts[3]) CUDA_TRY(cudaMemcpyAsync(s1, r.s1, counts[3] * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return PWMGPU_OK;
+  });
+}
+
+pwmgpu_status pwmgpu_wx_query(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which, int op, const uint64_t* d_a,
+                              const uint64_t* d_b, uint64_t count, uint64_t* d_out) {
+  if (!ctx || !wx || op < 0 || op > 2 || (count && (!d_a || !d_out || (op > 0 && !d_b)))) return PWMGPU_ERR_ARG;
+  const Structure& s = which ? wx->wt : wx->wm;
+  if (!s.present || !s.rs || s.huffman) return fail(ctx, PWMGPU_ERR_ARG, "queries need a plain structure with rank/select");
+  return guarded(ctx, [&]() {
+    QueryStructure q{s.levels, s.is_tree ? 1u : 0u, s.n, s.d_q_levels, s.d_zeros};
+    ProfScope ps(ctx, "queries", count * 24);
+    launch_queries(q, op, d_a, d_b, count, d_out, ctx->stream, &ctx->launches);
+    CUDA_TRY(cudaGetLastError());
+    return PWMGPU_OK;
+  });
+}
+
+void pwmgpu_wx_free(pwmgpu_wx* wx) {
+  if (!wx) return;
+  if (wx->ctx) cudaSetDevice(wx->ctx->device);
+  delete wx;
+}
+
+// ---- drop-in host-to-host builds ------------------------------------------------
+pwmgpu_status pwmgpu_compute(pwmgpu_ctx* ctx, const void* text, uint64_t size, uint32_t word_width, uint32_t levels,
+                             int is_tree, uint64_t* bv, uint64_t* zeros) {
+  if (!ctx) return PWMGPU_ERR_ARG;
+  if (size == 0) return PWMGPU_OK;  // pwm: empty structure
+  if (!text || !bv || (!is_tree && !zeros)) return fail(ctx, PWMGPU_ERR_ARG, "null text, bv or zeros");
+  return guarded(ctx, [&]() {
+    validate_plain(size, word_width, levels);
+    const uint32_t shape = is_tree ? PWMGPU_TREE : PWMGPU_MATRIX;
+    pwmgpu_wx*& wx = ctx->compute_cache;
+    if (!wx || wx->n != size || wx->width != word_width || wx->levels != levels || wx->flags != shape) {
+      delete wx;
+      wx = nullptr;
+      pwmgpu_status st = pwmgpu_wx_create(ctx, size, word_width, levels, shape, &wx);
+      if (st != PWMGPU_OK) return st;
+    }
+    void* d_text = ctx->grow("host_text", size * word_width);
+    CUDA_TRY(cudaMemcpyAsync(d_text, text, size * word_width, cudaMemcpyHostToDevice, ctx->stream));
+    build_plain(ctx, wx, d_text);
+    const Structure& s = is_tree ? wx->wt : wx->wm;
+    CUDA_TRY(cudaMemcpyAsync(bv, s.d_words, s.total_words * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    check_device_status(ctx);
+    if (!is_tree) std::memcpy(zeros, s.zeros.data(), levels * 8);
+    return PWMGPU_OK;
+  });
+}
+
+pwmgpu_status pwmgpu_huffman_codes(pwmgpu_ctx* ctx, const void* text, uint64_t size, uint32_t word_width, int is_tree,
+                                   uint64_t* code_len, uint64_t* code_word, uint64_t cap, uint64_t* num_codes,
+                                   uint64_t* level_sizes, uint32_t* levels) {
+  if (!ctx || !num_codes || !levels) return PWMGPU_ERR_ARG;
+  *num_codes = 0;
+  *levels = 0;
+  if (size == 0) return PWMGPU_OK;
+  if (!text) return PWMGPU_ERR_ARG;
+  return guarded(ctx, [&]() {
+    if (word_width != 1 && word_width != 2)
+      throw Fail{PWMGPU_ERR_ARG, "the code builder takes 8- or 16-bit texts; pass a code table for wider ones"};
+    void* d_text = ctx->grow("host_text", size * word_width);
+    CUDA_TRY(cudaMemcpyAsync(d_text, text, size * word_width, cudaMemcpyHostToDevice, ctx->stream));
+    uint64_t max_symbol = 0;
+    HuffCodes h = huffman_codes_device(ctx, d_text, size, word_width, is_tree != 0, &max_symbol);
+    if (h.levels > kMaxLevels) throw Fail{PWMGPU_ERR_ARG, "codes longer than 64 bits"};
+    *num_codes = max_symbol + 1;
+    *levels = h.levels;
+    if (code_len && code_word) {
+      if (cap < max_symbol + 1) throw Fail{PWMGPU_ERR_ARG, "code table capacity too small"};
+      std::memcpy(code_len, h.len.data(), (max_symbol + 1) * 8);
+      std::memcpy(code_word, h.word.data(), (max_symbol + 1) * 8);
+    }
+    if (level_sizes) std::memcpy(level_sizes, h.level_sizes.data(), h.levels * 8);
+    return PWMGPU_OK;
+  });
+}
+
+pwmgpu_status pwmgpu_compute_huffman(pwmgpu_ctx* ctx, const void* text, uint64_t size, uint32_t word_width,
+                                     int is_tree, const uint64_t* code_len, const uint64_t* code_word,
+                                     uint64_t num_codes, uint32_t levels, const uint64_t* level_sizes, uint64_t* bv,
+                                     uint64_t* zeros) {
+  if (!ctx) return PWMGPU_ERR_ARG;
+  if (size == 0) return PWMGPU_OK;
+  if (!text || !bv || (!is_tree && !zeros)) return fail(ctx, PWMGPU_ERR_ARG, "null text, bv or zeros");
+  return guarded(ctx, [&]() {
+    if (!valid_width(word_width)) throw Fail{PWMGPU_ERR_ARG, "word_width must be 1, 2 or 4"};
+    void* d_text = ctx->grow("host_text", size * word_width);
+    CUDA_TRY(cudaMemcpyAsync(d_text, text, size * word_width, cudaMemcpyHostToDevice, ctx->stream));
+    std::vector<uint64_t> len, word;
+    uint32_t L = levels;
+    if (code_len) {
+      if (!code_word || num_codes == 0) throw Fail{PWMGPU_ERR_ARG, "code table incomplete"};
+      len.assign(code_len, code_len + num_codes);
+      word.assign(code_word, code_word + num_codes);
+    } else {
+      uint64_t max_symbol = 0;
+      HuffCodes h = huffman_codes_device(ctx, d_text, size, word_width, is_tree != 0, &max_symbol);
+      len = h.len;
+      word = h.word;
+      L = h.levels;
+    }
+    Structure wm, wt;
+    build_huffman(ctx, d_text, size, word_width, is_tree != 0, len, word, L, wm, is_tree ? &wt : nullptr, false);
+    const Structure& s = is_tree ? wt : wm;
+    if (level_sizes)
+      for (uint32_t l = 0; l < L; ++l)
+        if (level_sizes[l] != s.bits[l]) throw Fail{PWMGPU_ERR_ARG, "level_sizes do not match the code table"};
+    CUDA_TRY(cudaMemcpyAsync(bv, s.d_words, s.total_words * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    if (!is_tree) std::memcpy(zeros, wm.zeros.data(), L * 8);
+    wm.release();
+    wt.release();
+    return PWMGPU_OK;
+  });
+}
+
+// ---- generators ------------------------------------------------------------------
+pwmgpu_status pwmgpu_generate(pwmgpu_ctx* ctx, int dist, uint64_t seed, uint64_t param, uint64_t n,
+                              uint32_t word_width, void* out, int on_device) {
+  if (!valid_width(word_width) || (n && !out) || dist < 0 || dist > 3) return PWMGPU_ERR_ARG;
+  GenTables g = gen_tables(dist, seed);
+  const uint64_t key = mix64(seed);
+  if (!on_device) {
+    for (uint64_t i = 0; i < n; ++i) {
+      const uint64_t v = gen_value(dist, key, param, i, g.thr.data(), uint32_t(g.thr.size()), g.perm.data());
+      if (word_width == 1) static_cast<uint8_t*>(out)[i] = uint8_t(v);
+      else if (word_width == 2) static_cast<uint16_t*>(out)[i] = uint16_t(v);
+      else static_cast<uint32_t*>(out)[i] = uint32_t(v);
+    }
+    return PWMGPU_OK;
+  }
+  if (!ctx) return PWMGPU_ERR_ARG;
+  return guarded(ctx, [&]() {
+    auto* d_thr = static_cast<uint64_t*>(ctx->grow("gen_thr", g.thr.size() * 8));
+    auto* d_perm = static_cast<uint32_t*>(ctx->grow("gen_perm", g.perm.size() * 4));
+    CUDA_TRY(cudaMemcpyAsync(d_thr, g.thr.data(), g.thr.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CUDA_TRY(cudaMemcpyAsync(d_perm, g.perm.data(), g.perm.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    launch_generate(dist, seed, param, n, word_width, out, d_thr, uint32_t(g.thr.size()), d_perm, ctx->stream,
+                    &ctx->launches);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return PWMGPU_OK;
+  });
+}
+
+}  // extern "C"

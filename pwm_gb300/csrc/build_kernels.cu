@@ -1,0 +1,247 @@
+// Histogram, wavelet-tree regroup, Huffman key and generator kernels.
+#include "gen.cuh"
+#include "kernels.cuh"
+
+namespace pwmgpu {
+
+namespace {
+
+constexpr int kHistThreads = 512;
+
+template <typename T, typename F>
+__device__ __forceinline__ void for_each_symbol_vec(const T* text, uint64_t n, uint64_t tid, uint64_t nthreads,
+                                                    F&& f) {
+  // 16-byte vectors over the aligned body, then the tail element by element.
+  constexpr int PER = 16 / sizeof(T);
+  const uint64_t nvec = (reinterpret_cast<uintptr_t>(text) % 16 == 0) ? n / PER : 0;
+  const uint4* v = reinterpret_cast<const uint4*>(text);
+  for (uint64_t i = tid; i < nvec; i += nthreads) {
+    uint4 x = __ldcs(v + i);
+    const T* s = reinterpret_cast<const T*>(&x);
+#pragma unroll
+    for (int k = 0; k < PER; ++k) f(uint64_t(s[k]));
+  }
+  for (uint64_t i = nvec * PER + tid; i < n; i += nthreads) f(uint64_t(text[i]));
+}
+
+// L <= 8: one 256-bin sub-histogram per warp; 9..13: one per CTA.
+template <typename T, int BINS, bool PER_WARP>
+__global__ void __launch_bounds__(kHistThreads) leaf_hist_smem(const T* text, uint64_t n, uint32_t levels,
+                                                               unsigned long long* hist, uint32_t* status) {
+  constexpr int WARPS = kHistThreads / 32;
+  constexpr int COPIES = PER_WARP ? WARPS : 1;
+  __shared__ uint32_t h[COPIES * BINS];
+  for (int i = threadIdx.x; i < COPIES * BINS; i += kHistThreads) h[i] = 0;
+  __syncthreads();
+  uint32_t* mine = h + (PER_WARP ? (threadIdx.x >> 5) * BINS : 0);
+  const uint64_t limit = 1ull << levels;
+  bool bad = false;
+  for_each_symbol_vec<T>(text, n, uint64_t(blockIdx.x) * kHistThreads + threadIdx.x,
+                         uint64_t(gridDim.x) * kHistThreads, [&](uint64_t c) {
+                           if (c >= limit) { bad = true; return; }
+                           atomicAdd(&mine[c], 1u);
+                         });
+  if (bad) atomicOr(status, kErrSymbol);
+  __syncthreads();
+  for (int b = threadIdx.x; b < int(limit); b += kHistThreads) {
+    uint64_t s = 0;
+    for (int w = 0; w < COPIES; ++w) s += h[w * BINS + b];
+    if (s) atomicAdd(&hist[b], (unsigned long long)s);
+  }
+}
+
+// L >= 14: global atomics, lanes holding the same symbol combined first.
+template <typename T>
+__global__ void __launch_bounds__(kHistThreads) leaf_hist_global(const T* text, uint64_t n, uint32_t levels,
+                                                                 unsigned long long* hist, uint32_t* status) {
+  const uint64_t limit = 1ull << levels;
+  const int lane = threadIdx.x & 31;
+  const uint64_t warp_id = (uint64_t(blockIdx.x) * kHistThreads + threadIdx.x) >> 5;
+  const uint64_t warps = (uint64_t(gridDim.x) * kHistThreads) >> 5;
+  bool bad = false;
+  for (uint64_t base = warp_id * 32; base < n; base += warps * 32) {
+    uint64_t i = base + lane;
+    uint64_t c = i < n ? uint64_t(text[i]) : ~0ull;
+    bool ok = i < n && c < limit;
+    if (i < n && c >= limit) bad = true;
+    uint32_t key = ok ? uint32_t(c) : 0xFFFFFFFFu;
+    uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+    if (ok && lane == __ffs(peers) - 1) atomicAdd(&hist[c], (unsigned long long)__popc(peers));
+  }
+  if (bad) atomicOr(status, kErrSymbol);
+}
+
+int hist_grid(uint64_t n, uint32_t width) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  uint64_t per_block = uint64_t(kHistThreads) * (16 / width) * 4;
+  uint64_t want = (n + per_block - 1) / per_block;
+  uint64_t cap = uint64_t(sms > 0 ? sms : 148) * 4;
+  return int(want < 1 ? 1 : (want > cap ? cap : want));
+}
+
+template <typename T>
+void hist_dispatch(const T* text, uint64_t n, uint32_t levels, unsigned long long* hist, uint32_t* status,
+                   cudaStream_t s) {
+  int grid = hist_grid(n, sizeof(T));
+  if (levels <= 8)
+    leaf_hist_smem<T, 256, true><<<grid, kHistThreads, 0, s>>>(text, n, levels, hist, status);
+  else if (levels <= 13)
+    leaf_hist_smem<T, 8192, false><<<grid, kHistThreads, 0, s>>>(text, n, levels, hist, status);
+  else
+    leaf_hist_global<T><<<grid, kHistThreads, 0, s>>>(text, n, levels, hist, status);
+}
+
+// ---------------------------------------------------------------------------
+// Tree level from the matrix level: one thread per output word gathers the
+// bit ranges of the prefix groups that cover it.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t bits_at(const uint64_t* level, uint64_t src, uint32_t take) {
+  // `take` (1..64) bits starting at bit position src, left-aligned.
+  const uint64_t w = src >> 6;
+  const uint32_t sh = uint32_t(src & 63);
+  uint64_t v = level[w] << sh;
+  if (sh != 0 && sh + take > 64) v |= level[w + 1] >> (64 - sh);
+  return take == 64 ? v : (v & ~(~0ull >> take));
+}
+
+__global__ void regroup_kernel(const uint64_t* __restrict__ matrix_level, uint64_t* __restrict__ tree_level,
+                               uint64_t nbits, const uint64_t* __restrict__ seg_tree,
+                               const uint64_t* __restrict__ seg_matrix, uint64_t nseg, uint32_t* status) {
+  const uint64_t nwords = (nbits + 63) >> 6;
+  for (uint64_t w = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; w < nwords;
+       w += uint64_t(gridDim.x) * blockDim.x) {
+    const uint64_t p0 = w << 6, end = min(p0 + 64, nbits);
+    uint64_t pos = p0, acc = 0;
+    while (pos < end) {
+      // last segment starting at or before pos
+      uint64_t lo = 0, hi = nseg;
+      while (hi - lo > 1) {
+        uint64_t mid = (lo + hi) >> 1;
+        if (seg_tree[mid] <= pos) lo = mid; else hi = mid;
+      }
+      const uint64_t seg_end = lo + 1 < nseg ? seg_tree[lo + 1] : nbits;
+      const uint64_t stop = min(end, seg_end);
+      const uint32_t take = uint32_t(stop - pos);
+      const uint64_t src = seg_matrix[lo] + (pos - seg_tree[lo]);
+      if (src + take > nbits || take == 0) {  // inconsistent segments: never read out of range
+        atomicOr(status, kErrBounds);
+        break;
+      }
+      acc |= bits_at(matrix_level, src, take) >> (pos - p0);
+      pos = stop;
+    }
+    tree_level[w] = acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Huffman code keys
+// ---------------------------------------------------------------------------
+template <typename T, typename K>
+__global__ void huffman_keys_kernel(const T* text, uint64_t n, const uint64_t* code_len, const uint64_t* code_word,
+                                    uint64_t ncodes, K* keys, uint32_t* status) {
+  constexpr uint32_t kBits = sizeof(K) * 8 - 8;
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    uint64_t c = uint64_t(text[i]);
+    uint64_t len = c < ncodes ? code_len[c] : 0;
+    if (len == 0 || len > kBits) {
+      atomicOr(status, kErrSymbol);
+      keys[i] = K(0);
+      continue;
+    }
+    keys[i] = K(((uint64_t(code_word[c]) << (kBits - len)) << 8) | len);
+  }
+}
+
+template <typename T>
+__global__ void symbol_hist_kernel(const T* text, uint64_t n, uint64_t nsym, unsigned long long* hist,
+                                   unsigned long long* first) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    uint64_t c = uint64_t(text[i]);
+    if (c < nsym) {
+      atomicAdd(&hist[c], 1ull);
+      if (first) atomicMin(&first[c], (unsigned long long)i);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Generators (gen.cuh)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void generate_kernel(int dist, uint64_t key, uint64_t param, uint64_t n, T* out, const uint64_t* thr,
+                                uint32_t nthr, const uint32_t* perm) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+    out[i] = T(gen_value(dist, key, param, i, thr, nthr, perm));
+}
+
+int grid_for(uint64_t n, int threads) {
+  uint64_t b = (n + threads - 1) / threads;
+  if (b > 4096) b = 4096;
+  return int(b < 1 ? 1 : b);
+}
+
+}  // namespace
+
+void launch_leaf_histogram(const void* text, uint64_t n, uint32_t width, uint32_t levels, unsigned long long* hist,
+                           uint32_t* status, cudaStream_t s, uint64_t* launches) {
+  if (n == 0) return;
+  switch (width) {
+    case 1: hist_dispatch(static_cast<const uint8_t*>(text), n, levels, hist, status, s); break;
+    case 2: hist_dispatch(static_cast<const uint16_t*>(text), n, levels, hist, status, s); break;
+    default: hist_dispatch(static_cast<const uint32_t*>(text), n, levels, hist, status, s); break;
+  }
+  ++*launches;
+}
+
+void launch_regroup(const uint64_t* matrix_level, uint64_t* tree_level, uint64_t nbits, const uint64_t* seg_tree,
+                    const uint64_t* seg_matrix, uint64_t nseg, uint32_t* status, cudaStream_t s, uint64_t* launches) {
+  const uint64_t nwords = (nbits + 63) >> 6;
+  if (nwords == 0) return;
+  regroup_kernel<<<grid_for(nwords, 256), 256, 0, s>>>(matrix_level, tree_level, nbits, seg_tree, seg_matrix, nseg,
+                                                       status);
+  ++*launches;
+}
+
+void launch_huffman_keys(const void* text, uint64_t n, uint32_t width, const uint64_t* code_len,
+                         const uint64_t* code_word, uint64_t ncodes, uint32_t key_bytes, void* keys,
+                         uint32_t* status, cudaStream_t s, uint64_t* launches) {
+  if (n == 0) return;
+  const int g = grid_for(n, 256);
+#define PWMGPU_HK(T)                                                                                            \
+  if (key_bytes == 4)                                                                                           \
+    huffman_keys_kernel<T, uint32_t><<<g, 256, 0, s>>>(static_cast<const T*>(text), n, code_len, code_word,    \
+                                                       ncodes, static_cast<uint32_t*>(keys), status);          \
+  else                                                                                                          \
+    huffman_keys_kernel<T, uint64_t><<<g, 256, 0, s>>>(static_cast<const T*>(text), n, code_len, code_word,    \
+                                                       ncodes, static_cast<uint64_t*>(keys), status);
+  if (width == 1) { PWMGPU_HK(uint8_t) } else if (width == 2) { PWMGPU_HK(uint16_t) } else { PWMGPU_HK(uint32_t) }
+#undef PWMGPU_HK
+  ++*launches;
+}
+
+void launch_symbol_histogram(const void* text, uint64_t n, uint32_t width, uint64_t nsym, unsigned long long* hist,
+                             unsigned long long* first, cudaStream_t s, uint64_t* launches) {
+  if (n == 0) return;
+  const int g = grid_for(n, 256);
+  if (width == 1) symbol_hist_kernel<<<g, 256, 0, s>>>(static_cast<const uint8_t*>(text), n, nsym, hist, first);
+  else if (width == 2) symbol_hist_kernel<<<g, 256, 0, s>>>(static_cast<const uint16_t*>(text), n, nsym, hist, first);
+  else symbol_hist_kernel<<<g, 256, 0, s>>>(static_cast<const uint32_t*>(text), n, nsym, hist, first);
+  ++*launches;
+}
+
+void launch_generate(int dist, uint64_t seed, uint64_t param, uint64_t n, uint32_t width, void* out,
+                     const uint64_t* thresholds, uint32_t nthr, const uint32_t* perm, cudaStream_t s,
+                     uint64_t* launches) {
+  if (n == 0) return;
+  const uint64_t key = mix64(seed);
+  const int g = grid_for(n, 256);
+  if (width == 1) generate_kernel<<<g, 256, 0, s>>>(dist, key, param, n, static_cast<uint8_t*>(out), thresholds, nthr, perm);
+  else if (width == 2) generate_kernel<<<g, 256, 0, s>>>(dist, key, param, n, static_cast<uint16_t*>(out), thresholds, nthr, perm);
+  else generate_kernel<<<g, 256, 0, s>>>(dist, key, param, n, static_cast<uint32_t*>(out), thresholds, nthr, perm);
+  ++*launches;
+}
+
+}  // namespace pwmgpu

@@ -1,0 +1,184 @@
+// Host-side O(2^L) and O(sigma * L) tables of a build: zero counts, the run
+// starts of every split pass and the prefix-group segments that turn matrix
+// levels into tree levels.  Pure integer code shared by the plain and the
+// Huffman paths.
+#pragma once
+
+#include <algorithm>
+#include <cstdint>
+#include <numeric>
+#include <unordered_map>
+#include <vector>
+
+namespace pwmgpu {
+
+struct PassPlan {
+  uint32_t level;  // first level of the pass
+  int K;           // levels of the pass
+  bool has_out;    // writes S_{level+K}
+};
+
+// Passes of up to kmax levels covering levels 0..L-1.
+inline std::vector<PassPlan> plan_passes(uint32_t L, int kmax) {
+  std::vector<PassPlan> p;
+  for (uint32_t l = 0; l < L;) {
+    int K = int(std::min<uint32_t>(uint32_t(kmax), L - l));
+    p.push_back({l, K, l + K < L});
+    l += uint32_t(K);
+  }
+  return p;
+}
+
+inline uint32_t rev_bits_host(uint64_t v, uint32_t bits) {
+  uint64_t r = 0;
+  for (uint32_t i = 0; i < bits; ++i) { r = (r << 1) | (v & 1); v >>= 1; }
+  return uint32_t(r);
+}
+
+// One weighted "code" of the text: the bits the levels test, its length
+// (levels it is present on) and how often it occurs.  Plain symbols are codes
+// of length L (the symbol's L low bits, MSB first).
+struct WeightedCode {
+  uint64_t word;   // code bits, MSB = level 0, right-aligned in `len` bits
+  uint32_t len;
+  uint64_t freq;
+};
+
+struct LevelTables {
+  std::vector<uint64_t> zeros;                 // per level
+  std::vector<uint64_t> level_bits;            // elements per level
+  std::vector<std::vector<uint64_t>> starts;   // per pass: sum_j 2^j entries, j-major
+  std::vector<std::vector<uint64_t>> seg_tree, seg_matrix;  // per level (level 0 unused)
+};
+
+inline uint32_t code_bit(const WeightedCode& c, uint32_t level) { return uint32_t(c.word >> (c.len - 1 - level)) & 1u; }
+
+// Tables of a plain text from its leaf histogram (2^L counts): dense
+// per-level prefix counts folded from the leaves.
+inline LevelTables build_tables_plain(const std::vector<uint64_t>& hist, uint32_t L, const std::vector<PassPlan>& plan,
+                                      bool want_tree) {
+  LevelTables t;
+  std::vector<std::vector<uint64_t>> cnt(L + 1);
+  cnt[L] = hist;
+  for (int m = int(L) - 1; m >= 0; --m) {
+    cnt[m].assign(size_t(1) << m, 0);
+    for (size_t p = 0; p < cnt[m].size(); ++p) cnt[m][p] = cnt[m + 1][2 * p] + cnt[m + 1][2 * p + 1];
+  }
+  const uint64_t n = cnt[0][0];
+  t.level_bits.assign(L, n);
+  t.zeros.assign(L, 0);
+  for (uint32_t m = 0; m < L; ++m)
+    for (size_t p = 0; p < cnt[m + 1].size(); p += 2) t.zeros[m] += cnt[m + 1][p];
+  t.starts.resize(plan.size());
+  for (size_t pi = 0; pi < plan.size(); ++pi) {
+    const auto& p = plan[pi];
+    std::vector<uint64_t> st(size_t((2 << p.K) - 2), 0);
+    for (int j = 1; j <= p.K; ++j) {
+      const auto& c = cnt[p.level + j];
+      std::vector<uint64_t> k(size_t(1) << j, 0);
+      const uint64_t mask = (uint64_t(1) << j) - 1;
+      for (size_t q = 0; q < c.size(); ++q) k[rev_bits_host(q & mask, uint32_t(j))] += c[q];
+      uint64_t run = 0;
+      for (size_t v = 0; v < k.size(); ++v) { st[size_t((1 << j) - 2) + v] = run; run += k[v]; }
+    }
+    t.starts[pi] = std::move(st);
+  }
+  if (want_tree) {
+    t.seg_tree.resize(L);
+    t.seg_matrix.resize(L);
+    for (uint32_t m = 1; m < L; ++m) {
+      const auto& c = cnt[m];
+      std::vector<uint64_t> mstart(c.size(), 0);
+      uint64_t run = 0;
+      for (size_t r = 0; r < c.size(); ++r) {
+        size_t p = rev_bits_host(r, m);
+        mstart[p] = run;
+        run += c[p];
+      }
+      std::vector<uint64_t> st, sm;
+      run = 0;
+      for (size_t p = 0; p < c.size(); ++p) {
+        if (c[p]) { st.push_back(run); sm.push_back(mstart[p]); }
+        run += c[p];
+      }
+      if (st.empty()) { st.push_back(0); sm.push_back(0); }
+      t.seg_tree[m] = std::move(st);
+      t.seg_matrix[m] = std::move(sm);
+    }
+  }
+  return t;
+}
+
+// Tables of a Huffman-shaped text from its weighted codes.  want_tree: also
+// the segments.
+inline LevelTables build_tables(const std::vector<WeightedCode>& codes, uint32_t L, const std::vector<PassPlan>& plan,
+                                bool want_tree) {
+  LevelTables t;
+  t.zeros.assign(L, 0);
+  t.level_bits.assign(L, 0);
+  for (const auto& c : codes) {
+    for (uint32_t m = 0; m < c.len && m < L; ++m) {
+      t.level_bits[m] += c.freq;
+      if (!code_bit(c, m)) t.zeros[m] += c.freq;
+    }
+  }
+  t.starts.resize(plan.size());
+  for (size_t pi = 0; pi < plan.size(); ++pi) {
+    const auto& p = plan[pi];
+    const int C = (2 << p.K) - 2;
+    std::vector<uint64_t> cnt(size_t(C), 0);
+    for (const auto& c : codes) {
+      uint32_t key = 0;
+      for (int j = 1; j <= p.K; ++j) {
+        if (p.level + j - 1 >= c.len) break;
+        key |= code_bit(c, p.level + j - 1) << (j - 1);
+        if (p.level + j < c.len) cnt[size_t((1 << j) - 2 + int(key))] += c.freq;  // alive at l+j
+      }
+    }
+    std::vector<uint64_t> st(size_t(C), 0);
+    for (int j = 1; j <= p.K; ++j) {
+      uint64_t run = 0;
+      for (int v = 0; v < (1 << j); ++v) {
+        st[size_t((1 << j) - 2 + v)] = run;
+        run += cnt[size_t((1 << j) - 2 + v)];
+      }
+    }
+    t.starts[pi] = std::move(st);
+  }
+  if (want_tree) {
+    t.seg_tree.resize(L);
+    t.seg_matrix.resize(L);
+    for (uint32_t m = 1; m < L; ++m) {
+      // prefix groups of level m among codes longer than m
+      std::vector<std::pair<uint64_t, uint64_t>> groups;  // (prefix, count)
+      groups.reserve(codes.size());
+      for (const auto& c : codes)
+        if (c.len > m) groups.emplace_back(c.word >> (c.len - m), c.freq);
+      std::sort(groups.begin(), groups.end());
+      std::vector<std::pair<uint64_t, uint64_t>> g;  // aggregated, natural prefix order
+      for (const auto& x : groups) {
+        if (!g.empty() && g.back().first == x.first) g.back().second += x.second;
+        else g.push_back(x);
+      }
+      std::vector<uint64_t> tree_start(g.size()), matrix_start(g.size());
+      uint64_t run = 0;
+      for (size_t i = 0; i < g.size(); ++i) { tree_start[i] = run; run += g[i].second; }
+      std::vector<size_t> order(g.size());
+      std::iota(order.begin(), order.end(), size_t(0));
+      std::sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+        return rev_bits_host(g[a].first, m) < rev_bits_host(g[b].first, m);
+      });
+      run = 0;
+      for (size_t i : order) { matrix_start[i] = run; run += g[i].second; }
+      std::vector<uint64_t> st, sm;
+      for (size_t i = 0; i < g.size(); ++i)
+        if (g[i].second) { st.push_back(tree_start[i]); sm.push_back(matrix_start[i]); }
+      if (st.empty()) { st.push_back(0); sm.push_back(0); }
+      t.seg_tree[m] = std::move(st);
+      t.seg_matrix[m] = std::move(sm);
+    }
+  }
+  return t;
+}
+
+}  // namespace pwmgpu

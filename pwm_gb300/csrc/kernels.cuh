@@ -1,0 +1,82 @@
+// Declarations of the kernel launchers shared by the host orchestration.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "split.cuh"
+
+namespace pwmgpu {
+
+// ---- histogram of the text ------------------------------------------------
+// Leaf histogram (2^levels bins, u64) of a device text; records kErrSymbol in
+// *status when a symbol is >= 2^levels.  hist must be zeroed.
+void launch_leaf_histogram(const void* text, uint64_t n, uint32_t width, uint32_t levels,
+                           unsigned long long* hist, uint32_t* status, cudaStream_t s, uint64_t* launches);
+
+// ---- split passes -----------------------------------------------------------
+// Geometry of the split pass for a key width: tile size in elements.
+uint32_t split_tile_elems(uint32_t key_bytes);
+// Dynamic shared memory of one CTA.
+size_t split_smem_bytes(uint32_t key_bytes, int K);
+void launch_split_pass(uint32_t key_bytes, bool huffman, int K, const SplitArgs& a, uint32_t L, cudaStream_t s,
+                       uint64_t* launches);
+
+// ---- wavelet tree from the matrix --------------------------------------------
+// Level `m` of the tree: the matrix level with its prefix groups reordered.
+// seg_tree/seg_matrix: nseg (>=1) group starts sorted by seg_tree, seg_tree[0] == 0.
+void launch_regroup(const uint64_t* matrix_level, uint64_t* tree_level, uint64_t nbits, const uint64_t* seg_tree,
+                    const uint64_t* seg_matrix, uint64_t nseg, uint32_t* status, cudaStream_t s, uint64_t* launches);
+
+// ---- Huffman keys -------------------------------------------------------------
+// key = (code << (keybits - 8 - len)) << 8 | len for every text symbol.
+void launch_huffman_keys(const void* text, uint64_t n, uint32_t width, const uint64_t* code_len,
+                         const uint64_t* code_word, uint64_t ncodes, uint32_t key_bytes, void* keys,
+                         uint32_t* status, cudaStream_t s, uint64_t* launches);
+// Histogram of symbols below `nsym` (u64 counts) and the first position of
+// every symbol (atomicMin; first must be filled with UINT64_MAX).
+void launch_symbol_histogram(const void* text, uint64_t n, uint32_t width, uint64_t nsym,
+                             unsigned long long* hist, unsigned long long* first, cudaStream_t s,
+                             uint64_t* launches);
+
+// ---- rank / select --------------------------------------------------------------
+struct RankSelectLevel {
+  const uint64_t* data;   // level words
+  uint64_t nwords;
+  uint64_t* l0;           // n0 = nwords / 67108863 + 1 entries
+  uint32_t* l12;          // 2 * (nwords / 32 + 1) u32
+  uint32_t* s0;           // capacity nwords * 64 / 8192 + 2
+  uint32_t* s1;
+  unsigned long long* meta;  // [0] ns0, [1] ns1, [2] total ones
+};
+// Builds pwm's rank/select blocks for `count` levels.  tmp must hold
+// max(ceil(nwords/32)) + 1 u32 per level plus per-CTA totals (see .cu).
+void launch_rank_select(const RankSelectLevel* host_levels, uint32_t count, RankSelectLevel* dev_levels,
+                        uint32_t* tmp, uint64_t tmp_words_per_level, cudaStream_t s, uint64_t* launches);
+
+struct QueryLevel {
+  const uint64_t* data;
+  uint64_t nwords;
+  const uint64_t* l0;
+  uint64_t n0;
+  const uint32_t* l12;
+  const uint32_t* s0;
+  const uint32_t* s1;
+  const unsigned long long* meta;
+};
+struct QueryStructure {
+  uint32_t levels;
+  uint32_t is_tree;
+  uint64_t n;
+  const QueryLevel* lv;        // device array of `levels`
+  const uint64_t* zeros;       // device array of `levels` (matrix)
+};
+void launch_queries(const QueryStructure& q, int op, const uint64_t* a, const uint64_t* b, uint64_t count,
+                    uint64_t* out, cudaStream_t s, uint64_t* launches);
+
+// ---- generators -------------------------------------------------------------------
+void launch_generate(int dist, uint64_t seed, uint64_t param, uint64_t n, uint32_t width, void* out,
+                     const uint64_t* thresholds, uint32_t nthr, const uint32_t* perm, cudaStream_t s,
+                     uint64_t* launches);
+
+}  // namespace pwmgpu

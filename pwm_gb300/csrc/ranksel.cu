@@ -1,0 +1,390 @@
+// Popcount rank/select support in pwm's layout and batched queries.
+//
+// Layout (include/queries/bin_rank_popcnt.hpp:32-86, popcnt_traits.hpp:
+// 12-21): per level, one l12 entry per L1 block of 32 words (2048 bits): the
+// u32 count of ones before the block (wrapping like pwm's u32) and the ones
+// of its first three 512-bit L2 blocks in 10-bit fields.  When the level has
+// a multiple of 32 words pwm keeps one more, zeroed, entry; so does this
+// layout.  l0 is all zero for levels below 2^32-1 bits (the only sizes
+// accepted).  Select samples (bin_select_popcnt.hpp:38-107): the position of
+// every 8192nd zero/one, taken in the L1 block where the running count first
+// exceeds the next sample number.
+#include "kernels.cuh"
+
+namespace pwmgpu {
+
+namespace {
+
+constexpr uint64_t kL1Bits = 2048, kL2Bits = 512, kL1Cover = 32, kL2Cover = 8, kSampleRate = 8192;
+constexpr int kRsThreads = 256;
+
+__device__ __forceinline__ uint32_t l2_of(const uint32_t* l12, uint64_t e, uint32_t i) {
+  return (l12[2 * e + 1] >> (10 * i)) & 1023u;
+}
+
+// Phase 1: per L1 block popcounts (warp per block), l2 fields, and the
+// exclusive prefix of block totals inside each CTA (256 blocks per CTA).
+__global__ void __launch_bounds__(kRsThreads) rs_blocks_kernel(const RankSelectLevel* lv, uint32_t* tmp,
+                                                              uint64_t tmp_stride) {
+  const RankSelectLevel L = lv[blockIdx.y];
+  const uint64_t nreal = (L.nwords + kL1Cover - 1) / kL1Cover;
+  const uint64_t first = uint64_t(blockIdx.x) * kRsThreads;
+  if (first >= nreal) return;
+  uint32_t* intra = tmp + blockIdx.y * tmp_stride;
+  uint32_t* cta_tot = intra + nreal;
+  __shared__ uint32_t tot[kRsThreads];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int e = warp; e < kRsThreads; e += kRsThreads / 32) {
+    const uint64_t blk = first + e;
+    uint32_t c = 0;
+    if (blk < nreal) {
+      uint64_t w = blk * kL1Cover + lane;
+      c = w < L.nwords ? __popcll(L.data[w]) : 0u;
+    }
+    c += __shfl_xor_sync(0xFFFFFFFFu, c, 1);
+    c += __shfl_xor_sync(0xFFFFFFFFu, c, 2);
+    c += __shfl_xor_sync(0xFFFFFFFFu, c, 4);   // per 8-lane group: one L2 block
+    uint32_t g1 = __shfl_sync(0xFFFFFFFFu, c, 8), g2 = __shfl_sync(0xFFFFFFFFu, c, 16),
+             g3 = __shfl_sync(0xFFFFFFFFu, c, 24);
+    if (lane == 0) {
+      tot[e] = c + g1 + g2 + g3;
+      if (blk < nreal) L.l12[2 * blk + 1] = (c & 1023u) | ((g1 & 1023u) << 10) | ((g2 & 1023u) << 20);
+    }
+  }
+  __syncthreads();
+  // exclusive scan of the 256 block totals (u32, wrapping)
+  uint32_t v = tot[threadIdx.x];
+  uint32_t x = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+    if (lane >= d) x += y;
+  }
+  __shared__ uint32_t wsum[kRsThreads / 32];
+  if (lane == 31) wsum[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t s = lane < kRsThreads / 32 ? wsum[lane] : 0;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      uint32_t y = __shfl_up_sync(0xFFFFFFFFu, s, d);
+      if (lane >= d) s += y;
+    }
+    if (lane < kRsThreads / 32) wsum[lane] = s;  // inclusive
+  }
+  __syncthreads();
+  const uint32_t warp_excl = warp ? wsum[warp - 1] : 0u;
+  const uint64_t blk = first + threadIdx.x;
+  if (blk < nreal) intra[blk] = warp_excl + x - v;
+  if (threadIdx.x == kRsThreads - 1) cta_tot[blockIdx.x] = warp_excl + x;
+}
+
+// Phase 2: one CTA per level scans the CTA totals (exclusive, u32 wrap) and
+// the exact u64 total of ones.
+__global__ void __launch_bounds__(1024) rs_scan_kernel(const RankSelectLevel* lv, uint32_t* tmp,
+                                                       uint64_t tmp_stride) {
+  const RankSelectLevel L = lv[blockIdx.x];
+  const uint64_t nreal = (L.nwords + kL1Cover - 1) / kL1Cover;
+  const uint64_t ncta = (nreal + kRsThreads - 1) / kRsThreads;
+  uint32_t* cta_tot = tmp + blockIdx.x * tmp_stride + nreal;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ unsigned long long wsum[32];
+  __shared__ unsigned long long carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (uint64_t base = 0; base < ncta; base += 1024) {
+    const uint64_t i = base + threadIdx.x;
+    const unsigned long long v = i < ncta ? cta_tot[i] : 0ull;
+    unsigned long long x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+      if (lane >= d) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      unsigned long long s = wsum[lane];
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, s, d);
+        if (lane >= d) s += y;
+      }
+      wsum[lane] = s;
+    }
+    __syncthreads();
+    const unsigned long long excl = carry + (warp ? wsum[warp - 1] : 0ull) + x - v;
+    if (i < ncta) cta_tot[i] = uint32_t(excl);  // now the CTA's exclusive offset
+    __syncthreads();
+    if (threadIdx.x == 1023) carry = excl + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) L.meta[2] = carry;  // total ones of the level
+}
+
+__device__ __forceinline__ uint32_t l1_value(const uint32_t* intra, const uint32_t* cta_off, uint64_t nreal,
+                                             uint64_t e) {
+  // pwm's l1 value of entry e; the extra entry past the real blocks is 0.
+  return e < nreal ? cta_off[e / kRsThreads] + intra[e] : 0u;
+}
+
+// Phase 3: l1 values and the select samples (one thread per L1 block).
+__global__ void __launch_bounds__(kRsThreads) rs_finish_kernel(const RankSelectLevel* lv, const uint32_t* tmp,
+                                                              uint64_t tmp_stride) {
+  const RankSelectLevel L = lv[blockIdx.y];
+  const uint64_t nreal = (L.nwords + kL1Cover - 1) / kL1Cover;
+  const uint64_t n12 = L.nwords / kL1Cover + 1;
+  const uint32_t* intra = tmp + blockIdx.y * tmp_stride;
+  const uint32_t* cta_off = intra + nreal;
+  const uint64_t b = uint64_t(blockIdx.x) * kRsThreads + threadIdx.x;
+  if (b < nreal) L.l12[2 * b] = l1_value(intra, cta_off, nreal, b);
+  if (b == 0 && n12 > nreal) { L.l12[2 * nreal] = 0; L.l12[2 * nreal + 1] = 0; }
+  if (b + 1 >= n12) return;  // pwm examines blocks 0 .. n12-2
+  const uint64_t ones_before = l1_value(intra, cta_off, nreal, b);
+  const uint64_t ones_through = l1_value(intra, cta_off, nreal, b + 1);
+  // select1
+  {
+    const uint64_t f_prev = ones_before;
+    const uint64_t s = f_prev == 0 ? 0 : (f_prev - 1 + kSampleRate - 1) / kSampleRate;
+    const uint64_t next = 1 + kSampleRate * s;
+    if (ones_through > next) {
+      uint32_t rem = uint32_t(next - ones_before);
+      uint32_t l2 = 0;
+      while (l2 < 3 && l2_of(L.l12, b, l2) < rem) rem -= l2_of(L.l12, b, l2++);
+      uint64_t wp = b * kL1Cover + l2 * kL2Cover;
+      while (wp < L.nwords && rem > uint32_t(__popcll(L.data[wp]))) rem -= __popcll(L.data[wp++]);
+      if (wp < L.nwords) {
+        L.s1[s] = uint32_t(word_select1(L.data[wp], rem) + 64 * wp);
+        atomicMax(&L.meta[1], (unsigned long long)(s + 1));
+      }
+    }
+  }
+  // select0
+  {
+    const uint64_t f_prev = b * kL1Bits - ones_before;
+    const uint64_t f_here = (b + 1) * kL1Bits - ones_through;
+    const uint64_t s = f_prev == 0 ? 0 : (f_prev - 1 + kSampleRate - 1) / kSampleRate;
+    const uint64_t next = 1 + kSampleRate * s;
+    if (f_here > next) {
+      uint32_t rem = uint32_t(next - f_prev);
+      uint32_t l2 = 0;
+      while (l2 < 3 && (kL2Bits - l2_of(L.l12, b, l2)) < rem) rem -= uint32_t(kL2Bits - l2_of(L.l12, b, l2++));
+      uint64_t wp = b * kL1Cover + l2 * kL2Cover;
+      while (wp < L.nwords && rem > uint32_t(__popcll(~L.data[wp]))) rem -= __popcll(~L.data[wp++]);
+      if (wp < L.nwords) {
+        L.s0[s] = uint32_t(word_select1(~L.data[wp], rem) + 64 * wp);
+        atomicMax(&L.meta[0], (unsigned long long)(s + 1));
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Queries (include/queries/query_support.hpp:39-178)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t q_rank1(const QueryLevel& L, uint64_t index) {
+  // bin_rank_popcnt::rank1 (bin_rank_popcnt.hpp:98-128); the index of pwm's
+  // extra zeroed L1 entry answers with the level's total instead of 0.
+  const uint64_t nreal = (L.nwords + kL1Cover - 1) / kL1Cover;
+  if (index > L.nwords * 64) index = L.nwords * 64;  // past the level: the padding holds no ones
+  const uint64_t l1 = index / kL1Bits;
+  if (l1 >= nreal) return L.meta[2];
+  uint64_t rem = index - l1 * kL1Bits;
+  uint64_t result = L.l12[2 * l1];
+  const uint64_t l2 = rem / kL2Bits;
+  rem -= l2 * kL2Bits;
+  for (uint32_t i = 0; i < l2; ++i) result += l2_of(L.l12, l1, i);
+  uint64_t off = l1 * kL1Cover + l2 * kL2Cover;
+  while (rem >= 64) { result += __popcll(L.data[off++]); rem -= 64; }
+  if (rem > 0) result += __popcll(L.data[off] >> (64 - rem));
+  return result;
+}
+__device__ __forceinline__ uint64_t q_rank0(const QueryLevel& L, uint64_t index) { return index - q_rank1(L, index); }
+
+// bin_select_popcnt::select (bin_select_popcnt.hpp:112-117, 166-241), with
+// the scan start at sample (occ-1)/8192 and the block scan and word walk
+// bounded by the real data (pwm reads past its arrays there).
+__device__ uint64_t q_select(const QueryLevel& L, int value, uint64_t occ) {
+  if (occ == 0) return 0;
+  const uint64_t nreal = (L.nwords + kL1Cover - 1) / kL1Cover;
+  const uint64_t ns = L.meta[value ? 1 : 0];
+  const uint32_t* samples = value ? L.s1 : L.s0;
+  const uint64_t sidx = (occ - 1) / kSampleRate;
+  uint64_t l1;
+  if (sidx < ns) {
+    l1 = samples[sidx];
+    if ((occ - 1) % kSampleRate == 0) return l1;
+    l1 /= kL1Bits;
+  } else {
+    l1 = ns ? samples[ns - 1] / kL1Bits : 0;
+  }
+  if (value == 0) {
+    while (l1 + 1 < nreal && (((l1 + 1) * kL1Bits) - L.l12[2 * (l1 + 1)]) < occ) ++l1;
+    occ -= (l1 * kL1Bits) - L.l12[2 * l1];
+  } else {
+    while (l1 + 1 < nreal && L.l12[2 * (l1 + 1)] < occ) ++l1;
+    occ -= L.l12[2 * l1];
+  }
+  uint32_t l2 = 0;
+  if (value == 0) {
+    while (l2 < 3 && occ > kL2Bits - l2_of(L.l12, l1, l2)) occ -= kL2Bits - l2_of(L.l12, l1, l2++);
+  } else {
+    while (l2 < 3 && occ > l2_of(L.l12, l1, l2)) occ -= l2_of(L.l12, l1, l2++);
+  }
+  const uint64_t last = kL2Cover * l2 + kL1Cover * l1;
+  uint64_t extra = 0;
+  for (;;) {
+    if (last + extra >= L.nwords) return ~0ull;
+    uint64_t w = L.data[last + extra];
+    if (value == 0) w = ~w;
+    const uint64_t pc = __popcll(w);
+    if (pc >= occ) return kL2Bits * l2 + kL1Bits * l1 + extra * 64 + word_select1(w, uint32_t(occ));
+    ++extra;
+    occ -= pc;
+  }
+}
+
+__device__ __forceinline__ bool bit_at(const uint64_t* d, uint64_t i) { return (d[i >> 6] >> (63 - (i & 63))) & 1; }
+
+__global__ void query_kernel(QueryStructure q, int op, const uint64_t* __restrict__ a, const uint64_t* __restrict__ b,
+                             uint64_t count, uint64_t* __restrict__ out) {
+  const uint32_t Lv = q.levels;
+  for (uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < count; t += uint64_t(gridDim.x) * blockDim.x) {
+    uint64_t result = 0;
+    if (op == 0 && a[t] >= q.n) {  // access past the text
+      result = ~0ull;
+    } else if (op == 0) {  // access
+      uint64_t index = a[t], word = 0;
+      if (q.is_tree) {
+        uint64_t start = 0, end = q.n;
+        for (uint32_t level = 0; level < Lv; ++level) {
+          const QueryLevel& L = q.lv[level];
+          const uint64_t left = q_rank0(L, start), right = q_rank0(L, end);
+          word <<= 1;
+          if (bit_at(L.data, start + index)) {
+            word |= 1;
+            index = q_rank1(L, start + index) - (start - left);
+            start = start + right - left;
+          } else {
+            index = q_rank0(L, start + index) - left;
+            end = start + right - left;
+          }
+        }
+      } else {
+        for (uint32_t level = 0; level < Lv; ++level) {
+          const QueryLevel& L = q.lv[level];
+          word <<= 1;
+          if (bit_at(L.data, index)) {
+            word |= 1;
+            index = q_rank1(L, index) + q.zeros[level];
+          } else {
+            index = q_rank0(L, index);
+          }
+        }
+      }
+      result = word;
+    } else if (op == 1) {  // rank(symbol, index)
+      const uint64_t sym = a[t];
+      uint64_t index = b[t];
+      if (index != 0) {
+        if (q.is_tree) {
+          uint64_t start = 0, end = q.n;
+          for (uint32_t level = 0; level < Lv; ++level) {
+            const QueryLevel& L = q.lv[level];
+            const uint64_t left = q_rank0(L, start), right = q_rank0(L, end);
+            if ((sym >> (Lv - level - 1)) & 1) {
+              index = q_rank1(L, start + index) - (start - left);
+              start = start + right - left;
+            } else {
+              index = q_rank0(L, start + index) - left;
+              end = start + right - left;
+            }
+          }
+          result = index;
+        } else {
+          uint64_t offset = 0;
+          for (uint32_t level = 0; level < Lv; ++level) {
+            const QueryLevel& L = q.lv[level];
+            if ((sym >> (Lv - level - 1)) & 1) {
+              index = q.zeros[level] + q_rank1(L, index);
+              offset = q.zeros[level] + q_rank1(L, offset);
+            } else {
+              index = q_rank0(L, index);
+              offset = q_rank0(L, offset);
+            }
+          }
+          result = index - offset;
+        }
+      }
+    } else {  // select(symbol, occ)
+      const uint64_t sym = a[t];
+      uint64_t occ = b[t];
+      if (occ != 0) {
+        uint64_t st[64], le[64];
+        if (q.is_tree) {
+          uint64_t start = 0, end = q.n;
+          for (uint32_t level = 0; level < Lv; ++level) {
+            const QueryLevel& L = q.lv[level];
+            const uint64_t left = q_rank0(L, start), right = q_rank0(L, end);
+            st[level] = start;
+            le[level] = left;
+            if ((sym >> (Lv - level - 1)) & 1) start = start + right - left;
+            else end = start + right - left;
+          }
+          for (int level = int(Lv) - 1; level >= 0; --level) {
+            const QueryLevel& L = q.lv[level];
+            const uint64_t adj = level == 0 ? 0 : 1;
+            if ((sym >> (Lv - level - 1)) & 1) occ = q_select(L, 1, st[level] - le[level] + occ) - st[level] + adj;
+            else occ = q_select(L, 0, le[level] + occ) - st[level] + adj;
+          }
+        } else {
+          uint64_t offset = 0;
+          for (uint32_t level = 0; level < Lv; ++level) {
+            const QueryLevel& L = q.lv[level];
+            if ((sym >> (Lv - level - 1)) & 1) offset = q.zeros[level] + q_rank1(L, offset);
+            else offset = q_rank0(L, offset);
+          }
+          occ += offset;
+          for (int level = int(Lv) - 1; level >= 0; --level) {
+            const QueryLevel& L = q.lv[level];
+            const uint64_t adj = level == 0 ? 0 : 1;
+            if ((sym >> (Lv - level - 1)) & 1) occ = q_select(L, 1, occ - q.zeros[level]) + adj;
+            else occ = q_select(L, 0, occ) + adj;
+          }
+        }
+        result = occ;
+      }
+    }
+    out[t] = result;
+  }
+}
+
+}  // namespace
+
+void launch_rank_select(const RankSelectLevel* host_levels, uint32_t count, RankSelectLevel* dev_levels,
+                        uint32_t* tmp, uint64_t tmp_words_per_level, cudaStream_t s, uint64_t* launches) {
+  if (count == 0) return;
+  uint64_t max_real = 0;
+  for (uint32_t i = 0; i < count; ++i) {
+    uint64_t nreal = (host_levels[i].nwords + kL1Cover - 1) / kL1Cover;
+    if (nreal > max_real) max_real = nreal;
+  }
+  if (max_real == 0) return;
+  const uint64_t ctas = (max_real + kRsThreads - 1) / kRsThreads;
+  dim3 g1(unsigned(ctas), count);
+  rs_blocks_kernel<<<g1, kRsThreads, 0, s>>>(dev_levels, tmp, tmp_words_per_level);
+  rs_scan_kernel<<<count, 1024, 0, s>>>(dev_levels, tmp, tmp_words_per_level);
+  rs_finish_kernel<<<g1, kRsThreads, 0, s>>>(dev_levels, tmp, tmp_words_per_level);
+  *launches += 3;
+}
+
+void launch_queries(const QueryStructure& q, int op, const uint64_t* a, const uint64_t* b, uint64_t count,
+                    uint64_t* out, cudaStream_t s, uint64_t* launches) {
+  if (count == 0) return;
+  uint64_t blocks = (count + 127) / 128;
+  if (blocks > 65535) blocks = 65535;
+  query_kernel<<<unsigned(blocks), 128, 0, s>>>(q, op, a, b, count, out);
+  ++*launches;
+}
+
+}  // namespace pwmgpu

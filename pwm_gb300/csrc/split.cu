@@ -1,0 +1,75 @@
+// Instantiations and launcher of the fused split pass (split.cuh).
+#include "kernels.cuh"
+
+namespace pwmgpu {
+
+namespace {
+
+constexpr int kSplitThreads = 512;
+
+template <int KB>
+struct SplitGeometry;
+template <> struct SplitGeometry<1> { static constexpr int ITEMS = 32; using Key = uint8_t; };
+template <> struct SplitGeometry<2> { static constexpr int ITEMS = 32; using Key = uint16_t; };
+template <> struct SplitGeometry<4> { static constexpr int ITEMS = 16; using Key = uint32_t; };
+template <> struct SplitGeometry<8> { static constexpr int ITEMS = 8; using Key = uint64_t; };
+
+template <int KB, bool HUFF, int K>
+void launch_one(const SplitArgs& a, uint32_t L, cudaStream_t s) {
+  using G = SplitGeometry<KB>;
+  using Key = typename G::Key;
+  using Tr = typename std::conditional<HUFF, HuffKeys<Key>, PlainKeys<Key>>::type;
+  using P = SplitPass<Key, Tr, K, kSplitThreads, G::ITEMS>;
+  auto kern = split_pass_kernel<Key, Tr, K, kSplitThreads, G::ITEMS>;
+  static bool configured = false;  // one attribute call per instantiation and process
+  const size_t smem = P::smem_bytes();
+  if (!configured) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    configured = true;
+  }
+  Tr tr{L};
+  kern<<<a.tiles, kSplitThreads, smem, s>>>(a, tr);
+}
+
+template <int KB, bool HUFF>
+void launch_k(int K, const SplitArgs& a, uint32_t L, cudaStream_t s) {
+  switch (K) {
+    case 1: launch_one<KB, HUFF, 1>(a, L, s); break;
+    case 2: launch_one<KB, HUFF, 2>(a, L, s); break;
+    case 3: launch_one<KB, HUFF, 3>(a, L, s); break;
+    default: launch_one<KB, HUFF, 4>(a, L, s); break;
+  }
+}
+
+}  // namespace
+
+uint32_t split_tile_elems(uint32_t key_bytes) {
+  switch (key_bytes) {
+    case 1: return kSplitThreads * SplitGeometry<1>::ITEMS;
+    case 2: return kSplitThreads * SplitGeometry<2>::ITEMS;
+    case 4: return kSplitThreads * SplitGeometry<4>::ITEMS;
+    default: return kSplitThreads * SplitGeometry<8>::ITEMS;
+  }
+}
+
+size_t split_smem_bytes(uint32_t key_bytes, int K) {
+  const size_t T = split_tile_elems(key_bytes);
+  return 2 * T * key_bytes + size_t(K > 1 ? K - 1 : 1) * (T / 32 + 1) * 4;
+}
+
+void launch_split_pass(uint32_t key_bytes, bool huffman, int K, const SplitArgs& a, uint32_t L, cudaStream_t s,
+                       uint64_t* launches) {
+  if (a.tiles == 0) return;
+  if (huffman) {
+    if (key_bytes == 4) launch_k<4, true>(K, a, L, s); else launch_k<8, true>(K, a, L, s);
+  } else {
+    switch (key_bytes) {
+      case 1: launch_k<1, false>(K, a, L, s); break;
+      case 2: launch_k<2, false>(K, a, L, s); break;
+      default: launch_k<4, false>(K, a, L, s); break;
+    }
+  }
+  ++*launches;
+}
+
+}  // namespace pwmgpu
