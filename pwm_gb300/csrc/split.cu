@@ -9,7 +9,7 @@ constexpr int kSplitThreads = 512;
 
 template <int KB>
 struct SplitGeometry;
-template <> struct SplitGeometry<1> { static constexpr int ITEMS = 32; using Key = uint8_t; };
+template <> struct SplitGeometry<1> { static constexpr int ITEMS = 64; using Key = uint8_t; };
 template <> struct SplitGeometry<2> { static constexpr int ITEMS = 32; using Key = uint16_t; };
 template <> struct SplitGeometry<4> { static constexpr int ITEMS = 16; using Key = uint32_t; };
 template <> struct SplitGeometry<8> { static constexpr int ITEMS = 8; using Key = uint64_t; };

@@ -10,13 +10,21 @@
 //
 //   * level l's bits are in tile order: each warp ballots 32 positions and
 //     stores the bit-reversed mask as one coalesced 32-bit chunk;
-//   * the tile is then stably split K times in shared memory (LSD order, bit
-//     l first); after split j the tile is sorted by key_j = bits l..l+j-1
-//     (bit l least significant) and holds 2^j runs, and run v of level l+j
-//     lands at  start_j[v] + (count of key_j == v in earlier tiles);
+//   * level l+j (0 < j < K) of S_{l+j} is S_l stably sorted by key_j = bits
+//     l..l+j-1 (bit l least significant): the tile contributes one run per
+//     value v of key_j, run v holding bit l+j of the tile's elements with
+//     key_j == v in tile order, and it lands at
+//         start_j[v] + (count of key_j == v in earlier tiles).
+//     The runs are built without moving keys: per round of 32 elements a warp
+//     ballots the members of every run and compacts their bits with one
+//     redux.sync.or (each member shifts its bit to its rank in the run);
+//   * only the final order (key_K, the sequence S_{l+K} for the next pass) is
+//     materialised: each key is stored once into its run in shared memory and
+//     the runs are copied out coalesced;
 //   * the per-tile run counts are exchanged between tiles with a decoupled
-//     look-back (one counter per run), so every tile learns its global run
-//     offsets with a single read of its input.
+//     look-back (one counter per finest run), walked 32 predecessors at a time
+//     by one warp per counter, so every tile learns its global run offsets
+//     with a single read of its input.
 //
 // Huffman-shaped matrices use the same pass over packed code keys: an
 // element is alive at level m while its code is longer than m, and the runs
@@ -77,82 +85,14 @@ struct SplitPass {
   static constexpr int WARPS = THREADS / 32;
   static constexpr int C = (2 << K) - 2;             // runs of all levels j = 1..K
   static constexpr int NLB = Traits::kDrops ? C : (1 << K);  // look-back counters
-  static constexpr int CHUNKS = T / 32;
-  static_assert(T % 64 == 0, "tile must cover whole words");
+  static constexpr int SWORDS = T / 32 + 2;          // words of one inner-level bit stream
+  static_assert(T % 64 == 0 && (T / WARPS) % 32 == 0, "tile must cover whole words and warp rounds");
   static constexpr size_t smem_bytes() {
-    return size_t(2) * T * sizeof(KeyT) + size_t(K > 1 ? K - 1 : 1) * (CHUNKS + 1) * 4;
+    return size_t(2) * T * sizeof(KeyT) + size_t(K > 1 ? K - 1 : 1) * SWORDS * 4;
   }
 };
 
-__device__ __forceinline__ int run_offset(int j) { return (1 << j) - 2; }
-
-// Stable split of in[0..n) by `bit` (zeros first) keeping only elements alive
-// at `keep_level`; returns the number of elements written to out.
-template <typename KeyT, typename Traits, int THREADS>
-__device__ __forceinline__ uint32_t block_split(const KeyT* in, KeyT* out, uint32_t n, const Traits& tr,
-                                                uint32_t bit_level, uint32_t keep_level, uint32_t* wz, uint32_t* wo) {
-  constexpr int WARPS = THREADS / 32;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t lt = (1u << lane) - 1u;
-  const uint32_t per = ((n + WARPS - 1) / WARPS + 31) & ~31u;
-  const uint32_t b0 = min(n, per * warp), b1 = min(n, b0 + per);
-  uint32_t z = 0, o = 0;
-  for (uint32_t base = b0; base < b1; base += 32) {
-    uint32_t e = base + lane;
-    bool in_range = e < b1;
-    KeyT k = in_range ? in[e] : KeyT(0);
-    bool keep = in_range && tr.alive(k, keep_level);
-    uint32_t b = tr.bit(k, bit_level);
-    z += __popc(__ballot_sync(0xFFFFFFFFu, keep && !b));
-    o += __popc(__ballot_sync(0xFFFFFFFFu, keep && b));
-  }
-  if (lane == 0) { wz[warp] = z; wo[warp] = o; }
-  __syncthreads();
-  if (warp == 0) {
-    uint32_t vz = lane < WARPS ? wz[lane] : 0, vo = lane < WARPS ? wo[lane] : 0;
-    uint32_t sz = vz, so = vo;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      uint32_t tz = __shfl_up_sync(0xFFFFFFFFu, sz, d), to = __shfl_up_sync(0xFFFFFFFFu, so, d);
-      if (lane >= d) { sz += tz; so += to; }
-    }
-    uint32_t total_z = __shfl_sync(0xFFFFFFFFu, sz, 31), total_o = __shfl_sync(0xFFFFFFFFu, so, 31);
-    if (lane < WARPS) { wz[lane] = sz - vz; wo[lane] = total_z + so - vo; }
-    if (lane == 0) { wz[WARPS] = total_z + total_o; }
-  }
-  __syncthreads();
-  uint32_t zb = wz[warp], ob = wo[warp];
-  for (uint32_t base = b0; base < b1; base += 32) {
-    uint32_t e = base + lane;
-    bool in_range = e < b1;
-    KeyT k = in_range ? in[e] : KeyT(0);
-    bool keep = in_range && tr.alive(k, keep_level);
-    uint32_t b = tr.bit(k, bit_level);
-    uint32_t m0 = __ballot_sync(0xFFFFFFFFu, keep && !b);
-    uint32_t m1 = __ballot_sync(0xFFFFFFFFu, keep && b);
-    if (keep) out[b ? ob + __popc(m1 & lt) : zb + __popc(m0 & lt)] = k;
-    zb += __popc(m0);
-    ob += __popc(m1);
-  }
-  uint32_t total = wz[WARPS];
-  __syncthreads();
-  return total;
-}
-
-// Pack bit `level` of keys[0..n) into sbits (position i at bit 31-(i%32) of
-// word i/32); words up to ceil(n/32) are written, the next one is zeroed.
-template <typename KeyT, typename Traits, int THREADS>
-__device__ __forceinline__ void pack_bits(const KeyT* keys, uint32_t n, const Traits& tr, uint32_t level,
-                                          uint32_t* sbits) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t nchunks = (n + 31) / 32;
-  for (uint32_t c = warp; c <= nchunks; c += THREADS / 32) {
-    uint32_t e = c * 32 + lane;
-    bool v = e < n && tr.bit(keys[e], level);
-    uint32_t mask = __ballot_sync(0xFFFFFFFFu, v);
-    if (lane == 0) sbits[c] = __brev(mask);
-  }
-}
+__device__ __forceinline__ constexpr int run_offset(int j) { return (1 << j) - 2; }
 
 // 32 stream bits starting at (possibly negative) bit offset `src` of sbits.
 __device__ __forceinline__ uint32_t extract32(const uint32_t* sbits, int64_t src) {
@@ -165,31 +105,60 @@ __device__ __forceinline__ uint32_t extract32(const uint32_t* sbits, int64_t src
   return __funnelshift_l(w1, w0, uint32_t(s & 31));
 }
 
+// Exclusive prefix over predecessor tiles of look-back counter `c`, walked by
+// one warp 32 tiles at a time; publishes this tile's inclusive value.
+__device__ __forceinline__ uint64_t warp_lookback(unsigned long long* lb, int nlb, uint32_t tile, int c, uint64_t mine,
+                                                  uint32_t* status) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long* row = lb + uint64_t(tile) * nlb + c;
+  if (tile == 0) {
+    if (lane == 0) st_volatile(row, kFlagPrefix | mine);
+    return 0;
+  }
+  uint64_t excl = 0;
+  int64_t base = int64_t(tile) - 1;
+  while (true) {
+    const int64_t t = base - lane;
+    uint64_t s = kFlagPrefix;  // before tile 0: an empty inclusive prefix
+    if (t >= 0) s = lookback_wait(lb + uint64_t(t) * nlb + c, status);
+    const uint32_t pmask = __ballot_sync(0xFFFFFFFFu, (s >> 62) == 2);
+    const int stop = pmask ? __ffs(pmask) - 1 : 31;
+    uint64_t v = lane <= stop ? (s & kCountMask) : 0;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, d);
+    excl += v;
+    if (pmask) break;
+    base -= 32;
+  }
+  if (lane == 0) st_volatile(row, kFlagPrefix | (excl + mine));
+  return excl;
+}
+
 template <typename KeyT, typename Traits, int K, int THREADS, int ITEMS>
 __global__ void __launch_bounds__(THREADS) split_pass_kernel(SplitArgs a, Traits tr) {
   using P = SplitPass<KeyT, Traits, K, THREADS, ITEMS>;
-  constexpr int T = P::T, C = P::C, NLB = P::NLB, WARPS = P::WARPS, CHUNKS = P::CHUNKS;
+  constexpr int T = P::T, C = P::C, NLB = P::NLB, WARPS = P::WARPS, SWORDS = P::SWORDS;
+  constexpr int FIN = run_offset(K);            // first finest run
+  constexpr int PER = T / WARPS;                // elements per warp
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  KeyT* buf0 = reinterpret_cast<KeyT*>(smem_raw);
-  KeyT* buf1 = buf0 + T;
-  uint32_t* sbits = reinterpret_cast<uint32_t*>(buf1 + T);
+  KeyT* keys = reinterpret_cast<KeyT*>(smem_raw);
+  KeyT* sorted = keys + T;
+  uint32_t* sbits = reinterpret_cast<uint32_t*>(sorted + T);
 
   __shared__ uint32_t s_tile;
-  __shared__ uint32_t cnt[C];          // run sizes of this tile, all levels j=1..K
-  __shared__ uint32_t lstart[C];       // run starts inside the tile
-  __shared__ unsigned long long gpos[C];  // global start of every run
+  __shared__ uint32_t cntw[WARPS][C];          // run sizes per warp
+  __shared__ uint32_t basew[WARPS][C];         // tile-local start of each warp's part of a run
+  __shared__ uint32_t cnt[C];                  // run sizes of the tile
+  __shared__ uint32_t lstart[C];               // tile-local run starts
+  __shared__ unsigned long long gpos[C];       // global run starts
   __shared__ unsigned long long pre[NLB];
-  __shared__ uint32_t wz[WARPS + 1], wo[WARPS + 1];
-  __shared__ uint32_t nstage[K + 1];
-  __shared__ uint32_t chunk_prefix[C + 1];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int Kp = int(a.levels_here);   // levels present in this pass (1..K)
+  const uint32_t lt = (1u << lane) - 1u;
   const bool has_out = a.out != nullptr;
-  const int splits = has_out ? Kp : Kp - 1;
 
   if (tid == 0) s_tile = atomicAdd(a.tile_counter, 1u);
-  for (int c = tid; c < C; c += THREADS) cnt[c] = 0;
+  for (int i = tid; i < (K > 1 ? K - 1 : 0) * SWORDS; i += THREADS) sbits[i] = 0;
   __syncthreads();
   const uint32_t tile = s_tile;
   const uint64_t tile_start = uint64_t(tile) * T;
@@ -200,117 +169,157 @@ __global__ void __launch_bounds__(THREADS) split_pass_kernel(SplitArgs a, Traits
   // ---- load the tile (16-byte vectors where the tile is full) ----------
   if (n == T && (reinterpret_cast<uintptr_t>(in) & 15) == 0) {
     const uint4* src = reinterpret_cast<const uint4*>(in);
-    uint4* dst = reinterpret_cast<uint4*>(buf0);
+    uint4* dst = reinterpret_cast<uint4*>(keys);
     constexpr int V = T * sizeof(KeyT) / 16;
 #pragma unroll 4
     for (int i = tid; i < V; i += THREADS) dst[i] = __ldcs(src + i);
   } else {
-    for (uint32_t i = tid; i < n; i += THREADS) buf0[i] = in[i];
+    for (uint32_t i = tid; i < n; i += THREADS) keys[i] = in[i];
   }
   __syncthreads();
 
-  // ---- run counts of every level of the pass (warp ballots) ------------
+  const uint32_t w0 = uint32_t(warp) * PER;
+  const uint32_t w1 = min(n, w0 + PER);
+
+  // ---- per-warp run counts (ballots per run value) ----------------------
   {
     uint32_t acc[C];
 #pragma unroll
     for (int c = 0; c < C; ++c) acc[c] = 0;
-    const uint32_t per = ((n + WARPS - 1) / WARPS + 31) & ~31u;
-    const uint32_t b0 = min(n, per * warp), b1 = min(n, b0 + per);
-    for (uint32_t base = b0; base < b1; base += 32) {
-      uint32_t e = base + lane;
-      bool ok = e < b1;
-      KeyT k = ok ? buf0[e] : KeyT(0);
+    for (uint32_t base = w0; base < w1; base += 32) {
+      const uint32_t e = base + lane;
+      const bool ok = e < w1;
+      const KeyT k = ok ? keys[e] : KeyT(0);
       uint32_t key = 0;
 #pragma unroll
       for (int j = 1; j <= K; ++j) {
         key |= tr.bit(k, a.level + j - 1) << (j - 1);
         if (Traits::kDrops || j == K) {
-          bool al = ok && j <= Kp && tr.alive(k, a.level + j);
+          const bool al = ok && tr.alive(k, a.level + j);
 #pragma unroll
           for (int v = 0; v < (1 << j); ++v)
             acc[run_offset(j) + v] += __popc(__ballot_sync(0xFFFFFFFFu, al && key == uint32_t(v)));
         }
       }
     }
+    if (!Traits::kDrops) {
+      // runs of levels j < K are unions of finest runs (key_j = low j bits)
+#pragma unroll
+      for (int j = 1; j < K; ++j)
+#pragma unroll
+        for (int v = 0; v < (1 << j); ++v) {
+          uint32_t s = 0;
+#pragma unroll
+          for (int h = 0; h < (1 << (K - j)); ++h) s += acc[FIN + v + (h << j)];
+          acc[run_offset(j) + v] = s;
+        }
+    }
     if (lane == 0) {
 #pragma unroll
-      for (int c = 0; c < C; ++c)
-        if (acc[c]) atomicAdd(&cnt[c], acc[c]);
+      for (int c = 0; c < C; ++c) cntw[warp][c] = acc[c];
     }
   }
   __syncthreads();
-  if (!Traits::kDrops) {
-    // derive the run counts of levels j < K from the finest runs
-    for (int c = tid; c < C - (1 << K); c += THREADS) {
-      int j = 1;
-      while (c >= run_offset(j + 1)) ++j;
-      int v = c - run_offset(j);
-      uint32_t s = 0;
-      for (int h = 0; h < (1 << (K - j)); ++h) s += cnt[run_offset(K) + v + (h << j)];
-      cnt[c] = s;
-    }
-    __syncthreads();
-  }
 
-  // ---- publish the tile's counts and look back over predecessors ---------
-  if (tid < NLB) {
-    const int c = Traits::kDrops ? tid : run_offset(K) + tid;
-    const uint64_t mine = cnt[c];
-    unsigned long long* row = a.lookback + uint64_t(tile) * NLB;
-    if (tile == 0) {
-      st_volatile(row + tid, kFlagPrefix | mine);
-      pre[tid] = 0;
-    } else {
-      st_volatile(row + tid, kFlagAggregate | mine);
-      uint64_t excl = 0;
-      for (int64_t t = int64_t(tile) - 1; t >= 0; --t) {
-        uint64_t s = lookback_wait(a.lookback + uint64_t(t) * NLB + tid, a.status);
-        excl += s & kCountMask;
-        if ((s >> 62) == 2) break;
-      }
-      st_volatile(row + tid, kFlagPrefix | (excl + mine));
-      pre[tid] = excl;
-    }
+  // ---- tile totals, local run starts, per-warp bases ---------------------
+  if (tid < C) {
+    uint32_t t = 0;
+    for (int w = 0; w < WARPS; ++w) t += cntw[w][tid];
+    cnt[tid] = t;
   }
-
-  // ---- level l bits in tile order (independent of the look-back) ---------
-  {
-    uint32_t* dst = reinterpret_cast<uint32_t*>(a.bv[0]);
-    uint32_t* dst_tree = reinterpret_cast<uint32_t*>(a.tree_level0);
-    const uint64_t q0 = tile_start >> 5;
-    const uint32_t nch = ((n + 63) / 64) * 2;  // whole words (zero padded)
-    for (uint32_t c = warp; c < nch; c += WARPS) {
-      uint32_t e = c * 32 + lane;
-      bool v = e < n && tr.bit(buf0[e], a.level);
-      uint32_t mask = __brev(__ballot_sync(0xFFFFFFFFu, v));
-      if (lane == 0) {
-        dst[chunk_u32_index(q0 + c)] = mask;
-        if (dst_tree) dst_tree[chunk_u32_index(q0 + c)] = mask;
-      }
-    }
-  }
-
-  // ---- local splits; pack the bits of the inner levels -------------------
-  KeyT* cur = buf0;
-  KeyT* nxt = buf1;
-  if (tid == 0) nstage[0] = n;
-  uint32_t ncur = n;
-  for (int j = 1; j <= splits; ++j) {
-    ncur = block_split<KeyT, Traits, THREADS>(cur, nxt, ncur, tr, a.level + j - 1, a.level + j, wz, wo);
-    KeyT* t = cur; cur = nxt; nxt = t;
-    if (j < Kp) pack_bits<KeyT, Traits, THREADS>(cur, ncur, tr, a.level + j, sbits + (j - 1) * (CHUNKS + 1));
-    if (tid == 0) nstage[j] = ncur;
-  }
-
-  // ---- run starts inside the tile and global run positions ---------------
-  __syncthreads();  // pre[] complete, splits done
+  __syncthreads();
   if (tid < C) {
     int j = 1;
     while (tid >= run_offset(j + 1)) ++j;
-    int v = tid - run_offset(j);
+    const int v = tid - run_offset(j);
     uint32_t s = 0;
     for (int u = 0; u < v; ++u) s += cnt[run_offset(j) + u];
     lstart[tid] = s;
+    for (int w = 0; w < WARPS; ++w) {
+      basew[w][tid] = s;
+      s += cntw[w][tid];
+    }
+  }
+  // publish this tile's aggregates; successors' walks need them
+  if (tid < NLB && tile != 0) {
+    const int c = Traits::kDrops ? tid : FIN + tid;
+    uint32_t t = 0;
+    for (int w = 0; w < WARPS; ++w) t += cntw[w][c];
+    st_volatile(a.lookback + uint64_t(tile) * NLB + tid, kFlagAggregate | t);
+  }
+  __syncthreads();
+
+  // ---- look-back right after the counts, so that inclusive prefixes travel
+  // ---- quickly down the tile chain; the other warps start their chunk -----
+  for (int c = warp; c < NLB; c += WARPS) {
+    const int cc = Traits::kDrops ? c : FIN + c;
+    const uint64_t p = warp_lookback(a.lookback, NLB, tile, c, cnt[cc], a.status);
+    if (lane == 0) pre[c] = p;
+  }
+
+  // ---- one pass over the tile: level l bits, inner runs, final order ------
+  {
+    uint32_t run_off[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) run_off[c] = basew[warp][c];
+    uint32_t* dst0 = reinterpret_cast<uint32_t*>(a.bv[0]);
+    uint32_t* dst_tree = reinterpret_cast<uint32_t*>(a.tree_level0);
+    const uint64_t q0 = tile_start >> 5;
+    const uint32_t wend = ((min(n, w0 + PER) + 63) & ~63u);  // whole words of level l (zero padded)
+    for (uint32_t base = w0; base < wend && base < w0 + PER; base += 32) {
+      const uint32_t e = base + lane;
+      const bool ok = e < w1;
+      const KeyT k = ok ? keys[e] : KeyT(0);
+      // level l: tile order
+      const uint32_t m0 = __brev(__ballot_sync(0xFFFFFFFFu, ok && tr.bit(k, a.level)));
+      if (lane == 0) {
+        dst0[chunk_u32_index(q0 + (base >> 5))] = m0;
+        if (dst_tree) dst_tree[chunk_u32_index(q0 + (base >> 5))] = m0;
+      }
+      if (base >= w1) continue;
+      uint32_t key = 0;
+#pragma unroll
+      for (int j = 1; j <= K; ++j) {
+        key |= tr.bit(k, a.level + j - 1) << (j - 1);
+        const bool al = ok && tr.alive(k, a.level + j);
+        if (j < K) {
+          const uint32_t b = tr.bit(k, a.level + j);
+          uint32_t* sb = sbits + (j - 1) * SWORDS;
+#pragma unroll
+          for (int v = 0; v < (1 << j); ++v) {
+            const int c = run_offset(j) + v;
+            const bool member = al && key == uint32_t(v);
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, member);
+            if (m == 0) continue;
+            const uint32_t r = __popc(m & lt);
+            const uint32_t bits = __reduce_or_sync(0xFFFFFFFFu, (member && b) ? (0x80000000u >> r) : 0u);
+            if (lane == 0) {
+              const uint32_t pos = run_off[c], sh = pos & 31, cntm = __popc(m);
+              atomicOr(&sb[pos >> 5], bits >> sh);
+              if (sh + cntm > 32) atomicOr(&sb[(pos >> 5) + 1], bits << (32 - sh));
+            }
+            run_off[c] += __popc(m);
+          }
+        } else if (has_out) {
+#pragma unroll
+          for (int v = 0; v < (1 << K); ++v) {
+            const int c = FIN + v;
+            const bool member = al && key == uint32_t(v);
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, member);
+            if (m == 0) continue;
+            if (member) sorted[run_off[c] + __popc(m & lt)] = k;
+            run_off[c] += __popc(m);
+          }
+        }
+      }
+    }
+  }
+
+  __syncthreads();  // pre[] (look-back) and the local runs are complete
+  if (tid < C) {
+    int j = 1;
+    while (tid >= run_offset(j + 1)) ++j;
+    const int v = tid - run_offset(j);
     uint64_t p;
     if (Traits::kDrops) {
       p = pre[tid];
@@ -318,65 +327,52 @@ __global__ void __launch_bounds__(THREADS) split_pass_kernel(SplitArgs a, Traits
       p = 0;
       for (int h = 0; h < (1 << (K - j)); ++h) p += pre[v + (h << j)];
     }
-    gpos[tid] = (j <= Kp) ? a.starts[tid] + p : 0;
+    gpos[tid] = a.starts[tid] + p;
   }
   __syncthreads();
 
-  // ---- inner-level bit runs: plain stores for whole chunks, OR at edges ---
-  if (Kp > 1) {
-    if (tid == 0) {
-      uint32_t q = 0;
-      for (int c = 0; c < C; ++c) {
-        chunk_prefix[c] = q;
-        int j = 1;
-        while (c >= run_offset(j + 1)) ++j;
-        uint32_t len = cnt[c];
-        if (j < Kp && len > 0) {
-          uint64_t g = gpos[c];
-          q += uint32_t(((g + len - 1) >> 5) - (g >> 5) + 1);
-        }
-      }
-      chunk_prefix[C] = q;
+  // ---- inner-level runs to HBM: plain stores for whole chunks, OR at edges ---
+#pragma unroll 1
+  for (int c = 0; c < FIN; ++c) {
+    const uint32_t len = cnt[c];
+    if (len == 0) continue;
+    int j = 1;
+    while (c >= run_offset(j + 1)) ++j;
+    const uint64_t g = gpos[c];
+    if (g + len > a.level_size[j]) {  // inconsistent run tables: never write out of range
+      if (tid == 0) atomicOr(a.status, kErrBounds);
+      continue;
     }
-    __syncthreads();
-    const uint32_t total_chunks = chunk_prefix[C];
-    for (uint32_t qi = tid; qi < total_chunks; qi += THREADS) {
-      int c = 0;
-      while (chunk_prefix[c + 1] <= qi) ++c;
-      int j = 1;
-      while (c >= run_offset(j + 1)) ++j;
-      const uint64_t g = gpos[c];
-      const uint32_t len = cnt[c];
-      if (g + len > a.level_size[j]) {  // inconsistent run tables: never write out of range
-        atomicOr(a.status, kErrBounds);
-        continue;
-      }
-      const uint64_t q = (g >> 5) + (qi - chunk_prefix[c]);
-      const int64_t d = int64_t(q << 5) - int64_t(g);         // chunk start relative to run start
-      const uint32_t* sb = sbits + (j - 1) * (CHUNKS + 1);
-      uint32_t val = extract32(sb, int64_t(lstart[c]) + d);
-      if (d < 0) val = extract32(sb, int64_t(lstart[c])) >> uint32_t(-d);
+    const uint32_t* sb = sbits + (j - 1) * SWORDS;
+    const uint64_t qa = g >> 5, qb = (g + len - 1) >> 5;
+    uint32_t* dst = reinterpret_cast<uint32_t*>(a.bv[j]);
+    for (uint64_t q = qa + tid; q <= qb; q += THREADS) {
+      const int64_t d = int64_t(q << 5) - int64_t(g);  // chunk start relative to the run start
+      const uint32_t val = d < 0 ? (extract32(sb, int64_t(lstart[c])) >> uint32_t(-d))
+                                 : extract32(sb, int64_t(lstart[c]) + d);
       const uint32_t lo = d < 0 ? uint32_t(-d) : 0u;
       const int64_t hi64 = int64_t(len) - d;
       const uint32_t hi = hi64 >= 32 ? 32u : uint32_t(hi64);
       const uint32_t mask = chunk_mask(lo, hi);
-      uint32_t* dst = reinterpret_cast<uint32_t*>(a.bv[j]) + chunk_u32_index(q);
-      if (mask == 0xFFFFFFFFu) *dst = val;
-      else atomicOr(dst, val & mask);
+      if (mask == 0xFFFFFFFFu) dst[chunk_u32_index(q)] = val;
+      else atomicOr(&dst[chunk_u32_index(q)], val & mask);
     }
   }
 
-  // ---- S_{l+K}: runs of the final split to their global positions --------
+  // ---- S_{l+K}: runs of the final order to their global positions ---------
   if (has_out) {
     KeyT* out = static_cast<KeyT*>(a.out);
-    const uint32_t nout = nstage[Kp];
-    constexpr int R = 1 << K;
-    for (uint32_t e = tid; e < nout; e += THREADS) {
-      int v = 0;
-      while (v + 1 < R && lstart[run_offset(K) + v + 1] <= e) ++v;
-      const uint64_t dst = gpos[run_offset(K) + v] + (e - lstart[run_offset(K) + v]);
-      if (dst < a.level_size[K]) out[dst] = cur[e];
-      else atomicOr(a.status, kErrBounds);
+#pragma unroll 1
+    for (int v = 0; v < (1 << K); ++v) {
+      const uint32_t len = cnt[FIN + v];
+      if (len == 0) continue;
+      const uint64_t g = gpos[FIN + v];
+      if (g + len > a.level_size[K]) {
+        if (tid == 0) atomicOr(a.status, kErrBounds);
+        continue;
+      }
+      const KeyT* src = sorted + lstart[FIN + v];
+      for (uint32_t i = tid; i < len; i += THREADS) out[g + i] = src[i];
     }
   }
 }
