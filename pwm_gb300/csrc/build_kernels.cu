@@ -106,30 +106,42 @@ __device__ __forceinline__ uint64_t bits_at(const uint64_t* level, uint64_t src,
   return take == 64 ? v : (v & ~(~0ull >> take));
 }
 
+constexpr int kRegroupWords = 8;  // consecutive output words per thread
+
 __global__ void regroup_kernel(const uint64_t* __restrict__ matrix_level, uint64_t* __restrict__ tree_level,
                                uint64_t nbits, const uint64_t* __restrict__ seg_tree,
                                const uint64_t* __restrict__ seg_matrix, uint64_t nseg, uint32_t* status) {
   const uint64_t nwords = (nbits + 63) >> 6;
-  for (uint64_t w = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; w < nwords;
-       w += uint64_t(gridDim.x) * blockDim.x) {
-    const uint64_t p0 = w << 6, end = min(p0 + 64, nbits);
-    uint64_t pos = p0, acc = 0;
+  const uint64_t first = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) * kRegroupWords;
+  if (first >= nwords) return;
+  // last segment starting at or before the first bit of this thread
+  uint64_t lo = 0, hi = nseg;
+  const uint64_t p0 = first << 6;
+  while (hi - lo > 1) {
+    const uint64_t mid = (lo + hi) >> 1;
+    if (seg_tree[mid] <= p0) lo = mid; else hi = mid;
+  }
+  uint64_t seg = lo;
+  uint64_t seg_start = seg_tree[seg];
+  uint64_t seg_end = seg + 1 < nseg ? seg_tree[seg + 1] : nbits;
+  const uint64_t last = min(nwords, first + kRegroupWords);
+  for (uint64_t w = first; w < last; ++w) {
+    const uint64_t wp = w << 6, end = min(wp + 64, nbits);
+    uint64_t pos = wp, acc = 0;
     while (pos < end) {
-      // last segment starting at or before pos
-      uint64_t lo = 0, hi = nseg;
-      while (hi - lo > 1) {
-        uint64_t mid = (lo + hi) >> 1;
-        if (seg_tree[mid] <= pos) lo = mid; else hi = mid;
+      while (pos >= seg_end) {  // advance to the segment holding pos (empty ones are skipped)
+        ++seg;
+        seg_start = seg_end;
+        seg_end = seg + 1 < nseg ? seg_tree[seg + 1] : nbits;
       }
-      const uint64_t seg_end = lo + 1 < nseg ? seg_tree[lo + 1] : nbits;
       const uint64_t stop = min(end, seg_end);
       const uint32_t take = uint32_t(stop - pos);
-      const uint64_t src = seg_matrix[lo] + (pos - seg_tree[lo]);
-      if (src + take > nbits || take == 0) {  // inconsistent segments: never read out of range
+      const uint64_t src = seg_matrix[seg] + (pos - seg_start);
+      if (src + take > nbits) {  // inconsistent segments: never read out of range
         atomicOr(status, kErrBounds);
         break;
       }
-      acc |= bits_at(matrix_level, src, take) >> (pos - p0);
+      acc |= bits_at(matrix_level, src, take) >> (pos - wp);
       pos = stop;
     }
     tree_level[w] = acc;
@@ -200,8 +212,9 @@ void launch_regroup(const uint64_t* matrix_level, uint64_t* tree_level, uint64_t
                     const uint64_t* seg_matrix, uint64_t nseg, uint32_t* status, cudaStream_t s, uint64_t* launches) {
   const uint64_t nwords = (nbits + 63) >> 6;
   if (nwords == 0) return;
-  regroup_kernel<<<grid_for(nwords, 256), 256, 0, s>>>(matrix_level, tree_level, nbits, seg_tree, seg_matrix, nseg,
-                                                       status);
+  const uint64_t threads = (nwords + kRegroupWords - 1) / kRegroupWords;
+  regroup_kernel<<<unsigned((threads + 255) / 256), 256, 0, s>>>(matrix_level, tree_level, nbits, seg_tree, seg_matrix,
+                                                                 nseg, status);
   ++*launches;
 }
 

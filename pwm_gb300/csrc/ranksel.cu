@@ -9,6 +9,8 @@
 // accepted).  Select samples (bin_select_popcnt.hpp:38-107): the position of
 // every 8192nd zero/one, taken in the L1 block where the running count first
 // exceeds the next sample number.
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace pwmgpu {
@@ -34,24 +36,27 @@ __global__ void __launch_bounds__(kRsThreads) rs_blocks_kernel(const RankSelectL
   uint32_t* cta_tot = intra + nreal;
   __shared__ uint32_t tot[kRsThreads];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int e = warp; e < kRsThreads; e += kRsThreads / 32) {
-    const uint64_t blk = first + e;
-    uint32_t c = 0;
+  {
+    // one thread per L1 block: 32 words as 16 independent 16-byte loads
+    const uint64_t blk = first + threadIdx.x;
+    uint32_t l2[4] = {0, 0, 0, 0};
     if (blk < nreal) {
-      uint64_t w = blk * kL1Cover + lane;
-      c = w < L.nwords ? __popcll(L.data[w]) : 0u;
+      const uint64_t w0 = blk * kL1Cover;
+      if (w0 + kL1Cover <= L.nwords) {
+        const uint4* p = reinterpret_cast<const uint4*>(L.data + w0);
+        uint4 v[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = __ldcs(p + i);
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+          l2[i >> 2] += __popc(v[i].x) + __popc(v[i].y) + __popc(v[i].z) + __popc(v[i].w);
+      } else {
+        for (uint64_t w = w0; w < L.nwords; ++w) l2[(w - w0) >> 3] += __popcll(L.data[w]);
+      }
+      L.l12[2 * blk + 1] = (l2[0] & 1023u) | ((l2[1] & 1023u) << 10) | ((l2[2] & 1023u) << 20);
     }
-    c += __shfl_xor_sync(0xFFFFFFFFu, c, 1);
-    c += __shfl_xor_sync(0xFFFFFFFFu, c, 2);
-    c += __shfl_xor_sync(0xFFFFFFFFu, c, 4);   // per 8-lane group: one L2 block
-    uint32_t g1 = __shfl_sync(0xFFFFFFFFu, c, 8), g2 = __shfl_sync(0xFFFFFFFFu, c, 16),
-             g3 = __shfl_sync(0xFFFFFFFFu, c, 24);
-    if (lane == 0) {
-      tot[e] = c + g1 + g2 + g3;
-      if (blk < nreal) L.l12[2 * blk + 1] = (c & 1023u) | ((g1 & 1023u) << 10) | ((g2 & 1023u) << 20);
-    }
+    tot[threadIdx.x] = l2[0] + l2[1] + l2[2] + l2[3];
   }
-  __syncthreads();
   // exclusive scan of the 256 block totals (u32, wrapping)
   uint32_t v = tot[threadIdx.x];
   uint32_t x = v;
@@ -128,7 +133,43 @@ __device__ __forceinline__ uint32_t l1_value(const uint32_t* intra, const uint32
   return e < nreal ? cta_off[e / kRsThreads] + intra[e] : 0u;
 }
 
-// Phase 3: l1 values and the select samples (one thread per L1 block).
+// Select-sample position inside L1 block b: the `rem`-th one (value 1) or
+// zero (value 0) counted from the block's first word, found by one warp (lane
+// = word).  pwm walks the L2 blocks and then the words of the block
+// (bin_select_popcnt.hpp:55-99); skipping whole L2 blocks first does not
+// change which word and rank it ends on, so this gives the same position.
+// rem == 0 is pwm's word_select1(first word, 0).  Returns false when the block
+// ends before the rem-th bit (pwm then takes no sample).
+__device__ __forceinline__ bool warp_block_select(const uint64_t* data, uint64_t nwords, uint64_t b, int value,
+                                                  uint32_t rem, uint64_t* pos) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t w = b * kL1Cover + lane;
+  uint64_t word = w < nwords ? data[w] : 0;
+  if (value == 0) word = ~word;
+  const uint32_t pc = w < nwords ? uint32_t(__popcll(word)) : 0u;
+  if (rem == 0) {
+    const uint64_t first = __shfl_sync(0xFFFFFFFFu, word, 0);
+    *pos = word_select1(first, 0) + 64 * (b * kL1Cover);
+    return true;
+  }
+  uint32_t incl = pc;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+    if (lane >= d) incl += y;
+  }
+  const uint32_t hit = __ballot_sync(0xFFFFFFFFu, incl >= rem && w < nwords);
+  if (!hit) return false;
+  const int src = __ffs(hit) - 1;
+  const uint32_t excl = __shfl_sync(0xFFFFFFFFu, incl - pc, src);
+  const uint64_t hw = __shfl_sync(0xFFFFFFFFu, word, src);
+  *pos = word_select1(hw, rem - excl) + 64 * (b * kL1Cover + src);
+  return true;
+}
+
+// Phase 3: l1 values and the select samples.  One thread decides for one L1
+// block; the blocks of a warp that take a sample are then searched one after
+// the other by the whole warp.
 __global__ void __launch_bounds__(kRsThreads) rs_finish_kernel(const RankSelectLevel* lv, const uint32_t* tmp,
                                                               uint64_t tmp_stride) {
   const RankSelectLevel L = lv[blockIdx.y];
@@ -136,46 +177,52 @@ __global__ void __launch_bounds__(kRsThreads) rs_finish_kernel(const RankSelectL
   const uint64_t n12 = L.nwords / kL1Cover + 1;
   const uint32_t* intra = tmp + blockIdx.y * tmp_stride;
   const uint32_t* cta_off = intra + nreal;
+  const int lane = threadIdx.x & 31;
   const uint64_t b = uint64_t(blockIdx.x) * kRsThreads + threadIdx.x;
-  if (b < nreal) L.l12[2 * b] = l1_value(intra, cta_off, nreal, b);
-  if (b == 0 && n12 > nreal) { L.l12[2 * nreal] = 0; L.l12[2 * nreal + 1] = 0; }
-  if (b + 1 >= n12) return;  // pwm examines blocks 0 .. n12-2
-  const uint64_t ones_before = l1_value(intra, cta_off, nreal, b);
-  const uint64_t ones_through = l1_value(intra, cta_off, nreal, b + 1);
-  // select1
-  {
-    const uint64_t f_prev = ones_before;
-    const uint64_t s = f_prev == 0 ? 0 : (f_prev - 1 + kSampleRate - 1) / kSampleRate;
-    const uint64_t next = 1 + kSampleRate * s;
-    if (ones_through > next) {
-      uint32_t rem = uint32_t(next - ones_before);
-      uint32_t l2 = 0;
-      while (l2 < 3 && l2_of(L.l12, b, l2) < rem) rem -= l2_of(L.l12, b, l2++);
-      uint64_t wp = b * kL1Cover + l2 * kL2Cover;
-      while (wp < L.nwords && rem > uint32_t(__popcll(L.data[wp]))) rem -= __popcll(L.data[wp++]);
-      if (wp < L.nwords) {
-        L.s1[s] = uint32_t(word_select1(L.data[wp], rem) + 64 * wp);
-        atomicMax(&L.meta[1], (unsigned long long)(s + 1));
-      }
+  if ((b & ~uint64_t(31)) >= nreal) return;  // whole warp past the level
+  bool need1 = false, need0 = false;
+  uint64_t s1 = 0, s0 = 0;
+  uint32_t rem1 = 0, rem0 = 0;
+  if (b < nreal) {
+    const uint64_t ones_before = l1_value(intra, cta_off, nreal, b);
+    L.l12[2 * b] = uint32_t(ones_before);
+    if (b == 0 && n12 > nreal) { L.l12[2 * nreal] = 0; L.l12[2 * nreal + 1] = 0; }
+    if (b + 1 < n12) {  // pwm examines blocks 0 .. n12-2
+      const uint64_t ones_through = l1_value(intra, cta_off, nreal, b + 1);
+      // sample s is taken in the first block whose running count exceeds
+      // 1 + 8192 s (bin_select_popcnt.hpp:55-99)
+      s1 = ones_before == 0 ? 0 : (ones_before - 1 + kSampleRate - 1) / kSampleRate;
+      const uint64_t next1 = 1 + kSampleRate * s1;
+      need1 = ones_through > next1;
+      rem1 = uint32_t(next1 - ones_before);
+      const uint64_t f_prev = b * kL1Bits - ones_before;
+      const uint64_t f_here = (b + 1) * kL1Bits - ones_through;
+      s0 = f_prev == 0 ? 0 : (f_prev - 1 + kSampleRate - 1) / kSampleRate;
+      const uint64_t next0 = 1 + kSampleRate * s0;
+      need0 = f_here > next0;
+      rem0 = uint32_t(next0 - f_prev);
     }
   }
-  // select0
-  {
-    const uint64_t f_prev = b * kL1Bits - ones_before;
-    const uint64_t f_here = (b + 1) * kL1Bits - ones_through;
-    const uint64_t s = f_prev == 0 ? 0 : (f_prev - 1 + kSampleRate - 1) / kSampleRate;
-    const uint64_t next = 1 + kSampleRate * s;
-    if (f_here > next) {
-      uint32_t rem = uint32_t(next - f_prev);
-      uint32_t l2 = 0;
-      while (l2 < 3 && (kL2Bits - l2_of(L.l12, b, l2)) < rem) rem -= uint32_t(kL2Bits - l2_of(L.l12, b, l2++));
-      uint64_t wp = b * kL1Cover + l2 * kL2Cover;
-      while (wp < L.nwords && rem > uint32_t(__popcll(~L.data[wp]))) rem -= __popcll(~L.data[wp++]);
-      if (wp < L.nwords) {
-        L.s0[s] = uint32_t(word_select1(~L.data[wp], rem) + 64 * wp);
-        atomicMax(&L.meta[0], (unsigned long long)(s + 1));
-      }
+  bool got1 = false, got0 = false;
+  for (int value = 1; value >= 0; --value) {
+    uint32_t todo = __ballot_sync(0xFFFFFFFFu, value ? need1 : need0);
+    while (todo) {
+      const int src = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const uint64_t bb = __shfl_sync(0xFFFFFFFFu, b, src);
+      const uint32_t rr = __shfl_sync(0xFFFFFFFFu, value ? rem1 : rem0, src);
+      const uint64_t ss = __shfl_sync(0xFFFFFFFFu, value ? s1 : s0, src);
+      uint64_t pos;
+      const bool ok = warp_block_select(L.data, L.nwords, bb, value, rr, &pos);
+      if (ok && lane == 0) (value ? L.s1 : L.s0)[ss] = uint32_t(pos);
+      if (lane == src) (value ? got1 : got0) = ok;
     }
+  }
+  // samples are taken in block order, so the count is fixed by the last
+  // block pwm examines (n12 - 2): the samples before it plus its own
+  if (n12 >= 2 && b == n12 - 2) {
+    L.meta[1] = s1 + (got1 ? 1 : 0);
+    L.meta[0] = s0 + (got0 ? 1 : 0);
   }
 }
 

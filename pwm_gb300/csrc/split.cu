@@ -5,14 +5,14 @@ namespace pwmgpu {
 
 namespace {
 
-constexpr int kSplitThreads = 512;
+constexpr int kSplitThreads = 256;
 
 template <int KB>
 struct SplitGeometry;
 template <> struct SplitGeometry<1> { static constexpr int ITEMS = 64; using Key = uint8_t; };
-template <> struct SplitGeometry<2> { static constexpr int ITEMS = 32; using Key = uint16_t; };
-template <> struct SplitGeometry<4> { static constexpr int ITEMS = 16; using Key = uint32_t; };
-template <> struct SplitGeometry<8> { static constexpr int ITEMS = 8; using Key = uint64_t; };
+template <> struct SplitGeometry<2> { static constexpr int ITEMS = 64; using Key = uint16_t; };
+template <> struct SplitGeometry<4> { static constexpr int ITEMS = 32; using Key = uint32_t; };
+template <> struct SplitGeometry<8> { static constexpr int ITEMS = 16; using Key = uint64_t; };
 
 template <int KB, bool HUFF, int K>
 void launch_one(const SplitArgs& a, uint32_t L, cudaStream_t s) {
