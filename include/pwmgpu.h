@@ -173,6 +173,35 @@ PWMGPU_API pwmgpu_status pwmgpu_wx_query(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, i
                                          const uint64_t* d_b, uint64_t count, uint64_t* d_out);
 PWMGPU_API void pwmgpu_wx_free(pwmgpu_wx* wx);
 
+/* Allocation-free rank/select build of one bit vector (device pointers).
+ *
+ * No counterpart in the reference: pwm builds rank/select support on the
+ * host with std::vector.  This entry point exists for callers that cannot
+ * allocate device memory while they run -- code that records CUDA graphs,
+ * plugins whose host framework owns every device buffer, serving loops that
+ * cannot afford an allocator's implicit synchronisation.  It calls no
+ * cudaMalloc/cudaFree and needs no context: its scratch is a fixed 4 MiB
+ * array in the library's device image, resident on every GPU that loads the
+ * library until the process exits.
+ *
+ * Input: `nwords` words of one level (pwm layout).  Outputs (caller
+ * allocated, device memory), identical to pwm's bin_rank_popcnt /
+ * bin_select_popcnt blocks and to pwmgpu_wx_rank_select_blocks:
+ *   d_l0       nwords/67108863 + 1 u64 (cleared here)
+ *   d_l12      2 * (nwords/32 + 1) u32
+ *   d_select0, d_select1   nwords*64/8192 + 2 u32 each
+ *   d_counts   3 u64: select0 samples, select1 samples, total ones (cleared here)
+ * Work is enqueued on `cuda_stream` (NULL: the default stream) of the current
+ * device.  The first call on a device looks up the scratch array's device
+ * address; make that first call before any stream capture.  All calls share
+ * the scratch: calls that overlap on the GPU race, so serialise them (one
+ * stream, or events).  nwords above PWMGPU_NOALLOC_RS_MAX_WORDS (about 2.1e9
+ * bits) returns PWMGPU_ERR_ARG without enqueuing anything. */
+#define PWMGPU_NOALLOC_RS_MAX_WORDS 33423360ull
+PWMGPU_API pwmgpu_status pwmgpu_rank_select_build_noalloc(const uint64_t* d_words, uint64_t nwords, uint64_t* d_l0,
+                                                          uint32_t* d_l12, uint32_t* d_select0, uint32_t* d_select1,
+                                                          uint64_t* d_counts, void* cuda_stream);
+
 /* ---------------------------------------------------------------------- */
 /* Seeded synthetic texts (counter-based, identical on host and device)     */
 /* ---------------------------------------------------------------------- */

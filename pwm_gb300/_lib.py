@@ -54,6 +54,7 @@ SIGNATURES = {
     "pwmgpu_wx_query": (i32, [vp, vp, i32, i32, vp, vp, u64, vp]),
     "pwmgpu_wx_free": (None, [vp]),
     "pwmgpu_generate": (i32, [vp, i32, u64, u64, u64, u32, vp, i32]),
+    "pwmgpu_rank_select_build_noalloc": (i32, [vp, u64, vp, vp, vp, vp, vp, vp]),
 }
 
 

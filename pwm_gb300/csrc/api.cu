@@ -1005,6 +1005,22 @@ pwmgpu_status pwmgpu_compute_huffman(pwmgpu_ctx* ctx, const void* text, uint64_t
   });
 }
 
+// ---- allocation-free rank/select ----------------------------------------------------
+pwmgpu_status pwmgpu_rank_select_build_noalloc(const uint64_t* d_words, uint64_t nwords, uint64_t* d_l0,
+                                               uint32_t* d_l12, uint32_t* d_select0, uint32_t* d_select1,
+                                               uint64_t* d_counts, void* cuda_stream) {
+  if ((nwords && !d_words) || !d_l0 || !d_l12 || !d_select0 || !d_select1 || !d_counts) return PWMGPU_ERR_ARG;
+  if (nwords > PWMGPU_NOALLOC_RS_MAX_WORDS || nwords > noalloc_rank_select_max_words()) return PWMGPU_ERR_ARG;
+  const cudaError_t e =
+      noalloc_rank_select_build(d_words, nwords, d_l0, d_l12, d_select0, d_select1,
+                                reinterpret_cast<unsigned long long*>(d_counts), static_cast<cudaStream_t>(cuda_stream));
+  if (e == cudaSuccess) return PWMGPU_OK;
+  if (e == cudaErrorInvalidValue) return PWMGPU_ERR_ARG;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver || e == cudaErrorNoKernelImageForDevice)
+    return PWMGPU_ERR_NO_DEVICE;
+  return PWMGPU_ERR_CUDA;
+}
+
 // ---- generators ------------------------------------------------------------------
 pwmgpu_status pwmgpu_generate(pwmgpu_ctx* ctx, int dist, uint64_t seed, uint64_t param, uint64_t n,
                               uint32_t word_width, void* out, int on_device) {

@@ -74,6 +74,12 @@ struct QueryStructure {
 void launch_queries(const QueryStructure& q, int op, const uint64_t* a, const uint64_t* b, uint64_t count,
                     uint64_t* out, cudaStream_t s, uint64_t* launches);
 
+// Allocation-free single-level rank/select build on file-scope device arrays
+// (see ranksel.cu); limit in words.
+uint64_t noalloc_rank_select_max_words();
+cudaError_t noalloc_rank_select_build(const uint64_t* words, uint64_t nwords, uint64_t* l0, uint32_t* l12,
+                                      uint32_t* s0, uint32_t* s1, unsigned long long* counts, cudaStream_t stream);
+
 // ---- generators -------------------------------------------------------------------
 void launch_generate(int dist, uint64_t seed, uint64_t param, uint64_t n, uint32_t width, void* out,
                      const uint64_t* thresholds, uint32_t nthr, const uint32_t* perm, cudaStream_t s,

@@ -10,6 +10,7 @@
 // every 8192nd zero/one, taken in the L1 block where the running count first
 // exceeds the next sample number.
 #include <algorithm>
+#include <mutex>
 
 #include "kernels.cuh"
 
@@ -432,6 +433,92 @@ void launch_queries(const QueryStructure& q, int op, const uint64_t* a, const ui
   if (blocks > 65535) blocks = 65535;
   query_kernel<<<unsigned(blocks), 128, 0, s>>>(q, op, a, b, count, out);
   ++*launches;
+}
+
+
+// ===========================================================================
+// Allocation-free rank/select build (pwmgpu_rank_select_build_noalloc).
+//
+// For callers that must not allocate device memory while they run: code that
+// records CUDA graphs, allocator-less plugins that receive every buffer from
+// their host framework, latency-critical serving loops that cannot afford an
+// allocator's implicit synchronisation.  The per-L1-block prefix counts the
+// build needs live in a fixed, file-scope device array instead of context
+// scratch, and the level descriptor the kernels read lives in a file-scope
+// device slot.  Both are resident on every GPU that loads this library until
+// the process exits.  Every call shares them: calls that overlap on the GPU
+// (different streams, or different host threads on one device) race and must
+// be serialised by the caller.
+// ===========================================================================
+namespace {
+
+// 4 MiB: prefix counts for up to kNoAllocMaxL1Blocks L1 blocks plus their
+// per-CTA totals.
+constexpr uint64_t kNoAllocScratchWords = uint64_t(1) << 20;
+constexpr uint64_t kNoAllocMaxL1Blocks = (uint64_t(1) << 20) - (uint64_t(1) << 12);
+
+static __device__ __align__(256) uint32_t g_noalloc_rs_scratch[kNoAllocScratchWords];
+static __device__ __align__(256) RankSelectLevel g_noalloc_rs_level[1];
+
+struct NoAllocSymbols {
+  bool ready = false;
+  uint32_t* scratch = nullptr;
+  RankSelectLevel* level = nullptr;
+};
+
+}  // namespace
+
+// Device addresses of the file-scope arrays for the current device, looked
+// up once per device (the first call on a device does it).
+cudaError_t noalloc_rank_select_symbols(uint32_t** scratch, RankSelectLevel** level) {
+  static std::mutex mu;
+  static NoAllocSymbols per_device[64];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(mu);
+  NoAllocSymbols& s = per_device[dev];
+  if (!s.ready) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_rs_scratch);
+    if (e != cudaSuccess) return e;
+    s.scratch = static_cast<uint32_t*>(p);
+    e = cudaGetSymbolAddress(&p, g_noalloc_rs_level);
+    if (e != cudaSuccess) return e;
+    s.level = static_cast<RankSelectLevel*>(p);
+    s.ready = true;
+  }
+  *scratch = s.scratch;
+  *level = s.level;
+  return cudaSuccess;
+}
+
+uint64_t noalloc_rank_select_max_words() { return kNoAllocMaxL1Blocks * kL1Cover; }
+
+// Enqueues the build of one level's blocks on `stream` using only the
+// file-scope arrays; outputs that must start at zero (l0, counts) are cleared
+// here.  Returns cudaErrorInvalidValue for levels above the limit.
+cudaError_t noalloc_rank_select_build(const uint64_t* words, uint64_t nwords, uint64_t* l0, uint32_t* l12,
+                                      uint32_t* s0, uint32_t* s1, unsigned long long* counts, cudaStream_t stream) {
+  if (nwords > noalloc_rank_select_max_words()) return cudaErrorInvalidValue;
+  uint32_t* scratch = nullptr;
+  RankSelectLevel* dev_level = nullptr;
+  cudaError_t e = noalloc_rank_select_symbols(&scratch, &dev_level);
+  if (e != cudaSuccess) return e;
+  const uint64_t n0 = nwords / (4294967295ull / 64) + 1;
+  e = cudaMemsetAsync(l0, 0, n0 * 8, stream);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(counts, 0, 3 * 8, stream);
+  if (e != cudaSuccess) return e;
+  RankSelectLevel host{words, nwords, l0, l12, s0, s1, counts};
+  e = cudaMemcpyToSymbolAsync(g_noalloc_rs_level, &host, sizeof(host), 0, cudaMemcpyHostToDevice, stream);
+  if (e != cudaSuccess) return e;
+  const uint64_t nreal = (nwords + kL1Cover - 1) / kL1Cover;
+  const uint64_t stride = nreal + (nreal + kRsThreads - 1) / kRsThreads + 1;
+  uint64_t launches = 0;
+  launch_rank_select(&host, 1, dev_level, scratch, stride, stream, &launches);
+  return cudaGetLastError();
 }
 
 }  // namespace pwmgpu
