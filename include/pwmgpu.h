@@ -173,6 +173,41 @@ PWMGPU_API pwmgpu_status pwmgpu_wx_query(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, i
                                          const uint64_t* d_b, uint64_t count, uint64_t* d_out);
 PWMGPU_API void pwmgpu_wx_free(pwmgpu_wx* wx);
 
+/* ---------------------------------------------------------------------- */
+/* Batches: many independent plain texts built by one CUDA graph           */
+/* ---------------------------------------------------------------------- */
+
+/* Texts i = 0..count-1 occupy symbols [offsets[i], offsets[i+1]) of one
+ * device buffer of word_width-byte symbols; text i has levels[i] (1..12)
+ * levels.  Every text gets a wavelet matrix (PWMGPU_MATRIX is required) and,
+ * with PWMGPU_TREE, a levelwise wavelet tree, each bit-identical to a single
+ * pwmgpu_compute of that text.  levels_per_pass (1..4) is the split-pass
+ * width; pwmgpu_batch_set_levels_per_pass changes it (autotuning). */
+typedef struct pwmgpu_batch pwmgpu_batch;
+PWMGPU_API pwmgpu_status pwmgpu_batch_create(pwmgpu_ctx* ctx, uint32_t count, const uint64_t* offsets,
+                                             const uint32_t* levels, uint32_t word_width, uint32_t shape_flags,
+                                             int levels_per_pass, pwmgpu_batch** out);
+/* Builds all texts of the batch from the device buffer d_texts.  The first
+ * call (and a call with another buffer or pass width) runs the build and
+ * records it as a CUDA graph; later calls replay the graph (one graph launch
+ * per batch).  Asynchronous; pwmgpu_batch_check synchronises and reports
+ * device-side errors. */
+PWMGPU_API pwmgpu_status pwmgpu_batch_build(pwmgpu_ctx* ctx, pwmgpu_batch* batch, const void* d_texts);
+PWMGPU_API pwmgpu_status pwmgpu_batch_set_levels_per_pass(pwmgpu_batch* batch, int levels_per_pass);
+PWMGPU_API pwmgpu_status pwmgpu_batch_check(pwmgpu_ctx* ctx, pwmgpu_batch* batch);
+/* Text `index`'s matrix (which = 0, with its zero counts) or tree (which = 1)
+ * in pwm's bit_vectors layout. */
+PWMGPU_API pwmgpu_status pwmgpu_batch_download(pwmgpu_ctx* ctx, const pwmgpu_batch* batch, uint32_t index, int which,
+                                               uint64_t* bv, uint64_t* zeros);
+PWMGPU_API void pwmgpu_batch_free(pwmgpu_batch* batch);
+/* Seeded batch of `count` 8-bit texts: log-normal lengths (median 2^16,
+ * sigma_ln 1.5, clamped to [2^10, 2^24]); 15% Zipf(1.0) byte texts with 8
+ * levels, 85% DNA-like texts over {0..4} (symbol 4 in geometric runs of mean
+ * 50, about 2% of the symbols) with 3 levels.  Writes offsets (count+1) and
+ * levels (count); texts (offsets[count] bytes) may be NULL to size the batch. */
+PWMGPU_API pwmgpu_status pwmgpu_generate_batch(uint64_t seed, uint32_t count, uint64_t* offsets, uint32_t* levels,
+                                               uint8_t* texts);
+
 /* Allocation-free rank/select build of one bit vector (device pointers).
  *
  * No counterpart in the reference: pwm builds rank/select support on the

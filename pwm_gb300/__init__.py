@@ -28,7 +28,8 @@ from ._lib import (GEN_DNA4, GEN_MIX16, GEN_UNIFORM, GEN_ZIPF256, MATRIX, Q_ACCE
                    RANK_SELECT, TREE, PwmGpuError)
 
 __all__ = ["Context", "default_context", "wavelet_structure", "bit_vectors", "algorithm_list",
-           "CONSTRUCTION_REGISTER", "DeviceStructure", "generate", "huffman_codes", "PwmGpuError"]
+           "CONSTRUCTION_REGISTER", "DeviceStructure", "Batch", "generate", "generate_batch", "huffman_codes",
+           "PwmGpuError"]
 
 _WIDTH_DTYPE = {1: np.uint8, 2: np.uint16, 4: np.uint32}
 
@@ -413,6 +414,70 @@ class DeviceStructure:
             self.free()
         except Exception:
             pass
+
+
+class Batch:
+    """A batch of independent plain texts built by one CUDA graph
+    (pwmgpu_batch_*): every text gets a wavelet matrix and, optionally, a
+    levelwise wavelet tree, bit-identical to a single build of that text."""
+
+    def __init__(self, offsets, levels, word_width=1, tree=True, levels_per_pass=2, context=None):
+        self.ctx = context or default_context()
+        self.offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+        self.levels = np.ascontiguousarray(levels, dtype=np.uint32)
+        self.count = int(self.levels.size)
+        self.word_width = int(word_width)
+        self.tree = bool(tree)
+        h = ctypes.c_void_p()
+        flags = MATRIX | (TREE if tree else 0)
+        self.ctx.check(self.ctx.lib.pwmgpu_batch_create(self.ctx.h, self.count, _u64p(self.offsets),
+                                                        _u32p(self.levels), self.word_width, flags,
+                                                        int(levels_per_pass), ctypes.byref(h)))
+        self.h = h
+
+    def build(self, d_texts_ptr):
+        self.ctx.check(self.ctx.lib.pwmgpu_batch_build(self.ctx.h, self.h, ctypes.c_void_p(int(d_texts_ptr))))
+
+    def set_levels_per_pass(self, k):
+        self.ctx.check(self.ctx.lib.pwmgpu_batch_set_levels_per_pass(self.h, int(k)))
+
+    def check(self):
+        self.ctx.check(self.ctx.lib.pwmgpu_batch_check(self.ctx.h, self.h))
+
+    def download(self, index, which=0):
+        n = int(self.offsets[index + 1] - self.offsets[index])
+        L = int(self.levels[index])
+        bvs = bit_vectors([n] * L)
+        zeros = np.zeros(max(L, 1), dtype=np.uint64)
+        self.ctx.check(self.ctx.lib.pwmgpu_batch_download(self.ctx.h, self.h, int(index), int(which), _u64p(bvs.data),
+                                                          _u64p(zeros)))
+        return wavelet_structure(bvs, None if which else [int(z) for z in zeros[:L]], bool(which))
+
+    def free(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.pwmgpu_batch_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def generate_batch(seed, count):
+    """Seeded batch of 8-bit texts (pwmgpu_generate_batch): (texts, offsets, levels)."""
+    lib = _lib.load()
+    offs = np.zeros(count + 1, dtype=np.uint64)
+    levels = np.zeros(max(count, 1), dtype=np.uint32)
+    st = lib.pwmgpu_generate_batch(int(seed), int(count), _u64p(offs), _u32p(levels), None)
+    if st != 0:
+        raise PwmGpuError(st, "pwmgpu_generate_batch failed")
+    texts = np.zeros(max(int(offs[-1]), 1), dtype=np.uint8)
+    st = lib.pwmgpu_generate_batch(int(seed), int(count), _u64p(offs), _u32p(levels), texts.ctypes.data)
+    if st != 0:
+        raise PwmGpuError(st, "pwmgpu_generate_batch failed")
+    return texts[:int(offs[-1])], offs, levels[:count]
 
 
 def generate(dist, seed, n, word_width, param=0, device_ptr=None, context=None):

@@ -54,6 +54,13 @@ SIGNATURES = {
     "pwmgpu_wx_query": (i32, [vp, vp, i32, i32, vp, vp, u64, vp]),
     "pwmgpu_wx_free": (None, [vp]),
     "pwmgpu_generate": (i32, [vp, i32, u64, u64, u64, u32, vp, i32]),
+    "pwmgpu_batch_create": (i32, [vp, u32, u64p, u32p, u32, u32, i32, ctypes.POINTER(vp)]),
+    "pwmgpu_batch_build": (i32, [vp, vp, vp]),
+    "pwmgpu_batch_set_levels_per_pass": (i32, [vp, i32]),
+    "pwmgpu_batch_check": (i32, [vp, vp]),
+    "pwmgpu_batch_download": (i32, [vp, vp, u32, i32, u64p, u64p]),
+    "pwmgpu_batch_free": (None, [vp]),
+    "pwmgpu_generate_batch": (i32, [u64, u32, u64p, u32p, vp]),
     "pwmgpu_rank_select_build_noalloc": (i32, [vp, u64, vp, vp, vp, vp, vp, vp]),
 }
 

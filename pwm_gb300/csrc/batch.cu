@@ -1,0 +1,188 @@
+// Kernels of the batched construction: many independent texts, each built
+// exactly like a single text (same split passes), with the per-text tables
+// that a single build derives on the host computed on the device instead, so
+// that a whole batch is one CUDA graph without host round trips.
+#include "kernels.cuh"
+
+namespace pwmgpu {
+
+namespace {
+
+constexpr int kBatchThreads = 256;
+
+__device__ __forceinline__ uint32_t rev_bits_dev(uint32_t v, uint32_t bits) {
+  return bits == 0 ? 0u : (__brev(v) >> (32 - bits));
+}
+
+// Leaf histogram of one chunk of one text (2^L <= 4096 bins in shared memory).
+template <typename T>
+__global__ void __launch_bounds__(kBatchThreads) batch_hist_kernel(const T* __restrict__ texts,
+                                                                   const BatchChunk* __restrict__ chunks,
+                                                                   const BatchText* __restrict__ info,
+                                                                   unsigned long long* hist, uint32_t* status) {
+  __shared__ uint32_t h[4096];
+  const BatchChunk c = chunks[blockIdx.x];
+  const BatchText t = info[c.text];
+  const uint32_t bins = 1u << t.levels;
+  for (uint32_t i = threadIdx.x; i < bins; i += kBatchThreads) h[i] = 0;
+  __syncthreads();
+  bool bad = false;
+  const T* p = texts + t.offset + c.start;
+  for (uint64_t i = threadIdx.x; i < c.len; i += kBatchThreads) {
+    const uint64_t s = uint64_t(p[i]);
+    if (s >= bins) { bad = true; continue; }
+    atomicAdd(&h[s], 1u);
+  }
+  if (bad) atomicOr(status, kErrSymbol);
+  __syncthreads();
+  unsigned long long* out = hist + t.hist_off;
+  for (uint32_t i = threadIdx.x; i < bins; i += kBatchThreads)
+    if (h[i]) atomicAdd(&out[i], (unsigned long long)h[i]);
+}
+
+// Per-text tables from the leaf histogram (one CTA per text, L <= 12):
+// matrix zero counts, the run starts of every split pass (passes of at most
+// kmax levels from level 0, the same plan as a single build) and the
+// tree's dense group segments of levels 1..L-1 (tree start, matrix start).
+__global__ void __launch_bounds__(kBatchThreads) batch_tables_kernel(const unsigned long long* __restrict__ hist,
+                                                                     const BatchText* __restrict__ info, int kmax,
+                                                                     uint64_t* zeros, uint64_t* starts,
+                                                                     uint64_t* segs) {
+  extern __shared__ unsigned long long cnt[];  // heap layout: node (m, p) at (1 << m) + p, m in [0, L]
+  const BatchText t = info[blockIdx.x];
+  const uint32_t L = t.levels;
+  const unsigned long long* h = hist + t.hist_off;
+  for (uint32_t p = threadIdx.x; p < (1u << L); p += kBatchThreads) cnt[(1u << L) + p] = h[p];
+  __syncthreads();
+  for (int m = int(L) - 1; m >= 0; --m) {
+    for (uint32_t p = threadIdx.x; p < (1u << m); p += kBatchThreads)
+      cnt[(1u << m) + p] = cnt[(2u << m) + 2 * p] + cnt[(2u << m) + 2 * p + 1];
+    __syncthreads();
+  }
+  // zeros[m]: symbols whose bit for level m is 0 = even (m+1)-prefixes
+  for (uint32_t m = threadIdx.x; m < L; m += kBatchThreads) {
+    unsigned long long z = 0;
+    for (uint32_t p = 0; p < (1u << (m + 1)); p += 2) z += cnt[(2u << m) + p];
+    zeros[t.zeros_off + m] = z;
+  }
+  // run starts: pass (l, K), level l+j, value v of key_j (bit l least
+  // significant) counts the (l+j)-prefixes q with rev_j(q mod 2^j) == v
+  {
+    uint32_t l = 0;
+    uint64_t off = t.starts_off;
+    for (uint32_t pass = 0; l < L; ++pass) {
+      const int K = int(min(uint32_t(kmax), L - l));
+      for (int j = 1 + int(threadIdx.x); j <= K; j += kBatchThreads) {
+        const uint32_t lev = l + uint32_t(j);
+        uint64_t* st = starts + off + ((1u << j) - 2);
+        if (lev <= L) {
+          unsigned long long run = 0;
+          for (uint32_t v = 0; v < (1u << j); ++v) {
+            unsigned long long c = 0;
+            const uint32_t q0 = rev_bits_dev(v, uint32_t(j));
+            for (uint32_t q = q0; q < (1u << lev); q += (1u << j)) c += cnt[(1u << lev) + q];
+            st[v] = run;
+            run += c;
+          }
+        } else {
+          for (uint32_t v = 0; v < (1u << j); ++v) st[v] = 0;
+        }
+      }
+      off += (2u << K) - 2;
+      l += uint32_t(K);
+    }
+  }
+  // tree segments, level m: groups in natural prefix order; the matrix holds
+  // them in bit-reversed order
+  for (uint32_t m = 1 + threadIdx.x; m < L; m += kBatchThreads) {
+    uint64_t* tree_start = segs + t.segs_off + 2 * ((1u << m) - 2);
+    uint64_t* matrix_start = tree_start + (1u << m);
+    unsigned long long run = 0;
+    for (uint32_t p = 0; p < (1u << m); ++p) {
+      tree_start[p] = run;
+      run += cnt[(1u << m) + p];
+    }
+    run = 0;
+    for (uint32_t r = 0; r < (1u << m); ++r) {
+      const uint32_t p = rev_bits_dev(r, m);
+      matrix_start[p] = run;
+      run += cnt[(1u << m) + p];
+    }
+  }
+}
+
+__device__ __forceinline__ uint64_t bits_at_dev(const uint64_t* level, uint64_t src, uint32_t take) {
+  const uint64_t w = src >> 6;
+  const uint32_t sh = uint32_t(src & 63);
+  uint64_t v = level[w] << sh;
+  if (sh != 0 && sh + take > 64) v |= level[w + 1] >> (64 - sh);
+  return take == 64 ? v : (v & ~(~0ull >> take));
+}
+
+// Tree level m of one text from its matrix level, one thread per word.
+__global__ void __launch_bounds__(kBatchThreads) batch_regroup_kernel(const BatchRegroup* __restrict__ items,
+                                                                      uint32_t* status) {
+  const BatchRegroup it = items[blockIdx.x];
+  const uint64_t nwords = (it.nbits + 63) >> 6;
+  const uint64_t nseg = it.nseg;
+  for (uint64_t w = it.word_begin + threadIdx.x; w < it.word_end && w < nwords; w += kBatchThreads) {
+    const uint64_t p0 = w << 6, end = min(p0 + 64, it.nbits);
+    uint64_t pos = p0, acc = 0;
+    while (pos < end) {
+      uint64_t lo = 0, hi = nseg;
+      while (hi - lo > 1) {
+        const uint64_t mid = (lo + hi) >> 1;
+        if (it.seg_tree[mid] <= pos) lo = mid; else hi = mid;
+      }
+      const uint64_t seg_end = lo + 1 < nseg ? it.seg_tree[lo + 1] : it.nbits;
+      const uint64_t stop = min(end, seg_end);
+      const uint32_t take = uint32_t(stop - pos);
+      const uint64_t src = it.seg_matrix[lo] + (pos - it.seg_tree[lo]);
+      if (take == 0 || src + take > it.nbits) {
+        atomicOr(status, kErrBounds);
+        break;
+      }
+      acc |= bits_at_dev(it.matrix, src, take) >> (pos - p0);
+      pos = stop;
+    }
+    it.tree[w] = acc;
+  }
+}
+
+}  // namespace
+
+void launch_batch_hist(const void* texts, uint32_t width, const BatchChunk* chunks, uint32_t nchunks,
+                       const BatchText* info, unsigned long long* hist, uint32_t* status, cudaStream_t s,
+                       uint64_t* launches) {
+  if (nchunks == 0) return;
+  if (width == 1)
+    batch_hist_kernel<<<nchunks, kBatchThreads, 0, s>>>(static_cast<const uint8_t*>(texts), chunks, info, hist, status);
+  else if (width == 2)
+    batch_hist_kernel<<<nchunks, kBatchThreads, 0, s>>>(static_cast<const uint16_t*>(texts), chunks, info, hist, status);
+  else
+    batch_hist_kernel<<<nchunks, kBatchThreads, 0, s>>>(static_cast<const uint32_t*>(texts), chunks, info, hist, status);
+  ++*launches;
+}
+
+void launch_batch_tables(const unsigned long long* hist, const BatchText* info, uint32_t ntexts, uint32_t max_levels,
+                         int kmax, uint64_t* zeros, uint64_t* starts, uint64_t* segs, cudaStream_t s,
+                         uint64_t* launches) {
+  if (ntexts == 0) return;
+  const size_t smem = (size_t(2) << max_levels) * 8;
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(batch_tables_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(8 << 13));
+    configured = true;
+  }
+  batch_tables_kernel<<<ntexts, kBatchThreads, smem, s>>>(hist, info, kmax, zeros, starts, segs);
+  ++*launches;
+}
+
+void launch_batch_regroup(const BatchRegroup* items, uint32_t nitems, uint32_t* status, cudaStream_t s,
+                          uint64_t* launches) {
+  if (nitems == 0) return;
+  batch_regroup_kernel<<<nitems, kBatchThreads, 0, s>>>(items, status);
+  ++*launches;
+}
+
+}  // namespace pwmgpu

@@ -21,6 +21,11 @@ uint32_t split_tile_elems(uint32_t key_bytes);
 size_t split_smem_bytes(uint32_t key_bytes, int K);
 void launch_split_pass(uint32_t key_bytes, bool huffman, int K, const SplitArgs& a, uint32_t L, cudaStream_t s,
                        uint64_t* launches);
+// Plain keys of a batch of texts: args[t] describes text t's pass, its tiles
+// are [tile_base[t], tile_base[t+1]) of the launch; counter zeroed.
+void launch_split_pass_batched(uint32_t key_bytes, int K, const SplitArgs* args, const uint32_t* tile_base,
+                               uint32_t ntexts, uint32_t tiles, uint32_t* counter, cudaStream_t s,
+                               uint64_t* launches);
 
 // ---- wavelet tree from the matrix --------------------------------------------
 // Level `m` of the tree: the matrix level with its prefix groups reordered.
@@ -79,6 +84,41 @@ void launch_queries(const QueryStructure& q, int op, const uint64_t* a, const ui
 uint64_t noalloc_rank_select_max_words();
 cudaError_t noalloc_rank_select_build(const uint64_t* words, uint64_t nwords, uint64_t* l0, uint32_t* l12,
                                       uint32_t* s0, uint32_t* s1, unsigned long long* counts, cudaStream_t stream);
+
+// ---- batches -------------------------------------------------------------------------
+struct BatchText {
+  uint64_t offset;      // first symbol of the text in the concatenated batch
+  uint64_t n;           // symbols
+  uint32_t levels;
+  uint32_t pad;
+  uint64_t hist_off;    // 2^levels leaf counts
+  uint64_t zeros_off;   // levels matrix zero counts
+  uint64_t starts_off;  // run starts of all passes
+  uint64_t segs_off;    // tree segments of levels 1..levels-1 (2*(2^levels - 2))
+};
+struct BatchChunk {
+  uint32_t text;
+  uint32_t pad;
+  uint64_t start;  // symbol offset inside the text
+  uint64_t len;
+};
+struct BatchRegroup {
+  const uint64_t* matrix;
+  uint64_t* tree;
+  uint64_t nbits;
+  const uint64_t* seg_tree;
+  const uint64_t* seg_matrix;
+  uint64_t nseg;
+  uint64_t word_begin, word_end;
+};
+void launch_batch_hist(const void* texts, uint32_t width, const BatchChunk* chunks, uint32_t nchunks,
+                       const BatchText* info, unsigned long long* hist, uint32_t* status, cudaStream_t s,
+                       uint64_t* launches);
+void launch_batch_tables(const unsigned long long* hist, const BatchText* info, uint32_t ntexts, uint32_t max_levels,
+                         int kmax, uint64_t* zeros, uint64_t* starts, uint64_t* segs, cudaStream_t s,
+                         uint64_t* launches);
+void launch_batch_regroup(const BatchRegroup* items, uint32_t nitems, uint32_t* status, cudaStream_t s,
+                          uint64_t* launches);
 
 // ---- generators -------------------------------------------------------------------
 void launch_generate(int dist, uint64_t seed, uint64_t param, uint64_t n, uint32_t width, void* out,

@@ -31,6 +31,23 @@ void launch_one(const SplitArgs& a, uint32_t L, cudaStream_t s) {
   kern<<<a.tiles, kSplitThreads, smem, s>>>(a, tr);
 }
 
+template <int KB, bool HUFF, int K>
+void launch_batched_one(const SplitArgs* args, const uint32_t* tile_base, uint32_t ntexts, uint32_t tiles,
+                        uint32_t* counter, cudaStream_t s) {
+  using G = SplitGeometry<KB>;
+  using Key = typename G::Key;
+  using Tr = typename std::conditional<HUFF, HuffKeys<Key>, PlainKeys<Key>>::type;
+  using P = SplitPass<Key, Tr, K, kSplitThreads, G::ITEMS>;
+  auto kern = split_pass_batched_kernel<Key, Tr, K, kSplitThreads, G::ITEMS>;
+  static bool configured = false;
+  const size_t smem = P::smem_bytes();
+  if (!configured) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    configured = true;
+  }
+  kern<<<tiles, kSplitThreads, smem, s>>>(args, tile_base, ntexts, counter);
+}
+
 template <int KB, bool HUFF>
 void launch_k(int K, const SplitArgs& a, uint32_t L, cudaStream_t s) {
   switch (K) {
@@ -42,6 +59,26 @@ void launch_k(int K, const SplitArgs& a, uint32_t L, cudaStream_t s) {
 }
 
 }  // namespace
+
+void launch_split_pass_batched(uint32_t key_bytes, int K, const SplitArgs* args, const uint32_t* tile_base,
+                               uint32_t ntexts, uint32_t tiles, uint32_t* counter, cudaStream_t s,
+                               uint64_t* launches) {
+  if (tiles == 0) return;
+#define PWMGPU_BK(KB)                                                                              \
+  switch (K) {                                                                                     \
+    case 1: launch_batched_one<KB, false, 1>(args, tile_base, ntexts, tiles, counter, s); break;   \
+    case 2: launch_batched_one<KB, false, 2>(args, tile_base, ntexts, tiles, counter, s); break;   \
+    case 3: launch_batched_one<KB, false, 3>(args, tile_base, ntexts, tiles, counter, s); break;   \
+    default: launch_batched_one<KB, false, 4>(args, tile_base, ntexts, tiles, counter, s); break;  \
+  }
+  switch (key_bytes) {
+    case 1: PWMGPU_BK(1) break;
+    case 2: PWMGPU_BK(2) break;
+    default: PWMGPU_BK(4) break;
+  }
+#undef PWMGPU_BK
+  ++*launches;
+}
 
 uint32_t split_tile_elems(uint32_t key_bytes) {
   switch (key_bytes) {

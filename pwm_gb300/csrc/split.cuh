@@ -74,6 +74,7 @@ struct SplitArgs {
   uint64_t level_size[kMaxPassLevels + 1];  // elements of levels l..l+K (K: S_out)
   uint32_t* status;
   uint32_t tiles;
+  uint32_t L;                // levels of the text (plain keys)
 };
 
 template <typename KeyT, typename Traits, int K, int THREADS, int ITEMS>
@@ -223,7 +224,46 @@ __device__ __forceinline__ void copy_run_bytes(unsigned char* dst, const unsigne
 }
 
 template <typename KeyT, typename Traits, int K, int THREADS, int ITEMS>
+__device__ __forceinline__ void split_pass_tile(const SplitArgs& a, const Traits& tr, uint32_t tile);
+
+// One text: tiles are taken in launch order from a.tile_counter.
+template <typename KeyT, typename Traits, int K, int THREADS, int ITEMS>
 __global__ void __launch_bounds__(THREADS, K <= 2 ? 4 : 3) split_pass_kernel(SplitArgs a, Traits tr) {
+  __shared__ uint32_t s_tile;
+  if (threadIdx.x == 0) s_tile = atomicAdd(a.tile_counter, 1u);
+  __syncthreads();
+  split_pass_tile<KeyT, Traits, K, THREADS, ITEMS>(a, tr, s_tile);
+}
+
+// A batch of texts: global tile g belongs to the text whose range
+// [tile_base[t], tile_base[t+1]) holds it; tiles are taken in launch order
+// from one counter, so the predecessors of a tile inside its text were taken
+// earlier (the look-back waits end).
+template <typename KeyT, typename Traits, int K, int THREADS, int ITEMS>
+__global__ void __launch_bounds__(THREADS, K <= 2 ? 4 : 3)
+    split_pass_batched_kernel(const SplitArgs* __restrict__ args, const uint32_t* __restrict__ tile_base,
+                              uint32_t ntexts, uint32_t* tile_counter) {
+  __shared__ uint32_t s_tile, s_text;
+  __shared__ SplitArgs s_args;
+  if (threadIdx.x == 0) {
+    const uint32_t g = atomicAdd(tile_counter, 1u);
+    uint32_t lo = 0, hi = ntexts;  // last text with tile_base <= g
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (tile_base[mid] <= g) lo = mid; else hi = mid;
+    }
+    s_text = lo;
+    s_tile = g - tile_base[lo];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) s_args = args[s_text];
+  __syncthreads();
+  const Traits tr{s_args.L};
+  split_pass_tile<KeyT, Traits, K, THREADS, ITEMS>(s_args, tr, s_tile);
+}
+
+template <typename KeyT, typename Traits, int K, int THREADS, int ITEMS>
+__device__ __forceinline__ void split_pass_tile(const SplitArgs& a, const Traits& tr, const uint32_t tile) {
   using P = SplitPass<KeyT, Traits, K, THREADS, ITEMS>;
   constexpr int T = P::T, C = P::C, WARPS = P::WARPS, SW = P::SW, KPL = P::KPL, ROUND = P::ROUND;
   constexpr int RUNS = P::RUNS, PERW = P::PERW, MASKW = P::MASKW;
@@ -235,7 +275,6 @@ __global__ void __launch_bounds__(THREADS, K <= 2 ? 4 : 3) split_pass_kernel(Spl
   uint32_t* sbits_all = reinterpret_cast<uint32_t*>(bufB + T);
   uint32_t* masks_all = sbits_all + (K > 1 ? K - 1 : 1) * WARPS * SW;
 
-  __shared__ uint32_t s_tile;
   __shared__ uint32_t runz[WARPS][K + 1][RUNS], runo[WARPS][K + 1][RUNS];  // per warp, per split
   __shared__ uint32_t cntw[WARPS][C];          // run sizes per warp
   __shared__ uint32_t cnt[C];                  // run sizes of the tile
@@ -246,13 +285,11 @@ __global__ void __launch_bounds__(THREADS, K <= 2 ? 4 : 3) split_pass_kernel(Spl
   const bool has_out = a.out != nullptr;
   const int D = has_out ? K : K - 1;  // splits of this pass
 
-  if (tid == 0) s_tile = atomicAdd(a.tile_counter, 1u);
   for (int i = tid; i < WARPS * (K + 1) * RUNS; i += THREADS) {
     (&runz[0][0][0])[i] = 0;
     (&runo[0][0][0])[i] = 0;
   }
   __syncthreads();
-  const uint32_t tile = s_tile;
   const uint64_t tile_start = uint64_t(tile) * T;
   const uint64_t remain = a.m - tile_start;
   const uint32_t n = remain < uint64_t(T) ? uint32_t(remain) : uint32_t(T);
