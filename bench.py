@@ -13,6 +13,7 @@ Ranks run independent replicas (weak scaling, no collective on the data path).
 restatement of wx_ppc + rank/select) on the host cores instead.
 """
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -151,6 +152,67 @@ def cpu_baseline(n_sample, steps=3):
             "seconds_per_step": t}
 
 
+def batched_vs_per_text(torch, pg, ctx, count=4096, seed=1, reps=3):
+    """4096 uneven uint8 texts (log-normal lengths, 85% DNA-like with 3
+    levels, 15% Zipf bytes with 8 levels): matrix + tree of every text, one
+    CUDA-graph launch per batch (pass width chosen by timing 1..4 levels per
+    pass) against a loop of per-text builds through the same library."""
+    import numpy as np
+    texts, offs, levels = pg.generate_batch(seed, count)
+    total = int(offs[-1])
+    d = torch.from_numpy(texts).cuda()
+    stream = torch.cuda.current_stream()
+    tune = {}
+    b = pg.Batch(offs, levels, word_width=1, tree=True, levels_per_pass=2, context=ctx)
+    for k in (1, 2, 3, 4):
+        b.set_levels_per_pass(k)
+        b.build(d.data_ptr())  # records the graph for this width
+        b.check()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        b.build(d.data_ptr())
+        e0.record(stream)
+        for _ in range(reps):
+            b.build(d.data_ptr())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        tune[k] = e0.elapsed_time(e1) / reps
+    best = min(tune, key=tune.get)
+    b.set_levels_per_pass(best)
+    b.build(d.data_ptr())
+    b.check()
+    batched_ms = tune[best]
+    # per-text builds: one device structure per text, built one after the other
+    per = []
+    for i in range(count):
+        n = int(offs[i + 1] - offs[i])
+        per.append(pg.DeviceStructure(n, 1, int(levels[i]), matrix=True, tree=True, context=ctx))
+    base = d.data_ptr()
+    for i in range(min(count, 64)):
+        per[i].build(base + int(offs[i]))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(count):
+        per[i].build(base + int(offs[i]))
+    torch.cuda.synchronize()
+    per_ms = (time.perf_counter() - t0) * 1e3
+    # spot check: batch == per-text for a few texts
+    same = True
+    for i in range(0, count, max(1, count // 16)):
+        a, c = b.download(i, 0), per[i].download(0)
+        same &= all(np.array_equal(np.asarray(a.bvs()[l]), np.asarray(c.bvs()[l])) for l in range(int(levels[i])))
+        same &= a.zeros() == c.zeros()
+        a, c = b.download(i, 1), per[i].download(1)
+        same &= all(np.array_equal(np.asarray(a.bvs()[l]), np.asarray(c.bvs()[l])) for l in range(int(levels[i])))
+    for x in per:
+        x.free()
+    b.free()
+    return {"texts": count, "symbols": total, "levels_mix": {"3": int((levels == 3).sum()), "8": int((levels == 8).sum())},
+            "batched_gbs": total / (batched_ms / 1e3) / 1e9, "batched_ms": batched_ms,
+            "per_text_gbs": total / (per_ms / 1e3) / 1e9, "per_text_ms": per_ms,
+            "speedup": per_ms / batched_ms, "levels_per_pass_ms": tune, "levels_per_pass": best,
+            "identical_to_per_text": bool(same), "structures": ["matrix", "tree"]}
+
+
 def run_reference(args, rank):
     if rank != 0:
         return 0
@@ -193,6 +255,7 @@ def main():
     ap.add_argument("--pass-levels", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -216,7 +279,10 @@ def main():
         if dist:
             dist.barrier()
 
-    stream = torch.cuda.current_stream()
+    # a dedicated stream, current for torch and given to the library, so that
+    # CUDA events recorded on it bracket the library's launches
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx = pg.Context(device=local, stream=ctypes_stream(stream))
     if args.pass_levels:
         ctx.set_pass_levels(args.pass_levels)
@@ -254,7 +320,7 @@ def main():
     clocks = sampler.stop()
     ds.check()
     launches = ctx.launches - launches0
-    buf = __import__("ctypes").create_string_buffer(1 << 16)
+    buf = ctypes.create_string_buffer(1 << 16)
     ctx.check(ctx.lib.pwmgpu_ctx_profile_read(ctx.h, buf, len(buf)))
     ctx.lib.pwmgpu_ctx_profile(ctx.h, 0)
     prof = parse_profile(buf.value.decode())
@@ -273,12 +339,13 @@ def main():
     zeros = np.zeros(LEVELS, dtype=np.uint64)
     zp = zeros.ctypes.data_as(pg._lib.u64p)
 
+    wm_ptr = ctypes.cast(out_wm.data_ptr(), pg._lib.u64p)
+    wt_ptr = ctypes.cast(out_wt.data_ptr(), pg._lib.u64p)
+
     def e2e_step():
         ctx.check(ctx.lib.pwmgpu_wx_build_host(ctx.h, ds.h, host_text.data_ptr()))
-        ctx.check(ctx.lib.pwmgpu_wx_download(ctx.h, ds.h, 0, pg._lib.u64p(pg._lib.u64(0)) if False else
-                                             __import__("ctypes").cast(out_wm.data_ptr(), pg._lib.u64p), zp))
-        ctx.check(ctx.lib.pwmgpu_wx_download(ctx.h, ds.h, 1, __import__("ctypes").cast(out_wt.data_ptr(),
-                                                                                       pg._lib.u64p), None))
+        ctx.check(ctx.lib.pwmgpu_wx_download(ctx.h, ds.h, 0, wm_ptr, zp))
+        ctx.check(ctx.lib.pwmgpu_wx_download(ctx.h, ds.h, 1, wt_ptr, None))
 
     e2e_step()
     barrier()
@@ -319,6 +386,8 @@ def main():
                 "clocks": clocks}
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(CPU_SAMPLE)
+        if world == 1 and not args.no_batch:
+            line["batched"] = batched_vs_per_text(torch, pg, ctx)
         print(json.dumps(line))
     ds.free()
     if dist:
