@@ -89,9 +89,19 @@ PWMGPU_API uint64_t pwmgpu_ctx_launch_count(const pwmgpu_ctx* ctx);
  * algorithmic_bytes", then clears the record. */
 PWMGPU_API pwmgpu_status pwmgpu_ctx_profile(pwmgpu_ctx* ctx, int enable);
 PWMGPU_API pwmgpu_status pwmgpu_ctx_profile_read(pwmgpu_ctx* ctx, char* buf, uint64_t cap);
-/* Tuning: levels fused into one split pass (1..4, default 4).  A pass reads
- * its input sequence once and writes the bits of that many levels. */
+/* Tuning: levels fused into one split pass (1..4).  A pass reads its input
+ * sequence once and writes the bits of that many levels.  Sets the width of
+ * both engines (defaults: 4 for the tile engine, 2 for the warp-pass engine). */
 PWMGPU_API pwmgpu_status pwmgpu_ctx_set_pass_levels(pwmgpu_ctx* ctx, int levels_per_pass);
+
+/* Split engines of plain builds.  TILE (default): CTA-wide splits of whole
+ * tiles that write matrix and tree levels together (levels <= 20).  WARP:
+ * warp-autonomous split passes that write the matrix, with the tree levels
+ * regrouped from it (every plain build; Huffman builds and batches always use
+ * it).  Both give identical structures. */
+#define PWMGPU_ENGINE_TILE 0
+#define PWMGPU_ENGINE_WARP 1
+PWMGPU_API pwmgpu_status pwmgpu_ctx_set_engine(pwmgpu_ctx* ctx, int engine);
 
 /* ---------------------------------------------------------------------- */
 /* Drop-in construction (host text in, host bit vectors out)               */

@@ -73,6 +73,10 @@ class Context:
     def set_pass_levels(self, k):
         self.check(self.lib.pwmgpu_ctx_set_pass_levels(self.h, int(k)))
 
+    def set_engine(self, engine):
+        """ENGINE_TILE (default) or ENGINE_WARP for plain builds."""
+        self.check(self.lib.pwmgpu_ctx_set_engine(self.h, int(engine)))
+
     def close(self):
         if getattr(self, "h", None):
             self.lib.pwmgpu_ctx_destroy(self.h)
@@ -84,6 +88,9 @@ class Context:
         except Exception:
             pass
 
+
+ENGINE_TILE = 0
+ENGINE_WARP = 1
 
 _default = None
 

@@ -39,6 +39,7 @@ SIGNATURES = {
     "pwmgpu_ctx_sync": (i32, [vp]),
     "pwmgpu_ctx_launch_count": (u64, [vp]),
     "pwmgpu_ctx_set_pass_levels": (i32, [vp, i32]),
+    "pwmgpu_ctx_set_engine": (i32, [vp, i32]),
     "pwmgpu_ctx_profile": (i32, [vp, i32]),
     "pwmgpu_ctx_profile_read": (i32, [vp, ctypes.c_char_p, u64]),
     "pwmgpu_wx_build_host": (i32, [vp, vp, vp]),

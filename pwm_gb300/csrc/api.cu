@@ -24,7 +24,8 @@ namespace {
 
 constexpr uint32_t kMaxLevels = 64;
 constexpr uint32_t kMaxPlainLevels = 24;  // the leaf histogram has 2^L bins
-constexpr int kDefaultPassLevels = 2;  // fastest measured width for 8-bit text
+constexpr int kDefaultPassLevels = 2;  // fastest measured width of the warp-pass engine for 8-bit text
+constexpr int kDefaultTileLevels = 4;  // levels per segmented tile pass
 
 struct Fail {
   pwmgpu_status st;
@@ -65,6 +66,8 @@ struct pwmgpu_ctx {
   uint32_t* d_status = nullptr;
   std::map<std::string, DevBuf> scratch;
   int pass_levels = kDefaultPassLevels;
+  int tile_levels = kDefaultTileLevels;
+  int engine = PWMGPU_ENGINE_TILE;
   pwmgpu_wx* compute_cache = nullptr;  // reused by pwmgpu_compute for equal shapes
   // CUDA-event timing of every launch group while profiling is on
   bool profiling = false;
@@ -397,6 +400,112 @@ void run_passes(pwmgpu_ctx* ctx, const void* keys, uint32_t key_bytes, uint32_t 
   CUDA_TRY(cudaStreamSynchronize(s));
 }
 
+// ---------------------------------------------------------------------------
+// Plain builds through the segmented tile passes: every pass writes its
+// matrix levels, and its tree levels when its segments are prefix groups;
+// the remaining tree levels come from the regroup.
+// ---------------------------------------------------------------------------
+void run_tile_passes(pwmgpu_ctx* ctx, const void* d_text, uint32_t width, uint32_t L,
+                     const std::vector<uint64_t>& hist, const LevelTables& tabs, Structure& wm, Structure* wt) {
+  cudaStream_t s = ctx->stream;
+  const uint64_t n = tabs.level_bits.empty() ? 0 : tabs.level_bits[0];
+  const uint32_t T = tile_pass_elems(width);
+  std::vector<uint32_t> regroup;
+  const auto passes = plan_tile_passes(hist, L, std::min(ctx->tile_levels, kTileMaxLevels), T, wt != nullptr, &regroup);
+
+  // one upload: per pass its segments, its level descriptor and its tables
+  std::vector<unsigned char> blob;
+  auto align16 = [&]() { blob.resize((blob.size() + 15) & ~size_t(15)); };
+  struct Offs { size_t segs, text, table; };
+  std::vector<Offs> offs(passes.size());
+  const uint64_t stride = L > 1 ? wm.offs[1] - wm.offs[0] : padded_words(n);
+  for (size_t pi = 0; pi < passes.size(); ++pi) {
+    const auto& p = passes[pi];
+    align16();
+    offs[pi].segs = blob.size();
+    for (const auto& h : p.segs) {
+      TileSeg d{h.in_begin, h.m, h.table, h.tile0, h.text};
+      const auto* b = reinterpret_cast<const unsigned char*>(&d);
+      blob.insert(blob.end(), b, b + sizeof d);
+    }
+    align16();
+    offs[pi].text = blob.size();
+    TileText tx{};
+    tx.wm = wm.d_words + wm.offs[p.level];
+    tx.wt = (wt && p.segmented) ? wt->d_words + wt->offs[p.level] : nullptr;
+    tx.stride = stride;
+    tx.nbits = n;
+    tx.shift = L - 1 - p.level;
+    const auto* b = reinterpret_cast<const unsigned char*>(&tx);
+    blob.insert(blob.end(), b, b + sizeof tx);
+    align16();
+    offs[pi].table = blob.size();
+    const auto* tb = reinterpret_cast<const unsigned char*>(p.table.data());
+    blob.insert(blob.end(), tb, tb + p.table.size() * 8);
+  }
+  auto* d_blob = static_cast<unsigned char*>(ctx->grow("tile_plan", std::max<size_t>(blob.size(), 16)));
+  CUDA_TRY(cudaMemcpyAsync(d_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice, s));
+
+  // runs are OR-ed into their edge chunks: zero the levels
+  CUDA_TRY(cudaMemsetAsync(wm.d_words, 0, wm.total_words * 8, s));
+  if (wt) CUDA_TRY(cudaMemsetAsync(wt->d_words, 0, wt->total_words * 8, s));
+
+  void* ping = ctx->grow("keys_a", std::max<uint64_t>(n, 1) * width);
+  void* pong = ctx->grow("keys_b", std::max<uint64_t>(n, 1) * width);
+  const void* in = d_text;
+  for (size_t pi = 0; pi < passes.size(); ++pi) {
+    const auto& p = passes[pi];
+    const int D = p.out ? p.K : p.K - 1;
+    const uint64_t nlb = uint64_t(1) << D;
+    const uint64_t lb_bytes = uint64_t(std::max<uint32_t>(p.tiles, 1)) * nlb * 8;
+    auto* lb = static_cast<unsigned long long*>(ctx->grow("lookback", lb_bytes + 64));
+    CUDA_TRY(cudaMemsetAsync(lb, 0, lb_bytes + 64, s));
+    TileArgs a{};
+    a.in = in;
+    a.out = p.out ? (in == ping ? pong : ping) : nullptr;
+    a.out_size = p.out ? n : 0;
+    a.segs = reinterpret_cast<const TileSeg*>(d_blob + offs[pi].segs);
+    a.texts = reinterpret_cast<const TileText*>(d_blob + offs[pi].text);
+    a.tables = reinterpret_cast<const uint64_t*>(d_blob + offs[pi].table);
+    a.lookback = lb;
+    a.tile_counter = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(lb) + lb_bytes);
+    a.status = ctx->d_status;
+    a.nsegs = uint32_t(p.segs.size());
+    a.tiles = p.tiles;
+    {
+      const uint64_t structs = (wt && p.segmented) ? 2 : 1;
+      ProfScope ps(ctx, "split_pass", structs * uint64_t(p.K) * (n * width + words_for(n) * 8));
+      launch_tile_pass(width, p.K, p.out, a, s, &ctx->launches);
+    }
+    CUDA_TRY(cudaGetLastError());
+    if (p.out) in = a.out;
+  }
+
+  if (wt && !regroup.empty()) {
+    size_t seg_words = 0;
+    for (uint32_t m : regroup) seg_words += 2 * tabs.seg_tree[m].size();
+    std::vector<uint64_t> segs;
+    segs.reserve(seg_words);
+    for (uint32_t m : regroup) {
+      segs.insert(segs.end(), tabs.seg_tree[m].begin(), tabs.seg_tree[m].end());
+      segs.insert(segs.end(), tabs.seg_matrix[m].begin(), tabs.seg_matrix[m].end());
+    }
+    uint64_t* d_segs = static_cast<uint64_t*>(ctx->grow("segs", std::max<size_t>(seg_words, 1) * 8));
+    CUDA_TRY(cudaMemcpyAsync(d_segs, segs.data(), seg_words * 8, cudaMemcpyHostToDevice, s));
+    size_t off = 0;
+    for (uint32_t m : regroup) {
+      const uint64_t ns = tabs.seg_tree[m].size();
+      ProfScope ps(ctx, "regroup", 2 * words_for(wm.bits[m]) * 8);
+      launch_regroup(wm.d_words + wm.offs[m], wt->d_words + wt->offs[m], wm.bits[m], d_segs + off, d_segs + off + ns,
+                     ns, ctx->d_status, s, &ctx->launches);
+      off += 2 * ns;
+    }
+    CUDA_TRY(cudaGetLastError());
+  }
+  // the host plan must outlive the async copies
+  CUDA_TRY(cudaStreamSynchronize(s));
+}
+
 void validate_plain(uint64_t n, uint32_t width, uint32_t levels) {
   if (!valid_width(width)) throw Fail{PWMGPU_ERR_ARG, "word_width must be 1, 2 or 4"};
   if (levels == 0 || levels > kMaxPlainLevels)
@@ -427,7 +536,10 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text) {
   const LevelTables tabs = build_tables_plain(hist, L, plan, want_tree);
   wx->wm.zeros = tabs.zeros;
   CUDA_TRY(cudaMemcpyAsync(wx->wm.d_zeros, wx->wm.zeros.data(), L * 8, cudaMemcpyHostToDevice, s));
-  run_passes(ctx, d_text, wx->width, wx->width, false, L, plan, tabs, wx->wm, want_tree ? &wx->wt : nullptr);
+  if (ctx->engine == PWMGPU_ENGINE_TILE && L <= kTilePlanMaxLevels)
+    run_tile_passes(ctx, d_text, wx->width, L, hist, tabs, wx->wm, want_tree ? &wx->wt : nullptr);
+  else
+    run_passes(ctx, d_text, wx->width, wx->width, false, L, plan, tabs, wx->wm, want_tree ? &wx->wt : nullptr);
   if (wx->wm.rs && !wx->wm_internal) build_rank_select(ctx, wx->wm);
   if (want_tree && wx->wt.rs) build_rank_select(ctx, wx->wt);
   CUDA_TRY(cudaGetLastError());
@@ -925,8 +1037,15 @@ pwmgpu_status pwmgpu_ctx_sync(pwmgpu_ctx* ctx) {
 uint64_t pwmgpu_ctx_launch_count(const pwmgpu_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
 pwmgpu_status pwmgpu_ctx_set_pass_levels(pwmgpu_ctx* ctx, int k) {
-  if (!ctx || k < 1 || k > kMaxPassLevels) return PWMGPU_ERR_ARG;
+  if (!ctx || k < 1 || k > kMaxPassLevels || k > kTileMaxLevels) return PWMGPU_ERR_ARG;
   ctx->pass_levels = k;
+  ctx->tile_levels = k;
+  return PWMGPU_OK;
+}
+
+pwmgpu_status pwmgpu_ctx_set_engine(pwmgpu_ctx* ctx, int engine) {
+  if (!ctx || (engine != PWMGPU_ENGINE_TILE && engine != PWMGPU_ENGINE_WARP)) return PWMGPU_ERR_ARG;
+  ctx->engine = engine;
   return PWMGPU_OK;
 }
 

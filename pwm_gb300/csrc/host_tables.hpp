@@ -10,6 +10,8 @@
 #include <unordered_map>
 #include <vector>
 
+#include "tile.cuh"
+
 namespace pwmgpu {
 
 struct PassPlan {
@@ -107,6 +109,101 @@ inline LevelTables build_tables_plain(const std::vector<uint64_t>& hist, uint32_
     }
   }
   return t;
+}
+
+// ---------------------------------------------------------------------------
+// Segmented tile passes of a plain text (levels <= kTilePlanMaxLevels).
+// Pass (l, K) splits S_l through levels l..l+K-1.  A pass is "segmented" when
+// each l-bit prefix group of S_l is its own segment: every run of those
+// levels then has one start in the matrix and one in the tree, so the pass
+// writes both.  Otherwise (l > 0 and groups too small or too many, or no
+// tree) one segment covers S_l, the pass writes the matrix only and the tree
+// levels of the pass come from the regroup.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kTilePlanMaxLevels = 20;
+
+struct TileSegHost {
+  uint64_t in_begin, m, table;
+  uint32_t tile0, text;
+};
+
+struct TilePassHost {
+  uint32_t level = 0;
+  int K = 0;
+  bool out = false;
+  bool segmented = false;
+  uint32_t tiles = 0;
+  std::vector<TileSegHost> segs;
+  std::vector<uint64_t> table;  // per segment: tile_table_size(K) entries
+};
+
+// hist: 2^L leaf counts.  T: keys per tile.  regroup: tree levels the passes
+// leave to the regroup (empty without a tree).
+inline std::vector<TilePassHost> plan_tile_passes(const std::vector<uint64_t>& hist, uint32_t L, int kmax, uint32_t T,
+                                                  bool want_tree, std::vector<uint32_t>* regroup) {
+  // natural prefix counts per level and their exclusive prefixes, in natural
+  // order (tree) and in key order (matrix: key = reversed prefix)
+  std::vector<std::vector<uint64_t>> cnt(L + 1), pren(L + 1), prek(L + 1);
+  cnt[L] = hist;
+  for (int m = int(L) - 1; m >= 0; --m) {
+    cnt[m].assign(size_t(1) << m, 0);
+    for (size_t p = 0; p < cnt[m].size(); ++p) cnt[m][p] = cnt[m + 1][2 * p] + cnt[m + 1][2 * p + 1];
+  }
+  for (uint32_t m = 0; m <= L; ++m) {
+    const size_t sz = cnt[m].size();
+    pren[m].assign(sz + 1, 0);
+    prek[m].assign(sz + 1, 0);
+    for (size_t p = 0; p < sz; ++p) pren[m][p + 1] = pren[m][p] + cnt[m][p];
+    for (size_t x = 0; x < sz; ++x) prek[m][x + 1] = prek[m][x] + cnt[m][rev_bits_host(x, m)];
+  }
+  const uint64_t n = cnt[0][0];
+  std::vector<TilePassHost> passes;
+  for (const auto& pp : plan_passes(L, kmax)) {
+    TilePassHost ps;
+    ps.level = pp.level;
+    ps.K = pp.K;
+    ps.out = pp.has_out;
+    const uint32_t l = pp.level;
+    const int K = pp.K;
+    const uint64_t groups = uint64_t(1) << l;
+    ps.segmented = want_tree && (l == 0 || (groups <= 65536 && n >= groups * 4 * uint64_t(T)));
+    const int TS = tile_table_size(K);
+    uint32_t tile = 0;
+    auto add_segment = [&](uint64_t begin, uint64_t m, const std::vector<uint64_t>& tab) {
+      if (m == 0) return;
+      ps.segs.push_back({begin, m, uint64_t(ps.table.size()), tile, 0u});
+      ps.table.insert(ps.table.end(), tab.begin(), tab.end());
+      tile += uint32_t((m + T - 1) / T);
+    };
+    std::vector<uint64_t> tab(size_t(TS), 0);
+    if (ps.segmented) {
+      for (uint64_t g = 0; g < groups; ++g) {
+        const uint64_t m = prek[l][g + 1] - prek[l][g];
+        if (m == 0) continue;
+        for (int j = 0; j < K; ++j)
+          for (int v = 0; v < (1 << j); ++v) {
+            const uint64_t x = (uint64_t(v) << l) | g;
+            tab[size_t(tile_wm_entry(j, v))] = prek[l + j][x];
+            tab[size_t(tile_wt_entry(K, j, v))] = pren[l + j][rev_bits_host(x, l + j)];
+          }
+        if (ps.out)
+          for (int v = 0; v < (1 << K); ++v) tab[size_t(tile_out_entry(K, v))] = prek[l + K][(uint64_t(v) << l) | g];
+        add_segment(prek[l][g], m, tab);
+      }
+    } else {
+      for (int j = 0; j < K; ++j)
+        for (int v = 0; v < (1 << j); ++v) tab[size_t(tile_wm_entry(j, v))] = prek[l + j][uint64_t(v) << l];
+      if (ps.out)
+        for (int v = 0; v < (1 << K); ++v) tab[size_t(tile_out_entry(K, v))] = prek[l + K][uint64_t(v) << l];
+      add_segment(0, n, tab);
+      if (want_tree && regroup)
+        for (int j = 0; j < K; ++j)
+          if (l + uint32_t(j) > 0) regroup->push_back(l + uint32_t(j));
+    }
+    ps.tiles = tile;
+    passes.push_back(std::move(ps));
+  }
+  return passes;
 }
 
 // Tables of a Huffman-shaped text from its weighted codes.  want_tree: also

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "split.cuh"
+#include "tile.cuh"
 
 namespace pwmgpu {
 
@@ -26,6 +27,12 @@ void launch_split_pass(uint32_t key_bytes, bool huffman, int K, const SplitArgs&
 void launch_split_pass_batched(uint32_t key_bytes, int K, const SplitArgs* args, const uint32_t* tile_base,
                                uint32_t ntexts, uint32_t tiles, uint32_t* counter, cudaStream_t s,
                                uint64_t* launches);
+
+// ---- segmented tile passes (plain keys, matrix and tree together) ------------
+// Keys of one tile for a key width.
+uint32_t tile_pass_elems(uint32_t key_bytes);
+// One pass of K levels over a.tiles tiles; `out`: the pass writes S_{l+K}.
+void launch_tile_pass(uint32_t key_bytes, int K, bool out, const TileArgs& a, cudaStream_t s, uint64_t* launches);
 
 // ---- wavelet tree from the matrix --------------------------------------------
 // Level `m` of the tree: the matrix level with its prefix groups reordered.

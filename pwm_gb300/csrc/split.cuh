@@ -159,6 +159,7 @@ struct LaneKeys {
     if constexpr (sizeof(KeyT) == 1 && !Traits::kDrops) {
       // four keys per word; the chosen bit of each byte gathered by a multiply
       const uint32_t sh = tr.L - 1 - level;
+      if (sh >= 8) return 0u;  // above the key width every bit is 0
       uint32_t m = 0;
 #pragma unroll
       for (int q = 0; q < 4; ++q) m |= ((((w[q] >> sh) & 0x01010101u) * 0x10204080u) >> 28) << (4 * q);

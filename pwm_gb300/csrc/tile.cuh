@@ -1,0 +1,498 @@
+// Segmented multi-level split pass for plain keys: one CTA sorts one tile of
+// a level sequence through K levels in shared memory and writes the bits of
+// those K levels straight into BOTH the wavelet matrix and the wavelet tree.
+//
+// Background (pwm's naive definition, include/wx_naive.hpp:81-153, and the
+// prefix sorting of include/construction/ps.hpp:13-66 with the bit-reversal
+// rho of include/util/permutation.hpp:16-51): the level-m sequence S_m of a
+// wavelet matrix is the text stably sorted by key_m, the first m symbol bits
+// read with the first bit least significant; level m holds bit m of every
+// element in S_m order.  The tree level m holds the same bits grouped by the
+// natural m-bit prefix instead.  Inside one group (one prefix) both keep text
+// order, so a group is one contiguous run in either structure and only the
+// run starts differ.
+//
+// A pass covers levels l..l+K-1 of one "segment" of S_l: either all of S_l
+// (the first pass, or any pass whose tree levels are left to a regroup), or
+// one l-bit prefix group of S_l, whose elements share key_l and therefore
+// land in every later level at group-specific run starts of both structures.
+// Per tile the kernel
+//   * loads the tile into shared memory (16-byte vectors; misaligned
+//     segments are realigned with funnel shifts);
+//   * runs D = K (or K-1 in the last pass) CTA-wide stable 1-bit splits in
+//     LSD order.  Each thread keeps V 16-byte vectors of keys in registers in
+//     a striped layout (conflict-free 128-bit shared loads), extracts the
+//     split bit of 16 bytes at once, ranks its keys with one packed warp scan
+//     of zero counts per two vectors plus a CTA scan of 8 warp totals, and
+//     stores every key once;
+//   * emits the bits of each level from the same register copy, in that
+//     level's order, into a shared bit stream;
+//   * tracks the tile's run sizes of key_1..key_D from the split counts;
+//   * exchanges the finest run counts (2^D per tile) with a decoupled look-back
+//     that restarts at every segment's first tile;
+//   * writes every run of every level to the matrix and the tree at
+//     table start + look-back prefix, and the runs of S_{l+K} to the next
+//     pass's input.
+#pragma once
+
+#include "common.cuh"
+
+namespace pwmgpu {
+
+constexpr int kTileMaxLevels = 4;
+
+// Table entries of one segment: matrix starts (level j, run v) at
+// (1 << j) - 1 + v, tree starts after them, then the S_out starts (2^K).
+__host__ __device__ constexpr int tile_table_size(int K) { return 2 * ((1 << K) - 1) + (1 << K); }
+__host__ __device__ constexpr int tile_wm_entry(int j, int v) { return (1 << j) - 1 + v; }
+__host__ __device__ constexpr int tile_wt_entry(int K, int j, int v) { return (1 << K) - 1 + (1 << j) - 1 + v; }
+__host__ __device__ constexpr int tile_out_entry(int K, int v) { return 2 * ((1 << K) - 1) + v; }
+
+struct TileSeg {
+  uint64_t in_begin;  // first key of the segment in the pass input
+  uint64_t m;         // keys of the segment
+  uint64_t table;     // offset of the segment's start table
+  uint32_t tile0;     // first global tile of the segment
+  uint32_t text;      // index of the structure pair the segment belongs to
+};
+
+struct TileText {
+  uint64_t* wm;     // matrix level l of the pass; level l+j at wm + j * stride
+  uint64_t* wt;     // tree level l (nullptr: no tree levels from this pass)
+  uint64_t stride;  // words between consecutive levels
+  uint64_t nbits;   // bits of every level
+  uint32_t shift;   // level l+j tests key bit (shift - j)
+  uint32_t pad;
+};
+
+struct TileArgs {
+  const void* in;
+  void* out;          // S_{l+K}; nullptr in the last pass
+  uint64_t out_size;  // keys of `out` (bounds check)
+  const TileSeg* segs;
+  const TileText* texts;
+  const uint64_t* tables;
+  unsigned long long* lookback;  // [tiles][1 << D], zeroed
+  uint32_t* tile_counter;        // zeroed
+  uint32_t* status;
+  uint32_t nsegs;
+  uint32_t tiles;
+};
+
+template <typename KeyT, int K, bool OUT, int THREADS, int V>
+struct TileCfg {
+  static constexpr int D = OUT ? K : K - 1;             // splits
+  static constexpr int KPL = 16 / int(sizeof(KeyT));    // keys per 16-byte vector
+  static constexpr int ITEMS = V * KPL;                  // keys per thread
+  static constexpr int T = THREADS * ITEMS;              // keys per tile
+  static constexpr int WARPS = THREADS / 32;
+  static constexpr int WSLICE = 32 * ITEMS;              // keys per warp
+  static constexpr int NVEC = THREADS * V;               // vectors per tile
+  static constexpr int SBW = T / 32 + 2;                 // stream words per level (+2 for funnel reads)
+  static constexpr int NLB = 1 << D;                     // look-back counters per tile
+  static constexpr int LPC = 32 / KPL;                   // lanes per 32-bit stream word
+  static_assert(T <= 32768, "zero counts are packed in 16 bits");
+  static_assert(K >= 1 && K <= kTileMaxLevels, "1..4 levels per pass");
+  static_assert(V % 2 == 0, "vectors are scanned in pairs");
+  static constexpr size_t smem_bytes() {
+    return size_t(2) * T * sizeof(KeyT) + size_t(K) * SBW * 4 + (D >= 2 ? size_t(NVEC) * 4 : 0);
+  }
+};
+
+// Split bits of the keys of one 16-byte vector, MSB first: bit KPL-1-i is the
+// bit of key i.
+template <typename KeyT>
+__device__ __forceinline__ uint32_t vector_bits(const uint4& v, uint32_t sh) {
+  if (sh >= 8 * sizeof(KeyT)) return 0u;  // above the key width every bit is 0
+  const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+  uint32_t m = 0;
+  if constexpr (sizeof(KeyT) == 1) {
+    // byte k of a word lands at bit 3-k: ((w >> sh) & 0x01010101) * 0x80402010 >> 28
+#pragma unroll
+    for (int q = 0; q < 4; ++q) m |= ((((w[q] >> sh) & 0x01010101u) * 0x80402010u) >> 28) << (12 - 4 * q);
+  } else if constexpr (sizeof(KeyT) == 2) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t t = (w[q] >> sh) & 0x00010001u;
+      m |= (((t << 1) | (t >> 16)) & 3u) << (6 - 2 * q);
+    }
+  } else if constexpr (sizeof(KeyT) == 4) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) m |= ((w[q] >> sh) & 1u) << (3 - q);
+  } else {
+    m = (uint32_t(((uint64_t(w[1]) << 32 | w[0]) >> sh) & 1u) << 1) | uint32_t(((uint64_t(w[3]) << 32 | w[2]) >> sh) & 1u);
+  }
+  return m;
+}
+
+// Key i of a 16-byte vector, as the low bits of a 32-bit register (64-bit
+// keys: the full key).  i is a constant after unrolling.
+template <typename KeyT>
+__device__ __forceinline__ auto vector_key(const uint4& v, int i) {
+  const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+  if constexpr (sizeof(KeyT) == 1) return uint32_t(w[i >> 2] >> (8 * (i & 3)));
+  else if constexpr (sizeof(KeyT) == 2) return uint32_t(w[i >> 1] >> (16 * (i & 1)));
+  else if constexpr (sizeof(KeyT) == 4) return w[i];
+  else return uint64_t(w[2 * i]) | (uint64_t(w[2 * i + 1]) << 32);
+}
+
+__device__ __forceinline__ void st_shared_key(uint32_t addr, uint32_t v, int bytes) {
+  if (bytes == 1) asm volatile("st.shared.u8 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+  else if (bytes == 2) asm volatile("st.shared.u16 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+  else asm volatile("st.shared.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_shared_key(uint32_t addr, uint64_t v, int) {
+  asm volatile("st.shared.u64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
+}
+
+// Stable 1-bit split of the keys of one vector: key i goes to the zero or the
+// one cursor (shared byte addresses), which advance.  FULL: all KPL keys are
+// valid; otherwise the first `valid`.
+template <typename KeyT, int KPL, bool FULL>
+__device__ __forceinline__ void scatter_vector(const uint4& v, uint32_t mb, uint32_t zd, uint32_t od, int valid) {
+  constexpr uint32_t KB = sizeof(KeyT);
+#pragma unroll
+  for (int i = 0; i < KPL; ++i) {
+    if (!FULL && i >= valid) break;
+    const uint32_t one = (mb >> (KPL - 1 - i)) & 1u;
+    st_shared_key(one ? od : zd, vector_key<KeyT>(v, i), int(KB));
+    od += one * KB;
+    zd += (one ^ 1u) * KB;
+  }
+}
+
+// Exclusive prefix over the predecessor tiles of this segment of look-back
+// counter c (one warp, 32 predecessors per step).  A segment's first tile
+// publishes its inclusive value at once, so no walk crosses a segment start.
+__device__ __forceinline__ uint64_t segment_lookback(unsigned long long* lb, int nlb, uint32_t tile, uint32_t first,
+                                                     int c, uint64_t mine, uint32_t* status) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long* row = lb + uint64_t(tile) * nlb + c;
+  if (tile == first) {
+    if (lane == 0) st_volatile(row, kFlagPrefix | mine);
+    return 0;
+  }
+  if (lane == 0) st_volatile(row, kFlagAggregate | mine);
+  uint64_t excl = 0;
+  int64_t base = int64_t(tile) - 1;
+  while (true) {
+    const int64_t t = base - lane;
+    uint64_t s = kFlagPrefix;  // before the segment: an empty inclusive prefix
+    if (t >= int64_t(first)) s = lookback_wait(lb + uint64_t(t) * nlb + c, status);
+    const uint32_t pmask = __ballot_sync(0xFFFFFFFFu, (s >> 62) == 2);
+    const int stop = pmask ? __ffs(pmask) - 1 : 31;
+    uint64_t x = lane <= stop ? (s & kCountMask) : 0;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) x += __shfl_xor_sync(0xFFFFFFFFu, x, d);
+    excl += x;
+    if (pmask) break;
+    base -= 32;
+  }
+  if (lane == 0) st_volatile(row, kFlagPrefix | (excl + mine));
+  return excl;
+}
+
+// 32 stream bits starting at bit `src` (>= 0) of a shared bit stream.
+__device__ __forceinline__ uint32_t stream32(const uint32_t* sb, uint32_t src) {
+  const uint32_t w0 = sb[src >> 5], w1 = sb[(src >> 5) + 1];
+  return __funnelshift_l(w1, w0, src & 31);
+}
+
+// One warp writes stream bits [src, src+len) to level bits [dst, dst+len):
+// whole 32-bit chunks are stored, chunks shared with other runs are OR-ed
+// (the level was zeroed).
+__device__ __forceinline__ void write_bit_run(uint64_t* level, uint64_t nbits, uint64_t dst, const uint32_t* sb,
+                                              uint32_t src, uint32_t len, uint32_t* status) {
+  if (len == 0) return;
+  const int lane = threadIdx.x & 31;
+  if (dst + len > nbits) {
+    if (lane == 0) atomicOr(status, kErrBounds);
+    return;
+  }
+  uint32_t* out = reinterpret_cast<uint32_t*>(level);
+  const uint64_t qa = dst >> 5, qb = (dst + len - 1) >> 5;
+  const uint32_t lead = uint32_t(dst & 31);  // bits of chunk qa before the run
+  for (uint64_t q = qa + lane; q <= qb; q += 32) {
+    const uint32_t k = uint32_t(q - qa);  // chunk index within the run
+    uint32_t val, lo = 0;
+    if (k == 0) {
+      val = stream32(sb, src) >> lead;
+      lo = lead;
+    } else {
+      val = stream32(sb, src + 32 * k - lead);
+    }
+    const uint64_t end_in_chunk = dst + len - (q << 5);  // run bits up to the end of this chunk
+    const uint32_t hi = end_in_chunk >= 32 ? 32u : uint32_t(end_in_chunk);
+    const uint32_t mask = chunk_mask(lo, hi);
+    if (mask == 0xFFFFFFFFu) out[chunk_u32_index(q)] = val;
+    else atomicOr(&out[chunk_u32_index(q)], val & mask);
+  }
+}
+
+// One warp copies `len` bytes from shared memory to global memory: byte
+// stores up to a 4-byte aligned destination, then 32-bit stores built from
+// funnel-shifted aligned shared words, then the tail.
+__device__ __forceinline__ void write_key_run(unsigned char* dst, const unsigned char* src, uint32_t len) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t head = min(len, uint32_t((4 - (reinterpret_cast<uintptr_t>(dst) & 3)) & 3));
+  if (uint32_t(lane) < head) dst[lane] = src[lane];
+  const uint32_t body = (len - head) >> 2;
+  const uint32_t so0 = uint32_t(reinterpret_cast<uintptr_t>(src + head) & 3);
+  const uint32_t* s32 = reinterpret_cast<const uint32_t*>(src + head - so0);
+  uint32_t* d32 = reinterpret_cast<uint32_t*>(dst + head);
+  for (uint32_t k = lane; k < body; k += 32) {
+    const uint32_t lo = s32[k], hi = so0 ? s32[k + 1] : 0u;
+    d32[k] = __funnelshift_r(lo, hi, 8 * so0);
+  }
+  const uint32_t done = head + 4 * body;
+  if (uint32_t(lane) < len - done) dst[done + lane] = src[done + lane];
+}
+
+// Load `bytes` bytes from global `src` (any alignment) into the 16-byte
+// aligned shared buffer `dst`, 16 bytes per thread step.  Bytes past the end
+// of the tile are not read beyond the 16-byte block that holds the last one.
+template <int THREADS>
+__device__ __forceinline__ void load_tile_bytes(uint4* dst, const unsigned char* src, uint32_t bytes) {
+  const uint32_t nv = (bytes + 15) >> 4;
+  const uintptr_t sa = reinterpret_cast<uintptr_t>(src);
+  const uint32_t off = uint32_t(sa & 15);
+  const uint4* a = reinterpret_cast<const uint4*>(sa - off);
+  if (off == 0) {
+    for (uint32_t k = threadIdx.x; k < nv; k += THREADS) dst[k] = __ldcs(a + k);
+    return;
+  }
+  const uint32_t wsh = off >> 2, bsh = 8 * (off & 3);
+  const uint32_t last_block = uint32_t((off + bytes - 1) >> 4);  // last aligned block holding tile bytes
+  for (uint32_t k = threadIdx.x; k < nv; k += THREADS) {
+    const uint4 lo = __ldcs(a + k);
+    const uint4 hi = k + 1 <= last_block ? __ldcs(a + k + 1) : make_uint4(0, 0, 0, 0);
+    const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+    uint32_t o[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      uint32_t x0 = 0, x1 = 0;
+      // select words wsh+i and wsh+i+1 without dynamic register indexing
+#pragma unroll
+      for (int s = 0; s < 4; ++s)
+        if (uint32_t(s) == wsh) { x0 = w[s + i]; x1 = w[s + i + 1]; }
+      o[i] = __funnelshift_r(x0, x1, bsh);
+    }
+    dst[k] = make_uint4(o[0], o[1], o[2], o[3]);
+  }
+}
+
+template <typename KeyT, int K, bool OUT, int THREADS, int V>
+__global__ void __launch_bounds__(THREADS, 4) tile_pass_kernel(TileArgs a) {
+  using C = TileCfg<KeyT, K, OUT, THREADS, V>;
+  constexpr int D = C::D, KPL = C::KPL, T = C::T, WARPS = C::WARPS, WSLICE = C::WSLICE, SBW = C::SBW;
+  constexpr int NLB = C::NLB, LPC = C::LPC;
+  constexpr uint32_t FULLV = (1u << KPL) - 1u;
+  constexpr int KB = int(sizeof(KeyT));
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  KeyT* buf0 = reinterpret_cast<KeyT*>(smem_raw);
+  uint32_t* sbits = reinterpret_cast<uint32_t*>(smem_raw + size_t(2) * T * KB);  // K streams of SBW words
+  uint32_t* meta = sbits + K * SBW;                                               // D >= 2: per vector
+
+  __shared__ uint32_t s_tile, s_seg;
+  __shared__ TileSeg s_sg;
+  __shared__ TileText s_tx;
+  __shared__ uint32_t s_wz[WARPS];
+  __shared__ uint32_t s_ztot;
+  __shared__ uint32_t rsz[D + 1][1 << D], rst[D + 1][1 << D];
+  __shared__ unsigned long long pre[NLB];
+  __shared__ unsigned long long s_table[tile_table_size(K)];
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    const uint32_t g = atomicAdd(a.tile_counter, 1u);
+    uint32_t lo = 0, hi = a.nsegs;  // last segment with tile0 <= g
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (a.segs[mid].tile0 <= g) lo = mid; else hi = mid;
+    }
+    s_tile = g;
+    s_seg = lo;
+  }
+  __syncthreads();
+  const uint32_t g = s_tile;
+  if (tid == 0) {
+    s_sg = a.segs[s_seg];
+    s_tx = a.texts[s_sg.text];
+  }
+  __syncthreads();
+  const uint32_t tl = g - s_sg.tile0;
+  const uint64_t tstart = uint64_t(tl) * T;
+  const uint32_t n = s_sg.m - tstart < uint64_t(T) ? uint32_t(s_sg.m - tstart) : uint32_t(T);
+  for (int i = tid; i < tile_table_size(K); i += THREADS) s_table[i] = a.tables[s_sg.table + i];
+
+  load_tile_bytes<THREADS>(reinterpret_cast<uint4*>(buf0),
+                           static_cast<const unsigned char*>(a.in) + (s_sg.in_begin + tstart) * KB, n * KB);
+  if (tid == 0) {
+    rsz[0][0] = n;
+    rst[0][0] = 0;
+  }
+  __syncthreads();
+
+  const uint32_t smem_base = uint32_t(__cvta_generic_to_shared(smem_raw));
+  const uint32_t shift = s_tx.shift;
+  // valid keys of this warp and before it
+  const uint32_t wbeg = uint32_t(warp) * WSLICE;
+  const uint32_t nw = n > wbeg ? min(n - wbeg, uint32_t(WSLICE)) : 0u;
+  const uint32_t vbefore = min(n, wbeg);
+
+  int cur = 0;
+#pragma unroll 1
+  for (int s = 0; s < K; ++s) {
+    const bool split = s < D;
+    const KeyT* cb = buf0 + cur * T;
+    const uint32_t sh = shift - uint32_t(s);
+    uint4 kv[V];
+    uint32_t mb[V];
+    int nv[V];
+#pragma unroll
+    for (int r = 0; r < V; ++r) {
+      const int gv = (warp * V + r) * 32 + lane;
+      kv[r] = reinterpret_cast<const uint4*>(cb)[gv];
+      const int rem = int(n) - gv * KPL;
+      nv[r] = rem >= KPL ? KPL : (rem > 0 ? rem : 0);
+      const uint32_t vm = nv[r] == KPL ? FULLV : (FULLV & ~((1u << (KPL - nv[r])) - 1u));
+      mb[r] = vector_bits<KeyT>(kv[r], sh) & vm;
+      // level l+s bits of this vector into stream s
+      uint32_t x = mb[r] << (32 - KPL * (1 + (lane % LPC)));
+#pragma unroll
+      for (int d = 1; d < LPC; d <<= 1) x |= __shfl_down_sync(0xFFFFFFFFu, x, d);
+      if (lane % LPC == 0) sbits[s * SBW + gv / LPC] = x;
+    }
+    if (!split) break;
+
+    // ---- zero counts, warp scan over (round, lane) order ------------------
+    uint32_t zc[V], ex[V];
+#pragma unroll
+    for (int r = 0; r < V; ++r) zc[r] = uint32_t(nv[r]) - __popc(mb[r]);
+    uint32_t rb = 0;
+#pragma unroll
+    for (int q = 0; q < V / 2; ++q) {
+      const uint32_t p = zc[2 * q] | (zc[2 * q + 1] << 16);
+      uint32_t x = p;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+        if (lane >= d) x += y;
+      }
+      const uint32_t tot = __shfl_sync(0xFFFFFFFFu, x, 31);
+      const uint32_t e = x - p;
+      ex[2 * q] = rb + (e & 0xFFFFu);
+      rb += tot & 0xFFFFu;
+      ex[2 * q + 1] = rb + (e >> 16);
+      rb += tot >> 16;
+    }
+    if (lane == 0) s_wz[warp] = rb;
+    __syncthreads();  // (A)
+    uint32_t ztot = 0, zpre = 0;
+#pragma unroll
+    for (int w = 0; w < WARPS; ++w) {
+      const uint32_t z = s_wz[w];
+      ztot += z;
+      zpre += w < warp ? z : 0u;
+    }
+    if (tid == 0) {
+      s_ztot = ztot;
+      if (s >= 2) {  // starts of the key_s runs (sizes written after the previous split)
+        uint32_t run = 0;
+        for (int v = 0; v < (1 << s); ++v) { rst[s][v] = run; run += rsz[s][v]; }
+      }
+    }
+    const uint32_t opre = vbefore - zpre;
+    const uint32_t nb = smem_base + uint32_t((cur ^ 1) * T * KB);
+#pragma unroll
+    for (int r = 0; r < V; ++r) {
+      const int gv = (warp * V + r) * 32 + lane;
+      const uint32_t before = min(nw, uint32_t((r * 32 + lane) * KPL));  // valid keys of the warp before the vector
+      const uint32_t zd = nb + (zpre + ex[r]) * KB;
+      const uint32_t od = nb + (ztot + opre + before - ex[r]) * KB;
+      if constexpr (D >= 2) {
+        if (s >= 1) meta[gv] = ((zpre + ex[r]) << 16) | mb[r];
+      }
+      if (nv[r] == KPL) scatter_vector<KeyT, KPL, true>(kv[r], mb[r], zd, od, KPL);
+      else if (nv[r] > 0) scatter_vector<KeyT, KPL, false>(kv[r], mb[r], zd, od, nv[r]);
+    }
+    __syncthreads();  // (B)
+    // ---- run sizes of key_{s+1} -------------------------------------------
+    if (s == 0) {
+      if (tid == 0) {
+        rsz[1][0] = ztot;
+        rsz[1][1] = n - ztot;
+        rst[1][0] = 0;
+        rst[1][1] = ztot;
+      }
+    } else if (tid < (2 << s)) {
+      const int v = tid & ((1 << s) - 1);
+      const uint32_t st = rst[s][v], en = st + rsz[s][v];
+      auto zb = [&](uint32_t p) -> uint32_t {  // zeros before tile position p in the pre-split order
+        if (p >= n) return s_ztot;
+        const uint32_t w = meta[p / KPL], k = p % KPL;
+        const uint32_t ones = k ? __popc((w & FULLV) >> (KPL - k)) : 0u;
+        return (w >> 16) + k - ones;
+      };
+      const uint32_t zin = zb(en) - zb(st);
+      rsz[s + 1][tid] = (tid >> s) ? rsz[s][v] - zin : zin;
+    }
+    cur ^= 1;
+  }
+  __syncthreads();
+  if constexpr (D >= 2) {
+    if (tid == 0) {
+      uint32_t run = 0;
+      for (int v = 0; v < (1 << D); ++v) { rst[D][v] = run; run += rsz[D][v]; }
+    }
+  }
+
+  // ---- look-back over the finest runs, restarted per segment --------------
+  if constexpr (D >= 1) {
+    __syncthreads();
+    for (int c = warp; c < NLB; c += WARPS) {
+      const uint64_t p = segment_lookback(a.lookback, NLB, g, s_sg.tile0, c, rsz[D][c], a.status);
+      if (lane == 0) pre[c] = p;
+    }
+  }
+  __syncthreads();
+
+  // ---- bits of levels l..l+K-1 to the matrix and the tree ------------------
+  // item = (structure, level j, run v); warp-strided; level 0 is one run
+  constexpr int ITEMS_PER_STRUCT = (1 << K) - 1;
+  const int nstruct = s_tx.wt ? 2 : 1;
+#pragma unroll 1
+  for (int it = warp; it < nstruct * ITEMS_PER_STRUCT; it += WARPS) {
+    const int st = it / ITEMS_PER_STRUCT;
+    const int e = it % ITEMS_PER_STRUCT;  // = (1 << j) - 1 + v
+    const int j = 31 - __clz(e + 1);
+    const int v = e + 1 - (1 << j);
+    uint64_t p;  // earlier tiles of the segment with key_j == v
+    if (j == 0) {
+      p = tstart;
+    } else {
+      p = 0;
+      for (int h = 0; h < (1 << (D - j)); ++h) p += pre[v + (h << j)];
+    }
+    const uint64_t dst = s_table[st ? tile_wt_entry(K, j, v) : tile_wm_entry(j, v)] + p;
+    uint64_t* level = (st ? s_tx.wt : s_tx.wm) + uint64_t(j) * s_tx.stride;
+    write_bit_run(level, s_tx.nbits, dst, sbits + j * SBW, rst[j][v], rsz[j][v], a.status);
+  }
+  if constexpr (OUT) {
+    const KeyT* cb = buf0 + cur * T;
+    for (int v = warp; v < (1 << K); v += WARPS) {
+      const uint32_t len = rsz[K][v];
+      if (len == 0) continue;
+      const uint64_t dst = s_table[tile_out_entry(K, v)] + pre[v];
+      if (dst + len > a.out_size) {
+        if (lane == 0) atomicOr(a.status, kErrBounds);
+        continue;
+      }
+      write_key_run(reinterpret_cast<unsigned char*>(static_cast<KeyT*>(a.out) + dst),
+                    reinterpret_cast<const unsigned char*>(cb + rst[K][v]), len * uint32_t(KB));
+    }
+  }
+}
+
+}  // namespace pwmgpu

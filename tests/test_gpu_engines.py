@@ -1,0 +1,142 @@
+"""GPU: the two split engines of plain builds (segmented tile passes, the
+default, and warp-autonomous passes) against the oracle, bit-exact, over the
+cases where their tilings differ: partial tiles, prefix-group segments of
+every size (segmented tree-writing passes and matrix-only passes with a
+regrouped tree), misaligned segment starts and text pointers, every pass
+width, and all key widths."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+DT = {1: np.uint8, 2: np.uint16, 4: np.uint32}
+TILE = {1: 16384, 2: 8192, 4: 4096}
+
+
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def build(pg, ctx, text, L, tree):
+    return pg.wx_ps(text.dtype.type, tree, context=ctx).compute(text, text.size, L)
+
+
+def check(pg, orc, ctx, text, L, label=""):
+    for tree in (False, True):
+        ws = build(pg, ctx, text, L, tree)
+        ref = orc.build(text, L, tree, "ps")
+        assert ws.levels() == L
+        for l in range(L):
+            assert np.array_equal(np.asarray(ws.bvs()[l]), ref.level(l)), f"{label} level {l} tree={tree}"
+        if not tree:
+            assert ws.zeros() == [int(z) for z in ref.zeros], label
+
+
+@pytest.fixture(scope="module")
+def engines(pg):
+    torch_cuda()
+    tile = pg.Context()
+    warp = pg.Context()
+    warp.set_engine(pg.ENGINE_WARP)
+    return tile, warp
+
+
+@pytest.mark.parametrize("width", [1, 2, 4])
+def test_partial_and_whole_tiles(pg, orc, engines, width):
+    tile, _ = engines
+    T = TILE[width]
+    rng = np.random.default_rng(width)
+    L = {1: 8, 2: 11, 4: 13}[width]
+    for n in (1, 2, 15, 16, 17, 31, 32, 33, T - 1, T, T + 1, 3 * T + 7):
+        text = rng.integers(0, 1 << L, n).astype(DT[width])
+        check(pg, orc, tile, text, L, f"n={n}")
+
+
+@pytest.mark.parametrize("L", list(range(1, 13)))
+def test_every_level_count_u8_u16(pg, orc, engines, L):
+    tile, _ = engines
+    rng = np.random.default_rng(100 + L)
+    width = 1 if L <= 8 else 2
+    n = 200_003
+    # skewed: a geometric symbol mix leaves some prefix groups empty, some tiny
+    g = np.minimum(rng.geometric(0.05, n) - 1, (1 << L) - 1)
+    text = np.where(rng.random(n) < 0.5, g, rng.integers(0, 1 << L, n)).astype(DT[width])
+    check(pg, orc, tile, text, L, f"L={L}")
+
+
+def test_segmented_deep_passes_u32(pg, orc, engines):
+    # u32 tiles hold 4096 keys: with 6M keys the passes at levels 4 and 8 run
+    # one segment per prefix group (tree levels written by the pass), the pass
+    # at level 12 does not (regrouped tree levels)
+    tile, _ = engines
+    rng = np.random.default_rng(7)
+    n = 6_000_000
+    text = rng.integers(0, 1 << 14, n).astype(np.uint32)
+    check(pg, orc, tile, text, 14, "u32 L=14")
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 4])
+def test_engines_agree(pg, orc, engines, k):
+    tile, warp = engines
+    tile.set_pass_levels(k)
+    try:
+        # 1.1M keys: the pass at level 4 runs one segment per prefix group
+        text = pg.generate(pg.GEN_ZIPF256, 40 + k, 1_100_003, 1)
+        for tree in (False, True):
+            a = build(pg, tile, text, 8, tree)
+            b = build(pg, warp, text, 8, tree)
+            for l in range(8):
+                assert np.array_equal(np.asarray(a.bvs()[l]), np.asarray(b.bvs()[l])), (k, tree, l)
+            if not tree:
+                assert a.zeros() == b.zeros()
+        check(pg, orc, tile, text[:300_000], 8, f"k={k}")
+    finally:
+        tile.set_pass_levels(4)
+
+
+def test_segmented_byte_text(pg, orc, engines):
+    tile, _ = engines
+    text = pg.generate(pg.GEN_ZIPF256, 5, 2_000_001, 1)
+    check(pg, orc, tile, text, 8, "zipf 2M")
+    t16 = pg.generate(pg.GEN_MIX16, 6, 3_000_001, 2)
+    check(pg, orc, tile, t16, 16, "mix16 3M")
+
+
+@pytest.mark.parametrize("L", [9, 12])
+def test_byte_text_with_more_levels_than_bits(pg, orc, engines, L):
+    # the top L-8 levels of a byte text are all zero bits
+    tile, warp = engines
+    text = pg.generate(pg.GEN_ZIPF256, 8, 150_001, 1)
+    check(pg, orc, tile, text, L, f"u8 L={L}")
+    check(pg, orc, warp, text, L, f"u8 L={L} warp")
+
+
+def test_constant_and_two_symbol_texts(pg, orc, engines):
+    tile, _ = engines
+    for text in (np.full(70_000, 0xA5, np.uint8), np.full(50_000, 0, np.uint8),
+                 np.tile(np.array([0, 255], np.uint8), 40_000), np.full(33_000, 3, np.uint16)):
+        L = 8 if text.dtype == np.uint8 else 9
+        check(pg, orc, tile, text, L, f"const {text[:2]}")
+
+
+def test_misaligned_device_text(pg, orc, engines):
+    torch = torch_cuda()
+    tile, _ = engines
+    rng = np.random.default_rng(3)
+    n = 123_457
+    host = rng.integers(0, 256, n + 16).astype(np.uint8)
+    d = torch.from_numpy(host).cuda()
+    for off in (0, 1, 3, 5, 15):
+        ds = pg.DeviceStructure(n, 1, 8, matrix=True, tree=True, context=tile)
+        ds.build(d.data_ptr() + off)
+        ds.check()
+        text = host[off:off + n]
+        for which, tree in ((0, False), (1, True)):
+            ws = ds.download(which)
+            ref = orc.build(text, 8, tree, "ps")
+            for l in range(8):
+                assert np.array_equal(np.asarray(ws.bvs()[l]), ref.level(l)), (off, tree, l)
+        ds.free()
