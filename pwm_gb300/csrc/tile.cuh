@@ -28,11 +28,14 @@
 //   * emits the bits of each level from the same register copy, in that
 //     level's order, into a shared bit stream;
 //   * tracks the tile's run sizes of key_1..key_D from the split counts;
-//   * exchanges the finest run counts (2^D per tile) with a decoupled look-back
-//     that restarts at every segment's first tile;
+//   * counts the tile's finest runs (key_D digits) right after loading it and
+//     publishes them at once; after its splits and the write of the level-l
+//     run (which needs no prefix) the CTA completes the decoupled look-back
+//     (restarted at every segment's first tile; counter-major state, one
+//     coalesced load per counter, 256 predecessors per round trip);
 //   * writes every run of every level to the matrix and the tree at
-//     table start + look-back prefix, and the runs of S_{l+K} to the next
-//     pass's input.
+//     table start + look-back prefix in 64-bit words (one warp per structure
+//     and level), and the runs of S_{l+K} to the next pass's input.
 #pragma once
 
 #include "common.cuh"
@@ -72,7 +75,7 @@ struct TileArgs {
   const TileSeg* segs;
   const TileText* texts;
   const uint64_t* tables;
-  unsigned long long* lookback;  // [tiles][1 << D], zeroed
+  unsigned long long* lookback;  // [1 << D][tiles] (counter-major), zeroed
   uint32_t* tile_counter;        // zeroed
   uint32_t* status;
   uint32_t nsegs;
@@ -125,6 +128,28 @@ __device__ __forceinline__ uint32_t vector_bits(const uint4& v, uint32_t sh) {
   return m;
 }
 
+// D-bit fields [lo, lo+D) of the keys of one 16-byte vector (fmask: the
+// field mask clipped to the key width).
+template <typename KeyT>
+__device__ __forceinline__ void vector_fields(const uint4& v, uint32_t lo, uint32_t fmask,
+                                              uint32_t (&f)[16 / sizeof(KeyT)]) {
+  const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    if constexpr (sizeof(KeyT) == 1) {
+      const uint32_t x = (w[q] >> lo) & (fmask * 0x01010101u);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) f[4 * q + k] = __byte_perm(x, 0u, 0x4440u + k);
+    } else if constexpr (sizeof(KeyT) == 2) {
+      const uint32_t x = (w[q] >> lo) & (fmask * 0x00010001u);
+      f[2 * q] = x & 0xFFFFu;
+      f[2 * q + 1] = x >> 16;
+    } else {
+      f[q] = (w[q] >> lo) & fmask;
+    }
+  }
+}
+
 // Key i of a 16-byte vector, as the low bits of a 32-bit register (64-bit
 // keys: the full key).  i is a constant after unrolling.
 template <typename KeyT>
@@ -145,87 +170,131 @@ __device__ __forceinline__ void st_shared_key(uint32_t addr, uint64_t v, int) {
   asm volatile("st.shared.u64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
 }
 
-// Stable 1-bit split of the keys of one vector: key i goes to the zero or the
-// one cursor (shared byte addresses), which advance.  FULL: all KPL keys are
-// valid; otherwise the first `valid`.
+// Stable 1-bit split of the keys of one vector: key i goes to the one cursor
+// plus the ones before it, or to the zero cursor plus the zeros before it
+// (shared byte addresses).  FULL: all KPL keys are valid; otherwise the
+// first `valid`.
 template <typename KeyT, int KPL, bool FULL>
 __device__ __forceinline__ void scatter_vector(const uint4& v, uint32_t mb, uint32_t zd, uint32_t od, int valid) {
   constexpr uint32_t KB = sizeof(KeyT);
 #pragma unroll
   for (int i = 0; i < KPL; ++i) {
     if (!FULL && i >= valid) break;
+    const uint32_t c = i ? __popc(mb >> (KPL - i)) : 0u;  // ones before key i
     const uint32_t one = (mb >> (KPL - 1 - i)) & 1u;
-    st_shared_key(one ? od : zd, vector_key<KeyT>(v, i), int(KB));
-    od += one * KB;
-    zd += (one ^ 1u) * KB;
+    st_shared_key(one ? od + c * KB : zd + (uint32_t(i) - c) * KB, vector_key<KeyT>(v, i), int(KB));
   }
 }
 
-// Exclusive prefix over the predecessor tiles of this segment of look-back
-// counter c (one warp, 32 predecessors per step).  A segment's first tile
-// publishes its inclusive value at once, so no walk crosses a segment start.
-__device__ __forceinline__ uint64_t segment_lookback(unsigned long long* lb, int nlb, uint32_t tile, uint32_t first,
-                                                     int c, uint64_t mine, uint32_t* status) {
-  const int lane = threadIdx.x & 31;
-  unsigned long long* row = lb + uint64_t(tile) * nlb + c;
-  if (tile == first) {
-    if (lane == 0) st_volatile(row, kFlagPrefix | mine);
-    return 0;
-  }
-  if (lane == 0) st_volatile(row, kFlagAggregate | mine);
-  uint64_t excl = 0;
+// Decoupled look-back of all NLB counters of a tile by the whole CTA.  The
+// state is counter-major (counter c of tile t at lb[c * tiles + t]): warp w
+// examines predecessors base-32w-31 .. base-32w, one coalesced load per
+// counter, so one round trip covers 32*WARPS predecessors (the inclusive
+// prefixes must propagate faster than tiles complete).  Per counter the walk
+// stops at the nearest inclusive prefix.  A segment's first tile publishes
+// its inclusive values at once, so no walk crosses a segment start.  The
+// tile's own aggregates (mine, at most one tile of keys each) were published
+// when it counted its keys.  Leaves the exclusive prefixes in pre[0..NLB)
+// and publishes the inclusive ones.  Called by every thread of the CTA.
+template <int NLB, int WARPS>
+__device__ __forceinline__ void segment_lookback_cta(unsigned long long* lb, uint32_t tiles, uint32_t tile,
+                                                     uint32_t first, const uint32_t* mine, unsigned long long* pre,
+                                                     unsigned long long (*wsum)[NLB], uint32_t* wmask,
+                                                     uint32_t* s_open, uint32_t* status) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid < NLB) pre[tid] = 0;
+  if (tile == first) return;  // its inclusive values went out with its counts
+  if (tid == 0) *s_open = (1u << NLB) - 1u;
+  __syncthreads();
   int64_t base = int64_t(tile) - 1;
-  while (true) {
-    const int64_t t = base - lane;
-    uint64_t s = kFlagPrefix;  // before the segment: an empty inclusive prefix
-    if (t >= int64_t(first)) s = lookback_wait(lb + uint64_t(t) * nlb + c, status);
-    const uint32_t pmask = __ballot_sync(0xFFFFFFFFu, (s >> 62) == 2);
-    const int stop = pmask ? __ffs(pmask) - 1 : 31;
-    uint64_t x = lane <= stop ? (s & kCountMask) : 0;
+  for (;;) {
+    const uint32_t open = *s_open;
+    if (!open) break;
+    const int64_t t = base - 32 * warp - lane;
+    const bool real = t >= int64_t(first);
+    const unsigned long long* col = lb + (real ? t : 0);
+    uint64_t v[NLB];
 #pragma unroll
-    for (int d = 16; d > 0; d >>= 1) x += __shfl_xor_sync(0xFFFFFFFFu, x, d);
-    excl += x;
-    if (pmask) break;
-    base -= 32;
+    for (int c = 0; c < NLB; ++c)
+      v[c] = (real && ((open >> c) & 1u)) ? ld_volatile(col + uint64_t(c) * tiles) : kFlagPrefix;
+    // wait (bounded) for counters a predecessor has not published yet
+    for (uint32_t spins = 0;; ++spins) {
+      bool missing = false;
+#pragma unroll
+      for (int c = 0; c < NLB; ++c) missing |= (v[c] >> 62) == 0;
+      if (!missing) break;
+      if (spins >= kSpinLimit) {
+        atomicOr(status, kErrTimeout);
+#pragma unroll
+        for (int c = 0; c < NLB; ++c)
+          if ((v[c] >> 62) == 0) v[c] = kFlagPrefix;
+        break;
+      }
+      __nanosleep(64);
+#pragma unroll
+      for (int c = 0; c < NLB; ++c)
+        if ((v[c] >> 62) == 0) v[c] = ld_volatile(col + uint64_t(c) * tiles);
+    }
+    uint32_t pbits = 0;
+#pragma unroll
+    for (int c = 0; c < NLB; ++c) {
+      if (!((open >> c) & 1u)) continue;
+      const bool isp = (v[c] >> 62) == 2;
+      const uint32_t pmask = __ballot_sync(0xFFFFFFFFu, isp);
+      const int stop = pmask ? __ffs(pmask) - 1 : 32;  // nearest inclusive prefix in this window
+      // aggregates before it are single-tile counts: a 32-bit warp sum
+      const uint32_t agg = __reduce_add_sync(0xFFFFFFFFu, (lane < stop && !isp) ? uint32_t(v[c]) : 0u);
+      const uint64_t pv = __shfl_sync(0xFFFFFFFFu, v[c] & kCountMask, pmask ? stop : 0);
+      if (lane == 0) wsum[warp][c] = uint64_t(agg) + (pmask ? pv : 0ull);
+      pbits |= pmask ? (1u << c) : 0u;
+    }
+    if (lane == 0) wmask[warp] = pbits;
+    __syncthreads();
+    if (tid < NLB && ((open >> tid) & 1u)) {
+      uint64_t e = pre[tid];
+      bool closed = false;
+      for (int w = 0; w < WARPS && !closed; ++w) {
+        e += wsum[w][tid];
+        closed = (wmask[w] >> tid) & 1u;
+      }
+      pre[tid] = e;
+      if (closed) atomicAnd(s_open, ~(1u << tid));
+    }
+    __syncthreads();
+    base -= 32 * WARPS;
   }
-  if (lane == 0) st_volatile(row, kFlagPrefix | (excl + mine));
-  return excl;
+  if (tid < NLB) st_volatile(lb + uint64_t(tid) * tiles + tile, kFlagPrefix | (pre[tid] + mine[tid]));
 }
 
-// 32 stream bits starting at bit `src` (>= 0) of a shared bit stream.
-__device__ __forceinline__ uint32_t stream32(const uint32_t* sb, uint32_t src) {
-  const uint32_t w0 = sb[src >> 5], w1 = sb[(src >> 5) + 1];
-  return __funnelshift_l(w1, w0, src & 31);
+// 64 stream bits starting at bit `x` of a shared bit stream (MSB first).
+__device__ __forceinline__ uint64_t stream64(const uint32_t* sb, uint32_t x) {
+  const uint32_t i = x >> 5, sh = x & 31;
+  const uint32_t w0 = sb[i], w1 = sb[i + 1], w2 = sb[i + 2];
+  const uint32_t hi = __funnelshift_l(w1, w0, sh), lo = __funnelshift_l(w2, w1, sh);
+  return (uint64_t(hi) << 32) | lo;
 }
 
-// One warp writes stream bits [src, src+len) to level bits [dst, dst+len):
-// whole 32-bit chunks are stored, chunks shared with other runs are OR-ed
-// (the level was zeroed).
-__device__ __forceinline__ void write_bit_run(uint64_t* level, uint64_t nbits, uint64_t dst, const uint32_t* sb,
-                                              uint32_t src, uint32_t len, uint32_t* status) {
+// Stream bits [src, src+len) to level bits [dst, dst+len), 64-bit words
+// k = k0, k0 + step, ... of the destination range: whole words are stored,
+// words shared with other runs are OR-ed (the level was zeroed).
+__device__ __forceinline__ void write_bits64(uint64_t* level, uint64_t nbits, uint64_t dst, const uint32_t* sb,
+                                             uint32_t src, uint32_t len, uint32_t k0, uint32_t step,
+                                             uint32_t* status) {
   if (len == 0) return;
-  const int lane = threadIdx.x & 31;
   if (dst + len > nbits) {
-    if (lane == 0) atomicOr(status, kErrBounds);
+    if (k0 == 0) atomicOr(status, kErrBounds);
     return;
   }
-  uint32_t* out = reinterpret_cast<uint32_t*>(level);
-  const uint64_t qa = dst >> 5, qb = (dst + len - 1) >> 5;
-  const uint32_t lead = uint32_t(dst & 31);  // bits of chunk qa before the run
-  for (uint64_t q = qa + lane; q <= qb; q += 32) {
-    const uint32_t k = uint32_t(q - qa);  // chunk index within the run
-    uint32_t val, lo = 0;
-    if (k == 0) {
-      val = stream32(sb, src) >> lead;
-      lo = lead;
-    } else {
-      val = stream32(sb, src + 32 * k - lead);
-    }
-    const uint64_t end_in_chunk = dst + len - (q << 5);  // run bits up to the end of this chunk
-    const uint32_t hi = end_in_chunk >= 32 ? 32u : uint32_t(end_in_chunk);
-    const uint32_t mask = chunk_mask(lo, hi);
-    if (mask == 0xFFFFFFFFu) out[chunk_u32_index(q)] = val;
-    else atomicOr(&out[chunk_u32_index(q)], val & mask);
+  uint64_t* out = level + (dst >> 6);
+  const uint32_t lead = uint32_t(dst & 63);
+  const uint32_t nwords = (lead + len + 63) >> 6;
+  const uint32_t tail = (lead + len) & 63;  // bits of the last word covered (0: all 64)
+  for (uint32_t k = k0; k < nwords; k += step) {
+    uint64_t val = k ? stream64(sb, src + 64 * k - lead) : (stream64(sb, src) >> lead);
+    uint64_t mask = k ? ~0ull : (~0ull >> lead);
+    if (k == nwords - 1 && tail) mask &= ~(~0ull >> tail);
+    if (mask == ~0ull) out[k] = val;
+    else atomicOr(reinterpret_cast<unsigned long long*>(out + k), (unsigned long long)(val & mask));
   }
 }
 
@@ -336,6 +405,48 @@ __global__ void __launch_bounds__(THREADS, 4) tile_pass_kernel(TileArgs a) {
 
   const uint32_t smem_base = uint32_t(__cvta_generic_to_shared(smem_raw));
   const uint32_t shift = s_tx.shift;
+
+  // ---- counts of the finest runs (key_D), published before the splits -----
+  // Every thread counts its keys into its own column of 2^D counters in the
+  // second key buffer (free until the first split scatters into it).
+  __shared__ uint32_t s_cnt[NLB], s_wcnt[WARPS][NLB];
+  if constexpr (D >= 1) {
+    constexpr int NB = 1 << D;
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(buf0 + T);
+#pragma unroll
+    for (int b = 0; b < NB; ++b) cnt[b * THREADS + tid] = 0;
+    const uint32_t lo = shift - uint32_t(D - 1);  // field bit D-1 is level l
+    const uint32_t fmask = uint32_t(NB - 1) & (KB < 4 ? (0xFFFFFFFFu >> (32 - 8 * KB)) >> lo : 0xFFFFFFFFu);
+    const uint32_t cbase = smem_base + uint32_t(T * KB) + uint32_t(tid) * 4u;
+#pragma unroll
+    for (int r = 0; r < V; ++r) {
+      const int gv = (warp * V + r) * 32 + lane;
+      const uint4 kv = reinterpret_cast<const uint4*>(buf0)[gv];
+      const int rem = int(n) - gv * KPL;
+      const int nvv = rem >= KPL ? KPL : (rem > 0 ? rem : 0);
+      uint32_t f[KPL];
+      vector_fields<KeyT>(kv, lo, fmask, f);
+#pragma unroll
+      for (int i = 0; i < KPL; ++i)
+        if (i < nvv) asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(cbase + f[i] * uint32_t(THREADS * 4)) : "memory");
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const uint32_t x = __reduce_add_sync(0xFFFFFFFFu, cnt[b * THREADS + tid]);
+      if (lane == 0) s_wcnt[warp][b] = x;
+    }
+    __syncthreads();
+    if (tid < NB) {
+      uint32_t t = 0;
+#pragma unroll
+      for (int w = 0; w < WARPS; ++w) t += s_wcnt[w][tid];
+      const int c = int(reverse_low_bits(uint32_t(tid), uint32_t(D)));  // key_D has level l least significant
+      s_cnt[c] = t;
+      st_volatile(a.lookback + uint64_t(c) * a.tiles + g, (g == s_sg.tile0 ? kFlagPrefix : kFlagAggregate) | t);
+    }
+    // the first split's scatter into the counter area follows its barrier (A)
+  }
   // valid keys of this warp and before it
   const uint32_t wbeg = uint32_t(warp) * WSLICE;
   const uint32_t nw = n > wbeg ? min(n - wbeg, uint32_t(WSLICE)) : 0u;
@@ -448,37 +559,35 @@ __global__ void __launch_bounds__(THREADS, 4) tile_pass_kernel(TileArgs a) {
     }
   }
 
-  // ---- look-back over the finest runs, restarted per segment --------------
+  // ---- level l (one run, needs no prefix), then the look-back -------------
+  const int nstruct = s_tx.wt ? 2 : 1;
+  for (int st = 0; st < nstruct; ++st) {
+    const uint64_t dst = s_table[st ? tile_wt_entry(K, 0, 0) : tile_wm_entry(0, 0)] + tstart;
+    write_bits64(st ? s_tx.wt : s_tx.wm, s_tx.nbits, dst, sbits, 0, n, uint32_t(tid), uint32_t(THREADS), a.status);
+  }
   if constexpr (D >= 1) {
-    __syncthreads();
-    for (int c = warp; c < NLB; c += WARPS) {
-      const uint64_t p = segment_lookback(a.lookback, NLB, g, s_sg.tile0, c, rsz[D][c], a.status);
-      if (lane == 0) pre[c] = p;
-    }
+    __shared__ unsigned long long wsum[WARPS][NLB];
+    __shared__ uint32_t wmask[WARPS], s_open;
+    if (tid < NLB && s_cnt[tid] != rsz[D][tid]) atomicOr(a.status, kErrBounds);  // counts must agree
+    segment_lookback_cta<NLB, WARPS>(a.lookback, a.tiles, g, s_sg.tile0, s_cnt, pre, wsum, wmask, &s_open,
+                                     a.status);
   }
   __syncthreads();
 
-  // ---- bits of levels l..l+K-1 to the matrix and the tree ------------------
-  // item = (structure, level j, run v); warp-strided; level 0 is one run
-  constexpr int ITEMS_PER_STRUCT = (1 << K) - 1;
-  const int nstruct = s_tx.wt ? 2 : 1;
+  // ---- levels 1..K-1: one warp per (structure, level), runs in order -------
 #pragma unroll 1
-  for (int it = warp; it < nstruct * ITEMS_PER_STRUCT; it += WARPS) {
-    const int st = it / ITEMS_PER_STRUCT;
-    const int e = it % ITEMS_PER_STRUCT;  // = (1 << j) - 1 + v
-    const int j = 31 - __clz(e + 1);
-    const int v = e + 1 - (1 << j);
-    uint64_t p;  // earlier tiles of the segment with key_j == v
-    if (j == 0) {
-      p = tstart;
-    } else {
-      p = 0;
-      for (int h = 0; h < (1 << (D - j)); ++h) p += pre[v + (h << j)];
-    }
-    const uint64_t dst = s_table[st ? tile_wt_entry(K, j, v) : tile_wm_entry(j, v)] + p;
+  for (int job = warp; job < nstruct * (K - 1); job += WARPS) {
+    const int st = job / (K - 1);
+    const int j = 1 + job % (K - 1);
     uint64_t* level = (st ? s_tx.wt : s_tx.wm) + uint64_t(j) * s_tx.stride;
-    write_bit_run(level, s_tx.nbits, dst, sbits + j * SBW, rst[j][v], rsz[j][v], a.status);
+    for (int v = 0; v < (1 << j); ++v) {
+      uint64_t p = 0;  // earlier tiles of the segment with key_j == v
+      for (int h = 0; h < (1 << (D - j)); ++h) p += pre[v + (h << j)];
+      const uint64_t dst = s_table[st ? tile_wt_entry(K, j, v) : tile_wm_entry(j, v)] + p;
+      write_bits64(level, s_tx.nbits, dst, sbits + j * SBW, rst[j][v], rsz[j][v], uint32_t(lane), 32u, a.status);
+    }
   }
+  // ---- runs of S_{l+K}: spread over all warps -------------------------------
   if constexpr (OUT) {
     const KeyT* cb = buf0 + cur * T;
     for (int v = warp; v < (1 << K); v += WARPS) {
