@@ -405,8 +405,16 @@ void run_passes(pwmgpu_ctx* ctx, const void* keys, uint32_t key_bytes, uint32_t 
 // matrix levels, and its tree levels when its segments are prefix groups;
 // the remaining tree levels come from the regroup.
 // ---------------------------------------------------------------------------
+struct TileFirstPass {
+  const unsigned long long* blockpre = nullptr;
+  const uint32_t* relpre = nullptr;
+  const uint32_t* tilecnt = nullptr;
+  uint32_t tiles_per_block = 0;
+};
+
 void run_tile_passes(pwmgpu_ctx* ctx, const void* d_text, uint32_t width, uint32_t L,
-                     const std::vector<uint64_t>& hist, const LevelTables& tabs, Structure& wm, Structure* wt) {
+                     const std::vector<uint64_t>& hist, const LevelTables& tabs, Structure& wm, Structure* wt,
+                     const TileFirstPass* first = nullptr) {
   cudaStream_t s = ctx->stream;
   const uint64_t n = tabs.level_bits.empty() ? 0 : tabs.level_bits[0];
   const uint32_t T = tile_pass_elems(width);
@@ -472,6 +480,12 @@ void run_tile_passes(pwmgpu_ctx* ctx, const void* d_text, uint32_t width, uint32
     a.status = ctx->d_status;
     a.nsegs = uint32_t(p.segs.size());
     a.tiles = p.tiles;
+    if (pi == 0 && first && p.segs.size() == 1) {
+      a.blockpre = first->blockpre;
+      a.relpre = first->relpre;
+      a.tilecnt = first->tilecnt;
+      a.tiles_per_block = first->tiles_per_block;
+    }
     {
       const uint64_t structs = (wt && p.segmented) ? 2 : 1;
       ProfScope ps(ctx, "split_pass", structs * uint64_t(p.K) * (n * width + words_for(n) * 8));
@@ -523,7 +537,29 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text) {
   const uint64_t bins = uint64_t(1) << L;
   auto* d_hist = static_cast<unsigned long long*>(ctx->grow("hist", bins * 8));
   CUDA_TRY(cudaMemsetAsync(d_hist, 0, bins * 8, s));
-  {
+  // Tile engine, levels <= 8: the histogram kernel also counts the finest runs
+  // of every tile of the first pass and scans them, so that pass neither
+  // counts nor looks back.
+  TileFirstPass first{};
+  const bool tile_engine = ctx->engine == PWMGPU_ENGINE_TILE && L <= kTilePlanMaxLevels;
+  const int K0 = std::min<int>(std::min(ctx->tile_levels, kTileMaxLevels), int(L));
+  const uint32_t D0 = uint32_t(K0 < int(L) ? K0 : K0 - 1);
+  if (tile_engine && L <= 8 && D0 >= 1) {
+    const uint32_t T = tile_pass_elems(wx->width);
+    const uint64_t tiles = (n + T - 1) / T;
+    const uint32_t per = tile_hist_tiles_per_block();
+    const uint64_t nblocks = (tiles + per - 1) / per;
+    const uint64_t NB = uint64_t(1) << D0;
+    auto* base = static_cast<unsigned char*>(ctx->grow("tile_first", tiles * NB * 8 + nblocks * NB * 8 + 256));
+    first.tilecnt = reinterpret_cast<uint32_t*>(base);
+    first.relpre = first.tilecnt + tiles * NB;
+    first.blockpre = reinterpret_cast<unsigned long long*>(base + ((tiles * NB * 8 + 15) & ~uint64_t(15)));
+    first.tiles_per_block = per;
+    ProfScope ps(ctx, "leaf_histogram", n * wx->width);
+    launch_tile_histogram(d_text, n, wx->width, L, D0, T, d_hist, const_cast<uint32_t*>(first.tilecnt),
+                          const_cast<uint32_t*>(first.relpre), const_cast<unsigned long long*>(first.blockpre),
+                          ctx->d_status, s, &ctx->launches);
+  } else {
     ProfScope ps(ctx, "leaf_histogram", n * wx->width);
     launch_leaf_histogram(d_text, n, wx->width, L, d_hist, ctx->d_status, s, &ctx->launches);
   }
@@ -536,8 +572,9 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text) {
   const LevelTables tabs = build_tables_plain(hist, L, plan, want_tree);
   wx->wm.zeros = tabs.zeros;
   CUDA_TRY(cudaMemcpyAsync(wx->wm.d_zeros, wx->wm.zeros.data(), L * 8, cudaMemcpyHostToDevice, s));
-  if (ctx->engine == PWMGPU_ENGINE_TILE && L <= kTilePlanMaxLevels)
-    run_tile_passes(ctx, d_text, wx->width, L, hist, tabs, wx->wm, want_tree ? &wx->wt : nullptr);
+  if (tile_engine)
+    run_tile_passes(ctx, d_text, wx->width, L, hist, tabs, wx->wm, want_tree ? &wx->wt : nullptr,
+                    first.blockpre ? &first : nullptr);
   else
     run_passes(ctx, d_text, wx->width, wx->width, false, L, plan, tabs, wx->wm, want_tree ? &wx->wt : nullptr);
   if (wx->wm.rs && !wx->wm_internal) build_rank_select(ctx, wx->wm);

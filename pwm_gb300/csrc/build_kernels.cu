@@ -71,6 +71,109 @@ __global__ void __launch_bounds__(kHistThreads) leaf_hist_global(const T* text, 
   if (bad) atomicOr(status, kErrSymbol);
 }
 
+// Leaf histogram (levels <= 8) that also counts, per tile of the first
+// tile pass (tile_keys symbols), its finest runs: the 2^D values of the first
+// D symbol bits read with the first bit least significant.  Block b walks
+// tiles [b*tiles_per_block, ...) in order; per tile it writes the counts and
+// their prefix inside the block, at the end the block's totals.
+template <typename T>
+__global__ void __launch_bounds__(kHistThreads) tile_hist_kernel(const T* text, uint64_t n, uint32_t levels,
+                                                                 uint32_t D, uint32_t tile_keys,
+                                                                 uint32_t tiles_per_block, unsigned long long* hist,
+                                                                 uint32_t* tilecnt, uint32_t* relpre,
+                                                                 unsigned long long* blocksum, uint32_t* status) {
+  constexpr int WARPS = kHistThreads / 32;
+  constexpr int BINS = 256;
+  __shared__ uint32_t h[WARPS * BINS];
+  __shared__ uint32_t s_tc[16];
+  const int tid = threadIdx.x;
+  for (int i = tid; i < WARPS * BINS; i += kHistThreads) h[i] = 0;
+  if (tid < 16) s_tc[tid] = 0;
+  __syncthreads();
+  uint32_t* mine = h + (tid >> 5) * BINS;
+  const uint32_t bins = 1u << levels, NB = 1u << D;
+  uint32_t prev = 0;  // thread b < bins: the block's count of symbol b so far
+  uint32_t rel = 0;   // thread c < NB: the block's count of run c before the current tile
+  bool bad = false;
+  const uint64_t first_tile = uint64_t(blockIdx.x) * tiles_per_block;
+  for (uint32_t k = 0; k < tiles_per_block; ++k) {
+    const uint64_t tile = first_tile + k;
+    const uint64_t start = tile * tile_keys;
+    if (start >= n) break;
+    const uint64_t len = n - start < tile_keys ? n - start : tile_keys;
+    const T* p = text + start;
+    auto count = [&](uint32_t c) {
+      if (c >= bins) { bad = true; return; }
+      atomicAdd(&mine[c], 1u);
+    };
+    constexpr int PER = 16 / sizeof(T);
+    const uint64_t nvec = (reinterpret_cast<uintptr_t>(p) % 16 == 0) ? len / PER : 0;
+    for (uint64_t i = tid; i < nvec; i += kHistThreads) {
+      const uint4 x = __ldcs(reinterpret_cast<const uint4*>(p) + i);
+      const T* s = reinterpret_cast<const T*>(&x);
+#pragma unroll
+      for (int q = 0; q < PER; ++q) count(uint32_t(s[q]));
+    }
+    for (uint64_t i = nvec * PER + tid; i < len; i += kHistThreads) count(uint32_t(p[i]));
+    __syncthreads();
+    if (tid < int(bins)) {
+      uint32_t tot = 0;
+#pragma unroll
+      for (int w = 0; w < WARPS; ++w) tot += h[w * BINS + tid];
+      const uint32_t x = tot - prev;
+      prev = tot;
+      // run of symbol b: its top D bits, first bit least significant
+      const uint32_t run = reverse_low_bits(uint32_t(tid) >> (levels - D), D);
+      if (x) atomicAdd(&s_tc[run], x);
+    }
+    __syncthreads();
+    if (tid < int(NB)) {
+      const uint32_t c = s_tc[tid];
+      tilecnt[tile * NB + tid] = c;
+      relpre[tile * NB + tid] = rel;
+      rel += c;
+      s_tc[tid] = 0;
+    }
+    __syncthreads();
+  }
+  if (bad) atomicOr(status, kErrSymbol);
+  if (tid < int(NB)) blocksum[uint64_t(blockIdx.x) * NB + tid] = rel;
+  if (tid < int(bins) && prev) atomicAdd(&hist[tid], (unsigned long long)prev);
+}
+
+// Exclusive prefix, per column, of the nblocks x NB block totals (in place);
+// one CTA.  Thread (j, c) = (tid / NB, tid % NB) owns a contiguous chunk of
+// blocks of column c.
+__global__ void __launch_bounds__(1024) tile_block_scan_kernel(unsigned long long* blocksum, uint32_t nblocks,
+                                                               uint32_t NB) {
+  __shared__ unsigned long long part[1024];
+  const uint32_t tid = threadIdx.x, c = tid % NB, j = tid / NB, P = 1024 / NB;
+  const uint32_t chunk = (nblocks + P - 1) / P;
+  const uint32_t b0 = j * chunk, b1 = min(nblocks, b0 + chunk);
+  unsigned long long sum = 0;
+  if (j < P)
+    for (uint32_t b = b0; b < b1; ++b) sum += blocksum[uint64_t(b) * NB + c];
+  part[tid] = sum;
+  __syncthreads();
+  if (j == 0) {
+    unsigned long long run = 0;
+    for (uint32_t q = 0; q < P; ++q) {
+      const unsigned long long v = part[q * NB + c];
+      part[q * NB + c] = run;
+      run += v;
+    }
+  }
+  __syncthreads();
+  if (j < P) {
+    unsigned long long run = part[tid];
+    for (uint32_t b = b0; b < b1; ++b) {
+      const unsigned long long v = blocksum[uint64_t(b) * NB + c];
+      blocksum[uint64_t(b) * NB + c] = run;
+      run += v;
+    }
+  }
+}
+
 int hist_grid(uint64_t n, uint32_t width) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -196,6 +299,28 @@ int grid_for(uint64_t n, int threads) {
 }
 
 }  // namespace
+
+uint32_t tile_hist_tiles_per_block() { return 16; }
+
+void launch_tile_histogram(const void* text, uint64_t n, uint32_t width, uint32_t levels, uint32_t D,
+                           uint32_t tile_keys, unsigned long long* hist, uint32_t* tilecnt, uint32_t* relpre,
+                           unsigned long long* blocksum, uint32_t* status, cudaStream_t s, uint64_t* launches) {
+  if (n == 0) return;
+  const uint32_t per = tile_hist_tiles_per_block();
+  const uint64_t tiles = (n + tile_keys - 1) / tile_keys;
+  const uint32_t nblocks = uint32_t((tiles + per - 1) / per);
+  if (width == 1)
+    tile_hist_kernel<<<nblocks, kHistThreads, 0, s>>>(static_cast<const uint8_t*>(text), n, levels, D, tile_keys, per,
+                                                      hist, tilecnt, relpre, blocksum, status);
+  else if (width == 2)
+    tile_hist_kernel<<<nblocks, kHistThreads, 0, s>>>(static_cast<const uint16_t*>(text), n, levels, D, tile_keys,
+                                                      per, hist, tilecnt, relpre, blocksum, status);
+  else
+    tile_hist_kernel<<<nblocks, kHistThreads, 0, s>>>(static_cast<const uint32_t*>(text), n, levels, D, tile_keys,
+                                                      per, hist, tilecnt, relpre, blocksum, status);
+  tile_block_scan_kernel<<<1, 1024, 0, s>>>(blocksum, nblocks, 1u << D);
+  *launches += 2;
+}
 
 void launch_leaf_histogram(const void* text, uint64_t n, uint32_t width, uint32_t levels, unsigned long long* hist,
                            uint32_t* status, cudaStream_t s, uint64_t* launches) {

@@ -15,6 +15,16 @@ namespace pwmgpu {
 void launch_leaf_histogram(const void* text, uint64_t n, uint32_t width, uint32_t levels,
                            unsigned long long* hist, uint32_t* status, cudaStream_t s, uint64_t* launches);
 
+// Leaf histogram of a text with levels <= 8 that also counts, per tile of
+// tile_keys symbols, the 2^D runs of the first D symbol bits (first bit least
+// significant): tilecnt[tile][run], relpre[tile][run] (prefix inside a block
+// of tile_hist_tiles_per_block() tiles) and blocksum[block][run], which the
+// launch turns into each block's exclusive prefix.  hist must be zeroed.
+uint32_t tile_hist_tiles_per_block();
+void launch_tile_histogram(const void* text, uint64_t n, uint32_t width, uint32_t levels, uint32_t D,
+                           uint32_t tile_keys, unsigned long long* hist, uint32_t* tilecnt, uint32_t* relpre,
+                           unsigned long long* blocksum, uint32_t* status, cudaStream_t s, uint64_t* launches);
+
 // ---- split passes -----------------------------------------------------------
 // Geometry of the split pass for a key width: tile size in elements.
 uint32_t split_tile_elems(uint32_t key_bytes);

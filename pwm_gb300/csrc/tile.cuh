@@ -80,6 +80,14 @@ struct TileArgs {
   uint32_t* status;
   uint32_t nsegs;
   uint32_t tiles;
+  // Optional (first pass of a text with one segment): the finest-run counts
+  // of every tile and their exclusive prefixes, from the histogram kernel:
+  // prefix = blockpre[tile / tiles_per_block] + relpre[tile].  The pass then
+  // neither counts nor looks back.
+  const unsigned long long* blockpre;
+  const uint32_t* relpre;
+  const uint32_t* tilecnt;
+  uint32_t tiles_per_block;
 };
 
 template <typename KeyT, int K, bool OUT, int THREADS, int V>
@@ -410,7 +418,13 @@ __global__ void __launch_bounds__(THREADS, 4) tile_pass_kernel(TileArgs a) {
   // Every thread counts its keys into its own column of 2^D counters in the
   // second key buffer (free until the first split scatters into it).
   __shared__ uint32_t s_cnt[NLB], s_wcnt[WARPS][NLB];
-  if constexpr (D >= 1) {
+  const bool given = a.blockpre != nullptr;  // prefixes from the histogram kernel
+  if (D >= 1 && given) {
+    if (tid < NLB) {
+      s_cnt[tid] = a.tilecnt[uint64_t(g) * NLB + tid];
+      pre[tid] = a.blockpre[uint64_t(g / a.tiles_per_block) * NLB + tid] + a.relpre[uint64_t(g) * NLB + tid];
+    }
+  } else if constexpr (D >= 1) {
     constexpr int NB = 1 << D;
     uint32_t* cnt = reinterpret_cast<uint32_t*>(buf0 + T);
 #pragma unroll
@@ -569,16 +583,18 @@ __global__ void __launch_bounds__(THREADS, 4) tile_pass_kernel(TileArgs a) {
     __shared__ unsigned long long wsum[WARPS][NLB];
     __shared__ uint32_t wmask[WARPS], s_open;
     if (tid < NLB && s_cnt[tid] != rsz[D][tid]) atomicOr(a.status, kErrBounds);  // counts must agree
-    segment_lookback_cta<NLB, WARPS>(a.lookback, a.tiles, g, s_sg.tile0, s_cnt, pre, wsum, wmask, &s_open,
-                                     a.status);
+    if (!given)
+      segment_lookback_cta<NLB, WARPS>(a.lookback, a.tiles, g, s_sg.tile0, s_cnt, pre, wsum, wmask, &s_open,
+                                       a.status);
   }
   __syncthreads();
 
   // ---- levels 1..K-1: one warp per (structure, level), runs in order -------
+  constexpr int KI = K > 1 ? K - 1 : 1;  // inner levels (none when K == 1)
 #pragma unroll 1
   for (int job = warp; job < nstruct * (K - 1); job += WARPS) {
-    const int st = job / (K - 1);
-    const int j = 1 + job % (K - 1);
+    const int st = job / KI;
+    const int j = 1 + job % KI;
     uint64_t* level = (st ? s_tx.wt : s_tx.wm) + uint64_t(j) * s_tx.stride;
     for (int v = 0; v < (1 << j); ++v) {
       uint64_t p = 0;  // earlier tiles of the segment with key_j == v
