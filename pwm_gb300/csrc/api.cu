@@ -100,6 +100,16 @@ struct pwmgpu_ctx {
     }
     return b.p;
   }
+  // Auxiliary stream for work that overlaps the main stream (zeroing the
+  // levels of a build while its histogram runs); created on first use.
+  cudaStream_t aux = nullptr;
+  cudaEvent_t aux_ready = nullptr, aux_done = nullptr;
+  void aux_init() {
+    if (aux) return;
+    CUDA_TRY(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&aux_ready, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&aux_done, cudaEventDisableTiming));
+  }
   ~pwmgpu_ctx();
 };
 
@@ -167,6 +177,12 @@ pwmgpu_ctx::~pwmgpu_ctx() {
   for (auto& kv : scratch)
     if (kv.second.p) cudaFree(kv.second.p);
   if (d_status) cudaFree(d_status);
+  if (aux) {
+    cudaStreamSynchronize(aux);
+    cudaStreamDestroy(aux);
+    cudaEventDestroy(aux_ready);
+    cudaEventDestroy(aux_done);
+  }
   if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
@@ -414,7 +430,7 @@ struct TileFirstPass {
 
 void run_tile_passes(pwmgpu_ctx* ctx, const void* d_text, uint32_t width, uint32_t L,
                      const std::vector<uint64_t>& hist, const LevelTables& tabs, Structure& wm, Structure* wt,
-                     const TileFirstPass* first = nullptr) {
+                     const TileFirstPass* first = nullptr, bool levels_zeroed = false) {
   cudaStream_t s = ctx->stream;
   const uint64_t n = tabs.level_bits.empty() ? 0 : tabs.level_bits[0];
   const uint32_t T = tile_pass_elems(width);
@@ -454,9 +470,12 @@ void run_tile_passes(pwmgpu_ctx* ctx, const void* d_text, uint32_t width, uint32
   auto* d_blob = static_cast<unsigned char*>(ctx->grow("tile_plan", std::max<size_t>(blob.size(), 16)));
   CUDA_TRY(cudaMemcpyAsync(d_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice, s));
 
-  // runs are OR-ed into their edge chunks: zero the levels
-  CUDA_TRY(cudaMemsetAsync(wm.d_words, 0, wm.total_words * 8, s));
-  if (wt) CUDA_TRY(cudaMemsetAsync(wt->d_words, 0, wt->total_words * 8, s));
+  // runs are OR-ed into their edge words: the levels must be zero (done here
+  // unless the caller zeroed them on the auxiliary stream)
+  if (!levels_zeroed) {
+    CUDA_TRY(cudaMemsetAsync(wm.d_words, 0, wm.total_words * 8, s));
+    if (wt) CUDA_TRY(cudaMemsetAsync(wt->d_words, 0, wt->total_words * 8, s));
+  }
 
   void* ping = ctx->grow("keys_a", std::max<uint64_t>(n, 1) * width);
   void* pong = ctx->grow("keys_b", std::max<uint64_t>(n, 1) * width);
@@ -537,11 +556,21 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text) {
   const uint64_t bins = uint64_t(1) << L;
   auto* d_hist = static_cast<unsigned long long*>(ctx->grow("hist", bins * 8));
   CUDA_TRY(cudaMemsetAsync(d_hist, 0, bins * 8, s));
+  // Tile engine: zero the levels (runs are OR-ed into their edge words) on the
+  // auxiliary stream, overlapping the histogram; the passes wait for it.
+  const bool tile_engine = ctx->engine == PWMGPU_ENGINE_TILE && L <= kTilePlanMaxLevels;
+  if (tile_engine) {
+    ctx->aux_init();
+    CUDA_TRY(cudaEventRecord(ctx->aux_ready, s));  // earlier work on the structures is done first
+    CUDA_TRY(cudaStreamWaitEvent(ctx->aux, ctx->aux_ready, 0));
+    CUDA_TRY(cudaMemsetAsync(wx->wm.d_words, 0, wx->wm.total_words * 8, ctx->aux));
+    if (wx->wt.present) CUDA_TRY(cudaMemsetAsync(wx->wt.d_words, 0, wx->wt.total_words * 8, ctx->aux));
+    CUDA_TRY(cudaEventRecord(ctx->aux_done, ctx->aux));
+  }
   // Tile engine, levels <= 8: the histogram kernel also counts the finest runs
   // of every tile of the first pass and scans them, so that pass neither
   // counts nor looks back.
   TileFirstPass first{};
-  const bool tile_engine = ctx->engine == PWMGPU_ENGINE_TILE && L <= kTilePlanMaxLevels;
   const int K0 = std::min<int>(std::min(ctx->tile_levels, kTileMaxLevels), int(L));
   const uint32_t D0 = uint32_t(K0 < int(L) ? K0 : K0 - 1);
   if (tile_engine && L <= 8 && D0 >= 1) {
@@ -572,9 +601,11 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text) {
   const LevelTables tabs = build_tables_plain(hist, L, plan, want_tree);
   wx->wm.zeros = tabs.zeros;
   CUDA_TRY(cudaMemcpyAsync(wx->wm.d_zeros, wx->wm.zeros.data(), L * 8, cudaMemcpyHostToDevice, s));
-  if (tile_engine)
+  if (tile_engine) {
+    CUDA_TRY(cudaStreamWaitEvent(s, ctx->aux_done, 0));
     run_tile_passes(ctx, d_text, wx->width, L, hist, tabs, wx->wm, want_tree ? &wx->wt : nullptr,
-                    first.blockpre ? &first : nullptr);
+                    first.blockpre ? &first : nullptr, true);
+  }
   else
     run_passes(ctx, d_text, wx->width, wx->width, false, L, plan, tabs, wx->wm, want_tree ? &wx->wt : nullptr);
   if (wx->wm.rs && !wx->wm_internal) build_rank_select(ctx, wx->wm);

@@ -135,42 +135,48 @@ __device__ __forceinline__ uint32_t l1_value(const uint32_t* intra, const uint32
 }
 
 // Select-sample position inside L1 block b: the `rem`-th one (value 1) or
-// zero (value 0) counted from the block's first word, found by one warp (lane
-// = word).  pwm walks the L2 blocks and then the words of the block
-// (bin_select_popcnt.hpp:55-99); skipping whole L2 blocks first does not
-// change which word and rank it ends on, so this gives the same position.
-// rem == 0 is pwm's word_select1(first word, 0).  Returns false when the block
-// ends before the rem-th bit (pwm then takes no sample).
-__device__ __forceinline__ bool warp_block_select(const uint64_t* data, uint64_t nwords, uint64_t b, int value,
-                                                  uint32_t rem, uint64_t* pos) {
-  const int lane = threadIdx.x & 31;
-  const uint64_t w = b * kL1Cover + lane;
-  uint64_t word = w < nwords ? data[w] : 0;
-  if (value == 0) word = ~word;
-  const uint32_t pc = w < nwords ? uint32_t(__popcll(word)) : 0u;
+// zero (value 0) counted from the block's first word, found by one thread.
+// pwm walks the L2 blocks and then the words of the block
+// (bin_select_popcnt.hpp:55-99); skipping whole L2 blocks by their counts
+// first does not change which word and rank it ends on, so this gives the
+// same position.  Only words of the level count (the last block may be
+// short).  rem == 0 is pwm's word_select1(first word, 0).  Returns false when
+// the block ends before the rem-th bit (pwm then takes no sample).
+__device__ __forceinline__ bool thread_block_select(const uint64_t* data, uint64_t nwords, const uint32_t* l12,
+                                                    uint64_t b, int value, uint32_t rem, uint64_t* pos) {
+  const uint64_t w0 = b * kL1Cover;
   if (rem == 0) {
-    const uint64_t first = __shfl_sync(0xFFFFFFFFu, word, 0);
-    *pos = word_select1(first, 0) + 64 * (b * kL1Cover);
+    const uint64_t first = value ? data[w0] : ~data[w0];
+    *pos = word_select1(first, 0) + 64 * w0;
     return true;
   }
-  uint32_t incl = pc;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-    if (lane >= d) incl += y;
+  // skip whole L2 blocks (8 words) by their counts; the fourth has no field
+  uint32_t sub = 0;
+  for (; sub < 3; ++sub) {
+    const uint64_t ws = w0 + kL2Cover * sub;
+    const uint64_t left = ws >= nwords ? 0 : nwords - ws;
+    const uint32_t words = uint32_t(left < kL2Cover ? left : kL2Cover);
+    const uint32_t ones = l2_of(l12, b, sub);
+    const uint32_t cnt = value ? ones : 64u * words - ones;
+    if (rem <= cnt) break;
+    rem -= cnt;
   }
-  const uint32_t hit = __ballot_sync(0xFFFFFFFFu, incl >= rem && w < nwords);
-  if (!hit) return false;
-  const int src = __ffs(hit) - 1;
-  const uint32_t excl = __shfl_sync(0xFFFFFFFFu, incl - pc, src);
-  const uint64_t hw = __shfl_sync(0xFFFFFFFFu, word, src);
-  *pos = word_select1(hw, rem - excl) + 64 * (b * kL1Cover + src);
-  return true;
+  const uint64_t ws = w0 + kL2Cover * sub;
+  for (uint32_t k = 0; k < kL2Cover; ++k) {
+    if (ws + k >= nwords) return false;
+    const uint64_t w = value ? data[ws + k] : ~data[ws + k];
+    const uint32_t pc = uint32_t(__popcll(w));
+    if (pc >= rem) {
+      *pos = word_select1(w, rem) + 64 * (ws + k);
+      return true;
+    }
+    rem -= pc;
+  }
+  return false;
 }
 
-// Phase 3: l1 values and the select samples.  One thread decides for one L1
-// block; the blocks of a warp that take a sample are then searched one after
-// the other by the whole warp.
+// Phase 3: l1 values and the select samples, one thread per L1 block (the
+// searches of a warp's blocks are independent, so their loads overlap).
 __global__ void __launch_bounds__(kRsThreads) rs_finish_kernel(const RankSelectLevel* lv, const uint32_t* tmp,
                                                               uint64_t tmp_stride) {
   const RankSelectLevel L = lv[blockIdx.y];
@@ -178,50 +184,36 @@ __global__ void __launch_bounds__(kRsThreads) rs_finish_kernel(const RankSelectL
   const uint64_t n12 = L.nwords / kL1Cover + 1;
   const uint32_t* intra = tmp + blockIdx.y * tmp_stride;
   const uint32_t* cta_off = intra + nreal;
-  const int lane = threadIdx.x & 31;
   const uint64_t b = uint64_t(blockIdx.x) * kRsThreads + threadIdx.x;
-  if ((b & ~uint64_t(31)) >= nreal) return;  // whole warp past the level
-  bool need1 = false, need0 = false;
-  uint64_t s1 = 0, s0 = 0;
-  uint32_t rem1 = 0, rem0 = 0;
-  if (b < nreal) {
-    const uint64_t ones_before = l1_value(intra, cta_off, nreal, b);
-    L.l12[2 * b] = uint32_t(ones_before);
-    if (b == 0 && n12 > nreal) { L.l12[2 * nreal] = 0; L.l12[2 * nreal + 1] = 0; }
-    if (b + 1 < n12) {  // pwm examines blocks 0 .. n12-2
-      const uint64_t ones_through = l1_value(intra, cta_off, nreal, b + 1);
-      // sample s is taken in the first block whose running count exceeds
-      // 1 + 8192 s (bin_select_popcnt.hpp:55-99)
-      s1 = ones_before == 0 ? 0 : (ones_before - 1 + kSampleRate - 1) / kSampleRate;
-      const uint64_t next1 = 1 + kSampleRate * s1;
-      need1 = ones_through > next1;
-      rem1 = uint32_t(next1 - ones_before);
-      const uint64_t f_prev = b * kL1Bits - ones_before;
-      const uint64_t f_here = (b + 1) * kL1Bits - ones_through;
-      s0 = f_prev == 0 ? 0 : (f_prev - 1 + kSampleRate - 1) / kSampleRate;
-      const uint64_t next0 = 1 + kSampleRate * s0;
-      need0 = f_here > next0;
-      rem0 = uint32_t(next0 - f_prev);
-    }
-  }
+  if (b >= nreal) return;
+  const uint64_t ones_before = l1_value(intra, cta_off, nreal, b);
+  L.l12[2 * b] = uint32_t(ones_before);
+  if (b == 0 && n12 > nreal) { L.l12[2 * nreal] = 0; L.l12[2 * nreal + 1] = 0; }
+  if (b + 1 >= n12) return;  // pwm examines blocks 0 .. n12-2
+  const uint64_t ones_through = l1_value(intra, cta_off, nreal, b + 1);
+  // sample s is taken in the first block whose running count exceeds
+  // 1 + 8192 s (bin_select_popcnt.hpp:55-99)
+  const uint64_t s1 = ones_before == 0 ? 0 : (ones_before - 1 + kSampleRate - 1) / kSampleRate;
+  const uint64_t next1 = 1 + kSampleRate * s1;
+  const bool need1 = ones_through > next1;
+  const uint64_t f_prev = b * kL1Bits - ones_before;
+  const uint64_t f_here = (b + 1) * kL1Bits - ones_through;
+  const uint64_t s0 = f_prev == 0 ? 0 : (f_prev - 1 + kSampleRate - 1) / kSampleRate;
+  const uint64_t next0 = 1 + kSampleRate * s0;
+  const bool need0 = f_here > next0;
   bool got1 = false, got0 = false;
-  for (int value = 1; value >= 0; --value) {
-    uint32_t todo = __ballot_sync(0xFFFFFFFFu, value ? need1 : need0);
-    while (todo) {
-      const int src = __ffs(todo) - 1;
-      todo &= todo - 1;
-      const uint64_t bb = __shfl_sync(0xFFFFFFFFu, b, src);
-      const uint32_t rr = __shfl_sync(0xFFFFFFFFu, value ? rem1 : rem0, src);
-      const uint64_t ss = __shfl_sync(0xFFFFFFFFu, value ? s1 : s0, src);
-      uint64_t pos;
-      const bool ok = warp_block_select(L.data, L.nwords, bb, value, rr, &pos);
-      if (ok && lane == 0) (value ? L.s1 : L.s0)[ss] = uint32_t(pos);
-      if (lane == src) (value ? got1 : got0) = ok;
-    }
+  uint64_t pos;
+  if (need1 && thread_block_select(L.data, L.nwords, L.l12, b, 1, uint32_t(next1 - ones_before), &pos)) {
+    L.s1[s1] = uint32_t(pos);
+    got1 = true;
+  }
+  if (need0 && thread_block_select(L.data, L.nwords, L.l12, b, 0, uint32_t(next0 - f_prev), &pos)) {
+    L.s0[s0] = uint32_t(pos);
+    got0 = true;
   }
   // samples are taken in block order, so the count is fixed by the last
   // block pwm examines (n12 - 2): the samples before it plus its own
-  if (n12 >= 2 && b == n12 - 2) {
+  if (b == n12 - 2) {
     L.meta[1] = s1 + (got1 ? 1 : 0);
     L.meta[0] = s0 + (got0 ? 1 : 0);
   }
