@@ -96,25 +96,50 @@ __global__ void __launch_bounds__(kHistThreads) tile_hist_kernel(const T* text, 
   uint32_t rel = 0;   // thread c < NB: the block's count of run c before the current tile
   bool bad = false;
   const uint64_t first_tile = uint64_t(blockIdx.x) * tiles_per_block;
+  auto count = [&](uint32_t c) {
+    if (c >= bins) { bad = true; return; }
+    atomicAdd(&mine[c], 1u);
+  };
+  constexpr int PER = 16 / sizeof(T);
+  // whole aligned tiles of 16 KB: two 16-byte vectors per thread, loaded one
+  // tile ahead so that the loads overlap the counting of the previous tile
+  const bool vec = tile_keys * sizeof(T) == 2 * 16 * kHistThreads && (reinterpret_cast<uintptr_t>(text) % 16) == 0;
+  auto full_tile = [&](uint64_t tile) { return vec && (tile + 1) * tile_keys <= n; };
+  uint4 ahead[2];
+  if (full_tile(first_tile)) {
+    const uint4* p = reinterpret_cast<const uint4*>(text + first_tile * tile_keys);
+    ahead[0] = __ldcs(p + tid);
+    ahead[1] = __ldcs(p + tid + kHistThreads);
+  }
   for (uint32_t k = 0; k < tiles_per_block; ++k) {
     const uint64_t tile = first_tile + k;
     const uint64_t start = tile * tile_keys;
     if (start >= n) break;
     const uint64_t len = n - start < tile_keys ? n - start : tile_keys;
     const T* p = text + start;
-    auto count = [&](uint32_t c) {
-      if (c >= bins) { bad = true; return; }
-      atomicAdd(&mine[c], 1u);
-    };
-    constexpr int PER = 16 / sizeof(T);
-    const uint64_t nvec = (reinterpret_cast<uintptr_t>(p) % 16 == 0) ? len / PER : 0;
-    for (uint64_t i = tid; i < nvec; i += kHistThreads) {
-      const uint4 x = __ldcs(reinterpret_cast<const uint4*>(p) + i);
-      const T* s = reinterpret_cast<const T*>(&x);
+    if (full_tile(tile)) {
+      const uint4 cur[2] = {ahead[0], ahead[1]};
+      if (k + 1 < tiles_per_block && full_tile(tile + 1)) {
+        const uint4* q = reinterpret_cast<const uint4*>(text + (tile + 1) * tile_keys);
+        ahead[0] = __ldcs(q + tid);
+        ahead[1] = __ldcs(q + tid + kHistThreads);
+      }
 #pragma unroll
-      for (int q = 0; q < PER; ++q) count(uint32_t(s[q]));
+      for (int v = 0; v < 2; ++v) {
+        const T* s = reinterpret_cast<const T*>(&cur[v]);
+#pragma unroll
+        for (int q = 0; q < PER; ++q) count(uint32_t(s[q]));
+      }
+    } else {
+      const uint64_t nvec = (reinterpret_cast<uintptr_t>(p) % 16 == 0) ? len / PER : 0;
+      for (uint64_t i = tid; i < nvec; i += kHistThreads) {
+        const uint4 x = __ldcs(reinterpret_cast<const uint4*>(p) + i);
+        const T* s = reinterpret_cast<const T*>(&x);
+#pragma unroll
+        for (int q = 0; q < PER; ++q) count(uint32_t(s[q]));
+      }
+      for (uint64_t i = nvec * PER + tid; i < len; i += kHistThreads) count(uint32_t(p[i]));
     }
-    for (uint64_t i = nvec * PER + tid; i < len; i += kHistThreads) count(uint32_t(p[i]));
     __syncthreads();
     if (tid < int(bins)) {
       uint32_t tot = 0;

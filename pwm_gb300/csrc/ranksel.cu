@@ -25,8 +25,11 @@ __device__ __forceinline__ uint32_t l2_of(const uint32_t* l12, uint64_t e, uint3
   return (l12[2 * e + 1] >> (10 * i)) & 1023u;
 }
 
-// Phase 1: per L1 block popcounts (warp per block), l2 fields, and the
-// exclusive prefix of block totals inside each CTA (256 blocks per CTA).
+// Phase 1: per L1 block popcounts, l2 fields, and the exclusive prefix of
+// block totals inside each CTA (256 blocks per CTA).  Warp w reads its 32
+// blocks (8 KB) with coalesced 16-byte loads: in step i, lanes 0-15 read
+// block 2i and lanes 16-31 block 2i+1, four lanes per 512-bit L2 block; the
+// counts are then gathered so that lane b holds block b's.
 __global__ void __launch_bounds__(kRsThreads) rs_blocks_kernel(const RankSelectLevel* lv, uint32_t* tmp,
                                                               uint64_t tmp_stride) {
   const RankSelectLevel L = lv[blockIdx.y];
@@ -38,25 +41,33 @@ __global__ void __launch_bounds__(kRsThreads) rs_blocks_kernel(const RankSelectL
   __shared__ uint32_t tot[kRsThreads];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   {
-    // one thread per L1 block: 32 words as 16 independent 16-byte loads
-    const uint64_t blk = first + threadIdx.x;
+    const uint64_t wb = first + 32 * uint64_t(warp);  // first block of this warp
+    const uint64_t ww = wb * kL1Cover;                 // first word of this warp
+    // 16-byte loads when the warp's words are all in the level and aligned
+    const bool full = ww + 32 * kL1Cover <= L.nwords && (reinterpret_cast<uintptr_t>(L.data) & 15) == 0;
     uint32_t l2[4] = {0, 0, 0, 0};
-    if (blk < nreal) {
-      const uint64_t w0 = blk * kL1Cover;
-      if (w0 + kL1Cover <= L.nwords) {
-        const uint4* p = reinterpret_cast<const uint4*>(L.data + w0);
-        uint4 v[16];
-#pragma unroll
-        for (int i = 0; i < 16; ++i) v[i] = __ldcs(p + i);
-#pragma unroll
-        for (int i = 0; i < 16; ++i)
-          l2[i >> 2] += __popc(v[i].x) + __popc(v[i].y) + __popc(v[i].z) + __popc(v[i].w);
+#pragma unroll 4
+    for (int i = 0; i < 16; ++i) {
+      const uint64_t w = ww + 2 * uint64_t(i * 32 + lane);  // first of this lane's two words
+      uint32_t c;
+      if (full) {
+        const uint4 v = __ldcs(reinterpret_cast<const uint4*>(L.data + w));
+        c = __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
       } else {
-        for (uint64_t w = w0; w < L.nwords; ++w) l2[(w - w0) >> 3] += __popcll(L.data[w]);
+        c = (w < L.nwords ? __popcll(L.data[w]) : 0) + (w + 1 < L.nwords ? __popcll(L.data[w + 1]) : 0);
       }
-      L.l12[2 * blk + 1] = (l2[0] & 1023u) | ((l2[1] & 1023u) << 10) | ((l2[2] & 1023u) << 20);
+      c += __shfl_xor_sync(0xFFFFFFFFu, c, 1);
+      c += __shfl_xor_sync(0xFFFFFFFFu, c, 2);
+      // lane 2i takes block 2i's four counts (lanes 0,4,8,12), lane 2i+1 block 2i+1's (16,20,24,28)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const uint32_t x = __shfl_sync(0xFFFFFFFFu, c, (lane & 1) * 16 + 4 * k);
+        if ((lane >> 1) == i) l2[k] = x;
+      }
     }
-    tot[threadIdx.x] = l2[0] + l2[1] + l2[2] + l2[3];
+    const uint64_t blk = wb + lane;
+    if (blk < nreal) L.l12[2 * blk + 1] = (l2[0] & 1023u) | ((l2[1] & 1023u) << 10) | ((l2[2] & 1023u) << 20);
+    tot[threadIdx.x] = blk < nreal ? l2[0] + l2[1] + l2[2] + l2[3] : 0u;
   }
   // exclusive scan of the 256 block totals (u32, wrapping)
   uint32_t v = tot[threadIdx.x];
