@@ -34,8 +34,8 @@
 //     (restarted at every segment's first tile; counter-major state, one
 //     coalesced load per counter, 256 predecessors per round trip);
 //   * writes every run of every level to the matrix and the tree at
-//     table start + look-back prefix in 64-bit words (one warp per structure
-//     and level), and the runs of S_{l+K} to the next pass's input.
+//     table start + look-back prefix in 64-bit words, and the runs of
+//     S_{l+K} to the next pass's input (one warp per run, round-robin).
 #pragma once
 
 #include "common.cuh"
@@ -589,25 +589,27 @@ __global__ void __launch_bounds__(THREADS, 4) tile_pass_kernel(TileArgs a) {
   }
   __syncthreads();
 
-  // ---- levels 1..K-1: one warp per (structure, level), runs in order -------
-  constexpr int KI = K > 1 ? K - 1 : 1;  // inner levels (none when K == 1)
-#pragma unroll 1
-  for (int job = warp; job < nstruct * (K - 1); job += WARPS) {
-    const int st = job / KI;
-    const int j = 1 + job % KI;
-    uint64_t* level = (st ? s_tx.wt : s_tx.wm) + uint64_t(j) * s_tx.stride;
-    for (int v = 0; v < (1 << j); ++v) {
-      uint64_t p = 0;  // earlier tiles of the segment with key_j == v
-      for (int h = 0; h < (1 << (D - j)); ++h) p += pre[v + (h << j)];
-      const uint64_t dst = s_table[st ? tile_wt_entry(K, j, v) : tile_wm_entry(j, v)] + p;
-      write_bits64(level, s_tx.nbits, dst, sbits + j * SBW, rst[j][v], rsz[j][v], uint32_t(lane), 32u, a.status);
-    }
+  // ---- runs of S_{l+K} and of levels 1..K-1, round-robin over the warps ---
+  // prefix of run v of key_j (j >= 1): the finest runs with key_j == v
+  __shared__ unsigned long long runpre[(1 << K)];
+  constexpr int NINNER = (1 << K) - 2;  // runs of levels 1..K-1 of one structure
+  if (tid < NINNER) {
+    int j = 1;
+    while (tid + 2 >= (2 << j)) ++j;
+    const int v = tid + 2 - (1 << j);
+    uint64_t p = 0;
+    for (int h = 0; h < (1 << (D - j)); ++h) p += pre[v + (h << j)];
+    runpre[tid] = p;
   }
-  // ---- runs of S_{l+K}: spread over all warps -------------------------------
-  if constexpr (OUT) {
-    const KeyT* cb = buf0 + cur * T;
-    for (int v = warp; v < (1 << K); v += WARPS) {
-      const uint32_t len = rsz[K][v];
+  __syncthreads();
+  constexpr int NOUT = OUT ? (1 << K) : 0;
+  const int items = NOUT + nstruct * NINNER;
+  const KeyT* cb = buf0 + cur * T;
+#pragma unroll 1
+  for (int it = warp; it < items; it += WARPS) {
+    if (it < NOUT) {
+      const int v = it;
+      const uint32_t len = rsz[D][v];
       if (len == 0) continue;
       const uint64_t dst = s_table[tile_out_entry(K, v)] + pre[v];
       if (dst + len > a.out_size) {
@@ -615,7 +617,16 @@ __global__ void __launch_bounds__(THREADS, 4) tile_pass_kernel(TileArgs a) {
         continue;
       }
       write_key_run(reinterpret_cast<unsigned char*>(static_cast<KeyT*>(a.out) + dst),
-                    reinterpret_cast<const unsigned char*>(cb + rst[K][v]), len * uint32_t(KB));
+                    reinterpret_cast<const unsigned char*>(cb + rst[D][v]), len * uint32_t(KB));
+    } else {
+      const int e = (it - NOUT) % (NINNER > 0 ? NINNER : 1);
+      const int st = (it - NOUT) / (NINNER > 0 ? NINNER : 1);
+      int j = 1;
+      while (e + 2 >= (2 << j)) ++j;
+      const int v = e + 2 - (1 << j);
+      uint64_t* level = (st ? s_tx.wt : s_tx.wm) + uint64_t(j) * s_tx.stride;
+      const uint64_t dst = s_table[st ? tile_wt_entry(K, j, v) : tile_wm_entry(j, v)] + runpre[e];
+      write_bits64(level, s_tx.nbits, dst, sbits + j * SBW, rst[j][v], rsz[j][v], uint32_t(lane), 32u, a.status);
     }
   }
 }
