@@ -103,12 +103,13 @@ struct pwmgpu_ctx {
   // Auxiliary stream for work that overlaps the main stream (zeroing the
   // levels of a build while its histogram runs); created on first use.
   cudaStream_t aux = nullptr;
-  cudaEvent_t aux_ready = nullptr, aux_done = nullptr;
+  cudaEvent_t aux_ready = nullptr, aux_done = nullptr, aux_done2 = nullptr;
   void aux_init() {
     if (aux) return;
     CUDA_TRY(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreateWithFlags(&aux_ready, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&aux_done, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&aux_done2, cudaEventDisableTiming));
   }
   ~pwmgpu_ctx();
 };
@@ -182,6 +183,7 @@ pwmgpu_ctx::~pwmgpu_ctx() {
     cudaStreamDestroy(aux);
     cudaEventDestroy(aux_ready);
     cudaEventDestroy(aux_done);
+    cudaEventDestroy(aux_done2);
   }
   if (own_stream && stream) cudaStreamDestroy(stream);
 }
@@ -430,7 +432,8 @@ struct TileFirstPass {
 
 void run_tile_passes(pwmgpu_ctx* ctx, const void* d_text, uint32_t width, uint32_t L,
                      const std::vector<uint64_t>& hist, const LevelTables& tabs, Structure& wm, Structure* wt,
-                     const TileFirstPass* first = nullptr, bool levels_zeroed = false) {
+                     const TileFirstPass* first = nullptr, bool levels_zeroed = false,
+                     cudaEvent_t deeper_zeroed = nullptr) {
   cudaStream_t s = ctx->stream;
   const uint64_t n = tabs.level_bits.empty() ? 0 : tabs.level_bits[0];
   const uint32_t T = tile_pass_elems(width);
@@ -487,6 +490,7 @@ void run_tile_passes(pwmgpu_ctx* ctx, const void* d_text, uint32_t width, uint32
     const uint64_t lb_bytes = uint64_t(std::max<uint32_t>(p.tiles, 1)) * nlb * 8;
     auto* lb = static_cast<unsigned long long*>(ctx->grow("lookback", lb_bytes + 64));
     CUDA_TRY(cudaMemsetAsync(lb, 0, lb_bytes + 64, s));
+    if (pi == 1 && deeper_zeroed) CUDA_TRY(cudaStreamWaitEvent(s, deeper_zeroed, 0));
     TileArgs a{};
     a.in = in;
     a.out = p.out ? (in == ping ? pong : ping) : nullptr;
@@ -559,13 +563,29 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text) {
   // Tile engine: zero the levels (runs are OR-ed into their edge words) on the
   // auxiliary stream, overlapping the histogram; the passes wait for it.
   const bool tile_engine = ctx->engine == PWMGPU_ENGINE_TILE && L <= kTilePlanMaxLevels;
+  // Level 0 is written in whole words by the first pass (its tiles start at
+  // multiples of 64 bits): only its padding words need zeroing.  The levels of
+  // the first pass are zeroed while the histogram runs, the deeper ones while
+  // the first pass runs.
+  const int Kz = std::min<int>(std::min(ctx->tile_levels, kTileMaxLevels), int(L));
   if (tile_engine) {
     ctx->aux_init();
     CUDA_TRY(cudaEventRecord(ctx->aux_ready, s));  // earlier work on the structures is done first
     CUDA_TRY(cudaStreamWaitEvent(ctx->aux, ctx->aux_ready, 0));
-    CUDA_TRY(cudaMemsetAsync(wx->wm.d_words, 0, wx->wm.total_words * 8, ctx->aux));
-    if (wx->wt.present) CUDA_TRY(cudaMemsetAsync(wx->wt.d_words, 0, wx->wt.total_words * 8, ctx->aux));
+    auto zero = [&](Structure& st, uint32_t l0, uint32_t l1) {
+      if (l1 > l0) CUDA_TRY(cudaMemsetAsync(st.d_words + st.offs[l0], 0, (st.offs[l1 - 1] - st.offs[l0] +
+                                                                        padded_words(st.bits[l1 - 1])) * 8, ctx->aux));
+    };
+    for (Structure* st : {&wx->wm, &wx->wt}) {
+      if (!st->present) continue;
+      const uint64_t real = words_for(st->bits[0]), pad = padded_words(st->bits[0]);
+      if (pad > real) CUDA_TRY(cudaMemsetAsync(st->d_words + real, 0, (pad - real) * 8, ctx->aux));
+      zero(*st, 1, uint32_t(Kz));
+    }
     CUDA_TRY(cudaEventRecord(ctx->aux_done, ctx->aux));
+    for (Structure* st : {&wx->wm, &wx->wt})
+      if (st->present) zero(*st, uint32_t(Kz), L);
+    CUDA_TRY(cudaEventRecord(ctx->aux_done2, ctx->aux));
   }
   // Tile engine, levels <= 8: the histogram kernel also counts the finest runs
   // of every tile of the first pass and scans them, so that pass neither
@@ -603,6 +623,7 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text) {
   CUDA_TRY(cudaMemcpyAsync(wx->wm.d_zeros, wx->wm.zeros.data(), L * 8, cudaMemcpyHostToDevice, s));
   if (tile_engine) {
     CUDA_TRY(cudaStreamWaitEvent(s, ctx->aux_done, 0));
+    CUDA_TRY(cudaStreamWaitEvent(s, ctx->aux_done2, 0));
     run_tile_passes(ctx, d_text, wx->width, L, hist, tabs, wx->wm, want_tree ? &wx->wt : nullptr,
                     first.blockpre ? &first : nullptr, true);
   }

@@ -284,7 +284,8 @@ __device__ __forceinline__ uint64_t stream64(const uint32_t* sb, uint32_t x) {
 
 // Stream bits [src, src+len) to level bits [dst, dst+len), 64-bit words
 // k = k0, k0 + step, ... of the destination range: whole words are stored,
-// words shared with other runs are OR-ed (the level was zeroed).
+// and so is the level's last word when this run fills it up to the level's
+// end; words shared with other runs are OR-ed (those were zeroed).
 __device__ __forceinline__ void write_bits64(uint64_t* level, uint64_t nbits, uint64_t dst, const uint32_t* sb,
                                              uint32_t src, uint32_t len, uint32_t k0, uint32_t step,
                                              uint32_t* status) {
@@ -297,18 +298,20 @@ __device__ __forceinline__ void write_bits64(uint64_t* level, uint64_t nbits, ui
   const uint32_t lead = uint32_t(dst & 63);
   const uint32_t nwords = (lead + len + 63) >> 6;
   const uint32_t tail = (lead + len) & 63;  // bits of the last word covered (0: all 64)
+  const bool at_end = dst + len == nbits;   // the run ends the level: the rest of its last word is padding
   for (uint32_t k = k0; k < nwords; k += step) {
     uint64_t val = k ? stream64(sb, src + 64 * k - lead) : (stream64(sb, src) >> lead);
     uint64_t mask = k ? ~0ull : (~0ull >> lead);
-    if (k == nwords - 1 && tail) mask &= ~(~0ull >> tail);
-    if (mask == ~0ull) out[k] = val;
+    const bool last = k == nwords - 1;
+    if (last && tail) mask &= ~(~0ull >> tail);
+    if (mask == ~0ull || (last && at_end && (k || !lead))) out[k] = val & mask;
     else atomicOr(reinterpret_cast<unsigned long long*>(out + k), (unsigned long long)(val & mask));
   }
 }
 
 // One warp copies `len` bytes from shared memory to global memory: byte
-// stores up to a 4-byte aligned destination, then 32-bit stores built from
-// funnel-shifted aligned shared words, then the tail.
+// stores up to a 4-byte aligned destination, then 32-bit stores whose source
+// bytes are funnel-shifted out of aligned shared words, then the tail.
 __device__ __forceinline__ void write_key_run(unsigned char* dst, const unsigned char* src, uint32_t len) {
   const int lane = threadIdx.x & 31;
   const uint32_t head = min(len, uint32_t((4 - (reinterpret_cast<uintptr_t>(dst) & 3)) & 3));
