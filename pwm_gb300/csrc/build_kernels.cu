@@ -76,18 +76,20 @@ __global__ void __launch_bounds__(kHistThreads) leaf_hist_global(const T* text, 
 // D symbol bits read with the first bit least significant.  Block b walks
 // tiles [b*tiles_per_block, ...) in order; per tile it writes the counts and
 // their prefix inside the block, at the end the block's totals.
+constexpr int kTileHistThreads = 256;
+
 template <typename T>
-__global__ void __launch_bounds__(kHistThreads) tile_hist_kernel(const T* text, uint64_t n, uint32_t levels,
+__global__ void __launch_bounds__(kTileHistThreads) tile_hist_kernel(const T* text, uint64_t n, uint32_t levels,
                                                                  uint32_t D, uint32_t tile_keys,
                                                                  uint32_t tiles_per_block, unsigned long long* hist,
                                                                  uint32_t* tilecnt, uint32_t* relpre,
                                                                  unsigned long long* blocksum, uint32_t* status) {
-  constexpr int WARPS = kHistThreads / 32;
+  constexpr int WARPS = kTileHistThreads / 32;
   constexpr int BINS = 256;
   __shared__ uint32_t h[WARPS * BINS];
   __shared__ uint32_t s_tc[16];
   const int tid = threadIdx.x;
-  for (int i = tid; i < WARPS * BINS; i += kHistThreads) h[i] = 0;
+  for (int i = tid; i < WARPS * BINS; i += kTileHistThreads) h[i] = 0;
   if (tid < 16) s_tc[tid] = 0;
   __syncthreads();
   uint32_t* mine = h + (tid >> 5) * BINS;
@@ -101,15 +103,20 @@ __global__ void __launch_bounds__(kHistThreads) tile_hist_kernel(const T* text, 
     atomicAdd(&mine[c], 1u);
   };
   constexpr int PER = 16 / sizeof(T);
-  // whole aligned tiles of 16 KB: two 16-byte vectors per thread, loaded one
-  // tile ahead so that the loads overlap the counting of the previous tile
-  const bool vec = tile_keys * sizeof(T) == 2 * 16 * kHistThreads && (reinterpret_cast<uintptr_t>(text) % 16) == 0;
+  // whole aligned tiles of HV 16-byte vectors per thread, loaded one tile
+  // ahead so that the loads overlap the counting of the previous tile
+  constexpr int HV = 4;
+  const uint32_t tile_vecs = uint32_t(tile_keys * sizeof(T) / 16);
+  const bool vec = tile_keys * sizeof(T) % (16 * kTileHistThreads) == 0 && tile_vecs <= HV * kTileHistThreads &&
+                   (reinterpret_cast<uintptr_t>(text) % 16) == 0;
+  const int nv = int(tile_vecs / kTileHistThreads);  // vectors per thread (1..HV)
   auto full_tile = [&](uint64_t tile) { return vec && (tile + 1) * tile_keys <= n; };
-  uint4 ahead[2];
+  uint4 ahead[HV];
   if (full_tile(first_tile)) {
     const uint4* p = reinterpret_cast<const uint4*>(text + first_tile * tile_keys);
-    ahead[0] = __ldcs(p + tid);
-    ahead[1] = __ldcs(p + tid + kHistThreads);
+#pragma unroll
+    for (int v = 0; v < HV; ++v)
+      if (v < nv) ahead[v] = __ldcs(p + tid + v * kTileHistThreads);
   }
   for (uint32_t k = 0; k < tiles_per_block; ++k) {
     const uint64_t tile = first_tile + k;
@@ -118,27 +125,31 @@ __global__ void __launch_bounds__(kHistThreads) tile_hist_kernel(const T* text, 
     const uint64_t len = n - start < tile_keys ? n - start : tile_keys;
     const T* p = text + start;
     if (full_tile(tile)) {
-      const uint4 cur[2] = {ahead[0], ahead[1]};
+      uint4 cur[HV];
+#pragma unroll
+      for (int v = 0; v < HV; ++v) cur[v] = ahead[v];
       if (k + 1 < tiles_per_block && full_tile(tile + 1)) {
         const uint4* q = reinterpret_cast<const uint4*>(text + (tile + 1) * tile_keys);
-        ahead[0] = __ldcs(q + tid);
-        ahead[1] = __ldcs(q + tid + kHistThreads);
+#pragma unroll
+        for (int v = 0; v < HV; ++v)
+          if (v < nv) ahead[v] = __ldcs(q + tid + v * kTileHistThreads);
       }
 #pragma unroll
-      for (int v = 0; v < 2; ++v) {
+      for (int v = 0; v < HV; ++v) {
+        if (v >= nv) break;
         const T* s = reinterpret_cast<const T*>(&cur[v]);
 #pragma unroll
         for (int q = 0; q < PER; ++q) count(uint32_t(s[q]));
       }
     } else {
       const uint64_t nvec = (reinterpret_cast<uintptr_t>(p) % 16 == 0) ? len / PER : 0;
-      for (uint64_t i = tid; i < nvec; i += kHistThreads) {
+      for (uint64_t i = tid; i < nvec; i += kTileHistThreads) {
         const uint4 x = __ldcs(reinterpret_cast<const uint4*>(p) + i);
         const T* s = reinterpret_cast<const T*>(&x);
 #pragma unroll
         for (int q = 0; q < PER; ++q) count(uint32_t(s[q]));
       }
-      for (uint64_t i = nvec * PER + tid; i < len; i += kHistThreads) count(uint32_t(p[i]));
+      for (uint64_t i = nvec * PER + tid; i < len; i += kTileHistThreads) count(uint32_t(p[i]));
     }
     __syncthreads();
     if (tid < int(bins)) {
@@ -335,13 +346,13 @@ void launch_tile_histogram(const void* text, uint64_t n, uint32_t width, uint32_
   const uint64_t tiles = (n + tile_keys - 1) / tile_keys;
   const uint32_t nblocks = uint32_t((tiles + per - 1) / per);
   if (width == 1)
-    tile_hist_kernel<<<nblocks, kHistThreads, 0, s>>>(static_cast<const uint8_t*>(text), n, levels, D, tile_keys, per,
+    tile_hist_kernel<<<nblocks, kTileHistThreads, 0, s>>>(static_cast<const uint8_t*>(text), n, levels, D, tile_keys, per,
                                                       hist, tilecnt, relpre, blocksum, status);
   else if (width == 2)
-    tile_hist_kernel<<<nblocks, kHistThreads, 0, s>>>(static_cast<const uint16_t*>(text), n, levels, D, tile_keys,
+    tile_hist_kernel<<<nblocks, kTileHistThreads, 0, s>>>(static_cast<const uint16_t*>(text), n, levels, D, tile_keys,
                                                       per, hist, tilecnt, relpre, blocksum, status);
   else
-    tile_hist_kernel<<<nblocks, kHistThreads, 0, s>>>(static_cast<const uint32_t*>(text), n, levels, D, tile_keys,
+    tile_hist_kernel<<<nblocks, kTileHistThreads, 0, s>>>(static_cast<const uint32_t*>(text), n, levels, D, tile_keys,
                                                       per, hist, tilecnt, relpre, blocksum, status);
   tile_block_scan_kernel<<<1, 1024, 0, s>>>(blocksum, nblocks, 1u << D);
   *launches += 2;

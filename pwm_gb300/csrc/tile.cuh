@@ -362,7 +362,7 @@ __device__ __forceinline__ void load_tile_bytes(uint4* dst, const unsigned char*
 }
 
 template <typename KeyT, int K, bool OUT, int THREADS, int V>
-__global__ void __launch_bounds__(THREADS, 4) tile_pass_kernel(TileArgs a) {
+__global__ void __launch_bounds__(THREADS, 1024 / THREADS) tile_pass_kernel(TileArgs a) {
   using C = TileCfg<KeyT, K, OUT, THREADS, V>;
   constexpr int D = C::D, KPL = C::KPL, T = C::T, WARPS = C::WARPS, WSLICE = C::WSLICE, SBW = C::SBW;
   constexpr int NLB = C::NLB, LPC = C::LPC;
