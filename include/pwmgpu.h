@@ -99,6 +99,12 @@ PWMGPU_API pwmgpu_status pwmgpu_ctx_set_pass_levels(pwmgpu_ctx* ctx, int levels_
  * warp-autonomous split passes that write the matrix, with the tree levels
  * regrouped from it (every plain build; Huffman builds and batches always use
  * it).  Both give identical structures. */
+/* Stream-ordered device allocations (cudaMallocAsync / cudaFreeAsync on the
+ * context's stream) for the structures and scratch of this context: freeing
+ * does not synchronise the device, so contexts on other streams keep running.
+ * Freed memory stays in the process's default pool. */
+PWMGPU_API pwmgpu_status pwmgpu_ctx_set_stream_ordered_alloc(pwmgpu_ctx* ctx, int enable);
+
 #define PWMGPU_ENGINE_TILE 0
 #define PWMGPU_ENGINE_WARP 1
 PWMGPU_API pwmgpu_status pwmgpu_ctx_set_engine(pwmgpu_ctx* ctx, int engine);
@@ -181,7 +187,68 @@ PWMGPU_API pwmgpu_status pwmgpu_wx_rank_select_blocks(pwmgpu_ctx* ctx, const pwm
  * SELECT(symbol a[i], occurrence b[i]).  Needs PWMGPU_RANK_SELECT. */
 PWMGPU_API pwmgpu_status pwmgpu_wx_query(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which, int op, const uint64_t* d_a,
                                          const uint64_t* d_b, uint64_t count, uint64_t* d_out);
+/* The same on host arrays, through the context's scratch and stream;
+ * returns when out[] holds the answers. */
+PWMGPU_API pwmgpu_status pwmgpu_wx_query_host(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which, int op,
+                                              const uint64_t* a, const uint64_t* b, uint64_t count, uint64_t* out);
 PWMGPU_API void pwmgpu_wx_free(pwmgpu_wx* wx);
+
+/* ---------------------------------------------------------------------- */
+/* Serving: continuous batching over device-resident structures            */
+/* ---------------------------------------------------------------------- */
+/* A server runs `slots` worker threads, each with its own context and CUDA
+ * stream.  Requests wait in one FIFO queue; the head is admitted when a slot
+ * is idle and its device bytes fit the HBM budget beside the resident
+ * structures and the requests in flight, so admitted requests overlap on the
+ * device.  A build request copies its text, builds the structure(s) with
+ * rank/select support, answers its first query batch and leaves the
+ * structure resident until pwmgpu_server_release; query requests answer
+ * further batches against a resident structure.  Answers are those of the
+ * same calls made alone (pwmgpu_wx_create / _build_host / _query_host). */
+typedef struct pwmgpu_server pwmgpu_server;
+typedef struct {
+  const void* text;          /* host symbols; valid until the request is done */
+  uint64_t size;             /* symbols (>= 1) */
+  uint32_t word_width;       /* 1, 2 or 4 */
+  uint32_t levels;           /* 1..24 */
+  uint32_t shape_flags;      /* PWMGPU_MATRIX and/or PWMGPU_TREE (rank/select implied) */
+  uint32_t query_structure;  /* 0: the matrix answers the queries, 1: the tree */
+  uint64_t nqueries;
+  const uint8_t* query_ops;  /* PWMGPU_Q_ACCESS / _RANK / _SELECT per query */
+  const uint64_t* query_a;   /* access: position; rank, select: symbol */
+  const uint64_t* query_b;   /* rank: position; select: occurrence; NULL if only accesses */
+  uint64_t* results;         /* host: nqueries answers, valid once the request is done */
+} pwmgpu_request;
+typedef struct {
+  uint64_t id;
+  int status;                /* pwmgpu_status of the request */
+  uint32_t slot;             /* worker that ran it */
+  double submit_s, start_s, done_s;  /* seconds since the server started */
+  uint64_t device_bytes;     /* resident bytes the request holds (build requests) */
+} pwmgpu_request_info;
+typedef struct {
+  uint64_t budget_bytes, in_use_bytes, peak_bytes;
+  uint64_t queued, running, completed;
+} pwmgpu_server_stats_t;
+
+PWMGPU_API pwmgpu_status pwmgpu_server_create(int device, uint64_t hbm_budget_bytes, uint32_t slots,
+                                              pwmgpu_server** out);
+/* ERR_OOM when the request can never fit the budget. */
+PWMGPU_API pwmgpu_status pwmgpu_server_submit(pwmgpu_server* s, const pwmgpu_request* req, uint64_t* id);
+PWMGPU_API pwmgpu_status pwmgpu_server_submit_queries(pwmgpu_server* s, uint64_t structure_id,
+                                                      uint32_t query_structure, uint64_t nqueries,
+                                                      const uint8_t* ops, const uint64_t* a, const uint64_t* b,
+                                                      uint64_t* results, uint64_t* id);
+/* Blocks until the request is done; returns its status. */
+PWMGPU_API pwmgpu_status pwmgpu_server_wait(pwmgpu_server* s, uint64_t id, pwmgpu_request_info* info);
+/* ERR_BUSY while the request is queued or running. */
+PWMGPU_API pwmgpu_status pwmgpu_server_poll(pwmgpu_server* s, uint64_t id, pwmgpu_request_info* info);
+PWMGPU_API const char* pwmgpu_server_error(pwmgpu_server* s, uint64_t id);
+/* Done build request: frees its structure (after its query requests);
+ * done query request: forgets it. */
+PWMGPU_API pwmgpu_status pwmgpu_server_release(pwmgpu_server* s, uint64_t id);
+PWMGPU_API pwmgpu_status pwmgpu_server_stats(pwmgpu_server* s, pwmgpu_server_stats_t* stats);
+PWMGPU_API void pwmgpu_server_destroy(pwmgpu_server* s);
 
 /* ---------------------------------------------------------------------- */
 /* Batches: many independent plain texts built by one CUDA graph           */

@@ -487,6 +487,100 @@ def generate_batch(seed, count):
     return texts[:int(offs[-1])], offs, levels[:count]
 
 
+class Server:
+    """pwmgpu_server: continuous batching of construction and query requests
+    over device-resident structures, admitted under an HBM budget."""
+
+    def __init__(self, budget_bytes, slots=8, device=0):
+        self.lib = _lib.load()
+        h = ctypes.c_void_p()
+        st = self.lib.pwmgpu_server_create(int(device), int(budget_bytes), int(slots), ctypes.byref(h))
+        if st != 0:
+            raise PwmGpuError(st, "server_create failed")
+        self.h = h
+        self._keep = {}  # host arrays that must outlive their requests
+
+    def _check(self, st, rid=None):
+        if st != 0:
+            msg = self.lib.pwmgpu_server_error(self.h, int(rid)).decode() if rid is not None else ""
+            raise PwmGpuError(st, msg)
+
+    def submit(self, text, levels, matrix=True, tree=False, which=0, ops=None, a=None, b=None):
+        """Build request for a host numpy text (uint8/16/32) with an optional
+        query batch (ops: uint8 kinds, a/b: uint64 operands).  Returns (id,
+        results array filled once the request is done)."""
+        text = np.ascontiguousarray(text)
+        nq = 0 if ops is None else len(ops)
+        ops = np.ascontiguousarray(ops, dtype=np.uint8) if nq else None
+        a = np.ascontiguousarray(a, dtype=np.uint64) if nq else None
+        b = np.ascontiguousarray(b, dtype=np.uint64) if (nq and b is not None) else None
+        res = np.zeros(max(nq, 1), dtype=np.uint64)
+        r = _lib.Request()
+        r.text = text.ctypes.data
+        r.size = text.size
+        r.word_width = text.dtype.itemsize
+        r.levels = int(levels)
+        r.shape_flags = (MATRIX if matrix else 0) | (TREE if tree else 0)
+        r.query_structure = int(which)
+        r.nqueries = nq
+        r.query_ops = ops.ctypes.data if nq else None
+        r.query_a = a.ctypes.data if nq else None
+        r.query_b = b.ctypes.data if b is not None else None
+        r.results = res.ctypes.data
+        rid = ctypes.c_uint64()
+        self._check(self.lib.pwmgpu_server_submit(self.h, ctypes.byref(r), ctypes.byref(rid)))
+        self._keep[rid.value] = (text, ops, a, b, res)
+        return rid.value, res[:nq]
+
+    def submit_queries(self, structure_id, ops, a, b=None, which=0):
+        ops = np.ascontiguousarray(ops, dtype=np.uint8)
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        b = np.ascontiguousarray(b, dtype=np.uint64) if b is not None else None
+        res = np.zeros(max(len(ops), 1), dtype=np.uint64)
+        rid = ctypes.c_uint64()
+        self._check(self.lib.pwmgpu_server_submit_queries(
+            self.h, int(structure_id), int(which), len(ops), ops.ctypes.data, a.ctypes.data,
+            b.ctypes.data if b is not None else None, res.ctypes.data, ctypes.byref(rid)))
+        self._keep[rid.value] = (ops, a, b, res)
+        return rid.value, res[:len(ops)]
+
+    def wait(self, rid):
+        """Blocks until the request is done; returns its info (raises on error)."""
+        info = _lib.RequestInfo()
+        st = self.lib.pwmgpu_server_wait(self.h, int(rid), ctypes.byref(info))
+        self._check(st, rid)
+        return info
+
+    def poll(self, rid):
+        """Info when done, None while queued or running."""
+        info = _lib.RequestInfo()
+        st = self.lib.pwmgpu_server_poll(self.h, int(rid), ctypes.byref(info))
+        if st == 7:
+            return None
+        self._check(st, rid)
+        return info
+
+    def release(self, rid):
+        self._check(self.lib.pwmgpu_server_release(self.h, int(rid)))
+        self._keep.pop(int(rid), None)
+
+    def stats(self):
+        st = _lib.ServerStats()
+        self._check(self.lib.pwmgpu_server_stats(self.h, ctypes.byref(st)))
+        return {k: int(getattr(st, k)) for k, _ in st._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pwmgpu_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def generate(dist, seed, n, word_width, param=0, device_ptr=None, context=None):
     """Seeded synthetic text (host numpy array, or into a device pointer)."""
     lib = _lib.load()

@@ -30,6 +30,22 @@ class View(ctypes.Structure):
                 ("level_bits", u64p), ("zeros", u64p)]
 
 
+class Request(ctypes.Structure):
+    _fields_ = [("text", vp), ("size", u64), ("word_width", u32), ("levels", u32), ("shape_flags", u32),
+                ("query_structure", u32), ("nqueries", u64), ("query_ops", vp), ("query_a", vp),
+                ("query_b", vp), ("results", vp)]
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [("id", u64), ("status", i32), ("slot", u32), ("submit_s", ctypes.c_double),
+                ("start_s", ctypes.c_double), ("done_s", ctypes.c_double), ("device_bytes", u64)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("budget_bytes", u64), ("in_use_bytes", u64), ("peak_bytes", u64), ("queued", u64),
+                ("running", u64), ("completed", u64)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "pwmgpu_ctx_create": (i32, [i32, vp, ctypes.POINTER(vp)]),
@@ -54,6 +70,17 @@ SIGNATURES = {
     "pwmgpu_wx_rank_select_blocks": (i32, [vp, vp, i32, u32, u64p, u32p, u32p, u32p, u64p]),
     "pwmgpu_wx_query": (i32, [vp, vp, i32, i32, vp, vp, u64, vp]),
     "pwmgpu_wx_free": (None, [vp]),
+    "pwmgpu_wx_query_host": (i32, [vp, vp, i32, i32, vp, vp, u64, vp]),
+    "pwmgpu_ctx_set_stream_ordered_alloc": (i32, [vp, i32]),
+    "pwmgpu_server_create": (i32, [i32, u64, u32, ctypes.POINTER(vp)]),
+    "pwmgpu_server_submit": (i32, [vp, ctypes.POINTER(Request), u64p]),
+    "pwmgpu_server_submit_queries": (i32, [vp, u64, u32, u64, vp, vp, vp, vp, u64p]),
+    "pwmgpu_server_wait": (i32, [vp, u64, ctypes.POINTER(RequestInfo)]),
+    "pwmgpu_server_poll": (i32, [vp, u64, ctypes.POINTER(RequestInfo)]),
+    "pwmgpu_server_error": (cstr, [vp, u64]),
+    "pwmgpu_server_release": (i32, [vp, u64]),
+    "pwmgpu_server_stats": (i32, [vp, ctypes.POINTER(ServerStats)]),
+    "pwmgpu_server_destroy": (None, [vp]),
     "pwmgpu_generate": (i32, [vp, i32, u64, u64, u64, u32, vp, i32]),
     "pwmgpu_batch_create": (i32, [vp, u32, u64p, u32p, u32, u32, i32, ctypes.POINTER(vp)]),
     "pwmgpu_batch_build": (i32, [vp, vp, vp]),

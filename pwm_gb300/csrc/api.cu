@@ -68,6 +68,8 @@ struct pwmgpu_ctx {
   int pass_levels = kDefaultPassLevels;
   int tile_levels = kDefaultTileLevels;
   int engine = PWMGPU_ENGINE_TILE;
+  bool async_alloc = false;  // stream-ordered allocations on `stream`
+  uint64_t scratch_bytes = 0;
   pwmgpu_wx* compute_cache = nullptr;  // reused by pwmgpu_compute for equal shapes
   // CUDA-event timing of every launch group while profiling is on
   bool profiling = false;
@@ -89,14 +91,21 @@ struct pwmgpu_ctx {
     auto& b = scratch[name];
     if (b.bytes < bytes) {
       if (b.p) {
-        CUDA_TRY(cudaStreamSynchronize(stream));
-        CUDA_TRY(cudaFree(b.p));
+        if (async_alloc) {
+          CUDA_TRY(cudaFreeAsync(b.p, stream));
+        } else {
+          CUDA_TRY(cudaStreamSynchronize(stream));
+          CUDA_TRY(cudaFree(b.p));
+        }
+        scratch_bytes -= b.bytes;
       }
       b.p = nullptr;
       b.bytes = 0;
       const size_t want = std::max<size_t>(bytes, 256);
-      CUDA_TRY(cudaMalloc(&b.p, want));
+      if (async_alloc) CUDA_TRY(cudaMallocAsync(&b.p, want, stream));
+      else CUDA_TRY(cudaMalloc(&b.p, want));
       b.bytes = want;
+      scratch_bytes += want;
     }
     return b.p;
   }
@@ -135,6 +144,8 @@ struct Structure {
   std::vector<RankSelectLevel> rs_levels;
   RankSelectLevel* d_rs_levels = nullptr;
   QueryLevel* d_q_levels = nullptr;
+  std::vector<QueryLevel> q_host;   // source of the asynchronous copy to d_q_levels
+  cudaStream_t alloc_stream = nullptr;  // stream-ordered allocations (nullptr: cudaMalloc)
 
   void set_layout(const std::vector<uint64_t>& level_bits) {
     levels = uint32_t(level_bits.size());
@@ -145,11 +156,16 @@ struct Structure {
     total_words = off;
   }
   void release() {
-    if (d_words) cudaFree(d_words);
-    if (d_zeros) cudaFree(d_zeros);
-    if (d_rs) cudaFree(d_rs);
-    if (d_rs_levels) cudaFree(d_rs_levels);
-    if (d_q_levels) cudaFree(d_q_levels);
+    auto fr = [&](void* p) {
+      if (!p) return;
+      if (alloc_stream) cudaFreeAsync(p, alloc_stream);
+      else cudaFree(p);
+    };
+    fr(d_words);
+    fr(d_zeros);
+    fr(d_rs);
+    fr(d_rs_levels);
+    fr(d_q_levels);
     d_words = nullptr; d_zeros = nullptr; d_rs = nullptr; d_rs_levels = nullptr; d_q_levels = nullptr;
     rs = false;
     rs_bytes = 0;
@@ -175,8 +191,13 @@ pwmgpu_ctx::~pwmgpu_ctx() {
   delete compute_cache;
   for (auto& r : prof) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto e : event_pool) cudaEventDestroy(e);
+  if (async_alloc && stream) cudaStreamSynchronize(stream);
   for (auto& kv : scratch)
-    if (kv.second.p) cudaFree(kv.second.p);
+    if (kv.second.p) {
+      if (async_alloc) cudaFreeAsync(kv.second.p, stream);
+      else cudaFree(kv.second.p);
+    }
+  if (async_alloc && stream) cudaStreamSynchronize(stream);
   if (d_status) cudaFree(d_status);
   if (aux) {
     cudaStreamSynchronize(aux);
@@ -239,6 +260,16 @@ uint64_t rs_n0(uint64_t nwords) { return nwords / (4294967295ull / 64) + 1; }
 uint64_t rs_n12(uint64_t nwords) { return nwords / 32 + 1; }
 uint64_t rs_ns(uint64_t nwords) { return nwords * 64 / 8192 + 2; }
 
+// cudaMalloc, or a stream-ordered allocation on `stream` (no device-wide
+// synchronisation when freed).
+template <typename P>
+void dev_alloc(P** p, size_t bytes, cudaStream_t stream) {
+  void* v = nullptr;
+  if (stream) CUDA_TRY(cudaMallocAsync(&v, bytes, stream));
+  else CUDA_TRY(cudaMalloc(&v, bytes));
+  *p = static_cast<P*>(v);
+}
+
 void alloc_rank_select(Structure& s) {
   size_t bytes = 0;
   std::vector<size_t> off0(s.levels), off12(s.levels), offs0(s.levels), offs1(s.levels), offm(s.levels);
@@ -256,10 +287,11 @@ void alloc_rank_select(Structure& s) {
     offm[l] = take(3 * 8);
   }
   s.rs_bytes = std::max<size_t>(bytes, 256);
-  CUDA_TRY(cudaMalloc(&s.d_rs, s.rs_bytes));
+  dev_alloc(&s.d_rs, s.rs_bytes, s.alloc_stream);
   char* base = static_cast<char*>(s.d_rs);
   s.rs_levels.resize(s.levels);
-  std::vector<QueryLevel> q(s.levels);
+  s.q_host.assign(s.levels, QueryLevel{});
+  auto& q = s.q_host;
   for (uint32_t l = 0; l < s.levels; ++l) {
     auto& r = s.rs_levels[l];
     r.data = s.d_words + s.offs[l];
@@ -272,26 +304,34 @@ void alloc_rank_select(Structure& s) {
     q[l] = QueryLevel{r.data, r.nwords, r.l0, rs_n0(r.nwords), r.l12, r.s0, r.s1, r.meta};
   }
   const size_t nl = std::max<uint32_t>(s.levels, 1);
-  CUDA_TRY(cudaMalloc(&s.d_rs_levels, sizeof(RankSelectLevel) * nl));
-  CUDA_TRY(cudaMalloc(&s.d_q_levels, sizeof(QueryLevel) * nl));
+  dev_alloc(&s.d_rs_levels, sizeof(RankSelectLevel) * nl, s.alloc_stream);
+  dev_alloc(&s.d_q_levels, sizeof(QueryLevel) * nl, s.alloc_stream);
   if (s.levels) {
-    CUDA_TRY(cudaMemcpy(s.d_rs_levels, s.rs_levels.data(), sizeof(RankSelectLevel) * s.levels,
-                        cudaMemcpyHostToDevice));
-    CUDA_TRY(cudaMemcpy(s.d_q_levels, q.data(), sizeof(QueryLevel) * s.levels, cudaMemcpyHostToDevice));
+    if (s.alloc_stream) {  // the host vectors live as long as the structure
+      CUDA_TRY(cudaMemcpyAsync(s.d_rs_levels, s.rs_levels.data(), sizeof(RankSelectLevel) * s.levels,
+                               cudaMemcpyHostToDevice, s.alloc_stream));
+      CUDA_TRY(cudaMemcpyAsync(s.d_q_levels, q.data(), sizeof(QueryLevel) * s.levels, cudaMemcpyHostToDevice,
+                               s.alloc_stream));
+    } else {
+      CUDA_TRY(cudaMemcpy(s.d_rs_levels, s.rs_levels.data(), sizeof(RankSelectLevel) * s.levels,
+                          cudaMemcpyHostToDevice));
+      CUDA_TRY(cudaMemcpy(s.d_q_levels, q.data(), sizeof(QueryLevel) * s.levels, cudaMemcpyHostToDevice));
+    }
   }
   s.rs = true;
 }
 
 void alloc_structure(Structure& s, const std::vector<uint64_t>& level_bits, uint64_t n, bool tree, bool huff,
-                     bool rank_select) {
+                     bool rank_select, cudaStream_t alloc_stream = nullptr) {
   s.release();
+  s.alloc_stream = alloc_stream;
   s.present = true;
   s.is_tree = tree;
   s.huffman = huff;
   s.n = n;
   s.set_layout(level_bits);
-  CUDA_TRY(cudaMalloc(&s.d_words, std::max<uint64_t>(s.total_words, 16) * 8));
-  CUDA_TRY(cudaMalloc(&s.d_zeros, std::max<uint32_t>(s.levels, 1) * 8));
+  dev_alloc(&s.d_words, std::max<uint64_t>(s.total_words, 16) * 8, alloc_stream);
+  dev_alloc(&s.d_zeros, std::max<uint32_t>(s.levels, 1) * 8, alloc_stream);
   if (rank_select) alloc_rank_select(s);
 }
 
@@ -1132,6 +1172,21 @@ pwmgpu_status pwmgpu_ctx_set_pass_levels(pwmgpu_ctx* ctx, int k) {
   return PWMGPU_OK;
 }
 
+pwmgpu_status pwmgpu_ctx_set_stream_ordered_alloc(pwmgpu_ctx* ctx, int enable) {
+  if (!ctx) return PWMGPU_ERR_ARG;
+  return guarded(ctx, [&]() {
+    if (enable && !ctx->async_alloc) {
+      // freed blocks stay in this process's pool for the next allocation
+      cudaMemPool_t pool;
+      CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, ctx->device));
+      uint64_t keep = ~uint64_t(0);
+      CUDA_TRY(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    }
+    ctx->async_alloc = enable != 0;
+    return PWMGPU_OK;
+  });
+}
+
 pwmgpu_status pwmgpu_ctx_set_engine(pwmgpu_ctx* ctx, int engine) {
   if (!ctx || (engine != PWMGPU_ENGINE_TILE && engine != PWMGPU_ENGINE_WARP)) return PWMGPU_ERR_ARG;
   ctx->engine = engine;
@@ -1194,9 +1249,10 @@ pwmgpu_status pwmgpu_wx_create(pwmgpu_ctx* ctx, uint64_t size, uint32_t word_wid
     wx->flags = shape_flags;
     const bool rs = shape_flags & PWMGPU_RANK_SELECT;
     std::vector<uint64_t> bits(levels, size);
-    alloc_structure(wx->wm, bits, size, false, false, rs && (shape_flags & PWMGPU_MATRIX));
+    cudaStream_t as = ctx->async_alloc ? ctx->stream : nullptr;
+    alloc_structure(wx->wm, bits, size, false, false, rs && (shape_flags & PWMGPU_MATRIX), as);
     wx->wm_internal = !(shape_flags & PWMGPU_MATRIX);
-    if (shape_flags & PWMGPU_TREE) alloc_structure(wx->wt, bits, size, true, false, rs);
+    if (shape_flags & PWMGPU_TREE) alloc_structure(wx->wt, bits, size, true, false, rs, as);
     *out = wx.release();
     return PWMGPU_OK;
   });
@@ -1294,6 +1350,29 @@ pwmgpu_status pwmgpu_wx_query(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which, i
     ProfScope ps(ctx, "queries", count * 24);
     launch_queries(q, op, d_a, d_b, count, d_out, ctx->stream, &ctx->launches);
     CUDA_TRY(cudaGetLastError());
+    return PWMGPU_OK;
+  });
+}
+
+pwmgpu_status pwmgpu_wx_query_host(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which, int op, const uint64_t* a,
+                                   const uint64_t* b, uint64_t count, uint64_t* out) {
+  if (!ctx || !wx || op < 0 || op > 2 || (count && (!a || !out || (op > 0 && !b)))) return PWMGPU_ERR_ARG;
+  if (count == 0) return PWMGPU_OK;
+  const Structure& s = which ? wx->wt : wx->wm;
+  if (!s.present || !s.rs || s.huffman) return fail(ctx, PWMGPU_ERR_ARG, "queries need a plain structure with rank/select");
+  return guarded(ctx, [&]() {
+    auto* d = static_cast<uint64_t*>(ctx->grow("query_io", count * 3 * 8));
+    cudaStream_t st = ctx->stream;
+    CUDA_TRY(cudaMemcpyAsync(d, a, count * 8, cudaMemcpyHostToDevice, st));
+    if (op > 0) CUDA_TRY(cudaMemcpyAsync(d + count, b, count * 8, cudaMemcpyHostToDevice, st));
+    QueryStructure q{s.levels, s.is_tree ? 1u : 0u, s.n, s.d_q_levels, s.d_zeros};
+    {
+      ProfScope ps(ctx, "queries", count * 24);
+      launch_queries(q, op, d, d + count, count, d + 2 * count, st, &ctx->launches);
+    }
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(out, d + 2 * count, count * 8, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
     return PWMGPU_OK;
   });
 }
