@@ -213,6 +213,93 @@ def batched_vs_per_text(torch, pg, ctx, count=4096, seed=1, reps=3):
             "identical_to_per_text": bool(same), "structures": ["matrix", "tree"]}
 
 
+def serving_requests(pg, count, seed=7, nq=10_000):
+    """The serving mix: the batched workload's uint8 texts (log-normal
+    lengths; 85% DNA-like with 3 levels, 15% Zipf bytes with 8 levels) plus 5%
+    uint32 texts uniform over 2^20 values with 20 levels (same length law,
+    clamped to 2^26); every request carries nq access/rank/select queries at
+    uniform positions, symbols taken from the text."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    texts, offs, levels = pg.generate_batch(seed, count)
+    reqs = []
+    for i in range(count):
+        if rng.random() < 0.05:
+            n = int(min(max(round(np.exp(rng.normal(np.log(2 ** 16), 1.5))), 2 ** 10), 2 ** 26))
+            t, L = rng.integers(0, 1 << 20, n).astype(np.uint32), 20
+        else:
+            t, L = texts[int(offs[i]):int(offs[i + 1])], int(levels[i])
+        n = t.size
+        ops = rng.integers(0, 3, nq).astype(np.uint8)
+        sym = t[rng.integers(0, n, nq)].astype(np.uint64)
+        counts = np.bincount(t.astype(np.int64), minlength=1 << L)
+        occ = 1 + np.floor(rng.random(nq) * counts[sym.astype(np.int64)]).astype(np.uint64)
+        a = np.where(ops == 0, rng.integers(0, n, nq).astype(np.uint64), sym)
+        b = np.where(ops == 1, rng.integers(0, n + 1, nq).astype(np.uint64), occ)
+        reqs.append((t, L, ops, a, b))
+    return reqs
+
+
+def serve_run(pg, reqs, rate, slots, budget):
+    """Poisson arrivals at `rate` requests/s (rate None: one at a time, each
+    submitted when the previous finished).  A collector waits for and
+    releases every request.  Returns latency and throughput figures."""
+    import numpy as np
+    srv = pg.Server(budget, slots=slots)
+    infos = [None] * len(reqs)
+    ids = [None] * len(reqs)
+    ready = threading.Semaphore(0)
+
+    def collector():
+        for k in range(len(reqs)):
+            ready.acquire()
+            infos[k] = srv.wait(ids[k])
+            srv.release(ids[k])
+
+    col = threading.Thread(target=collector)
+    col.start()
+    rng = np.random.default_rng(11)
+    t0 = time.perf_counter()
+    t_next = t0
+    for k, (t, L, ops, a, b) in enumerate(reqs):
+        if rate is not None:
+            t_next += rng.exponential(1.0 / rate)
+            delay = t_next - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+        ids[k], _ = srv.submit(t, L, ops=ops, a=a, b=b)
+        ready.release()
+        if rate is None:
+            srv.wait(ids[k])
+    col.join()
+    stats = srv.stats()
+    srv.close()
+    lat = np.array([i.done_s - i.submit_s for i in infos]) * 1e3
+    svc = np.array([i.done_s - i.start_s for i in infos]) * 1e3
+    span = max(i.done_s for i in infos) - min(i.submit_s for i in infos)
+    sym = sum(int(r[0].size) for r in reqs)
+    byt = sum(int(r[0].nbytes) for r in reqs)
+    return {"offered_req_s": rate, "requests": len(reqs), "throughput_req_s": len(reqs) / span,
+            "text_gbs": byt / span / 1e9, "symbols": sym, "queries_per_request": int(reqs[0][2].size),
+            "latency_ms_p50": float(np.percentile(lat, 50)), "latency_ms_p99": float(np.percentile(lat, 99)),
+            "service_ms_p50": float(np.percentile(svc, 50)), "service_ms_p99": float(np.percentile(svc, 99)),
+            "peak_device_bytes": stats["peak_bytes"], "slots": slots}
+
+
+def serving_bench(pg, count=400, slots=8, budget=150 * 10 ** 9):
+    """p50/p99 request latency and throughput of the continuous-batching
+    server at Poisson rates 100, 1000 and 10000 requests/s, next to
+    one-at-a-time construction (one slot, closed loop)."""
+    reqs = serving_requests(pg, count)
+    serve_run(pg, reqs[:16], None, 1, budget)  # warm-up
+    out = {"workload": "batched-workload uint8 texts + 5% uint32 (2^20 values, 20 levels); build (matrix + "
+                       "rank/select) then 10^4 access/rank/select queries per request; budget 150 GB",
+           "one_at_a_time": serve_run(pg, reqs, None, 1, budget), "rates": []}
+    for rate in (100, 1000, 10000):
+        out["rates"].append(serve_run(pg, reqs, rate, slots, budget))
+    return out
+
+
 def run_reference(args, rank):
     if rank != 0:
         return 0
@@ -256,6 +343,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -388,6 +476,8 @@ def main():
             line["cpu_baseline"] = cpu_baseline(CPU_SAMPLE)
         if world == 1 and not args.no_batch:
             line["batched"] = batched_vs_per_text(torch, pg, ctx)
+        if world == 1 and not args.no_serve:
+            line["serving"] = serving_bench(pg)
         print(json.dumps(line))
     ds.free()
     if dist:

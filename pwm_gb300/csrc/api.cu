@@ -86,6 +86,23 @@ struct pwmgpu_ctx {
     return e;
   }
 
+  // Grow-only pinned host buffer (contents undefined).
+  void* pinned = nullptr;
+  size_t pinned_bytes = 0;
+  void* grow_pinned(size_t bytes) {
+    if (pinned_bytes < bytes) {
+      if (pinned) {
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        CUDA_TRY(cudaFreeHost(pinned));
+      }
+      pinned = nullptr;
+      pinned_bytes = 0;
+      CUDA_TRY(cudaMallocHost(&pinned, bytes));
+      pinned_bytes = bytes;
+    }
+    return pinned;
+  }
+
   // Grow-only named scratch buffer (contents undefined).
   void* grow(const std::string& name, size_t bytes) {
     auto& b = scratch[name];
@@ -199,6 +216,7 @@ pwmgpu_ctx::~pwmgpu_ctx() {
     }
   if (async_alloc && stream) cudaStreamSynchronize(stream);
   if (d_status) cudaFree(d_status);
+  if (pinned) cudaFreeHost(pinned);
   if (aux) {
     cudaStreamSynchronize(aux);
     cudaStreamDestroy(aux);
@@ -471,14 +489,11 @@ struct TileFirstPass {
 };
 
 void run_tile_passes(pwmgpu_ctx* ctx, const void* d_text, uint32_t width, uint32_t L,
-                     const std::vector<uint64_t>& hist, const LevelTables& tabs, Structure& wm, Structure* wt,
-                     const TileFirstPass* first = nullptr, bool levels_zeroed = false,
-                     cudaEvent_t deeper_zeroed = nullptr) {
+                     const std::vector<TilePassHost>& passes, const std::vector<uint32_t>& regroup,
+                     const LevelTables& tabs, Structure& wm, Structure* wt, const TileFirstPass* first = nullptr,
+                     bool levels_zeroed = false, cudaEvent_t deeper_zeroed = nullptr) {
   cudaStream_t s = ctx->stream;
   const uint64_t n = tabs.level_bits.empty() ? 0 : tabs.level_bits[0];
-  const uint32_t T = tile_pass_elems(width);
-  std::vector<uint32_t> regroup;
-  const auto passes = plan_tile_passes(hist, L, std::min(ctx->tile_levels, kTileMaxLevels), T, wt != nullptr, &regroup);
 
   // one upload: per pass its segments, its level descriptor and its tables
   std::vector<unsigned char> blob;
@@ -653,18 +668,29 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text) {
     launch_leaf_histogram(d_text, n, wx->width, L, d_hist, ctx->d_status, s, &ctx->launches);
   }
   CUDA_TRY(cudaGetLastError());
-  std::vector<uint64_t> hist(bins);
-  CUDA_TRY(cudaMemcpyAsync(hist.data(), d_hist, bins * 8, cudaMemcpyDeviceToHost, s));
+  auto* h_hist = static_cast<uint64_t*>(ctx->grow_pinned(bins * 8));
+  CUDA_TRY(cudaMemcpyAsync(h_hist, d_hist, bins * 8, cudaMemcpyDeviceToHost, s));
   check_device_status(ctx);  // synchronises
-  const auto plan = plan_passes(L, ctx->pass_levels);
   const bool want_tree = wx->wt.present;
-  const LevelTables tabs = build_tables_plain(hist, L, plan, want_tree);
+  LevelTables tabs;
+  std::vector<PassPlan> plan;
+  std::vector<TilePassHost> tile_passes;
+  std::vector<uint32_t> regroup;
+  if (tile_engine) {
+    const auto cnt = fold_prefix_counts(h_hist, L);
+    tile_passes = plan_tile_passes(cnt, L, std::min(ctx->tile_levels, kTileMaxLevels), tile_pass_elems(wx->width),
+                                   want_tree, &regroup);
+    tabs = build_tables_tile(cnt, L, want_tree ? regroup : std::vector<uint32_t>{});
+  } else {
+    plan = plan_passes(L, ctx->pass_levels);
+    tabs = build_tables_plain(std::vector<uint64_t>(h_hist, h_hist + bins), L, plan, want_tree);
+  }
   wx->wm.zeros = tabs.zeros;
   CUDA_TRY(cudaMemcpyAsync(wx->wm.d_zeros, wx->wm.zeros.data(), L * 8, cudaMemcpyHostToDevice, s));
   if (tile_engine) {
     CUDA_TRY(cudaStreamWaitEvent(s, ctx->aux_done, 0));
     CUDA_TRY(cudaStreamWaitEvent(s, ctx->aux_done2, 0));
-    run_tile_passes(ctx, d_text, wx->width, L, hist, tabs, wx->wm, want_tree ? &wx->wt : nullptr,
+    run_tile_passes(ctx, d_text, wx->width, L, tile_passes, regroup, tabs, wx->wm, want_tree ? &wx->wt : nullptr,
                     first.blockpre ? &first : nullptr, true);
   }
   else

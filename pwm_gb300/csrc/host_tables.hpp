@@ -5,6 +5,7 @@
 #pragma once
 
 #include <algorithm>
+#include <array>
 #include <cstdint>
 #include <numeric>
 #include <unordered_map>
@@ -31,10 +32,22 @@ inline std::vector<PassPlan> plan_passes(uint32_t L, int kmax) {
   return p;
 }
 
+// The low `bits` bits of v reversed (bits <= 32), by byte table.
 inline uint32_t rev_bits_host(uint64_t v, uint32_t bits) {
-  uint64_t r = 0;
-  for (uint32_t i = 0; i < bits; ++i) { r = (r << 1) | (v & 1); v >>= 1; }
-  return uint32_t(r);
+  static const auto table = []() {
+    std::array<uint8_t, 256> t{};
+    for (uint32_t b = 0; b < 256; ++b) {
+      uint32_t r = 0;
+      for (uint32_t i = 0; i < 8; ++i) r |= ((b >> i) & 1u) << (7 - i);
+      t[b] = uint8_t(r);
+    }
+    return t;
+  }();
+  if (bits == 0) return 0;
+  const uint32_t x = uint32_t(v);
+  const uint32_t r = (uint32_t(table[x & 0xFF]) << 24) | (uint32_t(table[(x >> 8) & 0xFF]) << 16) |
+                     (uint32_t(table[(x >> 16) & 0xFF]) << 8) | uint32_t(table[x >> 24]);
+  return r >> (32 - bits);
 }
 
 // One weighted "code" of the text: the bits the levels test, its length
@@ -111,6 +124,53 @@ inline LevelTables build_tables_plain(const std::vector<uint64_t>& hist, uint32_
   return t;
 }
 
+// Natural-order prefix counts of every level m = 0..L (2^m bins) folded from
+// the leaf histogram.
+inline std::vector<std::vector<uint64_t>> fold_prefix_counts(const uint64_t* hist, uint32_t L) {
+  std::vector<std::vector<uint64_t>> cnt(L + 1);
+  cnt[L].assign(hist, hist + (size_t(1) << L));
+  for (int m = int(L) - 1; m >= 0; --m) {
+    cnt[m].assign(size_t(1) << m, 0);
+    const auto& c = cnt[m + 1];
+    for (size_t p = 0; p < cnt[m].size(); ++p) cnt[m][p] = c[2 * p] + c[2 * p + 1];
+  }
+  return cnt;
+}
+
+// Tables of a plain build through the tile engine: zero counts, level sizes
+// and the tree segments of the given levels (those the regroup writes).
+inline LevelTables build_tables_tile(const std::vector<std::vector<uint64_t>>& cnt, uint32_t L,
+                                     const std::vector<uint32_t>& tree_levels) {
+  LevelTables t;
+  const uint64_t n = cnt[0][0];
+  t.level_bits.assign(L, n);
+  t.zeros.assign(L, 0);
+  for (uint32_t m = 0; m < L; ++m)
+    for (size_t p = 0; p < cnt[m + 1].size(); p += 2) t.zeros[m] += cnt[m + 1][p];
+  t.seg_tree.resize(L);
+  t.seg_matrix.resize(L);
+  for (uint32_t m : tree_levels) {
+    const auto& c = cnt[m];
+    std::vector<uint64_t> mstart(c.size(), 0);
+    uint64_t run = 0;
+    for (size_t r = 0; r < c.size(); ++r) {
+      const size_t p = rev_bits_host(r, m);
+      mstart[p] = run;
+      run += c[p];
+    }
+    std::vector<uint64_t> st, sm;
+    run = 0;
+    for (size_t p = 0; p < c.size(); ++p) {
+      if (c[p]) { st.push_back(run); sm.push_back(mstart[p]); }
+      run += c[p];
+    }
+    if (st.empty()) { st.push_back(0); sm.push_back(0); }
+    t.seg_tree[m] = std::move(st);
+    t.seg_matrix[m] = std::move(sm);
+  }
+  return t;
+}
+
 // ---------------------------------------------------------------------------
 // Segmented tile passes of a plain text (levels <= kTilePlanMaxLevels).
 // Pass (l, K) splits S_l through levels l..l+K-1.  A pass is "segmented" when
@@ -137,26 +197,23 @@ struct TilePassHost {
   std::vector<uint64_t> table;  // per segment: tile_table_size(K) entries
 };
 
-// hist: 2^L leaf counts.  T: keys per tile.  regroup: tree levels the passes
-// leave to the regroup (empty without a tree).
-inline std::vector<TilePassHost> plan_tile_passes(const std::vector<uint64_t>& hist, uint32_t L, int kmax, uint32_t T,
-                                                  bool want_tree, std::vector<uint32_t>* regroup) {
-  // natural prefix counts per level and their exclusive prefixes, in natural
-  // order (tree) and in key order (matrix: key = reversed prefix)
-  std::vector<std::vector<uint64_t>> cnt(L + 1), pren(L + 1), prek(L + 1);
-  cnt[L] = hist;
-  for (int m = int(L) - 1; m >= 0; --m) {
-    cnt[m].assign(size_t(1) << m, 0);
-    for (size_t p = 0; p < cnt[m].size(); ++p) cnt[m][p] = cnt[m + 1][2 * p] + cnt[m + 1][2 * p + 1];
-  }
-  for (uint32_t m = 0; m <= L; ++m) {
+// cnt: the folded prefix counts (fold_prefix_counts).  T: keys per tile.
+// regroup: tree levels the passes leave to the regroup (empty without a
+// tree).  Exclusive prefixes over all 2^m groups of a level are built only
+// for the levels of segmented passes (few groups); a matrix-only pass needs
+// only the counts of its own K bits, folded from one level.
+inline std::vector<TilePassHost> plan_tile_passes(const std::vector<std::vector<uint64_t>>& cnt, uint32_t L, int kmax,
+                                                  uint32_t T, bool want_tree, std::vector<uint32_t>* regroup) {
+  const uint64_t n = cnt[0][0];
+  std::vector<std::vector<uint64_t>> pren(L + 1), prek(L + 1);
+  auto prefixes = [&](uint32_t m) {  // natural order (tree) and key order (matrix: reversed prefix)
+    if (!prek[m].empty()) return;
     const size_t sz = cnt[m].size();
     pren[m].assign(sz + 1, 0);
     prek[m].assign(sz + 1, 0);
     for (size_t p = 0; p < sz; ++p) pren[m][p + 1] = pren[m][p] + cnt[m][p];
     for (size_t x = 0; x < sz; ++x) prek[m][x + 1] = prek[m][x] + cnt[m][rev_bits_host(x, m)];
-  }
-  const uint64_t n = cnt[0][0];
+  };
   std::vector<TilePassHost> passes;
   for (const auto& pp : plan_passes(L, kmax)) {
     TilePassHost ps;
@@ -177,6 +234,7 @@ inline std::vector<TilePassHost> plan_tile_passes(const std::vector<uint64_t>& h
     };
     std::vector<uint64_t> tab(size_t(TS), 0);
     if (ps.segmented) {
+      for (uint32_t m = l; m <= l + uint32_t(K) && m <= L; ++m) prefixes(m);
       for (uint64_t g = 0; g < groups; ++g) {
         const uint64_t m = prek[l][g + 1] - prek[l][g];
         if (m == 0) continue;
@@ -191,10 +249,26 @@ inline std::vector<TilePassHost> plan_tile_passes(const std::vector<uint64_t>& h
         add_segment(prek[l][g], m, tab);
       }
     } else {
-      for (int j = 0; j < K; ++j)
-        for (int v = 0; v < (1 << j); ++v) tab[size_t(tile_wm_entry(j, v))] = prek[l + j][uint64_t(v) << l];
-      if (ps.out)
-        for (int v = 0; v < (1 << K); ++v) tab[size_t(tile_out_entry(K, v))] = prek[l + K][uint64_t(v) << l];
+      // counts of key_K (bits l..l+K-1, first least significant) over the
+      // whole text, from the natural prefixes of level l+K; key_j folds it
+      const uint32_t top = l + uint32_t(K);
+      std::vector<uint64_t> ck(size_t(1) << K, 0);
+      const auto& c = cnt[top];
+      const uint64_t fmask = (uint64_t(1) << K) - 1;
+      for (size_t p = 0; p < c.size(); ++p)
+        if (c[p]) ck[rev_bits_host(p & fmask, uint32_t(K))] += c[p];
+      for (int j = 0; j <= K; ++j) {
+        if (j < K || ps.out) {
+          uint64_t run = 0;
+          for (int v = 0; v < (1 << j); ++v) {
+            uint64_t cv = 0;  // key_j == v: the low j bits of key_K
+            for (int h = 0; h < (1 << (K - j)); ++h) cv += ck[size_t(v + (h << j))];
+            if (j < K) tab[size_t(tile_wm_entry(j, v))] = run;
+            else tab[size_t(tile_out_entry(K, v))] = run;
+            run += cv;
+          }
+        }
+      }
       add_segment(0, n, tab);
       if (want_tree && regroup)
         for (int j = 0; j < K; ++j)
