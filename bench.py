@@ -344,6 +344,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--engine", default="tile", choices=["tile", "warp"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -374,6 +375,8 @@ def main():
     ctx = pg.Context(device=local, stream=ctypes_stream(stream))
     if args.pass_levels:
         ctx.set_pass_levels(args.pass_levels)
+    if args.engine == "warp":
+        ctx.set_engine(pg.ENGINE_WARP)
     n = args.n
     text = torch.empty(n, dtype=torch.uint8, device="cuda")
     pg.generate(pg.GEN_ZIPF256, 1 + rank, n, 1, device_ptr=text.data_ptr(), context=ctx)
