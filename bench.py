@@ -332,6 +332,29 @@ def run_reference(args, rank):
     return 0
 
 
+# ---- replicas across ranks (one text per rank, no collective on the data
+# ---- path): the helpers the launch under torchrun uses, also run by the
+# ---- gloo tests on CPU
+def replica_seed(rank):
+    """Each rank builds its own text (weak scaling)."""
+    return 1 + rank
+
+
+def max_over_ranks(x, dist, device):
+    """The slowest rank's time (the job's time)."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world, n, seconds):
+    """Whole-job text GB/s: all ranks' symbols over the slowest rank's time."""
+    return world * n / seconds / 1e9
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -379,7 +402,7 @@ def main():
         ctx.set_engine(pg.ENGINE_WARP)
     n = args.n
     text = torch.empty(n, dtype=torch.uint8, device="cuda")
-    pg.generate(pg.GEN_ZIPF256, 1 + rank, n, 1, device_ptr=text.data_ptr(), context=ctx)
+    pg.generate(pg.GEN_ZIPF256, replica_seed(rank), n, 1, device_ptr=text.data_ptr(), context=ctx)
     ds = pg.DeviceStructure(n, 1, LEVELS, matrix=True, tree=True, rank_select=True, context=ctx)
     for _ in range(args.warmup):
         ds.build(text.data_ptr())
@@ -415,12 +438,8 @@ def main():
     ctx.check(ctx.lib.pwmgpu_ctx_profile_read(ctx.h, buf, len(buf)))
     ctx.lib.pwmgpu_ctx_profile(ctx.h, 0)
     prof = parse_profile(buf.value.decode())
-    ms = e0.elapsed_time(e1) / args.steps
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * n / (ms / 1e3) / 1e9
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dist, "cuda")
+    value = job_throughput(world, n, ms / 1e3)
 
     # ---- end to end through the public host API --------------------------
     host_text = text.cpu().pin_memory()
@@ -446,11 +465,8 @@ def main():
         e2e_step()
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / args.e2e_steps
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * n / e2e_s / 1e9
+    e2e_s = max_over_ranks(e2e_s, dist, "cuda")
+    e2e_value = job_throughput(world, n, e2e_s)
 
     if rank == 0:
         peak, peak_kind = measured_peak()
