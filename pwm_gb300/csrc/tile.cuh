@@ -283,9 +283,10 @@ __device__ __forceinline__ uint64_t stream64(const uint32_t* sb, uint32_t x) {
 }
 
 // Stream bits [src, src+len) to level bits [dst, dst+len), 64-bit words
-// k = k0, k0 + step, ... of the destination range: whole words are stored,
-// and so is the level's last word when this run fills it up to the level's
-// end; words shared with other runs are OR-ed (those were zeroed).
+// k = k0, k0 + step, ... of the destination range.  Words the run covers
+// whole are stored (the lean path); so is the level's last word when the run
+// fills it up to the level's end; the (at most two) words shared with other
+// runs are OR-ed (those were zeroed).
 __device__ __forceinline__ void write_bits64(uint64_t* level, uint64_t nbits, uint64_t dst, const uint32_t* sb,
                                              uint32_t src, uint32_t len, uint32_t k0, uint32_t step,
                                              uint32_t* status) {
@@ -299,13 +300,24 @@ __device__ __forceinline__ void write_bits64(uint64_t* level, uint64_t nbits, ui
   const uint32_t nwords = (lead + len + 63) >> 6;
   const uint32_t tail = (lead + len) & 63;  // bits of the last word covered (0: all 64)
   const bool at_end = dst + len == nbits;   // the run ends the level: the rest of its last word is padding
+  // whole words: [kb, ke)
+  const uint32_t kb = lead ? 1u : 0u;
+  const uint32_t ke = (tail == 0 || (at_end && nwords > kb)) ? nwords : nwords - 1;
+  const uint32_t base = src - lead;  // stream bit of destination word 0's first bit (+64k)
   for (uint32_t k = k0; k < nwords; k += step) {
-    uint64_t val = k ? stream64(sb, src + 64 * k - lead) : (stream64(sb, src) >> lead);
-    uint64_t mask = k ? ~0ull : (~0ull >> lead);
-    const bool last = k == nwords - 1;
-    if (last && tail) mask &= ~(~0ull >> tail);
-    if (mask == ~0ull || (last && at_end && (k || !lead))) out[k] = val & mask;
-    else atomicOr(reinterpret_cast<unsigned long long*>(out + k), (unsigned long long)(val & mask));
+    if (k >= kb && k < ke) {
+      const uint32_t x = base + 64 * k;
+      const uint32_t i = x >> 5, sh = x & 31;
+      const uint32_t w0 = sb[i], w1 = sb[i + 1], w2 = sb[i + 2];
+      uint64_t val = (uint64_t(__funnelshift_l(w1, w0, sh)) << 32) | __funnelshift_l(w2, w1, sh);
+      if (k == nwords - 1 && tail) val &= ~(~0ull >> tail);  // owned last word: clear the padding
+      out[k] = val;
+    } else {
+      uint64_t val = k ? stream64(sb, base + 64 * k) : (stream64(sb, src) >> lead);
+      uint64_t mask = k ? ~0ull : (~0ull >> lead);
+      if (k == nwords - 1 && tail) mask &= ~(~0ull >> tail);
+      atomicOr(reinterpret_cast<unsigned long long*>(out + k), (unsigned long long)(val & mask));
+    }
   }
 }
 
