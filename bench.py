@@ -213,6 +213,53 @@ def batched_vs_per_text(torch, pg, ctx, count=4096, seed=1, reps=3):
             "identical_to_per_text": bool(same), "structures": ["matrix", "tree"]}
 
 
+def other_workloads(torch, pg, ctx, reps=3):
+    """Build times of the other configured workloads (resident text, CUDA
+    events on the library's stream; the drop-in Huffman builds host to host):
+    2^26 DNA-like bytes with 2 levels (matrix + tree), 2^28 16-bit symbols
+    with 16 levels (plain matrix + tree, and Huffman-shaped matrix and tree
+    with pwm's codes from the host builder), 2^26 32-bit symbols over 2^20
+    values with 20 levels (matrix + rank/select)."""
+    import numpy as np
+    out = {}
+    stream = torch.cuda.current_stream()
+
+    def timed(name, n, width, levels, dist, param, tree, rs):
+        dtype = {1: torch.uint8, 2: torch.int16, 4: torch.int32}[width]
+        t = torch.empty(n, dtype=dtype, device="cuda")
+        pg.generate(dist, 3, n, width, param=param, device_ptr=t.data_ptr(), context=ctx)
+        ds = pg.DeviceStructure(n, width, levels, matrix=True, tree=tree, rank_select=rs, context=ctx)
+        ds.build(t.data_ptr())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            ds.build(t.data_ptr())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        ds.check()
+        ds.free()
+        out[name] = {"n": n, "word_width": width, "levels": levels, "structures": ["matrix"] + (["tree"] if tree else []),
+                     "rank_select": rs, "ms": ms, "text_gbs": n * width / ms / 1e6}
+        return t
+
+    timed("dna_2p26_levels2", 1 << 26, 1, 2, pg.GEN_DNA4, 0, True, False)
+    t16 = timed("mix16_2p28_levels16", 1 << 28, 2, 16, pg.GEN_MIX16, 0, True, False)
+    timed("uniform20_2p26_levels20", 1 << 26, 4, 20, pg.GEN_UNIFORM, 1 << 20, False, True)
+    host16 = t16.cpu().numpy().view(np.uint16)
+    del t16
+    for tree in (False, True):
+        t0 = time.perf_counter()
+        codes = pg.huffman_codes(host16, tree, ctx)
+        t1 = time.perf_counter()
+        ws = pg.wx_huff_ps(np.uint16, tree, context=ctx).compute(host16, host16.size, 0, codes=codes)
+        t2 = time.perf_counter()
+        out["mix16_2p28_huffman_" + ("tree" if tree else "matrix")] = {
+            "n": int(host16.size), "word_width": 2, "levels": ws.levels(), "codes_ms": (t1 - t0) * 1e3,
+            "build_host_to_host_ms": (t2 - t1) * 1e3, "text_gbs_host_to_host": host16.nbytes / (t2 - t1) / 1e9}
+    return out
+
+
 def serving_requests(pg, count, seed=7, nq=10_000):
     """The serving mix: the batched workload's uint8 texts (log-normal
     lengths; 85% DNA-like with 3 levels, 15% Zipf bytes with 8 levels) plus 5%
@@ -368,6 +415,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--engine", default="tile", choices=["tile", "warp"])
+    ap.add_argument("--no-other", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -497,6 +545,8 @@ def main():
             line["batched"] = batched_vs_per_text(torch, pg, ctx)
         if world == 1 and not args.no_serve:
             line["serving"] = serving_bench(pg)
+        if world == 1 and not args.no_other:
+            line["other_workloads"] = other_workloads(torch, pg, ctx)
         print(json.dumps(line))
     ds.free()
     if dist:

@@ -216,9 +216,17 @@ class _HuffmanConstruction(_PlainConstruction):
         code_word = np.ascontiguousarray(codes[1], dtype=np.uint64)
         if size == 0:
             return wavelet_structure(bit_vectors([]), None if self.is_tree else [], self.is_tree, True, codes)
-        nz = code_len[np.unique(t)] if code_len.size else code_len
-        L = int(nz.max()) if nz.size else 0
-        sizes = [int(np.sum(code_len[t] > l)) for l in range(L)] if L else []
+        if len(codes) >= 4:
+            # huffman_codes() already returns the level sizes of this text
+            L = int(codes[3])
+            sizes = [int(x) for x in codes[2][:L]]
+        else:
+            # level sizes from the symbol counts (huff_level_sizes_builder.hpp:13-46): one pass over the text
+            counts = np.bincount(t, minlength=code_len.size)[:code_len.size] if code_len.size else \
+                np.zeros(0, dtype=np.int64)
+            present = code_len[counts > 0]
+            L = int(present.max()) if present.size else 0
+            sizes = [int(counts[code_len > l].sum()) for l in range(L)] if L else []
         bvs = bit_vectors(sizes)
         zeros = np.zeros(max(L, 1), dtype=np.uint64)
         sz = np.array(sizes if sizes else [0], dtype=np.uint64)

@@ -1,4 +1,6 @@
 // Histogram, wavelet-tree regroup, Huffman key and generator kernels.
+#include <algorithm>
+
 #include "gen.cuh"
 #include "kernels.cuh"
 
@@ -210,6 +212,37 @@ __global__ void __launch_bounds__(1024) tile_block_scan_kernel(unsigned long lon
   }
 }
 
+// 14..16 levels: the bins split into ranges of 2^15 u32 counters held in
+// shared memory (128 KB); grid row r counts the symbols of range r in its
+// chunk of the text and adds its nonzero bins to the global histogram.
+// Skewed texts keep their hot bins on chip instead of contending in L2.
+constexpr int kRangeBins = 1 << 15;
+constexpr int kRangeThreads = 1024;
+
+template <typename T>
+__global__ void __launch_bounds__(kRangeThreads) leaf_hist_ranges(const T* text, uint64_t n, uint32_t levels,
+                                                                 uint64_t chunk, unsigned long long* hist,
+                                                                 uint32_t* status) {
+  extern __shared__ uint32_t hr[];
+  for (int i = threadIdx.x; i < kRangeBins; i += kRangeThreads) hr[i] = 0;
+  __syncthreads();
+  const uint64_t lo = uint64_t(blockIdx.y) * kRangeBins;
+  const uint64_t limit = 1ull << levels;
+  const uint64_t b = uint64_t(blockIdx.x) * chunk;
+  const uint64_t e = b + chunk < n ? b + chunk : n;
+  bool bad = false;
+  if (b < e)
+    for_each_symbol_vec<T>(text + b, e - b, threadIdx.x, kRangeThreads, [&](uint64_t c) {
+      if (c >= limit) { bad = true; return; }
+      const uint64_t r = c - lo;
+      if (r < kRangeBins) atomicAdd(&hr[r], 1u);
+    });
+  if (bad && blockIdx.y == 0) atomicOr(status, kErrSymbol);
+  __syncthreads();
+  for (int i = threadIdx.x; i < kRangeBins; i += kRangeThreads)
+    if (hr[i] && lo + i < limit) atomicAdd(&hist[lo + i], (unsigned long long)hr[i]);
+}
+
 int hist_grid(uint64_t n, uint32_t width) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -228,7 +261,22 @@ void hist_dispatch(const T* text, uint64_t n, uint32_t levels, unsigned long lon
     leaf_hist_smem<T, 256, true><<<grid, kHistThreads, 0, s>>>(text, n, levels, hist, status);
   else if (levels <= 13)
     leaf_hist_smem<T, 8192, false><<<grid, kHistThreads, 0, s>>>(text, n, levels, hist, status);
-  else
+  else if (levels <= 16) {
+    static bool configured = false;
+    if (!configured) {
+      cudaFuncSetAttribute(leaf_hist_ranges<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRangeBins * 4);
+      configured = true;
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint32_t ranges = uint32_t(((uint64_t(1) << levels) + kRangeBins - 1) / kRangeBins);
+    const uint64_t blocks = std::max<uint64_t>(1, std::min<uint64_t>(uint64_t(sms > 0 ? sms : 148),
+                                                                    (n + 65535) / 65536));
+    const uint64_t chunk = (((n + blocks - 1) / blocks) + 15) & ~uint64_t(15);  // keeps 16-byte alignment
+    dim3 g(unsigned((n + chunk - 1) / chunk), ranges);
+    leaf_hist_ranges<T><<<g, kRangeThreads, kRangeBins * 4, s>>>(text, n, levels, chunk, hist, status);
+  } else
     leaf_hist_global<T><<<grid, kHistThreads, 0, s>>>(text, n, levels, hist, status);
 }
 
