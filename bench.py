@@ -501,9 +501,8 @@ def main():
     wt_ptr = ctypes.cast(out_wt.data_ptr(), pg._lib.u64p)
 
     def e2e_step():
-        ctx.check(ctx.lib.pwmgpu_wx_build_host(ctx.h, ds.h, host_text.data_ptr()))
-        ctx.check(ctx.lib.pwmgpu_wx_download(ctx.h, ds.h, 0, wm_ptr, zp))
-        ctx.check(ctx.lib.pwmgpu_wx_download(ctx.h, ds.h, 1, wt_ptr, None))
+        # host text in, both structures out: the levels stream back while the build runs
+        ctx.check(ctx.lib.pwmgpu_wx_compute_host(ctx.h, ds.h, host_text.data_ptr(), wm_ptr, zp, wt_ptr))
 
     e2e_step()
     barrier()

@@ -94,20 +94,24 @@ PWMGPU_API pwmgpu_status pwmgpu_ctx_profile_read(pwmgpu_ctx* ctx, char* buf, uin
  * both engines (defaults: 4 for the tile engine, 2 for the warp-pass engine). */
 PWMGPU_API pwmgpu_status pwmgpu_ctx_set_pass_levels(pwmgpu_ctx* ctx, int levels_per_pass);
 
-/* Split engines of plain builds.  TILE (default): CTA-wide splits of whole
- * tiles that write matrix and tree levels together (levels <= 20).  WARP:
- * warp-autonomous split passes that write the matrix, with the tree levels
- * regrouped from it (every plain build; Huffman builds and batches always use
- * it).  Both give identical structures. */
 /* Stream-ordered device allocations (cudaMallocAsync / cudaFreeAsync on the
  * context's stream) for the structures and scratch of this context: freeing
  * does not synchronise the device, so contexts on other streams keep running.
  * Freed memory stays in the process's default pool. */
 PWMGPU_API pwmgpu_status pwmgpu_ctx_set_stream_ordered_alloc(pwmgpu_ctx* ctx, int enable);
 
+/* Split engines of plain builds.  TILE (default): CTA-wide splits of whole
+ * tiles that write matrix and tree levels together (levels <= 20).  WARP:
+ * warp-autonomous split passes that write the matrix, with the tree levels
+ * regrouped from it (every plain build; Huffman builds and batches always use
+ * it).  Both give identical structures. */
 #define PWMGPU_ENGINE_TILE 0
 #define PWMGPU_ENGINE_WARP 1
 PWMGPU_API pwmgpu_status pwmgpu_ctx_set_engine(pwmgpu_ctx* ctx, int engine);
+
+/* Bytes of text per piece when a pinned host text is uploaded in pieces
+ * (default 64 MiB; rounded to the histogram's blocks of 2^18 symbols). */
+PWMGPU_API pwmgpu_status pwmgpu_ctx_set_upload_piece_bytes(pwmgpu_ctx* ctx, uint64_t bytes);
 
 /* ---------------------------------------------------------------------- */
 /* Drop-in construction (host text in, host bit vectors out)               */
@@ -164,9 +168,17 @@ PWMGPU_API pwmgpu_status pwmgpu_wx_create(pwmgpu_ctx* ctx, uint64_t size, uint32
  * Asynchronous on the context's stream; errors detected on the device are
  * reported by the next call that synchronises (pwmgpu_wx_check). */
 PWMGPU_API pwmgpu_status pwmgpu_wx_build(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text);
-/* Same as pwmgpu_wx_build from a host text (copied in by the library; pinned
- * host memory makes the copy asynchronous). */
+/* Same as pwmgpu_wx_build from a host text (copied in by the library; from
+ * pinned host memory in pieces that the histogram follows as they arrive). */
 PWMGPU_API pwmgpu_status pwmgpu_wx_build_host(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* host_text);
+/* Host text in, host structures out: builds into `wx` and copies the matrix
+ * words (wm_bv, with its zeros) and the tree words (wt_bv) in the layout of
+ * pwmgpu_wx_download; any output may be NULL.  With pinned host arrays the
+ * text is uploaded in pieces and every level group is copied back as soon as
+ * its pass completes, overlapping the rest of the build.  Returns when the
+ * outputs are on the host. */
+PWMGPU_API pwmgpu_status pwmgpu_wx_compute_host(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* host_text,
+                                                uint64_t* wm_bv, uint64_t* wm_zeros, uint64_t* wt_bv);
 /* Synchronises and reports device-side errors (bad symbol, timeout). */
 PWMGPU_API pwmgpu_status pwmgpu_wx_check(pwmgpu_ctx* ctx, pwmgpu_wx* wx);
 /* which: 0 = matrix, 1 = tree. */

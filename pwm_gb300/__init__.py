@@ -77,6 +77,10 @@ class Context:
         """ENGINE_TILE (default) or ENGINE_WARP for plain builds."""
         self.check(self.lib.pwmgpu_ctx_set_engine(self.h, int(engine)))
 
+    def set_upload_piece_bytes(self, nbytes):
+        """Piece size of pinned host-text uploads (default 64 MiB)."""
+        self.check(self.lib.pwmgpu_ctx_set_upload_piece_bytes(self.h, int(nbytes)))
+
     def close(self):
         if getattr(self, "h", None):
             self.lib.pwmgpu_ctx_destroy(self.h)
@@ -380,6 +384,19 @@ class DeviceStructure:
     def build(self, d_text_ptr):
         """Builds from a device pointer (e.g. a torch tensor's data_ptr())."""
         self.ctx.check(self.ctx.lib.pwmgpu_wx_build(self.ctx.h, self.h, ctypes.c_void_p(int(d_text_ptr))))
+
+    def build_host(self, text_ptr):
+        """Builds from a host pointer (pinned memory is uploaded in pieces)."""
+        self.ctx.check(self.ctx.lib.pwmgpu_wx_build_host(self.ctx.h, self.h, ctypes.c_void_p(int(text_ptr))))
+
+    def compute_host(self, text_ptr, wm_ptr=None, wm_zeros=None, wt_ptr=None):
+        """Host text in, host words out (pointers to u64 arrays in the layout
+        of download(); pinned arrays stream the levels back during the build).
+        wm_zeros: a numpy u64 array of `levels` entries, or None."""
+        lib = self.ctx.lib
+        cast = lambda p: ctypes.cast(ctypes.c_void_p(int(p)), _lib.u64p) if p is not None else None
+        self.ctx.check(lib.pwmgpu_wx_compute_host(self.ctx.h, self.h, ctypes.c_void_p(int(text_ptr)), cast(wm_ptr),
+                                                  _u64p(wm_zeros) if wm_zeros is not None else None, cast(wt_ptr)))
 
     def check(self):
         self.ctx.check(self.ctx.lib.pwmgpu_wx_check(self.ctx.h, self.h))

@@ -59,6 +59,8 @@ SIGNATURES = {
     "pwmgpu_ctx_profile": (i32, [vp, i32]),
     "pwmgpu_ctx_profile_read": (i32, [vp, ctypes.c_char_p, u64]),
     "pwmgpu_wx_build_host": (i32, [vp, vp, vp]),
+    "pwmgpu_wx_compute_host": (i32, [vp, vp, vp, u64p, u64p, u64p]),
+    "pwmgpu_ctx_set_upload_piece_bytes": (i32, [vp, u64]),
     "pwmgpu_compute": (i32, [vp, vp, u64, u32, u32, i32, u64p, u64p]),
     "pwmgpu_huffman_codes": (i32, [vp, vp, u64, u32, i32, u64p, u64p, u64, u64p, u64p, u32p]),
     "pwmgpu_compute_huffman": (i32, [vp, vp, u64, u32, i32, u64p, u64p, u64, u32, u64p, u64p, u64p]),

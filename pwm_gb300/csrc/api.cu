@@ -2,6 +2,7 @@
 // structures, the drop-in host-to-host constructions, the Huffman code
 // builder, queries and generators.
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -68,6 +69,7 @@ struct pwmgpu_ctx {
   int pass_levels = kDefaultPassLevels;
   int tile_levels = kDefaultTileLevels;
   int engine = PWMGPU_ENGINE_TILE;
+  uint64_t upload_piece = uint64_t(64) << 20;  // bytes of text per uploaded piece
   bool async_alloc = false;  // stream-ordered allocations on `stream`
   uint64_t scratch_bytes = 0;
   pwmgpu_wx* compute_cache = nullptr;  // reused by pwmgpu_compute for equal shapes
@@ -136,6 +138,30 @@ struct pwmgpu_ctx {
     CUDA_TRY(cudaEventCreateWithFlags(&aux_ready, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&aux_done, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&aux_done2, cudaEventDisableTiming));
+  }
+  // Transfer streams of host-to-host builds (uploads, downloads) and the
+  // events that order them against the main stream; every call that uses
+  // them waits for them before it returns, so the events are reused.
+  cudaStream_t up = nullptr, down = nullptr;
+  std::vector<cudaEvent_t> xev;
+  size_t xev_used = 0;
+  void xfer_init() {
+    if (!up) {
+      CUDA_TRY(cudaStreamCreateWithFlags(&up, cudaStreamNonBlocking));
+      CUDA_TRY(cudaStreamCreateWithFlags(&down, cudaStreamNonBlocking));
+    }
+    xev_used = 0;
+  }
+  // an event recorded on `after`'s current work
+  cudaEvent_t mark(cudaStream_t after) {
+    if (xev_used == xev.size()) {
+      cudaEvent_t e;
+      CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      xev.push_back(e);
+    }
+    cudaEvent_t e = xev[xev_used++];
+    CUDA_TRY(cudaEventRecord(e, after));
+    return e;
   }
   ~pwmgpu_ctx();
 };
@@ -224,6 +250,12 @@ pwmgpu_ctx::~pwmgpu_ctx() {
     cudaEventDestroy(aux_done);
     cudaEventDestroy(aux_done2);
   }
+  for (cudaStream_t t : {up, down})
+    if (t) {
+      cudaStreamSynchronize(t);
+      cudaStreamDestroy(t);
+    }
+  for (auto e : xev) cudaEventDestroy(e);
   if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
@@ -486,12 +518,16 @@ struct TileFirstPass {
   const uint32_t* relpre = nullptr;
   const uint32_t* tilecnt = nullptr;
   uint32_t tiles_per_block = 0;
+  bool level0_written = false;  // the histogram kernel wrote level 0 of both structures
 };
 
+// after_pass(i) runs on the host once pass i is enqueued, and
+// after_pass(passes.size()) once the regroup is.
 void run_tile_passes(pwmgpu_ctx* ctx, const void* d_text, uint32_t width, uint32_t L,
                      const std::vector<TilePassHost>& passes, const std::vector<uint32_t>& regroup,
                      const LevelTables& tabs, Structure& wm, Structure* wt, const TileFirstPass* first = nullptr,
-                     bool levels_zeroed = false, cudaEvent_t deeper_zeroed = nullptr) {
+                     bool levels_zeroed = false, cudaEvent_t deeper_zeroed = nullptr,
+                     const std::function<void(size_t)>& after_pass = {}) {
   cudaStream_t s = ctx->stream;
   const uint64_t n = tabs.level_bits.empty() ? 0 : tabs.level_bits[0];
 
@@ -563,14 +599,17 @@ void run_tile_passes(pwmgpu_ctx* ctx, const void* d_text, uint32_t width, uint32
       a.relpre = first->relpre;
       a.tilecnt = first->tilecnt;
       a.tiles_per_block = first->tiles_per_block;
+      a.first_level_written = first->level0_written ? 1u : 0u;
     }
     {
       const uint64_t structs = (wt && p.segmented) ? 2 : 1;
-      ProfScope ps(ctx, "split_pass", structs * uint64_t(p.K) * (n * width + words_for(n) * 8));
+      const uint64_t skipped = a.first_level_written ? structs * words_for(n) * 8 : 0;
+      ProfScope ps(ctx, "split_pass", structs * uint64_t(p.K) * (n * width + words_for(n) * 8) - skipped);
       launch_tile_pass(width, p.K, p.out, a, s, &ctx->launches);
     }
     CUDA_TRY(cudaGetLastError());
     if (p.out) in = a.out;
+    if (after_pass) after_pass(pi);
   }
 
   if (wt && !regroup.empty()) {
@@ -594,6 +633,7 @@ void run_tile_passes(pwmgpu_ctx* ctx, const void* d_text, uint32_t width, uint32
     }
     CUDA_TRY(cudaGetLastError());
   }
+  if (after_pass) after_pass(passes.size());
   // the host plan must outlive the async copies
   CUDA_TRY(cudaStreamSynchronize(s));
 }
@@ -605,12 +645,54 @@ void validate_plain(uint64_t n, uint32_t width, uint32_t levels) {
   if (n >= (uint64_t(1) << 62)) throw Fail{PWMGPU_ERR_ARG, "size too large"};
 }
 
-// Plain build of a wx from a device text.
-void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text) {
+// Host ends of a plain build.  `text` (pinned: uploaded in pieces that the
+// histogram follows; else in one copy) is copied into the build's device
+// text; `wm` / `wt` receive the structures' words in their device layout,
+// streamed level group by level group as the passes complete when they are
+// pinned, else copied at the end.  The build returns once they are on the
+// host.
+struct HostIO {
+  const void* text = nullptr;
+  uint64_t* wm = nullptr;
+  uint64_t* wt = nullptr;
+};
+
+bool host_pinned(const void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+// Plain build of a wx from a device text (with `io`: from a host text, into
+// host arrays; d_text is then the device copy to fill).
+void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostIO* io = nullptr) {
   cudaStream_t s = ctx->stream;
   const uint32_t L = wx->levels;
   const uint64_t n = wx->n;
   if (n == 0) return;
+  const bool pinned_in = io && io->text && host_pinned(io->text);
+  uint64_t* host_out[2] = {io ? io->wm : nullptr, io ? io->wt : nullptr};
+  bool any_out = false, all_pinned = true;
+  for (int st = 0; st < 2; ++st)
+    if (host_out[st] && (st ? wx->wt.present : wx->wm.present)) {
+      any_out = true;
+      all_pinned = all_pinned && host_pinned(host_out[st]);
+    }
+  const bool stream_out = any_out && all_pinned;
+  if (pinned_in || stream_out) ctx->xfer_init();
+  // the transfer streams are idle again when the build returns or throws
+  struct XferDrain {
+    pwmgpu_ctx* c;
+    ~XferDrain() {
+      if (c->up) cudaStreamSynchronize(c->up);
+      if (c->down) cudaStreamSynchronize(c->down);
+    }
+  } drain{ctx};
+  if (io && io->text && !pinned_in)
+    CUDA_TRY(cudaMemcpyAsync(const_cast<void*>(d_text), io->text, n * wx->width, cudaMemcpyHostToDevice, s));
   CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, 4, s));
   const uint64_t bins = uint64_t(1) << L;
   auto* d_hist = static_cast<unsigned long long*>(ctx->grow("hist", bins * 8));
@@ -648,22 +730,60 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text) {
   TileFirstPass first{};
   const int K0 = std::min<int>(std::min(ctx->tile_levels, kTileMaxLevels), int(L));
   const uint32_t D0 = uint32_t(K0 < int(L) ? K0 : K0 - 1);
+  // words of each structure already streamed to the host (a prefix of level 0)
+  uint64_t sent[2] = {0, 0};
+  Structure* sts[2] = {&wx->wm, &wx->wt};
+  auto send = [&](int st, uint64_t w0, uint64_t w1) {  // after the main stream's current work
+    if (w1 <= w0) return;
+    CUDA_TRY(cudaStreamWaitEvent(ctx->down, ctx->mark(s), 0));
+    CUDA_TRY(cudaMemcpyAsync(host_out[st] + w0, sts[st]->d_words + w0, (w1 - w0) * 8, cudaMemcpyDeviceToHost,
+                             ctx->down));
+  };
   if (tile_engine && L <= 8 && D0 >= 1) {
     const uint32_t T = tile_pass_elems(wx->width);
     const uint64_t tiles = (n + T - 1) / T;
     const uint32_t per = tile_hist_tiles_per_block();
-    const uint64_t nblocks = (tiles + per - 1) / per;
+    const uint32_t nblocks = tile_hist_blocks(n, T);
     const uint64_t NB = uint64_t(1) << D0;
     auto* base = static_cast<unsigned char*>(ctx->grow("tile_first", tiles * NB * 8 + nblocks * NB * 8 + 256));
     first.tilecnt = reinterpret_cast<uint32_t*>(base);
     first.relpre = first.tilecnt + tiles * NB;
     first.blockpre = reinterpret_cast<unsigned long long*>(base + ((tiles * NB * 8 + 15) & ~uint64_t(15)));
     first.tiles_per_block = per;
-    ProfScope ps(ctx, "leaf_histogram", n * wx->width);
-    launch_tile_histogram(d_text, n, wx->width, L, D0, T, d_hist, const_cast<uint32_t*>(first.tilecnt),
-                          const_cast<uint32_t*>(first.relpre), const_cast<unsigned long long*>(first.blockpre),
-                          ctx->d_status, s, &ctx->launches);
+    first.level0_written = true;
+    uint64_t* l0[2] = {wx->wm.present ? wx->wm.d_words : nullptr, wx->wt.present ? wx->wt.d_words : nullptr};
+    if (!l0[0]) std::swap(l0[0], l0[1]);
+    // pieces of whole histogram blocks: uploaded, counted, their level-0 words sent back
+    const uint64_t block_keys = uint64_t(per) * T;
+    const uint32_t piece_blocks =
+        pinned_in ? uint32_t(std::max<uint64_t>(1, ctx->upload_piece / (block_keys * wx->width))) : nblocks;
+    ProfScope ps(ctx, "leaf_histogram", n * wx->width + (l0[1] ? 2 : 1) * words_for(n) * 8);
+    for (uint32_t b0 = 0; b0 < nblocks; b0 += piece_blocks) {
+      const uint32_t nb = std::min(piece_blocks, nblocks - b0);
+      const uint64_t k0 = uint64_t(b0) * block_keys, k1 = std::min(n, uint64_t(b0 + nb) * block_keys);
+      if (pinned_in) {
+        CUDA_TRY(cudaMemcpyAsync(static_cast<unsigned char*>(const_cast<void*>(d_text)) + k0 * wx->width,
+                                 static_cast<const unsigned char*>(io->text) + k0 * wx->width, (k1 - k0) * wx->width,
+                                 cudaMemcpyHostToDevice, ctx->up));
+        CUDA_TRY(cudaStreamWaitEvent(s, ctx->mark(ctx->up), 0));
+      }
+      launch_tile_histogram_blocks(d_text, n, wx->width, L, D0, T, b0, nb, d_hist,
+                                   const_cast<uint32_t*>(first.tilecnt), const_cast<uint32_t*>(first.relpre),
+                                   const_cast<unsigned long long*>(first.blockpre), l0[0], l0[1], ctx->d_status, s,
+                                   &ctx->launches);
+      if (stream_out) {
+        const uint64_t w1 = k1 == n ? words_for(n) : k1 / 64;
+        for (int st = 0; st < 2; ++st)
+          if (host_out[st] && sts[st]->present) {
+            send(st, sent[st], w1);
+            sent[st] = w1;
+          }
+      }
+    }
+    launch_tile_block_scan(const_cast<unsigned long long*>(first.blockpre), nblocks, D0, s, &ctx->launches);
   } else {
+    if (pinned_in) CUDA_TRY(cudaMemcpyAsync(const_cast<void*>(d_text), io->text, n * wx->width,
+                                            cudaMemcpyHostToDevice, s));
     ProfScope ps(ctx, "leaf_histogram", n * wx->width);
     launch_leaf_histogram(d_text, n, wx->width, L, d_hist, ctx->d_status, s, &ctx->launches);
   }
@@ -687,17 +807,54 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text) {
   }
   wx->wm.zeros = tabs.zeros;
   CUDA_TRY(cudaMemcpyAsync(wx->wm.d_zeros, wx->wm.zeros.data(), L * 8, cudaMemcpyHostToDevice, s));
+  // Streaming the structures back: after each pass its levels of the
+  // structures it completes (tree levels left to the regroup come last).
+  auto level_end = [&](const Structure& st, uint32_t m) { return m + 1 < st.levels ? st.offs[m + 1] : st.total_words; };
+  auto after_pass = [&](size_t pi) {
+    for (int st = 0; st < 2; ++st) {
+      if (!host_out[st] || !sts[st]->present) continue;
+      const Structure& S = *sts[st];
+      uint64_t w1 = sent[st];
+      if (pi < tile_passes.size()) {
+        const TilePassHost& p = tile_passes[pi];
+        if (st == 1 && !p.segmented) continue;
+        w1 = level_end(S, p.level + p.K - 1);
+      } else {
+        w1 = S.total_words;
+      }
+      // levels complete in order for the matrix; a tree level left to the
+      // regroup holds back the tree's later levels until the end
+      if (st == 1 && pi < tile_passes.size()) {
+        bool gap = false;
+        for (uint32_t m : regroup) gap |= level_end(S, m) <= w1;
+        if (gap) continue;
+      }
+      send(st, sent[st], w1);
+      sent[st] = std::max(sent[st], w1);
+    }
+  };
   if (tile_engine) {
     CUDA_TRY(cudaStreamWaitEvent(s, ctx->aux_done, 0));
     CUDA_TRY(cudaStreamWaitEvent(s, ctx->aux_done2, 0));
     run_tile_passes(ctx, d_text, wx->width, L, tile_passes, regroup, tabs, wx->wm, want_tree ? &wx->wt : nullptr,
-                    first.blockpre ? &first : nullptr, true);
+                    first.blockpre ? &first : nullptr, true, nullptr,
+                    stream_out ? std::function<void(size_t)>(after_pass) : std::function<void(size_t)>());
   }
   else
     run_passes(ctx, d_text, wx->width, wx->width, false, L, plan, tabs, wx->wm, want_tree ? &wx->wt : nullptr);
   if (wx->wm.rs && !wx->wm_internal) build_rank_select(ctx, wx->wm);
   if (want_tree && wx->wt.rs) build_rank_select(ctx, wx->wt);
   CUDA_TRY(cudaGetLastError());
+  if (any_out) {
+    for (int st = 0; st < 2; ++st) {
+      if (!host_out[st] || !sts[st]->present) continue;
+      const Structure& S = *sts[st];
+      if (stream_out) send(st, sent[st], S.total_words);
+      else CUDA_TRY(cudaMemcpyAsync(host_out[st], S.d_words, S.total_words * 8, cudaMemcpyDeviceToHost, s));
+    }
+    if (stream_out) CUDA_TRY(cudaStreamSynchronize(ctx->down));
+    CUDA_TRY(cudaStreamSynchronize(s));
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1219,6 +1376,12 @@ pwmgpu_status pwmgpu_ctx_set_engine(pwmgpu_ctx* ctx, int engine) {
   return PWMGPU_OK;
 }
 
+pwmgpu_status pwmgpu_ctx_set_upload_piece_bytes(pwmgpu_ctx* ctx, uint64_t bytes) {
+  if (!ctx || bytes == 0) return PWMGPU_ERR_ARG;
+  ctx->upload_piece = bytes;
+  return PWMGPU_OK;
+}
+
 pwmgpu_status pwmgpu_ctx_profile(pwmgpu_ctx* ctx, int enable) {
   if (!ctx) return PWMGPU_ERR_ARG;
   ctx->profiling = enable != 0;
@@ -1296,9 +1459,27 @@ pwmgpu_status pwmgpu_wx_build_host(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* h
   if (!ctx || !wx || (!host_text && wx->n)) return PWMGPU_ERR_ARG;
   return guarded(ctx, [&]() {
     void* d_text = ctx->grow("host_text", std::max<uint64_t>(wx->n * wx->width, 1));
-    if (wx->n)
-      CUDA_TRY(cudaMemcpyAsync(d_text, host_text, wx->n * wx->width, cudaMemcpyHostToDevice, ctx->stream));
-    build_plain(ctx, wx, d_text);
+    HostIO io;
+    io.text = host_text;
+    build_plain(ctx, wx, d_text, &io);
+    return PWMGPU_OK;
+  });
+}
+
+pwmgpu_status pwmgpu_wx_compute_host(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* host_text, uint64_t* wm_bv,
+                                     uint64_t* wm_zeros, uint64_t* wt_bv) {
+  if (!ctx || !wx || (!host_text && wx->n)) return PWMGPU_ERR_ARG;
+  if ((wm_bv && (!wx->wm.present || wx->wm_internal)) || (wt_bv && !wx->wt.present))
+    return fail(ctx, PWMGPU_ERR_ARG, "an output structure the wx does not hold");
+  return guarded(ctx, [&]() {
+    void* d_text = ctx->grow("host_text", std::max<uint64_t>(wx->n * wx->width, 1));
+    HostIO io;
+    io.text = host_text;
+    io.wm = wm_bv;
+    io.wt = wt_bv;
+    build_plain(ctx, wx, d_text, &io);
+    check_device_status(ctx);
+    if (wm_zeros && wx->wm.present && !wx->wm_internal) std::memcpy(wm_zeros, wx->wm.zeros.data(), wx->levels * 8);
     return PWMGPU_OK;
   });
 }
@@ -1426,10 +1607,11 @@ pwmgpu_status pwmgpu_compute(pwmgpu_ctx* ctx, const void* text, uint64_t size, u
       if (st != PWMGPU_OK) return st;
     }
     void* d_text = ctx->grow("host_text", size * word_width);
-    CUDA_TRY(cudaMemcpyAsync(d_text, text, size * word_width, cudaMemcpyHostToDevice, ctx->stream));
-    build_plain(ctx, wx, d_text);
+    HostIO io;
+    io.text = text;
+    (is_tree ? io.wt : io.wm) = bv;
+    build_plain(ctx, wx, d_text, &io);
     const Structure& s = is_tree ? wx->wt : wx->wm;
-    CUDA_TRY(cudaMemcpyAsync(bv, s.d_words, s.total_words * 8, cudaMemcpyDeviceToHost, ctx->stream));
     check_device_status(ctx);
     if (!is_tree) std::memcpy(zeros, s.zeros.data(), levels * 8);
     return PWMGPU_OK;

@@ -83,9 +83,11 @@ constexpr int kTileHistThreads = 256;
 template <typename T>
 __global__ void __launch_bounds__(kTileHistThreads) tile_hist_kernel(const T* text, uint64_t n, uint32_t levels,
                                                                  uint32_t D, uint32_t tile_keys,
-                                                                 uint32_t tiles_per_block, unsigned long long* hist,
-                                                                 uint32_t* tilecnt, uint32_t* relpre,
-                                                                 unsigned long long* blocksum, uint32_t* status) {
+                                                                 uint32_t tiles_per_block, uint32_t block0,
+                                                                 unsigned long long* hist, uint32_t* tilecnt,
+                                                                 uint32_t* relpre, unsigned long long* blocksum,
+                                                                 uint64_t* level0_a, uint64_t* level0_b,
+                                                                 uint32_t* status) {
   constexpr int WARPS = kTileHistThreads / 32;
   constexpr int BINS = 256;
   __shared__ uint32_t h[WARPS * BINS];
@@ -99,7 +101,16 @@ __global__ void __launch_bounds__(kTileHistThreads) tile_hist_kernel(const T* te
   uint32_t prev = 0;  // thread b < bins: the block's count of symbol b so far
   uint32_t rel = 0;   // thread c < NB: the block's count of run c before the current tile
   bool bad = false;
-  const uint64_t first_tile = uint64_t(blockIdx.x) * tiles_per_block;
+  const uint32_t block = block0 + blockIdx.x;
+  const uint64_t first_tile = uint64_t(block) * tiles_per_block;
+  const int lane = tid & 31, warp = tid >> 5;
+  const uint32_t l0shift = levels - 1;  // level 0 holds the symbols' top bit
+  // Level 0 of the structures (text order, MSB first): word of 64 symbols
+  // out of 64 / PER threads' vector bit masks.
+  auto store_level0 = [&](uint64_t word_index, uint64_t word) {
+    level0_a[word_index] = word;
+    if (level0_b) level0_b[word_index] = word;
+  };
   auto count = [&](uint32_t c) {
     if (c >= bins) { bad = true; return; }
     atomicAdd(&mine[c], 1u);
@@ -136,6 +147,19 @@ __global__ void __launch_bounds__(kTileHistThreads) tile_hist_kernel(const T* te
         for (int v = 0; v < HV; ++v)
           if (v < nv) ahead[v] = __ldcs(q + tid + v * kTileHistThreads);
       }
+      if (level0_a) {
+        constexpr int LPC = 32 / PER;  // threads per 32 symbols
+#pragma unroll
+        for (int v = 0; v < HV; ++v) {
+          if (v >= nv) break;
+          uint32_t x = vector_bits<T>(cur[v], l0shift) << (32 - PER * (1 + (lane % LPC)));
+#pragma unroll
+          for (int d = 1; d < LPC; d <<= 1) x |= __shfl_down_sync(0xFFFFFFFFu, x, d);
+          const uint32_t lo = __shfl_down_sync(0xFFFFFFFFu, x, LPC);
+          if (lane % (2 * LPC) == 0)
+            store_level0((start + uint64_t(tid + v * kTileHistThreads) * PER) >> 6, (uint64_t(x) << 32) | lo);
+        }
+      }
 #pragma unroll
       for (int v = 0; v < HV; ++v) {
         if (v >= nv) break;
@@ -152,6 +176,18 @@ __global__ void __launch_bounds__(kTileHistThreads) tile_hist_kernel(const T* te
         for (int q = 0; q < PER; ++q) count(uint32_t(s[q]));
       }
       for (uint64_t i = nvec * PER + tid; i < len; i += kTileHistThreads) count(uint32_t(p[i]));
+      if (level0_a) {
+        // a word of 64 symbols per warp from two ballots (bit k of a ballot
+        // is lane k: reversed, the first symbol is the most significant)
+        const uint64_t nw = (len + 63) >> 6;
+        for (uint64_t j = warp; j < nw; j += WARPS) {
+          const uint64_t i0 = j * 64 + lane, i1 = i0 + 32;
+          const bool b0 = i0 < len && ((uint32_t(p[i0]) >> l0shift) & 1u);
+          const bool b1 = i1 < len && ((uint32_t(p[i1]) >> l0shift) & 1u);
+          const uint32_t hi = __brev(__ballot_sync(0xFFFFFFFFu, b0)), lo = __brev(__ballot_sync(0xFFFFFFFFu, b1));
+          if (lane == 0) store_level0((start >> 6) + j, (uint64_t(hi) << 32) | lo);
+        }
+      }
     }
     __syncthreads();
     if (tid < int(bins)) {
@@ -175,7 +211,7 @@ __global__ void __launch_bounds__(kTileHistThreads) tile_hist_kernel(const T* te
     __syncthreads();
   }
   if (bad) atomicOr(status, kErrSymbol);
-  if (tid < int(NB)) blocksum[uint64_t(blockIdx.x) * NB + tid] = rel;
+  if (tid < int(NB)) blocksum[uint64_t(block) * NB + tid] = rel;
   if (tid < int(bins) && prev) atomicAdd(&hist[tid], (unsigned long long)prev);
 }
 
@@ -386,24 +422,34 @@ int grid_for(uint64_t n, int threads) {
 
 uint32_t tile_hist_tiles_per_block() { return 16; }
 
-void launch_tile_histogram(const void* text, uint64_t n, uint32_t width, uint32_t levels, uint32_t D,
-                           uint32_t tile_keys, unsigned long long* hist, uint32_t* tilecnt, uint32_t* relpre,
-                           unsigned long long* blocksum, uint32_t* status, cudaStream_t s, uint64_t* launches) {
-  if (n == 0) return;
-  const uint32_t per = tile_hist_tiles_per_block();
+uint32_t tile_hist_blocks(uint64_t n, uint32_t tile_keys) {
   const uint64_t tiles = (n + tile_keys - 1) / tile_keys;
-  const uint32_t nblocks = uint32_t((tiles + per - 1) / per);
-  if (width == 1)
-    tile_hist_kernel<<<nblocks, kTileHistThreads, 0, s>>>(static_cast<const uint8_t*>(text), n, levels, D, tile_keys, per,
-                                                      hist, tilecnt, relpre, blocksum, status);
-  else if (width == 2)
-    tile_hist_kernel<<<nblocks, kTileHistThreads, 0, s>>>(static_cast<const uint16_t*>(text), n, levels, D, tile_keys,
-                                                      per, hist, tilecnt, relpre, blocksum, status);
-  else
-    tile_hist_kernel<<<nblocks, kTileHistThreads, 0, s>>>(static_cast<const uint32_t*>(text), n, levels, D, tile_keys,
-                                                      per, hist, tilecnt, relpre, blocksum, status);
+  return uint32_t((tiles + tile_hist_tiles_per_block() - 1) / tile_hist_tiles_per_block());
+}
+
+void launch_tile_histogram_blocks(const void* text, uint64_t n, uint32_t width, uint32_t levels, uint32_t D,
+                                  uint32_t tile_keys, uint32_t block0, uint32_t nblk, unsigned long long* hist,
+                                  uint32_t* tilecnt, uint32_t* relpre, unsigned long long* blocksum,
+                                  uint64_t* level0_a, uint64_t* level0_b, uint32_t* status, cudaStream_t s,
+                                  uint64_t* launches) {
+  if (n == 0 || nblk == 0) return;
+  const uint32_t per = tile_hist_tiles_per_block();
+#define PWMGPU_TH(T)                                                                                          \
+  tile_hist_kernel<<<nblk, kTileHistThreads, 0, s>>>(static_cast<const T*>(text), n, levels, D, tile_keys, per, \
+                                                     block0, hist, tilecnt, relpre, blocksum, level0_a,        \
+                                                     level0_b, status)
+  if (width == 1) PWMGPU_TH(uint8_t);
+  else if (width == 2) PWMGPU_TH(uint16_t);
+  else PWMGPU_TH(uint32_t);
+#undef PWMGPU_TH
+  ++*launches;
+}
+
+void launch_tile_block_scan(unsigned long long* blocksum, uint32_t nblocks, uint32_t D, cudaStream_t s,
+                            uint64_t* launches) {
+  if (nblocks == 0) return;
   tile_block_scan_kernel<<<1, 1024, 0, s>>>(blocksum, nblocks, 1u << D);
-  *launches += 2;
+  ++*launches;
 }
 
 void launch_leaf_histogram(const void* text, uint64_t n, uint32_t width, uint32_t levels, unsigned long long* hist,

@@ -16,14 +16,24 @@ void launch_leaf_histogram(const void* text, uint64_t n, uint32_t width, uint32_
                            unsigned long long* hist, uint32_t* status, cudaStream_t s, uint64_t* launches);
 
 // Leaf histogram of a text with levels <= 8 that also counts, per tile of
-// tile_keys symbols, the 2^D runs of the first D symbol bits (first bit least
-// significant): tilecnt[tile][run], relpre[tile][run] (prefix inside a block
-// of tile_hist_tiles_per_block() tiles) and blocksum[block][run], which the
-// launch turns into each block's exclusive prefix.  hist must be zeroed.
+// tile_keys symbols (a multiple of 64), the 2^D runs of the first D symbol
+// bits (first bit least significant): tilecnt[tile][run], relpre[tile][run]
+// (prefix inside a block of tile_hist_tiles_per_block() tiles) and
+// blocksum[block][run].  Blocks [block0, block0 + nblk) of the
+// tile_hist_blocks(n, tile_keys) blocks run, so a text can be counted piece
+// by piece as it arrives; when level0_a is set, they also write level 0
+// (the symbols' top bits in text order) to level0_a and level0_b (if set).
+// hist must be zeroed.  launch_tile_block_scan then turns blocksum into each
+// block's exclusive prefix.
 uint32_t tile_hist_tiles_per_block();
-void launch_tile_histogram(const void* text, uint64_t n, uint32_t width, uint32_t levels, uint32_t D,
-                           uint32_t tile_keys, unsigned long long* hist, uint32_t* tilecnt, uint32_t* relpre,
-                           unsigned long long* blocksum, uint32_t* status, cudaStream_t s, uint64_t* launches);
+uint32_t tile_hist_blocks(uint64_t n, uint32_t tile_keys);
+void launch_tile_histogram_blocks(const void* text, uint64_t n, uint32_t width, uint32_t levels, uint32_t D,
+                                  uint32_t tile_keys, uint32_t block0, uint32_t nblk, unsigned long long* hist,
+                                  uint32_t* tilecnt, uint32_t* relpre, unsigned long long* blocksum,
+                                  uint64_t* level0_a, uint64_t* level0_b, uint32_t* status, cudaStream_t s,
+                                  uint64_t* launches);
+void launch_tile_block_scan(unsigned long long* blocksum, uint32_t nblocks, uint32_t D, cudaStream_t s,
+                            uint64_t* launches);
 
 // ---- split passes -----------------------------------------------------------
 // Geometry of the split pass for a key width: tile size in elements.

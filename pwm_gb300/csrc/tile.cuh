@@ -88,6 +88,7 @@ struct TileArgs {
   const uint32_t* relpre;
   const uint32_t* tilecnt;
   uint32_t tiles_per_block;
+  uint32_t first_level_written;  // level l is already written (by the histogram kernel)
 };
 
 template <typename KeyT, int K, bool OUT, int THREADS, int V>
@@ -590,7 +591,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tile_pass_kernel(Tile
 
   // ---- level l (one run, needs no prefix), then the look-back -------------
   const int nstruct = s_tx.wt ? 2 : 1;
-  for (int st = 0; st < nstruct; ++st) {
+  for (int st = 0; st < (a.first_level_written ? 0 : nstruct); ++st) {
     const uint64_t dst = s_table[st ? tile_wt_entry(K, 0, 0) : tile_wm_entry(0, 0)] + tstart;
     write_bits64(st ? s_tx.wt : s_tx.wm, s_tx.nbits, dst, sbits, 0, n, uint32_t(tid), uint32_t(THREADS), a.status);
   }
