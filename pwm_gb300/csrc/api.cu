@@ -128,17 +128,6 @@ struct pwmgpu_ctx {
     }
     return b.p;
   }
-  // Auxiliary stream for work that overlaps the main stream (zeroing the
-  // levels of a build while its histogram runs); created on first use.
-  cudaStream_t aux = nullptr;
-  cudaEvent_t aux_ready = nullptr, aux_done = nullptr, aux_done2 = nullptr;
-  void aux_init() {
-    if (aux) return;
-    CUDA_TRY(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
-    CUDA_TRY(cudaEventCreateWithFlags(&aux_ready, cudaEventDisableTiming));
-    CUDA_TRY(cudaEventCreateWithFlags(&aux_done, cudaEventDisableTiming));
-    CUDA_TRY(cudaEventCreateWithFlags(&aux_done2, cudaEventDisableTiming));
-  }
   // Transfer streams of host-to-host builds (uploads, downloads) and the
   // events that order them against the main stream; every call that uses
   // them waits for them before it returns, so the events are reused.
@@ -243,13 +232,6 @@ pwmgpu_ctx::~pwmgpu_ctx() {
   if (async_alloc && stream) cudaStreamSynchronize(stream);
   if (d_status) cudaFree(d_status);
   if (pinned) cudaFreeHost(pinned);
-  if (aux) {
-    cudaStreamSynchronize(aux);
-    cudaStreamDestroy(aux);
-    cudaEventDestroy(aux_ready);
-    cudaEventDestroy(aux_done);
-    cudaEventDestroy(aux_done2);
-  }
   for (cudaStream_t t : {up, down})
     if (t) {
       cudaStreamSynchronize(t);
@@ -381,6 +363,9 @@ void alloc_structure(Structure& s, const std::vector<uint64_t>& level_bits, uint
   s.n = n;
   s.set_layout(level_bits);
   dev_alloc(&s.d_words, std::max<uint64_t>(s.total_words, 16) * 8, alloc_stream);
+  // padding bits and words are never written by a build: zero from here on
+  if (alloc_stream) CUDA_TRY(cudaMemsetAsync(s.d_words, 0, std::max<uint64_t>(s.total_words, 16) * 8, alloc_stream));
+  else CUDA_TRY(cudaMemset(s.d_words, 0, std::max<uint64_t>(s.total_words, 16) * 8));
   dev_alloc(&s.d_zeros, std::max<uint32_t>(s.levels, 1) * 8, alloc_stream);
   if (rank_select) alloc_rank_select(s);
 }
@@ -504,8 +489,8 @@ void run_passes(pwmgpu_ctx* ctx, const void* keys, uint32_t key_bytes, uint32_t 
     }
     CUDA_TRY(cudaGetLastError());
   }
-  // host segment vectors must outlive the async copies
-  CUDA_TRY(cudaStreamSynchronize(s));
+  // (copies from pageable host vectors return once the data is staged, so
+  // the plan may go out of scope with the passes still running)
 }
 
 // ---------------------------------------------------------------------------
@@ -526,8 +511,10 @@ struct TileFirstPass {
 void run_tile_passes(pwmgpu_ctx* ctx, const void* d_text, uint32_t width, uint32_t L,
                      const std::vector<TilePassHost>& passes, const std::vector<uint32_t>& regroup,
                      const LevelTables& tabs, Structure& wm, Structure* wt, const TileFirstPass* first = nullptr,
-                     bool levels_zeroed = false, cudaEvent_t deeper_zeroed = nullptr,
                      const std::function<void(size_t)>& after_pass = {}) {
+  // Edge words are OR-ed, so every level is zeroed before its pass: the first
+  // pass's by the caller (below, or by the histogram kernel), the others by
+  // the pass before, a slab per tile.
   cudaStream_t s = ctx->stream;
   const uint64_t n = tabs.level_bits.empty() ? 0 : tabs.level_bits[0];
 
@@ -564,13 +551,6 @@ void run_tile_passes(pwmgpu_ctx* ctx, const void* d_text, uint32_t width, uint32
   auto* d_blob = static_cast<unsigned char*>(ctx->grow("tile_plan", std::max<size_t>(blob.size(), 16)));
   CUDA_TRY(cudaMemcpyAsync(d_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice, s));
 
-  // runs are OR-ed into their edge words: the levels must be zero (done here
-  // unless the caller zeroed them on the auxiliary stream)
-  if (!levels_zeroed) {
-    CUDA_TRY(cudaMemsetAsync(wm.d_words, 0, wm.total_words * 8, s));
-    if (wt) CUDA_TRY(cudaMemsetAsync(wt->d_words, 0, wt->total_words * 8, s));
-  }
-
   void* ping = ctx->grow("keys_a", std::max<uint64_t>(n, 1) * width);
   void* pong = ctx->grow("keys_b", std::max<uint64_t>(n, 1) * width);
   const void* in = d_text;
@@ -581,7 +561,6 @@ void run_tile_passes(pwmgpu_ctx* ctx, const void* d_text, uint32_t width, uint32
     const uint64_t lb_bytes = uint64_t(std::max<uint32_t>(p.tiles, 1)) * nlb * 8;
     auto* lb = static_cast<unsigned long long*>(ctx->grow("lookback", lb_bytes + 64));
     CUDA_TRY(cudaMemsetAsync(lb, 0, lb_bytes + 64, s));
-    if (pi == 1 && deeper_zeroed) CUDA_TRY(cudaStreamWaitEvent(s, deeper_zeroed, 0));
     TileArgs a{};
     a.in = in;
     a.out = p.out ? (in == ping ? pong : ping) : nullptr;
@@ -594,6 +573,15 @@ void run_tile_passes(pwmgpu_ctx* ctx, const void* d_text, uint32_t width, uint32
     a.status = ctx->d_status;
     a.nsegs = uint32_t(p.segs.size());
     a.tiles = p.tiles;
+    if (pi + 1 < passes.size()) {
+      const auto& q = passes[pi + 1];
+      const uint32_t l1 = q.level + q.K - 1;
+      a.zero_a = wm.d_words + wm.offs[q.level];
+      a.zero_b = wt ? wt->d_words + wt->offs[q.level] : nullptr;
+      a.zero_words = (l1 + 1 < wm.levels ? wm.offs[l1 + 1] : wm.total_words) - wm.offs[q.level];
+      const uint64_t per = (a.zero_words + p.tiles - 1) / std::max<uint32_t>(p.tiles, 1);
+      a.zero_per_tile = uint32_t((per + 1) & ~uint64_t(1));
+    }
     if (pi == 0 && first && p.segs.size() == 1) {
       a.blockpre = first->blockpre;
       a.relpre = first->relpre;
@@ -634,8 +622,8 @@ void run_tile_passes(pwmgpu_ctx* ctx, const void* d_text, uint32_t width, uint32
     CUDA_TRY(cudaGetLastError());
   }
   if (after_pass) after_pass(passes.size());
-  // the host plan must outlive the async copies
-  CUDA_TRY(cudaStreamSynchronize(s));
+  // (copies from pageable host vectors return once the data is staged, so
+  // the plan may go out of scope with the passes still running)
 }
 
 void validate_plain(uint64_t n, uint32_t width, uint32_t levels) {
@@ -697,39 +685,23 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   const uint64_t bins = uint64_t(1) << L;
   auto* d_hist = static_cast<unsigned long long*>(ctx->grow("hist", bins * 8));
   CUDA_TRY(cudaMemsetAsync(d_hist, 0, bins * 8, s));
-  // Tile engine: zero the levels (runs are OR-ed into their edge words) on the
-  // auxiliary stream, overlapping the histogram; the passes wait for it.
+  // Tile engine: level 0 is written in whole words (by the histogram kernel,
+  // or by the first pass, whose tiles start at multiples of 64 bits); the
+  // first pass's other levels are zeroed by the histogram kernel (levels <= 8)
+  // or here; the padding is zero from allocation.
   const bool tile_engine = ctx->engine == PWMGPU_ENGINE_TILE && L <= kTilePlanMaxLevels;
-  // Level 0 is written in whole words by the first pass (its tiles start at
-  // multiples of 64 bits): only its padding words need zeroing.  The levels of
-  // the first pass are zeroed while the histogram runs, the deeper ones while
-  // the first pass runs.
   const int Kz = std::min<int>(std::min(ctx->tile_levels, kTileMaxLevels), int(L));
-  if (tile_engine) {
-    ctx->aux_init();
-    CUDA_TRY(cudaEventRecord(ctx->aux_ready, s));  // earlier work on the structures is done first
-    CUDA_TRY(cudaStreamWaitEvent(ctx->aux, ctx->aux_ready, 0));
-    auto zero = [&](Structure& st, uint32_t l0, uint32_t l1) {
-      if (l1 > l0) CUDA_TRY(cudaMemsetAsync(st.d_words + st.offs[l0], 0, (st.offs[l1 - 1] - st.offs[l0] +
-                                                                        padded_words(st.bits[l1 - 1])) * 8, ctx->aux));
-    };
-    for (Structure* st : {&wx->wm, &wx->wt}) {
-      if (!st->present) continue;
-      const uint64_t real = words_for(st->bits[0]), pad = padded_words(st->bits[0]);
-      if (pad > real) CUDA_TRY(cudaMemsetAsync(st->d_words + real, 0, (pad - real) * 8, ctx->aux));
-      zero(*st, 1, uint32_t(Kz));
-    }
-    CUDA_TRY(cudaEventRecord(ctx->aux_done, ctx->aux));
+  const uint32_t D0 = uint32_t(Kz < int(L) ? Kz : Kz - 1);  // splits of the first pass
+  const bool tile_hist = tile_engine && L <= 8 && D0 >= 1;
+  if (tile_engine && !tile_hist && Kz > 1)
     for (Structure* st : {&wx->wm, &wx->wt})
-      if (st->present) zero(*st, uint32_t(Kz), L);
-    CUDA_TRY(cudaEventRecord(ctx->aux_done2, ctx->aux));
-  }
+      if (st->present)
+        CUDA_TRY(cudaMemsetAsync(st->d_words + st->offs[1], 0,
+                                 ((uint32_t(Kz) < L ? st->offs[Kz] : st->total_words) - st->offs[1]) * 8, s));
   // Tile engine, levels <= 8: the histogram kernel also counts the finest runs
   // of every tile of the first pass and scans them, so that pass neither
   // counts nor looks back.
   TileFirstPass first{};
-  const int K0 = std::min<int>(std::min(ctx->tile_levels, kTileMaxLevels), int(L));
-  const uint32_t D0 = uint32_t(K0 < int(L) ? K0 : K0 - 1);
   // words of each structure already streamed to the host (a prefix of level 0)
   uint64_t sent[2] = {0, 0};
   Structure* sts[2] = {&wx->wm, &wx->wt};
@@ -739,7 +711,7 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     CUDA_TRY(cudaMemcpyAsync(host_out[st] + w0, sts[st]->d_words + w0, (w1 - w0) * 8, cudaMemcpyDeviceToHost,
                              ctx->down));
   };
-  if (tile_engine && L <= 8 && D0 >= 1) {
+  if (tile_hist) {
     const uint32_t T = tile_pass_elems(wx->width);
     const uint64_t tiles = (n + T - 1) / T;
     const uint32_t per = tile_hist_tiles_per_block();
@@ -753,6 +725,14 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     first.level0_written = true;
     uint64_t* l0[2] = {wx->wm.present ? wx->wm.d_words : nullptr, wx->wt.present ? wx->wt.d_words : nullptr};
     if (!l0[0]) std::swap(l0[0], l0[1]);
+    // levels 1..Kz-1 of both structures, a slab per tile
+    HistZero hz;
+    if (Kz > 1) {
+      hz.a = l0[0] + wx->wm.offs[1];
+      hz.b = l0[1] ? l0[1] + wx->wm.offs[1] : nullptr;
+      hz.words = (uint32_t(Kz) < L ? wx->wm.offs[Kz] : wx->wm.total_words) - wx->wm.offs[1];
+      hz.per_tile = ((hz.words + tiles - 1) / tiles + 1) & ~uint64_t(1);
+    }
     // pieces of whole histogram blocks: uploaded, counted, their level-0 words sent back
     const uint64_t block_keys = uint64_t(per) * T;
     const uint32_t piece_blocks =
@@ -769,8 +749,8 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
       }
       launch_tile_histogram_blocks(d_text, n, wx->width, L, D0, T, b0, nb, d_hist,
                                    const_cast<uint32_t*>(first.tilecnt), const_cast<uint32_t*>(first.relpre),
-                                   const_cast<unsigned long long*>(first.blockpre), l0[0], l0[1], ctx->d_status, s,
-                                   &ctx->launches);
+                                   const_cast<unsigned long long*>(first.blockpre), l0[0], l0[1], hz, ctx->d_status,
+                                   s, &ctx->launches);
       if (stream_out) {
         const uint64_t w1 = k1 == n ? words_for(n) : k1 / 64;
         for (int st = 0; st < 2; ++st)
@@ -834,10 +814,8 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     }
   };
   if (tile_engine) {
-    CUDA_TRY(cudaStreamWaitEvent(s, ctx->aux_done, 0));
-    CUDA_TRY(cudaStreamWaitEvent(s, ctx->aux_done2, 0));
     run_tile_passes(ctx, d_text, wx->width, L, tile_passes, regroup, tabs, wx->wm, want_tree ? &wx->wt : nullptr,
-                    first.blockpre ? &first : nullptr, true, nullptr,
+                    first.blockpre ? &first : nullptr,
                     stream_out ? std::function<void(size_t)>(after_pass) : std::function<void(size_t)>());
   }
   else

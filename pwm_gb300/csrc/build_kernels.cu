@@ -87,20 +87,24 @@ __global__ void __launch_bounds__(kTileHistThreads) tile_hist_kernel(const T* te
                                                                  unsigned long long* hist, uint32_t* tilecnt,
                                                                  uint32_t* relpre, unsigned long long* blocksum,
                                                                  uint64_t* level0_a, uint64_t* level0_b,
-                                                                 uint32_t* status) {
+                                                                 HistZero zero, uint32_t* status) {
   constexpr int WARPS = kTileHistThreads / 32;
   constexpr int BINS = 256;
-  __shared__ uint32_t h[WARPS * BINS];
+  // One counter per (bin, lane) shared by the block's warps: lane k counts
+  // into column k, so the 32 lanes of an atomic never meet on an address or
+  // a bank, however skewed the text (at most 8 warps x 64 symbols x 16
+  // tiles = 8192 per counter).
+  __shared__ __align__(16) uint32_t h[BINS * 32];
   __shared__ uint32_t s_tc[16];
   const int tid = threadIdx.x;
-  for (int i = tid; i < WARPS * BINS; i += kTileHistThreads) h[i] = 0;
+  for (int i = tid; i < BINS * 32; i += kTileHistThreads) h[i] = 0;
   if (tid < 16) s_tc[tid] = 0;
   __syncthreads();
-  uint32_t* mine = h + (tid >> 5) * BINS;
-  const uint32_t bins = 1u << levels, NB = 1u << D;
+  uint32_t* mine = h + (tid & 31);
+  const uint32_t bins = 1u << levels, NB = 1u << D, binmask = bins - 1;
   uint32_t prev = 0;  // thread b < bins: the block's count of symbol b so far
   uint32_t rel = 0;   // thread c < NB: the block's count of run c before the current tile
-  bool bad = false;
+  uint32_t seen = 0;  // OR of the thread's symbols: one >= 2^levels sets a bit above the bins
   const uint32_t block = block0 + blockIdx.x;
   const uint64_t first_tile = uint64_t(block) * tiles_per_block;
   const int lane = tid & 31, warp = tid >> 5;
@@ -112,8 +116,8 @@ __global__ void __launch_bounds__(kTileHistThreads) tile_hist_kernel(const T* te
     if (level0_b) level0_b[word_index] = word;
   };
   auto count = [&](uint32_t c) {
-    if (c >= bins) { bad = true; return; }
-    atomicAdd(&mine[c], 1u);
+    seen |= c;
+    atomicAdd(&mine[(c & binmask) * 32], 1u);  // an out-of-range symbol fails the build below
   };
   constexpr int PER = 16 / sizeof(T);
   // whole aligned tiles of HV 16-byte vectors per thread, loaded one tile
@@ -137,6 +141,15 @@ __global__ void __launch_bounds__(kTileHistThreads) tile_hist_kernel(const T* te
     if (start >= n) break;
     const uint64_t len = n - start < tile_keys ? n - start : tile_keys;
     const T* p = text + start;
+    if (zero.words) {  // this tile's slab of the first pass's other levels
+      const uint64_t z0 = tile * zero.per_tile;
+      const uint64_t z1 = z0 + zero.per_tile < zero.words ? z0 + zero.per_tile : zero.words;
+      const uint4 zv = make_uint4(0u, 0u, 0u, 0u);
+      for (uint64_t w = z0 + 2 * uint64_t(tid); w < z1; w += 2 * kTileHistThreads) {
+        *reinterpret_cast<uint4*>(zero.a + w) = zv;
+        if (zero.b) *reinterpret_cast<uint4*>(zero.b + w) = zv;
+      }
+    }
     if (full_tile(tile)) {
       uint4 cur[HV];
 #pragma unroll
@@ -191,9 +204,15 @@ __global__ void __launch_bounds__(kTileHistThreads) tile_hist_kernel(const T* te
     }
     __syncthreads();
     if (tid < int(bins)) {
+      // row of 32 counters, its 16-byte pieces read in a rotated order so
+      // that the 8 threads of a quarter warp hit different banks
+      const uint4* row = reinterpret_cast<const uint4*>(h + tid * 32);
       uint32_t tot = 0;
 #pragma unroll
-      for (int w = 0; w < WARPS; ++w) tot += h[w * BINS + tid];
+      for (int k = 0; k < 8; ++k) {
+        const uint4 r = row[(k + tid) & 7];
+        tot += r.x + r.y + r.z + r.w;
+      }
       const uint32_t x = tot - prev;
       prev = tot;
       // run of symbol b: its top D bits, first bit least significant
@@ -210,7 +229,7 @@ __global__ void __launch_bounds__(kTileHistThreads) tile_hist_kernel(const T* te
     }
     __syncthreads();
   }
-  if (bad) atomicOr(status, kErrSymbol);
+  if (seen >> levels) atomicOr(status, kErrSymbol);
   if (tid < int(NB)) blocksum[uint64_t(block) * NB + tid] = rel;
   if (tid < int(bins) && prev) atomicAdd(&hist[tid], (unsigned long long)prev);
 }
@@ -430,14 +449,14 @@ uint32_t tile_hist_blocks(uint64_t n, uint32_t tile_keys) {
 void launch_tile_histogram_blocks(const void* text, uint64_t n, uint32_t width, uint32_t levels, uint32_t D,
                                   uint32_t tile_keys, uint32_t block0, uint32_t nblk, unsigned long long* hist,
                                   uint32_t* tilecnt, uint32_t* relpre, unsigned long long* blocksum,
-                                  uint64_t* level0_a, uint64_t* level0_b, uint32_t* status, cudaStream_t s,
-                                  uint64_t* launches) {
+                                  uint64_t* level0_a, uint64_t* level0_b, const HistZero& zero, uint32_t* status,
+                                  cudaStream_t s, uint64_t* launches) {
   if (n == 0 || nblk == 0) return;
   const uint32_t per = tile_hist_tiles_per_block();
 #define PWMGPU_TH(T)                                                                                          \
   tile_hist_kernel<<<nblk, kTileHistThreads, 0, s>>>(static_cast<const T*>(text), n, levels, D, tile_keys, per, \
                                                      block0, hist, tilecnt, relpre, blocksum, level0_a,        \
-                                                     level0_b, status)
+                                                     level0_b, zero, status)
   if (width == 1) PWMGPU_TH(uint8_t);
   else if (width == 2) PWMGPU_TH(uint16_t);
   else PWMGPU_TH(uint32_t);

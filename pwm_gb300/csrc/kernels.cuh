@@ -25,13 +25,22 @@ void launch_leaf_histogram(const void* text, uint64_t n, uint32_t width, uint32_
 // (the symbols' top bits in text order) to level0_a and level0_b (if set).
 // hist must be zeroed.  launch_tile_block_scan then turns blocksum into each
 // block's exclusive prefix.
+// With zero.words set, tile t also zeroes words [t * per_tile, (t + 1) *
+// per_tile) of [0, words) at zero.a (and zero.b): 16-byte aligned, even
+// counts.
+struct HistZero {
+  uint64_t* a = nullptr;
+  uint64_t* b = nullptr;
+  uint64_t words = 0;
+  uint64_t per_tile = 0;
+};
 uint32_t tile_hist_tiles_per_block();
 uint32_t tile_hist_blocks(uint64_t n, uint32_t tile_keys);
 void launch_tile_histogram_blocks(const void* text, uint64_t n, uint32_t width, uint32_t levels, uint32_t D,
                                   uint32_t tile_keys, uint32_t block0, uint32_t nblk, unsigned long long* hist,
                                   uint32_t* tilecnt, uint32_t* relpre, unsigned long long* blocksum,
-                                  uint64_t* level0_a, uint64_t* level0_b, uint32_t* status, cudaStream_t s,
-                                  uint64_t* launches);
+                                  uint64_t* level0_a, uint64_t* level0_b, const HistZero& zero, uint32_t* status,
+                                  cudaStream_t s, uint64_t* launches);
 void launch_tile_block_scan(unsigned long long* blocksum, uint32_t nblocks, uint32_t D, cudaStream_t s,
                             uint64_t* launches);
 

@@ -46,16 +46,7 @@ __global__ void __launch_bounds__(kRsThreads) rs_blocks_kernel(const RankSelectL
     // 16-byte loads when the warp's words are all in the level and aligned
     const bool full = ww + 32 * kL1Cover <= L.nwords && (reinterpret_cast<uintptr_t>(L.data) & 15) == 0;
     uint32_t l2[4] = {0, 0, 0, 0};
-#pragma unroll 4
-    for (int i = 0; i < 16; ++i) {
-      const uint64_t w = ww + 2 * uint64_t(i * 32 + lane);  // first of this lane's two words
-      uint32_t c;
-      if (full) {
-        const uint4 v = __ldcs(reinterpret_cast<const uint4*>(L.data + w));
-        c = __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
-      } else {
-        c = (w < L.nwords ? __popcll(L.data[w]) : 0) + (w + 1 < L.nwords ? __popcll(L.data[w + 1]) : 0);
-      }
+    auto gather = [&](int i, uint32_t c) {
       c += __shfl_xor_sync(0xFFFFFFFFu, c, 1);
       c += __shfl_xor_sync(0xFFFFFFFFu, c, 2);
       // lane 2i takes block 2i's four counts (lanes 0,4,8,12), lane 2i+1 block 2i+1's (16,20,24,28)
@@ -63,6 +54,22 @@ __global__ void __launch_bounds__(kRsThreads) rs_blocks_kernel(const RankSelectL
       for (int k = 0; k < 4; ++k) {
         const uint32_t x = __shfl_sync(0xFFFFFFFFu, c, (lane & 1) * 16 + 4 * k);
         if ((lane >> 1) == i) l2[k] = x;
+      }
+    };
+    if (full) {
+      // all 16 loads of the lane in flight before the first popcount
+      uint32_t c[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const uint4 v = __ldcs(reinterpret_cast<const uint4*>(L.data + ww + 2 * uint64_t(i * 32 + lane)));
+        c[i] = __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
+      }
+#pragma unroll
+      for (int i = 0; i < 16; ++i) gather(i, c[i]);
+    } else {
+      for (int i = 0; i < 16; ++i) {
+        const uint64_t w = ww + 2 * uint64_t(i * 32 + lane);  // first of this lane's two words
+        gather(i, (w < L.nwords ? __popcll(L.data[w]) : 0) + (w + 1 < L.nwords ? __popcll(L.data[w + 1]) : 0));
       }
     }
     const uint64_t blk = wb + lane;

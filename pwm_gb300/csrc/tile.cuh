@@ -89,6 +89,13 @@ struct TileArgs {
   const uint32_t* tilecnt;
   uint32_t tiles_per_block;
   uint32_t first_level_written;  // level l is already written (by the histogram kernel)
+  // Optional: words [0, zero_words) at zero_a (and zero_b) are zeroed, tile g
+  // taking words [g * zero_per_tile, (g + 1) * zero_per_tile): the levels of
+  // the next pass, whose edge words it ORs.  16-byte aligned, even counts.
+  uint64_t* zero_a;
+  uint64_t* zero_b;
+  uint64_t zero_words;
+  uint32_t zero_per_tile;
 };
 
 template <typename KeyT, int K, bool OUT, int THREADS, int V>
@@ -287,7 +294,9 @@ __device__ __forceinline__ uint64_t stream64(const uint32_t* sb, uint32_t x) {
 // k = k0, k0 + step, ... of the destination range.  Words the run covers
 // whole are stored (the lean path); so is the level's last word when the run
 // fills it up to the level's end; the (at most two) words shared with other
-// runs are OR-ed (those were zeroed).
+// runs are OR-ed, so those must be zero before the pass.  (Clearing the run's
+// own bits with an AND first would make zeroing unnecessary, but costs each
+// pass more in L2 atomics than the zeroing costs.)
 __device__ __forceinline__ void write_bits64(uint64_t* level, uint64_t nbits, uint64_t dst, const uint32_t* sb,
                                              uint32_t src, uint32_t len, uint32_t k0, uint32_t step,
                                              uint32_t* status) {
@@ -643,6 +652,17 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tile_pass_kernel(Tile
       uint64_t* level = (st ? s_tx.wt : s_tx.wm) + uint64_t(j) * s_tx.stride;
       const uint64_t dst = s_table[st ? tile_wt_entry(K, j, v) : tile_wm_entry(j, v)] + runpre[e];
       write_bits64(level, s_tx.nbits, dst, sbits + j * SBW, rst[j][v], rsz[j][v], uint32_t(lane), 32u, a.status);
+    }
+  }
+
+  // ---- this tile's slab of the next pass's levels --------------------------
+  if (a.zero_words) {
+    const uint64_t z0 = uint64_t(g) * a.zero_per_tile;
+    const uint64_t z1 = z0 + a.zero_per_tile < a.zero_words ? z0 + a.zero_per_tile : a.zero_words;
+    const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+    for (uint64_t w = z0 + 2 * uint64_t(tid); w < z1; w += 2 * THREADS) {
+      *reinterpret_cast<uint4*>(a.zero_a + w) = zero;
+      if (a.zero_b) *reinterpret_cast<uint4*>(a.zero_b + w) = zero;
     }
   }
 }

@@ -140,3 +140,40 @@ def test_misaligned_device_text(pg, orc, engines):
             for l in range(8):
                 assert np.array_equal(np.asarray(ws.bvs()[l]), ref.level(l)), (off, tree, l)
         ds.free()
+
+
+@pytest.mark.parametrize("width,L,n", [(1, 8, 1_000_003), (1, 5, 300_001), (2, 11, 700_001), (2, 16, 400_009),
+                                       (4, 13, 250_007), (4, 20, 200_003)])
+def test_rebuild_overwrites_every_bit(pg, orc, engines, width, L, n):
+    """Levels are not zeroed between builds: a structure first built from a
+    text whose every bit is 1 and then rebuilt in place from a random text
+    must equal the oracle's structures for the second text, with every
+    padding bit and word still zero."""
+    torch = torch_cuda()
+    tile, _ = engines
+    rng = np.random.default_rng(L)
+    ones = np.full(n, (1 << L) - 1, dtype=DT[width])
+    text = rng.integers(0, 1 << L, n).astype(DT[width])
+    ds = pg.DeviceStructure(n, width, L, matrix=True, tree=True, context=tile)
+    for t in (ones, text):
+        d = torch.from_numpy(t.view(np.uint8).copy()).cuda()
+        ds.build(d.data_ptr())
+        ds.check()
+    for which, tree in ((0, False), (1, True)):
+        v = ds.view(which)
+        words = np.zeros(v.total_words, dtype=np.uint64)
+        zeros = np.zeros(L, dtype=np.uint64)
+        tile.check(tile.lib.pwmgpu_wx_download(tile.h, ds.h, which, words.ctypes.data_as(pg._lib.u64p),
+                                                zeros.ctypes.data_as(pg._lib.u64p)))
+        ref = orc.build(text, L, tree, "ps")
+        real = (n + 63) // 64
+        for l in range(L):
+            off = int(v.level_offset[l])
+            end = int(v.level_offset[l + 1]) if l + 1 < L else int(v.total_words)
+            assert np.array_equal(words[off:off + real], ref.level(l)), (tree, l)
+            assert not words[off + real:end].any(), (tree, l, "padding words")
+            if n % 64:
+                assert int(words[off + real - 1]) & ((1 << (64 - n % 64)) - 1) == 0, (tree, l, "padding bits")
+        if not tree:
+            assert [int(z) for z in zeros] == [int(z) for z in ref.zeros]
+    ds.free()
