@@ -89,9 +89,11 @@ PWMGPU_API uint64_t pwmgpu_ctx_launch_count(const pwmgpu_ctx* ctx);
  * algorithmic_bytes", then clears the record. */
 PWMGPU_API pwmgpu_status pwmgpu_ctx_profile(pwmgpu_ctx* ctx, int enable);
 PWMGPU_API pwmgpu_status pwmgpu_ctx_profile_read(pwmgpu_ctx* ctx, char* buf, uint64_t cap);
-/* Tuning: levels fused into one split pass (1..4).  A pass reads its input
- * sequence once and writes the bits of that many levels.  Sets the width of
- * both engines (defaults: 4 for the tile engine, 2 for the warp-pass engine). */
+/* Tuning: levels fused into one split pass (1..4; 0 restores the default).
+ * A pass reads its input sequence once and writes the bits of that many
+ * levels.  Sets the width of both engines.  Defaults: the tile engine builds
+ * a text of up to 7 levels in one pass of all its levels and deeper texts in
+ * passes of 4; the warp-pass engine uses passes of 2. */
 PWMGPU_API pwmgpu_status pwmgpu_ctx_set_pass_levels(pwmgpu_ctx* ctx, int levels_per_pass);
 
 /* Stream-ordered device allocations (cudaMallocAsync / cudaFreeAsync on the

@@ -27,6 +27,7 @@ constexpr uint32_t kMaxLevels = 64;
 constexpr uint32_t kMaxPlainLevels = 24;  // the leaf histogram has 2^L bins
 constexpr int kDefaultPassLevels = 2;  // fastest measured width of the warp-pass engine for 8-bit text
 constexpr int kDefaultTileLevels = 4;  // levels per segmented tile pass
+constexpr uint32_t kSinglePassMaxLevels = 7;  // one tile pass for texts of at most this many levels
 
 struct Fail {
   pwmgpu_status st;
@@ -67,7 +68,7 @@ struct pwmgpu_ctx {
   uint32_t* d_status = nullptr;
   std::map<std::string, DevBuf> scratch;
   int pass_levels = kDefaultPassLevels;
-  int tile_levels = kDefaultTileLevels;
+  int tile_levels = 0;  // 0: automatic
   int engine = PWMGPU_ENGINE_TILE;
   uint64_t upload_piece = uint64_t(64) << 20;  // bytes of text per uploaded piece
   bool async_alloc = false;  // stream-ordered allocations on `stream`
@@ -132,6 +133,12 @@ struct pwmgpu_ctx {
   // events that order them against the main stream; every call that uses
   // them waits for them before it returns, so the events are reused.
   cudaStream_t up = nullptr, down = nullptr;
+  // recorded after the histogram of a build reaches the host
+  cudaEvent_t hist_ready = nullptr;
+  cudaEvent_t hist_event() {
+    if (!hist_ready) CUDA_TRY(cudaEventCreateWithFlags(&hist_ready, cudaEventDisableTiming));
+    return hist_ready;
+  }
   std::vector<cudaEvent_t> xev;
   size_t xev_used = 0;
   void xfer_init() {
@@ -238,6 +245,7 @@ pwmgpu_ctx::~pwmgpu_ctx() {
       cudaStreamDestroy(t);
     }
   for (auto e : xev) cudaEventDestroy(e);
+  if (hist_ready) cudaEventDestroy(hist_ready);
   if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
@@ -391,12 +399,13 @@ uint32_t read_status(pwmgpu_ctx* ctx) {
   return st;
 }
 
-void check_device_status(pwmgpu_ctx* ctx) {
-  const uint32_t st = read_status(ctx);
+void throw_status(uint32_t st) {
   if (st & kErrSymbol) throw Fail{PWMGPU_ERR_SYMBOL, "a text symbol is >= 2^levels (or has no Huffman code)"};
   if (st & kErrTimeout) throw Fail{PWMGPU_ERR_TIMEOUT, "a device-side look-back wait gave up"};
   if (st & kErrBounds) throw Fail{PWMGPU_ERR_CUDA, "a device-side bounds check tripped"};
 }
+
+void check_device_status(pwmgpu_ctx* ctx) { throw_status(read_status(ctx)); }
 
 // ---------------------------------------------------------------------------
 // The matrix passes and the tree regroup, shared by plain and Huffman builds
@@ -506,97 +515,119 @@ struct TileFirstPass {
   bool level0_written = false;  // the histogram kernel wrote level 0 of both structures
 };
 
-// after_pass(i) runs on the host once pass i is enqueued, and
-// after_pass(passes.size()) once the regroup is.
-void run_tile_passes(pwmgpu_ctx* ctx, const void* d_text, uint32_t width, uint32_t L,
-                     const std::vector<TilePassHost>& passes, const std::vector<uint32_t>& regroup,
-                     const LevelTables& tabs, Structure& wm, Structure* wt, const TileFirstPass* first = nullptr,
-                     const std::function<void(size_t)>& after_pass = {}) {
-  // Edge words are OR-ed, so every level is zeroed before its pass: the first
-  // pass's by the caller (below, or by the histogram kernel), the others by
-  // the pass before, a slab per tile.
-  cudaStream_t s = ctx->stream;
-  const uint64_t n = tabs.level_bits.empty() ? 0 : tabs.level_bits[0];
+// Device descriptors of passes [from, to): per pass its segments, its level
+// descriptor and its start tables, at offsets of one uploaded blob.
+struct TileBlob {
+  std::vector<unsigned char> bytes;
+  std::vector<size_t> segs, text, table;  // indexed by pass
+};
 
-  // one upload: per pass its segments, its level descriptor and its tables
-  std::vector<unsigned char> blob;
-  auto align16 = [&]() { blob.resize((blob.size() + 15) & ~size_t(15)); };
-  struct Offs { size_t segs, text, table; };
-  std::vector<Offs> offs(passes.size());
+TileBlob tile_blob(const std::vector<TilePassHost>& passes, size_t from, size_t to, uint32_t L, uint64_t n,
+                   const Structure& wm, const Structure* wt) {
+  TileBlob b;
+  b.segs.assign(passes.size(), 0);
+  b.text.assign(passes.size(), 0);
+  b.table.assign(passes.size(), 0);
+  auto align16 = [&]() { b.bytes.resize((b.bytes.size() + 15) & ~size_t(15)); };
+  auto put = [&](const void* p, size_t bytes) {
+    const auto* c = static_cast<const unsigned char*>(p);
+    b.bytes.insert(b.bytes.end(), c, c + bytes);
+  };
   const uint64_t stride = L > 1 ? wm.offs[1] - wm.offs[0] : padded_words(n);
-  for (size_t pi = 0; pi < passes.size(); ++pi) {
+  for (size_t pi = from; pi < to; ++pi) {
     const auto& p = passes[pi];
     align16();
-    offs[pi].segs = blob.size();
+    b.segs[pi] = b.bytes.size();
     for (const auto& h : p.segs) {
       TileSeg d{h.in_begin, h.m, h.table, h.tile0, h.text};
-      const auto* b = reinterpret_cast<const unsigned char*>(&d);
-      blob.insert(blob.end(), b, b + sizeof d);
+      put(&d, sizeof d);
     }
     align16();
-    offs[pi].text = blob.size();
+    b.text[pi] = b.bytes.size();
     TileText tx{};
     tx.wm = wm.d_words + wm.offs[p.level];
     tx.wt = (wt && p.segmented) ? wt->d_words + wt->offs[p.level] : nullptr;
     tx.stride = stride;
     tx.nbits = n;
     tx.shift = L - 1 - p.level;
-    const auto* b = reinterpret_cast<const unsigned char*>(&tx);
-    blob.insert(blob.end(), b, b + sizeof tx);
+    put(&tx, sizeof tx);
     align16();
-    offs[pi].table = blob.size();
-    const auto* tb = reinterpret_cast<const unsigned char*>(p.table.data());
-    blob.insert(blob.end(), tb, tb + p.table.size() * 8);
+    b.table[pi] = b.bytes.size();
+    put(p.table.data(), p.table.size() * 8);
   }
-  auto* d_blob = static_cast<unsigned char*>(ctx->grow("tile_plan", std::max<size_t>(blob.size(), 16)));
-  CUDA_TRY(cudaMemcpyAsync(d_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice, s));
+  if (b.bytes.empty()) b.bytes.resize(16);
+  return b;
+}
 
+// Enqueues pass pi (descriptors at d_blob) reading `in`; returns the keys it
+// writes for the next pass.  Edge words are OR-ed, so a pass's levels must be
+// zero: the first pass's are zeroed by the caller (or by the histogram
+// kernel), every other pass's by the pass before it, a slab per tile.  Only
+// level and width of passes[pi + 1] are read.
+const void* enqueue_tile_pass(pwmgpu_ctx* ctx, const std::vector<TilePassHost>& passes, size_t pi,
+                              const unsigned char* d_blob, const TileBlob& blob, const void* in, uint32_t width,
+                              uint64_t n, Structure& wm, Structure* wt, const TileFirstPass* first) {
+  cudaStream_t s = ctx->stream;
+  const auto& p = passes[pi];
   void* ping = ctx->grow("keys_a", std::max<uint64_t>(n, 1) * width);
   void* pong = ctx->grow("keys_b", std::max<uint64_t>(n, 1) * width);
-  const void* in = d_text;
-  for (size_t pi = 0; pi < passes.size(); ++pi) {
-    const auto& p = passes[pi];
-    const int D = p.out ? p.K : p.K - 1;
-    const uint64_t nlb = uint64_t(1) << D;
-    const uint64_t lb_bytes = uint64_t(std::max<uint32_t>(p.tiles, 1)) * nlb * 8;
-    auto* lb = static_cast<unsigned long long*>(ctx->grow("lookback", lb_bytes + 64));
-    CUDA_TRY(cudaMemsetAsync(lb, 0, lb_bytes + 64, s));
-    TileArgs a{};
-    a.in = in;
-    a.out = p.out ? (in == ping ? pong : ping) : nullptr;
-    a.out_size = p.out ? n : 0;
-    a.segs = reinterpret_cast<const TileSeg*>(d_blob + offs[pi].segs);
-    a.texts = reinterpret_cast<const TileText*>(d_blob + offs[pi].text);
-    a.tables = reinterpret_cast<const uint64_t*>(d_blob + offs[pi].table);
-    a.lookback = lb;
-    a.tile_counter = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(lb) + lb_bytes);
-    a.status = ctx->d_status;
-    a.nsegs = uint32_t(p.segs.size());
-    a.tiles = p.tiles;
-    if (pi + 1 < passes.size()) {
-      const auto& q = passes[pi + 1];
-      const uint32_t l1 = q.level + q.K - 1;
-      a.zero_a = wm.d_words + wm.offs[q.level];
-      a.zero_b = wt ? wt->d_words + wt->offs[q.level] : nullptr;
-      a.zero_words = (l1 + 1 < wm.levels ? wm.offs[l1 + 1] : wm.total_words) - wm.offs[q.level];
-      const uint64_t per = (a.zero_words + p.tiles - 1) / std::max<uint32_t>(p.tiles, 1);
-      a.zero_per_tile = uint32_t((per + 1) & ~uint64_t(1));
-    }
-    if (pi == 0 && first && p.segs.size() == 1) {
-      a.blockpre = first->blockpre;
-      a.relpre = first->relpre;
-      a.tilecnt = first->tilecnt;
-      a.tiles_per_block = first->tiles_per_block;
-      a.first_level_written = first->level0_written ? 1u : 0u;
-    }
-    {
-      const uint64_t structs = (wt && p.segmented) ? 2 : 1;
-      const uint64_t skipped = a.first_level_written ? structs * words_for(n) * 8 : 0;
-      ProfScope ps(ctx, "split_pass", structs * uint64_t(p.K) * (n * width + words_for(n) * 8) - skipped);
-      launch_tile_pass(width, p.K, p.out, a, s, &ctx->launches);
-    }
-    CUDA_TRY(cudaGetLastError());
-    if (p.out) in = a.out;
+  const int D = p.out ? p.K : p.K - 1;
+  const uint64_t nlb = uint64_t(1) << D;
+  const uint64_t lb_bytes = uint64_t(std::max<uint32_t>(p.tiles, 1)) * nlb * 8;
+  auto* lb = static_cast<unsigned long long*>(ctx->grow("lookback", lb_bytes + 64));
+  CUDA_TRY(cudaMemsetAsync(lb, 0, lb_bytes + 64, s));
+  TileArgs a{};
+  a.in = in;
+  a.out = p.out ? (in == ping ? pong : ping) : nullptr;
+  a.out_size = p.out ? n : 0;
+  a.segs = reinterpret_cast<const TileSeg*>(d_blob + blob.segs[pi]);
+  a.texts = reinterpret_cast<const TileText*>(d_blob + blob.text[pi]);
+  a.tables = reinterpret_cast<const uint64_t*>(d_blob + blob.table[pi]);
+  a.lookback = lb;
+  a.tile_counter = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(lb) + lb_bytes);
+  a.status = ctx->d_status;
+  a.nsegs = uint32_t(p.segs.size());
+  a.tiles = p.tiles;
+  if (pi + 1 < passes.size()) {
+    const auto& q = passes[pi + 1];
+    const uint32_t l1 = q.level + q.K - 1;
+    a.zero_a = wm.d_words + wm.offs[q.level];
+    a.zero_b = wt ? wt->d_words + wt->offs[q.level] : nullptr;
+    a.zero_words = (l1 + 1 < wm.levels ? wm.offs[l1 + 1] : wm.total_words) - wm.offs[q.level];
+    const uint64_t per = (a.zero_words + p.tiles - 1) / std::max<uint32_t>(p.tiles, 1);
+    a.zero_per_tile = uint32_t((per + 1) & ~uint64_t(1));
+  }
+  if (pi == 0 && first && p.segs.size() == 1) {
+    a.blockpre = first->blockpre;
+    a.relpre = first->relpre;
+    a.tilecnt = first->tilecnt;
+    a.tiles_per_block = first->tiles_per_block;
+    a.first_level_written = first->level0_written ? 1u : 0u;
+  }
+  {
+    const uint64_t structs = (wt && p.segmented) ? 2 : 1;
+    const uint64_t skipped = a.first_level_written ? structs * words_for(n) * 8 : 0;
+    ProfScope ps(ctx, "split_pass", structs * uint64_t(p.K) * (n * width + words_for(n) * 8) - skipped);
+    launch_tile_pass(width, p.K, p.out, a, s, &ctx->launches);
+  }
+  CUDA_TRY(cudaGetLastError());
+  return p.out ? a.out : in;
+}
+
+// Passes [from, passes.size()) and the regroup; `in` is the input of pass
+// `from` (the text for pass 0).  after_pass(i) runs on the host once pass i
+// is enqueued, and after_pass(passes.size()) once the regroup is.
+void run_tile_passes(pwmgpu_ctx* ctx, const void* in, uint32_t width, uint32_t L,
+                     const std::vector<TilePassHost>& passes, const std::vector<uint32_t>& regroup,
+                     const LevelTables& tabs, Structure& wm, Structure* wt, const TileFirstPass* first = nullptr,
+                     const std::function<void(size_t)>& after_pass = {}, size_t from = 0) {
+  cudaStream_t s = ctx->stream;
+  const uint64_t n = tabs.level_bits.empty() ? 0 : tabs.level_bits[0];
+  const TileBlob blob = tile_blob(passes, from, passes.size(), L, n, wm, wt);
+  auto* d_blob = static_cast<unsigned char*>(ctx->grow("tile_plan", blob.bytes.size()));
+  CUDA_TRY(cudaMemcpyAsync(d_blob, blob.bytes.data(), blob.bytes.size(), cudaMemcpyHostToDevice, s));
+  for (size_t pi = from; pi < passes.size(); ++pi) {
+    in = enqueue_tile_pass(ctx, passes, pi, d_blob, blob, in, width, n, wm, wt, first);
     if (after_pass) after_pass(pi);
   }
 
@@ -690,7 +721,18 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   // first pass's other levels are zeroed by the histogram kernel (levels <= 8)
   // or here; the padding is zero from allocation.
   const bool tile_engine = ctx->engine == PWMGPU_ENGINE_TILE && L <= kTilePlanMaxLevels;
-  const int Kz = std::min<int>(std::min(ctx->tile_levels, kTileMaxLevels), int(L));
+  // Pass width: by default a text of up to kSinglePassMaxLevels levels takes
+  // one pass of all its levels (the histogram kernel gives that pass its
+  // prefixes), deeper texts passes of kDefaultTileLevels; set_pass_levels(k)
+  // asks for k (<= 4).  At 8 levels one pass would write 127 runs per tile
+  // into each of the deepest levels of both structures, and the two 4-level
+  // passes are faster (measured: 5.9 against 6.2 ms for 2^30 bytes, while
+  // one pass wins at 5..7 levels).
+  const bool auto_k = ctx->tile_levels == 0;
+  const int kmax = (auto_k && L > uint32_t(kTileMaxLevels) && L <= kSinglePassMaxLevels)
+                       ? int(L)
+                       : std::min(auto_k ? kDefaultTileLevels : ctx->tile_levels, kTileMaxLevels);
+  const int Kz = std::min<int>(kmax, int(L));
   const uint32_t D0 = uint32_t(Kz < int(L) ? Kz : Kz - 1);  // splits of the first pass
   const bool tile_hist = tile_engine && L <= 8 && D0 >= 1;
   if (tile_engine && !tile_hist && Kz > 1)
@@ -725,9 +767,10 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     first.level0_written = true;
     uint64_t* l0[2] = {wx->wm.present ? wx->wm.d_words : nullptr, wx->wt.present ? wx->wt.d_words : nullptr};
     if (!l0[0]) std::swap(l0[0], l0[1]);
-    // levels 1..Kz-1 of both structures, a slab per tile
+    // levels 1..Kz-1 of both structures, a slab per tile (a pass of more
+    // than 4 levels clears its shared words itself)
     HistZero hz;
-    if (Kz > 1) {
+    if (Kz > 1 && Kz <= kTileMaxLevels) {
       hz.a = l0[0] + wx->wm.offs[1];
       hz.b = l0[1] ? l0[1] + wx->wm.offs[1] : nullptr;
       hz.words = (uint32_t(Kz) < L ? wx->wm.offs[Kz] : wx->wm.total_words) - wx->wm.offs[1];
@@ -768,18 +811,54 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     launch_leaf_histogram(d_text, n, wx->width, L, d_hist, ctx->d_status, s, &ctx->launches);
   }
   CUDA_TRY(cudaGetLastError());
-  auto* h_hist = static_cast<uint64_t*>(ctx->grow_pinned(bins * 8));
+  // the histogram and the status word go to pinned host memory
+  auto* h_hist = static_cast<uint64_t*>(ctx->grow_pinned(bins * 8 + 8));
+  auto* h_status = reinterpret_cast<uint32_t*>(h_hist + bins);
   CUDA_TRY(cudaMemcpyAsync(h_hist, d_hist, bins * 8, cudaMemcpyDeviceToHost, s));
-  check_device_status(ctx);  // synchronises
+  CUDA_TRY(cudaMemcpyAsync(h_status, ctx->d_status, 4, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaEventRecord(ctx->hist_event(), s));
   const bool want_tree = wx->wt.present;
+  // After the tile histogram the first pass needs nothing from the host but
+  // its start table, which a one-CTA kernel derives from the histogram: the
+  // pass runs while the host reads the histogram and plans the other passes
+  // (the host's plan gives the same first pass).
+  const void* next_in = d_text;
+  size_t from = 0;
+  if (tile_hist) {
+    const auto shape = plan_passes(L, Kz);
+    std::vector<TilePassHost> early(std::min<size_t>(shape.size(), 2));
+    for (size_t i = 0; i < early.size(); ++i) {
+      early[i].level = shape[i].level;
+      early[i].K = shape[i].K;
+      early[i].out = shape[i].has_out;
+    }
+    TilePassHost& p0 = early[0];
+    const uint32_t T = tile_pass_elems(wx->width);
+    p0.segmented = want_tree;
+    p0.tiles = uint32_t((n + T - 1) / T);
+    p0.segs.push_back({0, n, 0, 0, 0});
+    p0.table.assign(size_t(tile_table_size(p0.K)), 0);
+    const TileBlob b0 = tile_blob(early, 0, 1, L, n, wx->wm, want_tree ? &wx->wt : nullptr);
+    auto* d_b0 = static_cast<unsigned char*>(ctx->grow("tile_plan0", b0.bytes.size()));
+    CUDA_TRY(cudaMemcpyAsync(d_b0, b0.bytes.data(), b0.bytes.size(), cudaMemcpyHostToDevice, s));
+    launch_first_pass_table(d_hist, L, uint32_t(p0.K), p0.out, want_tree,
+                            reinterpret_cast<uint64_t*>(d_b0 + b0.table[0]), s, &ctx->launches);
+    next_in = enqueue_tile_pass(ctx, early, 0, d_b0, b0, d_text, wx->width, n, wx->wm,
+                                want_tree ? &wx->wt : nullptr, &first);
+    from = 1;
+  }
+  CUDA_TRY(cudaEventSynchronize(ctx->hist_event()));
+  if (*h_status) {
+    CUDA_TRY(cudaStreamSynchronize(s));  // the first pass may still read the text
+    throw_status(*h_status);
+  }
   LevelTables tabs;
   std::vector<PassPlan> plan;
   std::vector<TilePassHost> tile_passes;
   std::vector<uint32_t> regroup;
   if (tile_engine) {
     const auto cnt = fold_prefix_counts(h_hist, L);
-    tile_passes = plan_tile_passes(cnt, L, std::min(ctx->tile_levels, kTileMaxLevels), tile_pass_elems(wx->width),
-                                   want_tree, &regroup);
+    tile_passes = plan_tile_passes(cnt, L, kmax, tile_pass_elems(wx->width), want_tree, &regroup);
     tabs = build_tables_tile(cnt, L, want_tree ? regroup : std::vector<uint32_t>{});
   } else {
     plan = plan_passes(L, ctx->pass_levels);
@@ -814,9 +893,10 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     }
   };
   if (tile_engine) {
-    run_tile_passes(ctx, d_text, wx->width, L, tile_passes, regroup, tabs, wx->wm, want_tree ? &wx->wt : nullptr,
+    if (from == 1 && stream_out) after_pass(0);
+    run_tile_passes(ctx, next_in, wx->width, L, tile_passes, regroup, tabs, wx->wm, want_tree ? &wx->wt : nullptr,
                     first.blockpre ? &first : nullptr,
-                    stream_out ? std::function<void(size_t)>(after_pass) : std::function<void(size_t)>());
+                    stream_out ? std::function<void(size_t)>(after_pass) : std::function<void(size_t)>(), from);
   }
   else
     run_passes(ctx, d_text, wx->width, wx->width, false, L, plan, tabs, wx->wm, want_tree ? &wx->wt : nullptr);
@@ -1327,8 +1407,8 @@ pwmgpu_status pwmgpu_ctx_sync(pwmgpu_ctx* ctx) {
 uint64_t pwmgpu_ctx_launch_count(const pwmgpu_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
 pwmgpu_status pwmgpu_ctx_set_pass_levels(pwmgpu_ctx* ctx, int k) {
-  if (!ctx || k < 1 || k > kMaxPassLevels || k > kTileMaxLevels) return PWMGPU_ERR_ARG;
-  ctx->pass_levels = k;
+  if (!ctx || k < 0 || k > kMaxPassLevels || k > kTileMaxLevels) return PWMGPU_ERR_ARG;
+  ctx->pass_levels = k ? k : kDefaultPassLevels;
   ctx->tile_levels = k;
   return PWMGPU_OK;
 }

@@ -95,10 +95,10 @@ __global__ void __launch_bounds__(kTileHistThreads) tile_hist_kernel(const T* te
   // a bank, however skewed the text (at most 8 warps x 64 symbols x 16
   // tiles = 8192 per counter).
   __shared__ __align__(16) uint32_t h[BINS * 32];
-  __shared__ uint32_t s_tc[16];
+  __shared__ uint32_t s_tc[BINS / 2];  // runs of the first D <= 7 bits
   const int tid = threadIdx.x;
   for (int i = tid; i < BINS * 32; i += kTileHistThreads) h[i] = 0;
-  if (tid < 16) s_tc[tid] = 0;
+  if (tid < BINS / 2) s_tc[tid] = 0;
   __syncthreads();
   uint32_t* mine = h + (tid & 31);
   const uint32_t bins = 1u << levels, NB = 1u << D, binmask = bins - 1;
@@ -234,35 +234,89 @@ __global__ void __launch_bounds__(kTileHistThreads) tile_hist_kernel(const T* te
   if (tid < int(bins) && prev) atomicAdd(&hist[tid], (unsigned long long)prev);
 }
 
-// Exclusive prefix, per column, of the nblocks x NB block totals (in place);
-// one CTA.  Thread (j, c) = (tid / NB, tid % NB) owns a contiguous chunk of
-// blocks of column c.
-__global__ void __launch_bounds__(1024) tile_block_scan_kernel(unsigned long long* blocksum, uint32_t nblocks,
-                                                               uint32_t NB) {
-  __shared__ unsigned long long part[1024];
-  const uint32_t tid = threadIdx.x, c = tid % NB, j = tid / NB, P = 1024 / NB;
-  const uint32_t chunk = (nblocks + P - 1) / P;
-  const uint32_t b0 = j * chunk, b1 = min(nblocks, b0 + chunk);
+// Exclusive prefix, per column, of the nblocks x NB block totals (in place):
+// CTA c scans column c, each thread a run of consecutive blocks.
+__global__ void __launch_bounds__(256) tile_block_scan_kernel(unsigned long long* blocksum, uint32_t nblocks,
+                                                              uint32_t NB) {
+  const uint32_t c = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t per = (nblocks + 255) / 256;
+  const uint32_t b0 = min(nblocks, tid * per), b1 = min(nblocks, b0 + per);
   unsigned long long sum = 0;
-  if (j < P)
-    for (uint32_t b = b0; b < b1; ++b) sum += blocksum[uint64_t(b) * NB + c];
-  part[tid] = sum;
+  for (uint32_t b = b0; b < b1; ++b) sum += blocksum[uint64_t(b) * NB + c];
+  unsigned long long x = sum;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+    if (lane >= uint32_t(d)) x += y;
+  }
+  __shared__ unsigned long long wsum[8];
+  if (lane == 31) wsum[warp] = x;
   __syncthreads();
-  if (j == 0) {
-    unsigned long long run = 0;
-    for (uint32_t q = 0; q < P; ++q) {
-      const unsigned long long v = part[q * NB + c];
-      part[q * NB + c] = run;
-      run += v;
-    }
+  unsigned long long run = x - sum;
+  for (uint32_t w = 0; w < warp; ++w) run += wsum[w];
+  for (uint32_t b = b0; b < b1; ++b) {
+    const unsigned long long v = blocksum[uint64_t(b) * NB + c];
+    blocksum[uint64_t(b) * NB + c] = run;
+    run += v;
+  }
+}
+
+// Start table of the first tile pass of a text with levels <= 8 (one
+// segment, the whole text) from its leaf histogram: the entries the host's
+// plan gives that pass (matrix runs of key_j in key order, tree runs in
+// natural prefix order, runs of S_K; tree entries 0 without a tree).  One
+// CTA of 256 threads: thread b adds bin b to its key_j runs, then warp w
+// scans the runs of levels w and w + 8.
+__global__ void __launch_bounds__(256) first_pass_table_kernel(const unsigned long long* hist, uint32_t levels,
+                                                               uint32_t K, uint32_t out, uint32_t tree,
+                                                               uint64_t* table) {
+  constexpr int KM = kTileGivenMaxLevels;
+  __shared__ unsigned long long ck[KM + 1][1 << KM];  // counts of key_j == v
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (uint32_t i = tid; i < (KM + 1) << KM; i += blockDim.x) (&ck[0][0])[i] = 0;
+  __syncthreads();
+  if (tid < (1u << levels)) {
+    const unsigned long long c = hist[tid];
+    if (c)
+      for (uint32_t j = 0; j <= K; ++j) atomicAdd(&ck[j][reverse_low_bits(tid >> (levels - j), j)], c);
   }
   __syncthreads();
-  if (j < P) {
-    unsigned long long run = part[tid];
-    for (uint32_t b = b0; b < b1; ++b) {
-      const unsigned long long v = blocksum[uint64_t(b) * NB + c];
-      blocksum[uint64_t(b) * NB + c] = run;
-      run += v;
+  // exclusive scan over i < 2^j of ck[j][key(i)], written to entry(i); lane
+  // l takes i = 8l .. 8l+7
+  auto scan = [&](uint32_t j, auto key, auto entry) {
+    const uint32_t R = 1u << j;
+    unsigned long long v[8], sum = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const uint32_t i = 8 * lane + q;
+      v[q] = i < R ? ck[j][key(i)] : 0ull;
+      sum += v[q];
+    }
+    unsigned long long x = sum;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+      if (lane >= uint32_t(d)) x += y;
+    }
+    unsigned long long run = x - sum;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const uint32_t i = 8 * lane + q;
+      if (i < R) entry(i, run);
+      run += v[q];
+    }
+  };
+  for (uint32_t j = warp; j <= K; j += 8) {
+    if (j < K) {
+      scan(j, [](uint32_t v) { return v; },
+           [&](uint32_t v, unsigned long long p) { table[tile_wm_entry(int(j), int(v))] = p; });
+      scan(j, [&](uint32_t p) { return reverse_low_bits(p, j); },  // natural prefix order
+           [&](uint32_t p, unsigned long long q) {
+             table[tile_wt_entry(int(K), int(j), int(reverse_low_bits(p, j)))] = tree ? q : 0ull;
+           });
+    } else if (out) {
+      scan(j, [](uint32_t v) { return v; },
+           [&](uint32_t v, unsigned long long p) { table[tile_out_entry(int(K), int(v))] = p; });
     }
   }
 }
@@ -464,10 +518,16 @@ void launch_tile_histogram_blocks(const void* text, uint64_t n, uint32_t width, 
   ++*launches;
 }
 
+void launch_first_pass_table(const unsigned long long* hist, uint32_t levels, uint32_t K, bool out, bool tree,
+                             uint64_t* table, cudaStream_t s, uint64_t* launches) {
+  first_pass_table_kernel<<<1, 256, 0, s>>>(hist, levels, K, out ? 1u : 0u, tree ? 1u : 0u, table);
+  ++*launches;
+}
+
 void launch_tile_block_scan(unsigned long long* blocksum, uint32_t nblocks, uint32_t D, cudaStream_t s,
                             uint64_t* launches) {
   if (nblocks == 0) return;
-  tile_block_scan_kernel<<<1, 1024, 0, s>>>(blocksum, nblocks, 1u << D);
+  tile_block_scan_kernel<<<1u << D, 256, 0, s>>>(blocksum, nblocks, 1u << D);
   ++*launches;
 }
 

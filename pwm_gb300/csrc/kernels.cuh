@@ -43,6 +43,10 @@ void launch_tile_histogram_blocks(const void* text, uint64_t n, uint32_t width, 
                                   cudaStream_t s, uint64_t* launches);
 void launch_tile_block_scan(unsigned long long* blocksum, uint32_t nblocks, uint32_t D, cudaStream_t s,
                             uint64_t* launches);
+// Start table (tile_table_size(K) entries) of the first tile pass of a text
+// with levels <= 8 from its leaf histogram, on the device.
+void launch_first_pass_table(const unsigned long long* hist, uint32_t levels, uint32_t K, bool out, bool tree,
+                             uint64_t* table, cudaStream_t s, uint64_t* launches);
 
 // ---- split passes -----------------------------------------------------------
 // Geometry of the split pass for a key width: tile size in elements.

@@ -1,33 +1,18 @@
 // Launchers of the segmented tile pass (tile.cuh) for 1-, 2- and 4-byte keys.
 #include "kernels.cuh"
-#include "tile.cuh"
+#include "tile_launch.cuh"
 
 namespace pwmgpu {
 
 namespace {
 
-constexpr int kTileThreads = 256;
-constexpr int kTileVectors = 4;  // 16-byte vectors per thread: 64 bytes of keys
-
-template <typename KeyT, int K, bool OUT>
-void launch_one(const TileArgs& a, cudaStream_t s) {
-  using C = TileCfg<KeyT, K, OUT, kTileThreads, kTileVectors>;
-  auto kern = tile_pass_kernel<KeyT, K, OUT, kTileThreads, kTileVectors>;
-  static bool configured = false;  // attribute set once per instantiation
-  if (!configured) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(C::smem_bytes()));
-    configured = true;
-  }
-  kern<<<a.tiles, kTileThreads, C::smem_bytes(), s>>>(a);
-}
-
 template <typename KeyT, bool OUT>
 void launch_k(int K, const TileArgs& a, cudaStream_t s) {
   switch (K) {
-    case 1: launch_one<KeyT, 1, OUT>(a, s); break;
-    case 2: launch_one<KeyT, 2, OUT>(a, s); break;
-    case 3: launch_one<KeyT, 3, OUT>(a, s); break;
-    default: launch_one<KeyT, 4, OUT>(a, s); break;
+    case 1: launch_tile_one<KeyT, 1, OUT>(a, s); break;
+    case 2: launch_tile_one<KeyT, 2, OUT>(a, s); break;
+    case 3: launch_tile_one<KeyT, 3, OUT>(a, s); break;
+    default: launch_tile_one<KeyT, 4, OUT>(a, s); break;
   }
 }
 
@@ -45,7 +30,11 @@ uint32_t tile_pass_elems(uint32_t key_bytes) {
 
 void launch_tile_pass(uint32_t key_bytes, int K, bool out, const TileArgs& a, cudaStream_t s, uint64_t* launches) {
   if (a.tiles == 0) return;
-  if (key_bytes == 1) launch_key<uint8_t>(K, out, a, s);
+  if (K > kTileMaxLevels) {
+    // only as the last pass of a text whose prefixes the histogram gives
+    if (out || !a.blockpre || K > kTileGivenMaxLevels) return;
+    launch_tile_pass_deep(key_bytes, K, a, s);
+  } else if (key_bytes == 1) launch_key<uint8_t>(K, out, a, s);
   else if (key_bytes == 2) launch_key<uint16_t>(K, out, a, s);
   else launch_key<uint32_t>(K, out, a, s);
   ++*launches;

@@ -43,6 +43,10 @@
 namespace pwmgpu {
 
 constexpr int kTileMaxLevels = 4;
+// A last pass whose finest-run prefixes are given (the histogram kernel's, for
+// texts of at most 8 levels) neither counts nor looks back, and may split up
+// to 7 times: all levels of such a text in one pass.
+constexpr int kTileGivenMaxLevels = 8;
 
 // Table entries of one segment: matrix starts (level j, run v) at
 // (1 << j) - 1 + v, tree starts after them, then the S_out starts (2^K).
@@ -111,7 +115,8 @@ struct TileCfg {
   static constexpr int NLB = 1 << D;                     // look-back counters per tile
   static constexpr int LPC = 32 / KPL;                   // lanes per 32-bit stream word
   static_assert(T <= 32768, "zero counts are packed in 16 bits");
-  static_assert(K >= 1 && K <= kTileMaxLevels, "1..4 levels per pass");
+  static_assert(K >= 1 && K <= kTileGivenMaxLevels && (K <= kTileMaxLevels || !OUT),
+                "1..4 levels per pass; up to 8 in a last pass with given prefixes");
   static_assert(V % 2 == 0, "vectors are scanned in pairs");
   static constexpr size_t smem_bytes() {
     return size_t(2) * T * sizeof(KeyT) + size_t(K) * SBW * 4 + (D >= 2 ? size_t(NVEC) * 4 : 0);
@@ -383,8 +388,33 @@ __device__ __forceinline__ void load_tile_bytes(uint4* dst, const unsigned char*
   }
 }
 
+// Exclusive prefix of in[0..count) into out (count <= 128) by one warp, lane
+// i taking entries 4i..4i+3.
+__device__ __forceinline__ void warp_exclusive_scan(const uint32_t* in, uint32_t* out, int count, int lane) {
+  uint32_t v[4], sum = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int i = 4 * lane + q;
+    v[q] = i < count ? in[i] : 0u;
+    sum += v[q];
+  }
+  uint32_t x = sum;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+    if (lane >= d) x += y;
+  }
+  uint32_t run = x - sum;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int i = 4 * lane + q;
+    if (i < count) out[i] = run;
+    run += v[q];
+  }
+}
+
 template <typename KeyT, int K, bool OUT, int THREADS, int V>
-__global__ void __launch_bounds__(THREADS, 1024 / THREADS) tile_pass_kernel(TileArgs a) {
+__global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / THREADS) tile_pass_kernel(TileArgs a) {
   using C = TileCfg<KeyT, K, OUT, THREADS, V>;
   constexpr int D = C::D, KPL = C::KPL, T = C::T, WARPS = C::WARPS, WSLICE = C::WSLICE, SBW = C::SBW;
   constexpr int NLB = C::NLB, LPC = C::LPC;
@@ -442,14 +472,15 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tile_pass_kernel(Tile
   // ---- counts of the finest runs (key_D), published before the splits -----
   // Every thread counts its keys into its own column of 2^D counters in the
   // second key buffer (free until the first split scatters into it).
-  __shared__ uint32_t s_cnt[NLB], s_wcnt[WARPS][NLB];
+  __shared__ uint32_t s_cnt[NLB];
   const bool given = a.blockpre != nullptr;  // prefixes from the histogram kernel
   if (D >= 1 && given) {
     if (tid < NLB) {
       s_cnt[tid] = a.tilecnt[uint64_t(g) * NLB + tid];
       pre[tid] = a.blockpre[uint64_t(g / a.tiles_per_block) * NLB + tid] + a.relpre[uint64_t(g) * NLB + tid];
     }
-  } else if constexpr (D >= 1) {
+  } else if constexpr (D >= 1 && D <= kTileMaxLevels) {
+    __shared__ uint32_t s_wcnt[WARPS][NLB];
     constexpr int NB = 1 << D;
     uint32_t* cnt = reinterpret_cast<uint32_t*>(buf0 + T);
 #pragma unroll
@@ -485,6 +516,8 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tile_pass_kernel(Tile
       st_volatile(a.lookback + uint64_t(c) * a.tiles + g, (g == s_sg.tile0 ? kFlagPrefix : kFlagAggregate) | t);
     }
     // the first split's scatter into the counter area follows its barrier (A)
+  } else if constexpr (D > kTileMaxLevels) {
+    if (tid == 0) atomicOr(a.status, kErrBounds);  // deeper passes need their prefixes given
   }
   // valid keys of this warp and before it
   const uint32_t wbeg = uint32_t(warp) * WSLICE;
@@ -546,12 +579,14 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tile_pass_kernel(Tile
       ztot += z;
       zpre += w < warp ? z : 0u;
     }
-    if (tid == 0) {
-      s_ztot = ztot;
-      if (s >= 2) {  // starts of the key_s runs (sizes written after the previous split)
-        uint32_t run = 0;
-        for (int v = 0; v < (1 << s); ++v) { rst[s][v] = run; run += rsz[s][v]; }
-      }
+    if (tid == 0) s_ztot = ztot;
+    // starts of the key_s runs (sizes written after the previous split): a
+    // warp scan for the many runs of deep passes, else thread 0
+    if constexpr (K > kTileMaxLevels) {
+      if (s >= 2 && warp == 0) warp_exclusive_scan(rsz[s], rst[s], 1 << s, lane);
+    } else if (s >= 2 && tid == 0) {
+      uint32_t run = 0;
+      for (int v = 0; v < (1 << s); ++v) { rst[s][v] = run; run += rsz[s][v]; }
     }
     const uint32_t opre = vbefore - zpre;
     const uint32_t nb = smem_base + uint32_t((cur ^ 1) * T * KB);
@@ -592,7 +627,9 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tile_pass_kernel(Tile
   }
   __syncthreads();
   if constexpr (D >= 2) {
-    if (tid == 0) {
+    if constexpr (K > kTileMaxLevels) {
+      if (warp == 0) warp_exclusive_scan(rsz[D], rst[D], 1 << D, lane);
+    } else if (tid == 0) {
       uint32_t run = 0;
       for (int v = 0; v < (1 << D); ++v) { rst[D][v] = run; run += rsz[D][v]; }
     }
@@ -605,9 +642,11 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tile_pass_kernel(Tile
     write_bits64(st ? s_tx.wt : s_tx.wm, s_tx.nbits, dst, sbits, 0, n, uint32_t(tid), uint32_t(THREADS), a.status);
   }
   if constexpr (D >= 1) {
+    if (tid < NLB && s_cnt[tid] != rsz[D][tid]) atomicOr(a.status, kErrBounds);  // counts must agree
+  }
+  if constexpr (D >= 1 && D <= kTileMaxLevels) {
     __shared__ unsigned long long wsum[WARPS][NLB];
     __shared__ uint32_t wmask[WARPS], s_open;
-    if (tid < NLB && s_cnt[tid] != rsz[D][tid]) atomicOr(a.status, kErrBounds);  // counts must agree
     if (!given)
       segment_lookback_cta<NLB, WARPS>(a.lookback, a.tiles, g, s_sg.tile0, s_cnt, pre, wsum, wmask, &s_open,
                                        a.status);
@@ -627,6 +666,107 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tile_pass_kernel(Tile
     runpre[tid] = p;
   }
   __syncthreads();
+  if constexpr (K > kTileMaxLevels) {
+    // Levels 1..K-1 of both structures, word-parallel: a deep level has up to
+    // 2^(K-1) runs, most of them a few words long, so instead of a warp per
+    // run every thread takes destination words of the concatenated runs.
+    // Per (structure, level) list one warp scans the runs' word counts and
+    // stores a 16-byte record per run (first destination word, stream bit
+    // of that word, last whole word, lead and tail bits); a thread then
+    // finds its word's run by binary search.  The levels are not zeroed
+    // before this pass: a word shared with other runs is cleared in this
+    // run's bits, then set (writers of one word touch disjoint bits, so the
+    // atomics commute, and the runs of a level cover all of its bits).
+    constexpr int NC = 2 * (K - 1);         // lists
+    constexpr int MAXR = 1 << (K - 1);      // runs of the deepest level
+    constexpr int RPL = (MAXR + 31) / 32;   // runs per lane in a scan
+    constexpr int NREC = 2 * ((1 << K) - 2);
+    static_assert(size_t(NREC) * 16 + size_t(NC) * (MAXR + 1) * 4 <= size_t(2) * T * KB,
+                  "run records and word prefixes fit the key buffers");
+    uint4* rec = reinterpret_cast<uint4*>(smem_raw);                   // [NREC], the key buffers are free
+    uint32_t* wp = reinterpret_cast<uint32_t*>(smem_raw + NREC * 16);  // [NC][MAXR + 1]
+    __shared__ uint32_t s_cw[NC + 1];
+    const uint64_t nbits = s_tx.nbits;
+    for (int c = warp; c < NC; c += WARPS) {
+      const int st = c / (K - 1), j = 1 + c % (K - 1);
+      uint64_t* level = (st ? s_tx.wt : s_tx.wm) + uint64_t(j) * s_tx.stride;
+      uint4* rc = rec + st * ((1 << K) - 2) + (1 << j) - 2;
+      uint32_t cw[RPL], sum = 0;
+#pragma unroll
+      for (int q = 0; q < RPL; ++q) {
+        const int v = lane * RPL + q;
+        uint32_t w = 0;
+        if (st < nstruct && v < (1 << j)) {
+          const uint32_t len = rsz[j][v];
+          const uint64_t dst = s_table[st ? tile_wt_entry(K, j, v) : tile_wm_entry(j, v)] + runpre[(1 << j) - 2 + v];
+          if (len && dst + len > nbits) {
+            atomicOr(a.status, kErrBounds);
+          } else if (len) {
+            const uint32_t lead = uint32_t(dst & 63), tail = (lead + len) & 63;
+            w = (lead + len + 63) >> 6;
+            const uint32_t kb = lead ? 1u : 0u;
+            const uint32_t ke = (tail == 0 || (dst + len == nbits && w > kb)) ? w : w - 1;
+            const uint64_t out = reinterpret_cast<uint64_t>(level + (dst >> 6));
+            rc[v] = make_uint4(uint32_t(out), uint32_t(out >> 32), rst[j][v] - lead, ke | (lead << 16) | (tail << 24));
+          }
+        }
+        cw[q] = w;
+        sum += w;
+      }
+      uint32_t x = sum;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+        if (lane >= d) x += y;
+      }
+      uint32_t* w = wp + c * (MAXR + 1);
+      uint32_t run = x - sum;
+#pragma unroll
+      for (int q = 0; q < RPL; ++q) {
+        const int v = lane * RPL + q;
+        if (v < (1 << j)) w[v] = run;
+        run += cw[q];
+      }
+      if (lane == 31) {
+        w[1 << j] = x;
+        s_cw[c + 1] = x;
+      }
+    }
+    __syncthreads();
+    if (tid == 0) {
+      s_cw[0] = 0;
+      for (int c = 1; c <= NC; ++c) s_cw[c] += s_cw[c - 1];
+    }
+    __syncthreads();
+    const uint32_t total = s_cw[NC];
+    int c = 0;
+#pragma unroll 1
+    for (uint32_t f = uint32_t(tid); f < total; f += THREADS) {
+      while (s_cw[c + 1] <= f) ++c;
+      const int st = c / (K - 1), j = 1 + c % (K - 1);
+      const uint32_t* w = wp + c * (MAXR + 1);
+      const uint32_t k0 = f - s_cw[c];
+      int lo = 0, hi = 1 << j;  // the last run starting at or before word k0
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (w[mid] <= k0) lo = mid; else hi = mid;
+      }
+      const uint32_t k = k0 - w[lo], nw = w[lo + 1] - w[lo];
+      const uint4 r = rec[st * ((1 << K) - 2) + (1 << j) - 2 + lo];
+      uint64_t* out = reinterpret_cast<uint64_t*>(uint64_t(r.x) | (uint64_t(r.y) << 32));
+      const uint32_t base = r.z, ke = r.w & 0xFFFFu, lead = (r.w >> 16) & 0xFFu, tail = r.w >> 24;
+      const uint32_t* sb = sbits + j * SBW;
+      const uint64_t tmask = (k == nw - 1 && tail) ? ~(~0ull >> tail) : ~0ull;  // bits of the last word
+      if (k >= (lead ? 1u : 0u) && k < ke) {
+        out[k] = stream64(sb, base + 64 * k) & tmask;
+      } else {
+        const uint64_t val = k ? stream64(sb, base + 64 * k) : (stream64(sb, base + lead) >> lead);
+        const uint64_t mask = (k ? ~0ull : (~0ull >> lead)) & tmask;
+        atomicAnd(reinterpret_cast<unsigned long long*>(out + k), (unsigned long long)~mask);
+        atomicOr(reinterpret_cast<unsigned long long*>(out + k), (unsigned long long)(val & mask));
+      }
+    }
+  } else {
   constexpr int NOUT = OUT ? (1 << K) : 0;
   const int items = NOUT + nstruct * NINNER;
   const KeyT* cb = buf0 + cur * T;
@@ -653,6 +793,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tile_pass_kernel(Tile
       const uint64_t dst = s_table[st ? tile_wt_entry(K, j, v) : tile_wm_entry(j, v)] + runpre[e];
       write_bits64(level, s_tx.nbits, dst, sbits + j * SBW, rst[j][v], rsz[j][v], uint32_t(lane), 32u, a.status);
     }
+  }
   }
 
   // ---- this tile's slab of the next pass's levels --------------------------

@@ -94,7 +94,7 @@ def test_engines_agree(pg, orc, engines, k):
                 assert a.zeros() == b.zeros()
         check(pg, orc, tile, text[:300_000], 8, f"k={k}")
     finally:
-        tile.set_pass_levels(4)
+        tile.set_pass_levels(0)
 
 
 def test_segmented_byte_text(pg, orc, engines):
@@ -176,4 +176,37 @@ def test_rebuild_overwrites_every_bit(pg, orc, engines, width, L, n):
                 assert int(words[off + real - 1]) & ((1 << (64 - n % 64)) - 1) == 0, (tree, l, "padding bits")
         if not tree:
             assert [int(z) for z in zeros] == [int(z) for z in ref.zeros]
+    ds.free()
+
+
+@pytest.mark.parametrize("width,L", [(1, 5), (1, 6), (1, 7), (2, 7), (4, 6)])
+def test_single_pass_of_all_levels(pg, orc, engines, width, L):
+    """Texts of 5..7 levels take one tile pass of all their levels (given
+    prefixes, up to 64 runs per level and tile, shared words cleared and set
+    by the pass): partial tiles, skewed and uniform symbols, a misaligned
+    device text, and the same bits as passes of at most 4 levels."""
+    torch = torch_cuda()
+    tile, _ = engines
+    T = TILE[width]
+    rng = np.random.default_rng(width * 10 + L)
+    for n in (1, 63, T - 1, T + 1, 5 * T + 33, 400_001):
+        g = np.minimum(rng.geometric(0.08, n) - 1, (1 << L) - 1)
+        text = np.where(rng.random(n) < 0.6, g, rng.integers(0, 1 << L, n)).astype(DT[width])
+        check(pg, orc, tile, text, L, f"n={n}")
+    k4 = pg.Context()
+    k4.set_pass_levels(4)
+    text = rng.integers(0, 1 << L, 300_007).astype(DT[width])
+    for tree in (False, True):
+        a, b = build(pg, tile, text, L, tree), build(pg, k4, text, L, tree)
+        for l in range(L):
+            assert np.array_equal(np.asarray(a.bvs()[l]), np.asarray(b.bvs()[l])), (tree, l)
+    host = np.concatenate([np.zeros(3, DT[width]), text])
+    d = torch.from_numpy(host.view(np.uint8).copy()).cuda()
+    ds = pg.DeviceStructure(text.size, width, L, matrix=True, tree=True, context=tile)
+    ds.build(d.data_ptr() + 3 * width)
+    ds.check()
+    for which, tree in ((0, False), (1, True)):
+        ws, ref = ds.download(which), orc.build(text, L, tree, "ps")
+        for l in range(L):
+            assert np.array_equal(np.asarray(ws.bvs()[l]), ref.level(l)), (which, l)
     ds.free()
