@@ -336,6 +336,37 @@ __device__ __forceinline__ void write_bits64(uint64_t* level, uint64_t nbits, ui
   }
 }
 
+// write_bits64 for levels that were not zeroed: a shared word is cleared in
+// the run's bits before they are set.
+__device__ __forceinline__ void write_bits64_clear(uint64_t* level, uint64_t nbits, uint64_t dst, const uint32_t* sb,
+                                                   uint32_t src, uint32_t len, uint32_t k0, uint32_t step,
+                                                   uint32_t* status) {
+  if (len == 0) return;
+  if (dst + len > nbits) {
+    if (k0 == 0) atomicOr(status, kErrBounds);
+    return;
+  }
+  uint64_t* out = level + (dst >> 6);
+  const uint32_t lead = uint32_t(dst & 63);
+  const uint32_t nwords = (lead + len + 63) >> 6;
+  const uint32_t tail = (lead + len) & 63;
+  const bool at_end = dst + len == nbits;
+  const uint32_t kb = lead ? 1u : 0u;
+  const uint32_t ke = (tail == 0 || (at_end && nwords > kb)) ? nwords : nwords - 1;
+  const uint32_t base = src - lead;
+  for (uint32_t k = k0; k < nwords; k += step) {
+    const uint64_t tmask = (k == nwords - 1 && tail) ? ~(~0ull >> tail) : ~0ull;
+    if (k >= kb && k < ke) {
+      out[k] = stream64(sb, base + 64 * k) & tmask;
+    } else {
+      const uint64_t val = k ? stream64(sb, base + 64 * k) : (stream64(sb, src) >> lead);
+      const uint64_t mask = (k ? ~0ull : (~0ull >> lead)) & tmask;
+      atomicAnd(reinterpret_cast<unsigned long long*>(out + k), (unsigned long long)~mask);
+      atomicOr(reinterpret_cast<unsigned long long*>(out + k), (unsigned long long)(val & mask));
+    }
+  }
+}
+
 // One warp copies `len` bytes from shared memory to global memory: byte
 // stores up to a 4-byte aligned destination, then 32-bit stores whose source
 // bytes are funnel-shifted out of aligned shared words, then the tail.
@@ -677,7 +708,11 @@ __global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / T
     // before this pass: a word shared with other runs is cleared in this
     // run's bits, then set (writers of one word touch disjoint bits, so the
     // atomics commute, and the runs of a level cover all of its bits).
-    constexpr int NC = 2 * (K - 1);         // lists
+    // Levels 1..JW (runs of 32 words and more on average) go a warp per
+    // run, the deeper levels word-parallel.
+    constexpr int JW = 3;
+    constexpr int NCJ = K - 1 - JW;         // word-parallel levels per structure
+    constexpr int NC = 2 * NCJ;             // lists
     constexpr int MAXR = 1 << (K - 1);      // runs of the deepest level
     constexpr int RPL = (MAXR + 31) / 32;   // runs per lane in a scan
     constexpr int NREC = 2 * ((1 << K) - 2);
@@ -688,7 +723,7 @@ __global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / T
     __shared__ uint32_t s_cw[NC + 1];
     const uint64_t nbits = s_tx.nbits;
     for (int c = warp; c < NC; c += WARPS) {
-      const int st = c / (K - 1), j = 1 + c % (K - 1);
+      const int st = c / NCJ, j = JW + 1 + c % NCJ;
       uint64_t* level = (st ? s_tx.wt : s_tx.wm) + uint64_t(j) * s_tx.stride;
       uint4* rc = rec + st * ((1 << K) - 2) + (1 << j) - 2;
       uint32_t cw[RPL], sum = 0;
@@ -738,12 +773,24 @@ __global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / T
       for (int c = 1; c <= NC; ++c) s_cw[c] += s_cw[c - 1];
     }
     __syncthreads();
+    // levels 1..JW: a warp per run, round-robin
+    constexpr int NSH = (2 << JW) - 2;  // runs of levels 1..JW of one structure
+#pragma unroll 1
+    for (int it = warp; it < nstruct * NSH; it += WARPS) {
+      const int e = it % NSH, st = it / NSH;
+      int j = 1;
+      while (e + 2 >= (2 << j)) ++j;
+      const int v = e + 2 - (1 << j);
+      uint64_t* level = (st ? s_tx.wt : s_tx.wm) + uint64_t(j) * s_tx.stride;
+      const uint64_t dst = s_table[st ? tile_wt_entry(K, j, v) : tile_wm_entry(j, v)] + runpre[e];
+      write_bits64_clear(level, s_tx.nbits, dst, sbits + j * SBW, rst[j][v], rsz[j][v], uint32_t(lane), 32u, a.status);
+    }
     const uint32_t total = s_cw[NC];
     int c = 0;
 #pragma unroll 1
     for (uint32_t f = uint32_t(tid); f < total; f += THREADS) {
       while (s_cw[c + 1] <= f) ++c;
-      const int st = c / (K - 1), j = 1 + c % (K - 1);
+      const int st = c / NCJ, j = JW + 1 + c % NCJ;
       const uint32_t* w = wp + c * (MAXR + 1);
       const uint32_t k0 = f - s_cw[c];
       int lo = 0, hi = 1 << j;  // the last run starting at or before word k0
