@@ -378,18 +378,36 @@ void alloc_structure(Structure& s, const std::vector<uint64_t>& level_bits, uint
   if (rank_select) alloc_rank_select(s);
 }
 
-// Rank/select blocks of every level of a structure (asynchronous).
-void build_rank_select(pwmgpu_ctx* ctx, Structure& s) {
-  if (!s.rs || s.levels == 0) return;
-  CUDA_TRY(cudaMemsetAsync(s.d_rs, 0, s.rs_bytes, ctx->stream));
-  uint64_t max_real = 0;
-  for (auto& r : s.rs_levels) max_real = std::max<uint64_t>(max_real, (r.nwords + 31) / 32);
+// Rank/select blocks of every level of the given structures (asynchronous),
+// all levels in one launch sequence.  share_level0: a plain matrix and tree,
+// whose level 0 is the same bit vector: the tree's blocks of level 0 are a
+// copy of the matrix's.  The kernels write every entry that is read (l0 is
+// cleared by the scan kernel), so nothing is zeroed first.
+void build_rank_select(pwmgpu_ctx* ctx, Structure* wm, Structure* wt = nullptr, bool share_level0 = false) {
+  std::vector<RankSelectLevel> lv;
+  if (wm && wm->rs) lv.insert(lv.end(), wm->rs_levels.begin(), wm->rs_levels.end());
+  const bool copy0 = share_level0 && wm && wm->rs && wm->levels && wt && wt->rs && wt->levels;
+  if (wt && wt->rs) lv.insert(lv.end(), wt->rs_levels.begin() + (copy0 ? 1 : 0), wt->rs_levels.end());
+  if (lv.empty()) return;
+  cudaStream_t s = ctx->stream;
+  auto* d_lv = static_cast<RankSelectLevel*>(ctx->grow("rs_levels", lv.size() * sizeof(RankSelectLevel)));
+  CUDA_TRY(cudaMemcpyAsync(d_lv, lv.data(), lv.size() * sizeof(RankSelectLevel), cudaMemcpyHostToDevice, s));
+  uint64_t max_real = 0, bytes = 0;
+  for (auto& r : lv) {
+    max_real = std::max<uint64_t>(max_real, (r.nwords + 31) / 32);
+    bytes += r.nwords * 8 + (r.nwords / 32 + 1) * 8;
+  }
   const uint64_t stride = max_real + (max_real + 255) / 256 + 1;
-  uint32_t* tmp = static_cast<uint32_t*>(ctx->grow("rs_tmp", std::max<uint64_t>(stride * s.levels * 4, 256)));
-  uint64_t bytes = 0;
-  for (auto& r : s.rs_levels) bytes += r.nwords * 8 + (r.nwords / 32 + 1) * 8;
-  ProfScope ps(ctx, "rank_select", bytes);
-  launch_rank_select(s.rs_levels.data(), s.levels, s.d_rs_levels, tmp, stride, ctx->stream, &ctx->launches);
+  uint32_t* tmp = static_cast<uint32_t*>(ctx->grow("rs_tmp", std::max<uint64_t>(stride * lv.size() * 4, 256)));
+  {
+    ProfScope ps(ctx, "rank_select", bytes);
+    launch_rank_select(lv.data(), uint32_t(lv.size()), d_lv, tmp, stride, s, &ctx->launches);
+  }
+  if (copy0) {  // l0, l12, samples and meta of level 0 lie in this order in both structures
+    const RankSelectLevel &a = wm->rs_levels[0], &b = wt->rs_levels[0];
+    const size_t n = size_t(reinterpret_cast<const char*>(a.meta + 3) - reinterpret_cast<const char*>(a.l0));
+    CUDA_TRY(cudaMemcpyAsync(b.l0, a.l0, n, cudaMemcpyDeviceToDevice, s));
+  }
 }
 
 uint32_t read_status(pwmgpu_ctx* ctx) {
@@ -900,8 +918,7 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   }
   else
     run_passes(ctx, d_text, wx->width, wx->width, false, L, plan, tabs, wx->wm, want_tree ? &wx->wt : nullptr);
-  if (wx->wm.rs && !wx->wm_internal) build_rank_select(ctx, wx->wm);
-  if (want_tree && wx->wt.rs) build_rank_select(ctx, wx->wt);
+  build_rank_select(ctx, wx->wm.rs && !wx->wm_internal ? &wx->wm : nullptr, want_tree ? &wx->wt : nullptr, true);
   CUDA_TRY(cudaGetLastError());
   if (any_out) {
     for (int st = 0; st < 2; ++st) {
@@ -1093,8 +1110,7 @@ void build_huffman(pwmgpu_ctx* ctx, const void* d_text, uint64_t n, uint32_t wid
   launch_huffman_keys(d_text, n, width, d_len, d_word, ncodes, key_bytes, keys, ctx->d_status, s, &ctx->launches);
   run_passes(ctx, keys, key_bytes, width, true, levels, plan, tabs, wm, wt);
   check_device_status(ctx);
-  if (!is_tree && wm.rs) build_rank_select(ctx, wm);
-  if (wt && wt->rs) build_rank_select(ctx, *wt);
+  build_rank_select(ctx, !is_tree ? &wm : nullptr, wt);
 }
 
 // Host thresholds / permutation of a generator distribution.

@@ -111,6 +111,14 @@ __global__ void __launch_bounds__(1024) rs_scan_kernel(const RankSelectLevel* lv
   const uint64_t nreal = (L.nwords + kL1Cover - 1) / kL1Cover;
   const uint64_t ncta = (nreal + kRsThreads - 1) / kRsThreads;
   uint32_t* cta_tot = tmp + blockIdx.x * tmp_stride + nreal;
+  // l0: all zero below 2^32-1 bits per level (the only sizes built); the
+  // sample counts stay 0 for levels too short to examine a block
+  // (rs_finish_kernel writes them otherwise)
+  for (uint64_t i = threadIdx.x; i < L.nwords / (4294967295ull / 64) + 1; i += blockDim.x) L.l0[i] = 0;
+  if (threadIdx.x == 0) {
+    L.meta[0] = 0;
+    L.meta[1] = 0;
+  }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   __shared__ unsigned long long wsum[32];
   __shared__ unsigned long long carry;
