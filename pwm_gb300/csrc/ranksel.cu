@@ -177,12 +177,13 @@ __device__ __forceinline__ bool thread_block_select(const uint64_t* data, uint64
     return true;
   }
   // skip whole L2 blocks (8 words) by their counts; the fourth has no field
+  const uint32_t fields = l12[2 * b + 1];
   uint32_t sub = 0;
   for (; sub < 3; ++sub) {
     const uint64_t ws = w0 + kL2Cover * sub;
     const uint64_t left = ws >= nwords ? 0 : nwords - ws;
     const uint32_t words = uint32_t(left < kL2Cover ? left : kL2Cover);
-    const uint32_t ones = l2_of(l12, b, sub);
+    const uint32_t ones = (fields >> (10 * sub)) & 1023u;
     const uint32_t cnt = value ? ones : 64u * words - ones;
     if (rem <= cnt) break;
     rem -= cnt;
