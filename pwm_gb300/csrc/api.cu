@@ -593,7 +593,10 @@ const void* enqueue_tile_pass(pwmgpu_ctx* ctx, const std::vector<TilePassHost>& 
   const uint64_t nlb = uint64_t(1) << D;
   const uint64_t lb_bytes = uint64_t(std::max<uint32_t>(p.tiles, 1)) * nlb * 8;
   auto* lb = static_cast<unsigned long long*>(ctx->grow("lookback", lb_bytes + 64));
-  CUDA_TRY(cudaMemsetAsync(lb, 0, lb_bytes + 64, s));
+  // with given prefixes the pass reads only its tile counter
+  const bool given = pi == 0 && first && p.segs.size() == 1;
+  if (given) CUDA_TRY(cudaMemsetAsync(reinterpret_cast<unsigned char*>(lb) + lb_bytes, 0, 64, s));
+  else CUDA_TRY(cudaMemsetAsync(lb, 0, lb_bytes + 64, s));
   TileArgs a{};
   a.in = in;
   a.out = p.out ? (in == ping ? pong : ping) : nullptr;
@@ -615,13 +618,14 @@ const void* enqueue_tile_pass(pwmgpu_ctx* ctx, const std::vector<TilePassHost>& 
     const uint64_t per = (a.zero_words + p.tiles - 1) / std::max<uint32_t>(p.tiles, 1);
     a.zero_per_tile = uint32_t((per + 1) & ~uint64_t(1));
   }
-  if (pi == 0 && first && p.segs.size() == 1) {
+  if (given) {
     a.blockpre = first->blockpre;
     a.relpre = first->relpre;
     a.tilecnt = first->tilecnt;
     a.tiles_per_block = first->tiles_per_block;
     a.first_level_written = first->level0_written ? 1u : 0u;
   }
+  if (pi == 0 && first) a.clear_edges = 1u;  // the histogram kernel did not zero the first pass's levels
   {
     const uint64_t structs = (wt && p.segmented) ? 2 : 1;
     const uint64_t skipped = a.first_level_written ? structs * words_for(n) * 8 : 0;
@@ -785,15 +789,9 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     first.level0_written = true;
     uint64_t* l0[2] = {wx->wm.present ? wx->wm.d_words : nullptr, wx->wt.present ? wx->wt.d_words : nullptr};
     if (!l0[0]) std::swap(l0[0], l0[1]);
-    // levels 1..Kz-1 of both structures, a slab per tile (a pass of more
-    // than 4 levels clears its shared words itself)
-    HistZero hz;
-    if (Kz > 1 && Kz <= kTileMaxLevels) {
-      hz.a = l0[0] + wx->wm.offs[1];
-      hz.b = l0[1] ? l0[1] + wx->wm.offs[1] : nullptr;
-      hz.words = (uint32_t(Kz) < L ? wx->wm.offs[Kz] : wx->wm.total_words) - wx->wm.offs[1];
-      hz.per_tile = ((hz.words + tiles - 1) / tiles + 1) & ~uint64_t(1);
-    }
+    // (the first pass clears the shared words of its levels 1..Kz-1 itself,
+    // cheaper than zeroing them here; later passes' levels are zeroed by the
+    // pass before them)
     // pieces of whole histogram blocks: uploaded, counted, their level-0 words sent back
     const uint64_t block_keys = uint64_t(per) * T;
     const uint32_t piece_blocks =
@@ -810,8 +808,8 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
       }
       launch_tile_histogram_blocks(d_text, n, wx->width, L, D0, T, b0, nb, d_hist,
                                    const_cast<uint32_t*>(first.tilecnt), const_cast<uint32_t*>(first.relpre),
-                                   const_cast<unsigned long long*>(first.blockpre), l0[0], l0[1], hz, ctx->d_status,
-                                   s, &ctx->launches);
+                                   const_cast<unsigned long long*>(first.blockpre), l0[0], l0[1], ctx->d_status, s,
+                                   &ctx->launches);
       if (stream_out) {
         const uint64_t w1 = k1 == n ? words_for(n) : k1 / 64;
         for (int st = 0; st < 2; ++st)
@@ -821,7 +819,7 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
           }
       }
     }
-    launch_tile_block_scan(const_cast<unsigned long long*>(first.blockpre), nblocks, D0, s, &ctx->launches);
+    // (the block scan follows with the first pass's start table, below)
   } else {
     if (pinned_in) CUDA_TRY(cudaMemcpyAsync(const_cast<void*>(d_text), io->text, n * wx->width,
                                             cudaMemcpyHostToDevice, s));
@@ -859,8 +857,9 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     const TileBlob b0 = tile_blob(early, 0, 1, L, n, wx->wm, want_tree ? &wx->wt : nullptr);
     auto* d_b0 = static_cast<unsigned char*>(ctx->grow("tile_plan0", b0.bytes.size()));
     CUDA_TRY(cudaMemcpyAsync(d_b0, b0.bytes.data(), b0.bytes.size(), cudaMemcpyHostToDevice, s));
-    launch_first_pass_table(d_hist, L, uint32_t(p0.K), p0.out, want_tree,
-                            reinterpret_cast<uint64_t*>(d_b0 + b0.table[0]), s, &ctx->launches);
+    launch_tile_block_scan(const_cast<unsigned long long*>(first.blockpre), tile_hist_blocks(n, T), D0, d_hist, L,
+                           uint32_t(p0.K), p0.out, want_tree, reinterpret_cast<uint64_t*>(d_b0 + b0.table[0]), s,
+                           &ctx->launches);
     next_in = enqueue_tile_pass(ctx, early, 0, d_b0, b0, d_text, wx->width, n, wx->wm,
                                 want_tree ? &wx->wt : nullptr, &first);
     from = 1;

@@ -80,14 +80,16 @@ __global__ void __launch_bounds__(kHistThreads) leaf_hist_global(const T* text, 
 // their prefix inside the block, at the end the block's totals.
 constexpr int kTileHistThreads = 256;
 
-template <typename T>
+// BYTES8: 8-bit symbols and 8 levels, so that every byte is a bin: a key
+// costs a byte extract, an address and the atomic.
+template <typename T, bool BYTES8>
 __global__ void __launch_bounds__(kTileHistThreads) tile_hist_kernel(const T* text, uint64_t n, uint32_t levels,
                                                                  uint32_t D, uint32_t tile_keys,
                                                                  uint32_t tiles_per_block, uint32_t block0,
                                                                  unsigned long long* hist, uint32_t* tilecnt,
                                                                  uint32_t* relpre, unsigned long long* blocksum,
                                                                  uint64_t* level0_a, uint64_t* level0_b,
-                                                                 HistZero zero, uint32_t* status) {
+                                                                 uint32_t* status) {
   constexpr int WARPS = kTileHistThreads / 32;
   constexpr int BINS = 256;
   // One counter per (bin, lane) shared by the block's warps: lane k counts
@@ -141,15 +143,6 @@ __global__ void __launch_bounds__(kTileHistThreads) tile_hist_kernel(const T* te
     if (start >= n) break;
     const uint64_t len = n - start < tile_keys ? n - start : tile_keys;
     const T* p = text + start;
-    if (zero.words) {  // this tile's slab of the first pass's other levels
-      const uint64_t z0 = tile * zero.per_tile;
-      const uint64_t z1 = z0 + zero.per_tile < zero.words ? z0 + zero.per_tile : zero.words;
-      const uint4 zv = make_uint4(0u, 0u, 0u, 0u);
-      for (uint64_t w = z0 + 2 * uint64_t(tid); w < z1; w += 2 * kTileHistThreads) {
-        *reinterpret_cast<uint4*>(zero.a + w) = zv;
-        if (zero.b) *reinterpret_cast<uint4*>(zero.b + w) = zv;
-      }
-    }
     if (full_tile(tile)) {
       uint4 cur[HV];
 #pragma unroll
@@ -176,9 +169,17 @@ __global__ void __launch_bounds__(kTileHistThreads) tile_hist_kernel(const T* te
 #pragma unroll
       for (int v = 0; v < HV; ++v) {
         if (v >= nv) break;
-        const T* s = reinterpret_cast<const T*>(&cur[v]);
+        if constexpr (BYTES8) {
+          const uint32_t w[4] = {cur[v].x, cur[v].y, cur[v].z, cur[v].w};
 #pragma unroll
-        for (int q = 0; q < PER; ++q) count(uint32_t(s[q]));
+          for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) atomicAdd(&mine[__byte_perm(w[q], 0u, 0x4440u + k) * 32], 1u);
+        } else {
+          const T* s = reinterpret_cast<const T*>(&cur[v]);
+#pragma unroll
+          for (int q = 0; q < PER; ++q) count(uint32_t(s[q]));
+        }
       }
     } else {
       const uint64_t nvec = (reinterpret_cast<uintptr_t>(p) % 16 == 0) ? len / PER : 0;
@@ -234,90 +235,124 @@ __global__ void __launch_bounds__(kTileHistThreads) tile_hist_kernel(const T* te
   if (tid < int(bins) && prev) atomicAdd(&hist[tid], (unsigned long long)prev);
 }
 
-// Exclusive prefix, per column, of the nblocks x NB block totals (in place):
-// CTA c scans column c, each thread a run of consecutive blocks.
-__global__ void __launch_bounds__(256) tile_block_scan_kernel(unsigned long long* blocksum, uint32_t nblocks,
-                                                              uint32_t NB) {
-  const uint32_t c = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint32_t per = (nblocks + 255) / 256;
-  const uint32_t b0 = min(nblocks, tid * per), b1 = min(nblocks, b0 + per);
-  unsigned long long sum = 0;
-  for (uint32_t b = b0; b < b1; ++b) sum += blocksum[uint64_t(b) * NB + c];
-  unsigned long long x = sum;
+// After the tile histogram, one launch of NB + 1 CTAs of 1024 threads:
+//  * CTA c < NB: the exclusive prefix, per column c, of the nblocks x NB
+//    block totals (in place), each thread a run of up to 4 consecutive
+//    blocks (more in a loop for longer texts);
+//  * CTA NB: the start table of the first tile pass of a text with levels
+//    <= 8 (one segment, the whole text) from the leaf histogram, the entries
+//    the host's plan gives that pass: matrix runs of key_j in key order, tree
+//    runs in natural prefix order, runs of S_K; tree entries 0 without a
+//    tree.  A key_j run is a contiguous range of bins (those with the same
+//    j-bit prefix), so its count is a difference of the bins' prefix sums,
+//    and the tree's starts are those prefix sums themselves.
+template <int W>
+__device__ __forceinline__ unsigned long long block_exclusive_scan(unsigned long long v, unsigned long long* wsum,
+                                                                   unsigned long long* total) {
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long x = v;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
     const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, d);
     if (lane >= uint32_t(d)) x += y;
   }
-  __shared__ unsigned long long wsum[8];
   if (lane == 31) wsum[warp] = x;
   __syncthreads();
-  unsigned long long run = x - sum;
-  for (uint32_t w = 0; w < warp; ++w) run += wsum[w];
-  for (uint32_t b = b0; b < b1; ++b) {
-    const unsigned long long v = blocksum[uint64_t(b) * NB + c];
-    blocksum[uint64_t(b) * NB + c] = run;
-    run += v;
-  }
-}
-
-// Start table of the first tile pass of a text with levels <= 8 (one
-// segment, the whole text) from its leaf histogram: the entries the host's
-// plan gives that pass (matrix runs of key_j in key order, tree runs in
-// natural prefix order, runs of S_K; tree entries 0 without a tree).  One
-// CTA of 256 threads: thread b adds bin b to its key_j runs, then warp w
-// scans the runs of levels w and w + 8.
-__global__ void __launch_bounds__(256) first_pass_table_kernel(const unsigned long long* hist, uint32_t levels,
-                                                               uint32_t K, uint32_t out, uint32_t tree,
-                                                               uint64_t* table) {
-  constexpr int KM = kTileGivenMaxLevels;
-  __shared__ unsigned long long ck[KM + 1][1 << KM];  // counts of key_j == v
-  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (uint32_t i = tid; i < (KM + 1) << KM; i += blockDim.x) (&ck[0][0])[i] = 0;
-  __syncthreads();
-  if (tid < (1u << levels)) {
-    const unsigned long long c = hist[tid];
-    if (c)
-      for (uint32_t j = 0; j <= K; ++j) atomicAdd(&ck[j][reverse_low_bits(tid >> (levels - j), j)], c);
-  }
-  __syncthreads();
-  // exclusive scan over i < 2^j of ck[j][key(i)], written to entry(i); lane
-  // l takes i = 8l .. 8l+7
-  auto scan = [&](uint32_t j, auto key, auto entry) {
-    const uint32_t R = 1u << j;
-    unsigned long long v[8], sum = 0;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const uint32_t i = 8 * lane + q;
-      v[q] = i < R ? ck[j][key(i)] : 0ull;
-      sum += v[q];
-    }
-    unsigned long long x = sum;
+  if (warp == 0) {
+    unsigned long long w = lane < uint32_t(W) ? wsum[lane] : 0ull;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-      const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, d);
-      if (lane >= uint32_t(d)) x += y;
+      const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, w, d);
+      if (lane >= uint32_t(d)) w += y;
     }
-    unsigned long long run = x - sum;
+    if (lane < uint32_t(W)) wsum[lane] = w;  // inclusive
+  }
+  __syncthreads();
+  if (total) *total = wsum[W - 1];
+  return (warp ? wsum[warp - 1] : 0ull) + x - v;
+}
+
+__global__ void __launch_bounds__(1024) tile_block_scan_kernel(unsigned long long* blocksum, uint32_t nblocks,
+                                                               uint32_t NB, const unsigned long long* hist,
+                                                               uint32_t levels, uint32_t K, uint32_t out,
+                                                               uint32_t tree, uint64_t* table) {
+  __shared__ unsigned long long wsum[32];
+  const uint32_t tid = threadIdx.x;
+  if (blockIdx.x < NB) {
+    const uint32_t c = blockIdx.x;
+    const uint32_t per = (nblocks + 1023) / 1024;
+    const uint32_t b0 = min(nblocks, tid * per), b1 = min(nblocks, b0 + per);
+    unsigned long long v[4] = {0, 0, 0, 0}, sum = 0;
+    if (per <= 4) {
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const uint32_t i = 8 * lane + q;
-      if (i < R) entry(i, run);
-      run += v[q];
+      for (int q = 0; q < 4; ++q)
+        if (b0 + q < b1) v[q] = blocksum[uint64_t(b0 + q) * NB + c];
+      sum = v[0] + v[1] + v[2] + v[3];
+    } else {
+      for (uint32_t b = b0; b < b1; ++b) sum += blocksum[uint64_t(b) * NB + c];
     }
-  };
-  for (uint32_t j = warp; j <= K; j += 8) {
-    if (j < K) {
-      scan(j, [](uint32_t v) { return v; },
-           [&](uint32_t v, unsigned long long p) { table[tile_wm_entry(int(j), int(v))] = p; });
-      scan(j, [&](uint32_t p) { return reverse_low_bits(p, j); },  // natural prefix order
-           [&](uint32_t p, unsigned long long q) {
-             table[tile_wt_entry(int(K), int(j), int(reverse_low_bits(p, j)))] = tree ? q : 0ull;
-           });
-    } else if (out) {
-      scan(j, [](uint32_t v) { return v; },
-           [&](uint32_t v, unsigned long long p) { table[tile_out_entry(int(K), int(v))] = p; });
+    unsigned long long run = block_exclusive_scan<32>(sum, wsum, nullptr);
+    if (per <= 4) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (b0 + q < b1) {
+          blocksum[uint64_t(b0 + q) * NB + c] = run;
+          run += v[q];
+        }
+    } else {
+      for (uint32_t b = b0; b < b1; ++b) {
+        const unsigned long long x = blocksum[uint64_t(b) * NB + c];
+        blocksum[uint64_t(b) * NB + c] = run;
+        run += x;
+      }
     }
+    return;
+  }
+  if (!table) return;
+  // prefix sums over the bins in natural order: P[b] = bins before b
+  __shared__ unsigned long long P[(1 << kTileGivenMaxLevels) + 1];
+  const uint32_t bins = 1u << levels;
+  const unsigned long long cnt = tid < bins ? hist[tid] : 0ull;
+  unsigned long long total;
+  const unsigned long long ex = block_exclusive_scan<32>(cnt, wsum, &total);
+  if (tid < bins) P[tid] = ex;
+  if (tid == 0) P[bins] = total;
+  __syncthreads();
+  // warp j: level j (j < K: matrix and tree starts; j == K: runs of S_K)
+  const uint32_t warp = tid >> 5, lane = tid & 31;
+  if (warp > K || (warp == K && !out)) return;
+  const uint32_t j = warp, R = 1u << j, sh = levels - j;
+  // key order x: the run of natural prefix p = rev(x); lane takes x = 8 lane + q
+  unsigned long long v[8], sum = 0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const uint32_t x = 8 * lane + q;
+    v[q] = 0;
+    if (x < R) {
+      const uint32_t p = reverse_low_bits(x, j);
+      v[q] = P[(p + 1) << sh] - P[p << sh];
+    }
+    sum += v[q];
+  }
+  unsigned long long xs = sum;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, xs, d);
+    if (lane >= uint32_t(d)) xs += y;
+  }
+  unsigned long long run = xs - sum;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const uint32_t x = 8 * lane + q;
+    if (x < R) {
+      if (j < K) {
+        table[tile_wm_entry(int(j), int(x))] = run;
+        table[tile_wt_entry(int(K), int(j), int(x))] = tree ? P[reverse_low_bits(x, j) << sh] : 0ull;
+      } else {
+        table[tile_out_entry(int(K), int(x))] = run;
+      }
+    }
+    run += v[q];
   }
 }
 
@@ -503,31 +538,28 @@ uint32_t tile_hist_blocks(uint64_t n, uint32_t tile_keys) {
 void launch_tile_histogram_blocks(const void* text, uint64_t n, uint32_t width, uint32_t levels, uint32_t D,
                                   uint32_t tile_keys, uint32_t block0, uint32_t nblk, unsigned long long* hist,
                                   uint32_t* tilecnt, uint32_t* relpre, unsigned long long* blocksum,
-                                  uint64_t* level0_a, uint64_t* level0_b, const HistZero& zero, uint32_t* status,
-                                  cudaStream_t s, uint64_t* launches) {
+                                  uint64_t* level0_a, uint64_t* level0_b, uint32_t* status, cudaStream_t s,
+                                  uint64_t* launches) {
   if (n == 0 || nblk == 0) return;
   const uint32_t per = tile_hist_tiles_per_block();
-#define PWMGPU_TH(T)                                                                                          \
-  tile_hist_kernel<<<nblk, kTileHistThreads, 0, s>>>(static_cast<const T*>(text), n, levels, D, tile_keys, per, \
-                                                     block0, hist, tilecnt, relpre, blocksum, level0_a,        \
-                                                     level0_b, zero, status)
-  if (width == 1) PWMGPU_TH(uint8_t);
-  else if (width == 2) PWMGPU_TH(uint16_t);
-  else PWMGPU_TH(uint32_t);
+#define PWMGPU_TH(T, B8)                                                                                       \
+  tile_hist_kernel<T, B8><<<nblk, kTileHistThreads, 0, s>>>(static_cast<const T*>(text), n, levels, D, tile_keys, \
+                                                            per, block0, hist, tilecnt, relpre, blocksum,       \
+                                                            level0_a, level0_b, status)
+  if (width == 1 && levels == 8) PWMGPU_TH(uint8_t, true);
+  else if (width == 1) PWMGPU_TH(uint8_t, false);
+  else if (width == 2) PWMGPU_TH(uint16_t, false);
+  else PWMGPU_TH(uint32_t, false);
 #undef PWMGPU_TH
   ++*launches;
 }
 
-void launch_first_pass_table(const unsigned long long* hist, uint32_t levels, uint32_t K, bool out, bool tree,
-                             uint64_t* table, cudaStream_t s, uint64_t* launches) {
-  first_pass_table_kernel<<<1, 256, 0, s>>>(hist, levels, K, out ? 1u : 0u, tree ? 1u : 0u, table);
-  ++*launches;
-}
-
-void launch_tile_block_scan(unsigned long long* blocksum, uint32_t nblocks, uint32_t D, cudaStream_t s,
+void launch_tile_block_scan(unsigned long long* blocksum, uint32_t nblocks, uint32_t D, const unsigned long long* hist,
+                            uint32_t levels, uint32_t K, bool out, bool tree, uint64_t* table, cudaStream_t s,
                             uint64_t* launches) {
   if (nblocks == 0) return;
-  tile_block_scan_kernel<<<1u << D, 256, 0, s>>>(blocksum, nblocks, 1u << D);
+  tile_block_scan_kernel<<<(1u << D) + (table ? 1u : 0u), 1024, 0, s>>>(blocksum, nblocks, 1u << D, hist, levels, K,
+                                                                        out ? 1u : 0u, tree ? 1u : 0u, table);
   ++*launches;
 }
 

@@ -25,28 +25,19 @@ void launch_leaf_histogram(const void* text, uint64_t n, uint32_t width, uint32_
 // (the symbols' top bits in text order) to level0_a and level0_b (if set).
 // hist must be zeroed.  launch_tile_block_scan then turns blocksum into each
 // block's exclusive prefix.
-// With zero.words set, tile t also zeroes words [t * per_tile, (t + 1) *
-// per_tile) of [0, words) at zero.a (and zero.b): 16-byte aligned, even
-// counts.
-struct HistZero {
-  uint64_t* a = nullptr;
-  uint64_t* b = nullptr;
-  uint64_t words = 0;
-  uint64_t per_tile = 0;
-};
 uint32_t tile_hist_tiles_per_block();
 uint32_t tile_hist_blocks(uint64_t n, uint32_t tile_keys);
 void launch_tile_histogram_blocks(const void* text, uint64_t n, uint32_t width, uint32_t levels, uint32_t D,
                                   uint32_t tile_keys, uint32_t block0, uint32_t nblk, unsigned long long* hist,
                                   uint32_t* tilecnt, uint32_t* relpre, unsigned long long* blocksum,
-                                  uint64_t* level0_a, uint64_t* level0_b, const HistZero& zero, uint32_t* status,
-                                  cudaStream_t s, uint64_t* launches);
-void launch_tile_block_scan(unsigned long long* blocksum, uint32_t nblocks, uint32_t D, cudaStream_t s,
+                                  uint64_t* level0_a, uint64_t* level0_b, uint32_t* status, cudaStream_t s,
+                                  uint64_t* launches);
+// With `table` set, the same launch also writes the start table
+// (tile_table_size(K) entries) of the first tile pass of the text (levels <=
+// 8, one segment) from its leaf histogram.
+void launch_tile_block_scan(unsigned long long* blocksum, uint32_t nblocks, uint32_t D, const unsigned long long* hist,
+                            uint32_t levels, uint32_t K, bool out, bool tree, uint64_t* table, cudaStream_t s,
                             uint64_t* launches);
-// Start table (tile_table_size(K) entries) of the first tile pass of a text
-// with levels <= 8 from its leaf histogram, on the device.
-void launch_first_pass_table(const unsigned long long* hist, uint32_t levels, uint32_t K, bool out, bool tree,
-                             uint64_t* table, cudaStream_t s, uint64_t* launches);
 
 // ---- split passes -----------------------------------------------------------
 // Geometry of the split pass for a key width: tile size in elements.

@@ -93,6 +93,7 @@ struct TileArgs {
   const uint32_t* tilecnt;
   uint32_t tiles_per_block;
   uint32_t first_level_written;  // level l is already written (by the histogram kernel)
+  uint32_t clear_edges;          // the levels were not zeroed: shared words are cleared before they are set
   // Optional: words [0, zero_words) at zero_a (and zero_b) are zeroed, tile g
   // taking words [g * zero_per_tile, (g + 1) * zero_per_tile): the levels of
   // the next pass, whose edge words it ORs.  16-byte aligned, even counts.
@@ -838,7 +839,11 @@ __global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / T
       const int v = e + 2 - (1 << j);
       uint64_t* level = (st ? s_tx.wt : s_tx.wm) + uint64_t(j) * s_tx.stride;
       const uint64_t dst = s_table[st ? tile_wt_entry(K, j, v) : tile_wm_entry(j, v)] + runpre[e];
-      write_bits64(level, s_tx.nbits, dst, sbits + j * SBW, rst[j][v], rsz[j][v], uint32_t(lane), 32u, a.status);
+      if (a.clear_edges)
+        write_bits64_clear(level, s_tx.nbits, dst, sbits + j * SBW, rst[j][v], rsz[j][v], uint32_t(lane), 32u,
+                           a.status);
+      else
+        write_bits64(level, s_tx.nbits, dst, sbits + j * SBW, rst[j][v], rsz[j][v], uint32_t(lane), 32u, a.status);
     }
   }
   }
