@@ -216,10 +216,11 @@ def batched_vs_per_text(torch, pg, ctx, count=4096, seed=1, reps=3):
 def other_workloads(torch, pg, ctx, reps=3):
     """Build times of the other configured workloads (resident text, CUDA
     events on the library's stream; the drop-in Huffman builds host to host):
-    2^26 DNA-like bytes with 2 levels (matrix + tree), 2^28 16-bit symbols
-    with 16 levels (plain matrix + tree, and Huffman-shaped matrix and tree
-    with pwm's codes from the host builder), 2^26 32-bit symbols over 2^20
-    values with 20 levels (matrix + rank/select)."""
+    2^26 DNA-like bytes with 2 levels (matrix + tree), 2^30 bytes uniform
+    over 64 values with 6 levels (matrix + tree in one tile pass), 2^28
+    16-bit symbols with 16 levels (plain matrix + tree, and Huffman-shaped
+    matrix and tree with pwm's codes from the host builder), 2^26 32-bit
+    symbols over 2^20 values with 20 levels (matrix + rank/select)."""
     import numpy as np
     out = {}
     stream = torch.cuda.current_stream()
@@ -244,6 +245,7 @@ def other_workloads(torch, pg, ctx, reps=3):
         return t
 
     timed("dna_2p26_levels2", 1 << 26, 1, 2, pg.GEN_DNA4, 0, True, False)
+    timed("uniform64_2p30_levels6", 1 << 30, 1, 6, pg.GEN_UNIFORM, 64, True, False)
     t16 = timed("mix16_2p28_levels16", 1 << 28, 2, 16, pg.GEN_MIX16, 0, True, False)
     timed("uniform20_2p26_levels20", 1 << 26, 4, 20, pg.GEN_UNIFORM, 1 << 20, False, True)
     host16 = t16.cpu().numpy().view(np.uint16)
