@@ -217,7 +217,8 @@ def other_workloads(torch, pg, ctx, reps=3):
     """Build times of the other configured workloads (resident text, CUDA
     events on the library's stream; the drop-in Huffman builds host to host):
     2^26 DNA-like bytes with 2 levels (matrix + tree), 2^30 bytes uniform
-    over 64 values with 6 levels (matrix + tree in one tile pass), 2^28
+    over 64 values with 6 levels (matrix + tree in one tile pass), the 1 GiB
+    Zipf text built as 16 shards and merged (pwm's wx_dd_*), 2^28
     16-bit symbols with 16 levels (plain matrix + tree, and Huffman-shaped
     matrix and tree with pwm's codes from the host builder), 2^26 32-bit
     symbols over 2^20 values with 20 levels (matrix + rank/select)."""
@@ -225,27 +226,41 @@ def other_workloads(torch, pg, ctx, reps=3):
     out = {}
     stream = torch.cuda.current_stream()
 
-    def timed(name, n, width, levels, dist, param, tree, rs):
+    def timed(name, n, width, levels, dist, param, tree, rs, shards=0):
         dtype = {1: torch.uint8, 2: torch.int16, 4: torch.int32}[width]
         t = torch.empty(n, dtype=dtype, device="cuda")
         pg.generate(dist, 3, n, width, param=param, device_ptr=t.data_ptr(), context=ctx)
         ds = pg.DeviceStructure(n, width, levels, matrix=True, tree=tree, rank_select=rs, context=ctx)
-        ds.build(t.data_ptr())
+        build = (lambda: ds.build_sharded(t.data_ptr(), shards)) if shards else (lambda: ds.build(t.data_ptr()))
+        build()
+        ctx.lib.pwmgpu_ctx_profile(ctx.h, 1)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(reps):
-            ds.build(t.data_ptr())
+            build()
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / reps
+        buf = ctypes.create_string_buffer(1 << 16)
+        ctx.check(ctx.lib.pwmgpu_ctx_profile_read(ctx.h, buf, len(buf)))
+        ctx.lib.pwmgpu_ctx_profile(ctx.h, 0)
+        prof = parse_profile(buf.value.decode())
         ds.check()
         ds.free()
         out[name] = {"n": n, "word_width": width, "levels": levels, "structures": ["matrix"] + (["tree"] if tree else []),
                      "rank_select": rs, "ms": ms, "text_gbs": n * width / ms / 1e6}
+        if shards:
+            m = prof.get("merge", {})
+            out[name]["shards"] = shards
+            if m.get("ms"):
+                # the merge reads and writes every level of both structures once
+                out[name]["merge_ms"] = m["ms"] / reps
+                out[name]["merge_gbs"] = m["bytes"] / (m["ms"] / 1e3) / 1e9
         return t
 
     timed("dna_2p26_levels2", 1 << 26, 1, 2, pg.GEN_DNA4, 0, True, False)
     timed("uniform64_2p30_levels6", 1 << 30, 1, 6, pg.GEN_UNIFORM, 64, True, False)
+    timed("zipf_2p30_levels8_16_shards", 1 << 30, 1, 8, pg.GEN_ZIPF256, 0, True, False, shards=16)
     t16 = timed("mix16_2p28_levels16", 1 << 28, 2, 16, pg.GEN_MIX16, 0, True, False)
     timed("uniform20_2p26_levels20", 1 << 26, 4, 20, pg.GEN_UNIFORM, 1 << 20, False, True)
     host16 = t16.cpu().numpy().view(np.uint16)

@@ -45,6 +45,8 @@ typedef enum pwmgpu_status {
 #define PWMGPU_TREE 0x2u        /* levelwise wavelet tree: bit vectors              */
 #define PWMGPU_RANK_SELECT 0x4u /* popcount rank/select support for every level     */
 #define PWMGPU_HUFFMAN 0x8u     /* Huffman-shaped levels (codes given or built)     */
+#define PWMGPU_KEEP_HISTOGRAM 0x10u /* keep the leaf histogram on the host after a build
+                                     * (a shard to merge, pwmgpu_wx_merge)              */
 
 /* Query kinds for pwmgpu_wx_query. */
 #define PWMGPU_Q_ACCESS 0
@@ -206,6 +208,34 @@ PWMGPU_API pwmgpu_status pwmgpu_wx_query(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, i
 PWMGPU_API pwmgpu_status pwmgpu_wx_query_host(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which, int op,
                                               const uint64_t* a, const uint64_t* b, uint64_t count, uint64_t* out);
 PWMGPU_API void pwmgpu_wx_free(pwmgpu_wx* wx);
+
+/* ---------------------------------------------------------------------- */
+/* Domain decomposition (pwm's wx_dd_ps / wx_dd_pc: include/wx_dd_ps.hpp:  */
+/* 43-120, include/construction/merge.hpp:192-465)                        */
+/* ---------------------------------------------------------------------- */
+/* Structures built independently from consecutive slices of one text merge
+ * into the structures of the whole text, bit for bit those of one build:
+ * level l of the result is, block by block in the level's order (prefix
+ * order for the tree, bit-reversed prefix order for the matrix), the
+ * concatenation of the shards' runs of that block.  shards[i] holds slice i
+ * (created with PWMGPU_KEEP_HISTOGRAM and built), all of out's word width and
+ * levels and holding the structures out holds; out's size is the sum of
+ * theirs; the matrix zeros are summed.  Plain structures of at most 16
+ * levels.  Builds out's rank/select support when out has it. */
+PWMGPU_API pwmgpu_status pwmgpu_wx_merge(pwmgpu_ctx* ctx, const pwmgpu_wx* const* shards, uint32_t count,
+                                         pwmgpu_wx* out);
+/* pwmgpu_wx_build of a device text as `shards` slices built one by one and
+ * merged (pwm's slices: size/shards symbols, one more for each of the first
+ * size%shards). */
+PWMGPU_API pwmgpu_status pwmgpu_wx_build_sharded(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text,
+                                                 uint32_t shards);
+/* pwm's copy_bits (merge.hpp:19-190) on device arrays of 64-bit words: len
+ * bits from bit src_off of d_src to bit dst_off of d_dst (bit i is bit
+ * 63 - i%64 of word i/64); destination words the range covers whole are
+ * stored, the partial words at its ends OR-ed.  Asynchronous on cuda_stream
+ * (NULL: the default stream). */
+PWMGPU_API pwmgpu_status pwmgpu_copy_bits(uint64_t* d_dst, const uint64_t* d_src, uint64_t dst_off, uint64_t src_off,
+                                          uint64_t len, void* cuda_stream);
 
 /* ---------------------------------------------------------------------- */
 /* Serving: continuous batching over device-resident structures            */

@@ -117,6 +117,14 @@ class Oracle:
         L.orc_huff_codes.restype = ctypes.c_uint64
         L.orc_huff_naive.argtypes = [_vp, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int, _u64p, _u64p,
                                      ctypes.c_uint32, _u64p, _u64p, _u64p]
+        L.orc_copy_bits_u8.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]
+        L.orc_copy_bits_u64.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]
+
+    def copy_bits(self, dst, src, dst_off, src_off, length):
+        """pwm's copy_bits (merge.hpp:19-190) on numpy arrays of uint8 or
+        uint64 words; dst is updated in place."""
+        f = self.L.orc_copy_bits_u8 if dst.dtype == np.uint8 else self.L.orc_copy_bits_u64
+        f(dst.ctypes.data, src.ctypes.data, int(dst_off), int(src_off), int(length))
 
     # -- construction ------------------------------------------------------
     def build(self, text, levels, is_tree, variant="ps", threads=0):
@@ -275,6 +283,13 @@ class Reference:
         L.pwmref_select.argtypes = [ctypes.c_int, _u64p, ctypes.c_uint64, _u64p, ctypes.c_uint64, _u64p]
         L.pwmref_queries.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
                                      _u64p, _u64p, ctypes.c_uint64, _u64p]
+        L.pwmref_copy_bits_u8.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]
+        L.pwmref_copy_bits_u64.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]
+
+    def copy_bits(self, dst, src, dst_off, src_off, length):
+        """pwm's copy_bits on numpy arrays of uint8 or uint64 words (dst in place)."""
+        f = self.L.pwmref_copy_bits_u8 if dst.dtype == np.uint8 else self.L.pwmref_copy_bits_u64
+        f(dst.ctypes.data, src.ctypes.data, int(dst_off), int(src_off), int(length))
 
     def fixtures(self):
         out = []

@@ -835,6 +835,33 @@ void orc_decode(void* qp, uint64_t* out) {
 
 }  // extern "C"
 
+// pwm's copy_bits (include/construction/merge.hpp:19-190), the bit-range copy
+// of the domain-decomposition merge: `len` bits from bit src_off of src to
+// bit dst_off of dst (bit i of a word array is bit BITS-1-i%BITS of word
+// i/BITS).  The destination words the range covers whole are stored; the
+// partial words at its ends are OR-ed bit by bit.
+template <typename W>
+static void orc_copy_bits_t(W* dst, const W* src, uint64_t dst_off, uint64_t src_off, uint64_t len) {
+  constexpr uint64_t B = sizeof(W) * 8;
+  auto bit = [&](uint64_t i) -> W { return W((src[i / B] >> (B - 1 - i % B)) & 1u); };
+  const uint64_t end = dst_off + len;
+  while (dst_off % B != 0 && dst_off != end) {
+    dst[dst_off / B] |= W(bit(src_off++) << (B - 1 - dst_off % B));
+    ++dst_off;
+  }
+  while (end - dst_off >= B) {
+    W v = 0;
+    for (uint64_t k = 0; k < B; ++k) v = W((v << 1) | bit(src_off + k));
+    dst[dst_off / B] = v;
+    dst_off += B;
+    src_off += B;
+  }
+  while (dst_off != end) {
+    dst[dst_off / B] |= W(bit(src_off++) << (B - 1 - dst_off % B));
+    ++dst_off;
+  }
+}
+
 extern "C" {
 
 // CPU-baseline step (bench.py's cpu_baseline leg and `--impl reference` when
@@ -842,6 +869,13 @@ extern "C" {
 // the parallel prefix-counting restatement (orc_wx_ppc), then rank/select
 // support (bin_rank_popcnt + both bin_select_popcnt) for every level of both,
 // levels in parallel.  wm/wt hold levels*stride words each.
+void orc_copy_bits_u8(uint8_t* dst, const uint8_t* src, uint64_t dst_off, uint64_t src_off, uint64_t len) {
+  orc_copy_bits_t(dst, src, dst_off, src_off, len);
+}
+void orc_copy_bits_u64(uint64_t* dst, const uint64_t* src, uint64_t dst_off, uint64_t src_off, uint64_t len) {
+  orc_copy_bits_t(dst, src, dst_off, src_off, len);
+}
+
 int orc_cpu_step(const void* text, uint64_t n, uint32_t w, uint32_t levels, int threads, uint64_t* wm,
                  uint64_t* wt, const uint64_t* offsets, uint64_t* zeros) {
   if (threads <= 0) threads = omp_get_max_threads();

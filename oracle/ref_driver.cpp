@@ -199,4 +199,14 @@ uint64_t pwmref_queries(int is_tree, const uint8_t* text, uint64_t n, uint64_t l
   return count;
 }
 
+// pwm's copy_bits (include/construction/merge.hpp:19-190), the bit-range copy
+// of its domain-decomposition merge, on byte words (as test/bit_copy.cpp
+// calls it) and on 64-bit words (as merge_bit_vectors calls it).
+void pwmref_copy_bits_u8(uint8_t* dst, const uint8_t* src, uint64_t dst_off, uint64_t src_off, uint64_t len) {
+  copy_bits<uint8_t>(dst, src, dst_off, src_off, len);
+}
+void pwmref_copy_bits_u64(uint64_t* dst, const uint64_t* src, uint64_t dst_off, uint64_t src_off, uint64_t len) {
+  copy_bits<uint64_t>(dst, src, dst_off, src_off, len);
+}
+
 }  // extern "C"

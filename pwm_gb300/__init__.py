@@ -24,7 +24,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import (GEN_DNA4, GEN_MIX16, GEN_UNIFORM, GEN_ZIPF256, MATRIX, Q_ACCESS, Q_RANK, Q_SELECT,
+from ._lib import (GEN_DNA4, GEN_MIX16, GEN_UNIFORM, GEN_ZIPF256, KEEP_HISTOGRAM, MATRIX, Q_ACCESS, Q_RANK, Q_SELECT,
                    RANK_SELECT, TREE, PwmGpuError)
 
 __all__ = ["Context", "default_context", "wavelet_structure", "bit_vectors", "algorithm_list",
@@ -371,9 +371,11 @@ class DeviceStructure:
     """A device-resident build (pwmgpu_wx): matrix and/or tree, optional
     rank/select support, batched queries."""
 
-    def __init__(self, size, word_width, levels, matrix=True, tree=False, rank_select=False, context=None):
+    def __init__(self, size, word_width, levels, matrix=True, tree=False, rank_select=False, context=None,
+                 keep_histogram=False):
         self.ctx = context or default_context()
-        flags = (MATRIX if matrix else 0) | (TREE if tree else 0) | (RANK_SELECT if rank_select else 0)
+        flags = (MATRIX if matrix else 0) | (TREE if tree else 0) | (RANK_SELECT if rank_select else 0) | \
+            (KEEP_HISTOGRAM if keep_histogram else 0)
         h = ctypes.c_void_p()
         self.ctx.check(self.ctx.lib.pwmgpu_wx_create(self.ctx.h, int(size), int(word_width), int(levels), flags,
                                                      ctypes.byref(h)))
@@ -384,6 +386,17 @@ class DeviceStructure:
     def build(self, d_text_ptr):
         """Builds from a device pointer (e.g. a torch tensor's data_ptr())."""
         self.ctx.check(self.ctx.lib.pwmgpu_wx_build(self.ctx.h, self.h, ctypes.c_void_p(int(d_text_ptr))))
+
+    def build_sharded(self, d_text_ptr, shards):
+        """Builds from a device text as `shards` slices merged (pwm's wx_dd_*)."""
+        self.ctx.check(self.ctx.lib.pwmgpu_wx_build_sharded(self.ctx.h, self.h, ctypes.c_void_p(int(d_text_ptr)),
+                                                            int(shards)))
+
+    def merge(self, shards):
+        """This structure from built shards (DeviceStructures of consecutive
+        slices, created with keep_histogram=True)."""
+        arr = (ctypes.c_void_p * max(len(shards), 1))(*[s.h.value if hasattr(s.h, "value") else s.h for s in shards])
+        self.ctx.check(self.ctx.lib.pwmgpu_wx_merge(self.ctx.h, arr, len(shards), self.h))
 
     def build_host(self, text_ptr):
         """Builds from a host pointer (pinned memory is uploaded in pieces)."""
@@ -620,3 +633,16 @@ def generate(dist, seed, n, word_width, param=0, device_ptr=None, context=None):
     ctx.check(lib.pwmgpu_generate(ctx.h, int(dist), int(seed), int(param), int(n), int(word_width),
                                   ctypes.c_void_p(int(device_ptr)), 1))
     return None
+
+
+def copy_bits(d_dst_ptr, d_src_ptr, dst_off, src_off, length, stream=None):
+    """pwm's copy_bits (merge.hpp:19-190) on device arrays of 64-bit words:
+    `length` bits from bit src_off of the source to bit dst_off of the
+    destination; whole destination words are stored, partial ones OR-ed."""
+    st = _lib.load().pwmgpu_copy_bits(ctypes.c_void_p(int(d_dst_ptr)), ctypes.c_void_p(int(d_src_ptr)), int(dst_off),
+                                      int(src_off), int(length), ctypes.c_void_p(int(stream or 0)))
+    if st != 0:
+        raise PwmGpuError(st, "pwmgpu_copy_bits failed")
+
+
+__all__ += ["copy_bits"]

@@ -19,7 +19,7 @@ cstr = ctypes.c_char_p
 STATUS = {0: "PWMGPU_OK", 1: "PWMGPU_ERR_ARG", 2: "PWMGPU_ERR_OOM", 3: "PWMGPU_ERR_CUDA",
           4: "PWMGPU_ERR_TIMEOUT", 5: "PWMGPU_ERR_SYMBOL", 6: "PWMGPU_ERR_NO_DEVICE", 7: "PWMGPU_ERR_BUSY"}
 
-MATRIX, TREE, RANK_SELECT, HUFFMAN = 0x1, 0x2, 0x4, 0x8
+MATRIX, TREE, RANK_SELECT, HUFFMAN, KEEP_HISTOGRAM = 0x1, 0x2, 0x4, 0x8, 0x10
 Q_ACCESS, Q_RANK, Q_SELECT = 0, 1, 2
 GEN_UNIFORM, GEN_DNA4, GEN_ZIPF256, GEN_MIX16 = 0, 1, 2, 3
 
@@ -60,6 +60,9 @@ SIGNATURES = {
     "pwmgpu_ctx_profile_read": (i32, [vp, ctypes.c_char_p, u64]),
     "pwmgpu_wx_build_host": (i32, [vp, vp, vp]),
     "pwmgpu_wx_compute_host": (i32, [vp, vp, vp, u64p, u64p, u64p]),
+    "pwmgpu_wx_merge": (i32, [vp, ctypes.POINTER(vp), u32, vp]),
+    "pwmgpu_wx_build_sharded": (i32, [vp, vp, vp, u32]),
+    "pwmgpu_copy_bits": (i32, [vp, vp, u64, u64, u64, vp]),
     "pwmgpu_ctx_set_upload_piece_bytes": (i32, [vp, u64]),
     "pwmgpu_compute": (i32, [vp, vp, u64, u32, u32, i32, u64p, u64p]),
     "pwmgpu_huffman_codes": (i32, [vp, vp, u64, u32, i32, u64p, u64p, u64, u64p, u64p, u32p]),

@@ -74,6 +74,7 @@ struct pwmgpu_ctx {
   bool async_alloc = false;  // stream-ordered allocations on `stream`
   uint64_t scratch_bytes = 0;
   pwmgpu_wx* compute_cache = nullptr;  // reused by pwmgpu_compute for equal shapes
+  std::vector<std::unique_ptr<pwmgpu_wx>> shard_cache;  // reused by pwmgpu_wx_build_sharded
   // CUDA-event timing of every launch group while profiling is on
   bool profiling = false;
   std::vector<ProfRecord> prof;
@@ -133,6 +134,17 @@ struct pwmgpu_ctx {
   // events that order them against the main stream; every call that uses
   // them waits for them before it returns, so the events are reused.
   cudaStream_t up = nullptr, down = nullptr;
+  // A stream for rank/select of the levels the first passes complete, which
+  // runs beside the last pass (integer-bound, while rank/select is
+  // memory-bound); created on first use.
+  cudaStream_t side = nullptr;
+  cudaEvent_t side_go = nullptr, side_done = nullptr;
+  void side_init() {
+    if (side) return;
+    CUDA_TRY(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&side_go, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&side_done, cudaEventDisableTiming));
+  }
   // recorded after the histogram of a build reaches the host
   cudaEvent_t hist_ready = nullptr;
   cudaEvent_t hist_event() {
@@ -222,12 +234,15 @@ struct pwmgpu_wx {
   bool huffman = false;
   Structure wm, wt;
   bool wm_internal = false;  // matrix built only as the source of the tree
+  bool keep_hist = false;    // PWMGPU_KEEP_HISTOGRAM: the leaf histogram of the last build, for merges
+  std::vector<uint64_t> hist;
   ~pwmgpu_wx() { wm.release(); wt.release(); }
 };
 
 pwmgpu_ctx::~pwmgpu_ctx() {
   cudaSetDevice(device);
   delete compute_cache;
+  shard_cache.clear();  // structures free on the context's stream: before it goes
   for (auto& r : prof) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto e : event_pool) cudaEventDestroy(e);
   if (async_alloc && stream) cudaStreamSynchronize(stream);
@@ -239,11 +254,13 @@ pwmgpu_ctx::~pwmgpu_ctx() {
   if (async_alloc && stream) cudaStreamSynchronize(stream);
   if (d_status) cudaFree(d_status);
   if (pinned) cudaFreeHost(pinned);
-  for (cudaStream_t t : {up, down})
+  for (cudaStream_t t : {up, down, side})
     if (t) {
       cudaStreamSynchronize(t);
       cudaStreamDestroy(t);
     }
+  if (side_go) cudaEventDestroy(side_go);
+  if (side_done) cudaEventDestroy(side_done);
   for (auto e : xev) cudaEventDestroy(e);
   if (hist_ready) cudaEventDestroy(hist_ready);
   if (own_stream && stream) cudaStreamDestroy(stream);
@@ -383,25 +400,38 @@ void alloc_structure(Structure& s, const std::vector<uint64_t>& level_bits, uint
 // whose level 0 is the same bit vector: the tree's blocks of level 0 are a
 // copy of the matrix's.  The kernels write every entry that is read (l0 is
 // cleared by the scan kernel), so nothing is zeroed first.
-void build_rank_select(pwmgpu_ctx* ctx, Structure* wm, Structure* wt = nullptr, bool share_level0 = false) {
+//
+// Levels [lo, hi) only, on `stream` (default: the context's) with scratch
+// buffers named after `tag` (so that two groups can run at once); only the
+// context's stream is profiled.
+void build_rank_select(pwmgpu_ctx* ctx, Structure* wm, Structure* wt = nullptr, bool share_level0 = false,
+                       uint32_t lo = 0, uint32_t hi = ~0u, cudaStream_t stream = nullptr, const char* tag = "") {
   std::vector<RankSelectLevel> lv;
-  if (wm && wm->rs) lv.insert(lv.end(), wm->rs_levels.begin(), wm->rs_levels.end());
-  const bool copy0 = share_level0 && wm && wm->rs && wm->levels && wt && wt->rs && wt->levels;
-  if (wt && wt->rs) lv.insert(lv.end(), wt->rs_levels.begin() + (copy0 ? 1 : 0), wt->rs_levels.end());
-  if (lv.empty()) return;
-  cudaStream_t s = ctx->stream;
-  auto* d_lv = static_cast<RankSelectLevel*>(ctx->grow("rs_levels", lv.size() * sizeof(RankSelectLevel)));
-  CUDA_TRY(cudaMemcpyAsync(d_lv, lv.data(), lv.size() * sizeof(RankSelectLevel), cudaMemcpyHostToDevice, s));
-  uint64_t max_real = 0, bytes = 0;
-  for (auto& r : lv) {
-    max_real = std::max<uint64_t>(max_real, (r.nwords + 31) / 32);
-    bytes += r.nwords * 8 + (r.nwords / 32 + 1) * 8;
-  }
-  const uint64_t stride = max_real + (max_real + 255) / 256 + 1;
-  uint32_t* tmp = static_cast<uint32_t*>(ctx->grow("rs_tmp", std::max<uint64_t>(stride * lv.size() * 4, 256)));
-  {
-    ProfScope ps(ctx, "rank_select", bytes);
-    launch_rank_select(lv.data(), uint32_t(lv.size()), d_lv, tmp, stride, s, &ctx->launches);
+  auto add = [&](const Structure* st, uint32_t from) {
+    for (uint32_t l = std::max(lo, from); l < std::min(hi, st->levels); ++l) lv.push_back(st->rs_levels[l]);
+  };
+  if (wm && wm->rs) add(wm, 0);
+  const bool copy0 = share_level0 && lo == 0 && hi > 0 && wm && wm->rs && wm->levels && wt && wt->rs && wt->levels;
+  if (wt && wt->rs) add(wt, copy0 ? 1 : 0);
+  if (lv.empty() && !copy0) return;
+  cudaStream_t s = stream ? stream : ctx->stream;
+  const std::string t(tag);
+  if (!lv.empty()) {
+    auto* d_lv = static_cast<RankSelectLevel*>(ctx->grow("rs_levels" + t, lv.size() * sizeof(RankSelectLevel)));
+    CUDA_TRY(cudaMemcpyAsync(d_lv, lv.data(), lv.size() * sizeof(RankSelectLevel), cudaMemcpyHostToDevice, s));
+    uint64_t max_real = 0, bytes = 0;
+    for (auto& r : lv) {
+      max_real = std::max<uint64_t>(max_real, (r.nwords + 31) / 32);
+      bytes += r.nwords * 8 + (r.nwords / 32 + 1) * 8;
+    }
+    const uint64_t stride = max_real + (max_real + 255) / 256 + 1;
+    uint32_t* tmp = static_cast<uint32_t*>(ctx->grow("rs_tmp" + t, std::max<uint64_t>(stride * lv.size() * 4, 256)));
+    if (s == ctx->stream) {
+      ProfScope ps(ctx, "rank_select", bytes);
+      launch_rank_select(lv.data(), uint32_t(lv.size()), d_lv, tmp, stride, s, &ctx->launches);
+    } else {
+      launch_rank_select(lv.data(), uint32_t(lv.size()), d_lv, tmp, stride, s, &ctx->launches);
+    }
   }
   if (copy0) {  // l0, l12, samples and meta of level 0 lie in this order in both structures
     const RankSelectLevel &a = wm->rs_levels[0], &b = wt->rs_levels[0];
@@ -713,7 +743,11 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   cudaStream_t s = ctx->stream;
   const uint32_t L = wx->levels;
   const uint64_t n = wx->n;
-  if (n == 0) return;
+  if (n == 0) {
+    if (wx->keep_hist) wx->hist.assign(size_t(1) << L, 0);
+    wx->wm.zeros.assign(L, 0);
+    return;
+  }
   const bool pinned_in = io && io->text && host_pinned(io->text);
   uint64_t* host_out[2] = {io ? io->wm : nullptr, io ? io->wt : nullptr};
   bool any_out = false, all_pinned = true;
@@ -869,6 +903,7 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     CUDA_TRY(cudaStreamSynchronize(s));  // the first pass may still read the text
     throw_status(*h_status);
   }
+  if (wx->keep_hist) wx->hist.assign(h_hist, h_hist + bins);
   LevelTables tabs;
   std::vector<PassPlan> plan;
   std::vector<TilePassHost> tile_passes;
@@ -909,15 +944,33 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
       sent[st] = std::max(sent[st], w1);
     }
   };
+  // Rank/select: the levels of all passes but the last (when no tree level
+  // waits for the regroup) on the side stream as soon as the last pass
+  // starts, the others after it.
+  Structure* rs_wm = wx->wm.rs && !wx->wm_internal ? &wx->wm : nullptr;
+  Structure* rs_wt = want_tree && wx->wt.rs ? &wx->wt : nullptr;
+  const bool early_rs = tile_engine && (rs_wm || rs_wt) && tile_passes.size() >= 2 && regroup.empty();
+  const uint32_t late_level = early_rs ? tile_passes.back().level : 0;
+  auto rank_select_early = [&]() {
+    ctx->side_init();
+    CUDA_TRY(cudaEventRecord(ctx->side_go, s));
+    CUDA_TRY(cudaStreamWaitEvent(ctx->side, ctx->side_go, 0));
+    build_rank_select(ctx, rs_wm, rs_wt, true, 0, late_level, ctx->side, "_side");
+    CUDA_TRY(cudaEventRecord(ctx->side_done, ctx->side));
+  };
+  auto hook = [&](size_t pi) {
+    if (stream_out) after_pass(pi);
+    if (early_rs && pi + 2 == tile_passes.size()) rank_select_early();
+  };
   if (tile_engine) {
-    if (from == 1 && stream_out) after_pass(0);
+    if (from == 1) hook(0);
     run_tile_passes(ctx, next_in, wx->width, L, tile_passes, regroup, tabs, wx->wm, want_tree ? &wx->wt : nullptr,
-                    first.blockpre ? &first : nullptr,
-                    stream_out ? std::function<void(size_t)>(after_pass) : std::function<void(size_t)>(), from);
+                    first.blockpre ? &first : nullptr, std::function<void(size_t)>(hook), from);
   }
   else
     run_passes(ctx, d_text, wx->width, wx->width, false, L, plan, tabs, wx->wm, want_tree ? &wx->wt : nullptr);
-  build_rank_select(ctx, wx->wm.rs && !wx->wm_internal ? &wx->wm : nullptr, want_tree ? &wx->wt : nullptr, true);
+  build_rank_select(ctx, rs_wm, rs_wt, true, late_level);
+  if (early_rs) CUDA_TRY(cudaStreamWaitEvent(s, ctx->side_done, 0));
   CUDA_TRY(cudaGetLastError());
   if (any_out) {
     for (int st = 0; st < 2; ++st) {
@@ -1357,6 +1410,97 @@ struct BatchGen {
 // ===========================================================================
 // extern "C"
 // ===========================================================================
+namespace {
+
+std::unique_ptr<pwmgpu_wx> make_wx(pwmgpu_ctx* ctx, uint64_t size, uint32_t word_width, uint32_t levels,
+                                   uint32_t shape_flags) {
+  auto wx = std::make_unique<pwmgpu_wx>();
+  wx->ctx = ctx;
+  wx->n = size;
+  wx->width = word_width;
+  wx->levels = levels;
+  wx->flags = shape_flags;
+  wx->keep_hist = shape_flags & PWMGPU_KEEP_HISTOGRAM;
+  const bool rs = shape_flags & PWMGPU_RANK_SELECT;
+  std::vector<uint64_t> bits(levels, size);
+  cudaStream_t as = ctx->async_alloc ? ctx->stream : nullptr;
+  alloc_structure(wx->wm, bits, size, false, false, rs && (shape_flags & PWMGPU_MATRIX), as);
+  wx->wm_internal = !(shape_flags & PWMGPU_MATRIX);
+  if (shape_flags & PWMGPU_TREE) alloc_structure(wx->wt, bits, size, true, false, rs, as);
+  return wx;
+}
+
+constexpr uint32_t kMergeMaxLevels = 16;
+
+// pwm's merge_bit_vectors (merge.hpp:192-465) on the device: per level the
+// runs of every block and shard in the level's order, gathered word by word.
+void merge_shards(pwmgpu_ctx* ctx, const std::vector<const pwmgpu_wx*>& sh, pwmgpu_wx* out) {
+  const uint32_t L = out->levels, p = uint32_t(sh.size());
+  if (p == 0) throw Fail{PWMGPU_ERR_ARG, "no shards"};
+  if (out->huffman) throw Fail{PWMGPU_ERR_ARG, "merging takes plain structures"};
+  if (L > kMergeMaxLevels) throw Fail{PWMGPU_ERR_ARG, "merging takes structures of at most 16 levels"};
+  uint64_t total = 0;
+  for (const pwmgpu_wx* x : sh) {
+    if (!x || x->huffman) throw Fail{PWMGPU_ERR_ARG, "merging takes plain structures"};
+    if (x->width != out->width || x->levels != L) throw Fail{PWMGPU_ERR_ARG, "shards of another width or level count"};
+    if (x->hist.size() != (size_t(1) << L))
+      throw Fail{PWMGPU_ERR_ARG, "a shard without its histogram (create with PWMGPU_KEEP_HISTOGRAM and build it)"};
+    if (out->wt.present && !x->wt.present) throw Fail{PWMGPU_ERR_ARG, "a shard without the tree"};
+    total += x->n;
+  }
+  if (total != out->n) throw Fail{PWMGPU_ERR_ARG, "the shards' sizes do not add up to out's"};
+  cudaStream_t st = ctx->stream;
+  CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, 4, st));
+  std::vector<std::vector<std::vector<uint64_t>>> cnt(p);
+  for (uint32_t s = 0; s < p; ++s) cnt[s] = fold_prefix_counts(sh[s]->hist.data(), L);
+  for (int which = 0; which < 2; ++which) {
+    Structure& O = which ? out->wt : out->wm;
+    if (!O.present || out->n == 0) continue;
+    std::vector<MergeSeg> segs;
+    std::vector<size_t> seg_off(L + 1, 0);
+    for (uint32_t l = 0; l < L; ++l) {
+      seg_off[l] = segs.size();
+      std::vector<uint64_t> rd(p, 0);
+      uint64_t dst = 0;
+      for (uint64_t b = 0; b < (uint64_t(1) << l); ++b) {
+        const uint64_t pfx = which ? b : rev_bits_host(b, l);  // the tree in prefix order, the matrix bit-reversed
+        for (uint32_t s = 0; s < p; ++s) {
+          const uint64_t len = cnt[s][l][pfx];
+          if (!len) continue;
+          const Structure& S = which ? sh[s]->wt : sh[s]->wm;
+          segs.push_back({dst, rd[s], S.d_words + S.offs[l]});
+          dst += len;
+          rd[s] += len;
+        }
+      }
+    }
+    seg_off[L] = segs.size();
+    auto* d_segs = static_cast<MergeSeg*>(ctx->grow("merge_segs", std::max<size_t>(segs.size(), 1) * sizeof(MergeSeg)));
+    // (a copy from a pageable host vector returns once the data is staged)
+    CUDA_TRY(cudaMemcpyAsync(d_segs, segs.data(), segs.size() * sizeof(MergeSeg), cudaMemcpyHostToDevice, st));
+    for (uint32_t l = 0; l < L; ++l) {
+      ProfScope ps(ctx, "merge", 2 * words_for(O.bits[l]) * 8);
+      launch_merge_gather(d_segs + seg_off[l], seg_off[l + 1] - seg_off[l], O.d_words + O.offs[l], O.bits[l],
+                          ctx->d_status, st, &ctx->launches);
+    }
+    CUDA_TRY(cudaGetLastError());
+  }
+  out->wm.zeros.assign(L, 0);
+  for (const pwmgpu_wx* x : sh)
+    for (uint32_t l = 0; l < L && l < x->wm.zeros.size(); ++l) out->wm.zeros[l] += x->wm.zeros[l];
+  CUDA_TRY(cudaMemcpyAsync(out->wm.d_zeros, out->wm.zeros.data(), L * 8, cudaMemcpyHostToDevice, st));
+  if (out->keep_hist) {
+    out->hist.assign(size_t(1) << L, 0);
+    for (const pwmgpu_wx* x : sh)
+      for (size_t b = 0; b < out->hist.size(); ++b) out->hist[b] += x->hist[b];
+  }
+  build_rank_select(ctx, out->wm.rs && !out->wm_internal ? &out->wm : nullptr, out->wt.present ? &out->wt : nullptr,
+                    true);
+  check_device_status(ctx);  // synchronises: the shards may be freed after this
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* pwmgpu_status_string(pwmgpu_status s) {
@@ -1494,6 +1638,54 @@ pwmgpu_status pwmgpu_ctx_profile_read(pwmgpu_ctx* ctx, char* buf, uint64_t cap) 
 }
 
 // ---- device-resident structures --------------------------------------------
+
+pwmgpu_status pwmgpu_wx_merge(pwmgpu_ctx* ctx, const pwmgpu_wx* const* shards, uint32_t count, pwmgpu_wx* out) {
+  if (!ctx || !out || (count && !shards)) return PWMGPU_ERR_ARG;
+  return guarded(ctx, [&]() {
+    merge_shards(ctx, std::vector<const pwmgpu_wx*>(shards, shards + count), out);
+    return PWMGPU_OK;
+  });
+}
+
+pwmgpu_status pwmgpu_wx_build_sharded(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, uint32_t shards) {
+  if (!ctx || !wx || shards == 0 || (!d_text && wx->n)) return PWMGPU_ERR_ARG;
+  return guarded(ctx, [&]() {
+    if (shards == 1 || wx->n == 0 || wx->huffman) {
+      build_plain(ctx, wx, d_text);
+      return PWMGPU_OK;
+    }
+    const uint32_t shape = (wx->wm_internal ? 0u : PWMGPU_MATRIX) | (wx->wt.present ? PWMGPU_TREE : 0u) |
+                           PWMGPU_KEEP_HISTOGRAM;
+    // the shard structures stay in the context for the next build of this shape
+    auto& parts = ctx->shard_cache;
+    std::vector<const pwmgpu_wx*> view;
+    const uint64_t n = wx->n, base = n / shards, extra = n % shards;
+    if (parts.size() > shards) parts.resize(shards);
+    for (uint32_t s = 0; s < shards; ++s) {  // pwm's slices (wx_dd_ps.hpp:66-83)
+      const uint64_t size = base + (s < extra ? 1 : 0), off = s * base + std::min<uint64_t>(s, extra);
+      if (s == parts.size()) parts.emplace_back();
+      auto& part = parts[s];
+      if (!part || part->n != size || part->width != wx->width || part->levels != wx->levels || part->flags != shape)
+        part = make_wx(ctx, size, wx->width, wx->levels, shape);
+      build_plain(ctx, part.get(), static_cast<const unsigned char*>(d_text) + off * wx->width);
+      view.push_back(part.get());
+    }
+    merge_shards(ctx, view, wx);
+    return PWMGPU_OK;
+  });
+}
+
+pwmgpu_status pwmgpu_copy_bits(uint64_t* d_dst, const uint64_t* d_src, uint64_t dst_off, uint64_t src_off,
+                               uint64_t len, void* cuda_stream) {
+  if (len && (!d_dst || !d_src)) return PWMGPU_ERR_ARG;
+  launch_copy_bits(d_dst, d_src, dst_off, src_off, len, static_cast<cudaStream_t>(cuda_stream));
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) return PWMGPU_OK;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver || e == cudaErrorNoKernelImageForDevice)
+    return PWMGPU_ERR_NO_DEVICE;
+  return PWMGPU_ERR_CUDA;
+}
+
 pwmgpu_status pwmgpu_wx_create(pwmgpu_ctx* ctx, uint64_t size, uint32_t word_width, uint32_t levels,
                                uint32_t shape_flags, pwmgpu_wx** out) {
   if (!ctx || !out) return PWMGPU_ERR_ARG;
@@ -1503,19 +1695,7 @@ pwmgpu_status pwmgpu_wx_create(pwmgpu_ctx* ctx, uint64_t size, uint32_t word_wid
     if (!(shape_flags & (PWMGPU_MATRIX | PWMGPU_TREE))) throw Fail{PWMGPU_ERR_ARG, "need PWMGPU_MATRIX or PWMGPU_TREE"};
     if ((shape_flags & PWMGPU_RANK_SELECT) && size >= 4294967295ull - 64)
       throw Fail{PWMGPU_ERR_ARG, "rank/select support needs levels below 2^32-1 bits"};
-    auto wx = std::make_unique<pwmgpu_wx>();
-    wx->ctx = ctx;
-    wx->n = size;
-    wx->width = word_width;
-    wx->levels = levels;
-    wx->flags = shape_flags;
-    const bool rs = shape_flags & PWMGPU_RANK_SELECT;
-    std::vector<uint64_t> bits(levels, size);
-    cudaStream_t as = ctx->async_alloc ? ctx->stream : nullptr;
-    alloc_structure(wx->wm, bits, size, false, false, rs && (shape_flags & PWMGPU_MATRIX), as);
-    wx->wm_internal = !(shape_flags & PWMGPU_MATRIX);
-    if (shape_flags & PWMGPU_TREE) alloc_structure(wx->wt, bits, size, true, false, rs, as);
-    *out = wx.release();
+    *out = make_wx(ctx, size, word_width, levels, shape_flags).release();
     return PWMGPU_OK;
   });
 }

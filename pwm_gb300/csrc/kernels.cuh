@@ -39,6 +39,23 @@ void launch_tile_block_scan(unsigned long long* blocksum, uint32_t nblocks, uint
                             uint32_t levels, uint32_t K, bool out, bool tree, uint64_t* table, cudaStream_t s,
                             uint64_t* launches);
 
+// ---- merge of shards (merge.cu) -----------------------------------------------
+// A run of one shard's level in the merged level: destination bit `dst`,
+// its first bit `src_bit` in the shard's level `src`.  Sorted by dst; no
+// empty runs.
+struct MergeSeg {
+  uint64_t dst;
+  uint64_t src_bit;
+  const uint64_t* src;
+};
+// pwm's copy_bits (merge.hpp:19-190) on 64-bit words: whole destination
+// words stored, the partial words at the ends OR-ed.
+void launch_copy_bits(uint64_t* dst, const uint64_t* src, uint64_t dst_off, uint64_t src_off, uint64_t len,
+                      cudaStream_t s);
+// One merged level of nbits bits.
+void launch_merge_gather(const MergeSeg* segs, uint64_t nseg, uint64_t* dst, uint64_t nbits, uint32_t* status,
+                         cudaStream_t s, uint64_t* launches);
+
 // ---- split passes -----------------------------------------------------------
 // Geometry of the split pass for a key width: tile size in elements.
 uint32_t split_tile_elems(uint32_t key_bytes);
