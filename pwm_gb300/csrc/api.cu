@@ -1002,24 +1002,51 @@ HuffCodes build_huffman_codes(const std::vector<std::pair<uint64_t, uint64_t>>& 
   const uint64_t nsym = max_symbol + 1;
   std::vector<uint64_t> freq(nsym, 0);
   for (const auto& e : entries) freq[e.first] = e.second;
+  // pwm merges the two least frequent items of a std::priority_queue<Item,
+  // std::vector<Item>, std::greater<Item>> (ordered by occurrences only) and
+  // lengthens the codes of all symbols of the merged item, so a code length
+  // is the depth of the symbol's leaf in the tree of merges.  The same heap
+  // operations (push: push_back + push_heap, pop: pop_heap + pop_back) on
+  // (occurrences, node) pairs break ties identically; the depths come from
+  // one pass over the merge tree, parents before children.
   struct Item {
     uint64_t occ;
-    std::vector<uint64_t> syms;
+    uint32_t node;
     bool operator>(const Item& o) const { return occ > o.occ; }
   };
-  std::priority_queue<Item, std::vector<Item>, std::greater<Item>> pq;
+  std::vector<Item> heap;
+  const std::greater<Item> comp;
+  auto push = [&](Item it) {
+    heap.push_back(it);
+    std::push_heap(heap.begin(), heap.end(), comp);
+  };
+  auto pop = [&]() {
+    std::pop_heap(heap.begin(), heap.end(), comp);
+    const Item it = heap.back();
+    heap.pop_back();
+    return it;
+  };
   h.len.assign(nsym, 0);
   h.word.assign(nsym, 0);
-  for (const auto& e : entries) pq.emplace(Item{e.second, std::vector<uint64_t>{e.first}});
-  if (pq.size() == 1) ++h.len[pq.top().syms.front()];
-  while (pq.size() > 1) {
-    Item a = pq.top();
-    pq.pop();
-    Item b = pq.top();
-    pq.pop();
-    std::move(b.syms.begin(), b.syms.end(), std::back_inserter(a.syms));
-    for (uint64_t c : a.syms) ++h.len[c];
-    pq.emplace(Item{a.occ + b.occ, a.syms});
+  const size_t leaves = entries.size();
+  std::vector<uint32_t> child(2 * leaves, 0);  // node leaves + i: children of merge i at 2i, 2i + 1
+  heap.reserve(leaves);
+  for (size_t i = 0; i < leaves; ++i) push(Item{entries[i].second, uint32_t(i)});
+  if (heap.size() == 1) ++h.len[entries[0].first];
+  uint32_t merges = 0;
+  while (heap.size() > 1) {
+    const Item a = pop();
+    const Item b = pop();
+    child[2 * merges] = a.node;
+    child[2 * merges + 1] = b.node;
+    push(Item{a.occ + b.occ, uint32_t(leaves + merges)});
+    ++merges;
+  }
+  if (merges) {
+    std::vector<uint64_t> depth(leaves + merges, 0);
+    for (uint32_t i = merges; i-- > 0;)  // the last merge is the root
+      for (int k = 0; k < 2; ++k) depth[child[2 * i + k]] = depth[leaves + i] + 1;
+    for (size_t i = 0; i < leaves; ++i) h.len[entries[i].first] = depth[i];
   }
   std::vector<uint64_t> order(nsym);
   std::iota(order.begin(), order.end(), uint64_t(0));
@@ -1103,7 +1130,12 @@ HuffCodes huffman_codes_device(pwmgpu_ctx* ctx, const void* d_text, uint64_t n, 
   auto* d_first = static_cast<unsigned long long*>(ctx->grow("sym_first", nsym * 8));
   CUDA_TRY(cudaMemsetAsync(d_hist, 0, nsym * 8, s));
   CUDA_TRY(cudaMemsetAsync(d_first, 0xFF, nsym * 8, s));
-  launch_symbol_histogram(d_text, n, width, nsym, d_hist, width == 1 ? nullptr : d_first, s, &ctx->launches);
+  CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, 4, s));
+  {
+    ProfScope ps(ctx, "symbol_histogram", n * width);
+    launch_symbol_histogram(d_text, n, width, nsym, d_hist, width == 1 ? nullptr : d_first, ctx->d_status, s,
+                            &ctx->launches);
+  }
   std::vector<uint64_t> count(nsym), first(nsym);
   CUDA_TRY(cudaMemcpyAsync(count.data(), d_hist, nsym * 8, cudaMemcpyDeviceToHost, s));
   CUDA_TRY(cudaMemcpyAsync(first.data(), d_first, nsym * 8, cudaMemcpyDeviceToHost, s));
@@ -1125,10 +1157,15 @@ void build_huffman(pwmgpu_ctx* ctx, const void* d_text, uint64_t n, uint32_t wid
   const uint64_t ncodes = code_len.size();
   // symbol histogram for the weighted codes
   const uint64_t nsym = ncodes;
-  auto* d_hist = static_cast<unsigned long long*>(ctx->grow("sym_hist", std::max<uint64_t>(nsym, 1) * 8));
+  // 8- and 16-bit texts count every value (symbols past the table fail below)
+  const uint64_t bins = std::max<uint64_t>(width <= 2 ? uint64_t(1) << (8 * width) : nsym, std::max<uint64_t>(nsym, 1));
+  auto* d_hist = static_cast<unsigned long long*>(ctx->grow("sym_hist", bins * 8));
   CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, 4, s));
-  CUDA_TRY(cudaMemsetAsync(d_hist, 0, std::max<uint64_t>(nsym, 1) * 8, s));
-  launch_symbol_histogram(d_text, n, width, nsym, d_hist, nullptr, s, &ctx->launches);
+  CUDA_TRY(cudaMemsetAsync(d_hist, 0, bins * 8, s));
+  {
+    ProfScope ps(ctx, "symbol_histogram", n * width);
+    launch_symbol_histogram(d_text, n, width, nsym, d_hist, nullptr, ctx->d_status, s, &ctx->launches);
+  }
   std::vector<uint64_t> count(nsym);
   CUDA_TRY(cudaMemcpyAsync(count.data(), d_hist, nsym * 8, cudaMemcpyDeviceToHost, s));
   CUDA_TRY(cudaStreamSynchronize(s));

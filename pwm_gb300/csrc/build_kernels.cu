@@ -498,6 +498,19 @@ __global__ void huffman_keys_kernel(const T* text, uint64_t n, const uint64_t* c
   }
 }
 
+// First occurrence of every symbol: an atomicMin only where the index is
+// below the value already there, read with a plain (L1-cacheable) load, so
+// that the hot symbols, whose first occurrence the early blocks set, cost
+// neither atomics nor L2 traffic.  A stale cached value is never below the
+// current one (values only decrease), so it costs at most an extra atomic.
+template <typename T>
+__global__ void first_occurrence_kernel(const T* text, uint64_t n, unsigned long long* first) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    unsigned long long* f = &first[uint64_t(text[i])];
+    if (i < *f) atomicMin(f, (unsigned long long)i);
+  }
+}
+
 template <typename T>
 __global__ void symbol_hist_kernel(const T* text, uint64_t n, uint64_t nsym, unsigned long long* hist,
                                    unsigned long long* first) {
@@ -602,12 +615,20 @@ void launch_huffman_keys(const void* text, uint64_t n, uint32_t width, const uin
 }
 
 void launch_symbol_histogram(const void* text, uint64_t n, uint32_t width, uint64_t nsym, unsigned long long* hist,
-                             unsigned long long* first, cudaStream_t s, uint64_t* launches) {
+                             unsigned long long* first, uint32_t* status, cudaStream_t s, uint64_t* launches) {
   if (n == 0) return;
   const int g = grid_for(n, 256);
-  if (width == 1) symbol_hist_kernel<<<g, 256, 0, s>>>(static_cast<const uint8_t*>(text), n, nsym, hist, first);
-  else if (width == 2) symbol_hist_kernel<<<g, 256, 0, s>>>(static_cast<const uint16_t*>(text), n, nsym, hist, first);
-  else symbol_hist_kernel<<<g, 256, 0, s>>>(static_cast<const uint32_t*>(text), n, nsym, hist, first);
+  if (width <= 2) {
+    // every value is a bin: the shared-memory leaf histograms of 8 / 16 levels
+    launch_leaf_histogram(text, n, width, 8 * width, hist, status, s, launches);
+    if (first) {
+      if (width == 1) first_occurrence_kernel<<<g, 256, 0, s>>>(static_cast<const uint8_t*>(text), n, first);
+      else first_occurrence_kernel<<<g, 256, 0, s>>>(static_cast<const uint16_t*>(text), n, first);
+      ++*launches;
+    }
+    return;
+  }
+  symbol_hist_kernel<<<g, 256, 0, s>>>(static_cast<const uint32_t*>(text), n, nsym, hist, first);
   ++*launches;
 }
 

@@ -319,28 +319,34 @@ inline LevelTables build_tables(const std::vector<WeightedCode>& codes, uint32_t
   if (want_tree) {
     t.seg_tree.resize(L);
     t.seg_matrix.resize(L);
+    // codes by their left-aligned code word: at every level the prefixes of
+    // the longer codes then come in prefix order, so no level sorts them
+    std::vector<size_t> by_word;
+    by_word.reserve(codes.size());
+    for (size_t i = 0; i < codes.size(); ++i)
+      if (codes[i].len > 1) by_word.push_back(i);
+    auto aligned = [&](size_t i) { return codes[i].word << (64 - codes[i].len); };
+    std::sort(by_word.begin(), by_word.end(), [&](size_t a, size_t b) { return aligned(a) < aligned(b); });
+    std::vector<std::pair<uint64_t, uint64_t>> g;     // (prefix, count) in natural prefix order
+    std::vector<std::pair<uint64_t, size_t>> rorder;  // (bit-reversed prefix, group)
     for (uint32_t m = 1; m < L; ++m) {
       // prefix groups of level m among codes longer than m
-      std::vector<std::pair<uint64_t, uint64_t>> groups;  // (prefix, count)
-      groups.reserve(codes.size());
-      for (const auto& c : codes)
-        if (c.len > m) groups.emplace_back(c.word >> (c.len - m), c.freq);
-      std::sort(groups.begin(), groups.end());
-      std::vector<std::pair<uint64_t, uint64_t>> g;  // aggregated, natural prefix order
-      for (const auto& x : groups) {
-        if (!g.empty() && g.back().first == x.first) g.back().second += x.second;
-        else g.push_back(x);
+      g.clear();
+      for (size_t i : by_word) {
+        const auto& c = codes[i];
+        if (c.len <= m) continue;
+        const uint64_t pfx = c.word >> (c.len - m);
+        if (!g.empty() && g.back().first == pfx) g.back().second += c.freq;
+        else g.emplace_back(pfx, c.freq);
       }
       std::vector<uint64_t> tree_start(g.size()), matrix_start(g.size());
       uint64_t run = 0;
       for (size_t i = 0; i < g.size(); ++i) { tree_start[i] = run; run += g[i].second; }
-      std::vector<size_t> order(g.size());
-      std::iota(order.begin(), order.end(), size_t(0));
-      std::sort(order.begin(), order.end(), [&](size_t a, size_t b) {
-        return rev_bits_host(g[a].first, m) < rev_bits_host(g[b].first, m);
-      });
+      rorder.resize(g.size());
+      for (size_t i = 0; i < g.size(); ++i) rorder[i] = {rev_bits_host(g[i].first, m), i};
+      std::sort(rorder.begin(), rorder.end());
       run = 0;
-      for (size_t i : order) { matrix_start[i] = run; run += g[i].second; }
+      for (const auto& r : rorder) { matrix_start[r.second] = run; run += g[r.second].second; }
       std::vector<uint64_t> st, sm;
       for (size_t i = 0; i < g.size(); ++i)
         if (g[i].second) { st.push_back(tree_start[i]); sm.push_back(matrix_start[i]); }

@@ -86,10 +86,12 @@ void launch_regroup(const uint64_t* matrix_level, uint64_t* tree_level, uint64_t
 void launch_huffman_keys(const void* text, uint64_t n, uint32_t width, const uint64_t* code_len,
                          const uint64_t* code_word, uint64_t ncodes, uint32_t key_bytes, void* keys,
                          uint32_t* status, cudaStream_t s, uint64_t* launches);
-// Histogram of symbols below `nsym` (u64 counts) and the first position of
-// every symbol (atomicMin; first must be filled with UINT64_MAX).
+// Histogram of the symbols (u64 counts; 8- and 16-bit texts: all 2^8 / 2^16
+// values, so hist needs that many entries; 32-bit texts: symbols below nsym)
+// and, with `first` (filled with UINT64_MAX), the first position of every
+// symbol.  hist must be zeroed.
 void launch_symbol_histogram(const void* text, uint64_t n, uint32_t width, uint64_t nsym,
-                             unsigned long long* hist, unsigned long long* first, cudaStream_t s,
+                             unsigned long long* hist, unsigned long long* first, uint32_t* status, cudaStream_t s,
                              uint64_t* launches);
 
 // ---- rank / select --------------------------------------------------------------
