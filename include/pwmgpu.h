@@ -117,6 +117,12 @@ PWMGPU_API pwmgpu_status pwmgpu_ctx_set_engine(pwmgpu_ctx* ctx, int engine);
  * (default 64 MiB; rounded to the histogram's blocks of 2^18 symbols). */
 PWMGPU_API pwmgpu_status pwmgpu_ctx_set_upload_piece_bytes(pwmgpu_ctx* ctx, uint64_t bytes);
 
+/* Chunks (1..16, default 4) in which a host-to-host build with pinned
+ * outputs launches its first pass (and later passes of at most 64
+ * segments), so that the words each chunk completes go back while the next
+ * chunks run; 1 launches each pass whole and streams level groups per pass. */
+PWMGPU_API pwmgpu_status pwmgpu_ctx_set_stream_chunks(pwmgpu_ctx* ctx, uint32_t chunks);
+
 /* ---------------------------------------------------------------------- */
 /* Drop-in construction (host text in, host bit vectors out)               */
 /* ---------------------------------------------------------------------- */

@@ -2,6 +2,7 @@
 // structures, the drop-in host-to-host constructions, the Huffman code
 // builder, queries and generators.
 #include <algorithm>
+#include <array>
 #include <functional>
 #include <cmath>
 #include <cstdio>
@@ -71,6 +72,7 @@ struct pwmgpu_ctx {
   int tile_levels = 0;  // 0: automatic
   int engine = PWMGPU_ENGINE_TILE;
   uint64_t upload_piece = uint64_t(64) << 20;  // bytes of text per uploaded piece
+  uint32_t stream_chunks = 4;                   // chunks of a pass whose words stream to pinned outputs
   bool async_alloc = false;  // stream-ordered allocations on `stream`
   uint64_t scratch_bytes = 0;
   pwmgpu_wx* compute_cache = nullptr;  // reused by pwmgpu_compute for equal shapes
@@ -612,9 +614,15 @@ TileBlob tile_blob(const std::vector<TilePassHost>& passes, size_t from, size_t 
 // zero: the first pass's are zeroed by the caller (or by the histogram
 // kernel), every other pass's by the pass before it, a slab per tile.  Only
 // level and width of passes[pi + 1] are read.
+//
+// bounds: tile boundaries 0 = t_0 < t_1 < ... = tiles of separate launches
+// (chunks, for streaming the finished words of each); after_chunk(c) runs on
+// the host once chunk c is enqueued.
 const void* enqueue_tile_pass(pwmgpu_ctx* ctx, const std::vector<TilePassHost>& passes, size_t pi,
                               const unsigned char* d_blob, const TileBlob& blob, const void* in, uint32_t width,
-                              uint64_t n, Structure& wm, Structure* wt, const TileFirstPass* first) {
+                              uint64_t n, Structure& wm, Structure* wt, const TileFirstPass* first,
+                              const std::vector<uint32_t>& bounds = {},
+                              const std::function<void(size_t)>& after_chunk = {}) {
   cudaStream_t s = ctx->stream;
   const auto& p = passes[pi];
   void* ping = ctx->grow("keys_a", std::max<uint64_t>(n, 1) * width);
@@ -656,15 +664,31 @@ const void* enqueue_tile_pass(pwmgpu_ctx* ctx, const std::vector<TilePassHost>& 
     a.first_level_written = first->level0_written ? 1u : 0u;
   }
   if (pi == 0 && first) a.clear_edges = 1u;  // the histogram kernel did not zero the first pass's levels
-  {
-    const uint64_t structs = (wt && p.segmented) ? 2 : 1;
-    const uint64_t skipped = a.first_level_written ? structs * words_for(n) * 8 : 0;
-    ProfScope ps(ctx, "split_pass", structs * uint64_t(p.K) * (n * width + words_for(n) * 8) - skipped);
-    launch_tile_pass(width, p.K, p.out, a, s, &ctx->launches);
+  const std::vector<uint32_t> b = bounds.size() >= 2 ? bounds : std::vector<uint32_t>{0, p.tiles};
+  const uint64_t structs = (wt && p.segmented) ? 2 : 1;
+  const uint64_t skipped = a.first_level_written ? structs * words_for(n) * 8 : 0;
+  const uint64_t bytes = structs * uint64_t(p.K) * (n * width + words_for(n) * 8) - skipped;
+  for (size_t c = 0; c + 1 < b.size(); ++c) {
+    if (c) CUDA_TRY(cudaMemsetAsync(a.tile_counter, 0, 4, s));
+    a.tile_base = b[c];
+    a.launch_tiles = b[c + 1] - b[c];
+    {
+      ProfScope ps(ctx, "split_pass", p.tiles ? bytes * a.launch_tiles / p.tiles : 0);
+      launch_tile_pass(width, p.K, p.out, a, s, &ctx->launches);
+    }
+    CUDA_TRY(cudaGetLastError());
+    if (after_chunk) after_chunk(c);
   }
-  CUDA_TRY(cudaGetLastError());
   return p.out ? a.out : in;
 }
+
+// Passes launched in chunks of tiles: bounds(pi) gives pass pi's tile bounds
+// (empty: one launch), after(pi, c) runs on the host once chunk c of pass pi
+// is enqueued.
+struct PassChunks {
+  std::function<std::vector<uint32_t>(size_t)> bounds;
+  std::function<void(size_t, size_t)> after;
+};
 
 // Passes [from, passes.size()) and the regroup; `in` is the input of pass
 // `from` (the text for pass 0).  after_pass(i) runs on the host once pass i
@@ -672,14 +696,19 @@ const void* enqueue_tile_pass(pwmgpu_ctx* ctx, const std::vector<TilePassHost>& 
 void run_tile_passes(pwmgpu_ctx* ctx, const void* in, uint32_t width, uint32_t L,
                      const std::vector<TilePassHost>& passes, const std::vector<uint32_t>& regroup,
                      const LevelTables& tabs, Structure& wm, Structure* wt, const TileFirstPass* first = nullptr,
-                     const std::function<void(size_t)>& after_pass = {}, size_t from = 0) {
+                     const std::function<void(size_t)>& after_pass = {}, size_t from = 0,
+                     const PassChunks* chunks = nullptr) {
   cudaStream_t s = ctx->stream;
   const uint64_t n = tabs.level_bits.empty() ? 0 : tabs.level_bits[0];
   const TileBlob blob = tile_blob(passes, from, passes.size(), L, n, wm, wt);
   auto* d_blob = static_cast<unsigned char*>(ctx->grow("tile_plan", blob.bytes.size()));
   CUDA_TRY(cudaMemcpyAsync(d_blob, blob.bytes.data(), blob.bytes.size(), cudaMemcpyHostToDevice, s));
   for (size_t pi = from; pi < passes.size(); ++pi) {
-    in = enqueue_tile_pass(ctx, passes, pi, d_blob, blob, in, width, n, wm, wt, first);
+    std::vector<uint32_t> bounds;
+    std::function<void(size_t)> after_chunk;
+    if (chunks && chunks->bounds) bounds = chunks->bounds(pi);
+    if (chunks && chunks->after) after_chunk = [chunks, pi](size_t c) { chunks->after(pi, c); };
+    in = enqueue_tile_pass(ctx, passes, pi, d_blob, blob, in, width, n, wm, wt, first, bounds, after_chunk);
     if (after_pass) after_pass(pi);
   }
 
@@ -722,6 +751,54 @@ void validate_plain(uint64_t n, uint32_t width, uint32_t levels) {
 // streamed level group by level group as the passes complete when they are
 // pinned, else copied at the end.  The build returns once they are on the
 // host.
+// Words of a structure's levels that become complete as bit ranges of them
+// are written: a word is complete once all its bits are (bits past the
+// level's end count as written); each word is reported once.
+class LevelCompletion {
+ public:
+  LevelCompletion(uint32_t levels, uint64_t nbits) : done_(levels), nbits_(nbits) {}
+  // Bits [a, b) of level m (of level_words words) are written: appends the
+  // words [w0, w1) of the level that this completes.
+  void add(uint32_t m, uint64_t a, uint64_t b, uint64_t level_words, std::vector<std::pair<uint64_t, uint64_t>>& out) {
+    if (a >= b) return;
+    if (b > nbits_ || m >= done_.size()) throw Fail{PWMGPU_ERR_CUDA, "internal: range past the level"};
+    auto& iv = done_[m];
+    uint64_t A = a, B = b;
+    auto it = iv.upper_bound(a);
+    if (it != iv.begin()) {
+      auto pv = std::prev(it);
+      if (pv->second > a) throw Fail{PWMGPU_ERR_CUDA, "internal: range written twice"};
+      if (pv->second == a) {
+        A = pv->first;
+        iv.erase(pv);
+      }
+    }
+    while (it != iv.end() && it->first <= B) {
+      if (it->first < B) throw Fail{PWMGPU_ERR_CUDA, "internal: range written twice"};
+      B = it->second;
+      it = iv.erase(it);
+    }
+    iv[A] = B;
+    // [a, b) touches words [a/64, ceil(b/64)) (to the level's end if it
+    // reaches it), none complete before; those inside [A, B) are now
+    const uint64_t c0 = (A + 63) / 64, c1 = B == nbits_ ? level_words : B / 64;
+    const uint64_t w0 = std::max(c0, a / 64), w1 = std::min(c1, b == nbits_ ? level_words : (b + 63) / 64);
+    if (w0 < w1) out.emplace_back(w0, w1);
+  }
+  bool complete(uint32_t m) const {
+    const auto& iv = done_[m];
+    return nbits_ == 0 || (iv.size() == 1 && iv.begin()->first == 0 && iv.begin()->second == nbits_);
+  }
+
+ private:
+  std::vector<std::map<uint64_t, uint64_t>> done_;
+  uint64_t nbits_;
+};
+
+// Most chunks of a pass whose finished words stream to the host while the
+// next chunks run.
+constexpr uint32_t kMaxStreamChunks = 16;
+
 struct HostIO {
   const void* text = nullptr;
   uint64_t* wm = nullptr;
@@ -800,6 +877,13 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   // of every tile of the first pass and scans them, so that pass neither
   // counts nor looks back.
   TileFirstPass first{};
+  // pinned host words: the histogram, the status word and the block prefix
+  // rows at the bounds of a chunked first pass
+  const uint64_t NB0 = uint64_t(1) << D0;
+  auto* h_hist = static_cast<uint64_t*>(
+      ctx->grow_pinned((bins + 1 + uint64_t(kMaxStreamChunks) * (uint64_t(1) << kTileGivenMaxLevels)) * 8));
+  auto* h_status = reinterpret_cast<uint32_t*>(h_hist + bins);
+  uint64_t* h_rows = h_hist + bins + 1;
   // words of each structure already streamed to the host (a prefix of level 0)
   uint64_t sent[2] = {0, 0};
   Structure* sts[2] = {&wx->wm, &wx->wt};
@@ -862,8 +946,6 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   }
   CUDA_TRY(cudaGetLastError());
   // the histogram and the status word go to pinned host memory
-  auto* h_hist = static_cast<uint64_t*>(ctx->grow_pinned(bins * 8 + 8));
-  auto* h_status = reinterpret_cast<uint32_t*>(h_hist + bins);
   CUDA_TRY(cudaMemcpyAsync(h_hist, d_hist, bins * 8, cudaMemcpyDeviceToHost, s));
   CUDA_TRY(cudaMemcpyAsync(h_status, ctx->d_status, 4, cudaMemcpyDeviceToHost, s));
   CUDA_TRY(cudaEventRecord(ctx->hist_event(), s));
@@ -874,6 +956,13 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   // (the host's plan gives the same first pass).
   const void* next_in = d_text;
   size_t from = 0;
+  // a host-to-host build runs the first pass in chunks of whole histogram
+  // blocks (blk0: block bounds; ev0: an event after each chunk) and reads the
+  // block prefixes at their bounds, so that the words each chunk finishes go
+  // back while the next ones run
+  std::vector<uint32_t> blk0;
+  std::vector<cudaEvent_t> ev0;
+  cudaEvent_t rows_ev = nullptr;
   if (tile_hist) {
     const auto shape = plan_passes(L, Kz);
     std::vector<TilePassHost> early(std::min<size_t>(shape.size(), 2));
@@ -894,8 +983,20 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     launch_tile_block_scan(const_cast<unsigned long long*>(first.blockpre), tile_hist_blocks(n, T), D0, d_hist, L,
                            uint32_t(p0.K), p0.out, want_tree, reinterpret_cast<uint64_t*>(d_b0 + b0.table[0]), s,
                            &ctx->launches);
-    next_in = enqueue_tile_pass(ctx, early, 0, d_b0, b0, d_text, wx->width, n, wx->wm,
-                                want_tree ? &wx->wt : nullptr, &first);
+    std::vector<uint32_t> bounds0;
+    const uint32_t nblk = tile_hist_blocks(n, T);
+    const uint32_t C = ctx->stream_chunks;
+    if (stream_out && C > 1 && nblk >= 2 * C) {
+      for (uint32_t c = 0; c <= C; ++c) blk0.push_back(uint32_t(uint64_t(nblk) * c / C));
+      for (uint32_t c = 1; c < C; ++c)
+        CUDA_TRY(cudaMemcpyAsync(h_rows + (c - 1) * NB0, first.blockpre + uint64_t(blk0[c]) * NB0, NB0 * 8,
+                                 cudaMemcpyDeviceToHost, s));
+      rows_ev = ctx->mark(s);
+      for (uint32_t b : blk0)
+        bounds0.push_back(uint32_t(std::min<uint64_t>(p0.tiles, uint64_t(b) * first.tiles_per_block)));
+    }
+    next_in = enqueue_tile_pass(ctx, early, 0, d_b0, b0, d_text, wx->width, n, wx->wm, want_tree ? &wx->wt : nullptr,
+                                &first, bounds0, [&](size_t) { ev0.push_back(ctx->mark(s)); });
     from = 1;
   }
   CUDA_TRY(cudaEventSynchronize(ctx->hist_event()));
@@ -908,8 +1009,9 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   std::vector<PassPlan> plan;
   std::vector<TilePassHost> tile_passes;
   std::vector<uint32_t> regroup;
+  std::vector<std::vector<uint64_t>> cnt;  // natural-prefix counts per level
   if (tile_engine) {
-    const auto cnt = fold_prefix_counts(h_hist, L);
+    cnt = fold_prefix_counts(h_hist, L);
     tile_passes = plan_tile_passes(cnt, L, kmax, tile_pass_elems(wx->width), want_tree, &regroup);
     tabs = build_tables_tile(cnt, L, want_tree ? regroup : std::vector<uint32_t>{});
   } else {
@@ -921,11 +1023,142 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   // Streaming the structures back: after each pass its levels of the
   // structures it completes (tree levels left to the regroup come last).
   auto level_end = [&](const Structure& st, uint32_t m) { return m + 1 < st.levels ? st.offs[m + 1] : st.total_words; };
+  // Chunked streaming (every tree level from the passes): the first pass's
+  // chunks, and later passes of few segments in chunks of whole segments; a
+  // word goes back once all its bits are written.
+  const bool chunk_stream = stream_out && tile_engine && regroup.empty();
+  std::vector<char> streamed(tile_passes.size(), 0);
+  std::vector<LevelCompletion> done(2, LevelCompletion(L, n));
+  std::vector<std::array<uint64_t, 3>> pend;  // (structure, first word, end word)
+  std::vector<std::pair<uint64_t, uint64_t>> fresh;
+  auto active = [&](int st) { return host_out[st] != nullptr && sts[st]->present; };
+  auto note = [&](int st, uint32_t m, uint64_t a, uint64_t b) {  // bits [a, b) of level m written
+    const Structure& S = *sts[st];
+    fresh.clear();
+    done[st].add(m, a, b, level_end(S, m) - S.offs[m], fresh);
+    for (const auto& w : fresh) pend.push_back({uint64_t(st), S.offs[m] + w.first, S.offs[m] + w.second});
+  };
+  auto flush = [&](cudaEvent_t after) {  // the pending words, once `after` has happened
+    if (pend.empty()) return;
+    std::sort(pend.begin(), pend.end());
+    CUDA_TRY(cudaStreamWaitEvent(ctx->down, after, 0));
+    for (size_t i = 0; i < pend.size();) {
+      const int st = int(pend[i][0]);
+      const uint64_t w0 = pend[i][1];
+      uint64_t w1 = pend[i][2];
+      size_t k = i + 1;
+      for (; k < pend.size() && pend[k][0] == pend[i][0] && pend[k][1] == w1; ++k) w1 = pend[k][2];
+      if (w1 > sts[st]->total_words) throw Fail{PWMGPU_ERR_CUDA, "internal: words past the structure"};
+      CUDA_TRY(cudaMemcpyAsync(host_out[st] + w0, sts[st]->d_words + w0, (w1 - w0) * 8, cudaMemcpyDeviceToHost,
+                               ctx->down));
+      i = k;
+    }
+    pend.clear();
+  };
+  auto check_levels = [&](const TilePassHost& p, uint32_t m0) {
+    for (int st = 0; st < 2; ++st)
+      if (active(st) && (st == 0 || p.segmented))
+        for (uint32_t m = m0; m < p.level + uint32_t(p.K); ++m)
+          if (!done[st].complete(m)) throw Fail{PWMGPU_ERR_CUDA, "internal: a streamed level is incomplete"};
+  };
+  // start of each natural prefix of level m in the matrix (key order) and the tree
+  auto level_starts = [&](uint32_t m, bool tree) {
+    std::vector<uint64_t> st(cnt[m].size());
+    uint64_t run = 0;
+    for (uint64_t y = 0; y < st.size(); ++y) {
+      const uint64_t q = tree ? y : rev_bits_host(y, m);
+      st[q] = run;
+      run += cnt[m][q];
+    }
+    return st;
+  };
+  if (chunk_stream && blk0.size() >= 2 && ev0.size() + 1 == blk0.size() && !tile_passes.empty() &&
+      tile_passes[0].K == Kz) {
+    const TilePassHost& p = tile_passes[0];
+    CUDA_TRY(cudaEventSynchronize(rows_ev));
+    // keys of each natural prefix of level j in the histogram blocks before bound c
+    auto before = [&](size_t c, uint32_t j) {
+      if (c + 1 == blk0.size()) return cnt[j];
+      std::vector<uint64_t> r(size_t(1) << j, 0);
+      if (c == 0) return r;
+      const uint64_t* row = h_rows + (c - 1) * NB0;  // key order of the first D0 bits
+      for (uint64_t x = 0; x < NB0; ++x) r[rev_bits_host(x, D0) >> (D0 - j)] += row[x];
+      return r;
+    };
+    std::vector<std::vector<uint64_t>> start[2];
+    for (int st = 0; st < 2; ++st)
+      for (uint32_t j = 0; j < uint32_t(p.K); ++j) start[st].push_back(level_starts(j, st == 1));
+    for (int st = 0; st < 2; ++st)  // level 0 went back with the upload
+      if (active(st)) note(st, 0, 0, n);
+    pend.clear();
+    for (size_t c = 0; c + 1 < blk0.size(); ++c) {
+      if (c == 0)
+        for (int st = 0; st < 2; ++st)
+          if (active(st) && sent[st] < level_end(*sts[st], 0)) pend.push_back({uint64_t(st), sent[st], level_end(*sts[st], 0)});
+      for (uint32_t j = 1; j < uint32_t(p.K); ++j) {
+        const auto lo = before(c, j), hi = before(c + 1, j);
+        for (uint64_t q = 0; q < lo.size(); ++q)
+          for (int st = 0; st < 2; ++st)
+            if (active(st)) note(st, j, start[st][j][q] + lo[q], start[st][j][q] + hi[q]);
+      }
+      flush(ev0[c]);
+    }
+    check_levels(p, 0);
+    streamed[0] = 1;
+  }
+  // later passes: chunks of whole segments (the host knows each segment's runs)
+  std::vector<std::vector<uint32_t>> seg_bounds(tile_passes.size());
+  PassChunks chunks;
+  chunks.bounds = [&](size_t pi) {
+    std::vector<uint32_t> b;
+    const TilePassHost& p = tile_passes[pi];
+    if (!chunk_stream || pi == 0 || !p.segmented || p.segs.size() < 2 || p.segs.size() > 64) return b;
+    auto& sb = seg_bounds[pi];
+    sb.assign(1, 0);
+    for (uint32_t c = 1; c < ctx->stream_chunks; ++c) {
+      const uint64_t target = uint64_t(p.tiles) * c / ctx->stream_chunks;
+      uint32_t i = sb.back() + 1;
+      while (i < p.segs.size() && p.segs[i].tile0 < target) ++i;
+      if (i < p.segs.size()) sb.push_back(i);
+    }
+    sb.push_back(uint32_t(p.segs.size()));
+    for (uint32_t i : sb) b.push_back(i < p.segs.size() ? p.segs[i].tile0 : p.tiles);
+    return b;
+  };
+  chunks.after = [&](size_t pi, size_t c) {
+    if (seg_bounds[pi].empty()) return;
+    const TilePassHost& p = tile_passes[pi];
+    const uint32_t l = p.level;
+    for (uint32_t i = seg_bounds[pi][c]; i < seg_bounds[pi][c + 1]; ++i) {
+      const TileSegHost& sg = p.segs[i];
+      const uint64_t* tab = p.table.data() + sg.table;
+      for (int j = 0; j < p.K; ++j)
+        for (int v = 0; v < (1 << j); ++v) {
+          const uint64_t x = (uint64_t(v) << l) | sg.group;
+          const uint64_t m = cnt[l + j][rev_bits_host(x, l + uint32_t(j))];
+          for (int st = 0; st < 2; ++st)
+            if (active(st)) {
+              const uint64_t b = tab[st ? tile_wt_entry(p.K, j, v) : tile_wm_entry(j, v)];
+              note(st, l + uint32_t(j), b, b + m);
+            }
+        }
+    }
+    flush(ctx->mark(s));
+    if (c + 2 == seg_bounds[pi].size()) {
+      check_levels(p, l);
+      streamed[pi] = 1;
+    }
+  };
   auto after_pass = [&](size_t pi) {
     for (int st = 0; st < 2; ++st) {
       if (!host_out[st] || !sts[st]->present) continue;
       const Structure& S = *sts[st];
       uint64_t w1 = sent[st];
+      if (pi < tile_passes.size() && streamed[pi]) {  // sent chunk by chunk
+        const TilePassHost& p = tile_passes[pi];
+        sent[st] = std::max(sent[st], level_end(S, p.level + p.K - 1));
+        continue;
+      }
       if (pi < tile_passes.size()) {
         const TilePassHost& p = tile_passes[pi];
         if (st == 1 && !p.segmented) continue;
@@ -965,7 +1198,8 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   if (tile_engine) {
     if (from == 1) hook(0);
     run_tile_passes(ctx, next_in, wx->width, L, tile_passes, regroup, tabs, wx->wm, want_tree ? &wx->wt : nullptr,
-                    first.blockpre ? &first : nullptr, std::function<void(size_t)>(hook), from);
+                    first.blockpre ? &first : nullptr, std::function<void(size_t)>(hook), from,
+                    chunk_stream ? &chunks : nullptr);
   }
   else
     run_passes(ctx, d_text, wx->width, wx->width, false, L, plan, tabs, wx->wm, want_tree ? &wx->wt : nullptr);
@@ -1633,6 +1867,12 @@ pwmgpu_status pwmgpu_ctx_set_engine(pwmgpu_ctx* ctx, int engine) {
 pwmgpu_status pwmgpu_ctx_set_upload_piece_bytes(pwmgpu_ctx* ctx, uint64_t bytes) {
   if (!ctx || bytes == 0) return PWMGPU_ERR_ARG;
   ctx->upload_piece = bytes;
+  return PWMGPU_OK;
+}
+
+pwmgpu_status pwmgpu_ctx_set_stream_chunks(pwmgpu_ctx* ctx, uint32_t chunks) {
+  if (!ctx || chunks == 0 || chunks > kMaxStreamChunks) return PWMGPU_ERR_ARG;
+  ctx->stream_chunks = chunks;
   return PWMGPU_OK;
 }
 

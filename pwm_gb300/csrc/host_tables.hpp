@@ -185,6 +185,7 @@ constexpr uint32_t kTilePlanMaxLevels = 20;
 struct TileSegHost {
   uint64_t in_begin, m, table;
   uint32_t tile0, text;
+  uint64_t group = 0;  // the segment's group of level `level` (key order)
 };
 
 struct TilePassHost {
@@ -226,9 +227,9 @@ inline std::vector<TilePassHost> plan_tile_passes(const std::vector<std::vector<
     ps.segmented = want_tree && (l == 0 || (groups <= 65536 && n >= groups * 4 * uint64_t(T)));
     const int TS = tile_table_size(K);
     uint32_t tile = 0;
-    auto add_segment = [&](uint64_t begin, uint64_t m, const std::vector<uint64_t>& tab) {
+    auto add_segment = [&](uint64_t begin, uint64_t m, const std::vector<uint64_t>& tab, uint64_t group) {
       if (m == 0) return;
-      ps.segs.push_back({begin, m, uint64_t(ps.table.size()), tile, 0u});
+      ps.segs.push_back({begin, m, uint64_t(ps.table.size()), tile, 0u, group});
       ps.table.insert(ps.table.end(), tab.begin(), tab.end());
       tile += uint32_t((m + T - 1) / T);
     };
@@ -246,7 +247,7 @@ inline std::vector<TilePassHost> plan_tile_passes(const std::vector<std::vector<
           }
         if (ps.out)
           for (int v = 0; v < (1 << K); ++v) tab[size_t(tile_out_entry(K, v))] = prek[l + K][(uint64_t(v) << l) | g];
-        add_segment(prek[l][g], m, tab);
+        add_segment(prek[l][g], m, tab, g);
       }
     } else {
       // counts of key_K (bits l..l+K-1, first least significant) over the
@@ -269,7 +270,7 @@ inline std::vector<TilePassHost> plan_tile_passes(const std::vector<std::vector<
           }
         }
       }
-      add_segment(0, n, tab);
+      add_segment(0, n, tab, 0);
       if (want_tree && regroup)
         for (int j = 0; j < K; ++j)
           if (l + uint32_t(j) > 0) regroup->push_back(l + uint32_t(j));

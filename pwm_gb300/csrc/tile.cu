@@ -29,7 +29,7 @@ uint32_t tile_pass_elems(uint32_t key_bytes) {
 }
 
 void launch_tile_pass(uint32_t key_bytes, int K, bool out, const TileArgs& a, cudaStream_t s, uint64_t* launches) {
-  if (a.tiles == 0) return;
+  if (a.launch_tiles == 0) return;
   if (K > kTileMaxLevels) {
     // only as the last pass of a text whose prefixes the histogram gives
     if (out || !a.blockpre || K > kTileGivenMaxLevels) return;

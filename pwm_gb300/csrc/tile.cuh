@@ -83,7 +83,9 @@ struct TileArgs {
   uint32_t* tile_counter;        // zeroed
   uint32_t* status;
   uint32_t nsegs;
-  uint32_t tiles;
+  uint32_t tiles;       // tiles of the whole pass (the look-back state's stride)
+  uint32_t tile_base;   // this launch takes tiles [tile_base, tile_base + launch_tiles)
+  uint32_t launch_tiles;
   // Optional (first pass of a text with one segment): the finest-run counts
   // of every tile and their exclusive prefixes, from the histogram kernel:
   // prefix = blockpre[tile / tiles_per_block] + relpre[tile].  The pass then
@@ -469,7 +471,7 @@ __global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / T
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) {
-    const uint32_t g = atomicAdd(a.tile_counter, 1u);
+    const uint32_t g = a.tile_base + atomicAdd(a.tile_counter, 1u);
     uint32_t lo = 0, hi = a.nsegs;  // last segment with tile0 <= g
     while (hi - lo > 1) {
       const uint32_t mid = (lo + hi) >> 1;

@@ -18,7 +18,7 @@ void launch_tile_one(const TileArgs& a, cudaStream_t s) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(C::smem_bytes()));
     configured = true;
   }
-  kern<<<a.tiles, kTileThreads, C::smem_bytes(), s>>>(a);
+  kern<<<a.launch_tiles, kTileThreads, C::smem_bytes(), s>>>(a);
 }
 
 // Last passes of 5..8 levels with given prefixes (tile_deep.cu).

@@ -167,3 +167,38 @@ def test_drop_in_compute_pinned(pg, orc, contexts):
         check_against_oracle(orc, text, L, None if tree else words, zeros, words if tree else None,
                              None if tree else v, v if tree else None)
         ds.free()
+
+
+@pytest.mark.parametrize("chunks", [1, 3, 16])
+@pytest.mark.parametrize("width,L,n", [(1, 8, 4_500_007), (1, 5, 3_000_001), (2, 8, 1_100_003), (1, 8, 100_003)])
+def test_stream_chunks(pg, orc, width, L, n, chunks):
+    """Passes launched in chunks whose finished words stream back (or, for
+    texts too small to chunk, whole) give the same structures."""
+    torch = torch_cuda()
+    ctx = pg.Context()
+    ctx.set_upload_piece_bytes(1 << 20)
+    ctx.set_stream_chunks(chunks)
+    rng = np.random.default_rng(chunks * 7 + L)
+    g = np.minimum(rng.geometric(0.02, n) - 1, (1 << L) - 1)
+    text = np.where(rng.random(n) < 0.7, g, rng.integers(0, 1 << L, n)).astype(DT[width])
+    ds = pg.DeviceStructure(n, width, L, matrix=True, tree=True, rank_select=True, context=ctx)
+    vm, vt = ds.view(0), ds.view(1)
+    wm = host_u64(torch, vm.total_words, True)
+    wt = host_u64(torch, vt.total_words, True)
+    wm.fill_(-1)  # every word, padding included, must be written
+    wt.fill_(-1)
+    zeros = np.zeros(L, dtype=np.uint64)
+    ds.compute_host(host_text(torch, text, True).data_ptr(), wm.data_ptr(), zeros, wt.data_ptr())
+    wm_np = wm.numpy().view(np.uint64)[:vm.total_words]
+    wt_np = wt.numpy().view(np.uint64)[:vt.total_words]
+    check_against_oracle(orc, text, L, wm_np, zeros, wt_np, vm, vt)
+    for which, got in ((0, wm_np), (1, wt_np)):
+        ref_words = np.zeros(got.size, dtype=np.uint64)
+        ctx.check(ctx.lib.pwmgpu_wx_download(ctx.h, ds.h, which, ref_words.ctypes.data_as(pg._lib.u64p), None))
+        assert np.array_equal(ref_words, got), which
+    ds.free()
+    with pytest.raises(pg.PwmGpuError):
+        ctx.set_stream_chunks(0)
+    with pytest.raises(pg.PwmGpuError):
+        ctx.set_stream_chunks(17)
+    ctx.close()
