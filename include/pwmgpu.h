@@ -213,6 +213,26 @@ PWMGPU_API pwmgpu_status pwmgpu_wx_query(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, i
  * returns when out[] holds the answers. */
 PWMGPU_API pwmgpu_status pwmgpu_wx_query_host(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which, int op,
                                               const uint64_t* a, const uint64_t* b, uint64_t count, uint64_t* out);
+/* Device-resident Huffman-shaped structure: exactly one of PWMGPU_MATRIX or
+ * PWMGPU_TREE (pwm's matrix and tree use different codes), optionally
+ * PWMGPU_RANK_SELECT, built from a non-empty device text.  Codes come from
+ * the caller (code_len/code_word, num_codes entries; levels = the longest
+ * code of a symbol that occurs) or, when code_len is NULL, from the builder
+ * of pwmgpu_huffman_codes (8- and 16-bit texts).  The levels are those of
+ * pwmgpu_compute_huffman (pwmgpu_wx_view / _download read them).  With
+ * rank/select, pwmgpu_wx_query answers ACCESS (the symbol), RANK (occurrences
+ * before an index, the index clamped to the size) and SELECT (position of the
+ * b-th occurrence, b >= 1; all ones when there are fewer; 0 for b = 0) by
+ * walking the symbol's code: pwm's query_support has no Huffman queries
+ * (include/queries/query_support.hpp:43,55,67 print "NOT YET IMPLEMENTED").
+ * Plain builds (pwmgpu_wx_build and the like) refuse such a wx. */
+PWMGPU_API pwmgpu_status pwmgpu_wx_build_huffman(pwmgpu_ctx* ctx, const void* d_text, uint64_t size,
+                                                 uint32_t word_width, uint32_t shape_flags, const uint64_t* code_len,
+                                                 const uint64_t* code_word, uint64_t num_codes, pwmgpu_wx** out);
+/* The code table of a Huffman-shaped wx: num_codes receives its entries;
+ * code_len / code_word (both or neither) receive them when cap allows. */
+PWMGPU_API pwmgpu_status pwmgpu_wx_codes(const pwmgpu_wx* wx, uint64_t* code_len, uint64_t* code_word, uint64_t cap,
+                                         uint64_t* num_codes);
 PWMGPU_API void pwmgpu_wx_free(pwmgpu_wx* wx);
 
 /* ---------------------------------------------------------------------- */

@@ -387,6 +387,38 @@ class DeviceStructure:
         self.size, self.word_width, self.levels = int(size), int(word_width), int(levels)
         self.matrix, self.tree, self.rank_select = matrix, tree, rank_select
 
+    @classmethod
+    def huffman(cls, d_text_ptr, size, word_width, tree=False, rank_select=True, codes=None, context=None):
+        """A Huffman-shaped matrix or tree built from a device text
+        (pwmgpu_wx_build_huffman); codes: (code_len, code_word) u64 arrays,
+        or None for pwm's builder.  Queries walk the symbols' codes."""
+        self = cls.__new__(cls)
+        self.ctx = context or default_context()
+        flags = (TREE if tree else MATRIX) | (RANK_SELECT if rank_select else 0)
+        h = ctypes.c_void_p()
+        if codes is not None:
+            ln = np.ascontiguousarray(codes[0], dtype=np.uint64)
+            wd = np.ascontiguousarray(codes[1], dtype=np.uint64)
+            args = (_u64p(ln), _u64p(wd), ln.size)
+        else:
+            args = (None, None, 0)
+        self.ctx.check(self.ctx.lib.pwmgpu_wx_build_huffman(self.ctx.h, ctypes.c_void_p(int(d_text_ptr)), int(size),
+                                                            int(word_width), flags, *args, ctypes.byref(h)))
+        self.h = h
+        v = self.view(1 if tree else 0)
+        self.size, self.word_width, self.levels = int(size), int(word_width), int(v.levels)
+        self.matrix, self.tree, self.rank_select = not tree, tree, rank_select
+        return self
+
+    def codes(self):
+        """(code_len, code_word) of a Huffman-shaped structure."""
+        n = ctypes.c_uint64(0)
+        self.ctx.check(self.ctx.lib.pwmgpu_wx_codes(self.h, None, None, 0, ctypes.byref(n)))
+        ln = np.zeros(max(n.value, 1), dtype=np.uint64)
+        wd = np.zeros(max(n.value, 1), dtype=np.uint64)
+        self.ctx.check(self.ctx.lib.pwmgpu_wx_codes(self.h, _u64p(ln), _u64p(wd), n.value, ctypes.byref(n)))
+        return ln[:n.value], wd[:n.value]
+
     def build(self, d_text_ptr):
         """Builds from a device pointer (e.g. a torch tensor's data_ptr())."""
         self.ctx.check(self.ctx.lib.pwmgpu_wx_build(self.ctx.h, self.h, ctypes.c_void_p(int(d_text_ptr))))

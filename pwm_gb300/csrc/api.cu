@@ -238,7 +238,15 @@ struct pwmgpu_wx {
   bool wm_internal = false;  // matrix built only as the source of the tree
   bool keep_hist = false;    // PWMGPU_KEEP_HISTOGRAM: the leaf histogram of the last build, for merges
   std::vector<uint64_t> hist;
-  ~pwmgpu_wx() { wm.release(); wt.release(); }
+  // Huffman-shaped: the code table, and its device copy for queries
+  std::vector<uint64_t> code_len, code_word;
+  uint64_t* d_huff = nullptr;
+  HuffQueryTables hq{};
+  ~pwmgpu_wx() {
+    wm.release();
+    wt.release();
+    if (d_huff) cudaFree(d_huff);
+  }
 };
 
 pwmgpu_ctx::~pwmgpu_ctx() {
@@ -1415,6 +1423,7 @@ void build_huffman(pwmgpu_ctx* ctx, const void* d_text, uint64_t n, uint32_t wid
   if (counted != n) throw Fail{PWMGPU_ERR_SYMBOL, "a text symbol is outside the code table"};
   uint32_t maxlen = 0;
   for (auto& c : wc) maxlen = std::max(maxlen, c.len);
+  if (levels == 0) levels = maxlen;  // the longest code of a symbol that occurs
   if (maxlen != levels) throw Fail{PWMGPU_ERR_ARG, "levels must equal the longest code length"};
   const uint32_t key_bytes = maxlen <= 24 ? 4 : 8;
   const auto plan = plan_passes(levels, ctx->pass_levels);
@@ -1926,8 +1935,9 @@ pwmgpu_status pwmgpu_wx_merge(pwmgpu_ctx* ctx, const pwmgpu_wx* const* shards, u
 
 pwmgpu_status pwmgpu_wx_build_sharded(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, uint32_t shards) {
   if (!ctx || !wx || shards == 0 || (!d_text && wx->n)) return PWMGPU_ERR_ARG;
+  if (wx->huffman) return fail(ctx, PWMGPU_ERR_ARG, "a Huffman-shaped wx is built by pwmgpu_wx_build_huffman");
   return guarded(ctx, [&]() {
-    if (shards == 1 || wx->n == 0 || wx->huffman) {
+    if (shards == 1 || wx->n == 0) {
       build_plain(ctx, wx, d_text);
       return PWMGPU_OK;
     }
@@ -1979,6 +1989,7 @@ pwmgpu_status pwmgpu_wx_create(pwmgpu_ctx* ctx, uint64_t size, uint32_t word_wid
 
 pwmgpu_status pwmgpu_wx_build(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text) {
   if (!ctx || !wx || (!d_text && wx->n)) return PWMGPU_ERR_ARG;
+  if (wx->huffman) return fail(ctx, PWMGPU_ERR_ARG, "a Huffman-shaped wx is built by pwmgpu_wx_build_huffman");
   return guarded(ctx, [&]() {
     build_plain(ctx, wx, d_text);
     return PWMGPU_OK;
@@ -1987,6 +1998,7 @@ pwmgpu_status pwmgpu_wx_build(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text
 
 pwmgpu_status pwmgpu_wx_build_host(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* host_text) {
   if (!ctx || !wx || (!host_text && wx->n)) return PWMGPU_ERR_ARG;
+  if (wx->huffman) return fail(ctx, PWMGPU_ERR_ARG, "a Huffman-shaped wx is built by pwmgpu_wx_build_huffman");
   return guarded(ctx, [&]() {
     void* d_text = ctx->grow("host_text", std::max<uint64_t>(wx->n * wx->width, 1));
     HostIO io;
@@ -1999,6 +2011,7 @@ pwmgpu_status pwmgpu_wx_build_host(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* h
 pwmgpu_status pwmgpu_wx_compute_host(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* host_text, uint64_t* wm_bv,
                                      uint64_t* wm_zeros, uint64_t* wt_bv) {
   if (!ctx || !wx || (!host_text && wx->n)) return PWMGPU_ERR_ARG;
+  if (wx->huffman) return fail(ctx, PWMGPU_ERR_ARG, "a Huffman-shaped wx is built by pwmgpu_wx_build_huffman");
   if ((wm_bv && (!wx->wm.present || wx->wm_internal)) || (wt_bv && !wx->wt.present))
     return fail(ctx, PWMGPU_ERR_ARG, "an output structure the wx does not hold");
   return guarded(ctx, [&]() {
@@ -2081,11 +2094,13 @@ pwmgpu_status pwmgpu_wx_query(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which, i
                               const uint64_t* d_b, uint64_t count, uint64_t* d_out) {
   if (!ctx || !wx || op < 0 || op > 2 || (count && (!d_a || !d_out || (op > 0 && !d_b)))) return PWMGPU_ERR_ARG;
   const Structure& s = which ? wx->wt : wx->wm;
-  if (!s.present || !s.rs || s.huffman) return fail(ctx, PWMGPU_ERR_ARG, "queries need a plain structure with rank/select");
+  if (!s.present || !s.rs || (which == 0 && wx->wm_internal))
+    return fail(ctx, PWMGPU_ERR_ARG, "queries need a structure with rank/select");
   return guarded(ctx, [&]() {
     QueryStructure q{s.levels, s.is_tree ? 1u : 0u, s.n, s.d_q_levels, s.d_zeros};
     ProfScope ps(ctx, "queries", count * 24);
-    launch_queries(q, op, d_a, d_b, count, d_out, ctx->stream, &ctx->launches);
+    if (s.huffman) launch_huff_queries(q, wx->hq, op, d_a, d_b, count, d_out, ctx->stream, &ctx->launches);
+    else launch_queries(q, op, d_a, d_b, count, d_out, ctx->stream, &ctx->launches);
     CUDA_TRY(cudaGetLastError());
     return PWMGPU_OK;
   });
@@ -2096,7 +2111,8 @@ pwmgpu_status pwmgpu_wx_query_host(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int whi
   if (!ctx || !wx || op < 0 || op > 2 || (count && (!a || !out || (op > 0 && !b)))) return PWMGPU_ERR_ARG;
   if (count == 0) return PWMGPU_OK;
   const Structure& s = which ? wx->wt : wx->wm;
-  if (!s.present || !s.rs || s.huffman) return fail(ctx, PWMGPU_ERR_ARG, "queries need a plain structure with rank/select");
+  if (!s.present || !s.rs || (which == 0 && wx->wm_internal))
+    return fail(ctx, PWMGPU_ERR_ARG, "queries need a structure with rank/select");
   return guarded(ctx, [&]() {
     auto* d = static_cast<uint64_t*>(ctx->grow("query_io", count * 3 * 8));
     cudaStream_t st = ctx->stream;
@@ -2105,13 +2121,94 @@ pwmgpu_status pwmgpu_wx_query_host(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int whi
     QueryStructure q{s.levels, s.is_tree ? 1u : 0u, s.n, s.d_q_levels, s.d_zeros};
     {
       ProfScope ps(ctx, "queries", count * 24);
-      launch_queries(q, op, d, d + count, count, d + 2 * count, st, &ctx->launches);
+      if (s.huffman) launch_huff_queries(q, wx->hq, op, d, d + count, count, d + 2 * count, st, &ctx->launches);
+      else launch_queries(q, op, d, d + count, count, d + 2 * count, st, &ctx->launches);
     }
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(out, d + 2 * count, count * 8, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     return PWMGPU_OK;
   });
+}
+
+pwmgpu_status pwmgpu_wx_build_huffman(pwmgpu_ctx* ctx, const void* d_text, uint64_t size, uint32_t word_width,
+                                      uint32_t shape_flags, const uint64_t* code_len, const uint64_t* code_word,
+                                      uint64_t num_codes, pwmgpu_wx** out) {
+  if (!ctx || !out || !d_text) return PWMGPU_ERR_ARG;
+  *out = nullptr;
+  return guarded(ctx, [&]() {
+    if (!valid_width(word_width)) throw Fail{PWMGPU_ERR_ARG, "word_width must be 1, 2 or 4"};
+    if (size == 0) throw Fail{PWMGPU_ERR_ARG, "a Huffman-shaped structure needs a non-empty text"};
+    const bool tree = shape_flags & PWMGPU_TREE;
+    if (tree == bool(shape_flags & PWMGPU_MATRIX))
+      throw Fail{PWMGPU_ERR_ARG, "a Huffman-shaped wx holds one structure: PWMGPU_MATRIX or PWMGPU_TREE"};
+    const bool rs = shape_flags & PWMGPU_RANK_SELECT;
+    if (rs && size >= 4294967295ull - 64) throw Fail{PWMGPU_ERR_ARG, "rank/select support needs levels below 2^32-1 bits"};
+    auto wx = std::make_unique<pwmgpu_wx>();
+    wx->ctx = ctx;
+    wx->n = size;
+    wx->width = word_width;
+    wx->flags = shape_flags;
+    wx->huffman = true;
+    uint32_t L = 0;
+    if (code_len) {
+      if (!code_word || num_codes == 0) throw Fail{PWMGPU_ERR_ARG, "code table incomplete"};
+      wx->code_len.assign(code_len, code_len + num_codes);
+      wx->code_word.assign(code_word, code_word + num_codes);
+    } else {
+      uint64_t max_symbol = 0;
+      HuffCodes h = huffman_codes_device(ctx, d_text, size, word_width, tree, &max_symbol);
+      wx->code_len = h.len;
+      wx->code_word = h.word;
+      L = h.levels;
+    }
+    for (uint64_t c = 0; c < wx->code_len.size(); ++c) {
+      if (wx->code_len[c] > 56) throw Fail{PWMGPU_ERR_ARG, "codes longer than 56 bits"};
+      if (wx->code_len[c]) wx->code_word[c] &= (uint64_t(1) << wx->code_len[c]) - 1;
+    }
+    build_huffman(ctx, d_text, size, word_width, tree, wx->code_len, wx->code_word, L, wx->wm,
+                  tree ? &wx->wt : nullptr, rs);
+    const Structure& S = tree ? wx->wt : wx->wm;
+    wx->levels = S.levels;
+    if (tree) {  // the matrix was only the tree's source
+      wx->wm.release();
+      wx->wm.present = false;
+      wx->wm_internal = true;
+    }
+    // device tables for queries: codes per symbol, codes sorted by (length, word), level sizes
+    const uint64_t nsym = wx->code_len.size();
+    std::vector<std::pair<uint64_t, uint64_t>> dec;
+    for (uint64_t c = 0; c < nsym; ++c)
+      if (wx->code_len[c]) dec.emplace_back((wx->code_len[c] << 56) | wx->code_word[c], c);
+    std::sort(dec.begin(), dec.end());
+    std::vector<uint64_t> blob;
+    blob.reserve(2 * nsym + 2 * dec.size() + S.levels);
+    blob.insert(blob.end(), wx->code_len.begin(), wx->code_len.end());
+    blob.insert(blob.end(), wx->code_word.begin(), wx->code_word.end());
+    for (const auto& d : dec) blob.push_back(d.first);
+    for (const auto& d : dec) blob.push_back(d.second);
+    blob.insert(blob.end(), S.bits.begin(), S.bits.end());
+    CUDA_TRY(cudaMalloc(&wx->d_huff, std::max<size_t>(blob.size(), 1) * 8));
+    CUDA_TRY(cudaMemcpyAsync(wx->d_huff, blob.data(), blob.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    const uint64_t* d = wx->d_huff;
+    wx->hq = HuffQueryTables{d, d + nsym, nsym, d + 2 * nsym, d + 2 * nsym + dec.size(), dec.size(),
+                             d + 2 * nsym + 2 * dec.size()};
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));  // the pageable table copy has been read
+    *out = wx.release();
+    return PWMGPU_OK;
+  });
+}
+
+pwmgpu_status pwmgpu_wx_codes(const pwmgpu_wx* wx, uint64_t* code_len, uint64_t* code_word, uint64_t cap,
+                              uint64_t* num_codes) {
+  if (!wx || !num_codes || !wx->huffman) return PWMGPU_ERR_ARG;
+  *num_codes = wx->code_len.size();
+  if (code_len || code_word) {
+    if (!code_len || !code_word || cap < wx->code_len.size()) return PWMGPU_ERR_ARG;
+    std::memcpy(code_len, wx->code_len.data(), wx->code_len.size() * 8);
+    std::memcpy(code_word, wx->code_word.data(), wx->code_word.size() * 8);
+  }
+  return PWMGPU_OK;
 }
 
 void pwmgpu_wx_free(pwmgpu_wx* wx) {

@@ -129,6 +129,19 @@ struct QueryStructure {
 void launch_queries(const QueryStructure& q, int op, const uint64_t* a, const uint64_t* b, uint64_t count,
                     uint64_t* out, cudaStream_t s, uint64_t* launches);
 
+// Code table of a Huffman-shaped structure, as its queries read it.
+struct HuffQueryTables {
+  const uint64_t* code_len;    // per symbol (0: no code)
+  const uint64_t* code_word;   // per symbol: code_len bits, level 0's bit most significant
+  uint64_t nsym;
+  const uint64_t* dec_key;     // (length << 56) | word of every code, ascending
+  const uint64_t* dec_sym;     // the symbol of dec_key[i]
+  uint64_t ndec;
+  const uint64_t* level_bits;  // bits of each level
+};
+void launch_huff_queries(const QueryStructure& q, const HuffQueryTables& h, int op, const uint64_t* a,
+                         const uint64_t* b, uint64_t count, uint64_t* out, cudaStream_t s, uint64_t* launches);
+
 // Allocation-free single-level rank/select build on file-scope device arrays
 // (see ranksel.cu); limit in words.
 uint64_t noalloc_rank_select_max_words();

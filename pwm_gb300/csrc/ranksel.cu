@@ -426,7 +426,175 @@ __global__ void query_kernel(QueryStructure q, int op, const uint64_t* __restric
   }
 }
 
+// ---------------------------------------------------------------------------
+// Queries on Huffman-shaped structures (pwm's query_support has none: it
+// prints "NOT YET IMPLEMENTED", include/queries/query_support.hpp:43,55,67).
+//
+// Level l holds bit l of every code longer than l.  In both shapes the codes
+// that end at a level sort behind all codes that go on: the matrix's codes
+// (huff_codes.hpp:204-245) take, length by length, the largest bit-reversed
+// words, and the tree's are negated canonical codes (:246-283), the largest
+// prefixes.  So level l + 1 is a prefix of level l's entries reordered as the
+// plain structures reorder them (the matrix by its stable 0/1 partition, the
+// tree within each node), and the plain position arithmetic holds; a code
+// ends where its position falls past the next level's size.
+// ---------------------------------------------------------------------------
+__device__ uint64_t huff_decode(const HuffQueryTables& h, uint32_t len, uint64_t word) {
+  const uint64_t key = (uint64_t(len) << 56) | word;
+  uint64_t lo = 0, hi = h.ndec;
+  while (lo < hi) {
+    const uint64_t mid = (lo + hi) >> 1;
+    if (h.dec_key[mid] < key) lo = mid + 1; else hi = mid;
+  }
+  return lo < h.ndec && h.dec_key[lo] == key ? h.dec_sym[lo] : ~0ull;
+}
+
+__global__ void huff_query_kernel(QueryStructure q, HuffQueryTables h, int op, const uint64_t* __restrict__ a,
+                                  const uint64_t* __restrict__ b, uint64_t count, uint64_t* __restrict__ out) {
+  const uint32_t Lv = q.levels;
+  for (uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < count; t += uint64_t(gridDim.x) * blockDim.x) {
+    uint64_t result = ~0ull;
+    if (op == 0) {  // access: read bits until the code ends
+      if (a[t] < q.n) {
+        uint64_t index = a[t], word = 0;
+        if (q.is_tree) {
+          uint64_t start = 0, end = q.n;
+          for (uint32_t level = 0; level < Lv; ++level) {
+            const QueryLevel& L = q.lv[level];
+            const uint64_t left = q_rank0(L, start), right = q_rank0(L, end);
+            const bool one = bit_at(L.data, start + index);
+            word = (word << 1) | (one ? 1u : 0u);
+            if (one) {
+              index = q_rank1(L, start + index) - (start - left);
+              start = start + right - left;
+            } else {
+              index = q_rank0(L, start + index) - left;
+              end = start + right - left;
+            }
+            if (level + 1 == Lv || start + index >= h.level_bits[level + 1]) {
+              result = huff_decode(h, level + 1, word);
+              break;
+            }
+          }
+        } else {
+          for (uint32_t level = 0; level < Lv; ++level) {
+            const QueryLevel& L = q.lv[level];
+            const bool one = bit_at(L.data, index);
+            word = (word << 1) | (one ? 1u : 0u);
+            index = one ? q.zeros[level] + q_rank1(L, index) : q_rank0(L, index);
+            if (level + 1 == Lv || index >= h.level_bits[level + 1]) {
+              result = huff_decode(h, level + 1, word);
+              break;
+            }
+          }
+        }
+      }
+      out[t] = result;
+      continue;
+    }
+    // rank(symbol, index) / select(symbol, occurrence): walk the symbol's code
+    const uint64_t sym = a[t];
+    const uint32_t len = sym < h.nsym ? uint32_t(h.code_len[sym]) : 0u;
+    const uint64_t code = len ? h.code_word[sym] : 0;
+    if (len == 0 || len > Lv) {  // a symbol without a code does not occur
+      out[t] = (op == 1 || b[t] == 0) ? 0 : ~0ull;
+      continue;
+    }
+    auto bit = [&](uint32_t level) { return (code >> (len - 1 - level)) & 1; };
+    if (op == 1) {
+      uint64_t index = b[t] < q.n ? b[t] : q.n;
+      if (q.is_tree) {
+        uint64_t start = 0, end = q.n;
+        for (uint32_t level = 0; level < len && index; ++level) {
+          const QueryLevel& L = q.lv[level];
+          const uint64_t left = q_rank0(L, start), right = q_rank0(L, end);
+          if (bit(level)) {
+            index = q_rank1(L, start + index) - (start - left);
+            start = start + right - left;
+          } else {
+            index = q_rank0(L, start + index) - left;
+            end = start + right - left;
+          }
+        }
+        result = index;
+      } else {
+        uint64_t offset = 0;
+        for (uint32_t level = 0; level < len; ++level) {
+          const QueryLevel& L = q.lv[level];
+          if (bit(level)) {
+            index = q.zeros[level] + q_rank1(L, index);
+            offset = q.zeros[level] + q_rank1(L, offset);
+          } else {
+            index = q_rank0(L, index);
+            offset = q_rank0(L, offset);
+          }
+        }
+        result = index - offset;
+      }
+    } else {
+      uint64_t occ = b[t];
+      if (occ == 0) {
+        result = 0;  // as the plain structures' select
+      } else {
+        if (q.is_tree) {
+          uint64_t st[64], le[64];
+          uint64_t start = 0, end = q.n;
+          for (uint32_t level = 0; level < len; ++level) {
+            const QueryLevel& L = q.lv[level];
+            const uint64_t left = q_rank0(L, start), right = q_rank0(L, end);
+            st[level] = start;
+            le[level] = left;
+            if (bit(level)) start = start + right - left;
+            else end = start + right - left;
+          }
+          if (occ <= end - start) {  // the symbol's node holds its occurrences
+            for (int level = int(len) - 1; level >= 0; --level) {
+              const QueryLevel& L = q.lv[level];
+              const uint64_t adj = level == 0 ? 0 : 1;
+              if (bit(uint32_t(level))) occ = q_select(L, 1, st[level] - le[level] + occ) - st[level] + adj;
+              else occ = q_select(L, 0, le[level] + occ) - st[level] + adj;
+            }
+            result = occ;
+          }
+        } else {
+          uint64_t offset = 0, end = q.n;
+          for (uint32_t level = 0; level < len; ++level) {
+            const QueryLevel& L = q.lv[level];
+            if (bit(level)) {
+              offset = q.zeros[level] + q_rank1(L, offset);
+              end = q.zeros[level] + q_rank1(L, end);
+            } else {
+              offset = q_rank0(L, offset);
+              end = q_rank0(L, end);
+            }
+          }
+          if (occ <= end - offset) {
+            occ += offset;
+            for (int level = int(len) - 1; level >= 0; --level) {
+              const QueryLevel& L = q.lv[level];
+              const uint64_t adj = level == 0 ? 0 : 1;
+              if (bit(uint32_t(level))) occ = q_select(L, 1, occ - q.zeros[level]) + adj;
+              else occ = q_select(L, 0, occ) + adj;
+            }
+            result = occ;
+          }
+        }
+      }
+    }
+    out[t] = result;
+  }
+}
+
 }  // namespace
+
+void launch_huff_queries(const QueryStructure& q, const HuffQueryTables& h, int op, const uint64_t* a,
+                         const uint64_t* b, uint64_t count, uint64_t* out, cudaStream_t s, uint64_t* launches) {
+  if (count == 0) return;
+  uint64_t blocks = (count + 127) / 128;
+  if (blocks > 65535) blocks = 65535;
+  huff_query_kernel<<<unsigned(blocks), 128, 0, s>>>(q, h, op, a, b, count, out);
+  ++*launches;
+}
 
 void launch_rank_select(const RankSelectLevel* host_levels, uint32_t count, RankSelectLevel* dev_levels,
                         uint32_t* tmp, uint64_t tmp_words_per_level, cudaStream_t s, uint64_t* launches) {
