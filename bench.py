@@ -274,6 +274,52 @@ def other_workloads(torch, pg, ctx, reps=3):
         out["mix16_2p28_huffman_" + ("tree" if tree else "matrix")] = {
             "n": int(host16.size), "word_width": 2, "levels": ws.levels(), "codes_ms": (t1 - t0) * 1e3,
             "build_host_to_host_ms": (t2 - t1) * 1e3, "text_gbs_host_to_host": host16.nbytes / (t2 - t1) / 1e9}
+    out["queries_mix16_2p28"] = query_rates(torch, pg, ctx, host16)
+    return out
+
+
+def query_rates(torch, pg, ctx, host16, nq=1 << 22, reps=3):
+    """Access/rank/select rates (millions of queries per second) on the 2^28
+    16-bit text: the plain matrix (16 levels) against the Huffman-shaped
+    matrix with pwm's codes, whose queries walk only their symbol's code.
+    Uniform positions, symbols drawn from the text, occurrences uniform
+    within each symbol's count; device arrays, CUDA events."""
+    import numpy as np
+    rng = np.random.default_rng(11)
+    n = host16.size
+    d_text = torch.from_numpy(host16.view(np.int16)).cuda()
+    sym_np = host16[rng.integers(0, n, nq)].astype(np.int64)
+    counts = np.bincount(host16, minlength=1 << 16)
+    occ_np = 1 + np.floor(rng.random(nq) * counts[sym_np]).astype(np.int64)
+    pos = torch.from_numpy(rng.integers(0, n, nq).astype(np.int64)).cuda()
+    sym = torch.from_numpy(sym_np).cuda()
+    occ = torch.from_numpy(occ_np).cuda()
+    res = torch.empty(nq, dtype=torch.int64, device="cuda")
+    stream = torch.cuda.current_stream()
+    codes = pg.huffman_codes(host16, False, ctx)
+    plain = pg.DeviceStructure(n, 2, 16, matrix=True, rank_select=True, context=ctx)
+    plain.build(d_text.data_ptr())
+    huff = pg.DeviceStructure.huffman(d_text.data_ptr(), n, 2, tree=False, rank_select=True, codes=codes[:2],
+                                      context=ctx)
+    out = {"queries": nq, "mean_code_length": float((codes[0] * counts[:codes[0].size]).sum()) / n}
+    for name, ds in (("plain_matrix", plain), ("huffman_matrix", huff)):
+        rates = {}
+        for op, opname, a, b in ((pg.Q_ACCESS, "access", pos, None), (pg.Q_RANK, "rank", sym, pos),
+                                 (pg.Q_SELECT, "select", sym, occ)):
+            def run():
+                ds.query(0, op, a.data_ptr(), b.data_ptr() if b is not None else None, nq, res.data_ptr())
+            run()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                run()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            rates[opname + "_mqps"] = nq * reps / (e0.elapsed_time(e1) / 1e3) / 1e6
+        ds.check()
+        out[name] = rates
+    plain.free()
+    huff.free()
     return out
 
 
