@@ -213,6 +213,20 @@ PWMGPU_API pwmgpu_status pwmgpu_wx_query(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, i
  * returns when out[] holds the answers. */
 PWMGPU_API pwmgpu_status pwmgpu_wx_query_host(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which, int op,
                                               const uint64_t* a, const uint64_t* b, uint64_t count, uint64_t* out);
+/* Semi-external construction of a host text larger than the device memory
+ * (pwm's semi_in, include/external_memory/semi_in/pc_semi_external.hpp:16-230,
+ * which reads its text twice).  The text streams through the GPU in pieces
+ * that fit about `device_budget` bytes (0: half the free device memory):
+ * once for the leaf histogram, once to build each piece, whose runs go to
+ * the host arrays at their global positions.  wm_bv / wt_bv (either may be
+ * NULL, not both) receive the structures in the layout of
+ * pwmgpu_wx_download (levels of round_up(ceil(size/64), 16) words),
+ * wm_zeros (may be NULL) the matrix zeros.  The result equals a plain
+ * build's bit for bit.  The budget must hold a piece of 2^16 symbols. */
+PWMGPU_API pwmgpu_status pwmgpu_compute_semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t size,
+                                                      uint32_t word_width, uint32_t levels, uint64_t* wm_bv,
+                                                      uint64_t* wm_zeros, uint64_t* wt_bv, uint64_t device_budget);
+
 /* Device-resident Huffman-shaped structure: exactly one of PWMGPU_MATRIX or
  * PWMGPU_TREE (pwm's matrix and tree use different codes), optionally
  * PWMGPU_RANK_SELECT, built from a non-empty device text.  Codes come from

@@ -262,6 +262,28 @@ def huffman_codes(text, is_tree, context=None):
     return ln[:nc.value].copy(), wd[:nc.value].copy(), sizes[:lv.value].copy(), lv.value
 
 
+def compute_semi_external(text, levels, matrix=True, tree=True, device_budget=0, context=None, out=None):
+    """Semi-external build of a host text (pwmgpu_compute_semi_external):
+    the text streams through the GPU in pieces within about device_budget
+    bytes.  Returns (matrix words, matrix zeros, tree words) in the layout of
+    DeviceStructure.download (None for a structure not asked for).  out:
+    optional (matrix, tree) u64 arrays to fill (e.g. pinned memory)."""
+    ctx = context or default_context()
+    t = np.ascontiguousarray(text)
+    n, w = t.size, t.dtype.itemsize
+    lw = (((n + 63) // 64) + 15) // 16 * 16
+    if out is None:
+        out = (np.zeros(levels * lw, np.uint64) if matrix else None, np.zeros(levels * lw, np.uint64) if tree else None)
+    wm, wt = out
+    zeros = np.zeros(levels, np.uint64) if matrix else None
+    cast = lambda a: _u64p(a) if isinstance(a, np.ndarray) else (
+        ctypes.cast(ctypes.c_void_p(int(a.data_ptr())), _lib.u64p) if a is not None else None)
+    ctx.check(ctx.lib.pwmgpu_compute_semi_external(ctx.h, ctypes.c_void_p(t.ctypes.data), n, w, int(levels), cast(wm),
+                                                   _u64p(zeros) if zeros is not None else None, cast(wt),
+                                                   int(device_budget)))
+    return wm, zeros, wt
+
+
 def _variant(name, base, doc):
     return type(name, (base,), {"__doc__": doc})
 

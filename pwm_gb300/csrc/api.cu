@@ -1710,6 +1710,218 @@ std::unique_ptr<pwmgpu_wx> make_wx(pwmgpu_ctx* ctx, uint64_t size, uint32_t word
   return wx;
 }
 
+// ---------------------------------------------------------------------------
+// Semi-external construction (pwm's semi_in, include/external_memory/semi_in/
+// pc_semi_external.hpp:16-230, which reads its text twice: once for the
+// histogram and the first level, once to place every bit).  A host text is
+// streamed through the GPU in pieces that fit a device budget: the first
+// pass accumulates the leaf histogram, which gives every group's global
+// start; the second builds each piece as a shard (matrix and/or tree) and
+// sends each of its runs to the host arrays at the group's start plus the
+// bits earlier pieces put there -- pwm's merge of slices (merge.hpp:
+// 192-465) with the destination in host memory.  Words a run covers whole go
+// by DMA from a staging buffer that holds them shifted into place; words two
+// runs share, and all words of short runs, come back in one copy per piece
+// and are OR-ed together on the host at the end.
+// ---------------------------------------------------------------------------
+constexpr uint64_t kSemiMinPiece = uint64_t(1) << 16;
+constexpr uint64_t kSemiDmaMinWords = 512;  // shorter runs go through the host's OR
+
+void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width, uint32_t L, uint64_t* out_wm,
+                   uint64_t* wm_zeros, uint64_t* out_wt, uint64_t budget) {
+  cudaStream_t s = ctx->stream;
+  const bool want_tree = out_wt != nullptr;
+  const int nout = (out_wm ? 1 : 0) + (out_wt ? 1 : 0);
+  if (budget == 0) {
+    size_t free_b = 0, total_b = 0;
+    CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    budget = free_b / 2;
+  }
+  // device bytes per symbol of a piece: its text, the build's two key
+  // buffers, the shard's structures and the staging of the outputs
+  const double per_sym = 3.0 * width + (want_tree ? 2 : 1) * L / 8.0 + nout * L / 8.0 + 1.0;
+  uint64_t P = uint64_t(double(budget) / per_sym) & ~(kSemiMinPiece - 1);
+  if (P < kSemiMinPiece) throw Fail{PWMGPU_ERR_ARG, "device budget below one piece of 2^16 symbols"};
+  P = std::min(P, (n + kSemiMinPiece - 1) & ~(kSemiMinPiece - 1));
+  const auto* txt = static_cast<const unsigned char*>(text);
+  auto* d_piece = static_cast<unsigned char*>(ctx->grow("semi_text", P * width));
+  // pass 1: the leaf histogram
+  const uint64_t bins = uint64_t(1) << L;
+  auto* d_hist = static_cast<unsigned long long*>(ctx->grow("semi_hist", bins * 8));
+  CUDA_TRY(cudaMemsetAsync(d_hist, 0, bins * 8, s));
+  CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, 4, s));
+  for (uint64_t a = 0; a < n; a += P) {
+    const uint64_t m = std::min(P, n - a);
+    CUDA_TRY(cudaMemcpyAsync(d_piece, txt + a * width, m * width, cudaMemcpyHostToDevice, s));
+    ProfScope ps(ctx, "leaf_histogram", m * width);
+    launch_leaf_histogram(d_piece, m, width, L, d_hist, ctx->d_status, s, &ctx->launches);
+  }
+  std::vector<uint64_t> hist(bins);
+  CUDA_TRY(cudaMemcpyAsync(hist.data(), d_hist, bins * 8, cudaMemcpyDeviceToHost, s));
+  check_device_status(ctx);
+  const auto cnt = fold_prefix_counts(hist.data(), L);
+  if (wm_zeros) {
+    const LevelTables t = build_tables_tile(cnt, L, {});
+    std::memcpy(wm_zeros, t.zeros.data(), L * 8);
+  }
+  // start of each natural prefix of level m in the matrix (key order) or the tree
+  auto starts = [](const std::vector<uint64_t>& c, uint32_t m, bool tree) {
+    std::vector<uint64_t> st(c.size());
+    uint64_t run = 0;
+    for (uint64_t y = 0; y < c.size(); ++y) {
+      const uint64_t q = tree ? y : rev_bits_host(y, m);
+      st[q] = run;
+      run += c[q];
+    }
+    return st;
+  };
+  struct Out {
+    int st;             // 0 matrix, 1 tree
+    uint64_t* host;
+    std::vector<std::vector<uint64_t>> gstart;
+  };
+  std::vector<Out> outs;
+  if (out_wm) outs.push_back({0, out_wm, {}});
+  if (out_wt) outs.push_back({1, out_wt, {}});
+  for (auto& o : outs)
+    for (uint32_t l = 0; l < L; ++l) o.gstart.push_back(starts(cnt[l], l, o.st == 1));
+  std::vector<std::vector<uint64_t>> placed(L);  // per level and prefix: bits earlier pieces placed
+  for (uint32_t l = 0; l < L; ++l) placed[l].assign(cnt[l].size(), 0);
+  const uint64_t lw = padded_words(n);  // words per level of the host arrays
+  // pass 2
+  std::vector<std::array<uint64_t, 3>> acc;  // (output, word, bits) OR-ed at the end
+  struct Pinned {
+    void* p = nullptr;
+    size_t bytes = 0;
+    void* get(size_t b) {
+      if (b > bytes) {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+        CUDA_TRY(cudaMallocHost(&p, b));
+        bytes = b;
+      }
+      return p;
+    }
+    ~Pinned() {
+      if (p) cudaFreeHost(p);
+    }
+  } small_host;
+  std::unique_ptr<pwmgpu_wx> shard;
+  for (uint64_t a = 0; a < n; a += P) {
+    const uint64_t m = std::min(P, n - a);
+    if (!shard || shard->n != m) {
+      shard.reset();
+      shard = make_wx(ctx, m, width, L, (out_wm ? PWMGPU_MATRIX : 0u) | (want_tree ? PWMGPU_TREE : 0u) |
+                                           PWMGPU_KEEP_HISTOGRAM);
+    }
+    CUDA_TRY(cudaMemcpyAsync(d_piece, txt + a * width, m * width, cudaMemcpyHostToDevice, s));
+    build_plain(ctx, shard.get(), d_piece);
+    const auto pc = fold_prefix_counts(shard->hist.data(), L);
+    // the piece's runs: short ones first, then the long ones (their edge
+    // words are gathered behind the short runs' words)
+    std::vector<StageSeg> segs_small, segs_big;
+    std::vector<std::array<uint64_t, 2>> meta_small, meta_big;  // (output, first absolute destination word)
+    for (size_t oi = 0; oi < outs.size(); ++oi) {
+      const Out& o = outs[oi];
+      const Structure& S = o.st ? shard->wt : shard->wm;
+      for (uint32_t l = 0; l < L; ++l) {
+        const auto ls = starts(pc[l], l, o.st == 1);
+        for (uint64_t q = 0; q < pc[l].size(); ++q) {
+          const uint64_t c = pc[l][q];
+          if (!c) continue;
+          const uint64_t dst = o.gstart[l][q] + placed[l][q];
+          StageSeg sg{S.d_words + S.offs[l], ls[q], dst, c, 0};
+          const uint64_t words = ((dst + c + 63) >> 6) - (dst >> 6);
+          const uint64_t edges = ((dst & 63) ? 1 : 0) + (((dst + c) & 63) ? 1 : 0);
+          const std::array<uint64_t, 2> mt{uint64_t(oi), uint64_t(l) * lw + (dst >> 6)};
+          if (words >= edges + kSemiDmaMinWords) {
+            segs_big.push_back(sg);
+            meta_big.push_back(mt);
+          } else {
+            segs_small.push_back(sg);
+            meta_small.push_back(mt);
+          }
+        }
+      }
+    }
+    for (uint32_t l = 0; l < L; ++l)
+      for (uint64_t q = 0; q < pc[l].size(); ++q) placed[l][q] += pc[l][q];
+    uint64_t stage = 0;
+    for (auto& sg : segs_small) {
+      sg.stage = stage;
+      stage += ((sg.dst_bit + sg.len + 63) >> 6) - (sg.dst_bit >> 6);
+    }
+    const uint64_t small_words = stage;
+    std::vector<uint64_t> edge_idx;  // staging words of the long runs' partial edge words
+    std::vector<std::array<uint64_t, 2>> edge_meta;
+    for (size_t i = 0; i < segs_big.size(); ++i) {
+      StageSeg& sg = segs_big[i];
+      sg.stage = stage;
+      const uint64_t words = ((sg.dst_bit + sg.len + 63) >> 6) - (sg.dst_bit >> 6);
+      if (sg.dst_bit & 63) {
+        edge_idx.push_back(stage);
+        edge_meta.push_back({meta_big[i][0], meta_big[i][1]});
+      }
+      if ((sg.dst_bit + sg.len) & 63) {
+        edge_idx.push_back(stage + words - 1);
+        edge_meta.push_back({meta_big[i][0], meta_big[i][1] + words - 1});
+      }
+      stage += words;
+    }
+    const uint64_t total = stage;
+    std::vector<StageSeg> segs(segs_small);
+    segs.insert(segs.end(), segs_big.begin(), segs_big.end());
+    const uint64_t back = small_words + edge_idx.size();  // words that come back to the host per piece
+    auto* d_stage = static_cast<uint64_t*>(ctx->grow("semi_stage", (total + back + 1) * 8));
+    auto* d_segs = static_cast<StageSeg*>(ctx->grow("semi_segs", std::max<size_t>(segs.size(), 1) * sizeof(StageSeg)));
+    auto* d_eidx = static_cast<uint64_t*>(ctx->grow("semi_eidx", std::max<size_t>(edge_idx.size(), 1) * 8));
+    CUDA_TRY(cudaMemcpyAsync(d_segs, segs.data(), segs.size() * sizeof(StageSeg), cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(d_eidx, edge_idx.data(), edge_idx.size() * 8, cudaMemcpyHostToDevice, s));
+    {
+      ProfScope ps(ctx, "semi_stage", total * 16);
+      launch_stage_segments(d_segs, segs.size(), d_stage, total, ctx->d_status, s, &ctx->launches);
+    }
+    // the long runs' edge words behind the short runs' words, one copy back
+    uint64_t* d_back = d_stage + total;
+    if (small_words) CUDA_TRY(cudaMemcpyAsync(d_back, d_stage, small_words * 8, cudaMemcpyDeviceToDevice, s));
+    launch_gather_words(d_stage, d_eidx, edge_idx.size(), d_back + small_words, s, &ctx->launches);
+    CUDA_TRY(cudaGetLastError());
+    auto* h_back = static_cast<uint64_t*>(small_host.get(std::max<uint64_t>(back, 1) * 8));
+    CUDA_TRY(cudaMemcpyAsync(h_back, d_back, back * 8, cudaMemcpyDeviceToHost, s));
+    // the long runs' whole words straight into the host arrays
+    for (size_t i = 0; i < segs_big.size(); ++i) {
+      const StageSeg& sg = segs_big[i];
+      const uint64_t words = ((sg.dst_bit + sg.len + 63) >> 6) - (sg.dst_bit >> 6);
+      const uint64_t j0 = (sg.dst_bit & 63) ? 1 : 0, j1 = words - (((sg.dst_bit + sg.len) & 63) ? 1 : 0);
+      uint64_t* h = outs[meta_big[i][0]].host + meta_big[i][1];
+      CUDA_TRY(cudaMemcpyAsync(h + j0, d_stage + sg.stage + j0, (j1 - j0) * 8, cudaMemcpyDeviceToHost, s));
+    }
+    CUDA_TRY(cudaStreamSynchronize(s));
+    check_device_status(ctx);
+    for (size_t i = 0; i < segs_small.size(); ++i) {
+      const StageSeg& sg = segs_small[i];
+      const uint64_t words = ((sg.dst_bit + sg.len + 63) >> 6) - (sg.dst_bit >> 6);
+      for (uint64_t j = 0; j < words; ++j) acc.push_back({meta_small[i][0], meta_small[i][1] + j, h_back[sg.stage + j]});
+    }
+    for (size_t e = 0; e < edge_idx.size(); ++e) acc.push_back({edge_meta[e][0], edge_meta[e][1], h_back[small_words + e]});
+  }
+  for (uint32_t l = 0; l < L; ++l)
+    if (placed[l] != cnt[l]) throw Fail{PWMGPU_ERR_CUDA, "internal: pieces do not add up to the text"};
+  // words shared by runs: OR of their parts; padding words past each level: zero
+  std::sort(acc.begin(), acc.end());
+  for (size_t i = 0; i < acc.size();) {
+    uint64_t v = 0;
+    size_t k = i;
+    for (; k < acc.size() && acc[k][0] == acc[i][0] && acc[k][1] == acc[i][1]; ++k) v |= acc[k][2];
+    outs[acc[i][0]].host[acc[i][1]] = v;
+    i = k;
+  }
+  for (const Out& o : outs)
+    for (uint32_t l = 0; l < L; ++l)
+      std::fill(o.host + uint64_t(l) * lw + words_for(n), o.host + uint64_t(l + 1) * lw, uint64_t(0));
+}
+
 constexpr uint32_t kMergeMaxLevels = 16;
 
 // pwm's merge_bit_vectors (merge.hpp:192-465) on the device: per level the
@@ -2127,6 +2339,21 @@ pwmgpu_status pwmgpu_wx_query_host(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int whi
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(out, d + 2 * count, count * 8, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
+    return PWMGPU_OK;
+  });
+}
+
+pwmgpu_status pwmgpu_compute_semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t size, uint32_t word_width,
+                                           uint32_t levels, uint64_t* wm_bv, uint64_t* wm_zeros, uint64_t* wt_bv,
+                                           uint64_t device_budget) {
+  if (!ctx || (size && !text) || (!wm_bv && !wt_bv)) return PWMGPU_ERR_ARG;
+  return guarded(ctx, [&]() {
+    validate_plain(size, word_width, levels);
+    if (size == 0) {
+      if (wm_zeros) std::memset(wm_zeros, 0, levels * 8);
+      return PWMGPU_OK;
+    }
+    semi_external(ctx, text, size, word_width, levels, wm_bv, wm_zeros, wt_bv, device_budget);
     return PWMGPU_OK;
   });
 }

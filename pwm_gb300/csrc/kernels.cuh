@@ -48,6 +48,21 @@ struct MergeSeg {
   uint64_t src_bit;
   const uint64_t* src;
 };
+
+// A bit range of a built piece bound for host arrays (semi-external builds):
+// `len` bits from bit `src_bit` of `src` go to bit `dst_bit` of a host level;
+// the destination words [dst_bit / 64, ceil((dst_bit + len) / 64)) are staged
+// from staging word `stage` on, bits outside the range zero.
+struct StageSeg {
+  const uint64_t* src;
+  uint64_t src_bit, dst_bit, len, stage;
+};
+// Segments sorted by `stage`; total: staging words (the end of the last).
+void launch_stage_segments(const StageSeg* segs, uint64_t nseg, uint64_t* staging, uint64_t total, uint32_t* status,
+                           cudaStream_t s, uint64_t* launches);
+// out[i] = words[idx[i]].
+void launch_gather_words(const uint64_t* words, const uint64_t* idx, uint64_t count, uint64_t* out, cudaStream_t s,
+                         uint64_t* launches);
 // pwm's copy_bits (merge.hpp:19-190) on 64-bit words: whole destination
 // words stored, the partial words at the ends OR-ed.
 void launch_copy_bits(uint64_t* dst, const uint64_t* src, uint64_t dst_off, uint64_t src_off, uint64_t len,

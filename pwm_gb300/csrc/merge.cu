@@ -101,7 +101,52 @@ __global__ void __launch_bounds__(256) merge_gather_kernel(const MergeSeg* segs,
   }
 }
 
+// Staging word w, thread per word: the segment whose staged words hold it
+// (binary search over the stage offsets), then its bits shifted into place.
+__global__ void stage_segments_kernel(const StageSeg* segs, uint64_t nseg, uint64_t* staging, uint64_t total,
+                                      uint32_t* status) {
+  for (uint64_t w = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; w < total;
+       w += uint64_t(gridDim.x) * blockDim.x) {
+    uint64_t lo = 0, hi = nseg;  // the last segment with stage <= w
+    while (hi - lo > 1) {
+      const uint64_t mid = (lo + hi) >> 1;
+      if (segs[mid].stage <= w) lo = mid; else hi = mid;
+    }
+    const StageSeg sg = segs[lo];
+    const uint64_t dw = (sg.dst_bit >> 6) + (w - sg.stage);
+    const uint64_t end = sg.dst_bit + sg.len;
+    const uint64_t b0 = dw * 64 > sg.dst_bit ? dw * 64 : sg.dst_bit, b1 = dw * 64 + 64 < end ? dw * 64 + 64 : end;
+    if (sg.stage > w || b0 >= b1) {  // inconsistent layout: never read out of range
+      atomicOr(status, kErrBounds);
+      staging[w] = 0;
+      continue;
+    }
+    staging[w] = bits_from(sg.src, sg.src_bit + (b0 - sg.dst_bit), uint32_t(b1 - b0)) >> (b0 - dw * 64);
+  }
+}
+
+__global__ void gather_words_kernel(const uint64_t* words, const uint64_t* idx, uint64_t count, uint64_t* out) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += uint64_t(gridDim.x) * blockDim.x)
+    out[i] = words[idx[i]];
+}
+
 }  // namespace
+
+void launch_stage_segments(const StageSeg* segs, uint64_t nseg, uint64_t* staging, uint64_t total, uint32_t* status,
+                           cudaStream_t s, uint64_t* launches) {
+  if (nseg == 0 || total == 0) return;
+  const uint64_t blocks = (total + 255) / 256;
+  stage_segments_kernel<<<unsigned(blocks < 65535 ? blocks : 65535), 256, 0, s>>>(segs, nseg, staging, total, status);
+  ++*launches;
+}
+
+void launch_gather_words(const uint64_t* words, const uint64_t* idx, uint64_t count, uint64_t* out, cudaStream_t s,
+                         uint64_t* launches) {
+  if (count == 0) return;
+  const uint64_t blocks = (count + 255) / 256;
+  gather_words_kernel<<<unsigned(blocks < 4096 ? blocks : 4096), 256, 0, s>>>(words, idx, count, out);
+  ++*launches;
+}
 
 void launch_copy_bits(uint64_t* dst, const uint64_t* src, uint64_t dst_off, uint64_t src_off, uint64_t len,
                       cudaStream_t s) {
