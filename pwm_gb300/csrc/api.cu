@@ -843,14 +843,16 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     }
   const bool stream_out = any_out && all_pinned;
   if (pinned_in || stream_out) ctx->xfer_init();
-  // the transfer streams are idle again when the build returns or throws
+  // the transfer streams this build uses are idle again when it returns or throws
   struct XferDrain {
     pwmgpu_ctx* c;
+    bool used;
     ~XferDrain() {
+      if (!used) return;
       if (c->up) cudaStreamSynchronize(c->up);
       if (c->down) cudaStreamSynchronize(c->down);
     }
-  } drain{ctx};
+  } drain{ctx, pinned_in || stream_out};
   if (io && io->text && !pinned_in)
     CUDA_TRY(cudaMemcpyAsync(const_cast<void*>(d_text), io->text, n * wx->width, cudaMemcpyHostToDevice, s));
   CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, 4, s));
@@ -1004,7 +1006,9 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
         bounds0.push_back(uint32_t(std::min<uint64_t>(p0.tiles, uint64_t(b) * first.tiles_per_block)));
     }
     next_in = enqueue_tile_pass(ctx, early, 0, d_b0, b0, d_text, wx->width, n, wx->wm, want_tree ? &wx->wt : nullptr,
-                                &first, bounds0, [&](size_t) { ev0.push_back(ctx->mark(s)); });
+                                &first, bounds0, [&](size_t) {
+                                  if (!blk0.empty()) ev0.push_back(ctx->mark(s));
+                                });
     from = 1;
   }
   CUDA_TRY(cudaEventSynchronize(ctx->hist_event()));
@@ -1737,24 +1741,65 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
     CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
     budget = free_b / 2;
   }
-  // device bytes per symbol of a piece: its text, the build's two key
-  // buffers, the shard's structures and the staging of the outputs
-  const double per_sym = 3.0 * width + (want_tree ? 2 : 1) * L / 8.0 + nout * L / 8.0 + 1.0;
+  // device bytes per symbol of a piece: two text buffers, the build's two
+  // key buffers, the shard's structures and two stagings of the outputs
+  const double per_sym = 4.0 * width + (want_tree ? 2 : 1) * L / 8.0 + 2.0 * nout * L / 8.0 + 1.0;
   uint64_t P = uint64_t(double(budget) / per_sym) & ~(kSemiMinPiece - 1);
   if (P < kSemiMinPiece) throw Fail{PWMGPU_ERR_ARG, "device budget below one piece of 2^16 symbols"};
   P = std::min(P, (n + kSemiMinPiece - 1) & ~(kSemiMinPiece - 1));
   const auto* txt = static_cast<const unsigned char*>(text);
-  auto* d_piece = static_cast<unsigned char*>(ctx->grow("semi_text", P * width));
-  // pass 1: the leaf histogram
+  ctx->xfer_init();
+  // every stream is idle again when this returns or throws (buffers below
+  // are freed then)
+  struct Drain {
+    pwmgpu_ctx* c;
+    ~Drain() {
+      cudaStreamSynchronize(c->up);
+      cudaStreamSynchronize(c->down);
+      cudaStreamSynchronize(c->stream);
+    }
+  };
+  // buffers owned here, double-buffered by piece parity
+  struct DevBuf2 {
+    void* p[2] = {nullptr, nullptr};
+    size_t bytes[2] = {0, 0};
+    bool pinned = false;
+    // grows buffer b; the caller has made sure no copy or kernel uses it
+    void* get(int b, size_t want) {
+      if (want > bytes[b]) {
+        if (p[b]) pinned ? cudaFreeHost(p[b]) : cudaFree(p[b]);
+        p[b] = nullptr;
+        bytes[b] = 0;
+        if (pinned) CUDA_TRY(cudaMallocHost(&p[b], want));
+        else CUDA_TRY(cudaMalloc(&p[b], want));
+        bytes[b] = want;
+      }
+      return p[b];
+    }
+    ~DevBuf2() {
+      for (int b = 0; b < 2; ++b)
+        if (p[b]) pinned ? cudaFreeHost(p[b]) : cudaFree(p[b]);
+    }
+  };
+  DevBuf2 pieces, stages, backs;
+  backs.pinned = true;
+  Drain drain{ctx};
+  for (int b = 0; b < 2; ++b) pieces.get(b, P * width);
+  // pass 1: the leaf histogram, uploads beside the counting
   const uint64_t bins = uint64_t(1) << L;
   auto* d_hist = static_cast<unsigned long long*>(ctx->grow("semi_hist", bins * 8));
   CUDA_TRY(cudaMemsetAsync(d_hist, 0, bins * 8, s));
   CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, 4, s));
-  for (uint64_t a = 0; a < n; a += P) {
+  cudaEvent_t used[2] = {nullptr, nullptr};  // the last work on s that read text buffer b
+  for (uint64_t a = 0, k = 0; a < n; a += P, ++k) {
+    const int b = int(k & 1);
     const uint64_t m = std::min(P, n - a);
-    CUDA_TRY(cudaMemcpyAsync(d_piece, txt + a * width, m * width, cudaMemcpyHostToDevice, s));
+    if (used[b]) CUDA_TRY(cudaStreamWaitEvent(ctx->up, used[b], 0));
+    CUDA_TRY(cudaMemcpyAsync(pieces.p[b], txt + a * width, m * width, cudaMemcpyHostToDevice, ctx->up));
+    CUDA_TRY(cudaStreamWaitEvent(s, ctx->mark(ctx->up), 0));
     ProfScope ps(ctx, "leaf_histogram", m * width);
-    launch_leaf_histogram(d_piece, m, width, L, d_hist, ctx->d_status, s, &ctx->launches);
+    launch_leaf_histogram(pieces.p[b], m, width, L, d_hist, ctx->d_status, s, &ctx->launches);
+    used[b] = ctx->mark(s);
   }
   std::vector<uint64_t> hist(bins);
   CUDA_TRY(cudaMemcpyAsync(hist.data(), d_hist, bins * 8, cudaMemcpyDeviceToHost, s));
@@ -1776,7 +1821,7 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
     return st;
   };
   struct Out {
-    int st;             // 0 matrix, 1 tree
+    int st;  // 0 matrix, 1 tree
     uint64_t* host;
     std::vector<std::vector<uint64_t>> gstart;
   };
@@ -1788,124 +1833,151 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
   std::vector<std::vector<uint64_t>> placed(L);  // per level and prefix: bits earlier pieces placed
   for (uint32_t l = 0; l < L; ++l) placed[l].assign(cnt[l].size(), 0);
   const uint64_t lw = padded_words(n);  // words per level of the host arrays
-  // pass 2
+  // A piece's runs bound for the host: short ones first in the staging, then
+  // the long ones, whose partial edge words are gathered behind the short
+  // runs' words so that one copy brings back everything the host ORs.
+  struct PieceOut {
+    std::vector<StageSeg> segs;                  // short runs, then long runs
+    std::vector<std::array<uint64_t, 2>> meta;   // per run: (output, first absolute word)
+    size_t nsmall = 0;
+    uint64_t small_words = 0, total = 0;
+    std::vector<uint64_t> edge_idx;              // staging words of the long runs' partial edges
+    std::vector<std::array<uint64_t, 2>> edge_meta;
+    cudaEvent_t done = nullptr;                  // its copies back have finished
+    bool pending = false;
+  };
+  PieceOut po[2];
   std::vector<std::array<uint64_t, 3>> acc;  // (output, word, bits) OR-ed at the end
-  struct Pinned {
-    void* p = nullptr;
-    size_t bytes = 0;
-    void* get(size_t b) {
-      if (b > bytes) {
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        bytes = 0;
-        CUDA_TRY(cudaMallocHost(&p, b));
-        bytes = b;
-      }
-      return p;
+  auto collect = [&](PieceOut& q, int b) {   // the host's share of a piece, once its copies are back
+    if (!q.pending) return;
+    CUDA_TRY(cudaEventSynchronize(q.done));
+    const auto* h_back = static_cast<const uint64_t*>(backs.p[b]);
+    for (size_t i = 0; i < q.nsmall; ++i) {
+      const StageSeg& sg = q.segs[i];
+      const uint64_t words = ((sg.dst_bit + sg.len + 63) >> 6) - (sg.dst_bit >> 6);
+      for (uint64_t j = 0; j < words; ++j) acc.push_back({q.meta[i][0], q.meta[i][1] + j, h_back[sg.stage + j]});
     }
-    ~Pinned() {
-      if (p) cudaFreeHost(p);
-    }
-  } small_host;
+    for (size_t e = 0; e < q.edge_idx.size(); ++e)
+      acc.push_back({q.edge_meta[e][0], q.edge_meta[e][1], h_back[q.small_words + e]});
+    q.pending = false;
+  };
+  // pass 2: piece k uploads (up) while piece k-1 builds (s) and piece k-2's
+  // words go back (down); the host ORs piece k-1's share meanwhile
   std::unique_ptr<pwmgpu_wx> shard;
-  for (uint64_t a = 0; a < n; a += P) {
+  for (int b = 0; b < 2; ++b) used[b] = nullptr;
+  cudaEvent_t uploaded[2] = {nullptr, nullptr};
+  auto upload = [&](uint64_t a, int b) {  // into text buffer b once the build that read it is done
+    if (used[b]) CUDA_TRY(cudaStreamWaitEvent(ctx->up, used[b], 0));
+    CUDA_TRY(cudaMemcpyAsync(pieces.p[b], txt + a * width, std::min(P, n - a) * width, cudaMemcpyHostToDevice,
+                             ctx->up));
+    uploaded[b] = ctx->mark(ctx->up);
+  };
+  upload(0, 0);
+  for (uint64_t a = 0, k = 0; a < n; a += P, ++k) {
+    const int b = int(k & 1);
     const uint64_t m = std::min(P, n - a);
+    CUDA_TRY(cudaStreamWaitEvent(s, uploaded[b], 0));
     if (!shard || shard->n != m) {
+      if (shard) CUDA_TRY(cudaStreamSynchronize(s));
       shard.reset();
       shard = make_wx(ctx, m, width, L, (out_wm ? PWMGPU_MATRIX : 0u) | (want_tree ? PWMGPU_TREE : 0u) |
                                            PWMGPU_KEEP_HISTOGRAM);
     }
-    CUDA_TRY(cudaMemcpyAsync(d_piece, txt + a * width, m * width, cudaMemcpyHostToDevice, s));
-    build_plain(ctx, shard.get(), d_piece);
+    build_plain(ctx, shard.get(), pieces.p[b]);
     const auto pc = fold_prefix_counts(shard->hist.data(), L);
-    // the piece's runs: short ones first, then the long ones (their edge
-    // words are gathered behind the short runs' words)
-    std::vector<StageSeg> segs_small, segs_big;
-    std::vector<std::array<uint64_t, 2>> meta_small, meta_big;  // (output, first absolute destination word)
+    PieceOut& q = po[b];
+    collect(q, b);  // piece k-2 (its buffers are reused now)
+    q = PieceOut{};
+    std::vector<StageSeg> big;
+    std::vector<std::array<uint64_t, 2>> big_meta;
     for (size_t oi = 0; oi < outs.size(); ++oi) {
       const Out& o = outs[oi];
       const Structure& S = o.st ? shard->wt : shard->wm;
       for (uint32_t l = 0; l < L; ++l) {
         const auto ls = starts(pc[l], l, o.st == 1);
-        for (uint64_t q = 0; q < pc[l].size(); ++q) {
-          const uint64_t c = pc[l][q];
+        for (uint64_t x = 0; x < pc[l].size(); ++x) {
+          const uint64_t c = pc[l][x];
           if (!c) continue;
-          const uint64_t dst = o.gstart[l][q] + placed[l][q];
-          StageSeg sg{S.d_words + S.offs[l], ls[q], dst, c, 0};
+          const uint64_t dst = o.gstart[l][x] + placed[l][x];
+          const StageSeg sg{S.d_words + S.offs[l], ls[x], dst, c, 0};
           const uint64_t words = ((dst + c + 63) >> 6) - (dst >> 6);
           const uint64_t edges = ((dst & 63) ? 1 : 0) + (((dst + c) & 63) ? 1 : 0);
           const std::array<uint64_t, 2> mt{uint64_t(oi), uint64_t(l) * lw + (dst >> 6)};
           if (words >= edges + kSemiDmaMinWords) {
-            segs_big.push_back(sg);
-            meta_big.push_back(mt);
+            big.push_back(sg);
+            big_meta.push_back(mt);
           } else {
-            segs_small.push_back(sg);
-            meta_small.push_back(mt);
+            q.segs.push_back(sg);
+            q.meta.push_back(mt);
           }
         }
       }
     }
     for (uint32_t l = 0; l < L; ++l)
-      for (uint64_t q = 0; q < pc[l].size(); ++q) placed[l][q] += pc[l][q];
+      for (uint64_t x = 0; x < pc[l].size(); ++x) placed[l][x] += pc[l][x];
+    q.nsmall = q.segs.size();
     uint64_t stage = 0;
-    for (auto& sg : segs_small) {
+    for (auto& sg : q.segs) {
       sg.stage = stage;
       stage += ((sg.dst_bit + sg.len + 63) >> 6) - (sg.dst_bit >> 6);
     }
-    const uint64_t small_words = stage;
-    std::vector<uint64_t> edge_idx;  // staging words of the long runs' partial edge words
-    std::vector<std::array<uint64_t, 2>> edge_meta;
-    for (size_t i = 0; i < segs_big.size(); ++i) {
-      StageSeg& sg = segs_big[i];
+    q.small_words = stage;
+    for (size_t i = 0; i < big.size(); ++i) {
+      StageSeg sg = big[i];
       sg.stage = stage;
       const uint64_t words = ((sg.dst_bit + sg.len + 63) >> 6) - (sg.dst_bit >> 6);
       if (sg.dst_bit & 63) {
-        edge_idx.push_back(stage);
-        edge_meta.push_back({meta_big[i][0], meta_big[i][1]});
+        q.edge_idx.push_back(stage);
+        q.edge_meta.push_back(big_meta[i]);
       }
       if ((sg.dst_bit + sg.len) & 63) {
-        edge_idx.push_back(stage + words - 1);
-        edge_meta.push_back({meta_big[i][0], meta_big[i][1] + words - 1});
+        q.edge_idx.push_back(stage + words - 1);
+        q.edge_meta.push_back({big_meta[i][0], big_meta[i][1] + words - 1});
       }
+      q.segs.push_back(sg);
+      q.meta.push_back(big_meta[i]);
       stage += words;
     }
-    const uint64_t total = stage;
-    std::vector<StageSeg> segs(segs_small);
-    segs.insert(segs.end(), segs_big.begin(), segs_big.end());
-    const uint64_t back = small_words + edge_idx.size();  // words that come back to the host per piece
-    auto* d_stage = static_cast<uint64_t*>(ctx->grow("semi_stage", (total + back + 1) * 8));
-    auto* d_segs = static_cast<StageSeg*>(ctx->grow("semi_segs", std::max<size_t>(segs.size(), 1) * sizeof(StageSeg)));
-    auto* d_eidx = static_cast<uint64_t*>(ctx->grow("semi_eidx", std::max<size_t>(edge_idx.size(), 1) * 8));
-    CUDA_TRY(cudaMemcpyAsync(d_segs, segs.data(), segs.size() * sizeof(StageSeg), cudaMemcpyHostToDevice, s));
-    CUDA_TRY(cudaMemcpyAsync(d_eidx, edge_idx.data(), edge_idx.size() * 8, cudaMemcpyHostToDevice, s));
+    q.total = stage;
+    const uint64_t back = q.small_words + q.edge_idx.size();  // words the host ORs
+    // staging b and its return buffer were last read by piece k-2's copies,
+    // collected above; the segment tables go in front of the staged words
+    const size_t seg_bytes = (q.segs.size() * sizeof(StageSeg) + 15) & ~size_t(15);
+    const size_t idx_bytes = (q.edge_idx.size() * 8 + 15) & ~size_t(15);
+    auto* base = static_cast<unsigned char*>(stages.get(b, seg_bytes + idx_bytes + (q.total + back + 1) * 8));
+    auto* d_segs = reinterpret_cast<StageSeg*>(base);
+    auto* d_eidx = reinterpret_cast<uint64_t*>(base + seg_bytes);
+    auto* d_stage = reinterpret_cast<uint64_t*>(base + seg_bytes + idx_bytes);
+    auto* h_back = static_cast<uint64_t*>(backs.get(b, std::max<uint64_t>(back, 1) * 8));
+    CUDA_TRY(cudaMemcpyAsync(d_segs, q.segs.data(), q.segs.size() * sizeof(StageSeg), cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(d_eidx, q.edge_idx.data(), q.edge_idx.size() * 8, cudaMemcpyHostToDevice, s));
     {
-      ProfScope ps(ctx, "semi_stage", total * 16);
-      launch_stage_segments(d_segs, segs.size(), d_stage, total, ctx->d_status, s, &ctx->launches);
+      ProfScope ps(ctx, "semi_stage", q.total * 16);
+      launch_stage_segments(d_segs, q.segs.size(), d_stage, q.total, ctx->d_status, s, &ctx->launches);
     }
-    // the long runs' edge words behind the short runs' words, one copy back
-    uint64_t* d_back = d_stage + total;
-    if (small_words) CUDA_TRY(cudaMemcpyAsync(d_back, d_stage, small_words * 8, cudaMemcpyDeviceToDevice, s));
-    launch_gather_words(d_stage, d_eidx, edge_idx.size(), d_back + small_words, s, &ctx->launches);
+    uint64_t* d_back = d_stage + q.total;
+    if (q.small_words)
+      CUDA_TRY(cudaMemcpyAsync(d_back, d_stage, q.small_words * 8, cudaMemcpyDeviceToDevice, s));
+    launch_gather_words(d_stage, d_eidx, q.edge_idx.size(), d_back + q.small_words, s, &ctx->launches);
     CUDA_TRY(cudaGetLastError());
-    auto* h_back = static_cast<uint64_t*>(small_host.get(std::max<uint64_t>(back, 1) * 8));
-    CUDA_TRY(cudaMemcpyAsync(h_back, d_back, back * 8, cudaMemcpyDeviceToHost, s));
-    // the long runs' whole words straight into the host arrays
-    for (size_t i = 0; i < segs_big.size(); ++i) {
-      const StageSeg& sg = segs_big[i];
+    used[b] = ctx->mark(s);  // the build read text buffer b; the staging is complete
+    CUDA_TRY(cudaStreamWaitEvent(ctx->down, used[b], 0));
+    CUDA_TRY(cudaMemcpyAsync(h_back, d_back, back * 8, cudaMemcpyDeviceToHost, ctx->down));
+    for (size_t i = q.nsmall; i < q.segs.size(); ++i) {  // the long runs' whole words into the host arrays
+      const StageSeg& sg = q.segs[i];
       const uint64_t words = ((sg.dst_bit + sg.len + 63) >> 6) - (sg.dst_bit >> 6);
       const uint64_t j0 = (sg.dst_bit & 63) ? 1 : 0, j1 = words - (((sg.dst_bit + sg.len) & 63) ? 1 : 0);
-      uint64_t* h = outs[meta_big[i][0]].host + meta_big[i][1];
-      CUDA_TRY(cudaMemcpyAsync(h + j0, d_stage + sg.stage + j0, (j1 - j0) * 8, cudaMemcpyDeviceToHost, s));
+      uint64_t* h = outs[q.meta[i][0]].host + q.meta[i][1];
+      CUDA_TRY(cudaMemcpyAsync(h + j0, d_stage + sg.stage + j0, (j1 - j0) * 8, cudaMemcpyDeviceToHost, ctx->down));
     }
-    CUDA_TRY(cudaStreamSynchronize(s));
-    check_device_status(ctx);
-    for (size_t i = 0; i < segs_small.size(); ++i) {
-      const StageSeg& sg = segs_small[i];
-      const uint64_t words = ((sg.dst_bit + sg.len + 63) >> 6) - (sg.dst_bit >> 6);
-      for (uint64_t j = 0; j < words; ++j) acc.push_back({meta_small[i][0], meta_small[i][1] + j, h_back[sg.stage + j]});
-    }
-    for (size_t e = 0; e < edge_idx.size(); ++e) acc.push_back({edge_meta[e][0], edge_meta[e][1], h_back[small_words + e]});
+    q.done = ctx->mark(ctx->down);
+    q.pending = true;
+    if (a + P < n) upload(a + P, b ^ 1);  // piece k+1 goes up beside piece k's copies back
+    collect(po[b ^ 1], b ^ 1);  // piece k-1, while piece k runs
   }
+  collect(po[0], 0);
+  collect(po[1], 1);
+  check_device_status(ctx);
   for (uint32_t l = 0; l < L; ++l)
     if (placed[l] != cnt[l]) throw Fail{PWMGPU_ERR_CUDA, "internal: pieces do not add up to the text"};
   // words shared by runs: OR of their parts; padding words past each level: zero

@@ -101,7 +101,7 @@ def test_semi_external_edges(pg, orc):
     torch_cuda()
     # one symbol, a text shorter than a piece, an empty text
     for text, L in ((np.full(300_000, 3, np.uint8), 2), (np.arange(1000, dtype=np.uint16) % 977, 10)):
-        wm, zeros, wt = pg.compute_semi_external(text, L, device_budget=MiB)
+        wm, zeros, wt = pg.compute_semi_external(text, L, device_budget=4 * MiB)
         check(orc, text, L, wm, zeros, wt)
     wm, zeros, wt = pg.compute_semi_external(np.zeros(0, np.uint8), 4, device_budget=MiB)
     assert not zeros.any()
