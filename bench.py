@@ -263,6 +263,19 @@ def other_workloads(torch, pg, ctx, reps=3):
     timed("zipf_2p30_levels8_16_shards", 1 << 30, 1, 8, pg.GEN_ZIPF256, 0, True, False, shards=16)
     t16 = timed("mix16_2p28_levels16", 1 << 28, 2, 16, pg.GEN_MIX16, 0, True, False)
     timed("uniform20_2p26_levels20", 1 << 26, 4, 20, pg.GEN_UNIFORM, 1 << 20, False, True)
+    # pwm's reduce_alphabet on the device (the 2^28 16-bit text; histogram,
+    # first occurrences, host ranking of the symbols, remap): wall time
+    out16 = torch.empty_like(t16)
+    pg.reduce_alphabet(t16.data_ptr(), t16.numel(), 2, out16.data_ptr(), context=ctx)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        max_char = pg.reduce_alphabet(t16.data_ptr(), t16.numel(), 2, out16.data_ptr(), context=ctx)
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) / reps * 1e3
+    out["alphabet_reduction_mix16_2p28"] = {"n": int(t16.numel()), "word_width": 2, "distinct_symbols": max_char + 1,
+                                            "ms": ms, "text_gbs": t16.numel() * 2 / ms / 1e6}
+    del out16
     host16 = t16.cpu().numpy().view(np.uint16)
     del t16
     for tree in (False, True):

@@ -213,6 +213,15 @@ PWMGPU_API pwmgpu_status pwmgpu_wx_query(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, i
  * returns when out[] holds the answers. */
 PWMGPU_API pwmgpu_status pwmgpu_wx_query_host(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which, int op,
                                               const uint64_t* a, const uint64_t* b, uint64_t count, uint64_t* out);
+/* pwm's reduce_alphabet (include/util/alphabet_util.hpp:18-45) on the
+ * device: the symbols of d_text renumbered 0, 1, ... in order of first
+ * occurrence into d_out (same width; d_out == d_text allowed); *max_char
+ * receives the number of distinct symbols - 1, what pwm returns (all ones
+ * for an empty text).  8-bit symbol 255 is renumbered like any other (pwm's
+ * table stops at 254).  32-bit texts: symbols below 2^24. */
+PWMGPU_API pwmgpu_status pwmgpu_reduce_alphabet(pwmgpu_ctx* ctx, const void* d_text, uint64_t size, uint32_t word_width,
+                                                void* d_out, uint64_t* max_char);
+
 /* Semi-external construction of a host text larger than the device memory
  * (pwm's semi_in, include/external_memory/semi_in/pc_semi_external.hpp:16-230,
  * which reads its text twice).  The text streams through the GPU in pieces

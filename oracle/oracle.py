@@ -120,6 +120,21 @@ class Oracle:
         L.orc_copy_bits_u8.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]
         L.orc_copy_bits_u64.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]
 
+    @staticmethod
+    def reduce_alphabet(text):
+        """pwm's reduce_alphabet (include/util/alphabet_util.hpp:18-45): the
+        symbols renumbered 0, 1, ... in order of first occurrence; returns
+        (renumbered text, distinct symbols - 1), the latter all ones (0 - 1
+        in uint64) for an empty text.  Parity unpinned: the reference header
+        includes STXXL and does not compile here."""
+        t = np.asarray(text)
+        if t.size == 0:
+            return t.copy(), (1 << 64) - 1
+        syms, first = np.unique(t, return_index=True)
+        rank = np.empty(syms.size, dtype=np.uint64)
+        rank[np.argsort(first, kind="stable")] = np.arange(syms.size, dtype=np.uint64)
+        return rank[np.searchsorted(syms, t)].astype(t.dtype), syms.size - 1
+
     def copy_bits(self, dst, src, dst_off, src_off, length):
         """pwm's copy_bits (merge.hpp:19-190) on numpy arrays of uint8 or
         uint64 words; dst is updated in place."""

@@ -262,6 +262,18 @@ def huffman_codes(text, is_tree, context=None):
     return ln[:nc.value].copy(), wd[:nc.value].copy(), sizes[:lv.value].copy(), lv.value
 
 
+def reduce_alphabet(d_text_ptr, size, word_width, d_out_ptr=None, context=None):
+    """pwm's reduce_alphabet on a device text (pwmgpu_reduce_alphabet):
+    symbols renumbered by first occurrence into d_out_ptr (default: in
+    place); returns max_char = distinct symbols - 1."""
+    ctx = context or default_context()
+    mc = ctypes.c_uint64(0)
+    out = d_text_ptr if d_out_ptr is None else d_out_ptr
+    ctx.check(ctx.lib.pwmgpu_reduce_alphabet(ctx.h, ctypes.c_void_p(int(d_text_ptr)), int(size), int(word_width),
+                                             ctypes.c_void_p(int(out)), ctypes.byref(mc)))
+    return mc.value
+
+
 def compute_semi_external(text, levels, matrix=True, tree=True, device_budget=0, context=None, out=None):
     """Semi-external build of a host text (pwmgpu_compute_semi_external):
     the text streams through the GPU in pieces within about device_budget

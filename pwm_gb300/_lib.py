@@ -68,6 +68,7 @@ SIGNATURES = {
     "pwmgpu_wx_build_huffman": (i32, [vp, vp, u64, u32, u32, u64p, u64p, u64, ctypes.POINTER(vp)]),
     "pwmgpu_wx_codes": (i32, [vp, u64p, u64p, u64, u64p]),
     "pwmgpu_compute_semi_external": (i32, [vp, vp, u64, u32, u32, u64p, u64p, u64p, u64]),
+    "pwmgpu_reduce_alphabet": (i32, [vp, vp, u64, u32, vp, u64p]),
     "pwmgpu_compute": (i32, [vp, vp, u64, u32, u32, i32, u64p, u64p]),
     "pwmgpu_huffman_codes": (i32, [vp, vp, u64, u32, i32, u64p, u64p, u64, u64p, u64p, u32p]),
     "pwmgpu_compute_huffman": (i32, [vp, vp, u64, u32, i32, u64p, u64p, u64, u32, u64p, u64p, u64p]),

@@ -1729,6 +1729,7 @@ std::unique_ptr<pwmgpu_wx> make_wx(pwmgpu_ctx* ctx, uint64_t size, uint32_t word
 // and are OR-ed together on the host at the end.
 // ---------------------------------------------------------------------------
 constexpr uint64_t kSemiMinPiece = uint64_t(1) << 16;
+constexpr uint64_t kAlphabetMaxSymbol = uint64_t(1) << 24;  // 32-bit alphabet reduction: one bin per value
 constexpr uint64_t kSemiDmaMinWords = 512;  // shorter runs go through the host's OR
 
 void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width, uint32_t L, uint64_t* out_wm,
@@ -2411,6 +2412,54 @@ pwmgpu_status pwmgpu_wx_query_host(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int whi
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(out, d + 2 * count, count * 8, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
+    return PWMGPU_OK;
+  });
+}
+
+pwmgpu_status pwmgpu_reduce_alphabet(pwmgpu_ctx* ctx, const void* d_text, uint64_t size, uint32_t word_width,
+                                     void* d_out, uint64_t* max_char) {
+  if (!ctx || !max_char || (size && (!d_text || !d_out))) return PWMGPU_ERR_ARG;
+  return guarded(ctx, [&]() {
+    if (!valid_width(word_width)) throw Fail{PWMGPU_ERR_ARG, "word_width must be 1, 2 or 4"};
+    *max_char = ~uint64_t(0);  // pwm: no symbol, 0 - 1
+    if (size == 0) return PWMGPU_OK;
+    cudaStream_t s = ctx->stream;
+    CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, 4, s));
+    uint64_t nsym = word_width == 1 ? 256 : 65536;
+    if (word_width == 4) {
+      auto* d_max = static_cast<unsigned int*>(ctx->grow("alpha_max", 4));
+      CUDA_TRY(cudaMemsetAsync(d_max, 0, 4, s));
+      launch_max_symbol(static_cast<const uint32_t*>(d_text), size, d_max, s, &ctx->launches);
+      unsigned int mx = 0;
+      CUDA_TRY(cudaMemcpyAsync(&mx, d_max, 4, cudaMemcpyDeviceToHost, s));
+      CUDA_TRY(cudaStreamSynchronize(s));
+      if (mx >= kAlphabetMaxSymbol) throw Fail{PWMGPU_ERR_ARG, "32-bit symbols must be below 2^24"};
+      nsym = uint64_t(mx) + 1;
+    }
+    // symbol counts and first occurrences, then ids in order of first occurrence
+    auto* d_hist = static_cast<unsigned long long*>(ctx->grow("sym_hist", nsym * 8));
+    auto* d_first = static_cast<unsigned long long*>(ctx->grow("sym_first", nsym * 8));
+    CUDA_TRY(cudaMemsetAsync(d_hist, 0, nsym * 8, s));
+    CUDA_TRY(cudaMemsetAsync(d_first, 0xFF, nsym * 8, s));
+    {
+      ProfScope ps(ctx, "symbol_histogram", size * word_width);
+      launch_symbol_histogram(d_text, size, word_width, nsym, d_hist, d_first, ctx->d_status, s, &ctx->launches);
+    }
+    std::vector<uint64_t> count(nsym), first(nsym);
+    CUDA_TRY(cudaMemcpyAsync(count.data(), d_hist, nsym * 8, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(first.data(), d_first, nsym * 8, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    std::vector<uint32_t> present;
+    for (uint64_t c = 0; c < nsym; ++c)
+      if (count[c]) present.push_back(uint32_t(c));
+    std::sort(present.begin(), present.end(), [&](uint32_t a, uint32_t b) { return first[a] < first[b]; });
+    std::vector<uint32_t> map(nsym, 0);
+    for (size_t i = 0; i < present.size(); ++i) map[present[i]] = uint32_t(i);
+    auto* d_map = static_cast<uint32_t*>(ctx->grow("alpha_map", nsym * 4));
+    CUDA_TRY(cudaMemcpyAsync(d_map, map.data(), nsym * 4, cudaMemcpyHostToDevice, s));
+    launch_remap(d_text, size, word_width, d_map, nsym, d_out, ctx->d_status, s, &ctx->launches);
+    check_device_status(ctx);  // also: the map's pageable copy has been read
+    *max_char = present.size() - 1;
     return PWMGPU_OK;
   });
 }

@@ -523,6 +523,32 @@ __global__ void symbol_hist_kernel(const T* text, uint64_t n, uint64_t nsym, uns
   }
 }
 
+// Largest symbol of a 32-bit text (warp maxima, one atomic per warp).
+__global__ void max_symbol_kernel(const uint32_t* text, uint64_t n, unsigned int* out) {
+  uint32_t m = 0;
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+    m = max(m, text[i]);
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) m = max(m, __shfl_xor_sync(0xFFFFFFFFu, m, d));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// out[i] = map[text[i]] (pwm's reduce_alphabet renumbering); symbols past the
+// map set the status and write 0.
+template <typename T>
+__global__ void remap_kernel(const T* text, uint64_t n, const uint32_t* map, uint64_t nmap, T* out,
+                             uint32_t* status) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    const uint64_t c = uint64_t(text[i]);
+    if (c < nmap) {
+      out[i] = T(map[c]);
+    } else {
+      atomicOr(status, kErrSymbol);
+      out[i] = T(0);
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Generators (gen.cuh)
 // ---------------------------------------------------------------------------
@@ -629,6 +655,27 @@ void launch_symbol_histogram(const void* text, uint64_t n, uint32_t width, uint6
     return;
   }
   symbol_hist_kernel<<<g, 256, 0, s>>>(static_cast<const uint32_t*>(text), n, nsym, hist, first);
+  ++*launches;
+}
+
+void launch_max_symbol(const uint32_t* text, uint64_t n, unsigned int* out, cudaStream_t s, uint64_t* launches) {
+  if (n == 0) return;
+  max_symbol_kernel<<<grid_for(n, 256), 256, 0, s>>>(text, n, out);
+  ++*launches;
+}
+
+void launch_remap(const void* text, uint64_t n, uint32_t width, const uint32_t* map, uint64_t nmap, void* out,
+                  uint32_t* status, cudaStream_t s, uint64_t* launches) {
+  if (n == 0) return;
+  const int g = grid_for(n, 256);
+  if (width == 1)
+    remap_kernel<<<g, 256, 0, s>>>(static_cast<const uint8_t*>(text), n, map, nmap, static_cast<uint8_t*>(out), status);
+  else if (width == 2)
+    remap_kernel<<<g, 256, 0, s>>>(static_cast<const uint16_t*>(text), n, map, nmap, static_cast<uint16_t*>(out),
+                                   status);
+  else
+    remap_kernel<<<g, 256, 0, s>>>(static_cast<const uint32_t*>(text), n, map, nmap, static_cast<uint32_t*>(out),
+                                   status);
   ++*launches;
 }
 

@@ -26,6 +26,11 @@ void launch_leaf_histogram(const void* text, uint64_t n, uint32_t width, uint32_
 // hist must be zeroed.  launch_tile_block_scan then turns blocksum into each
 // block's exclusive prefix.
 uint32_t tile_hist_tiles_per_block();
+// Largest symbol of a 32-bit text into *out (zeroed by the caller).
+void launch_max_symbol(const uint32_t* text, uint64_t n, unsigned int* out, cudaStream_t s, uint64_t* launches);
+// out[i] = map[text[i]] (same width; in place allowed).
+void launch_remap(const void* text, uint64_t n, uint32_t width, const uint32_t* map, uint64_t nmap, void* out,
+                  uint32_t* status, cudaStream_t s, uint64_t* launches);
 uint32_t tile_hist_blocks(uint64_t n, uint32_t tile_keys);
 void launch_tile_histogram_blocks(const void* text, uint64_t n, uint32_t width, uint32_t levels, uint32_t D,
                                   uint32_t tile_keys, uint32_t block0, uint32_t nblk, unsigned long long* hist,
