@@ -123,6 +123,11 @@ PWMGPU_API pwmgpu_status pwmgpu_ctx_set_upload_piece_bytes(pwmgpu_ctx* ctx, uint
  * chunks run; 1 launches each pass whole and streams level groups per pass. */
 PWMGPU_API pwmgpu_status pwmgpu_ctx_set_stream_chunks(pwmgpu_ctx* ctx, uint32_t chunks);
 
+/* Frees what the context keeps between calls (scratch buffers, cached shard
+ * structures of sharded and semi-external builds, pinned staging) after its
+ * streams finish; later calls allocate again. */
+PWMGPU_API pwmgpu_status pwmgpu_ctx_release_scratch(pwmgpu_ctx* ctx);
+
 /* ---------------------------------------------------------------------- */
 /* Drop-in construction (host text in, host bit vectors out)               */
 /* ---------------------------------------------------------------------- */
@@ -231,7 +236,9 @@ PWMGPU_API pwmgpu_status pwmgpu_reduce_alphabet(pwmgpu_ctx* ctx, const void* d_t
  * NULL, not both) receive the structures in the layout of
  * pwmgpu_wx_download (levels of round_up(ceil(size/64), 16) words),
  * wm_zeros (may be NULL) the matrix zeros.  The result equals a plain
- * build's bit for bit.  The budget must hold a piece of 2^16 symbols. */
+ * build's bit for bit.  The budget must hold a piece of 2^16 symbols.  The
+ * context keeps the piece buffers for the next call (pwmgpu_ctx_release_scratch
+ * frees them). */
 PWMGPU_API pwmgpu_status pwmgpu_compute_semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t size,
                                                       uint32_t word_width, uint32_t levels, uint64_t* wm_bv,
                                                       uint64_t* wm_zeros, uint64_t* wt_bv, uint64_t device_budget);

@@ -81,6 +81,10 @@ class Context:
         """Piece size of pinned host-text uploads (default 64 MiB)."""
         self.check(self.lib.pwmgpu_ctx_set_upload_piece_bytes(self.h, int(nbytes)))
 
+    def release_scratch(self):
+        """Frees the buffers and cached structures the context keeps between calls."""
+        self.check(self.lib.pwmgpu_ctx_release_scratch(self.h))
+
     def set_stream_chunks(self, chunks):
         """Chunks of the passes whose words stream to pinned outputs (1..16, default 4)."""
         self.check(self.lib.pwmgpu_ctx_set_stream_chunks(self.h, int(chunks)))

@@ -77,6 +77,7 @@ struct pwmgpu_ctx {
   uint64_t scratch_bytes = 0;
   pwmgpu_wx* compute_cache = nullptr;  // reused by pwmgpu_compute for equal shapes
   std::vector<std::unique_ptr<pwmgpu_wx>> shard_cache;  // reused by pwmgpu_wx_build_sharded
+  std::unique_ptr<pwmgpu_wx> semi_shard[2];             // semi-external pieces: full-size and last
   // CUDA-event timing of every launch group while profiling is on
   bool profiling = false;
   std::vector<ProfRecord> prof;
@@ -107,6 +108,29 @@ struct pwmgpu_ctx {
       pinned_bytes = bytes;
     }
     return pinned;
+  }
+
+  // Grow-only named pinned host buffers (contents undefined); the caller
+  // makes sure no copy uses one that grows.
+  std::map<std::string, std::pair<void*, size_t>> pinned_named;
+  void* grow_pinned_named(const std::string& name, size_t bytes) {
+    auto& b = pinned_named[name];
+    if (b.second < bytes) {
+      if (b.first) CUDA_TRY(cudaFreeHost(b.first));
+      b.first = nullptr;
+      b.second = 0;
+      CUDA_TRY(cudaMallocHost(&b.first, bytes));
+      b.second = bytes;
+    }
+    return b.first;
+  }
+  void release_pinned() {
+    if (pinned) cudaFreeHost(pinned);
+    pinned = nullptr;
+    pinned_bytes = 0;
+    for (auto& kv : pinned_named)
+      if (kv.second.first) cudaFreeHost(kv.second.first);
+    pinned_named.clear();
   }
 
   // Grow-only named scratch buffer (contents undefined).
@@ -253,6 +277,8 @@ pwmgpu_ctx::~pwmgpu_ctx() {
   cudaSetDevice(device);
   delete compute_cache;
   shard_cache.clear();  // structures free on the context's stream: before it goes
+  semi_shard[0].reset();
+  semi_shard[1].reset();
   for (auto& r : prof) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto e : event_pool) cudaEventDestroy(e);
   if (async_alloc && stream) cudaStreamSynchronize(stream);
@@ -263,7 +289,9 @@ pwmgpu_ctx::~pwmgpu_ctx() {
     }
   if (async_alloc && stream) cudaStreamSynchronize(stream);
   if (d_status) cudaFree(d_status);
-  if (pinned) cudaFreeHost(pinned);
+  for (cudaStream_t t : {up, down, side})
+    if (t) cudaStreamSynchronize(t);
+  release_pinned();
   for (cudaStream_t t : {up, down, side})
     if (t) {
       cudaStreamSynchronize(t);
@@ -1760,32 +1788,15 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
       cudaStreamSynchronize(c->stream);
     }
   };
-  // buffers owned here, double-buffered by piece parity
-  struct DevBuf2 {
-    void* p[2] = {nullptr, nullptr};
-    size_t bytes[2] = {0, 0};
-    bool pinned = false;
-    // grows buffer b; the caller has made sure no copy or kernel uses it
-    void* get(int b, size_t want) {
-      if (want > bytes[b]) {
-        if (p[b]) pinned ? cudaFreeHost(p[b]) : cudaFree(p[b]);
-        p[b] = nullptr;
-        bytes[b] = 0;
-        if (pinned) CUDA_TRY(cudaMallocHost(&p[b], want));
-        else CUDA_TRY(cudaMalloc(&p[b], want));
-        bytes[b] = want;
-      }
-      return p[b];
-    }
-    ~DevBuf2() {
-      for (int b = 0; b < 2; ++b)
-        if (p[b]) pinned ? cudaFreeHost(p[b]) : cudaFree(p[b]);
-    }
-  };
-  DevBuf2 pieces, stages, backs;
-  backs.pinned = true;
+  // Buffers double-buffered by piece parity, kept in the context for the
+  // next call: two piece texts, two stagings (with their run tables) and two
+  // pinned return buffers.  A staging or return buffer grows only after the
+  // piece that used it two steps before has been collected.
   Drain drain{ctx};
-  for (int b = 0; b < 2; ++b) pieces.get(b, P * width);
+  void* piece_buf[2] = {ctx->grow("semi_text0", P * width), ctx->grow("semi_text1", P * width)};
+  const char* stage_name[2] = {"semi_stage0", "semi_stage1"};
+  const char* back_name[2] = {"semi_back0", "semi_back1"};
+  void* back_buf[2] = {nullptr, nullptr};
   // pass 1: the leaf histogram, uploads beside the counting
   const uint64_t bins = uint64_t(1) << L;
   auto* d_hist = static_cast<unsigned long long*>(ctx->grow("semi_hist", bins * 8));
@@ -1796,10 +1807,10 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
     const int b = int(k & 1);
     const uint64_t m = std::min(P, n - a);
     if (used[b]) CUDA_TRY(cudaStreamWaitEvent(ctx->up, used[b], 0));
-    CUDA_TRY(cudaMemcpyAsync(pieces.p[b], txt + a * width, m * width, cudaMemcpyHostToDevice, ctx->up));
+    CUDA_TRY(cudaMemcpyAsync(piece_buf[b], txt + a * width, m * width, cudaMemcpyHostToDevice, ctx->up));
     CUDA_TRY(cudaStreamWaitEvent(s, ctx->mark(ctx->up), 0));
     ProfScope ps(ctx, "leaf_histogram", m * width);
-    launch_leaf_histogram(pieces.p[b], m, width, L, d_hist, ctx->d_status, s, &ctx->launches);
+    launch_leaf_histogram(piece_buf[b], m, width, L, d_hist, ctx->d_status, s, &ctx->launches);
     used[b] = ctx->mark(s);
   }
   std::vector<uint64_t> hist(bins);
@@ -1852,7 +1863,7 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
   auto collect = [&](PieceOut& q, int b) {   // the host's share of a piece, once its copies are back
     if (!q.pending) return;
     CUDA_TRY(cudaEventSynchronize(q.done));
-    const auto* h_back = static_cast<const uint64_t*>(backs.p[b]);
+    const auto* h_back = static_cast<const uint64_t*>(back_buf[b]);
     for (size_t i = 0; i < q.nsmall; ++i) {
       const StageSeg& sg = q.segs[i];
       const uint64_t words = ((sg.dst_bit + sg.len + 63) >> 6) - (sg.dst_bit >> 6);
@@ -1864,12 +1875,11 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
   };
   // pass 2: piece k uploads (up) while piece k-1 builds (s) and piece k-2's
   // words go back (down); the host ORs piece k-1's share meanwhile
-  std::unique_ptr<pwmgpu_wx> shard;
   for (int b = 0; b < 2; ++b) used[b] = nullptr;
   cudaEvent_t uploaded[2] = {nullptr, nullptr};
   auto upload = [&](uint64_t a, int b) {  // into text buffer b once the build that read it is done
     if (used[b]) CUDA_TRY(cudaStreamWaitEvent(ctx->up, used[b], 0));
-    CUDA_TRY(cudaMemcpyAsync(pieces.p[b], txt + a * width, std::min(P, n - a) * width, cudaMemcpyHostToDevice,
+    CUDA_TRY(cudaMemcpyAsync(piece_buf[b], txt + a * width, std::min(P, n - a) * width, cudaMemcpyHostToDevice,
                              ctx->up));
     uploaded[b] = ctx->mark(ctx->up);
   };
@@ -1878,13 +1888,17 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
     const int b = int(k & 1);
     const uint64_t m = std::min(P, n - a);
     CUDA_TRY(cudaStreamWaitEvent(s, uploaded[b], 0));
-    if (!shard || shard->n != m) {
-      if (shard) CUDA_TRY(cudaStreamSynchronize(s));
-      shard.reset();
-      shard = make_wx(ctx, m, width, L, (out_wm ? PWMGPU_MATRIX : 0u) | (want_tree ? PWMGPU_TREE : 0u) |
-                                           PWMGPU_KEEP_HISTOGRAM);
+    // the shard structures of full pieces and of a shorter last piece stay in
+    // the context for the next call of the same shape
+    const uint32_t shape = (out_wm ? PWMGPU_MATRIX : 0u) | (want_tree ? PWMGPU_TREE : 0u) | PWMGPU_KEEP_HISTOGRAM;
+    auto& slot = ctx->semi_shard[m == P ? 0 : 1];
+    if (!slot || slot->n != m || slot->width != width || slot->levels != L || slot->flags != shape) {
+      CUDA_TRY(cudaStreamSynchronize(s));
+      slot.reset();
+      slot = make_wx(ctx, m, width, L, shape);
     }
-    build_plain(ctx, shard.get(), pieces.p[b]);
+    pwmgpu_wx* shard = slot.get();
+    build_plain(ctx, shard, piece_buf[b]);
     const auto pc = fold_prefix_counts(shard->hist.data(), L);
     PieceOut& q = po[b];
     collect(q, b);  // piece k-2 (its buffers are reused now)
@@ -1945,11 +1959,12 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
     // collected above; the segment tables go in front of the staged words
     const size_t seg_bytes = (q.segs.size() * sizeof(StageSeg) + 15) & ~size_t(15);
     const size_t idx_bytes = (q.edge_idx.size() * 8 + 15) & ~size_t(15);
-    auto* base = static_cast<unsigned char*>(stages.get(b, seg_bytes + idx_bytes + (q.total + back + 1) * 8));
+    auto* base = static_cast<unsigned char*>(ctx->grow(stage_name[b], seg_bytes + idx_bytes + (q.total + back + 1) * 8));
     auto* d_segs = reinterpret_cast<StageSeg*>(base);
     auto* d_eidx = reinterpret_cast<uint64_t*>(base + seg_bytes);
     auto* d_stage = reinterpret_cast<uint64_t*>(base + seg_bytes + idx_bytes);
-    auto* h_back = static_cast<uint64_t*>(backs.get(b, std::max<uint64_t>(back, 1) * 8));
+    auto* h_back = static_cast<uint64_t*>(ctx->grow_pinned_named(back_name[b], std::max<uint64_t>(back, 1) * 8));
+    back_buf[b] = h_back;
     CUDA_TRY(cudaMemcpyAsync(d_segs, q.segs.data(), q.segs.size() * sizeof(StageSeg), cudaMemcpyHostToDevice, s));
     CUDA_TRY(cudaMemcpyAsync(d_eidx, q.edge_idx.data(), q.edge_idx.size() * 8, cudaMemcpyHostToDevice, s));
     {
@@ -2162,6 +2177,29 @@ pwmgpu_status pwmgpu_ctx_set_upload_piece_bytes(pwmgpu_ctx* ctx, uint64_t bytes)
   if (!ctx || bytes == 0) return PWMGPU_ERR_ARG;
   ctx->upload_piece = bytes;
   return PWMGPU_OK;
+}
+
+pwmgpu_status pwmgpu_ctx_release_scratch(pwmgpu_ctx* ctx) {
+  if (!ctx) return PWMGPU_ERR_ARG;
+  return guarded(ctx, [&]() {
+    for (cudaStream_t t : {ctx->stream, ctx->up, ctx->down, ctx->side})
+      if (t) CUDA_TRY(cudaStreamSynchronize(t));
+    delete ctx->compute_cache;
+    ctx->compute_cache = nullptr;
+    ctx->shard_cache.clear();
+    ctx->semi_shard[0].reset();
+    ctx->semi_shard[1].reset();
+    for (auto& kv : ctx->scratch)
+      if (kv.second.p) {
+        if (ctx->async_alloc) CUDA_TRY(cudaFreeAsync(kv.second.p, ctx->stream));
+        else CUDA_TRY(cudaFree(kv.second.p));
+      }
+    ctx->scratch.clear();
+    ctx->scratch_bytes = 0;
+    if (ctx->async_alloc) CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    ctx->release_pinned();
+    return PWMGPU_OK;
+  });
 }
 
 pwmgpu_status pwmgpu_ctx_set_stream_chunks(pwmgpu_ctx* ctx, uint32_t chunks) {

@@ -87,12 +87,20 @@ def test_semi_external_equals_in_memory_build(pg):
     ref_z = np.zeros(L, np.uint64)
     ds.compute_host(text.ctypes.data, ref_m.ctypes.data, ref_z, ref_t.ctypes.data)
     pin_text = torch.from_numpy(text.copy()).pin_memory()
-    out_m = torch.zeros(vm.total_words, dtype=torch.int64).pin_memory()
-    out_t = torch.zeros(vt.total_words, dtype=torch.int64).pin_memory()
-    _, zeros, _ = pg.compute_semi_external(pin_text.numpy(), L, device_budget=8 * MiB, out=(out_m, out_t))
-    assert np.array_equal(out_m.numpy().view(np.uint64), ref_m)
-    assert np.array_equal(out_t.numpy().view(np.uint64), ref_t)
-    assert np.array_equal(zeros, ref_z)
+    ctx = pg.Context()
+    # twice (the second call reuses the context's piece buffers and shards),
+    # then again after the context released them
+    for release in (False, False, True):
+        if release:
+            ctx.release_scratch()
+        out_m = torch.zeros(vm.total_words, dtype=torch.int64).pin_memory()
+        out_t = torch.zeros(vt.total_words, dtype=torch.int64).pin_memory()
+        _, zeros, _ = pg.compute_semi_external(pin_text.numpy(), L, device_budget=8 * MiB, out=(out_m, out_t),
+                                               context=ctx)
+        assert np.array_equal(out_m.numpy().view(np.uint64), ref_m)
+        assert np.array_equal(out_t.numpy().view(np.uint64), ref_t)
+        assert np.array_equal(zeros, ref_z)
+    ctx.close()
     ds.free()
     del rng
 
