@@ -124,10 +124,36 @@ struct pwmgpu_ctx {
     }
     return b.first;
   }
+  // Grow-only host buffer the device writes directly (mapped): results the
+  // host waits for that must not queue behind bulk copies.
+  void* mapped = nullptr;
+  uint64_t* mapped_dev = nullptr;
+  size_t mapped_bytes = 0;
+  uint64_t* grow_mapped(size_t bytes) {
+    if (mapped_bytes < bytes) {
+      if (mapped) {
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        CUDA_TRY(cudaFreeHost(mapped));
+      }
+      mapped = nullptr;
+      mapped_dev = nullptr;
+      mapped_bytes = 0;
+      CUDA_TRY(cudaHostAlloc(&mapped, bytes, cudaHostAllocMapped));
+      void* dp = nullptr;
+      CUDA_TRY(cudaHostGetDevicePointer(&dp, mapped, 0));
+      mapped_dev = static_cast<uint64_t*>(dp);
+      mapped_bytes = bytes;
+    }
+    return static_cast<uint64_t*>(mapped);
+  }
   void release_pinned() {
     if (pinned) cudaFreeHost(pinned);
     pinned = nullptr;
     pinned_bytes = 0;
+    if (mapped) cudaFreeHost(mapped);
+    mapped = nullptr;
+    mapped_dev = nullptr;
+    mapped_bytes = 0;
     for (auto& kv : pinned_named)
       if (kv.second.first) cudaFreeHost(kv.second.first);
     pinned_named.clear();
@@ -915,13 +941,15 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   // of every tile of the first pass and scans them, so that pass neither
   // counts nor looks back.
   TileFirstPass first{};
-  // pinned host words: the histogram, the status word and the block prefix
-  // rows at the bounds of a chunked first pass
+  // host words the device writes: the histogram and the status word (mapped,
+  // written by a kernel: they must not wait behind downloads in flight), and
+  // the block prefix rows at the bounds of a chunked first pass (pinned)
   const uint64_t NB0 = uint64_t(1) << D0;
-  auto* h_hist = static_cast<uint64_t*>(
-      ctx->grow_pinned((bins + 1 + uint64_t(kMaxStreamChunks) * (uint64_t(1) << kTileGivenMaxLevels)) * 8));
+  uint64_t* h_hist = ctx->grow_mapped((bins + 1) * 8);
+  uint64_t* d_hist_host = ctx->mapped_dev;
   auto* h_status = reinterpret_cast<uint32_t*>(h_hist + bins);
-  uint64_t* h_rows = h_hist + bins + 1;
+  auto* h_rows = static_cast<uint64_t*>(
+      ctx->grow_pinned(uint64_t(kMaxStreamChunks) * (uint64_t(1) << kTileGivenMaxLevels) * 8));
   // words of each structure already streamed to the host (a prefix of level 0)
   uint64_t sent[2] = {0, 0};
   Structure* sts[2] = {&wx->wm, &wx->wt};
@@ -983,9 +1011,8 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     launch_leaf_histogram(d_text, n, wx->width, L, d_hist, ctx->d_status, s, &ctx->launches);
   }
   CUDA_TRY(cudaGetLastError());
-  // the histogram and the status word go to pinned host memory
-  CUDA_TRY(cudaMemcpyAsync(h_hist, d_hist, bins * 8, cudaMemcpyDeviceToHost, s));
-  CUDA_TRY(cudaMemcpyAsync(h_status, ctx->d_status, 4, cudaMemcpyDeviceToHost, s));
+  // the histogram and the status word to the host
+  launch_readback(d_hist, bins, ctx->d_status, d_hist_host, s, &ctx->launches);
   CUDA_TRY(cudaEventRecord(ctx->hist_event(), s));
   const bool want_tree = wx->wt.present;
   // After the tile histogram the first pass needs nothing from the host but

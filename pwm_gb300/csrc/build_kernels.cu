@@ -523,6 +523,15 @@ __global__ void symbol_hist_kernel(const T* text, uint64_t n, uint64_t nsym, uns
   }
 }
 
+// n words and a status word into host-mapped memory: small results the host
+// waits for, written by the SMs instead of a copy engine, so that they do not
+// queue behind bulk downloads.
+__global__ void readback_kernel(const unsigned long long* src, uint64_t n, const uint32_t* status, uint64_t* dst) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+    dst[i] = src[i];
+  if (blockIdx.x == 0 && threadIdx.x == 0) dst[n] = status ? *status : 0u;
+}
+
 // Largest symbol of a 32-bit text (warp maxima, one atomic per warp).
 __global__ void max_symbol_kernel(const uint32_t* text, uint64_t n, unsigned int* out) {
   uint32_t m = 0;
@@ -655,6 +664,13 @@ void launch_symbol_histogram(const void* text, uint64_t n, uint32_t width, uint6
     return;
   }
   symbol_hist_kernel<<<g, 256, 0, s>>>(static_cast<const uint32_t*>(text), n, nsym, hist, first);
+  ++*launches;
+}
+
+void launch_readback(const unsigned long long* src, uint64_t n, const uint32_t* status, uint64_t* dst,
+                     cudaStream_t s, uint64_t* launches) {
+  const uint64_t blocks = (n + 255) / 256;
+  readback_kernel<<<unsigned(blocks < 1024 ? (blocks ? blocks : 1) : 1024), 256, 0, s>>>(src, n, status, dst);
   ++*launches;
 }
 

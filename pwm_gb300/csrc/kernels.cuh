@@ -26,6 +26,9 @@ void launch_leaf_histogram(const void* text, uint64_t n, uint32_t width, uint32_
 // hist must be zeroed.  launch_tile_block_scan then turns blocksum into each
 // block's exclusive prefix.
 uint32_t tile_hist_tiles_per_block();
+// dst[0..n) = src[0..n), dst[n] = *status (dst: host-mapped memory).
+void launch_readback(const unsigned long long* src, uint64_t n, const uint32_t* status, uint64_t* dst,
+                     cudaStream_t s, uint64_t* launches);
 // Largest symbol of a 32-bit text into *out (zeroed by the caller).
 void launch_max_symbol(const uint32_t* text, uint64_t n, unsigned int* out, cudaStream_t s, uint64_t* launches);
 // out[i] = map[text[i]] (same width; in place allowed).
