@@ -1824,30 +1824,6 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
   const char* stage_name[2] = {"semi_stage0", "semi_stage1"};
   const char* back_name[2] = {"semi_back0", "semi_back1"};
   void* back_buf[2] = {nullptr, nullptr};
-  // pass 1: the leaf histogram, uploads beside the counting
-  const uint64_t bins = uint64_t(1) << L;
-  auto* d_hist = static_cast<unsigned long long*>(ctx->grow("semi_hist", bins * 8));
-  CUDA_TRY(cudaMemsetAsync(d_hist, 0, bins * 8, s));
-  CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, 4, s));
-  cudaEvent_t used[2] = {nullptr, nullptr};  // the last work on s that read text buffer b
-  for (uint64_t a = 0, k = 0; a < n; a += P, ++k) {
-    const int b = int(k & 1);
-    const uint64_t m = std::min(P, n - a);
-    if (used[b]) CUDA_TRY(cudaStreamWaitEvent(ctx->up, used[b], 0));
-    CUDA_TRY(cudaMemcpyAsync(piece_buf[b], txt + a * width, m * width, cudaMemcpyHostToDevice, ctx->up));
-    CUDA_TRY(cudaStreamWaitEvent(s, ctx->mark(ctx->up), 0));
-    ProfScope ps(ctx, "leaf_histogram", m * width);
-    launch_leaf_histogram(piece_buf[b], m, width, L, d_hist, ctx->d_status, s, &ctx->launches);
-    used[b] = ctx->mark(s);
-  }
-  std::vector<uint64_t> hist(bins);
-  CUDA_TRY(cudaMemcpyAsync(hist.data(), d_hist, bins * 8, cudaMemcpyDeviceToHost, s));
-  check_device_status(ctx);
-  const auto cnt = fold_prefix_counts(hist.data(), L);
-  if (wm_zeros) {
-    const LevelTables t = build_tables_tile(cnt, L, {});
-    std::memcpy(wm_zeros, t.zeros.data(), L * 8);
-  }
   // start of each natural prefix of level m in the matrix (key order) or the tree
   auto starts = [](const std::vector<uint64_t>& c, uint32_t m, bool tree) {
     std::vector<uint64_t> st(c.size());
@@ -1867,10 +1843,43 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
   std::vector<Out> outs;
   if (out_wm) outs.push_back({0, out_wm, {}});
   if (out_wt) outs.push_back({1, out_wt, {}});
-  for (auto& o : outs)
-    for (uint32_t l = 0; l < L; ++l) o.gstart.push_back(starts(cnt[l], l, o.st == 1));
-  std::vector<std::vector<uint64_t>> placed(L);  // per level and prefix: bits earlier pieces placed
-  for (uint32_t l = 0; l < L; ++l) placed[l].assign(cnt[l].size(), 0);
+  std::vector<std::vector<uint64_t>> cnt;     // the text's prefix counts per level
+  std::vector<std::vector<uint64_t>> placed;  // per level and prefix: bits earlier pieces placed
+  auto setup = [&](const uint64_t* hist) {    // global starts and zeros from the leaf histogram
+    cnt = fold_prefix_counts(hist, L);
+    if (wm_zeros) {
+      const LevelTables t = build_tables_tile(cnt, L, {});
+      std::memcpy(wm_zeros, t.zeros.data(), L * 8);
+    }
+    for (auto& o : outs)
+      for (uint32_t l = 0; l < L; ++l) o.gstart.push_back(starts(cnt[l], l, o.st == 1));
+    placed.assign(L, {});
+    for (uint32_t l = 0; l < L; ++l) placed[l].assign(cnt[l].size(), 0);
+  };
+  // pass 1: the leaf histogram, uploads beside the counting (a text of one
+  // piece skips it: that piece's own histogram is the text's)
+  const bool single = n <= P;
+  const uint64_t bins = uint64_t(1) << L;
+  cudaEvent_t used[2] = {nullptr, nullptr};  // the last work on s that read text buffer b
+  if (!single) {
+    auto* d_hist = static_cast<unsigned long long*>(ctx->grow("semi_hist", bins * 8));
+    CUDA_TRY(cudaMemsetAsync(d_hist, 0, bins * 8, s));
+    CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, 4, s));
+    for (uint64_t a = 0, k = 0; a < n; a += P, ++k) {
+      const int b = int(k & 1);
+      const uint64_t m = std::min(P, n - a);
+      if (used[b]) CUDA_TRY(cudaStreamWaitEvent(ctx->up, used[b], 0));
+      CUDA_TRY(cudaMemcpyAsync(piece_buf[b], txt + a * width, m * width, cudaMemcpyHostToDevice, ctx->up));
+      CUDA_TRY(cudaStreamWaitEvent(s, ctx->mark(ctx->up), 0));
+      ProfScope ps(ctx, "leaf_histogram", m * width);
+      launch_leaf_histogram(piece_buf[b], m, width, L, d_hist, ctx->d_status, s, &ctx->launches);
+      used[b] = ctx->mark(s);
+    }
+    std::vector<uint64_t> hist(bins);
+    CUDA_TRY(cudaMemcpyAsync(hist.data(), d_hist, bins * 8, cudaMemcpyDeviceToHost, s));
+    check_device_status(ctx);
+    setup(hist.data());
+  }
   const uint64_t lw = padded_words(n);  // words per level of the host arrays
   // A piece's runs bound for the host: short ones first in the staging, then
   // the long ones, whose partial edge words are gathered behind the short
@@ -1903,6 +1912,9 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
   // pass 2: piece k uploads (up) while piece k-1 builds (s) and piece k-2's
   // words go back (down); the host ORs piece k-1's share meanwhile
   for (int b = 0; b < 2; ++b) used[b] = nullptr;
+  // the staging kernels' own status word (every shard build clears the context's)
+  auto* d_stage_status = static_cast<uint32_t*>(ctx->grow("semi_status", 4));
+  CUDA_TRY(cudaMemsetAsync(d_stage_status, 0, 4, s));
   cudaEvent_t uploaded[2] = {nullptr, nullptr};
   auto upload = [&](uint64_t a, int b) {  // into text buffer b once the build that read it is done
     if (used[b]) CUDA_TRY(cudaStreamWaitEvent(ctx->up, used[b], 0));
@@ -1926,6 +1938,7 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
     }
     pwmgpu_wx* shard = slot.get();
     build_plain(ctx, shard, piece_buf[b]);
+    if (single) setup(shard->hist.data());
     const auto pc = fold_prefix_counts(shard->hist.data(), L);
     PieceOut& q = po[b];
     collect(q, b);  // piece k-2 (its buffers are reused now)
@@ -1996,7 +2009,7 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
     CUDA_TRY(cudaMemcpyAsync(d_eidx, q.edge_idx.data(), q.edge_idx.size() * 8, cudaMemcpyHostToDevice, s));
     {
       ProfScope ps(ctx, "semi_stage", q.total * 16);
-      launch_stage_segments(d_segs, q.segs.size(), d_stage, q.total, ctx->d_status, s, &ctx->launches);
+      launch_stage_segments(d_segs, q.segs.size(), d_stage, q.total, d_stage_status, s, &ctx->launches);
     }
     uint64_t* d_back = d_stage + q.total;
     if (q.small_words)
@@ -2021,6 +2034,10 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
   collect(po[0], 0);
   collect(po[1], 1);
   check_device_status(ctx);
+  uint32_t stage_status = 0;
+  CUDA_TRY(cudaMemcpyAsync(&stage_status, d_stage_status, 4, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  throw_status(stage_status);
   for (uint32_t l = 0; l < L; ++l)
     if (placed[l] != cnt[l]) throw Fail{PWMGPU_ERR_CUDA, "internal: pieces do not add up to the text"};
   // words shared by runs: OR of their parts; padding words past each level: zero
