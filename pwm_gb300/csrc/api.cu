@@ -1052,8 +1052,12 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     const uint32_t nblk = tile_hist_blocks(n, T);
     const uint32_t C = ctx->stream_chunks;
     if (stream_out && C > 1 && nblk >= 2 * C) {
-      for (uint32_t c = 0; c <= C; ++c) blk0.push_back(uint32_t(uint64_t(nblk) * c / C));
-      for (uint32_t c = 1; c < C; ++c)
+      // chunk c of C takes a share c + 1 of C (C + 1) / 2: the first is small,
+      // so that downloads start early, later ones overlap the downloads
+      for (uint32_t c = 0; c <= C; ++c)
+        blk0.push_back(uint32_t(uint64_t(nblk) * (c * (c + 1) / 2) / (C * (C + 1) / 2)));
+      blk0.erase(std::unique(blk0.begin(), blk0.end()), blk0.end());
+      for (size_t c = 1; c + 1 < blk0.size(); ++c)
         CUDA_TRY(cudaMemcpyAsync(h_rows + (c - 1) * NB0, first.blockpre + uint64_t(blk0[c]) * NB0, NB0 * 8,
                                  cudaMemcpyDeviceToHost, s));
       rows_ev = ctx->mark(s);
@@ -1183,7 +1187,7 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     auto& sb = seg_bounds[pi];
     sb.assign(1, 0);
     for (uint32_t c = 1; c < ctx->stream_chunks; ++c) {
-      const uint64_t target = uint64_t(p.tiles) * c / ctx->stream_chunks;
+      const uint64_t target = uint64_t(p.tiles) * (c * (c + 1) / 2) / (ctx->stream_chunks * (ctx->stream_chunks + 1) / 2);
       uint32_t i = sb.back() + 1;
       while (i < p.segs.size() && p.segs[i].tile0 < target) ++i;
       if (i < p.segs.size()) sb.push_back(i);
