@@ -941,13 +941,19 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   // of every tile of the first pass and scans them, so that pass neither
   // counts nor looks back.
   TileFirstPass first{};
-  // host words the device writes: the histogram and the status word (mapped,
-  // written by a kernel: they must not wait behind downloads in flight), and
-  // the block prefix rows at the bounds of a chunked first pass (pinned)
+  // host words the device writes (mapped, written by kernels: they must not
+  // wait behind downloads in flight): the prefix counts of every level, flat
+  // (level m at 2^m - 1; level L is the leaf histogram), the zero bits of
+  // every level and the status word; and (pinned) the block prefix rows at
+  // the bounds of a chunked first pass
   const uint64_t NB0 = uint64_t(1) << D0;
-  uint64_t* h_hist = ctx->grow_mapped((bins + 1) * 8);
-  uint64_t* d_hist_host = ctx->mapped_dev;
-  auto* h_status = reinterpret_cast<uint32_t*>(h_hist + bins);
+  const uint64_t flat_words = (bins << 1) - 1;
+  uint64_t* h_flat = ctx->grow_mapped((flat_words + L + 1) * 8);
+  uint64_t* d_flat_host = ctx->mapped_dev;
+  uint64_t* h_hist = h_flat + bins - 1;
+  const uint64_t* h_zeros = h_flat + flat_words;
+  auto* h_status = reinterpret_cast<uint32_t*>(h_flat + flat_words + L);
+  auto* d_level_zeros = static_cast<unsigned long long*>(ctx->grow("level_zeros", uint64_t(L) * 8));
   auto* h_rows = static_cast<uint64_t*>(
       ctx->grow_pinned(uint64_t(kMaxStreamChunks) * (uint64_t(1) << kTileGivenMaxLevels) * 8));
   // words of each structure already streamed to the host (a prefix of level 0)
@@ -1011,8 +1017,10 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     launch_leaf_histogram(d_text, n, wx->width, L, d_hist, ctx->d_status, s, &ctx->launches);
   }
   CUDA_TRY(cudaGetLastError());
-  // the histogram and the status word to the host
-  launch_readback(d_hist, bins, ctx->d_status, d_hist_host, s, &ctx->launches);
+  // prefix counts, zero bits and the status word to the host
+  CUDA_TRY(cudaMemsetAsync(d_level_zeros, 0, uint64_t(L) * 8, s));
+  launch_fold_levels(d_hist, L, d_flat_host, d_level_zeros, s, &ctx->launches);
+  launch_readback(d_level_zeros, L, ctx->d_status, d_flat_host + flat_words, s, &ctx->launches);
   CUDA_TRY(cudaEventRecord(ctx->hist_event(), s));
   const bool want_tree = wx->wt.present;
   // After the tile histogram the first pass needs nothing from the host but
@@ -1080,11 +1088,11 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   std::vector<PassPlan> plan;
   std::vector<TilePassHost> tile_passes;
   std::vector<uint32_t> regroup;
-  std::vector<std::vector<uint64_t>> cnt;  // natural-prefix counts per level
+  PrefixCounts cnt;  // natural-prefix counts per level
   if (tile_engine) {
-    cnt = fold_prefix_counts(h_hist, L);
+    cnt = PrefixCounts::view(h_flat, L);
     tile_passes = plan_tile_passes(cnt, L, kmax, tile_pass_elems(wx->width), want_tree, &regroup);
-    tabs = build_tables_tile(cnt, L, want_tree ? regroup : std::vector<uint32_t>{});
+    tabs = build_tables_tile(cnt, L, want_tree ? regroup : std::vector<uint32_t>{}, h_zeros);
   } else {
     plan = plan_passes(L, ctx->pass_levels);
     tabs = build_tables_plain(std::vector<uint64_t>(h_hist, h_hist + bins), L, plan, want_tree);
@@ -1149,7 +1157,7 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     CUDA_TRY(cudaEventSynchronize(rows_ev));
     // keys of each natural prefix of level j in the histogram blocks before bound c
     auto before = [&](size_t c, uint32_t j) {
-      if (c + 1 == blk0.size()) return cnt[j];
+      if (c + 1 == blk0.size()) return std::vector<uint64_t>(cnt[j].begin(), cnt[j].end());
       std::vector<uint64_t> r(size_t(1) << j, 0);
       if (c == 0) return r;
       const uint64_t* row = h_rows + (c - 1) * NB0;  // key order of the first D0 bits
@@ -1829,7 +1837,7 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
   const char* back_name[2] = {"semi_back0", "semi_back1"};
   void* back_buf[2] = {nullptr, nullptr};
   // start of each natural prefix of level m in the matrix (key order) or the tree
-  auto starts = [](const std::vector<uint64_t>& c, uint32_t m, bool tree) {
+  auto starts = [](const CountSpan c, uint32_t m, bool tree) {
     std::vector<uint64_t> st(c.size());
     uint64_t run = 0;
     for (uint64_t y = 0; y < c.size(); ++y) {
@@ -1847,7 +1855,7 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
   std::vector<Out> outs;
   if (out_wm) outs.push_back({0, out_wm, {}});
   if (out_wt) outs.push_back({1, out_wt, {}});
-  std::vector<std::vector<uint64_t>> cnt;     // the text's prefix counts per level
+  PrefixCounts cnt;                          // the text's prefix counts per level
   std::vector<std::vector<uint64_t>> placed;  // per level and prefix: bits earlier pieces placed
   auto setup = [&](const uint64_t* hist) {    // global starts and zeros from the leaf histogram
     cnt = fold_prefix_counts(hist, L);
@@ -2043,7 +2051,8 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
   CUDA_TRY(cudaStreamSynchronize(s));
   throw_status(stage_status);
   for (uint32_t l = 0; l < L; ++l)
-    if (placed[l] != cnt[l]) throw Fail{PWMGPU_ERR_CUDA, "internal: pieces do not add up to the text"};
+    if (!std::equal(placed[l].begin(), placed[l].end(), cnt[l].begin()))
+      throw Fail{PWMGPU_ERR_CUDA, "internal: pieces do not add up to the text"};
   // words shared by runs: OR of their parts; padding words past each level: zero
   std::sort(acc.begin(), acc.end());
   for (size_t i = 0; i < acc.size();) {
@@ -2079,7 +2088,7 @@ void merge_shards(pwmgpu_ctx* ctx, const std::vector<const pwmgpu_wx*>& sh, pwmg
   if (total != out->n) throw Fail{PWMGPU_ERR_ARG, "the shards' sizes do not add up to out's"};
   cudaStream_t st = ctx->stream;
   CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, 4, st));
-  std::vector<std::vector<std::vector<uint64_t>>> cnt(p);
+  std::vector<PrefixCounts> cnt(p);
   for (uint32_t s = 0; s < p; ++s) cnt[s] = fold_prefix_counts(sh[s]->hist.data(), L);
   for (int which = 0; which < 2; ++which) {
     Structure& O = which ? out->wt : out->wm;

@@ -532,6 +532,56 @@ __global__ void readback_kernel(const unsigned long long* src, uint64_t n, const
   if (blockIdx.x == 0 && threadIdx.x == 0) dst[n] = status ? *status : 0u;
 }
 
+// Natural-prefix counts of every level from the leaf histogram, flat (level
+// m's 2^m counts at offset 2^m - 1), and the zero bits of every level
+// (zeros[m]: the counts of the even prefixes of level m + 1).  One launch
+// folds level `top` (read from `leaves`, and then copied to the flat array,
+// or from the flat array) `down` <= 10 levels down; a block takes 1024
+// entries of level top, halves them `down` times in shared memory and adds
+// its even entries of each level into zeros with one atomic per level.
+__global__ void __launch_bounds__(256) fold_levels_kernel(uint64_t* flat, const unsigned long long* leaves,
+                                                          uint32_t top, uint32_t down, unsigned long long* zeros) {
+  __shared__ uint64_t v[1024];
+  __shared__ unsigned long long s_even;
+  const uint64_t n_top = 1ull << top;
+  const uint64_t base = uint64_t(blockIdx.x) * 1024;
+  const uint64_t* src = leaves ? reinterpret_cast<const uint64_t*>(leaves) : flat + (n_top - 1);
+  for (int i = threadIdx.x; i < 1024; i += 256) {
+    const uint64_t x = base + i < n_top ? src[base + i] : 0;
+    v[i] = x;
+    if (leaves && base + i < n_top) flat[n_top - 1 + base + i] = x;
+  }
+  __syncthreads();
+  for (uint32_t d = 1; d <= down; ++d) {
+    const uint32_t k = 1024u >> d;  // entries of level top - d in this block
+    if (threadIdx.x == 0) s_even = 0;
+    __syncthreads();
+    uint64_t sums[2], even = 0;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const uint32_t i = threadIdx.x + 256u * r;
+      sums[r] = i < k ? v[2 * i] + v[2 * i + 1] : 0;
+      even += i < k ? v[2 * i] : 0;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) even += __shfl_xor_sync(0xFFFFFFFFu, even, o);
+    if ((threadIdx.x & 31) == 0 && even) atomicAdd(&s_even, (unsigned long long)even);
+    __syncthreads();  // every read of the level above is done
+    const uint32_t m = top - d;
+    const uint64_t n_m = 1ull << m, b_m = base >> d;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const uint32_t i = threadIdx.x + 256u * r;
+      if (i < k) {
+        v[i] = sums[r];
+        if (b_m + i < n_m) flat[n_m - 1 + b_m + i] = sums[r];
+      }
+    }
+    if (threadIdx.x == 0 && s_even) atomicAdd(&zeros[m], s_even);
+    __syncthreads();
+  }
+}
+
 // Largest symbol of a 32-bit text (warp maxima, one atomic per warp).
 __global__ void max_symbol_kernel(const uint32_t* text, uint64_t n, unsigned int* out) {
   uint32_t m = 0;
@@ -672,6 +722,21 @@ void launch_readback(const unsigned long long* src, uint64_t n, const uint32_t* 
   const uint64_t blocks = (n + 255) / 256;
   readback_kernel<<<unsigned(blocks < 1024 ? (blocks ? blocks : 1) : 1024), 256, 0, s>>>(src, n, status, dst);
   ++*launches;
+}
+
+void launch_fold_levels(const unsigned long long* hist, uint32_t levels, uint64_t* flat, unsigned long long* zeros,
+                        cudaStream_t s, uint64_t* launches) {
+  uint32_t top = levels;
+  bool first = true;
+  for (;;) {
+    const uint32_t down = top < 10u ? top : 10u;
+    const uint64_t blocks = ((1ull << top) + 1023) / 1024;
+    fold_levels_kernel<<<unsigned(blocks), 256, 0, s>>>(flat, first ? hist : nullptr, top, down, zeros);
+    ++*launches;
+    first = false;
+    if (down == top) break;  // level 0 written
+    top -= down;
+  }
 }
 
 void launch_max_symbol(const uint32_t* text, uint64_t n, unsigned int* out, cudaStream_t s, uint64_t* launches) {

@@ -124,33 +124,76 @@ inline LevelTables build_tables_plain(const std::vector<uint64_t>& hist, uint32_
   return t;
 }
 
-// Natural-order prefix counts of every level m = 0..L (2^m bins) folded from
-// the leaf histogram.
-inline std::vector<std::vector<uint64_t>> fold_prefix_counts(const uint64_t* hist, uint32_t L) {
-  std::vector<std::vector<uint64_t>> cnt(L + 1);
-  cnt[L].assign(hist, hist + (size_t(1) << L));
-  for (int m = int(L) - 1; m >= 0; --m) {
-    cnt[m].assign(size_t(1) << m, 0);
-    const auto& c = cnt[m + 1];
-    for (size_t p = 0; p < cnt[m].size(); ++p) cnt[m][p] = c[2 * p] + c[2 * p + 1];
+// The counts of one level (a view).
+struct CountSpan {
+  const uint64_t* p;
+  size_t n;
+  size_t size() const { return n; }
+  const uint64_t& operator[](size_t i) const { return p[i]; }
+  const uint64_t* begin() const { return p; }
+  const uint64_t* end() const { return p + n; }
+};
+
+// Natural-order prefix counts of every level m = 0..L (2^m counts each),
+// flat: level m at offset 2^m - 1.  Either owned (folded on the host) or a
+// view of counts the device folded (fold_levels_kernel).
+class PrefixCounts {
+ public:
+  PrefixCounts() = default;
+  static PrefixCounts view(const uint64_t* flat, uint32_t L) {
+    PrefixCounts c;
+    c.ext_ = flat;
+    c.L_ = L;
+    return c;
   }
-  return cnt;
-}
+  static PrefixCounts fold(const uint64_t* hist, uint32_t L) {
+    PrefixCounts c;
+    c.L_ = L;
+    c.own_.resize((size_t(2) << L) - 1);
+    uint64_t* f = c.own_.data();
+    std::copy(hist, hist + (size_t(1) << L), f + (size_t(1) << L) - 1);
+    for (int m = int(L) - 1; m >= 0; --m) {
+      const uint64_t* up = f + (size_t(2) << m) - 1;
+      uint64_t* o = f + (size_t(1) << m) - 1;
+      for (size_t x = 0; x < (size_t(1) << m); ++x) o[x] = up[2 * x] + up[2 * x + 1];
+    }
+    return c;
+  }
+  CountSpan operator[](uint32_t m) const { return {base() + (size_t(1) << m) - 1, size_t(1) << m}; }
+  uint32_t levels() const { return L_; }
+  bool empty() const { return !ext_ && own_.empty(); }
+
+ private:
+  const uint64_t* base() const { return ext_ ? ext_ : own_.data(); }
+  const uint64_t* ext_ = nullptr;
+  std::vector<uint64_t> own_;
+  uint32_t L_ = 0;
+};
+
+inline PrefixCounts fold_prefix_counts(const uint64_t* hist, uint32_t L) { return PrefixCounts::fold(hist, L); }
 
 // Tables of a plain build through the tile engine: zero counts, level sizes
 // and the tree segments of the given levels (those the regroup writes).
-inline LevelTables build_tables_tile(const std::vector<std::vector<uint64_t>>& cnt, uint32_t L,
-                                     const std::vector<uint32_t>& tree_levels) {
+// zeros: the zero bits of every level when the device counted them, else
+// they are summed here.
+inline LevelTables build_tables_tile(const PrefixCounts& cnt, uint32_t L, const std::vector<uint32_t>& tree_levels,
+                                     const uint64_t* zeros = nullptr) {
   LevelTables t;
   const uint64_t n = cnt[0][0];
   t.level_bits.assign(L, n);
   t.zeros.assign(L, 0);
-  for (uint32_t m = 0; m < L; ++m)
-    for (size_t p = 0; p < cnt[m + 1].size(); p += 2) t.zeros[m] += cnt[m + 1][p];
+  if (zeros) {
+    t.zeros.assign(zeros, zeros + L);
+  } else {
+    for (uint32_t m = 0; m < L; ++m) {
+      const CountSpan c = cnt[m + 1];
+      for (size_t p = 0; p < c.size(); p += 2) t.zeros[m] += c[p];
+    }
+  }
   t.seg_tree.resize(L);
   t.seg_matrix.resize(L);
   for (uint32_t m : tree_levels) {
-    const auto& c = cnt[m];
+    const CountSpan c = cnt[m];
     std::vector<uint64_t> mstart(c.size(), 0);
     uint64_t run = 0;
     for (size_t r = 0; r < c.size(); ++r) {
@@ -203,7 +246,7 @@ struct TilePassHost {
 // tree).  Exclusive prefixes over all 2^m groups of a level are built only
 // for the levels of segmented passes (few groups); a matrix-only pass needs
 // only the counts of its own K bits, folded from one level.
-inline std::vector<TilePassHost> plan_tile_passes(const std::vector<std::vector<uint64_t>>& cnt, uint32_t L, int kmax,
+inline std::vector<TilePassHost> plan_tile_passes(const PrefixCounts& cnt, uint32_t L, int kmax,
                                                   uint32_t T, bool want_tree, std::vector<uint32_t>* regroup) {
   const uint64_t n = cnt[0][0];
   std::vector<std::vector<uint64_t>> pren(L + 1), prek(L + 1);
@@ -254,10 +297,13 @@ inline std::vector<TilePassHost> plan_tile_passes(const std::vector<std::vector<
       // whole text, from the natural prefixes of level l+K; key_j folds it
       const uint32_t top = l + uint32_t(K);
       std::vector<uint64_t> ck(size_t(1) << K, 0);
-      const auto& c = cnt[top];
-      const uint64_t fmask = (uint64_t(1) << K) - 1;
-      for (size_t p = 0; p < c.size(); ++p)
-        if (c[p]) ck[rev_bits_host(p & fmask, uint32_t(K))] += c[p];
+      const CountSpan c = cnt[top];
+      // sums over the prefixes with the same last K bits, then reversed
+      const size_t R = size_t(1) << K;
+      std::vector<uint64_t> low(R, 0);
+      for (size_t p = 0; p < c.size(); p += R)
+        for (size_t r = 0; r < R; ++r) low[r] += c[p + r];
+      for (size_t r = 0; r < R; ++r) ck[rev_bits_host(r, uint32_t(K))] += low[r];
       for (int j = 0; j <= K; ++j) {
         if (j < K || ps.out) {
           uint64_t run = 0;

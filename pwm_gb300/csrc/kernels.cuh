@@ -26,6 +26,11 @@ void launch_leaf_histogram(const void* text, uint64_t n, uint32_t width, uint32_
 // hist must be zeroed.  launch_tile_block_scan then turns blocksum into each
 // block's exclusive prefix.
 uint32_t tile_hist_tiles_per_block();
+// Prefix counts of levels 0..levels from the leaf histogram into `flat`
+// (level m at offset 2^m - 1; host-mapped memory allowed), the zero bits of
+// each level added into zeros[0..levels) (zeroed by the caller).
+void launch_fold_levels(const unsigned long long* hist, uint32_t levels, uint64_t* flat, unsigned long long* zeros,
+                        cudaStream_t s, uint64_t* launches);
 // dst[0..n) = src[0..n), dst[n] = *status (dst: host-mapped memory).
 void launch_readback(const unsigned long long* src, uint64_t n, const uint32_t* status, uint64_t* dst,
                      cudaStream_t s, uint64_t* launches);
