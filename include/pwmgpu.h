@@ -136,8 +136,10 @@ PWMGPU_API pwmgpu_status pwmgpu_ctx_release_scratch(pwmgpu_ctx* ctx);
  *   wx_ps  include/wx_ps.hpp:37-56      wx_pc   include/wx_pc.hpp:36-57
  *   wx_ppc include/wx_ppc.hpp:36-58     wx_pps  include/wx_pps.hpp:38-69
  *   wx_pc_ss / wx_ppc_ss / wx_dd_ps / wx_dd_pc / wx_dd_pc_ss (same output)
- * `text`: host array of `size` symbols of `word_width` bytes (1, 2 or 4),
- * each < 2^levels.  `bv`: host array of levels * round_up(ceil(size/64), 16)
+ * `text`: host array of `size` symbols of `word_width` bytes (1, 2, 4, or 5
+ * for pwm's packed little-endian uint40_t, registered by pwm for wm_pc /
+ * wt_pc: src/register/sequential_prefix_counting.cpp:16-47, widened to 32
+ * bits on the device), each < 2^levels.  `bv`: host array of levels * round_up(ceil(size/64), 16)
  * words.  `zeros`: host array of `levels` u64 for a matrix (is_tree == 0),
  * ignored for a tree; all L entries are written, like wx_ps / wx_pc.
  * size == 0 writes nothing (pwm returns an empty structure). */
@@ -176,7 +178,8 @@ PWMGPU_API pwmgpu_status pwmgpu_compute_huffman(pwmgpu_ctx* ctx, const void* tex
 
 /* Allocates device storage for a build of `size` symbols with `levels`
  * levels; shape_flags: PWMGPU_MATRIX and/or PWMGPU_TREE, optionally
- * PWMGPU_RANK_SELECT. */
+ * PWMGPU_RANK_SELECT.  word_width 1, 2, 4 or 5 (40-bit symbols: the builds,
+ * host or device text, widen them to 32 bits first). */
 PWMGPU_API pwmgpu_status pwmgpu_wx_create(pwmgpu_ctx* ctx, uint64_t size, uint32_t word_width, uint32_t levels,
                                           uint32_t shape_flags, pwmgpu_wx** out);
 /* Builds into `wx` from a device text (same size/width/levels as created).

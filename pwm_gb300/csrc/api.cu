@@ -280,11 +280,13 @@ struct Structure {
 struct pwmgpu_wx {
   pwmgpu_ctx* ctx = nullptr;
   uint64_t n = 0;
-  uint32_t width = 1;
+  uint32_t width = 1;     // key bytes of the build
+  uint32_t in_width = 0;  // bytes of an input symbol when they differ (5: pwm's uint40_t, widened to 4)
   uint32_t levels = 0;
   uint32_t flags = 0;
   bool huffman = false;
   Structure wm, wt;
+  uint32_t input_width() const { return in_width ? in_width : width; }
   bool wm_internal = false;  // matrix built only as the source of the tree
   bool keep_hist = false;    // PWMGPU_KEEP_HISTOGRAM: the leaf histogram of the last build, for merges
   std::vector<uint64_t> hist;
@@ -350,6 +352,9 @@ pwmgpu_status guarded(pwmgpu_ctx* ctx, F&& f) {
 }
 
 bool valid_width(uint32_t w) { return w == 1 || w == 2 || w == 4; }
+// Plain builds also take pwm's 40-bit symbols (uint40_t), widened to 32 bits
+// on the device first.
+bool valid_plain_width(uint32_t w) { return valid_width(w) || w == 5; }
 
 // Records CUDA events on the context's stream around one launch group when
 // profiling is on; `bytes` is the algorithmic traffic of the group.
@@ -800,8 +805,9 @@ void run_tile_passes(pwmgpu_ctx* ctx, const void* in, uint32_t width, uint32_t L
   // the plan may go out of scope with the passes still running)
 }
 
-void validate_plain(uint64_t n, uint32_t width, uint32_t levels) {
-  if (!valid_width(width)) throw Fail{PWMGPU_ERR_ARG, "word_width must be 1, 2 or 4"};
+void validate_plain(uint64_t n, uint32_t width, uint32_t levels, bool allow40 = false) {
+  if (!(allow40 ? valid_plain_width(width) : valid_width(width)))
+    throw Fail{PWMGPU_ERR_ARG, allow40 ? "word_width must be 1, 2, 4 or 5" : "word_width must be 1, 2 or 4"};
   if (levels == 0 || levels > kMaxPlainLevels)
     throw Fail{PWMGPU_ERR_ARG, "levels must be in 1..24 (the leaf histogram has 2^levels bins)"};
   if (n >= (uint64_t(1) << 62)) throw Fail{PWMGPU_ERR_ARG, "size too large"};
@@ -1768,7 +1774,8 @@ std::unique_ptr<pwmgpu_wx> make_wx(pwmgpu_ctx* ctx, uint64_t size, uint32_t word
   auto wx = std::make_unique<pwmgpu_wx>();
   wx->ctx = ctx;
   wx->n = size;
-  wx->width = word_width;
+  wx->width = word_width == 5 ? 4 : word_width;
+  wx->in_width = word_width == 5 ? 5 : 0;
   wx->levels = levels;
   wx->flags = shape_flags;
   wx->keep_hist = shape_flags & PWMGPU_KEEP_HISTOGRAM;
@@ -2067,6 +2074,24 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
       std::fill(o.host + uint64_t(l) * lw + words_for(n), o.host + uint64_t(l + 1) * lw, uint64_t(0));
 }
 
+// The device text of a build in its key width: 40-bit symbols widened into
+// scratch, others as they are.
+const void* build_input(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, const void* d_text) {
+  if (wx->in_width != 5) return d_text;
+  auto* wide = static_cast<uint32_t*>(ctx->grow("wide_text", std::max<uint64_t>(wx->n, 1) * 4));
+  launch_widen40(d_text, wx->n, wide, ctx->stream, &ctx->launches);
+  CUDA_TRY(cudaGetLastError());
+  return wide;
+}
+
+// A host text of 40-bit symbols: copied up and widened; the build then runs
+// from the device text with only the outputs on the host.
+const void* upload_wide_host_text(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, const void* host_text) {
+  void* d40 = ctx->grow("text40", std::max<uint64_t>(wx->n, 1) * 5);
+  CUDA_TRY(cudaMemcpyAsync(d40, host_text, wx->n * 5, cudaMemcpyHostToDevice, ctx->stream));
+  return build_input(ctx, wx, d40);
+}
+
 constexpr uint32_t kMergeMaxLevels = 16;
 
 // pwm's merge_bit_vectors (merge.hpp:192-465) on the device: per level the
@@ -2317,6 +2342,7 @@ pwmgpu_status pwmgpu_wx_build_sharded(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void
   if (!ctx || !wx || shards == 0 || (!d_text && wx->n)) return PWMGPU_ERR_ARG;
   if (wx->huffman) return fail(ctx, PWMGPU_ERR_ARG, "a Huffman-shaped wx is built by pwmgpu_wx_build_huffman");
   return guarded(ctx, [&]() {
+    d_text = build_input(ctx, wx, d_text);
     if (shards == 1 || wx->n == 0) {
       build_plain(ctx, wx, d_text);
       return PWMGPU_OK;
@@ -2358,7 +2384,7 @@ pwmgpu_status pwmgpu_wx_create(pwmgpu_ctx* ctx, uint64_t size, uint32_t word_wid
   if (!ctx || !out) return PWMGPU_ERR_ARG;
   *out = nullptr;
   return guarded(ctx, [&]() {
-    validate_plain(size, word_width, levels);
+    validate_plain(size, word_width, levels, true);
     if (!(shape_flags & (PWMGPU_MATRIX | PWMGPU_TREE))) throw Fail{PWMGPU_ERR_ARG, "need PWMGPU_MATRIX or PWMGPU_TREE"};
     if ((shape_flags & PWMGPU_RANK_SELECT) && size >= 4294967295ull - 64)
       throw Fail{PWMGPU_ERR_ARG, "rank/select support needs levels below 2^32-1 bits"};
@@ -2371,7 +2397,7 @@ pwmgpu_status pwmgpu_wx_build(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text
   if (!ctx || !wx || (!d_text && wx->n)) return PWMGPU_ERR_ARG;
   if (wx->huffman) return fail(ctx, PWMGPU_ERR_ARG, "a Huffman-shaped wx is built by pwmgpu_wx_build_huffman");
   return guarded(ctx, [&]() {
-    build_plain(ctx, wx, d_text);
+    build_plain(ctx, wx, build_input(ctx, wx, d_text));
     return PWMGPU_OK;
   });
 }
@@ -2380,6 +2406,10 @@ pwmgpu_status pwmgpu_wx_build_host(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* h
   if (!ctx || !wx || (!host_text && wx->n)) return PWMGPU_ERR_ARG;
   if (wx->huffman) return fail(ctx, PWMGPU_ERR_ARG, "a Huffman-shaped wx is built by pwmgpu_wx_build_huffman");
   return guarded(ctx, [&]() {
+    if (wx->in_width == 5) {
+      build_plain(ctx, wx, upload_wide_host_text(ctx, wx, host_text));
+      return PWMGPU_OK;
+    }
     void* d_text = ctx->grow("host_text", std::max<uint64_t>(wx->n * wx->width, 1));
     HostIO io;
     io.text = host_text;
@@ -2395,12 +2425,16 @@ pwmgpu_status pwmgpu_wx_compute_host(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void*
   if ((wm_bv && (!wx->wm.present || wx->wm_internal)) || (wt_bv && !wx->wt.present))
     return fail(ctx, PWMGPU_ERR_ARG, "an output structure the wx does not hold");
   return guarded(ctx, [&]() {
-    void* d_text = ctx->grow("host_text", std::max<uint64_t>(wx->n * wx->width, 1));
     HostIO io;
-    io.text = host_text;
     io.wm = wm_bv;
     io.wt = wt_bv;
-    build_plain(ctx, wx, d_text, &io);
+    if (wx->in_width == 5) {
+      build_plain(ctx, wx, upload_wide_host_text(ctx, wx, host_text), &io);
+    } else {
+      void* d_text = ctx->grow("host_text", std::max<uint64_t>(wx->n * wx->width, 1));
+      io.text = host_text;
+      build_plain(ctx, wx, d_text, &io);
+    }
     check_device_status(ctx);
     if (wm_zeros && wx->wm.present && !wx->wm_internal) std::memcpy(wm_zeros, wx->wm.zeros.data(), wx->levels * 8);
     return PWMGPU_OK;
@@ -2667,20 +2701,24 @@ pwmgpu_status pwmgpu_compute(pwmgpu_ctx* ctx, const void* text, uint64_t size, u
   if (size == 0) return PWMGPU_OK;  // pwm: empty structure
   if (!text || !bv || (!is_tree && !zeros)) return fail(ctx, PWMGPU_ERR_ARG, "null text, bv or zeros");
   return guarded(ctx, [&]() {
-    validate_plain(size, word_width, levels);
+    validate_plain(size, word_width, levels, true);
     const uint32_t shape = is_tree ? PWMGPU_TREE : PWMGPU_MATRIX;
     pwmgpu_wx*& wx = ctx->compute_cache;
-    if (!wx || wx->n != size || wx->width != word_width || wx->levels != levels || wx->flags != shape) {
+    if (!wx || wx->n != size || wx->input_width() != word_width || wx->levels != levels || wx->flags != shape) {
       delete wx;
       wx = nullptr;
       pwmgpu_status st = pwmgpu_wx_create(ctx, size, word_width, levels, shape, &wx);
       if (st != PWMGPU_OK) return st;
     }
-    void* d_text = ctx->grow("host_text", size * word_width);
     HostIO io;
-    io.text = text;
     (is_tree ? io.wt : io.wm) = bv;
-    build_plain(ctx, wx, d_text, &io);
+    if (wx->in_width == 5) {
+      build_plain(ctx, wx, upload_wide_host_text(ctx, wx, text), &io);
+    } else {
+      void* d_text = ctx->grow("host_text", size * word_width);
+      io.text = text;
+      build_plain(ctx, wx, d_text, &io);
+    }
     const Structure& s = is_tree ? wx->wt : wx->wm;
     check_device_status(ctx);
     if (!is_tree) std::memcpy(zeros, s.zeros.data(), levels * 8);

@@ -582,6 +582,17 @@ __global__ void __launch_bounds__(256) fold_levels_kernel(uint64_t* flat, const 
   }
 }
 
+// 40-bit symbols (pwm's uint40_t: 5 little-endian bytes, packed) widened to
+// 32 bits; a value of 2^32 or more becomes 0xFFFFFFFF, which the histogram
+// rejects as a symbol past the levels (at most 24).
+__global__ void widen40_kernel(const uint8_t* in, uint64_t n, uint32_t* out) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    const uint8_t* r = in + 5 * i;
+    const uint32_t v = uint32_t(r[0]) | (uint32_t(r[1]) << 8) | (uint32_t(r[2]) << 16) | (uint32_t(r[3]) << 24);
+    out[i] = r[4] ? 0xFFFFFFFFu : v;
+  }
+}
+
 // Largest symbol of a 32-bit text (warp maxima, one atomic per warp).
 __global__ void max_symbol_kernel(const uint32_t* text, uint64_t n, unsigned int* out) {
   uint32_t m = 0;
@@ -721,6 +732,12 @@ void launch_readback(const unsigned long long* src, uint64_t n, const uint32_t* 
                      cudaStream_t s, uint64_t* launches) {
   const uint64_t blocks = (n + 255) / 256;
   readback_kernel<<<unsigned(blocks < 1024 ? (blocks ? blocks : 1) : 1024), 256, 0, s>>>(src, n, status, dst);
+  ++*launches;
+}
+
+void launch_widen40(const void* in, uint64_t n, uint32_t* out, cudaStream_t s, uint64_t* launches) {
+  if (n == 0) return;
+  widen40_kernel<<<grid_for(n, 256), 256, 0, s>>>(static_cast<const uint8_t*>(in), n, out);
   ++*launches;
 }
 

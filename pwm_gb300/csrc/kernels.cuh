@@ -26,6 +26,9 @@ void launch_leaf_histogram(const void* text, uint64_t n, uint32_t width, uint32_
 // hist must be zeroed.  launch_tile_block_scan then turns blocksum into each
 // block's exclusive prefix.
 uint32_t tile_hist_tiles_per_block();
+// 40-bit symbols (5 little-endian bytes each) widened to 32 bits (values of
+// 2^32 and more become 0xFFFFFFFF).
+void launch_widen40(const void* in, uint64_t n, uint32_t* out, cudaStream_t s, uint64_t* launches);
 // Prefix counts of levels 0..levels from the leaf histogram into `flat`
 // (level m at offset 2^m - 1; host-mapped memory allowed), the zero bits of
 // each level added into zeros[0..levels) (zeroed by the caller).

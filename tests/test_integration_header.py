@@ -11,7 +11,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REF = os.environ.get("PWM_REFERENCE", "/root/reference")
 
 PROGRAM = r'''
+#include <cstdint>
 #include <iostream>
+#include "util/uint_t.hpp"
 #include "wx_gpu.hpp"
 #include "util/decode.hpp"
 // pwm's registration contract, restricted to internal memory (the reference
@@ -22,13 +24,18 @@ template <typename T> struct registered {
 };
 static_assert(registered<wx_gpu<uint8_t, false>>::ok && registered<wx_gpu<uint8_t, true>>::ok, "");
 static_assert(registered<wx_gpu_huff<uint8_t, false>>::ok, "");
+// pwm registers wm_pc / wt_pc for 40-bit alphabets too (uint40_t: 5 packed bytes)
+static_assert(sizeof(uint40_t) == 5 && wx_gpu<uint40_t, false>::word_width == 5, "");
 int main() {
   std::vector<uint8_t> t = {3, 1, 4, 1, 5, 9, 2, 6};
   try {
     auto wm = wx_gpu<uint8_t, false>::compute(t.data(), t.size(), 4);
     auto wt = wx_gpu<uint8_t, true>::compute(t.data(), t.size(), 4);
     auto h = wx_gpu_huff<uint8_t, true>::compute(t.data(), t.size(), 0);
-    std::cout << decode_wm(wm.bvs(), wm.zeros(), t.size()).size() << decode_wt(wt.bvs(), t.size()).size() << "\n";
+    std::vector<uint40_t> t40(t.begin(), t.end());
+    auto w40 = wx_gpu<uint40_t, false>::compute(t40.data(), t40.size(), 4);
+    std::cout << decode_wm(wm.bvs(), wm.zeros(), t.size()).size() << decode_wt(wt.bvs(), t.size()).size()
+              << decode_wm(w40.bvs(), w40.zeros(), t.size()).size() << "\n";
   } catch (const std::exception& e) {
     std::cout << "runtime: " << e.what() << "\n";
     return 2;
