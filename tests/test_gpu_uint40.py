@@ -104,5 +104,7 @@ def test_u40_rejects_out_of_range(pg):
     st = ctx.lib.pwmgpu_compute(ctx.h, np.zeros(30, np.uint8).ctypes.data, 10, 3, 4, 0,
                                 bv.ctypes.data_as(pg._lib.u64p), zeros.ctypes.data_as(pg._lib.u64p))
     assert st != 0
-    with pytest.raises(pg.PwmGpuError):
-        pg.compute_semi_external(np.zeros((10, 5), np.uint8), 4)
+    out = np.zeros(4 * 16, np.uint64)
+    st = ctx.lib.pwmgpu_compute_semi_external(ctx.h, np.zeros(50, np.uint8).ctypes.data, 10, 5, 4,
+                                              out.ctypes.data_as(pg._lib.u64p), None, None, 0)
+    assert st != 0
