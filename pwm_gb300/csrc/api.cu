@@ -1824,8 +1824,7 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
   P = std::min(P, (n + kSemiMinPiece - 1) & ~(kSemiMinPiece - 1));
   const auto* txt = static_cast<const unsigned char*>(text);
   ctx->xfer_init();
-  // every stream is idle again when this returns or throws (buffers below
-  // are freed then)
+  // every stream is idle again when this returns or throws
   struct Drain {
     pwmgpu_ctx* c;
     ~Drain() {
@@ -1839,7 +1838,8 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
   // pinned return buffers.  A staging or return buffer grows only after the
   // piece that used it two steps before has been collected.
   Drain drain{ctx};
-  void* piece_buf[2] = {ctx->grow("semi_text0", P * width), ctx->grow("semi_text1", P * width)};
+  const bool single = n <= P;  // one piece: its own histogram is the text's
+  void* piece_buf[2] = {ctx->grow("semi_text0", P * width), single ? nullptr : ctx->grow("semi_text1", P * width)};
   const char* stage_name[2] = {"semi_stage0", "semi_stage1"};
   const char* back_name[2] = {"semi_back0", "semi_back1"};
   void* back_buf[2] = {nullptr, nullptr};
@@ -1876,8 +1876,7 @@ void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width
     for (uint32_t l = 0; l < L; ++l) placed[l].assign(cnt[l].size(), 0);
   };
   // pass 1: the leaf histogram, uploads beside the counting (a text of one
-  // piece skips it: that piece's own histogram is the text's)
-  const bool single = n <= P;
+  // piece skips it)
   const uint64_t bins = uint64_t(1) << L;
   cudaEvent_t used[2] = {nullptr, nullptr};  // the last work on s that read text buffer b
   if (!single) {
