@@ -17,6 +17,8 @@
 
 #include "../../include/pwmgpu.h"
 #include "gen.cuh"
+#include "host_huffman.hpp"
+#include "host_stream.hpp"
 #include "host_tables.hpp"
 #include "kernels.cuh"
 
@@ -813,60 +815,16 @@ void validate_plain(uint64_t n, uint32_t width, uint32_t levels, bool allow40 = 
   if (n >= (uint64_t(1) << 62)) throw Fail{PWMGPU_ERR_ARG, "size too large"};
 }
 
+// Most chunks of a pass whose finished words stream to the host while the
+// next chunks run.
+constexpr uint32_t kMaxStreamChunks = 16;
+
 // Host ends of a plain build.  `text` (pinned: uploaded in pieces that the
 // histogram follows; else in one copy) is copied into the build's device
 // text; `wm` / `wt` receive the structures' words in their device layout,
 // streamed level group by level group as the passes complete when they are
 // pinned, else copied at the end.  The build returns once they are on the
 // host.
-// Words of a structure's levels that become complete as bit ranges of them
-// are written: a word is complete once all its bits are (bits past the
-// level's end count as written); each word is reported once.
-class LevelCompletion {
- public:
-  LevelCompletion(uint32_t levels, uint64_t nbits) : done_(levels), nbits_(nbits) {}
-  // Bits [a, b) of level m (of level_words words) are written: appends the
-  // words [w0, w1) of the level that this completes.
-  void add(uint32_t m, uint64_t a, uint64_t b, uint64_t level_words, std::vector<std::pair<uint64_t, uint64_t>>& out) {
-    if (a >= b) return;
-    if (b > nbits_ || m >= done_.size()) throw Fail{PWMGPU_ERR_CUDA, "internal: range past the level"};
-    auto& iv = done_[m];
-    uint64_t A = a, B = b;
-    auto it = iv.upper_bound(a);
-    if (it != iv.begin()) {
-      auto pv = std::prev(it);
-      if (pv->second > a) throw Fail{PWMGPU_ERR_CUDA, "internal: range written twice"};
-      if (pv->second == a) {
-        A = pv->first;
-        iv.erase(pv);
-      }
-    }
-    while (it != iv.end() && it->first <= B) {
-      if (it->first < B) throw Fail{PWMGPU_ERR_CUDA, "internal: range written twice"};
-      B = it->second;
-      it = iv.erase(it);
-    }
-    iv[A] = B;
-    // [a, b) touches words [a/64, ceil(b/64)) (to the level's end if it
-    // reaches it), none complete before; those inside [A, B) are now
-    const uint64_t c0 = (A + 63) / 64, c1 = B == nbits_ ? level_words : B / 64;
-    const uint64_t w0 = std::max(c0, a / 64), w1 = std::min(c1, b == nbits_ ? level_words : (b + 63) / 64);
-    if (w0 < w1) out.emplace_back(w0, w1);
-  }
-  bool complete(uint32_t m) const {
-    const auto& iv = done_[m];
-    return nbits_ == 0 || (iv.size() == 1 && iv.begin()->first == 0 && iv.begin()->second == nbits_);
-  }
-
- private:
-  std::vector<std::map<uint64_t, uint64_t>> done_;
-  uint64_t nbits_;
-};
-
-// Most chunks of a pass whose finished words stream to the host while the
-// next chunks run.
-constexpr uint32_t kMaxStreamChunks = 16;
-
 struct HostIO {
   const void* text = nullptr;
   uint64_t* wm = nullptr;
@@ -1120,7 +1078,8 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   auto note = [&](int st, uint32_t m, uint64_t a, uint64_t b) {  // bits [a, b) of level m written
     const Structure& S = *sts[st];
     fresh.clear();
-    done[st].add(m, a, b, level_end(S, m) - S.offs[m], fresh);
+    if (!done[st].add(m, a, b, level_end(S, m) - S.offs[m], fresh))
+      throw Fail{PWMGPU_ERR_CUDA, "internal: a streamed range past its level or written twice"};
     for (const auto& w : fresh) pend.push_back({uint64_t(st), S.offs[m] + w.first, S.offs[m] + w.second});
   };
   auto flush = [&](cudaEvent_t after) {  // the pending words, once `after` has happened
@@ -1301,138 +1260,6 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     if (stream_out) CUDA_TRY(cudaStreamSynchronize(ctx->down));
     CUDA_TRY(cudaStreamSynchronize(s));
   }
-}
-
-// ---------------------------------------------------------------------------
-// Huffman codes: pwm's canonical_huff_codes (include/huffman/huff_codes.hpp:
-// 140-285) with the same standard containers, so that priority-queue and
-// sort ties break the same way.
-// ---------------------------------------------------------------------------
-struct HuffCodes {
-  std::vector<uint64_t> len, word, level_sizes;
-  uint32_t levels = 0;
-};
-
-// entries: (symbol, frequency) in pwm's histogram order.
-HuffCodes build_huffman_codes(const std::vector<std::pair<uint64_t, uint64_t>>& entries, uint64_t max_symbol,
-                              bool is_tree) {
-  HuffCodes h;
-  if (entries.empty()) return h;
-  const uint64_t nsym = max_symbol + 1;
-  std::vector<uint64_t> freq(nsym, 0);
-  for (const auto& e : entries) freq[e.first] = e.second;
-  // pwm merges the two least frequent items of a std::priority_queue<Item,
-  // std::vector<Item>, std::greater<Item>> (ordered by occurrences only) and
-  // lengthens the codes of all symbols of the merged item, so a code length
-  // is the depth of the symbol's leaf in the tree of merges.  The same heap
-  // operations (push: push_back + push_heap, pop: pop_heap + pop_back) on
-  // (occurrences, node) pairs break ties identically; the depths come from
-  // one pass over the merge tree, parents before children.
-  struct Item {
-    uint64_t occ;
-    uint32_t node;
-    bool operator>(const Item& o) const { return occ > o.occ; }
-  };
-  std::vector<Item> heap;
-  const std::greater<Item> comp;
-  auto push = [&](Item it) {
-    heap.push_back(it);
-    std::push_heap(heap.begin(), heap.end(), comp);
-  };
-  auto pop = [&]() {
-    std::pop_heap(heap.begin(), heap.end(), comp);
-    const Item it = heap.back();
-    heap.pop_back();
-    return it;
-  };
-  h.len.assign(nsym, 0);
-  h.word.assign(nsym, 0);
-  const size_t leaves = entries.size();
-  std::vector<uint32_t> child(2 * leaves, 0);  // node leaves + i: children of merge i at 2i, 2i + 1
-  heap.reserve(leaves);
-  for (size_t i = 0; i < leaves; ++i) push(Item{entries[i].second, uint32_t(i)});
-  if (heap.size() == 1) ++h.len[entries[0].first];
-  uint32_t merges = 0;
-  while (heap.size() > 1) {
-    const Item a = pop();
-    const Item b = pop();
-    child[2 * merges] = a.node;
-    child[2 * merges + 1] = b.node;
-    push(Item{a.occ + b.occ, uint32_t(leaves + merges)});
-    ++merges;
-  }
-  if (merges) {
-    std::vector<uint64_t> depth(leaves + merges, 0);
-    for (uint32_t i = merges; i-- > 0;)  // the last merge is the root
-      for (int k = 0; k < 2; ++k) depth[child[2 * i + k]] = depth[leaves + i] + 1;
-    for (size_t i = 0; i < leaves; ++i) h.len[entries[i].first] = depth[i];
-  }
-  std::vector<uint64_t> order(nsym);
-  std::iota(order.begin(), order.end(), uint64_t(0));
-  std::sort(order.begin(), order.end(), [&](uint64_t a, uint64_t b) { return h.len[a] < h.len[b]; });
-  h.levels = uint32_t(h.len[order.back()]);
-  std::vector<uint64_t> sizes(h.levels, 0);
-  uint64_t k = 0;
-  while (k < nsym && h.len[order[k]] == 0) ++k;
-  if (!is_tree) {
-    uint64_t cur = 1;
-    std::vector<uint64_t> words{0, 1};
-    while (k < nsym) {
-      if (h.len[order[k]] > cur) {
-        for (uint64_t i = cur; i < h.len[order[k]]; ++i) {
-          std::vector<uint64_t> nw;
-          nw.reserve(words.size() * 2);
-          for (uint64_t cw : words) nw.push_back(cw << 1);
-          for (uint64_t cw : words) nw.push_back((cw << 1) + 1);
-          words = std::move(nw);
-        }
-        cur = h.len[order[k]];
-      }
-      while (k < nsym && h.len[order[k]] == cur) {
-        const uint64_t sy = order[k++];
-        h.word[sy] = words.back();
-        words.pop_back();
-        sizes[h.len[sy] - 1] += freq[sy];
-      }
-    }
-  } else {
-    uint64_t cw = 0;
-    auto gen = [&]() {
-      const uint64_t sy = order[k];
-      h.word[sy] = (~cw) & ((uint64_t(1) << h.len[sy]) - 1);
-      sizes[h.len[sy] - 1] += freq[sy];
-    };
-    gen();
-    for (++k; k < nsym; ++k) {
-      cw = (cw + 1) << (h.len[order[k]] - h.len[order[k - 1]]);
-      gen();
-    }
-  }
-  for (uint64_t i = h.levels - 1; i > 0; --i) sizes[i - 1] += sizes[i];
-  h.level_sizes = sizes;
-  return h;
-}
-
-// pwm's histogram order (include/util/histogram.hpp:39-76): ascending symbols
-// for 8-bit texts; for wider texts the iteration order of a
-// std::unordered_map filled in order of first occurrence.
-template <typename A>
-std::vector<std::pair<uint64_t, uint64_t>> histogram_order(const std::vector<uint64_t>& count,
-                                                           const std::vector<uint64_t>& first, uint32_t width) {
-  std::vector<std::pair<uint64_t, uint64_t>> out;
-  if (width == 1) {
-    for (uint64_t c = 0; c < count.size(); ++c)
-      if (count[c]) out.emplace_back(c, count[c]);
-    return out;
-  }
-  std::vector<uint64_t> syms;
-  for (uint64_t c = 0; c < count.size(); ++c)
-    if (count[c]) syms.push_back(c);
-  std::sort(syms.begin(), syms.end(), [&](uint64_t a, uint64_t b) { return first[a] < first[b]; });
-  std::unordered_map<A, uint64_t> m;
-  for (uint64_t c : syms) m.emplace(A(c), count[c]);
-  for (const auto& e : m) out.emplace_back(uint64_t(e.first), e.second);
-  return out;
 }
 
 // Symbol histogram + first occurrences of a device text on the GPU, then the

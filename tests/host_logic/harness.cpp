@@ -1,0 +1,88 @@
+// Host-logic harness for tests/test_host_logic.py: runs the library's pure
+// C++ host code (pwm_gb300/csrc/host_huffman.hpp, host_stream.hpp) on inputs
+// from stdin and prints the results.
+//
+//   harness huff <is_tree> <width>   stdin: nsym, then "count first" per symbol
+//                                    stdout: levels, level sizes, then "len word" per symbol
+//   harness lc <seed> <trials>       randomized self-check of LevelCompletion
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "../../pwm_gb300/csrc/host_huffman.hpp"
+#include "../../pwm_gb300/csrc/host_stream.hpp"
+
+using namespace pwmgpu;
+
+static int huff(bool is_tree, uint32_t width) {
+  unsigned long long nsym = 0;
+  if (scanf("%llu", &nsym) != 1) return 2;
+  std::vector<uint64_t> count(nsym), first(nsym);
+  uint64_t max_symbol = 0;
+  for (uint64_t c = 0; c < nsym; ++c) {
+    unsigned long long k = 0, f = 0;
+    if (scanf("%llu %llu", &k, &f) != 2) return 2;
+    count[c] = k;
+    first[c] = f;
+    if (k) max_symbol = c;
+  }
+  const auto entries = width == 1 ? histogram_order<uint8_t>(count, first, 1) : histogram_order<uint16_t>(count, first, 2);
+  const HuffCodes h = build_huffman_codes(entries, max_symbol, is_tree);
+  printf("%u\n", h.levels);
+  for (uint64_t s : h.level_sizes) printf("%llu ", (unsigned long long)s);
+  printf("\n");
+  for (size_t c = 0; c < h.len.size(); ++c) printf("%llu %llu\n", (unsigned long long)h.len[c], (unsigned long long)h.word[c]);
+  return 0;
+}
+
+// Random partitions of levels into bit ranges, recorded in random order: every
+// word must be reported exactly once, only once all its bits are written, and
+// overlapping or out-of-range ranges must be refused.
+static int lc(uint64_t seed, int trials) {
+  std::mt19937_64 rng(seed);
+  for (int trial = 0; trial < trials; ++trial) {
+    const uint64_t n = rng() % 3000 + 1;
+    const uint64_t lw = (n + 63) / 64 + rng() % 4;
+    std::vector<uint64_t> cuts{0, n};
+    const int k = int(rng() % 16);
+    for (int i = 0; i < k; ++i) cuts.push_back(rng() % (n + 1));
+    std::sort(cuts.begin(), cuts.end());
+    std::vector<std::pair<uint64_t, uint64_t>> parts;
+    for (size_t i = 0; i + 1 < cuts.size(); ++i) parts.push_back({cuts[i], cuts[i + 1]});
+    std::shuffle(parts.begin(), parts.end(), rng);
+    LevelCompletion done(2, n);
+    std::vector<int> sent(lw, 0), written(n, 0);
+    for (auto& p : parts) {
+      std::vector<std::pair<uint64_t, uint64_t>> out;
+      if (!done.add(1, p.first, p.second, lw, out)) { printf("refused a valid range\n"); return 1; }
+      for (uint64_t b = p.first; b < p.second; ++b) written[b] = 1;
+      for (auto& w : out)
+        for (uint64_t x = w.first; x < w.second; ++x) {
+          if (x >= lw || sent[x]) { printf("word %llu reported twice or past the level\n", (unsigned long long)x); return 1; }
+          for (uint64_t b = x * 64; b < x * 64 + 64 && b < n; ++b)
+            if (!written[b]) { printf("word %llu reported early\n", (unsigned long long)x); return 1; }
+          sent[x] = 1;
+        }
+    }
+    for (uint64_t x = 0; x < lw; ++x)
+      if (!sent[x]) { printf("word %llu never reported\n", (unsigned long long)x); return 1; }
+    if (!done.complete(1)) { printf("level not complete\n"); return 1; }
+    std::vector<std::pair<uint64_t, uint64_t>> out;
+    if (parts.size() && parts[0].second > parts[0].first && done.add(1, parts[0].first, parts[0].second, lw, out)) {
+      printf("accepted a range twice\n");
+      return 1;
+    }
+    if (done.add(1, 0, n + 1, lw, out) || done.add(2, 0, 1, lw, out)) { printf("accepted an invalid range\n"); return 1; }
+  }
+  printf("ok\n");
+  return 0;
+}
+
+int main(int argc, char** argv) {
+  if (argc >= 4 && !strcmp(argv[1], "huff")) return huff(atoi(argv[2]) != 0, uint32_t(atoi(argv[3])));
+  if (argc >= 4 && !strcmp(argv[1], "lc")) return lc(strtoull(argv[2], nullptr, 10), atoi(argv[3]));
+  fprintf(stderr, "usage: harness huff <is_tree> <width> | lc <seed> <trials>\n");
+  return 2;
+}
