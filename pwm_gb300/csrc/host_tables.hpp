@@ -11,7 +11,7 @@
 #include <unordered_map>
 #include <vector>
 
-#include "tile.cuh"
+#include "tile_layout.hpp"
 
 namespace pwmgpu {
 

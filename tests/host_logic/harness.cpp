@@ -5,6 +5,8 @@
 //   harness huff <is_tree> <width>   stdin: nsym, then "count first" per symbol
 //                                    stdout: levels, level sizes, then "len word" per symbol
 //   harness lc <seed> <trials>       randomized self-check of LevelCompletion
+//   harness plan <L> <tree> <kmax> <T>  stdin: the 2^L leaf counts
+//                                    stdout: the tile-pass plan (host_tables.hpp)
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -13,6 +15,7 @@
 
 #include "../../pwm_gb300/csrc/host_huffman.hpp"
 #include "../../pwm_gb300/csrc/host_stream.hpp"
+#include "../../pwm_gb300/csrc/host_tables.hpp"
 
 using namespace pwmgpu;
 
@@ -80,9 +83,41 @@ static int lc(uint64_t seed, int trials) {
   return 0;
 }
 
+// The plan of a plain tile build from its leaf histogram: zero counts, tree
+// levels left to the regroup, and per pass its segments and start tables.
+static int plan(uint32_t L, bool tree, int kmax, uint32_t T) {
+  std::vector<uint64_t> hist(size_t(1) << L);
+  for (auto& h : hist) {
+    unsigned long long v = 0;
+    if (scanf("%llu", &v) != 1) return 2;
+    h = v;
+  }
+  const PrefixCounts cnt = fold_prefix_counts(hist.data(), L);
+  std::vector<uint32_t> regroup;
+  const auto passes = plan_tile_passes(cnt, L, kmax, T, tree, &regroup);
+  const LevelTables t = build_tables_tile(cnt, L, tree ? regroup : std::vector<uint32_t>{});
+  printf("zeros");
+  for (uint64_t z : t.zeros) printf(" %llu", (unsigned long long)z);
+  printf("\nregroup");
+  for (uint32_t r : regroup) printf(" %u", r);
+  printf("\n");
+  for (const auto& p : passes) {
+    printf("pass %u %d %d %d %u %zu\n", p.level, p.K, int(p.out), int(p.segmented), p.tiles, p.segs.size());
+    for (const auto& sg : p.segs) {
+      printf("seg %llu %llu %u %llu\ntable", (unsigned long long)sg.in_begin, (unsigned long long)sg.m, sg.tile0,
+             (unsigned long long)sg.group);
+      for (int i = 0; i < tile_table_size(p.K); ++i) printf(" %llu", (unsigned long long)p.table[sg.table + i]);
+      printf("\n");
+    }
+  }
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc >= 6 && !strcmp(argv[1], "plan"))
+    return plan(uint32_t(atoi(argv[2])), atoi(argv[3]) != 0, atoi(argv[4]), uint32_t(atoi(argv[5])));
   if (argc >= 4 && !strcmp(argv[1], "huff")) return huff(atoi(argv[2]) != 0, uint32_t(atoi(argv[3])));
   if (argc >= 4 && !strcmp(argv[1], "lc")) return lc(strtoull(argv[2], nullptr, 10), atoi(argv[3]));
-  fprintf(stderr, "usage: harness huff <is_tree> <width> | lc <seed> <trials>\n");
+  fprintf(stderr, "usage: harness huff <is_tree> <width> | lc <seed> <trials> | plan <L> <tree> <kmax> <T>\n");
   return 2;
 }

@@ -76,3 +76,99 @@ def test_code_tables_match_pwm_seeded(pg, harness, golden_seeded, tree):
 def test_stream_tracker(harness):
     r = subprocess.run([harness, "lc", "2024", "3000"], capture_output=True, text=True)
     assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr
+
+
+def rev(x, bits):
+    return int(format(x, "0%db" % bits)[::-1], 2) if bits else 0
+
+
+def expected_plan(hist, L, tree, kmax, T):
+    """The pass plan restated from first principles: a run of the matrix's
+    level m starts at the count of elements whose key_m (first m bits, first
+    bit least significant) is smaller, a run of the tree's at the count of
+    elements with a smaller m-bit prefix."""
+    n = int(hist.sum())
+    cnt = {m: hist.reshape(1 << m, -1).sum(axis=1).astype(np.int64) for m in range(L + 1)}
+    pn = {m: np.concatenate([[0], np.cumsum(cnt[m])]) for m in cnt}
+    pk = {m: np.concatenate([[0], np.cumsum([cnt[m][rev(x, m)] for x in range(1 << m)])]) for m in cnt}
+    zeros = [int(cnt[m + 1][0::2].sum()) for m in range(L)]
+    regroup, passes, l = [], [], 0
+    while l < L:
+        K = min(kmax, L - l)
+        out = l + K < L
+        groups = 1 << l
+        seg = tree and (l == 0 or (groups <= 65536 and n >= groups * 4 * T))
+        TS = 2 * ((1 << K) - 1) + (1 << K)
+        segs, tiles = [], 0
+        if seg:
+            for g in range(groups):
+                m = int(cnt[l][rev(g, l)])
+                if m == 0:
+                    continue
+                tab = [0] * TS
+                for j in range(K):
+                    for v in range(1 << j):
+                        x = (v << l) | g
+                        tab[(1 << j) - 1 + v] = int(pk[l + j][x])
+                        tab[(1 << K) - 1 + (1 << j) - 1 + v] = int(pn[l + j][rev(x, l + j)])
+                if out:
+                    for v in range(1 << K):
+                        tab[2 * ((1 << K) - 1) + v] = int(pk[l + K][(v << l) | g])
+                segs.append((int(pk[l][g]), m, tiles, g, tab))
+                tiles += (m + T - 1) // T
+        else:
+            tab = [0] * TS
+            for j in range(K + (1 if out else 0)):
+                ck = np.zeros(1 << j, dtype=np.int64)  # key of bits l..l+j-1, first least significant
+                for p, c in enumerate(cnt[l + j]):
+                    ck[rev(p & ((1 << j) - 1), j)] += c
+                run = np.concatenate([[0], np.cumsum(ck)])[:-1]
+                base = (1 << j) - 1 if j < K else 2 * ((1 << K) - 1)
+                for v in range(1 << j):
+                    tab[base + v] = int(run[v])
+            segs.append((0, n, 0, 0, tab))
+            tiles = (n + T - 1) // T
+            if tree:
+                regroup += [l + j for j in range(K) if l + j > 0]
+        passes.append(((l, K, int(out), int(seg), tiles), segs))
+        l += K
+    return zeros, regroup, passes
+
+
+def run_plan(harness, hist, L, tree, kmax, T):
+    r = subprocess.run([harness, "plan", str(L), str(int(tree)), str(kmax), str(T)],
+                       input=" ".join(str(int(x)) for x in hist), capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.strip().split("\n")
+    zeros = [int(x) for x in lines[0].split()[1:]]
+    regroup = [int(x) for x in lines[1].split()[1:]]
+    passes, i = [], 2
+    while i < len(lines):
+        f = lines[i].split()
+        head = tuple(int(x) for x in f[1:6])
+        nseg = int(f[6])
+        segs = []
+        for s in range(nseg):
+            a = [int(x) for x in lines[i + 1 + 2 * s].split()[1:]]
+            tab = [int(x) for x in lines[i + 2 + 2 * s].split()[1:]]
+            segs.append((a[0], a[1], a[2], a[3], tab))
+        passes.append((head, segs))
+        i += 1 + 2 * nseg
+    return zeros, regroup, passes
+
+
+@pytest.mark.parametrize("L,tree,kmax,T,scale", [
+    (8, True, 4, 16384, 20000),   # both passes segmented (prefixes per group)
+    (8, True, 4, 16384, 3),       # a small text: the second pass leaves the tree to the regroup
+    (12, False, 4, 4096, 50),     # matrix only: one segment per pass
+    (13, True, 3, 8192, 400),     # passes of 3 levels, segmented and not
+    (6, True, 6, 16384, 9),       # all levels in one pass
+    (1, True, 4, 16384, 7),
+])
+def test_pass_plan(harness, L, tree, kmax, T, scale):
+    rng = np.random.default_rng(L * 7 + scale)
+    hist = rng.integers(0, scale + 1, 1 << L).astype(np.int64)
+    hist[rng.random(1 << L) < 0.2] = 0  # empty groups
+    if hist.sum() == 0:
+        hist[0] = 1
+    assert run_plan(harness, hist, L, tree, kmax, T) == expected_plan(hist, L, tree, kmax, T)
