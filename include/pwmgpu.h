@@ -226,7 +226,9 @@ PWMGPU_API pwmgpu_status pwmgpu_wx_query_host(pwmgpu_ctx* ctx, const pwmgpu_wx* 
  * occurrence into d_out (same width; d_out == d_text allowed); *max_char
  * receives the number of distinct symbols - 1, what pwm returns (all ones
  * for an empty text).  8-bit symbol 255 is renumbered like any other (pwm's
- * table stops at 254).  32-bit texts: symbols below 2^24. */
+ * table stops at 254).  word_width 1, 2, 4 or 5 (pwm's 40-bit uint40_t, packed
+ * little-endian); 32-bit symbols from 2^24 up and 40-bit symbols go through a
+ * device hash table (texts of at most 2^30 symbols). */
 PWMGPU_API pwmgpu_status pwmgpu_reduce_alphabet(pwmgpu_ctx* ctx, const void* d_text, uint64_t size, uint32_t word_width,
                                                 void* d_out, uint64_t* max_char);
 

@@ -1630,7 +1630,8 @@ std::unique_ptr<pwmgpu_wx> make_wx(pwmgpu_ctx* ctx, uint64_t size, uint32_t word
 // and are OR-ed together on the host at the end.
 // ---------------------------------------------------------------------------
 constexpr uint64_t kSemiMinPiece = uint64_t(1) << 16;
-constexpr uint64_t kAlphabetMaxSymbol = uint64_t(1) << 24;  // 32-bit alphabet reduction: one bin per value
+constexpr uint64_t kAlphabetMaxSymbol = uint64_t(1) << 24;  // 32-bit alphabet reduction: one bin per value below
+constexpr uint64_t kAlphabetHashMaxSymbols = uint64_t(1) << 30;  // wider symbols: through a hash table
 constexpr uint64_t kSemiDmaMinWords = 512;  // shorter runs go through the host's OR
 
 void semi_external(pwmgpu_ctx* ctx, const void* text, uint64_t n, uint32_t width, uint32_t L, uint64_t* out_wm,
@@ -2371,16 +2372,62 @@ pwmgpu_status pwmgpu_wx_query_host(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int whi
   });
 }
 
+// pwm's reduce_alphabet for symbols too wide for one bin per value (40-bit,
+// or 32-bit from 2^24 up): a device hash table finds the distinct symbols and
+// their first positions, the host numbers them by first position, and the
+// text is renumbered through the table.  Returns the distinct symbols - 1.
+uint64_t reduce_alphabet_hashed(pwmgpu_ctx* ctx, const void* d_text, uint64_t n, uint32_t width, void* d_out) {
+  if (n > kAlphabetHashMaxSymbols) throw Fail{PWMGPU_ERR_ARG, "alphabet reduction of wide symbols: at most 2^30 symbols"};
+  cudaStream_t s = ctx->stream;
+  uint64_t cap = 1024;
+  while (cap < 2 * n) cap <<= 1;
+  auto* keys = static_cast<unsigned long long*>(ctx->grow("alpha_keys", cap * 8));
+  auto* first = static_cast<unsigned long long*>(ctx->grow("alpha_first", cap * 8));
+  auto* slot_ids = static_cast<uint32_t*>(ctx->grow("alpha_slot_ids", cap * 4));
+  auto* count = static_cast<unsigned long long*>(ctx->grow("alpha_count", 8));
+  auto* triples = static_cast<uint64_t*>(ctx->grow("alpha_triples", n * 24));
+  CUDA_TRY(cudaMemsetAsync(keys, 0xFF, cap * 8, s));
+  CUDA_TRY(cudaMemsetAsync(first, 0xFF, cap * 8, s));
+  CUDA_TRY(cudaMemsetAsync(count, 0, 8, s));
+  launch_alphabet_insert(d_text, width, n, keys, first, cap, ctx->d_status, s, &ctx->launches);
+  launch_alphabet_collect(keys, first, cap, count, triples, s, &ctx->launches);
+  uint64_t sigma = 0;
+  CUDA_TRY(cudaMemcpyAsync(&sigma, count, 8, cudaMemcpyDeviceToHost, s));
+  check_device_status(ctx);
+  if (sigma == 0 || sigma > n) throw Fail{PWMGPU_ERR_CUDA, "internal: alphabet table inconsistent"};
+  std::vector<uint64_t> t(3 * sigma);
+  CUDA_TRY(cudaMemcpyAsync(t.data(), triples, sigma * 24, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  std::vector<uint64_t> order(sigma);
+  std::iota(order.begin(), order.end(), uint64_t(0));
+  std::sort(order.begin(), order.end(), [&](uint64_t a, uint64_t b) { return t[3 * a + 2] < t[3 * b + 2]; });
+  std::vector<uint64_t> slots(sigma);
+  std::vector<uint32_t> ids(sigma);
+  for (uint64_t r = 0; r < sigma; ++r) {
+    slots[r] = t[3 * order[r]];
+    ids[r] = uint32_t(r);
+  }
+  // slots and ids go where the triples were (no longer needed on the device)
+  CUDA_TRY(cudaMemcpyAsync(triples, slots.data(), sigma * 8, cudaMemcpyHostToDevice, s));
+  auto* d_ids = reinterpret_cast<uint32_t*>(triples + sigma);
+  CUDA_TRY(cudaMemcpyAsync(d_ids, ids.data(), sigma * 4, cudaMemcpyHostToDevice, s));
+  launch_scatter_ids(triples, d_ids, sigma, slot_ids, s, &ctx->launches);
+  launch_alphabet_remap(d_text, width, n, keys, slot_ids, cap, d_out, ctx->d_status, s, &ctx->launches);
+  check_device_status(ctx);  // also: the pageable copies above have been read
+  return sigma - 1;
+}
+
 pwmgpu_status pwmgpu_reduce_alphabet(pwmgpu_ctx* ctx, const void* d_text, uint64_t size, uint32_t word_width,
                                      void* d_out, uint64_t* max_char) {
   if (!ctx || !max_char || (size && (!d_text || !d_out))) return PWMGPU_ERR_ARG;
   return guarded(ctx, [&]() {
-    if (!valid_width(word_width)) throw Fail{PWMGPU_ERR_ARG, "word_width must be 1, 2 or 4"};
+    if (!valid_plain_width(word_width)) throw Fail{PWMGPU_ERR_ARG, "word_width must be 1, 2, 4 or 5"};
     *max_char = ~uint64_t(0);  // pwm: no symbol, 0 - 1
     if (size == 0) return PWMGPU_OK;
     cudaStream_t s = ctx->stream;
     CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, 4, s));
     uint64_t nsym = word_width == 1 ? 256 : 65536;
+    bool hashed = word_width == 5;
     if (word_width == 4) {
       auto* d_max = static_cast<unsigned int*>(ctx->grow("alpha_max", 4));
       CUDA_TRY(cudaMemsetAsync(d_max, 0, 4, s));
@@ -2388,8 +2435,12 @@ pwmgpu_status pwmgpu_reduce_alphabet(pwmgpu_ctx* ctx, const void* d_text, uint64
       unsigned int mx = 0;
       CUDA_TRY(cudaMemcpyAsync(&mx, d_max, 4, cudaMemcpyDeviceToHost, s));
       CUDA_TRY(cudaStreamSynchronize(s));
-      if (mx >= kAlphabetMaxSymbol) throw Fail{PWMGPU_ERR_ARG, "32-bit symbols must be below 2^24"};
+      hashed = mx >= kAlphabetMaxSymbol;
       nsym = uint64_t(mx) + 1;
+    }
+    if (hashed) {
+      *max_char = reduce_alphabet_hashed(ctx, d_text, size, word_width, d_out);
+      return PWMGPU_OK;
     }
     // symbol counts and first occurrences, then ids in order of first occurrence
     auto* d_hist = static_cast<unsigned long long*>(ctx->grow("sym_hist", nsym * 8));

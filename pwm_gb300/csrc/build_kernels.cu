@@ -593,6 +593,100 @@ __global__ void widen40_kernel(const uint8_t* in, uint64_t n, uint32_t* out) {
   }
 }
 
+// Alphabet reduction of arbitrary 32- and 40-bit symbols: an open-addressing
+// hash table (power-of-two capacity, at least twice the text) keyed by the
+// symbol, each slot keeping the symbol's first position.  Probing is linear
+// and bounded by the capacity; a table that fills up sets the status.
+__device__ __forceinline__ uint64_t symbol_at(const uint8_t* text, uint32_t width, uint64_t i) {
+  if (width == 4) return reinterpret_cast<const uint32_t*>(text)[i];
+  const uint8_t* r = text + 5 * i;  // 40-bit: 5 little-endian bytes
+  return uint64_t(r[0]) | (uint64_t(r[1]) << 8) | (uint64_t(r[2]) << 16) | (uint64_t(r[3]) << 24) |
+         (uint64_t(r[4]) << 32);
+}
+__device__ __forceinline__ uint64_t slot_hash(uint64_t v) {  // splitmix64 finaliser
+  v ^= v >> 30;
+  v *= 0xbf58476d1ce4e5b9ull;
+  v ^= v >> 27;
+  v *= 0x94d049bb133111ebull;
+  return v ^ (v >> 31);
+}
+constexpr uint64_t kEmptySlot = ~0ull;  // no symbol has 64 bits
+
+__global__ void alphabet_insert_kernel(const uint8_t* text, uint32_t width, uint64_t n, unsigned long long* keys,
+                                       unsigned long long* first, uint64_t mask, uint32_t* status) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    const uint64_t v = symbol_at(text, width, i);
+    uint64_t h = slot_hash(v) & mask;
+    bool placed = false;
+    for (uint64_t probe = 0; probe <= mask; ++probe) {
+      // a slot, once set, never changes: a value read past L1 is final unless
+      // empty, and then the CAS decides (its return value, not a re-read)
+      unsigned long long k = *reinterpret_cast<volatile unsigned long long*>(&keys[h]);
+      if (k == kEmptySlot) {
+        const unsigned long long old = atomicCAS(&keys[h], kEmptySlot, (unsigned long long)v);
+        k = old == kEmptySlot ? v : old;
+      }
+      if (k == v) {
+        // first positions only decrease, so a stale value costs an extra atomic at most
+        if (i < first[h]) atomicMin(&first[h], (unsigned long long)i);
+        placed = true;
+        break;
+      }
+      h = (h + 1) & mask;
+    }
+    if (!placed) atomicOr(status, kErrBounds);
+  }
+}
+
+// The occupied slots, compacted: (slot, symbol, first position) per distinct symbol.
+__global__ void alphabet_collect_kernel(const unsigned long long* keys, const unsigned long long* first, uint64_t cap,
+                                        unsigned long long* count, uint64_t* out) {
+  for (uint64_t h = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; h < cap; h += uint64_t(gridDim.x) * blockDim.x) {
+    if (keys[h] == kEmptySlot) continue;
+    const unsigned long long k = atomicAdd(count, 1ull);
+    out[3 * k] = h;
+    out[3 * k + 1] = keys[h];
+    out[3 * k + 2] = first[h];
+  }
+}
+
+// Each symbol replaced by its slot's id, written in the text's width.
+__global__ void alphabet_remap_kernel(const uint8_t* text, uint32_t width, uint64_t n, const unsigned long long* keys,
+                                      const uint32_t* ids, uint64_t mask, uint8_t* out, uint32_t* status) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    const uint64_t v = symbol_at(text, width, i);
+    uint64_t h = slot_hash(v) & mask;
+    uint32_t id = 0;
+    bool found = false;
+    for (uint64_t probe = 0; probe <= mask; ++probe) {
+      const unsigned long long k = keys[h];
+      if (k == v) {
+        id = ids[h];
+        found = true;
+        break;
+      }
+      if (k == kEmptySlot) break;
+      h = (h + 1) & mask;
+    }
+    if (!found) atomicOr(status, kErrBounds);
+    if (width == 4) {
+      reinterpret_cast<uint32_t*>(out)[i] = id;
+    } else {
+      uint8_t* r = out + 5 * i;
+      r[0] = uint8_t(id);
+      r[1] = uint8_t(id >> 8);
+      r[2] = uint8_t(id >> 16);
+      r[3] = uint8_t(id >> 24);
+      r[4] = 0;
+    }
+  }
+}
+
+__global__ void scatter_ids_kernel(const uint64_t* slots, const uint32_t* ids, uint64_t count, uint32_t* slot_ids) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += uint64_t(gridDim.x) * blockDim.x)
+    slot_ids[slots[i]] = ids[i];
+}
+
 // Largest symbol of a 32-bit text (warp maxima, one atomic per warp).
 __global__ void max_symbol_kernel(const uint32_t* text, uint64_t n, unsigned int* out) {
   uint32_t m = 0;
@@ -754,6 +848,37 @@ void launch_fold_levels(const unsigned long long* hist, uint32_t levels, uint64_
     if (down == top) break;  // level 0 written
     top -= down;
   }
+}
+
+void launch_alphabet_insert(const void* text, uint32_t width, uint64_t n, unsigned long long* keys,
+                            unsigned long long* first, uint64_t cap, uint32_t* status, cudaStream_t s,
+                            uint64_t* launches) {
+  if (n == 0) return;
+  alphabet_insert_kernel<<<grid_for(n, 256), 256, 0, s>>>(static_cast<const uint8_t*>(text), width, n, keys, first,
+                                                         cap - 1, status);
+  ++*launches;
+}
+
+void launch_alphabet_collect(const unsigned long long* keys, const unsigned long long* first, uint64_t cap,
+                             unsigned long long* count, uint64_t* out, cudaStream_t s, uint64_t* launches) {
+  alphabet_collect_kernel<<<grid_for(cap, 256), 256, 0, s>>>(keys, first, cap, count, out);
+  ++*launches;
+}
+
+void launch_scatter_ids(const uint64_t* slots, const uint32_t* ids, uint64_t count, uint32_t* slot_ids, cudaStream_t s,
+                        uint64_t* launches) {
+  if (count == 0) return;
+  scatter_ids_kernel<<<grid_for(count, 256), 256, 0, s>>>(slots, ids, count, slot_ids);
+  ++*launches;
+}
+
+void launch_alphabet_remap(const void* text, uint32_t width, uint64_t n, const unsigned long long* keys,
+                           const uint32_t* slot_ids, uint64_t cap, void* out, uint32_t* status, cudaStream_t s,
+                           uint64_t* launches) {
+  if (n == 0) return;
+  alphabet_remap_kernel<<<grid_for(n, 256), 256, 0, s>>>(static_cast<const uint8_t*>(text), width, n, keys, slot_ids,
+                                                        cap - 1, static_cast<uint8_t*>(out), status);
+  ++*launches;
 }
 
 void launch_max_symbol(const uint32_t* text, uint64_t n, unsigned int* out, cudaStream_t s, uint64_t* launches) {

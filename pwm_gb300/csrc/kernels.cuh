@@ -37,6 +37,21 @@ void launch_fold_levels(const unsigned long long* hist, uint32_t levels, uint64_
 // dst[0..n) = src[0..n), dst[n] = *status (dst: host-mapped memory).
 void launch_readback(const unsigned long long* src, uint64_t n, const uint32_t* status, uint64_t* dst,
                      cudaStream_t s, uint64_t* launches);
+// Alphabet reduction of 32- or 40-bit symbols (width 4 or 5) through a hash
+// table of `cap` (a power of two, at least twice the text) slots: keys set to
+// all ones and first positions to all ones by the caller; insert, collect the
+// occupied slots as (slot, symbol, first) triples (count zeroed by the
+// caller), scatter the ids the host assigns to their slots, remap.
+void launch_alphabet_insert(const void* text, uint32_t width, uint64_t n, unsigned long long* keys,
+                            unsigned long long* first, uint64_t cap, uint32_t* status, cudaStream_t s,
+                            uint64_t* launches);
+void launch_alphabet_collect(const unsigned long long* keys, const unsigned long long* first, uint64_t cap,
+                             unsigned long long* count, uint64_t* out, cudaStream_t s, uint64_t* launches);
+void launch_scatter_ids(const uint64_t* slots, const uint32_t* ids, uint64_t count, uint32_t* slot_ids, cudaStream_t s,
+                        uint64_t* launches);
+void launch_alphabet_remap(const void* text, uint32_t width, uint64_t n, const unsigned long long* keys,
+                           const uint32_t* slot_ids, uint64_t cap, void* out, uint32_t* status, cudaStream_t s,
+                           uint64_t* launches);
 // Largest symbol of a 32-bit text into *out (zeroed by the caller).
 void launch_max_symbol(const uint32_t* text, uint64_t n, unsigned int* out, cudaStream_t s, uint64_t* launches);
 // out[i] = map[text[i]] (same width; in place allowed).

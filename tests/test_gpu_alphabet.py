@@ -51,6 +51,31 @@ def test_reduce_alphabet_fixtures_and_edges(pg, orc, golden_fixtures):
         assert mc == wmc and np.array_equal(got, want)
     d = torch.zeros(1, dtype=torch.uint8, device="cuda")
     assert pg.reduce_alphabet(d.data_ptr(), 0, 1) == (1 << 64) - 1  # pwm: 0 - 1
-    big = torch.from_numpy(np.array([1 << 24, 3], np.uint32).view(np.uint8)).cuda()
-    with pytest.raises(pg.PwmGpuError):
-        pg.reduce_alphabet(big.data_ptr(), 2, 4)
+
+
+def to_u40(v):
+    v = np.asarray(v, dtype=np.uint64)
+    b = np.zeros((v.size, 5), np.uint8)
+    for k in range(5):
+        b[:, k] = ((v >> np.uint64(8 * k)) & np.uint64(0xFF)).astype(np.uint8)
+    return b.reshape(-1)
+
+
+@pytest.mark.parametrize("in_place", [False, True])
+def test_reduce_wide_symbols(pg, orc, in_place):
+    """32-bit symbols from 2^24 up and 40-bit symbols (pwm's uint40_t) go
+    through a device hash table."""
+    torch = torch_cuda()
+    rng = np.random.default_rng(5)
+    for width, top, n, distinct in ((4, 1 << 32, 1_000_003, 5000), (4, 1 << 32, 300_001, 250_000),
+                                    (5, 1 << 40, 700_001, 20000), (5, 1 << 40, 3, 2)):
+        vals = rng.choice(rng.integers(0, top, distinct, dtype=np.uint64), n)
+        vals[0] = top - 1  # the largest value
+        want, wmc = orc.reduce_alphabet(vals)
+        raw = vals.astype(np.uint32).view(np.uint8) if width == 4 else to_u40(vals)
+        d = torch.from_numpy(raw.copy()).cuda()
+        out = d if in_place else torch.empty_like(d)
+        mc = pg.reduce_alphabet(d.data_ptr(), n, width, out.data_ptr())
+        got = out.cpu().numpy()
+        expect = want.astype(np.uint32).view(np.uint8) if width == 4 else to_u40(want)
+        assert mc == wmc and np.array_equal(got, expect), (width, n)
