@@ -1949,18 +1949,9 @@ void merge_shards(pwmgpu_ctx* ctx, const std::vector<const pwmgpu_wx*>& sh, pwmg
     std::vector<size_t> seg_off(L + 1, 0);
     for (uint32_t l = 0; l < L; ++l) {
       seg_off[l] = segs.size();
-      std::vector<uint64_t> rd(p, 0);
-      uint64_t dst = 0;
-      for (uint64_t b = 0; b < (uint64_t(1) << l); ++b) {
-        const uint64_t pfx = which ? b : rev_bits_host(b, l);  // the tree in prefix order, the matrix bit-reversed
-        for (uint32_t s = 0; s < p; ++s) {
-          const uint64_t len = cnt[s][l][pfx];
-          if (!len) continue;
-          const Structure& S = which ? sh[s]->wt : sh[s]->wm;
-          segs.push_back({dst, rd[s], S.d_words + S.offs[l]});
-          dst += len;
-          rd[s] += len;
-        }
+      for (const MergeRun& r : plan_merge_level(cnt, l, which == 1)) {
+        const Structure& S = which ? sh[r.shard]->wt : sh[r.shard]->wm;
+        segs.push_back({r.dst, r.src_bit, S.d_words + S.offs[l]});
       }
     }
     seg_off[L] = segs.size();

@@ -327,6 +327,35 @@ inline std::vector<TilePassHost> plan_tile_passes(const PrefixCounts& cnt, uint3
   return passes;
 }
 
+// One run of a merge of shards (pwm's merge_bit_vectors, include/
+// construction/merge.hpp:192-465): bits [src_bit, src_bit + len) of level l of
+// shard `shard` go to bit `dst` of level l of the merged structure.
+struct MergeRun {
+  uint64_t dst, shard, src_bit, len;
+};
+
+// The runs of level l of a merged structure, in destination order: block by
+// block in the level's order (the tree's natural prefix order, the matrix's
+// bit-reversed one), each block the shards' runs of it in shard order; a
+// shard's level holds its runs in the same order, so its read position is the
+// sum of its earlier runs.  cnt: the shards' prefix counts.
+inline std::vector<MergeRun> plan_merge_level(const std::vector<PrefixCounts>& cnt, uint32_t l, bool tree) {
+  std::vector<MergeRun> runs;
+  std::vector<uint64_t> rd(cnt.size(), 0);
+  uint64_t dst = 0;
+  for (uint64_t b = 0; b < (uint64_t(1) << l); ++b) {
+    const uint64_t pfx = tree ? b : rev_bits_host(b, l);
+    for (size_t s = 0; s < cnt.size(); ++s) {
+      const uint64_t len = cnt[s][l][pfx];
+      if (!len) continue;
+      runs.push_back({dst, uint64_t(s), rd[s], len});
+      dst += len;
+      rd[s] += len;
+    }
+  }
+  return runs;
+}
+
 // Tables of a Huffman-shaped text from its weighted codes.  want_tree: also
 // the segments.
 inline LevelTables build_tables(const std::vector<WeightedCode>& codes, uint32_t L, const std::vector<PassPlan>& plan,

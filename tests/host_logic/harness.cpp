@@ -7,6 +7,8 @@
 //   harness lc <seed> <trials>       randomized self-check of LevelCompletion
 //   harness plan <L> <tree> <kmax> <T>  stdin: the 2^L leaf counts
 //                                    stdout: the tile-pass plan (host_tables.hpp)
+//   harness merge <L> <shards> <tree>    stdin: each shard's 2^L leaf counts
+//                                    stdout: per level, the merge runs "dst shard src len"
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -113,7 +115,29 @@ static int plan(uint32_t L, bool tree, int kmax, uint32_t T) {
   return 0;
 }
 
+static int merge(uint32_t L, uint32_t shards, bool tree) {
+  std::vector<PrefixCounts> cnt;
+  std::vector<uint64_t> hist(size_t(1) << L);
+  for (uint32_t s = 0; s < shards; ++s) {
+    for (auto& h : hist) {
+      unsigned long long v = 0;
+      if (scanf("%llu", &v) != 1) return 2;
+      h = v;
+    }
+    cnt.push_back(fold_prefix_counts(hist.data(), L));
+  }
+  for (uint32_t l = 0; l < L; ++l) {
+    printf("level %u\n", l);
+    for (const MergeRun& r : plan_merge_level(cnt, l, tree))
+      printf("%llu %llu %llu %llu\n", (unsigned long long)r.dst, (unsigned long long)r.shard,
+             (unsigned long long)r.src_bit, (unsigned long long)r.len);
+  }
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc >= 5 && !strcmp(argv[1], "merge"))
+    return merge(uint32_t(atoi(argv[2])), uint32_t(atoi(argv[3])), atoi(argv[4]) != 0);
   if (argc >= 6 && !strcmp(argv[1], "plan"))
     return plan(uint32_t(atoi(argv[2])), atoi(argv[3]) != 0, atoi(argv[4]), uint32_t(atoi(argv[5])));
   if (argc >= 4 && !strcmp(argv[1], "huff")) return huff(atoi(argv[2]) != 0, uint32_t(atoi(argv[3])));

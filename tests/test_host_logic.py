@@ -172,3 +172,41 @@ def test_pass_plan(harness, L, tree, kmax, T, scale):
     if hist.sum() == 0:
         hist[0] = 1
     assert run_plan(harness, hist, L, tree, kmax, T) == expected_plan(hist, L, tree, kmax, T)
+
+
+def expected_merge(hists, L, tree):
+    """pwm's merge order restated: level l of the merged structure is, block by
+    block in the level's order (natural prefixes for the tree, bit-reversed
+    for the matrix), the concatenation of the shards' runs of that block."""
+    levels = []
+    for l in range(L):
+        counts = [h.reshape(1 << l, -1).sum(axis=1) for h in hists]
+        runs, dst, rd = [], 0, [0] * len(hists)
+        for b in range(1 << l):
+            pfx = b if tree else rev(b, l)
+            for s, c in enumerate(counts):
+                if c[pfx]:
+                    runs.append((dst, s, rd[s], int(c[pfx])))
+                    dst += int(c[pfx])
+                    rd[s] += int(c[pfx])
+        assert dst == sum(int(h.sum()) for h in hists)
+        levels.append(runs)
+    return levels
+
+
+@pytest.mark.parametrize("L,shards,tree", [(8, 4, True), (8, 4, False), (5, 7, True), (11, 3, False), (1, 2, True)])
+def test_merge_plan(harness, L, shards, tree):
+    rng = np.random.default_rng(L * 31 + shards)
+    hists = [rng.integers(0, 20, 1 << L) * (rng.random(1 << L) < 0.6) for _ in range(shards)]
+    hists[1 % shards][:] = 0  # an empty shard
+    r = subprocess.run([harness, "merge", str(L), str(shards), str(int(tree))],
+                       input=" ".join(str(int(x)) for h in hists for x in h), capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got, cur = [], None
+    for ln in r.stdout.strip().split("\n"):
+        if ln.startswith("level"):
+            cur = []
+            got.append(cur)
+        else:
+            cur.append(tuple(int(x) for x in ln.split()))
+    assert got == expected_merge(hists, L, tree)
