@@ -64,3 +64,16 @@ def test_host_generator_is_deterministic(lib):
     assert (m < 2000).mean() > 0.5  # the geometric half is concentrated on small ids
     u = pg.generate(pg.GEN_UNIFORM, 1, 100_000, 4, param=1 << 20)
     assert u.max() < (1 << 20)
+
+
+def test_header_compiles_as_c(tmp_path):
+    """include/pwmgpu.h is a C header (plain types, C linkage): a C99 program
+    that takes the address of every declared entry point compiles cleanly."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    refs = "\n".join("  (void)&%s;" % s for s in _lib.declared_symbols())
+    src = tmp_path / "use_abi.c"
+    src.write_text('#include "pwmgpu.h"\nint main(void) {\n%s\n  return 0;\n}\n' % refs)
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-c",
+                        f"-I{os.path.join(root, 'include')}", str(src), "-o", str(tmp_path / "use_abi.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
