@@ -123,6 +123,21 @@ PWMGPU_API pwmgpu_status pwmgpu_ctx_set_upload_piece_bytes(pwmgpu_ctx* ctx, uint
  * chunks run; 1 launches each pass whole and streams level groups per pass. */
 PWMGPU_API pwmgpu_status pwmgpu_ctx_set_stream_chunks(pwmgpu_ctx* ctx, uint32_t chunks);
 
+/* Bound on the polls of one decoupled look-back wait of the tile engine
+ * (each poll sleeps about 64 ns; 0 restores the default of 2^24, about a
+ * second).  A wait that runs out records a timeout in the context's status
+ * word and the kernel carries on with a zero prefix, so it always returns;
+ * the call that reads the status (pwmgpu_wx_check, the host-to-host calls)
+ * returns PWMGPU_ERR_TIMEOUT and the context stays usable. */
+PWMGPU_API pwmgpu_status pwmgpu_ctx_set_spin_limit(pwmgpu_ctx* ctx, uint32_t polls);
+
+/* Failure injection for tests, on the host side: while enabled, every
+ * look-back pass of a device-text plain build is launched without its first
+ * tile, so that tile never publishes its counts and the tiles of its segment
+ * wait until the spin limit.  The build then reports PWMGPU_ERR_TIMEOUT (its
+ * output is undefined, every write stays in bounds).  Off by default. */
+PWMGPU_API pwmgpu_status pwmgpu_ctx_test_withhold_tile(pwmgpu_ctx* ctx, int enable);
+
 /* Frees what the context keeps between calls (scratch buffers, cached shard
  * structures of sharded and semi-external builds, pinned staging) after its
  * streams finish; later calls allocate again. */
@@ -394,24 +409,26 @@ PWMGPU_API pwmgpu_status pwmgpu_generate_batch(uint64_t seed, uint32_t count, ui
  *
  * No counterpart in the reference: pwm builds rank/select support on the
  * host with std::vector.  This entry point exists for callers that cannot
- * allocate device memory while they run -- code that records CUDA graphs,
- * plugins whose host framework owns every device buffer, serving loops that
- * cannot afford an allocator's implicit synchronisation.  It calls no
- * cudaMalloc/cudaFree and needs no context: its scratch is a fixed 4 MiB
- * array in the library's device image, resident on every GPU that loads the
- * library until the process exits.
+ * allocate device memory while they run -- plugins whose host framework owns
+ * every device buffer and hands them in, serving loops that cannot afford an
+ * allocator's implicit synchronisation.  It calls no cudaMalloc/cudaFree and
+ * needs no context: its scratch is a fixed 4 MiB array in the library's
+ * device image, resident on every GPU that loads the library until the
+ * process exits.
  *
  * Input: `nwords` words of one level (pwm layout).  Outputs (caller
  * allocated, device memory), identical to pwm's bin_rank_popcnt /
  * bin_select_popcnt blocks and to pwmgpu_wx_rank_select_blocks:
  *   d_l0       nwords/67108863 + 1 u64 (cleared here)
- *   d_l12      2 * (nwords/32 + 1) u32
+ *   d_l12      2 * (nwords/32 + 1) u32 (for nwords == 0 one zeroed entry)
  *   d_select0, d_select1   nwords*64/8192 + 2 u32 each
  *   d_counts   3 u64: select0 samples, select1 samples, total ones (cleared here)
  * Work is enqueued on `cuda_stream` (NULL: the default stream) of the current
  * device.  The first call on a device looks up the scratch array's device
- * address; make that first call before any stream capture.  All calls share
- * the scratch: calls that overlap on the GPU race, so serialise them (one
+ * address and keeps it for the life of the process; make that first call
+ * before any stream capture, and do not call this entry point again after a
+ * cudaDeviceReset.  All calls share the scratch and keep the last call's
+ * contents: calls that overlap on the GPU race, so serialise them (one
  * stream, or events).  nwords above PWMGPU_NOALLOC_RS_MAX_WORDS (about 2.1e9
  * bits) returns PWMGPU_ERR_ARG without enqueuing anything. */
 #define PWMGPU_NOALLOC_RS_MAX_WORDS 33423360ull

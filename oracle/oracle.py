@@ -26,12 +26,20 @@ _vp = ctypes.c_void_p
 DTYPES = {1: np.uint8, 2: np.uint16, 4: np.uint32}
 
 
+def reference_tree():
+    """The pwm source tree named by the PWM_REFERENCE environment variable,
+    or None when it is unset or absent."""
+    p = os.environ.get("PWM_REFERENCE")
+    return p if p and os.path.isdir(p) else None
+
+
 def build(ref=False):
-    """Compile liborc.so (and the reference shim when `ref` and the
-    reference tree exist)."""
+    """Compile liborc.so (and the reference shim when `ref` and the pwm
+    source tree named by PWM_REFERENCE exist)."""
     subprocess.run(["make", "-s", "-C", HERE, "liborc.so"], check=True)
-    if ref and os.path.isdir(os.environ.get("PWM_REFERENCE", "/root/reference")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    tree = reference_tree()
+    if ref and tree:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={tree}"], check=True)
 
 
 def _p(a, t=_u64p):
@@ -82,8 +90,12 @@ class Oracle:
             f = getattr(L, name)
             f.argtypes = [_vp, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, _u64p, _u64p, _u64p]
             f.restype = ctypes.c_int
-        L.orc_wx_ppc.argtypes = [_vp, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
-                                 _u64p, _u64p, _u64p, ctypes.c_int]
+        for name in ("orc_wx_ppc", "orc_wx_dd_ps"):
+            getattr(L, name).argtypes = [_vp, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
+                                         _u64p, _u64p, _u64p, ctypes.c_int]
+        L.orc_generate.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32,
+                                   _vp, ctypes.c_int]
+        L.orc_generate_batch.argtypes = [ctypes.c_uint64, ctypes.c_uint32, _u64p, _u32p, _vp]
         L.orc_rank_l0_size.argtypes = [ctypes.c_uint64]
         L.orc_rank_l0_size.restype = ctypes.c_uint64
         L.orc_rank_l12_size.argtypes = [ctypes.c_uint64]
@@ -111,7 +123,7 @@ class Oracle:
             getattr(L, name).argtypes = [_vp, ctypes.c_uint64, ctypes.c_uint64]
             getattr(L, name).restype = ctypes.c_uint64
         L.orc_cpu_step.argtypes = [_vp, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, _u64p,
-                                   _u64p, _u64p, _u64p]
+                                   _u64p, _u64p, _u64p, ctypes.c_int]
         L.orc_huff_codes.argtypes = [_vp, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int, _u64p, _u64p,
                                      ctypes.c_uint64, _u64p, _u32p]
         L.orc_huff_codes.restype = ctypes.c_uint64
@@ -125,8 +137,8 @@ class Oracle:
         """pwm's reduce_alphabet (include/util/alphabet_util.hpp:18-45): the
         symbols renumbered 0, 1, ... in order of first occurrence; returns
         (renumbered text, distinct symbols - 1), the latter all ones (0 - 1
-        in uint64) for an empty text.  Parity unpinned: the reference header
-        includes STXXL and does not compile here."""
+        in uint64) for an empty text.  Pinned by tests/golden/alphabet.json,
+        outputs of pwm's own function."""
         t = np.asarray(text)
         if t.size == 0:
             return t.copy(), (1 << 64) - 1
@@ -150,9 +162,9 @@ class Oracle:
         words = np.zeros(max(total, 1), dtype=np.uint64)
         zeros = np.zeros(max(levels, 1), dtype=np.uint64)
         f = {"ps": self.L.orc_wx_ps, "pc": self.L.orc_wx_pc, "naive": self.L.orc_wx_naive,
-             "ppc": self.L.orc_wx_ppc}[variant]
+             "ppc": self.L.orc_wx_ppc, "dd_ps": self.L.orc_wx_dd_ps}[variant]
         args = [text.ctypes.data_as(_vp), n, w, levels, int(is_tree), _p(words), _p(offs), _p(zeros)]
-        if variant == "ppc":
+        if variant in ("ppc", "dd_ps"):
             args.append(threads)
         f(*args)
         if n == 0:
@@ -164,12 +176,33 @@ class Oracle:
         return (np.zeros(max(total, 1), dtype=np.uint64), np.zeros(max(total, 1), dtype=np.uint64), offs,
                 np.zeros(max(levels, 1), dtype=np.uint64))
 
-    def cpu_step(self, text, levels, threads, bufs):
-        """CPU baseline step: matrix + tree (parallel prefix counting) and
+    CPU_VARIANTS = {"ppc": 0, "dd_ps": 1}
+
+    def cpu_step(self, text, levels, threads, bufs, variant="ppc"):
+        """CPU baseline step: matrix + tree with pwm's parallel prefix
+        counting (wx_ppc) or domain decomposition (wx_dd_ps), then
         rank/select support of every level."""
         wm, wt, offs, zeros = bufs
         self.L.orc_cpu_step(text.ctypes.data_as(_vp), text.size, text.dtype.itemsize, levels, threads, _p(wm), _p(wt),
-                            _p(offs), _p(zeros))
+                            _p(offs), _p(zeros), self.CPU_VARIANTS[variant])
+
+    def generate(self, dist, seed, n, width, param=0, threads=0):
+        """Seeded synthetic text, identical to pwm_gb300.generate (the shared
+        generator header), produced without the GPU library."""
+        out = np.empty(n, dtype=DTYPES[width])
+        if n:
+            self.L.orc_generate(int(dist), int(seed), int(param), int(n), int(width), out.ctypes.data_as(_vp),
+                                int(threads))
+        return out
+
+    def generate_batch(self, seed, count):
+        """The batched workload's texts (pwm_gb300.generate_batch's)."""
+        offs = np.zeros(count + 1, dtype=np.uint64)
+        levels = np.zeros(max(count, 1), dtype=np.uint32)
+        self.L.orc_generate_batch(int(seed), int(count), _p(offs), _p(levels, _u32p), None)
+        texts = np.zeros(max(int(offs[-1]), 1), dtype=np.uint8)
+        self.L.orc_generate_batch(int(seed), int(count), _p(offs), _p(levels, _u32p), texts.ctypes.data_as(_vp))
+        return texts[:int(offs[-1])], offs, levels[:count]
 
     # -- rank / select -----------------------------------------------------
     def rank_select_blocks(self, level_words):
@@ -300,6 +333,14 @@ class Reference:
                                      _u64p, _u64p, ctypes.c_uint64, _u64p]
         L.pwmref_copy_bits_u8.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]
         L.pwmref_copy_bits_u64.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]
+        L.pwmref_reduce_alphabet.argtypes = [ctypes.c_uint32, _vp, ctypes.c_uint64]
+        L.pwmref_reduce_alphabet.restype = ctypes.c_uint64
+
+    def reduce_alphabet(self, text):
+        """pwm's own reduce_alphabet: (renumbered copy, max_char)."""
+        t = np.ascontiguousarray(text).copy()
+        m = self.L.pwmref_reduce_alphabet(t.dtype.itemsize, t.ctypes.data_as(_vp), t.size)
+        return t, m
 
     def copy_bits(self, dst, src, dst_off, src_off, length):
         """pwm's copy_bits on numpy arrays of uint8 or uint64 words (dst in place)."""

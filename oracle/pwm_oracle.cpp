@@ -30,6 +30,10 @@
 #include <vector>
 #include <omp.h>
 
+// The seeded input generator shared with the GPU library (plain C++): the
+// oracle produces the same texts without loading the GPU library.
+#include "../pwm_gb300/csrc/gen.hpp"
+
 namespace {
 
 inline uint64_t sym_at(const void* t, uint32_t w, uint64_t i) {
@@ -96,6 +100,10 @@ uint64_t orc_layout(uint32_t levels, const uint64_t* level_bits, uint64_t* offse
 // Plain construction
 // ---------------------------------------------------------------------------
 
+}  // extern "C"
+
+namespace {
+
 // Prefix sorting, restating ps() (include/construction/ps.hpp:13-66) with the
 // helpers scan_text_compute_first_level_bv_and_last_level_hist
 // (building_blocks.hpp:72-85), compute_borders_optional_zeros_rho
@@ -103,19 +111,30 @@ uint64_t orc_layout(uint32_t levels, const uint64_t* level_bits, uint64_t* offse
 // (building_blocks.hpp:155-162).  The WM visits prefix blocks in bit-reversed
 // order: the live rho of ctx_generic.hpp:41-67 equals reverse_bits(i, level)
 // at level `level` (permutation.hpp:16-29).  `bv` holds levels*stride words
-// in the flat layout, `zeros` receives all L zero counts for a WM.
-int orc_wx_ps(const void* text, uint64_t n, uint32_t w, uint32_t levels, int is_tree,
-              uint64_t* bv, const uint64_t* offsets, uint64_t* zeros) {
+// in the flat layout, `zeros` receives all L zero counts for a WM.  Templated
+// on the symbol type like pwm's (the sorted copy holds symbols, ps.hpp:18).
+// When `level_hist` is given it also keeps pwm's hist_at_level(l) for every
+// level (ctx_options::hist::all_level, ctx_generic.hpp:126-255):
+// level_hist[l][x] = symbols whose l-bit prefix is x, level_hist[0][0] = n
+// (ps.hpp:64); wx_dd_ps merges with them.
+template <typename T>
+int ps_core(const T* text, uint64_t n, uint32_t levels, int is_tree, uint64_t* bv, const uint64_t* offsets,
+            uint64_t* zeros, std::vector<std::vector<uint64_t>>* level_hist) {
   if (n == 0 || levels == 0) return 0;  // wx_ps.hpp:39-45: empty structure
   const uint64_t sigma = 1ULL << levels;
   std::vector<uint64_t> hist(sigma, 0), next(sigma, 0), borders(sigma, 0);
-  std::vector<uint64_t> sorted(n);
+  std::vector<T> sorted(n);
   // Hot loop 1: level-0 bits plus the leaf histogram.
   write_bits(bv + offsets[0], n, [&](uint64_t i) {
-    uint64_t c = sym_at(text, w, i);
+    const uint64_t c = text[i];
     ++hist[c];
     return (c >> (levels - 1)) & 1ULL;
   });
+  if (level_hist) {
+    level_hist->assign(levels + 1, std::vector<uint64_t>());
+    (*level_hist)[levels] = hist;
+    (*level_hist)[0].assign(1, n);
+  }
   if (!is_tree) {
     for (uint32_t l = 0; l < levels; ++l) zeros[l] = 0;
     for (uint64_t c = 0; c < sigma; c += 2) zeros[levels - 1] += hist[c];
@@ -125,6 +144,7 @@ int orc_wx_ps(const void* text, uint64_t n, uint32_t w, uint32_t levels, int is_
     cur >>= 1;
     for (uint64_t i = 0; i < cur; ++i) next[i] = hist[2 * i] + hist[2 * i + 1];
     std::swap(hist, next);
+    if (level_hist) (*level_hist)[level].assign(hist.begin(), hist.begin() + cur);
     // borders in rho order
     uint64_t run = 0;
     for (uint64_t i = 0; i < cur; ++i) {
@@ -136,14 +156,165 @@ int orc_wx_ps(const void* text, uint64_t n, uint32_t w, uint32_t levels, int is_
     // Hot loop 2: stable counting sort by the level-bit prefix.
     const uint32_t shift = levels - level;
     for (uint64_t i = 0; i < n; ++i) {
-      uint64_t c = sym_at(text, w, i);
-      sorted[borders[c >> shift]++] = c;
+      const T c = text[i];
+      sorted[borders[uint64_t(c) >> shift]++] = c;
     }
     // Hot loop 3: pack the bits of the sorted sequence.
     const uint32_t bit = levels - 1 - level;
-    write_bits(bv + offsets[level], n, [&](uint64_t i) { return (sorted[i] >> bit) & 1ULL; });
+    write_bits(bv + offsets[level], n, [&](uint64_t i) { return (uint64_t(sorted[i]) >> bit) & 1ULL; });
   }
   return 0;
+}
+
+int ps_dispatch(const void* text, uint64_t n, uint32_t w, uint32_t levels, int is_tree, uint64_t* bv,
+                const uint64_t* offsets, uint64_t* zeros, std::vector<std::vector<uint64_t>>* level_hist) {
+  switch (w) {
+    case 1: return ps_core(static_cast<const uint8_t*>(text), n, levels, is_tree, bv, offsets, zeros, level_hist);
+    case 2: return ps_core(static_cast<const uint16_t*>(text), n, levels, is_tree, bv, offsets, zeros, level_hist);
+    case 4: return ps_core(static_cast<const uint32_t*>(text), n, levels, is_tree, bv, offsets, zeros, level_hist);
+    default: return ps_core(static_cast<const uint64_t*>(text), n, levels, is_tree, bv, offsets, zeros, level_hist);
+  }
+}
+
+// Bits [src_off, src_off + len) of `src` into bits [dst_off, dst_off + len)
+// of `dst` (MSB-first positions), OR-ed into destination words that start
+// zeroed.  Callers give each thread whole destination words.
+void or_bits(uint64_t* dst, uint64_t dst_off, const uint64_t* src, uint64_t src_off, uint64_t len) {
+  while (len) {
+    const uint64_t d = dst_off & 63, take = std::min<uint64_t>(64 - d, len);
+    // `take` source bits starting at src_off, left-aligned
+    const uint64_t s = src_off & 63;
+    uint64_t v = src[src_off >> 6] << s;
+    if (s && s + take > 64) v |= src[(src_off >> 6) + 1] >> (64 - s);
+    v &= take == 64 ? ~0ULL : ~(~0ULL >> take);
+    dst[dst_off >> 6] |= v >> d;
+    dst_off += take;
+    src_off += take;
+    len -= take;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_wx_ps(const void* text, uint64_t n, uint32_t w, uint32_t levels, int is_tree,
+              uint64_t* bv, const uint64_t* offsets, uint64_t* zeros) {
+  return ps_dispatch(text, n, w, levels, is_tree, bv, offsets, zeros, nullptr);
+}
+
+// Domain decomposition, restating wx_dd_ps::compute (include/wx_dd_ps.hpp:
+// 43-120) with merge_bit_vectors (include/construction/merge.hpp:192-465):
+// `threads` shards; shard s builds the slice of n/threads symbols (one more
+// for each of the first n%threads shards, wx_dd_ps.hpp:79-83) with ps(),
+// keeping every level's prefix histogram; level l of the result is, block by
+// block in the level's order (prefix order for the tree, bit-reversed prefix
+// order for the matrix: rho, permutation.hpp:16-29), the concatenation of
+// the shards' runs of that block; the matrix zeros are the shards' sums
+// (wx_dd_ps.hpp:106-113).  As in pwm, the merge splits the destination into
+// word-aligned ranges, one per thread (merge.hpp:296-306); the bit copy is
+// this file's own.  threads <= 1 is plain ps (wx_dd_ps.hpp:57-62).
+int orc_wx_dd_ps(const void* text, uint64_t n, uint32_t w, uint32_t levels, int is_tree, uint64_t* bv,
+                 const uint64_t* offsets, uint64_t* zeros, int threads) {
+  if (n == 0 || levels == 0) return 0;
+  if (threads <= 0) threads = omp_get_max_threads();
+  if (threads <= 1) return ps_dispatch(text, n, w, levels, is_tree, bv, offsets, zeros, nullptr);
+  const uint64_t shards = uint64_t(threads);
+  struct Shard {
+    uint64_t size = 0, begin = 0;
+    std::vector<uint64_t> words, offs, zeros;
+    std::vector<std::vector<uint64_t>> hist;
+  };
+  std::vector<Shard> sh(shards);
+  for (uint64_t s = 0; s < shards; ++s) {
+    sh[s].size = n / shards + (s < n % shards ? 1 : 0);
+    sh[s].begin = s * (n / shards) + std::min<uint64_t>(s, n % shards);
+  }
+#pragma omp parallel for schedule(static, 1) num_threads(threads)
+  for (int64_t si = 0; si < int64_t(shards); ++si) {
+    Shard& x = sh[size_t(si)];
+    x.offs.resize(levels);
+    uint64_t total = 0;
+    for (uint32_t l = 0; l < levels; ++l) { x.offs[l] = total; total += padded_words(x.size); }
+    x.words.assign(std::max<uint64_t>(total, 1), 0);
+    x.zeros.assign(levels, 0);
+    x.hist.assign(levels + 1, std::vector<uint64_t>());
+    if (x.size) {
+      ps_dispatch(static_cast<const uint8_t*>(text) + x.begin * w, x.size, w, levels, is_tree, x.words.data(),
+                  x.offs.data(), x.zeros.data(), &x.hist);
+    } else {
+      for (uint32_t l = 0; l <= levels; ++l) x.hist[l].assign(size_t(1) << l, 0);
+    }
+  }
+  // per level: (destination bit, shard, source bit, length) of every
+  // non-empty run, in destination order
+  struct Seg { uint64_t dst, shard, src, len; };
+  std::vector<std::vector<Seg>> segs(levels);
+  for (uint32_t l = 0; l < levels; ++l) {
+    std::vector<uint64_t> cursor(shards, 0);
+    uint64_t dst = 0;
+    const uint64_t blocks = uint64_t(1) << l;
+    for (uint64_t b = 0; b < blocks; ++b) {
+      const uint64_t prefix = is_tree ? b : reverse_bits(b, l);
+      for (uint64_t s = 0; s < shards; ++s) {
+        const uint64_t len = sh[s].hist[l][prefix];
+        if (len) segs[l].push_back({dst, s, cursor[s], len});
+        dst += len;
+        cursor[s] += len;
+      }
+    }
+  }
+  const uint64_t nw = words_for(n);
+#pragma omp parallel for schedule(static, 1) num_threads(threads)
+  for (int64_t t = 0; t < int64_t(shards); ++t) {
+    const uint64_t w0 = uint64_t(t) * (nw / shards) + std::min<uint64_t>(uint64_t(t), nw % shards);
+    const uint64_t w1 = w0 + nw / shards + (uint64_t(t) < nw % shards ? 1 : 0);
+    const uint64_t lo = w0 * 64, hi = std::min(w1 * 64, n);
+    for (uint32_t l = 0; l < levels; ++l) {
+      uint64_t* out = bv + offsets[l];
+      std::memset(out + w0, 0, (w1 - w0) * 8);
+      if (lo >= hi) continue;
+      const auto& sg = segs[l];
+      // first segment ending after lo
+      size_t k = size_t(std::upper_bound(sg.begin(), sg.end(), lo,
+                                         [](uint64_t v, const Seg& g) { return v < g.dst + g.len; }) - sg.begin());
+      for (; k < sg.size() && sg[k].dst < hi; ++k) {
+        const Seg& g = sg[k];
+        const uint64_t a = std::max(g.dst, lo), e = std::min(g.dst + g.len, hi);
+        const Shard& x = sh[g.shard];
+        or_bits(out, a, x.words.data() + x.offs[l], g.src + (a - g.dst), e - a);
+      }
+    }
+  }
+  if (!is_tree) {
+    for (uint32_t l = 0; l < levels; ++l) {
+      zeros[l] = 0;
+      for (uint64_t s = 0; s < shards; ++s) zeros[l] += sh[s].zeros[l];
+    }
+  }
+  return 0;
+}
+
+// Seeded synthetic texts, identical to the GPU library's pwmgpu_generate
+// (same header): dist 0 uniform over [0, param), 1 DNA-like, 2 Zipf(1.0) over
+// 256 symbols permuted, 3 the 16-bit mixture.
+void orc_generate(int dist, uint64_t seed, uint64_t param, uint64_t n, uint32_t w, void* out, int threads) {
+  if (threads <= 0) threads = omp_get_max_threads();
+  const pwmgpu::GenTables g = pwmgpu::gen_tables(dist, seed);
+  const uint64_t key = pwmgpu::mix64(seed);
+#pragma omp parallel for schedule(static) num_threads(threads)
+  for (int64_t i = 0; i < int64_t(n); ++i) {
+    const uint64_t v = pwmgpu::gen_value(dist, key, param, uint64_t(i), g.thr.data(), uint32_t(g.thr.size()),
+                                         g.perm.data());
+    if (w == 1) static_cast<uint8_t*>(out)[i] = uint8_t(v);
+    else if (w == 2) static_cast<uint16_t*>(out)[i] = uint16_t(v);
+    else static_cast<uint32_t*>(out)[i] = uint32_t(v);
+  }
+}
+
+// The batched workload's texts (pwmgpu_generate_batch, same header).
+void orc_generate_batch(uint64_t seed, uint32_t count, uint64_t* offsets, uint32_t* levels, uint8_t* texts) {
+  pwmgpu::generate_batch_host(seed, count, offsets, levels, texts);
 }
 
 // Prefix counting, restating pc() (include/construction/pc.hpp:12-56): the
@@ -232,10 +403,13 @@ int orc_wx_naive(const void* text, uint64_t n, uint32_t w, uint32_t levels, int 
 // leaves, then every level filled independently (one level per thread,
 // dynamic schedule) with write_symbol_bit semantics.  Like pwm's wx_ppc it
 // does not compute zeros[L-1] (left 0, see ppc.hpp:19-90).
-int orc_wx_ppc(const void* text, uint64_t n, uint32_t w, uint32_t levels, int is_tree,
-               uint64_t* bv, const uint64_t* offsets, uint64_t* zeros, int threads) {
-  if (n == 0 || levels == 0) return 0;
-  if (threads <= 0) threads = omp_get_max_threads();
+}  // extern "C"
+
+namespace {
+
+template <typename T>
+int ppc_core(const T* text, uint64_t n, uint32_t levels, int is_tree, uint64_t* bv, const uint64_t* offsets,
+             uint64_t* zeros, int threads) {
   const uint64_t sigma = 1ULL << levels;
   const uint64_t nw = words_for(n);
   std::vector<std::vector<uint64_t>> local(threads, std::vector<uint64_t>(sigma, 0));
@@ -247,7 +421,7 @@ int orc_wx_ppc(const void* text, uint64_t n, uint32_t w, uint32_t levels, int is
     for (int64_t wi = 0; wi < int64_t(nw); ++wi) {
       uint64_t start = uint64_t(wi) * 64, end = std::min(n, start + 64), word = 0;
       for (uint64_t i = start; i < end; ++i) {
-        uint64_t c = sym_at(text, w, i);
+        const uint64_t c = text[i];
         ++h[c];
         word = (word << 1) | ((c >> (levels - 1)) & 1ULL);
       }
@@ -278,12 +452,28 @@ int orc_wx_ppc(const void* text, uint64_t n, uint32_t w, uint32_t levels, int is
     std::memset(lv, 0, nw * 8);
     const uint32_t pshift = levels - level, bshift = pshift - 1;
     for (uint64_t i = 0; i < n; ++i) {
-      uint64_t c = sym_at(text, w, i);
+      const uint64_t c = text[i];
       uint64_t pos = borders[c >> pshift]++;
       lv[pos >> 6] |= ((c >> bshift) & 1ULL) << (63 - (pos & 63));
     }
   }
   return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_wx_ppc(const void* text, uint64_t n, uint32_t w, uint32_t levels, int is_tree,
+               uint64_t* bv, const uint64_t* offsets, uint64_t* zeros, int threads) {
+  if (n == 0 || levels == 0) return 0;
+  if (threads <= 0) threads = omp_get_max_threads();
+  switch (w) {
+    case 1: return ppc_core(static_cast<const uint8_t*>(text), n, levels, is_tree, bv, offsets, zeros, threads);
+    case 2: return ppc_core(static_cast<const uint16_t*>(text), n, levels, is_tree, bv, offsets, zeros, threads);
+    case 4: return ppc_core(static_cast<const uint32_t*>(text), n, levels, is_tree, bv, offsets, zeros, threads);
+    default: return ppc_core(static_cast<const uint64_t*>(text), n, levels, is_tree, bv, offsets, zeros, threads);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -864,11 +1054,6 @@ static void orc_copy_bits_t(W* dst, const W* src, uint64_t dst_off, uint64_t src
 
 extern "C" {
 
-// CPU-baseline step (bench.py's cpu_baseline leg and `--impl reference` when
-// the reference shim is not loadable): wavelet matrix and wavelet tree with
-// the parallel prefix-counting restatement (orc_wx_ppc), then rank/select
-// support (bin_rank_popcnt + both bin_select_popcnt) for every level of both,
-// levels in parallel.  wm/wt hold levels*stride words each.
 void orc_copy_bits_u8(uint8_t* dst, const uint8_t* src, uint64_t dst_off, uint64_t src_off, uint64_t len) {
   orc_copy_bits_t(dst, src, dst_off, src_off, len);
 }
@@ -876,11 +1061,22 @@ void orc_copy_bits_u64(uint64_t* dst, const uint64_t* src, uint64_t dst_off, uin
   orc_copy_bits_t(dst, src, dst_off, src_off, len);
 }
 
+// CPU-baseline step (bench.py's cpu_baseline leg and `--impl reference`):
+// wavelet matrix and wavelet tree with pwm's parallel prefix counting
+// (variant 0, orc_wx_ppc) or its domain decomposition (variant 1,
+// orc_wx_dd_ps), then rank/select support (bin_rank_popcnt + both
+// bin_select_popcnt) for every level of both, levels in parallel.  wm/wt hold
+// levels*stride words each.
 int orc_cpu_step(const void* text, uint64_t n, uint32_t w, uint32_t levels, int threads, uint64_t* wm,
-                 uint64_t* wt, const uint64_t* offsets, uint64_t* zeros) {
+                 uint64_t* wt, const uint64_t* offsets, uint64_t* zeros, int variant) {
   if (threads <= 0) threads = omp_get_max_threads();
-  orc_wx_ppc(text, n, w, levels, 0, wm, offsets, zeros, threads);
-  orc_wx_ppc(text, n, w, levels, 1, wt, offsets, nullptr, threads);
+  if (variant == 1) {
+    orc_wx_dd_ps(text, n, w, levels, 0, wm, offsets, zeros, threads);
+    orc_wx_dd_ps(text, n, w, levels, 1, wt, offsets, nullptr, threads);
+  } else {
+    orc_wx_ppc(text, n, w, levels, 0, wm, offsets, zeros, threads);
+    orc_wx_ppc(text, n, w, levels, 1, wt, offsets, nullptr, threads);
+  }
   const uint64_t nw = words_for(n);
 #pragma omp parallel for schedule(dynamic, 1) num_threads(threads)
   for (int job = 0; job < int(2 * levels); ++job) {

@@ -1,9 +1,9 @@
 // oracle/ref_driver.cpp -- TEST INFRASTRUCTURE ONLY.
 //
 // A thin extern "C" shim over kurpicz/pwm's own in-memory construction,
-// query and Huffman headers.  oracle/build_ref.sh compiles it against the
-// reference source tree into oracle/_ref/libpwmref.so (nothing of the
-// reference is copied into this repository).  tests/golden/make_golden.py
+// query and Huffman headers.  `make -C oracle ref REF=<pwm tree>` compiles it
+// against the reference source tree into oracle/_ref/libpwmref.so (nothing of
+// the reference is copied into this repository).  tests/golden/make_golden.py
 // uses it to pin the oracle restatement and to record golden vectors; tests
 // use it directly when the library is present.
 //
@@ -13,6 +13,7 @@
 #include <cstdint>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "wx_naive.hpp"
@@ -35,6 +36,8 @@
 #include "queries/query_support.hpp"
 #undef private
 #include "test/util/util.hpp"
+// ref_stub/ shadows external_memory/stxxl_helper.hpp (declarations only)
+#include "util/alphabet_util.hpp"
 
 namespace {
 
@@ -197,6 +200,22 @@ uint64_t pwmref_queries(int is_tree, const uint8_t* text, uint64_t n, uint64_t l
     else out[i] = qs.select(uint8_t(a[i]), b[i]);
   }
   return count;
+}
+
+// pwm's reduce_alphabet (include/util/alphabet_util.hpp:18-45) on a copy of
+// the text, written back to `text`; returns pwm's max_char.  pwm's 8-bit
+// table has 255 entries, so 8-bit texts must not hold symbol 255.
+uint64_t pwmref_reduce_alphabet(uint32_t width, void* text, uint64_t n) {
+  auto run = [&](auto* t) {
+    using A = std::remove_pointer_t<decltype(t)>;
+    std::vector<A> v(t, t + n);
+    const uint64_t m = reduce_alphabet(v);
+    std::memcpy(t, v.data(), n * sizeof(A));
+    return m;
+  };
+  if (width == 1) return run(static_cast<uint8_t*>(text));
+  if (width == 2) return run(static_cast<uint16_t*>(text));
+  return run(static_cast<uint32_t*>(text));
 }
 
 // pwm's copy_bits (include/construction/merge.hpp:19-190), the bit-range copy

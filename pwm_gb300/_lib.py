@@ -65,6 +65,8 @@ SIGNATURES = {
     "pwmgpu_copy_bits": (i32, [vp, vp, u64, u64, u64, vp]),
     "pwmgpu_ctx_set_upload_piece_bytes": (i32, [vp, u64]),
     "pwmgpu_ctx_set_stream_chunks": (i32, [vp, u32]),
+    "pwmgpu_ctx_set_spin_limit": (i32, [vp, u32]),
+    "pwmgpu_ctx_test_withhold_tile": (i32, [vp, i32]),
     "pwmgpu_ctx_release_scratch": (i32, [vp]),
     "pwmgpu_wx_build_huffman": (i32, [vp, vp, u64, u32, u32, u64p, u64p, u64, ctypes.POINTER(vp)]),
     "pwmgpu_wx_codes": (i32, [vp, u64p, u64p, u64, u64p]),

@@ -16,7 +16,7 @@
 #include <vector>
 
 #include "../../include/pwmgpu.h"
-#include "gen.cuh"
+#include "gen.hpp"
 #include "host_huffman.hpp"
 #include "host_stream.hpp"
 #include "host_tables.hpp"
@@ -75,6 +75,8 @@ struct pwmgpu_ctx {
   int engine = PWMGPU_ENGINE_TILE;
   uint64_t upload_piece = uint64_t(64) << 20;  // bytes of text per uploaded piece
   uint32_t stream_chunks = 4;                   // chunks of a pass whose words stream to pinned outputs
+  uint32_t spin_limit = kSpinLimit;             // polls of one look-back wait of the tile engine
+  bool withhold_first_tile = false;             // test hook: look-back passes skip their first tile
   bool async_alloc = false;  // stream-ordered allocations on `stream`
   uint64_t scratch_bytes = 0;
   pwmgpu_wx* compute_cache = nullptr;  // reused by pwmgpu_compute for equal shapes
@@ -733,7 +735,9 @@ const void* enqueue_tile_pass(pwmgpu_ctx* ctx, const std::vector<TilePassHost>& 
     a.first_level_written = first->level0_written ? 1u : 0u;
   }
   if (pi == 0 && first) a.clear_edges = 1u;  // the histogram kernel did not zero the first pass's levels
-  const std::vector<uint32_t> b = bounds.size() >= 2 ? bounds : std::vector<uint32_t>{0, p.tiles};
+  a.spin_limit = ctx->spin_limit;
+  std::vector<uint32_t> b = bounds.size() >= 2 ? bounds : std::vector<uint32_t>{0, p.tiles};
+  if (ctx->withhold_first_tile && !given && p.tiles >= 2 && bounds.size() < 2) b = {1, p.tiles};  // tile 0 never publishes
   const uint64_t structs = (wt && p.segmented) ? 2 : 1;
   const uint64_t skipped = a.first_level_written ? structs * words_for(n) * 8 : 0;
   const uint64_t bytes = structs * uint64_t(p.K) * (n * width + words_for(n) * 8) - skipped;
@@ -1347,62 +1351,6 @@ void build_huffman(pwmgpu_ctx* ctx, const void* d_text, uint64_t n, uint32_t wid
   run_passes(ctx, keys, key_bytes, width, true, levels, plan, tabs, wm, wt);
   check_device_status(ctx);
   build_rank_select(ctx, !is_tree ? &wm : nullptr, wt);
-}
-
-// Host thresholds / permutation of a generator distribution.
-struct GenTables {
-  std::vector<uint64_t> thr;
-  std::vector<uint32_t> perm;
-};
-
-std::vector<uint64_t> thresholds_from_weights(const std::vector<double>& w) {
-  double total = 0;
-  for (double x : w) total += x;
-  std::vector<uint64_t> thr(w.size());
-  double cum = 0;
-  const double scale = 9007199254740992.0;  // 2^53
-  for (size_t i = 0; i < w.size(); ++i) {
-    cum += w[i];
-    double v = (cum / total) * scale;
-    thr[i] = v >= scale ? (uint64_t(1) << 53) : uint64_t(v);
-  }
-  thr.back() = uint64_t(1) << 53;
-  return thr;
-}
-
-GenTables gen_tables(int dist, uint64_t seed) {
-  GenTables g;
-  if (dist == PWMGPU_GEN_DNA4) {
-    g.thr = thresholds_from_weights({0.3, 0.2, 0.2, 0.3});
-  } else if (dist == PWMGPU_GEN_ZIPF256) {
-    std::vector<double> w(256);
-    for (int r = 1; r <= 256; ++r) w[size_t(r - 1)] = 1.0 / double(r);
-    g.thr = thresholds_from_weights(w);
-    g.perm.resize(256);
-    std::iota(g.perm.begin(), g.perm.end(), 0u);
-    const uint64_t pkey = mix64(seed ^ 0x5bd1e9955bd1e995ull);
-    for (uint32_t j = 255; j > 0; --j) {
-      const uint32_t k = uint32_t(mix64(pkey + j) % (j + 1));
-      std::swap(g.perm[j], g.perm[k]);
-    }
-  } else if (dist == PWMGPU_GEN_MIX16) {
-    // geometric(p = 0.01) on {0, 1, ...} clamped to 65535: cumulative
-    // 1 - q^(k+1) with q^(k+1) by repeated multiplication.
-    const double q = 0.99;
-    std::vector<uint64_t> thr(65536);
-    double qk = 1.0;
-    const double scale = 9007199254740992.0;
-    for (uint32_t k = 0; k < 65536; ++k) {
-      qk *= q;
-      double v = (1.0 - qk) * scale;
-      thr[k] = v >= scale ? (uint64_t(1) << 53) : uint64_t(v);
-    }
-    thr.back() = uint64_t(1) << 53;
-    g.thr = std::move(thr);
-  }
-  if (g.thr.empty()) g.thr.push_back(uint64_t(1) << 53);
-  if (g.perm.empty()) g.perm.push_back(0);
-  return g;
 }
 
 }  // namespace
@@ -2105,6 +2053,18 @@ pwmgpu_status pwmgpu_ctx_release_scratch(pwmgpu_ctx* ctx) {
 pwmgpu_status pwmgpu_ctx_set_stream_chunks(pwmgpu_ctx* ctx, uint32_t chunks) {
   if (!ctx || chunks == 0 || chunks > kMaxStreamChunks) return PWMGPU_ERR_ARG;
   ctx->stream_chunks = chunks;
+  return PWMGPU_OK;
+}
+
+pwmgpu_status pwmgpu_ctx_set_spin_limit(pwmgpu_ctx* ctx, uint32_t polls) {
+  if (!ctx) return PWMGPU_ERR_ARG;
+  ctx->spin_limit = polls ? polls : kSpinLimit;
+  return PWMGPU_OK;
+}
+
+pwmgpu_status pwmgpu_ctx_test_withhold_tile(pwmgpu_ctx* ctx, int enable) {
+  if (!ctx) return PWMGPU_ERR_ARG;
+  ctx->withhold_first_tile = enable != 0;
   return PWMGPU_OK;
 }
 
@@ -2848,57 +2808,7 @@ void pwmgpu_batch_free(pwmgpu_batch* b) {
 pwmgpu_status pwmgpu_generate_batch(uint64_t seed, uint32_t count, uint64_t* offsets, uint32_t* levels,
                                     uint8_t* texts) {
   if (!offsets || !levels) return PWMGPU_ERR_ARG;
-  // lengths: round(exp(N(ln 2^16, 1.5^2))) clamped to [2^10, 2^24]
-  const uint64_t key = mix64(seed ^ 0x0ba7c4ull);
-  const double two_pi = 6.283185307179586;
-  offsets[0] = 0;
-  for (uint32_t i = 0; i < count; ++i) {
-    const double u1 = (double((mix64(key + 2ull * i) >> 11) + 1)) / 9007199254740993.0;
-    const double u2 = double(mix64(key + 2ull * i + 1) >> 11) / 9007199254740992.0;
-    const double z = std::sqrt(-2.0 * std::log(u1)) * std::cos(two_pi * u2);
-    double len = std::floor(std::exp(std::log(65536.0) + 1.5 * z) + 0.5);
-    len = std::min(std::max(len, 1024.0), 16777216.0);
-    offsets[i + 1] = offsets[i] + uint64_t(len);
-    // 15% byte-alphabet Zipf(1.0) texts with 8 levels, the rest 5-symbol DNA-like texts with 3 levels
-    levels[i] = (mix64(key ^ (0x5eedull + i)) % 100) < 15 ? 8 : 3;
-  }
-  if (!texts) return PWMGPU_OK;
-  const GenTables zipf = gen_tables(PWMGPU_GEN_ZIPF256, seed);
-  const std::vector<uint64_t> dna = thresholds_from_weights({0.29, 0.2, 0.2, 0.29});
-  // runs of symbol 4: a run starts with probability ps, lengths geometric
-  // with mean 50; ps makes symbol 4 about 2% of the text
-  const double ps = 0.02 / (50.0 * 0.98 + 0.02);
-  const uint64_t ps_thr = uint64_t(ps * 9007199254740992.0);
-  std::vector<uint64_t> geo(4096);
-  {
-    double qk = 1.0;
-    for (size_t k = 0; k < geo.size(); ++k) {
-      qk *= 0.98;
-      geo[k] = uint64_t((1.0 - qk) * 9007199254740992.0);
-    }
-    geo.back() = uint64_t(1) << 53;
-  }
-  for (uint32_t i = 0; i < count; ++i) {
-    uint8_t* out = texts + offsets[i];
-    const uint64_t n = offsets[i + 1] - offsets[i];
-    const uint64_t tkey = mix64(key + 0x9e37ull * (i + 1));
-    if (levels[i] == 8) {
-      for (uint64_t p = 0; p < n; ++p)
-        out[p] = uint8_t(gen_value(PWMGPU_GEN_ZIPF256, tkey, 0, p, zipf.thr.data(), uint32_t(zipf.thr.size()),
-                                   zipf.perm.data()));
-      continue;
-    }
-    for (uint64_t p = 0; p < n;) {
-      const uint64_t r = mix64(tkey + p);
-      if ((r >> 11) < ps_thr) {
-        const uint64_t run = 1 + search_thresholds(geo.data(), uint32_t(geo.size()), mix64(r) >> 11);
-        for (uint64_t k = 0; k < run && p < n; ++k) out[p++] = 4;
-      } else {
-        out[p] = uint8_t(search_thresholds(dna.data(), uint32_t(dna.size()), mix64(r ^ 0xd1ceull) >> 11));
-        ++p;
-      }
-    }
-  }
+  generate_batch_host(seed, count, offsets, levels, texts);
   return PWMGPU_OK;
 }
 
@@ -2906,17 +2816,11 @@ pwmgpu_status pwmgpu_generate_batch(uint64_t seed, uint32_t count, uint64_t* off
 pwmgpu_status pwmgpu_generate(pwmgpu_ctx* ctx, int dist, uint64_t seed, uint64_t param, uint64_t n,
                               uint32_t word_width, void* out, int on_device) {
   if (!valid_width(word_width) || (n && !out) || dist < 0 || dist > 3) return PWMGPU_ERR_ARG;
-  GenTables g = gen_tables(dist, seed);
-  const uint64_t key = mix64(seed);
   if (!on_device) {
-    for (uint64_t i = 0; i < n; ++i) {
-      const uint64_t v = gen_value(dist, key, param, i, g.thr.data(), uint32_t(g.thr.size()), g.perm.data());
-      if (word_width == 1) static_cast<uint8_t*>(out)[i] = uint8_t(v);
-      else if (word_width == 2) static_cast<uint16_t*>(out)[i] = uint16_t(v);
-      else static_cast<uint32_t*>(out)[i] = uint32_t(v);
-    }
+    generate_host(dist, seed, param, n, word_width, out);
     return PWMGPU_OK;
   }
+  const GenTables g = gen_tables(dist, seed);
   if (!ctx) return PWMGPU_ERR_ARG;
   return guarded(ctx, [&]() {
     auto* d_thr = static_cast<uint64_t*>(ctx->grow("gen_thr", g.thr.size() * 8));

@@ -1,7 +1,7 @@
 // Histogram, wavelet-tree regroup, Huffman key and generator kernels.
 #include <algorithm>
 
-#include "gen.cuh"
+#include "gen.hpp"
 #include "kernels.cuh"
 
 namespace pwmgpu {
@@ -714,7 +714,7 @@ __global__ void remap_kernel(const T* text, uint64_t n, const uint32_t* map, uin
 }
 
 // ---------------------------------------------------------------------------
-// Generators (gen.cuh)
+// Generators (gen.hpp)
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void generate_kernel(int dist, uint64_t key, uint64_t param, uint64_t n, T* out, const uint64_t* thr,

@@ -11,9 +11,10 @@ constexpr uint32_t kErrSymbol = 1u;   // a symbol >= 2^levels was seen
 constexpr uint32_t kErrTimeout = 2u;  // a bounded spin-wait gave up
 constexpr uint32_t kErrBounds = 4u;   // a kernel-side bounds check tripped
 
-// Upper bound on the polls of one decoupled look-back wait (each poll sleeps
-// ~100 ns), ~1.5 s in total; after that the kernel records kErrTimeout and
-// carries on with a zero prefix so that it always terminates.
+// Default upper bound on the polls of one decoupled look-back wait (each poll
+// sleeps ~64-100 ns), ~1.5 s in total; after that the kernel records
+// kErrTimeout and carries on with a zero prefix so that it always terminates.
+// The tile engine takes its bound per launch (pwmgpu_ctx_set_spin_limit).
 constexpr uint32_t kSpinLimit = 1u << 24;
 
 __host__ __device__ inline uint64_t words_for(uint64_t bits) { return (bits + 63) >> 6; }

@@ -626,16 +626,16 @@ void launch_queries(const QueryStructure& q, int op, const uint64_t* a, const ui
 // ===========================================================================
 // Allocation-free rank/select build (pwmgpu_rank_select_build_noalloc).
 //
-// For callers that must not allocate device memory while they run: code that
-// records CUDA graphs, allocator-less plugins that receive every buffer from
-// their host framework, latency-critical serving loops that cannot afford an
-// allocator's implicit synchronisation.  The per-L1-block prefix counts the
-// build needs live in a fixed, file-scope device array instead of context
-// scratch, and the level descriptor the kernels read lives in a file-scope
-// device slot.  Both are resident on every GPU that loads this library until
-// the process exits.  Every call shares them: calls that overlap on the GPU
-// (different streams, or different host threads on one device) race and must
-// be serialised by the caller.
+// For callers that must not allocate device memory while they run:
+// allocator-less plugins that receive every buffer from their host framework,
+// and latency-critical serving loops that cannot afford an allocator's
+// implicit synchronisation.  The per-L1-block prefix counts the build needs
+// live in a fixed, file-scope device array instead of context scratch, and
+// the level descriptor the kernels read lives in a file-scope device slot.
+// Both are resident on every GPU that loads this library until the process
+// exits.  Every call shares them: calls that overlap on the GPU (different
+// streams, or different host threads on one device) race and must be
+// serialised by the caller.
 // ===========================================================================
 namespace {
 
@@ -647,6 +647,11 @@ constexpr uint64_t kNoAllocMaxL1Blocks = (uint64_t(1) << 20) - (uint64_t(1) << 1
 static __device__ __align__(256) uint32_t g_noalloc_rs_scratch[kNoAllocScratchWords];
 static __device__ __align__(256) RankSelectLevel g_noalloc_rs_level[1];
 
+// Stores the level descriptor into its file-scope slot in stream order: the
+// values travel as a kernel parameter, so no host buffer has to outlive the
+// call.
+__global__ void noalloc_set_level_kernel(RankSelectLevel level) { g_noalloc_rs_level[0] = level; }
+
 struct NoAllocSymbols {
   bool ready = false;
   uint32_t* scratch = nullptr;
@@ -656,7 +661,9 @@ struct NoAllocSymbols {
 }  // namespace
 
 // Device addresses of the file-scope arrays for the current device, looked
-// up once per device (the first call on a device does it).
+// up once per device (the first call on a device does it) and kept for the
+// life of the process: after a cudaDeviceReset the module may load at other
+// addresses, so the entry point must not be used across a device reset.
 cudaError_t noalloc_rank_select_symbols(uint32_t** scratch, RankSelectLevel** level) {
   static std::mutex mu;
   static NoAllocSymbols per_device[64];
@@ -698,9 +705,13 @@ cudaError_t noalloc_rank_select_build(const uint64_t* words, uint64_t nwords, ui
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(counts, 0, 3 * 8, stream);
   if (e != cudaSuccess) return e;
+  if (nwords == 0) {
+    // pwm keeps one zeroed l12 entry for an empty level; no kernel runs
+    e = cudaMemsetAsync(l12, 0, 2 * sizeof(uint32_t), stream);
+    return e;
+  }
   RankSelectLevel host{words, nwords, l0, l12, s0, s1, counts};
-  e = cudaMemcpyToSymbolAsync(g_noalloc_rs_level, &host, sizeof(host), 0, cudaMemcpyHostToDevice, stream);
-  if (e != cudaSuccess) return e;
+  noalloc_set_level_kernel<<<1, 1, 0, stream>>>(host);
   const uint64_t nreal = (nwords + kL1Cover - 1) / kL1Cover;
   const uint64_t stride = nreal + (nreal + kRsThreads - 1) / kRsThreads + 1;
   uint64_t launches = 0;

@@ -92,6 +92,7 @@ struct TileArgs {
   uint64_t* zero_b;
   uint64_t zero_words;
   uint32_t zero_per_tile;
+  uint32_t spin_limit;  // polls of one look-back wait before it gives up (kErrTimeout)
 };
 
 template <typename KeyT, int K, bool OUT, int THREADS, int V>
@@ -208,12 +209,14 @@ __device__ __forceinline__ void scatter_vector(const uint4& v, uint32_t mb, uint
 // its inclusive values at once, so no walk crosses a segment start.  The
 // tile's own aggregates (mine, at most one tile of keys each) were published
 // when it counted its keys.  Leaves the exclusive prefixes in pre[0..NLB)
-// and publishes the inclusive ones.  Called by every thread of the CTA.
+// and publishes the inclusive ones.  Called by every thread of the CTA.  A
+// wait gives up after `spin_limit` polls (~64 ns apart): kErrTimeout, and the
+// missing counts are taken as zero, so the kernel always returns.
 template <int NLB, int WARPS>
 __device__ __forceinline__ void segment_lookback_cta(unsigned long long* lb, uint32_t tiles, uint32_t tile,
                                                      uint32_t first, const uint32_t* mine, unsigned long long* pre,
                                                      unsigned long long (*wsum)[NLB], uint32_t* wmask,
-                                                     uint32_t* s_open, uint32_t* status) {
+                                                     uint32_t* s_open, uint32_t* status, uint32_t spin_limit) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid < NLB) pre[tid] = 0;
   if (tile == first) return;  // its inclusive values went out with its counts
@@ -236,7 +239,7 @@ __device__ __forceinline__ void segment_lookback_cta(unsigned long long* lb, uin
 #pragma unroll
       for (int c = 0; c < NLB; ++c) missing |= (v[c] >> 62) == 0;
       if (!missing) break;
-      if (spins >= kSpinLimit) {
+      if (spins >= spin_limit) {
         atomicOr(status, kErrTimeout);
 #pragma unroll
         for (int c = 0; c < NLB; ++c)
@@ -672,7 +675,7 @@ __global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / T
     __shared__ uint32_t wmask[WARPS], s_open;
     if (!given)
       segment_lookback_cta<NLB, WARPS>(a.lookback, a.tiles, g, s_sg.tile0, s_cnt, pre, wsum, wmask, &s_open,
-                                       a.status);
+                                       a.status, a.spin_limit);
   }
   __syncthreads();
 

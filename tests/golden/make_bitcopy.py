@@ -2,10 +2,9 @@
 bit-range copy of its domain-decomposition merge (include/construction/
 merge.hpp:19-190).
 
-Run in a checkout that has the pwm source tree (default /root/reference,
-override with PWM_REFERENCE):
+Run in a checkout that has the pwm source tree (PWM_REFERENCE names it):
 
-    make -C oracle ref && python tests/golden/make_bitcopy.py
+    make -C oracle ref REF=$PWM_REFERENCE && python tests/golden/make_bitcopy.py
 
 Two sources, both run through pwm's own copy_bits (oracle/_ref/libpwmref.so):
 
@@ -28,7 +27,7 @@ sys.path.insert(0, ROOT)
 
 from oracle.oracle import Reference  # noqa: E402
 
-REF = os.environ.get("PWM_REFERENCE", "/root/reference")
+REF = os.environ.get("PWM_REFERENCE")
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -54,6 +53,8 @@ def test_file_cases(path):
 
 
 def main():
+    if not REF or not Reference.available():
+        sys.exit("set PWM_REFERENCE to the pwm source tree and run `make -C oracle ref REF=$PWM_REFERENCE` first")
     ref = Reference()
     cases = test_file_cases(os.path.join(REF, "test", "bit_copy.cpp"))
     assert cases and all(c["steps"] for c in cases), "no BitCopy cases found"

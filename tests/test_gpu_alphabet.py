@@ -79,3 +79,22 @@ def test_reduce_wide_symbols(pg, orc, in_place):
         got = out.cpu().numpy()
         expect = want.astype(np.uint32).view(np.uint8) if width == 4 else to_u40(want)
         assert mc == wmc and np.array_equal(got, expect), (width, n)
+
+
+def test_reduce_alphabet_matches_pwm_golden(pg):
+    """Against pwm's own reduce_alphabet (tests/golden/alphabet.json, recorded
+    by running pwm's function on the shared generator's texts)."""
+    import hashlib
+    import json
+    import os
+    from conftest import GOLDEN
+    torch = torch_cuda()
+    with open(os.path.join(GOLDEN, "alphabet.json")) as f:
+        cases = json.load(f)["cases"]
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a, a.dtype.newbyteorder("<")).tobytes()).hexdigest()
+    for c in cases:
+        t = pg.generate(c["dist"], c["seed"], c["n"], c["width"], param=c["param"])
+        assert sha(t) == c["text_sha256"], c["name"]
+        got, mc = run(pg, torch, t, False)
+        assert mc == c["max_char"], c["name"]
+        assert sha(got) == c["out_sha256"], c["name"]

@@ -1,14 +1,14 @@
 """CPU: include/wx_gpu.hpp (the pwm-side drop-in classes) compiles against
 pwm's own headers and links against libpwmgpu.so, registered through pwm's
-CONSTRUCTION_REGISTER contract.  Needs the pwm source tree (skipped where it
-is absent, e.g. on GPU hosts)."""
+CONSTRUCTION_REGISTER contract.  Needs the pwm source tree, named by the
+PWM_REFERENCE environment variable (skipped where it is unset or absent)."""
 import os
 import subprocess
 
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("PWM_REFERENCE", "/root/reference")
+REF = os.environ.get("PWM_REFERENCE") or ""
 
 PROGRAM = r'''
 #include <cstdint>
@@ -45,7 +45,8 @@ int main() {
 '''
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "include")), reason="pwm source tree not present")
+@pytest.mark.skipif(not REF or not os.path.isdir(os.path.join(REF, "include")),
+                    reason="PWM_REFERENCE unset or not a pwm source tree")
 def test_drop_in_header_compiles_and_links(tmp_path):
     src = tmp_path / "use_wx_gpu.cpp"
     src.write_text(PROGRAM)

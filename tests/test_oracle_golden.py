@@ -13,7 +13,7 @@ def test_fixture_count(golden_fixtures):
     assert any(c["text_hex"] == "" for c in golden_fixtures)
 
 
-@pytest.mark.parametrize("variant", ["ps", "pc", "naive", "ppc"])
+@pytest.mark.parametrize("variant", ["ps", "pc", "naive", "ppc", "dd_ps"])
 @pytest.mark.parametrize("tree", [False, True])
 def test_fixtures_construction(orc, golden_fixtures, variant, tree):
     key = "wt" if tree else "wm"
@@ -89,20 +89,24 @@ def test_fixtures_huffman(orc, golden_fixtures, tree):
             assert [int(z) for z in s.zeros] == g["zeros"]
 
 
-def test_seeded_texts_are_pinned(pg, golden_seeded):
+def test_seeded_texts_are_pinned(pg, orc, golden_seeded):
+    import hashlib
     for case in golden_seeded:
         text = seeded_text(pg, case)
-        import hashlib
         assert hashlib.sha256(text.astype(text.dtype.newbyteorder("<")).tobytes()).hexdigest() == case["text_sha256"]
+        # the oracle's copy of the generator gives the same text without the GPU library
+        mine = orc.generate(case["dist"], case["seed"], case["n"], case["width"], param=case["param"])
+        assert np.array_equal(mine, text), case["name"]
 
 
+@pytest.mark.parametrize("variant", ["ps", "dd_ps"])
 @pytest.mark.parametrize("tree", [False, True])
-def test_seeded_construction_and_blocks(orc, pg, golden_seeded, tree):
+def test_seeded_construction_and_blocks(orc, pg, golden_seeded, tree, variant):
     key = "wt" if tree else "wm"
     for case in golden_seeded:
         text = seeded_text(pg, case)
         L = case["levels"]
-        s = orc.build(text, L, tree, "ps")
+        s = orc.build(text, L, tree, variant, threads=5)
         g = case[key]
         assert [sha_words(s.level(l)) for l in range(L)] == g["sha256"], case["name"]
         if not tree:
@@ -166,3 +170,38 @@ def test_oracle_against_reference_directly(orc):
             t = rng.integers(0, 1 << L, n).astype(dt)
             for tree in (False, True):
                 assert orc.build(t, L, tree, "ps").same_bits(ref.build(t, L, tree, "ps"))
+
+
+def test_config_texts_are_pinned(orc):
+    """The benchmark workloads' texts at full size, from the oracle's copy of
+    the generator, hash to the inputs pwm was run on (tests/golden/configs.json)."""
+    import hashlib
+    import json
+    import os
+    from conftest import GOLDEN
+    with open(os.path.join(GOLDEN, "configs.json")) as f:
+        cases = json.load(f)["cases"]
+    for c in cases:
+        t = orc.generate(c["dist"], c["seed"], c["n"], c["width"], param=c["param"])
+        assert hashlib.sha256(t.astype(t.dtype.newbyteorder("<")).tobytes()).hexdigest() == c["text_sha256"], c["name"]
+
+
+@pytest.mark.parametrize("variant", ["dd_ps", "ppc"])
+def test_config_dna_2p26_matches_pwm(orc, variant):
+    """The oracle's parallel restatements (the CPU baseline's code) on the
+    2^26 DNA-like text against pwm's hashes at that size."""
+    import json
+    import os
+    from conftest import GOLDEN
+    with open(os.path.join(GOLDEN, "configs.json")) as f:
+        c = next(x for x in json.load(f)["cases"] if x["name"] == "dna4_2p26_l2")
+    t = orc.generate(c["dist"], c["seed"], c["n"], c["width"], param=c["param"])
+    for tree, key in ((False, "wm"), (True, "wt")):
+        s = orc.build(t, c["levels"], tree, variant, threads=8)
+        assert [sha_words(s.level(l)) for l in range(s.levels)] == c[key]["sha256"], (variant, key)
+        if not tree and variant != "ppc":  # pwm's wx_ppc leaves zeros[L-1] at 0
+            assert [int(z) for z in s.zeros] == c[key]["zeros"]
+        for l, gb in enumerate(c[key + "_rank_select"]):
+            l0, l12, s0, s1 = orc.rank_select_blocks(s.level(l))
+            assert sha_u32(l12) == gb["l12_sha256"] and sha_u32(s0) == gb["s0_sha256"] and \
+                sha_u32(s1) == gb["s1_sha256"], (variant, key, l)
