@@ -402,14 +402,17 @@ def serving_requests(pg, count, seed=7, nq=10_000):
         occ = 1 + np.floor(rng.random(nq) * counts[sym.astype(np.int64)]).astype(np.uint64)
         a = np.where(ops == 0, rng.integers(0, n, nq).astype(np.uint64), sym)
         b = np.where(ops == 1, rng.integers(0, n + 1, nq).astype(np.uint64), occ)
-        reqs.append((t, L, ops, a, b))
+        reqs.append((t, L, ops, a, b, i % 2))  # queries alternate between the matrix and the tree
     return reqs
 
 
 def serve_run(pg, reqs, rate, slots, budget):
     """Poisson arrivals at `rate` requests/s (rate None: one at a time, each
-    submitted when the previous finished).  A collector waits for and
-    releases every request.  Returns latency and throughput figures."""
+    submitted when the previous finished; "saturate": all submitted at once,
+    the server's maximum throughput).  Every request builds a matrix and a
+    tree with rank/select, then answers its queries on one of them.  A
+    collector waits for and releases every request.  Returns latency and
+    throughput figures."""
     import numpy as np
     srv = pg.Server(budget, slots=slots)
     infos = [None] * len(reqs)
@@ -427,13 +430,13 @@ def serve_run(pg, reqs, rate, slots, budget):
     rng = np.random.default_rng(11)
     t0 = time.perf_counter()
     t_next = t0
-    for k, (t, L, ops, a, b) in enumerate(reqs):
-        if rate is not None:
+    for k, (t, L, ops, a, b, which) in enumerate(reqs):
+        if rate is not None and rate != "saturate":
             t_next += rng.exponential(1.0 / rate)
             delay = t_next - time.perf_counter()
             if delay > 0:
                 time.sleep(delay)
-        ids[k], _ = srv.submit(t, L, ops=ops, a=a, b=b)
+        ids[k], _ = srv.submit(t, L, matrix=True, tree=True, which=which, ops=ops, a=a, b=b)
         ready.release()
         if rate is None:
             srv.wait(ids[k])
@@ -452,17 +455,21 @@ def serve_run(pg, reqs, rate, slots, budget):
             "peak_device_bytes": stats["peak_bytes"], "slots": slots}
 
 
-def serving_bench(pg, count=400, slots=8, budget=150 * 10 ** 9):
+def serving_bench(pg, count=2000, slots=8, budget=150 * 10 ** 9):
     """p50/p99 request latency and throughput of the continuous-batching
-    server at Poisson rates 100, 1000 and 10000 requests/s, next to
-    one-at-a-time construction (one slot, closed loop)."""
+    server over `count` requests per offered rate: Poisson rates 100, 1000
+    and 10000 requests/s and saturation (all requests at once), next to
+    one-at-a-time construction (one slot, closed loop).  `at_saturation`
+    repeats the figures of the saturated run (the highest throughput)."""
     reqs = serving_requests(pg, count)
-    serve_run(pg, reqs[:16], None, 1, budget)  # warm-up
-    out = {"workload": "batched-workload uint8 texts + 5% uint32 (2^20 values, 20 levels); build (matrix + "
-                       "rank/select) then 10^4 access/rank/select queries per request; budget 150 GB",
-           "one_at_a_time": serve_run(pg, reqs, None, 1, budget), "rates": []}
-    for rate in (100, 1000, 10000):
+    serve_run(pg, reqs[:64], None, 1, budget)  # warm-up
+    out = {"workload": "batched-workload uint8 texts + 5% uint32 (2^20 values, 20 levels); build (matrix + tree + "
+                       "rank/select) then 10^4 access/rank/select queries per request on the matrix or the tree "
+                       "(alternating); budget 150 GB",
+           "requests_per_rate": count, "one_at_a_time": serve_run(pg, reqs, None, 1, budget), "rates": []}
+    for rate in (100, 1000, 10000, "saturate"):
         out["rates"].append(serve_run(pg, reqs, rate, slots, budget))
+    out["at_saturation"] = out["rates"][-1]
     return out
 
 

@@ -13,7 +13,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libpwmgpu.so")
 OBJ = os.path.join(HERE, "_build")
-SOURCES = ["api.cu", "build_kernels.cu", "split.cu", "tile.cu", "tile_deep.cu", "ranksel.cu", "batch.cu", "serve.cu", "merge.cu"]
+SOURCES = ["abi.cu", "engine.cu", "plain.cu", "huffman.cu", "shards.cu", "batch_host.cu", "build_kernels.cu", "split.cu",
+           "tile.cu", "tile_deep.cu", "ranksel.cu", "batch.cu", "serve.cu", "merge.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-fvisibility=hidden", "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-warn-spills"]
