@@ -356,6 +356,39 @@ __global__ void __launch_bounds__(1024) tile_block_scan_kernel(unsigned long lon
   }
 }
 
+// Start table of a first tile pass from folded prefix counts: warp j takes
+// level j (2^j <= 16 prefixes, a lane each).  Key order x holds the natural
+// prefix p = rev(x): the matrix starts are exclusive sums in key order, the
+// tree starts exclusive sums in natural order; warp K gives the runs of S_K.
+__global__ void __launch_bounds__(160) tile_first_table_kernel(const uint64_t* flat, uint32_t K, uint32_t out,
+                                                                uint32_t tree, uint64_t* table) {
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp > K || (warp == K && !out)) return;
+  const uint32_t j = warp, R = 1u << j;
+  const uint64_t* c = flat + (R - 1);
+  const uint32_t p = lane < R ? reverse_low_bits(lane, j) : 0u;
+  const unsigned long long in_key = lane < R ? c[p] : 0ull, in_nat = lane < R ? c[lane] : 0ull;
+  unsigned long long xk = in_key, xn = in_nat;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const unsigned long long yk = __shfl_up_sync(0xFFFFFFFFu, xk, d);
+    const unsigned long long yn = __shfl_up_sync(0xFFFFFFFFu, xn, d);
+    if (lane >= uint32_t(d)) {
+      xk += yk;
+      xn += yn;
+    }
+  }
+  const unsigned long long key_pre = xk - in_key;
+  const unsigned long long nat_pre_p = __shfl_sync(0xFFFFFFFFu, xn - in_nat, p);  // natural prefix before p
+  if (lane >= R) return;
+  if (j < K) {
+    table[tile_wm_entry(int(j), int(lane))] = key_pre;
+    table[tile_wt_entry(int(K), int(j), int(lane))] = tree ? nat_pre_p : 0ull;
+  } else {
+    table[tile_out_entry(int(K), int(lane))] = key_pre;
+  }
+}
+
 // 14..16 levels: the bins split into ranges of 2^15 u32 counters held in
 // shared memory (128 KB); grid row r counts the symbols of range r in its
 // chunk of the text and adds its nonzero bins to the global histogram.
@@ -763,6 +796,12 @@ void launch_tile_block_scan(unsigned long long* blocksum, uint32_t nblocks, uint
   if (nblocks == 0) return;
   tile_block_scan_kernel<<<(1u << D) + (table ? 1u : 0u), 1024, 0, s>>>(blocksum, nblocks, 1u << D, hist, levels, K,
                                                                         out ? 1u : 0u, tree ? 1u : 0u, table);
+  ++*launches;
+}
+
+void launch_tile_first_table(const uint64_t* flat, uint32_t K, bool out, bool tree, uint64_t* table, cudaStream_t s,
+                             uint64_t* launches) {
+  tile_first_table_kernel<<<1, 32 * (K + 1), 0, s>>>(flat, K, out ? 1u : 0u, tree ? 1u : 0u, table);
   ++*launches;
 }
 

@@ -69,6 +69,12 @@ void launch_tile_histogram_blocks(const void* text, uint64_t n, uint32_t width, 
 void launch_tile_block_scan(unsigned long long* blocksum, uint32_t nblocks, uint32_t D, const unsigned long long* hist,
                             uint32_t levels, uint32_t K, bool out, bool tree, uint64_t* table, cudaStream_t s,
                             uint64_t* launches);
+// The start table of the first tile pass of a text of any level count (one
+// segment: the whole text) from the natural prefix counts of its levels 0..K
+// (`flat`: level m at offset 2^m - 1, as launch_fold_levels writes them), so
+// that the pass can start before the host plans the later ones.
+void launch_tile_first_table(const uint64_t* flat, uint32_t K, bool out, bool tree, uint64_t* table, cudaStream_t s,
+                             uint64_t* launches);
 
 // ---- merge of shards (merge.cu) -----------------------------------------------
 // A run of one shard's level in the merged level: destination bit `dst`,

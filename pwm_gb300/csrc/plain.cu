@@ -418,6 +418,38 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
                                   if (!blk0.empty()) ev0.push_back(ctx->mark(s));
                                 });
     from = 1;
+  } else if (tile_engine && !stream_out && L > 8 && Kz < int(L)) {
+    // Deeper texts: the first pass counts its tiles and looks back (the tile
+    // histogram covers at most 8 levels), but its start table still follows
+    // from the device's prefix counts of levels 0..Kz, so it starts before
+    // the host reads them and plans the later passes (which took the GPU
+    // idle for ~1.3 ms at 16 levels, 2^28 symbols).  The memset above zeroed
+    // its levels 1..Kz-1.
+    const auto shape = plan_passes(L, Kz);
+    std::vector<TilePassHost> early(2);
+    for (size_t i = 0; i < early.size(); ++i) {
+      early[i].level = shape[i].level;
+      early[i].K = shape[i].K;
+      early[i].out = shape[i].has_out;
+    }
+    TilePassHost& p0 = early[0];
+    const uint32_t T = tile_pass_elems(wx->width);
+    p0.segmented = want_tree;
+    p0.tiles = uint32_t((n + T - 1) / T);
+    p0.segs.push_back({0, n, 0, 0, 0});
+    p0.table.assign(size_t(tile_table_size(p0.K)), 0);
+    const TileBlob b0 = tile_blob(early, 0, 1, L, n, wx->wm, want_tree ? &wx->wt : nullptr);
+    auto* d_b0 = static_cast<unsigned char*>(ctx->grow("tile_plan0", b0.bytes.size()));
+    CUDA_TRY(cudaMemcpyAsync(d_b0, b0.bytes.data(), b0.bytes.size(), cudaMemcpyHostToDevice, s));
+    launch_tile_first_table(d_flat_host, uint32_t(p0.K), p0.out, want_tree,
+                            reinterpret_cast<uint64_t*>(d_b0 + b0.table[0]), s, &ctx->launches);
+    // the look-back state sized for every later pass now (a later pass has at
+    // most 2^16 segments, each adding at most one partial tile), so that no
+    // later pass reallocates it, which would wait for this one
+    ctx->grow("lookback", (uint64_t(p0.tiles) + 65536 + 16) * (uint64_t(1) << kTileMaxLevels) * 8 + 64);
+    next_in = enqueue_tile_pass(ctx, early, 0, d_b0, b0, d_text, wx->width, n, wx->wm, want_tree ? &wx->wt : nullptr,
+                                nullptr);
+    from = 1;
   }
   CUDA_TRY(cudaEventSynchronize(ctx->hist_event()));
   if (*h_status) {
