@@ -171,64 +171,77 @@ def cpu_baseline(n):
                       "leg); one warm-up and one timed step per leg"}
 
 
-def batched_vs_per_text(torch, pg, ctx, count=4096, seed=1, reps=3):
-    """4096 uneven uint8 texts (log-normal lengths, 85% DNA-like with 3
-    levels, 15% Zipf bytes with 8 levels): matrix + tree of every text, one
-    CUDA-graph launch per batch (pass width chosen by timing 1..4 levels per
-    pass) against a loop of per-text builds through the same library."""
+def batched_vs_per_text(torch, pg, ctx, count=4096, seed=1, reps=5):
+    """The batched workload: 4096 uint8 texts (log-normal lengths, 85%
+    DNA-like with 3 levels, 15% Zipf bytes with 8 levels), matrix + tree of
+    every text.  Batched: one CUDA graph per build whose persistent kernel
+    takes (text, pass, tile) items from a device work queue, tile sizes tuned
+    per text class by the library (first build, cached in the context).
+    Per text: each text its own single-text batch (the same kernels, one
+    graph launch per text), launched back to back on the stream with no host
+    synchronisation in between.  CUDA events; texts resident on the device."""
     import numpy as np
     texts, offs, levels = pg.generate_batch(seed, count)
     total = int(offs[-1])
     d = torch.from_numpy(texts).cuda()
     stream = torch.cuda.current_stream()
-    tune = {}
-    b = pg.Batch(offs, levels, word_width=1, tree=True, levels_per_pass=2, context=ctx)
-    for k in (1, 2, 3, 4):
-        b.set_levels_per_pass(k)
-        b.build(d.data_ptr())  # records the graph for this width
-        b.check()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        b.build(d.data_ptr())
-        e0.record(stream)
-        for _ in range(reps):
-            b.build(d.data_ptr())
-        e1.record(stream)
-        torch.cuda.synchronize()
-        tune[k] = e0.elapsed_time(e1) / reps
-    best = min(tune, key=tune.get)
-    b.set_levels_per_pass(best)
-    b.build(d.data_ptr())
+    t0 = time.perf_counter()
+    b = pg.Batch(offs, levels, word_width=1, tree=True, context=ctx)
+    b.build(d.data_ptr())  # tunes new classes, plans, records the graph
     b.check()
-    batched_ms = tune[best]
-    # per-text builds: one device structure per text, built one after the other
+    first_build_s = time.perf_counter() - t0
+    for _ in range(3):
+        b.build(d.data_ptr())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        b.build(d.data_ptr())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    b.check()
+    batched_ms = e0.elapsed_time(e1) / reps
+    vpt = [b.tile_vectors(i) for i in range(count)]
+    # per-text: a batch of one text each (graphs recorded up front, untimed)
+    base = d.data_ptr()
     per = []
     for i in range(count):
-        n = int(offs[i + 1] - offs[i])
-        per.append(pg.DeviceStructure(n, 1, int(levels[i]), matrix=True, tree=True, context=ctx))
-    base = d.data_ptr()
-    for i in range(min(count, 64)):
-        per[i].build(base + int(offs[i]))
+        one = np.array([0, int(offs[i + 1] - offs[i])], dtype=np.uint64)
+        x = pg.Batch(one, levels[i:i + 1], word_width=1, tree=True, context=ctx)
+        x.build(base + int(offs[i]))
+        per.append(x)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
     for i in range(count):
         per[i].build(base + int(offs[i]))
+    e0.record(stream)
+    for _ in range(2):
+        for i in range(count):
+            per[i].build(base + int(offs[i]))
+    e1.record(stream)
     torch.cuda.synchronize()
-    per_ms = (time.perf_counter() - t0) * 1e3
+    per_ms = e0.elapsed_time(e1) / 2
     # spot check: batch == per-text for a few texts
     same = True
     for i in range(0, count, max(1, count // 16)):
-        a, c = b.download(i, 0), per[i].download(0)
-        same &= all(np.array_equal(np.asarray(a.bvs()[l]), np.asarray(c.bvs()[l])) for l in range(int(levels[i])))
-        same &= a.zeros() == c.zeros()
-        a, c = b.download(i, 1), per[i].download(1)
-        same &= all(np.array_equal(np.asarray(a.bvs()[l]), np.asarray(c.bvs()[l])) for l in range(int(levels[i])))
+        a_, c = b.download(i, 0), per[i].download(0, 0)
+        same &= all(np.array_equal(np.asarray(a_.bvs()[l]), np.asarray(c.bvs()[l])) for l in range(int(levels[i])))
+        same &= a_.zeros() == c.zeros()
+        a_, c = b.download(i, 1), per[i].download(0, 1)
+        same &= all(np.array_equal(np.asarray(a_.bvs()[l]), np.asarray(c.bvs()[l])) for l in range(int(levels[i])))
     for x in per:
         x.free()
     b.free()
+    lens = (offs[1:] - offs[:-1]).astype(np.float64)
+    alg = float(2 * (lens * levels.astype(np.float64)).sum() + 2 * 8 * (np.ceil(lens / 64) * levels).sum())
+    peak, peak_kind = measured_peak()
     return {"texts": count, "symbols": total, "levels_mix": {"3": int((levels == 3).sum()), "8": int((levels == 8).sum())},
             "batched_gbs": total / (batched_ms / 1e3) / 1e9, "batched_ms": batched_ms,
             "per_text_gbs": total / (per_ms / 1e3) / 1e9, "per_text_ms": per_ms,
-            "speedup": per_ms / batched_ms, "levels_per_pass_ms": tune, "levels_per_pass": best,
+            "speedup": per_ms / batched_ms, "engine": "tile (persistent work queue)",
+            "tile_vectors_per_thread": {str(v): vpt.count(v) for v in sorted(set(vpt))},
+            "first_build_s": first_build_s,
+            "roofline": {"algorithmic_bytes": alg, "achieved_gbs": alg / (batched_ms / 1e3) / 1e9,
+                         "frac": alg / (batched_ms / 1e3) / 1e9 / peak, "peak": peak, "peak_source": peak_kind},
+            "per_text": "each text a batch of one (one graph launch per text), launched back to back, no host sync",
             "identical_to_per_text": bool(same), "structures": ["matrix", "tree"]}
 
 
@@ -303,9 +316,34 @@ def other_workloads(torch, pg, ctx, reps=3):
         t1 = time.perf_counter()
         ws = pg.wx_huff_ps(np.uint16, tree, context=ctx).compute(host16, host16.size, 0, codes=codes)
         t2 = time.perf_counter()
+        # device-resident: the same codes, a device text, the structure kept in
+        # HBM; the kernels' time from the library's CUDA events, and the call
+        d_text = torch.from_numpy(host16.view(np.int16)).cuda()
+        torch.cuda.synchronize()
+        ds = pg.DeviceStructure.huffman(d_text.data_ptr(), host16.size, 2, tree=tree, rank_select=False,
+                                        codes=codes[:2], context=ctx)
+        ds.free()
+        ctx.lib.pwmgpu_ctx_profile(ctx.h, 1)
+        t3 = time.perf_counter()
+        ds = pg.DeviceStructure.huffman(d_text.data_ptr(), host16.size, 2, tree=tree, rank_select=False,
+                                        codes=codes[:2], context=ctx)
+        ds.check()
+        t4 = time.perf_counter()
+        buf = ctypes.create_string_buffer(1 << 16)
+        ctx.check(ctx.lib.pwmgpu_ctx_profile_read(ctx.h, buf, len(buf)))
+        ctx.lib.pwmgpu_ctx_profile(ctx.h, 0)
+        prof = parse_profile(buf.value.decode())
+        kern_ms = sum(v["ms"] for v in prof.values())
+        hbytes = sum(v["bytes"] for k, v in prof.items() if k == "split_pass")
+        ds.free()
+        del d_text
         out["mix16_2p28_huffman_" + ("tree" if tree else "matrix")] = {
             "n": int(host16.size), "word_width": 2, "levels": ws.levels(), "codes_ms": (t1 - t0) * 1e3,
-            "build_host_to_host_ms": (t2 - t1) * 1e3, "text_gbs_host_to_host": host16.nbytes / (t2 - t1) / 1e9}
+            "build_host_to_host_ms": (t2 - t1) * 1e3, "text_gbs_host_to_host": host16.nbytes / (t2 - t1) / 1e9,
+            "device_call_ms": (t4 - t3) * 1e3, "device_kernels_ms": kern_ms,
+            "device_kernel_groups": {k: round(v["ms"], 3) for k, v in prof.items()},
+            "split_pass_roofline_frac": (hbytes / (prof["split_pass"]["ms"] / 1e3) / 1e9 / measured_peak()[0])
+            if prof.get("split_pass", {}).get("ms") else None}
     out["queries_mix16_2p28"] = query_rates(torch, pg, ctx, host16)
     del host16
     out["semi_external_zipf_2p31_levels8"] = semi_external_rate(torch, pg, ctx)

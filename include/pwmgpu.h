@@ -117,6 +117,14 @@ PWMGPU_API pwmgpu_status pwmgpu_ctx_set_engine(pwmgpu_ctx* ctx, int engine);
  * (default 64 MiB; rounded to the histogram's blocks of 2^18 symbols). */
 PWMGPU_API pwmgpu_status pwmgpu_ctx_set_upload_piece_bytes(pwmgpu_ctx* ctx, uint64_t bytes);
 
+/* Host threads that move pageable host buffers (host-to-host builds,
+ * downloads) through the context's ring of 4 pinned 16 MiB staging pieces,
+ * one piece filled or drained on the host while the copy engine moves the
+ * one before: -1 (default) up to 8 threads, as the host has cores; 0 hands
+ * pageable buffers to cudaMemcpyAsync unstaged.  Pinned buffers and copies
+ * under one piece are never staged. */
+PWMGPU_API pwmgpu_status pwmgpu_ctx_set_host_copy_threads(pwmgpu_ctx* ctx, int threads);
+
 /* Chunks (1..16, default 4) in which a host-to-host build with pinned
  * outputs launches its first pass (and later passes of at most 64
  * segments), so that the words each chunk completes go back while the next
@@ -378,8 +386,18 @@ PWMGPU_API void pwmgpu_server_destroy(pwmgpu_server* s);
  * device buffer of word_width-byte symbols; text i has levels[i] (1..12)
  * levels.  Every text gets a wavelet matrix (PWMGPU_MATRIX is required) and,
  * with PWMGPU_TREE, a levelwise wavelet tree, each bit-identical to a single
- * pwmgpu_compute of that text.  levels_per_pass (1..4) is the split-pass
- * width; pwmgpu_batch_set_levels_per_pass changes it (autotuning). */
+ * pwmgpu_compute of that text (pwm's wx_ps::compute, include/wx_ps.hpp:37-56,
+ * text by text).
+ *
+ * Engines (the context's, pwmgpu_ctx_set_engine, at creation): TILE (default)
+ * builds every pass of every text in one persistent kernel that takes
+ * (text, pass, tile) items from a device work queue, passes of 4 levels, the
+ * tables of every pass derived on the device; the tile size of each text
+ * (1, 2 or 4 16-byte vectors per thread) is the fastest measured for its
+ * (word width, levels, log2 length) class, measured on the first build that
+ * meets the class and cached in the context.  WARP runs a kernel per pass
+ * shape with passes of levels_per_pass (1..4) levels and regroups the trees
+ * from the matrices; levels_per_pass applies to it only. */
 typedef struct pwmgpu_batch pwmgpu_batch;
 PWMGPU_API pwmgpu_status pwmgpu_batch_create(pwmgpu_ctx* ctx, uint32_t count, const uint64_t* offsets,
                                              const uint32_t* levels, uint32_t word_width, uint32_t shape_flags,
@@ -391,6 +409,14 @@ PWMGPU_API pwmgpu_status pwmgpu_batch_create(pwmgpu_ctx* ctx, uint32_t count, co
  * device-side errors. */
 PWMGPU_API pwmgpu_status pwmgpu_batch_build(pwmgpu_ctx* ctx, pwmgpu_batch* batch, const void* d_texts);
 PWMGPU_API pwmgpu_status pwmgpu_batch_set_levels_per_pass(pwmgpu_batch* batch, int levels_per_pass);
+/* Tile engine: every text's tiles take vectors_per_thread (1, 2 or 4) 16-byte
+ * vectors per thread instead of the tuned size (0: tuned again); the next
+ * build plans and records the batch anew. */
+PWMGPU_API pwmgpu_status pwmgpu_batch_set_tile_vectors(pwmgpu_batch* batch, uint32_t vectors_per_thread);
+/* The vectors per thread text `index` was built with (0 on the warp engine,
+ * or before the first build). */
+PWMGPU_API pwmgpu_status pwmgpu_batch_tile_vectors(const pwmgpu_batch* batch, uint32_t index,
+                                                   uint32_t* vectors_per_thread);
 PWMGPU_API pwmgpu_status pwmgpu_batch_check(pwmgpu_ctx* ctx, pwmgpu_batch* batch);
 /* Text `index`'s matrix (which = 0, with its zero counts) or tree (which = 1)
  * in pwm's bit_vectors layout. */

@@ -81,6 +81,11 @@ class Context:
         """Piece size of pinned host-text uploads (default 64 MiB)."""
         self.check(self.lib.pwmgpu_ctx_set_upload_piece_bytes(self.h, int(nbytes)))
 
+    def set_host_copy_threads(self, threads):
+        """Host threads that move pageable buffers through pinned staging
+        pieces (-1: automatic, up to 8; 0: unstaged driver copies)."""
+        self.check(self.lib.pwmgpu_ctx_set_host_copy_threads(self.h, int(threads)))
+
     def release_scratch(self):
         """Frees the buffers and cached structures the context keeps between calls."""
         self.check(self.lib.pwmgpu_ctx_release_scratch(self.h))
@@ -538,7 +543,10 @@ class DeviceStructure:
 class Batch:
     """A batch of independent plain texts built by one CUDA graph
     (pwmgpu_batch_*): every text gets a wavelet matrix and, optionally, a
-    levelwise wavelet tree, bit-identical to a single build of that text."""
+    levelwise wavelet tree, bit-identical to a single build of that text.
+    The context's engine at creation decides how: the tile engine (default,
+    one persistent kernel over a device work queue, tile sizes tuned per
+    text class) or the warp-pass engine."""
 
     def __init__(self, offsets, levels, word_width=1, tree=True, levels_per_pass=2, context=None):
         self.ctx = context or default_context()
@@ -558,7 +566,19 @@ class Batch:
         self.ctx.check(self.ctx.lib.pwmgpu_batch_build(self.ctx.h, self.h, ctypes.c_void_p(int(d_texts_ptr))))
 
     def set_levels_per_pass(self, k):
+        """Warp-pass engine: levels per pass (the tile engine takes 4)."""
         self.ctx.check(self.ctx.lib.pwmgpu_batch_set_levels_per_pass(self.h, int(k)))
+
+    def set_tile_vectors(self, v):
+        """Tile engine: tiles of v (1, 2, 4) vectors per thread for every
+        text, or 0 for the size tuned per text class."""
+        self.ctx.check(self.ctx.lib.pwmgpu_batch_set_tile_vectors(self.h, int(v)))
+
+    def tile_vectors(self, index):
+        """Vectors per thread text `index` was built with (0: warp engine)."""
+        v = ctypes.c_uint32(0)
+        self.ctx.check(self.ctx.lib.pwmgpu_batch_tile_vectors(self.h, int(index), ctypes.byref(v)))
+        return v.value
 
     def check(self):
         self.ctx.check(self.ctx.lib.pwmgpu_batch_check(self.ctx.h, self.h))

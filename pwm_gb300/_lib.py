@@ -64,6 +64,7 @@ SIGNATURES = {
     "pwmgpu_wx_build_sharded": (i32, [vp, vp, vp, u32]),
     "pwmgpu_copy_bits": (i32, [vp, vp, u64, u64, u64, vp]),
     "pwmgpu_ctx_set_upload_piece_bytes": (i32, [vp, u64]),
+    "pwmgpu_ctx_set_host_copy_threads": (i32, [vp, i32]),
     "pwmgpu_ctx_set_stream_chunks": (i32, [vp, u32]),
     "pwmgpu_ctx_set_spin_limit": (i32, [vp, u32]),
     "pwmgpu_ctx_test_withhold_tile": (i32, [vp, i32]),
@@ -98,6 +99,8 @@ SIGNATURES = {
     "pwmgpu_batch_create": (i32, [vp, u32, u64p, u32p, u32, u32, i32, ctypes.POINTER(vp)]),
     "pwmgpu_batch_build": (i32, [vp, vp, vp]),
     "pwmgpu_batch_set_levels_per_pass": (i32, [vp, i32]),
+    "pwmgpu_batch_set_tile_vectors": (i32, [vp, u32]),
+    "pwmgpu_batch_tile_vectors": (i32, [vp, u32, u32p]),
     "pwmgpu_batch_check": (i32, [vp, vp]),
     "pwmgpu_batch_download": (i32, [vp, vp, u32, i32, u64p, u64p]),
     "pwmgpu_batch_free": (None, [vp]),

@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libpwmgpu.so")
 OBJ = os.path.join(HERE, "_build")
 SOURCES = ["abi.cu", "engine.cu", "plain.cu", "huffman.cu", "shards.cu", "batch_host.cu", "build_kernels.cu", "split.cu",
-           "tile.cu", "tile_deep.cu", "ranksel.cu", "batch.cu", "serve.cu", "merge.cu"]
+           "tile.cu", "tile_deep.cu", "tile_batch.cu", "ranksel.cu", "batch.cu", "serve.cu", "merge.cu", "staging.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-fvisibility=hidden", "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-warn-spills"]
@@ -55,7 +55,7 @@ def build(verbose=False, force=False):
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     if force or _stale(OUT, objs):
-        cmd = [cc] + ARCH + ["-shared", "-o", OUT] + objs + ["-Xcompiler", "-fPIC"]
+        cmd = [cc] + ARCH + ["-shared", "-o", OUT] + objs + ["-Xcompiler", "-fPIC", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")

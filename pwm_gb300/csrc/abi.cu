@@ -105,6 +105,15 @@ pwmgpu_status pwmgpu_ctx_set_upload_piece_bytes(pwmgpu_ctx* ctx, uint64_t bytes)
   return PWMGPU_OK;
 }
 
+pwmgpu_status pwmgpu_ctx_set_host_copy_threads(pwmgpu_ctx* ctx, int threads) {
+  if (!ctx || threads < -1 || threads > 256) return PWMGPU_ERR_ARG;
+  return guarded(ctx, [&]() {
+    if (threads != ctx->host_copy_threads) ctx->copy_pool.reset();
+    ctx->host_copy_threads = threads;
+    return PWMGPU_OK;
+  });
+}
+
 pwmgpu_status pwmgpu_ctx_release_scratch(pwmgpu_ctx* ctx) {
   if (!ctx) return PWMGPU_ERR_ARG;
   return guarded(ctx, [&]() {
@@ -329,9 +338,7 @@ pwmgpu_status pwmgpu_wx_download(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which
   const Structure& s = which ? wx->wt : wx->wm;
   if (!s.present) return PWMGPU_ERR_ARG;
   return guarded(ctx, [&]() {
-    if (s.total_words)
-      CUDA_TRY(cudaMemcpyAsync(bv, s.d_words, s.total_words * 8, cudaMemcpyDeviceToHost, ctx->stream));
-    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    device_to_host(ctx, bv, s.d_words, s.total_words * 8, ctx->stream);
     if (zeros && !s.is_tree) std::memcpy(zeros, s.zeros.data(), s.levels * 8);
     return PWMGPU_OK;
   });
@@ -599,7 +606,7 @@ pwmgpu_status pwmgpu_huffman_codes(pwmgpu_ctx* ctx, const void* text, uint64_t s
     if (word_width != 1 && word_width != 2)
       throw Fail{PWMGPU_ERR_ARG, "the code builder takes 8- or 16-bit texts; pass a code table for wider ones"};
     void* d_text = ctx->grow("host_text", size * word_width);
-    CUDA_TRY(cudaMemcpyAsync(d_text, text, size * word_width, cudaMemcpyHostToDevice, ctx->stream));
+    host_to_device(ctx, d_text, text, size * word_width, ctx->stream);
     uint64_t max_symbol = 0;
     HuffCodes h = huffman_codes_device(ctx, d_text, size, word_width, is_tree != 0, &max_symbol);
     if (h.levels > kMaxLevels) throw Fail{PWMGPU_ERR_ARG, "codes longer than 64 bits"};
@@ -625,7 +632,7 @@ pwmgpu_status pwmgpu_compute_huffman(pwmgpu_ctx* ctx, const void* text, uint64_t
   return guarded(ctx, [&]() {
     if (!valid_width(word_width)) throw Fail{PWMGPU_ERR_ARG, "word_width must be 1, 2 or 4"};
     void* d_text = ctx->grow("host_text", size * word_width);
-    CUDA_TRY(cudaMemcpyAsync(d_text, text, size * word_width, cudaMemcpyHostToDevice, ctx->stream));
+    host_to_device(ctx, d_text, text, size * word_width, ctx->stream);
     std::vector<uint64_t> len, word;
     uint32_t L = levels;
     if (code_len) {
@@ -645,8 +652,7 @@ pwmgpu_status pwmgpu_compute_huffman(pwmgpu_ctx* ctx, const void* text, uint64_t
     if (level_sizes)
       for (uint32_t l = 0; l < L; ++l)
         if (level_sizes[l] != s.bits[l]) throw Fail{PWMGPU_ERR_ARG, "level_sizes do not match the code table"};
-    CUDA_TRY(cudaMemcpyAsync(bv, s.d_words, s.total_words * 8, cudaMemcpyDeviceToHost, ctx->stream));
-    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    device_to_host(ctx, bv, s.d_words, s.total_words * 8, ctx->stream);
     if (!is_tree) std::memcpy(zeros, wm.zeros.data(), L * 8);
     wm.release();
     wt.release();

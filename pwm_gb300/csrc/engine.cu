@@ -23,6 +23,7 @@ pwmgpu_ctx::~pwmgpu_ctx() {
   for (cudaStream_t t : {up, down, side})
     if (t) cudaStreamSynchronize(t);
   release_pinned();
+  release_staging(this);
   for (cudaStream_t t : {up, down, side})
     if (t) {
       cudaStreamSynchronize(t);

@@ -25,6 +25,7 @@
 #include "host_stream.hpp"
 #include "host_tables.hpp"
 #include "kernels.cuh"
+#include "staging.hpp"
 
 namespace pwmgpu {
 
@@ -36,6 +37,9 @@ constexpr uint32_t kSinglePassMaxLevels = 7;  // one tile pass for texts of at m
 constexpr uint32_t kMaxStreamChunks = 16;  // chunks of a pass whose finished words stream to pinned outputs
 constexpr uint64_t kAlphabetMaxSymbol = uint64_t(1) << 24;  // 32-bit alphabet reduction: one bin per value below
 constexpr uint64_t kAlphabetHashMaxSymbols = uint64_t(1) << 30;  // wider symbols: through a hash table
+constexpr uint64_t kStagePiece = uint64_t(16) << 20;  // bytes of one pinned staging piece
+constexpr unsigned kStagePieces = 4;                  // pieces in the staging ring
+constexpr unsigned kStageAutoThreads = 8;             // host copy threads by default (at most)
 
 struct Fail {
   pwmgpu_status st;
@@ -81,7 +85,16 @@ struct pwmgpu_ctx {
   uint64_t upload_piece = uint64_t(64) << 20;  // bytes of text per uploaded piece
   uint32_t stream_chunks = 4;                   // chunks of a pass whose words stream to pinned outputs
   uint32_t spin_limit = kSpinLimit;             // polls of one look-back wait of the tile engine
+  // batched tile engine: vectors per thread of the tiles of each (key width,
+  // levels, log2 length) class, measured on first use
+  std::map<uint32_t, uint32_t> batch_tune;
   bool withhold_first_tile = false;             // test hook: look-back passes skip their first tile
+  // pageable host buffers move through pinned staging pieces filled and
+  // drained by host threads (-1: automatic count, 0: the driver copies them)
+  int host_copy_threads = -1;
+  std::unique_ptr<CopyPool> copy_pool;
+  void* stage = nullptr;
+  cudaEvent_t stage_ev[kStagePieces] = {};
   bool async_alloc = false;  // stream-ordered allocations on `stream`
   uint64_t scratch_bytes = 0;
   pwmgpu_wx* compute_cache = nullptr;  // reused by pwmgpu_compute for equal shapes
@@ -410,6 +423,15 @@ struct HostIO {
 // Plain build of a wx from a device text (with `io`: from a host text, into
 // host arrays; d_text is then the device copy to fill).
 void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostIO* io = nullptr);
+
+// ---- host copies (staging.cu) -----------------------------------------------------
+bool host_pinned(const void* p);
+// Host to device on `s`; returns once `h_src` may be reused.  Pageable
+// memory of a piece or more goes through the pinned staging ring.
+void host_to_device(pwmgpu_ctx* ctx, void* d_dst, const void* h_src, uint64_t bytes, cudaStream_t s);
+// Device to host after the work on `s`; returns once `h_dst` holds the bytes.
+void device_to_host(pwmgpu_ctx* ctx, void* h_dst, const void* d_src, uint64_t bytes, cudaStream_t s);
+void release_staging(pwmgpu_ctx* ctx);
 
 // ---- Huffman-shaped builds (huffman.cu) ------------------------------------------
 // Symbol histogram + first occurrences of a device text on the GPU, then the

@@ -196,15 +196,6 @@ void run_tile_passes(pwmgpu_ctx* ctx, const void* in, uint32_t width, uint32_t L
   // the plan may go out of scope with the passes still running)
 }
 
-bool host_pinned(const void* p) {
-  cudaPointerAttributes a{};
-  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return a.type == cudaMemoryTypeHost;
-}
-
 }  // namespace
 
 namespace pwmgpu {
@@ -248,8 +239,7 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
       if (c->down) cudaStreamSynchronize(c->down);
     }
   } drain{ctx, pinned_in || stream_out};
-  if (io && io->text && !pinned_in)
-    CUDA_TRY(cudaMemcpyAsync(const_cast<void*>(d_text), io->text, n * wx->width, cudaMemcpyHostToDevice, s));
+  if (io && io->text && !pinned_in) host_to_device(ctx, const_cast<void*>(d_text), io->text, n * wx->width, s);
   CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, 4, s));
   const uint64_t bins = uint64_t(1) << L;
   auto* d_hist = static_cast<unsigned long long*>(ctx->grow("hist", bins * 8));
@@ -664,7 +654,7 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
       if (!host_out[st] || !sts[st]->present) continue;
       const Structure& S = *sts[st];
       if (stream_out) send(st, sent[st], S.total_words);
-      else CUDA_TRY(cudaMemcpyAsync(host_out[st], S.d_words, S.total_words * 8, cudaMemcpyDeviceToHost, s));
+      else device_to_host(ctx, host_out[st], S.d_words, S.total_words * 8, s);
     }
     if (stream_out) CUDA_TRY(cudaStreamSynchronize(ctx->down));
     CUDA_TRY(cudaStreamSynchronize(s));

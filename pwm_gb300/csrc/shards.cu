@@ -324,7 +324,7 @@ const void* build_input(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, const void* d_text
 // from the device text with only the outputs on the host.
 const void* upload_wide_host_text(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, const void* host_text) {
   void* d40 = ctx->grow("text40", std::max<uint64_t>(wx->n, 1) * 5);
-  CUDA_TRY(cudaMemcpyAsync(d40, host_text, wx->n * 5, cudaMemcpyHostToDevice, ctx->stream));
+  host_to_device(ctx, d40, host_text, wx->n * 5, ctx->stream);
   return build_input(ctx, wx, d40);
 }
 

@@ -58,6 +58,10 @@ struct TileText {
   uint64_t stride;  // words between consecutive levels
   uint64_t nbits;   // bits of every level
   uint32_t shift;   // level l+j tests key bit (shift - j)
+  // Batched passes (tile_pass_body with BATCH) only; zero otherwise:
+  uint32_t vpt;         // 16-byte vectors per thread of this text's tiles (1, 2 or 4)
+  uint32_t wait_idx;    // ~0u, or a counter in TileArgs::done this pass waits for ...
+  uint32_t signal_idx;  // ~0u, or a counter each of its tiles adds one to when done
   uint32_t pad;
 };
 
@@ -93,6 +97,10 @@ struct TileArgs {
   uint64_t zero_words;
   uint32_t zero_per_tile;
   uint32_t spin_limit;  // polls of one look-back wait before it gives up (kErrTimeout)
+  // Batched passes: the per-(text, pass) tile counters (TileText::wait_idx /
+  // signal_idx) and the tiles each counter must reach.
+  unsigned int* done;
+  const unsigned int* need;
 };
 
 template <typename KeyT, int K, bool OUT, int THREADS, int V>
@@ -439,8 +447,14 @@ __device__ __forceinline__ void warp_exclusive_scan(const uint32_t* in, uint32_t
   }
 }
 
-template <typename KeyT, int K, bool OUT, int THREADS, int V>
-__global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / THREADS) tile_pass_kernel(TileArgs a) {
+// One tile of a pass: tile g of the launch's segments.  BATCH: a pass of a
+// batch of texts inside the persistent kernel (tile_batch.cu): the tile size
+// is the text's own (TileText::vpt vectors per thread, a warp's slice
+// shrinking with it), the tile first waits until every tile of the text's
+// previous pass is done and afterwards counts itself done; otherwise
+// TileText's batch fields are ignored.
+template <typename KeyT, int K, bool OUT, int THREADS, int V, bool BATCH>
+__device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in) {
   using C = TileCfg<KeyT, K, OUT, THREADS, V>;
   constexpr int D = C::D, KPL = C::KPL, T = C::T, WARPS = C::WARPS, WSLICE = C::WSLICE, SBW = C::SBW;
   constexpr int NLB = C::NLB, LPC = C::LPC;
@@ -463,7 +477,7 @@ __global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / T
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) {
-    const uint32_t g = a.tile_base + atomicAdd(a.tile_counter, 1u);
+    const uint32_t g = g_in;
     uint32_t lo = 0, hi = a.nsegs;  // last segment with tile0 <= g
     while (hi - lo > 1) {
       const uint32_t mid = (lo + hi) >> 1;
@@ -479,9 +493,28 @@ __global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / T
     s_tx = a.texts[s_sg.text];
   }
   __syncthreads();
+  if constexpr (BATCH) {
+    if (s_tx.wait_idx != ~0u) {  // the text's previous pass wrote this pass's input
+      if (tid == 0) {
+        const volatile unsigned int* dp = a.done + s_tx.wait_idx;
+        const unsigned int need = a.need[s_tx.wait_idx];
+        for (uint32_t spins = 0; *dp < need; ++spins) {
+          if (spins >= a.spin_limit) {
+            atomicOr(a.status, kErrTimeout);
+            break;
+          }
+          __nanosleep(128);
+        }
+        __threadfence();
+      }
+      __syncthreads();
+    }
+  }
+  const int VP = BATCH ? int(s_tx.vpt) : V;  // vectors per thread of this tile
+  const uint32_t TT = BATCH ? uint32_t(THREADS * VP * KPL) : uint32_t(T);
   const uint32_t tl = g - s_sg.tile0;
-  const uint64_t tstart = uint64_t(tl) * T;
-  const uint32_t n = s_sg.m - tstart < uint64_t(T) ? uint32_t(s_sg.m - tstart) : uint32_t(T);
+  const uint64_t tstart = uint64_t(tl) * TT;
+  const uint32_t n = s_sg.m - tstart < uint64_t(TT) ? uint32_t(s_sg.m - tstart) : TT;
   for (int i = tid; i < tile_table_size(K); i += THREADS) s_table[i] = a.tables[s_sg.table + i];
 
   load_tile_bytes<THREADS>(reinterpret_cast<uint4*>(buf0),
@@ -516,7 +549,8 @@ __global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / T
     const uint32_t cbase = smem_base + uint32_t(T * KB) + uint32_t(tid) * 4u;
 #pragma unroll
     for (int r = 0; r < V; ++r) {
-      const int gv = (warp * V + r) * 32 + lane;
+      if (BATCH && r >= VP) break;
+      const int gv = (warp * VP + r) * 32 + lane;
       const uint4 kv = reinterpret_cast<const uint4*>(buf0)[gv];
       const int rem = int(n) - gv * KPL;
       const int nvv = rem >= KPL ? KPL : (rem > 0 ? rem : 0);
@@ -546,8 +580,9 @@ __global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / T
     if (tid == 0) atomicOr(a.status, kErrBounds);  // deeper passes need their prefixes given
   }
   // valid keys of this warp and before it
-  const uint32_t wbeg = uint32_t(warp) * WSLICE;
-  const uint32_t nw = n > wbeg ? min(n - wbeg, uint32_t(WSLICE)) : 0u;
+  const uint32_t wslice = BATCH ? uint32_t(32 * VP * KPL) : uint32_t(WSLICE);
+  const uint32_t wbeg = uint32_t(warp) * wslice;
+  const uint32_t nw = n > wbeg ? min(n - wbeg, wslice) : 0u;
   const uint32_t vbefore = min(n, wbeg);
 
   int cur = 0;
@@ -561,7 +596,13 @@ __global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / T
     int nv[V];
 #pragma unroll
     for (int r = 0; r < V; ++r) {
-      const int gv = (warp * V + r) * 32 + lane;
+      if (BATCH && r >= VP) {  // beyond this tile's vectors (uniform over the CTA)
+        kv[r] = make_uint4(0u, 0u, 0u, 0u);
+        nv[r] = 0;
+        mb[r] = 0;
+        continue;
+      }
+      const int gv = (warp * VP + r) * 32 + lane;
       kv[r] = reinterpret_cast<const uint4*>(cb)[gv];
       const int rem = int(n) - gv * KPL;
       nv[r] = rem >= KPL ? KPL : (rem > 0 ? rem : 0);
@@ -618,7 +659,8 @@ __global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / T
     const uint32_t nb = smem_base + uint32_t((cur ^ 1) * T * KB);
 #pragma unroll
     for (int r = 0; r < V; ++r) {
-      const int gv = (warp * V + r) * 32 + lane;
+      if (BATCH && r >= VP) break;
+      const int gv = (warp * VP + r) * 32 + lane;
       const uint32_t before = min(nw, uint32_t((r * 32 + lane) * KPL));  // valid keys of the warp before the vector
       const uint32_t zd = nb + (zpre + ex[r]) * KB;
       const uint32_t od = nb + (ztot + opre + before - ex[r]) * KB;
@@ -665,7 +707,11 @@ __global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / T
   const int nstruct = s_tx.wt ? 2 : 1;
   for (int st = 0; st < (a.first_level_written ? 0 : nstruct); ++st) {
     const uint64_t dst = s_table[st ? tile_wt_entry(K, 0, 0) : tile_wm_entry(0, 0)] + tstart;
-    write_bits64(st ? s_tx.wt : s_tx.wm, s_tx.nbits, dst, sbits, 0, n, uint32_t(tid), uint32_t(THREADS), a.status);
+    if (a.clear_edges)
+      write_bits64_clear(st ? s_tx.wt : s_tx.wm, s_tx.nbits, dst, sbits, 0, n, uint32_t(tid), uint32_t(THREADS),
+                         a.status);
+    else
+      write_bits64(st ? s_tx.wt : s_tx.wm, s_tx.nbits, dst, sbits, 0, n, uint32_t(tid), uint32_t(THREADS), a.status);
   }
   if constexpr (D >= 1) {
     if (tid < NLB && s_cnt[tid] != rsz[D][tid]) atomicOr(a.status, kErrBounds);  // counts must agree
@@ -852,6 +898,23 @@ __global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / T
       if (a.zero_b) *reinterpret_cast<uint4*>(a.zero_b + w) = zero;
     }
   }
+  if constexpr (BATCH) {
+    if (s_tx.signal_idx != ~0u) {  // every thread's writes are visible before the count
+      __threadfence();
+      __syncthreads();
+      if (tid == 0) atomicAdd(a.done + s_tx.signal_idx, 1u);
+    }
+  }
+}
+
+// A launch of one pass: each CTA takes the next tile from the launch's tile
+// counter.
+template <typename KeyT, int K, bool OUT, int THREADS, int V>
+__global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / THREADS) tile_pass_kernel(TileArgs a) {
+  __shared__ uint32_t s_g;
+  if (threadIdx.x == 0) s_g = a.tile_base + atomicAdd(a.tile_counter, 1u);
+  __syncthreads();
+  tile_pass_body<KeyT, K, OUT, THREADS, V, false>(a, s_g);
 }
 
 }  // namespace pwmgpu

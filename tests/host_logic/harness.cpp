@@ -18,6 +18,7 @@
 #include "../../pwm_gb300/csrc/host_huffman.hpp"
 #include "../../pwm_gb300/csrc/host_stream.hpp"
 #include "../../pwm_gb300/csrc/host_tables.hpp"
+#include "../../pwm_gb300/csrc/staging.hpp"
 
 using namespace pwmgpu;
 
@@ -135,7 +136,34 @@ static int merge(uint32_t L, uint32_t shards, bool tree) {
   return 0;
 }
 
+// The staging copy pool: every size around its slice and 4 KiB boundaries,
+// with 1..9 threads, copies exactly the bytes asked for and nothing past them.
+static int copy(unsigned seed) {
+  std::mt19937_64 rng(seed);
+  const uint64_t sizes[] = {0, 1, 4095, 4096, 4097, (1u << 20) - 1, 1u << 20, (1u << 20) + 1, 3u << 20,
+                            (5u << 20) + 12345, 33u << 20};
+  for (unsigned threads = 1; threads <= 9; ++threads) {
+    pwmgpu::CopyPool pool(threads);
+    if (pool.threads() != threads) return 3;
+    for (uint64_t n : sizes) {
+      std::vector<unsigned char> src(n + 64), dst(n + 64, 0xA5);
+      for (auto& c : src) c = (unsigned char)(rng() & 0xFF);
+      pool.copy(dst.data() + 7, src.data() + 7, n);
+      for (uint64_t i = 0; i < n + 64; ++i) {
+        const bool inside = i >= 7 && i < 7 + n;
+        if (dst[i] != (inside ? src[i] : 0xA5)) {
+          printf("threads %u size %llu byte %llu\n", threads, (unsigned long long)n, (unsigned long long)i);
+          return 1;
+        }
+      }
+    }
+  }
+  printf("ok\n");
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc >= 3 && !strcmp(argv[1], "copy")) return copy(unsigned(atoi(argv[2])));
   if (argc >= 5 && !strcmp(argv[1], "merge"))
     return merge(uint32_t(atoi(argv[2])), uint32_t(atoi(argv[3])), atoi(argv[4]) != 0);
   if (argc >= 6 && !strcmp(argv[1], "plan"))

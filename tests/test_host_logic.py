@@ -6,7 +6,9 @@
   equal pwm's own tables on the golden fixtures (8-bit) and, by hash, on the
   seeded 16-bit texts;
 * the streaming tracker (pwm_gb300/csrc/host_stream.hpp) reports every word
-  of a level exactly once, and only once all its bits are written."""
+  of a level exactly once, and only once all its bits are written;
+* the host threads that fill and drain the pinned staging pieces
+  (pwm_gb300/csrc/staging.hpp) copy exactly the bytes asked for."""
 import os
 import subprocess
 
@@ -23,7 +25,7 @@ SRC = os.path.join(ROOT, "tests", "host_logic", "harness.cpp")
 @pytest.fixture(scope="module")
 def harness(tmp_path_factory):
     exe = str(tmp_path_factory.mktemp("host_logic") / "harness")
-    r = subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-o", exe, SRC], capture_output=True, text=True)
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-pthread", "-o", exe, SRC], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
     return exe
 
@@ -210,3 +212,8 @@ def test_merge_plan(harness, L, shards, tree):
         else:
             cur.append(tuple(int(x) for x in ln.split()))
     assert got == expected_merge(hists, L, tree)
+
+
+def test_staging_copy_pool(harness):
+    r = subprocess.run([harness, "copy", "7"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr
