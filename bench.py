@@ -311,11 +311,21 @@ def other_workloads(torch, pg, ctx, reps=3):
     host16 = t16.cpu().numpy().view(np.uint16)
     del t16
     for tree in (False, True):
+        pg.huffman_codes(host16, tree, ctx)  # warm-up (staging ring, scratch)
         t0 = time.perf_counter()
         codes = pg.huffman_codes(host16, tree, ctx)
+        codes_ms = (time.perf_counter() - t0) * 1e3
+        cons = pg.wx_huff_ps(np.uint16, tree, context=ctx)
+        cons.compute(host16, host16.size, 0, codes=codes)
         t1 = time.perf_counter()
-        ws = pg.wx_huff_ps(np.uint16, tree, context=ctx).compute(host16, host16.size, 0, codes=codes)
+        ws = cons.compute(host16, host16.size, 0, codes=codes)
         t2 = time.perf_counter()
+        # the same call with pageable buffers handed to the driver unstaged
+        ctx.set_host_copy_threads(0)
+        u0 = time.perf_counter()
+        cons.compute(host16, host16.size, 0, codes=codes)
+        u1 = time.perf_counter()
+        ctx.set_host_copy_threads(-1)
         # device-resident: the same codes, a device text, the structure kept in
         # HBM; the kernels' time from the library's CUDA events, and the call
         d_text = torch.from_numpy(host16.view(np.int16)).cuda()
@@ -338,8 +348,9 @@ def other_workloads(torch, pg, ctx, reps=3):
         ds.free()
         del d_text
         out["mix16_2p28_huffman_" + ("tree" if tree else "matrix")] = {
-            "n": int(host16.size), "word_width": 2, "levels": ws.levels(), "codes_ms": (t1 - t0) * 1e3,
+            "n": int(host16.size), "word_width": 2, "levels": ws.levels(), "codes_ms": codes_ms,
             "build_host_to_host_ms": (t2 - t1) * 1e3, "text_gbs_host_to_host": host16.nbytes / (t2 - t1) / 1e9,
+            "build_host_to_host_unstaged_ms": (u1 - u0) * 1e3,
             "device_call_ms": (t4 - t3) * 1e3, "device_kernels_ms": kern_ms,
             "device_kernel_groups": {k: round(v["ms"], 3) for k, v in prof.items()},
             "split_pass_roofline_frac": (hbytes / (prof["split_pass"]["ms"] / 1e3) / 1e9 / measured_peak()[0])
