@@ -14,30 +14,55 @@ __device__ __forceinline__ uint32_t rev_bits_dev(uint32_t v, uint32_t bits) {
   return bits == 0 ? 0u : (__brev(v) >> (32 - bits));
 }
 
-// Leaf histogram of one chunk of one text (2^L <= 4096 bins in shared memory).
+// Leaf histogram of one chunk of one text (2^L <= 4096 bins in shared
+// memory).  The bins are kept in 4096 >> L interleaved copies (at most one
+// per thread; bin s of copy c at s * copies + c, so the lanes of a warp hit
+// different banks), which spreads the atomics of texts with few levels over
+// the copies instead of piling them on a handful of words.  The chunk is
+// read in 16-byte vectors between its unaligned ends.
 template <typename T>
 __global__ void __launch_bounds__(kBatchThreads) batch_hist_kernel(const T* __restrict__ texts,
                                                                    const BatchChunk* __restrict__ chunks,
                                                                    const BatchText* __restrict__ info,
                                                                    unsigned long long* hist, uint32_t* status) {
+  constexpr uint32_t E = 16 / sizeof(T);  // symbols per vector
   __shared__ uint32_t h[4096];
   const BatchChunk c = chunks[blockIdx.x];
   const BatchText t = info[c.text];
   const uint32_t bins = 1u << t.levels;
-  for (uint32_t i = threadIdx.x; i < bins; i += kBatchThreads) h[i] = 0;
+  const uint32_t copies = min(uint32_t(kBatchThreads), 4096u >> t.levels);
+  const uint32_t mine = threadIdx.x % copies;
+  for (uint32_t i = threadIdx.x; i < bins * copies; i += kBatchThreads) h[i] = 0;
   __syncthreads();
   bool bad = false;
+  auto count = [&](uint32_t s) {
+    if (s >= bins) bad = true;
+    else atomicAdd(&h[s * copies + mine], 1u);
+  };
   const T* p = texts + t.offset + c.start;
-  for (uint64_t i = threadIdx.x; i < c.len; i += kBatchThreads) {
-    const uint64_t s = uint64_t(p[i]);
-    if (s >= bins) { bad = true; continue; }
-    atomicAdd(&h[s], 1u);
+  const uint64_t head = min(c.len, uint64_t((16u - (reinterpret_cast<uintptr_t>(p) & 15u)) & 15u) / sizeof(T));
+  const uint64_t nv = (c.len - head) / E;
+  if (threadIdx.x < head) count(uint32_t(p[threadIdx.x]));
+  const uint4* v = reinterpret_cast<const uint4*>(p + head);
+  for (uint64_t k = threadIdx.x; k < nv; k += kBatchThreads) {
+    const uint4 x = __ldcs(v + k);
+    const uint32_t w[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+    for (uint32_t e = 0; e < E; ++e) {
+      if constexpr (sizeof(T) == 1) count((w[e >> 2] >> (8 * (e & 3))) & 0xFFu);
+      else if constexpr (sizeof(T) == 2) count((w[e >> 1] >> (16 * (e & 1))) & 0xFFFFu);
+      else count(w[e]);
+    }
   }
+  for (uint64_t i = head + nv * E + threadIdx.x; i < c.len; i += kBatchThreads) count(uint32_t(p[i]));
   if (bad) atomicOr(status, kErrSymbol);
   __syncthreads();
   unsigned long long* out = hist + t.hist_off;
-  for (uint32_t i = threadIdx.x; i < bins; i += kBatchThreads)
-    if (h[i]) atomicAdd(&out[i], (unsigned long long)h[i]);
+  for (uint32_t s = threadIdx.x; s < bins; s += kBatchThreads) {
+    uint32_t sum = 0;
+    for (uint32_t k = 0; k < copies; ++k) sum += h[s * copies + k];
+    if (sum) atomicAdd(&out[s], (unsigned long long)sum);
+  }
 }
 
 // Per-text tables from the leaf histogram (one CTA per text, L <= 12):

@@ -241,13 +241,17 @@ struct TilePassHost {
   std::vector<uint64_t> table;  // per segment: tile_table_size(K) entries
 };
 
-// cnt: the folded prefix counts (fold_prefix_counts).  T: keys per tile.
-// regroup: tree levels the passes leave to the regroup (empty without a
-// tree).  Exclusive prefixes over all 2^m groups of a level are built only
-// for the levels of segmented passes (few groups); a matrix-only pass needs
-// only the counts of its own K bits, folded from one level.
+// cnt: the folded prefix counts (fold_prefix_counts).  tile_keys(l): keys
+// per tile of the pass starting at level l (its key width may narrow as the
+// passes go on).  regroup: tree levels the passes leave to the regroup
+// (empty without a tree).  Exclusive prefixes over all 2^m groups of a level
+// are built only for the levels of segmented passes (few groups); a
+// matrix-only pass needs only the counts of its own K bits, folded from one
+// level.
+template <typename TileKeys>
 inline std::vector<TilePassHost> plan_tile_passes(const PrefixCounts& cnt, uint32_t L, int kmax,
-                                                  uint32_t T, bool want_tree, std::vector<uint32_t>* regroup) {
+                                                  TileKeys tile_keys, bool want_tree,
+                                                  std::vector<uint32_t>* regroup) {
   const uint64_t n = cnt[0][0];
   std::vector<std::vector<uint64_t>> pren(L + 1), prek(L + 1);
   auto prefixes = [&](uint32_t m) {  // natural order (tree) and key order (matrix: reversed prefix)
@@ -267,6 +271,7 @@ inline std::vector<TilePassHost> plan_tile_passes(const PrefixCounts& cnt, uint3
     const uint32_t l = pp.level;
     const int K = pp.K;
     const uint64_t groups = uint64_t(1) << l;
+    const uint32_t T = tile_keys(l);
     ps.segmented = want_tree && (l == 0 || (groups <= 65536 && n >= groups * 4 * uint64_t(T)));
     const int TS = tile_table_size(K);
     uint32_t tile = 0;
@@ -325,6 +330,12 @@ inline std::vector<TilePassHost> plan_tile_passes(const PrefixCounts& cnt, uint3
     passes.push_back(std::move(ps));
   }
   return passes;
+}
+
+// The same with T keys per tile in every pass.
+inline std::vector<TilePassHost> plan_tile_passes(const PrefixCounts& cnt, uint32_t L, int kmax, uint32_t T,
+                                                  bool want_tree, std::vector<uint32_t>* regroup) {
+  return plan_tile_passes(cnt, L, kmax, [T](uint32_t) { return T; }, want_tree, regroup);
 }
 
 // One run of a merge of shards (pwm's merge_bit_vectors, include/

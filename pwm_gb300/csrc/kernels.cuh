@@ -125,7 +125,12 @@ void launch_split_pass_batched(uint32_t key_bytes, int K, const SplitArgs* args,
 // Keys of one tile for a key width.
 uint32_t tile_pass_elems(uint32_t key_bytes);
 // One pass of K levels over a.tiles tiles; `out`: the pass writes S_{l+K}.
-void launch_tile_pass(uint32_t key_bytes, int K, bool out, const TileArgs& a, cudaStream_t s, uint64_t* launches);
+// The narrowest key width (1, 2 or 4 bytes) holding `bits` bits.
+uint32_t tile_key_bytes(uint32_t bits);
+// One tile pass over keys of key_bytes; a pass writing S_{l+K} (out) writes
+// it in keys of out_bytes <= key_bytes, their low bits.
+void launch_tile_pass(uint32_t key_bytes, uint32_t out_bytes, int K, bool out, const TileArgs& a, cudaStream_t s,
+                      uint64_t* launches);
 
 // ---- wavelet tree from the matrix --------------------------------------------
 // Level `m` of the tree: the matrix level with its prefix groups reordered.

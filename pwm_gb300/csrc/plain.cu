@@ -21,6 +21,14 @@ struct TileFirstPass {
   bool level0_written = false;  // the histogram kernel wrote level 0 of both structures
 };
 
+// Key width of S_l for the pass starting at level l of an L-level text of
+// `width`-byte symbols: the text itself at l = 0; later the narrowest width
+// that holds the L - l bits the remaining levels split on (a pass writes
+// only the low bits of its keys), never wider than the text.
+uint32_t tile_pass_key_bytes(uint32_t width, uint32_t L, uint32_t l) {
+  return l == 0 ? width : std::min(width, tile_key_bytes(L - l));
+}
+
 // Device descriptors of passes [from, to): per pass its segments, its level
 // descriptor and its start tables, at offsets of one uploaded blob.
 struct TileBlob {
@@ -83,6 +91,8 @@ const void* enqueue_tile_pass(pwmgpu_ctx* ctx, const std::vector<TilePassHost>& 
   const auto& p = passes[pi];
   void* ping = ctx->grow("keys_a", std::max<uint64_t>(n, 1) * width);
   void* pong = ctx->grow("keys_b", std::max<uint64_t>(n, 1) * width);
+  const uint32_t in_bytes = tile_pass_key_bytes(width, wm.levels, pi == 0 ? 0u : p.level);
+  const uint32_t out_bytes = tile_pass_key_bytes(width, wm.levels, p.level + uint32_t(p.K));
   const int D = p.out ? p.K : p.K - 1;
   const uint64_t nlb = uint64_t(1) << D;
   const uint64_t lb_bytes = uint64_t(std::max<uint32_t>(p.tiles, 1)) * nlb * 8;
@@ -132,7 +142,7 @@ const void* enqueue_tile_pass(pwmgpu_ctx* ctx, const std::vector<TilePassHost>& 
     a.launch_tiles = b[c + 1] - b[c];
     {
       ProfScope ps(ctx, "split_pass", p.tiles ? bytes * a.launch_tiles / p.tiles : 0);
-      launch_tile_pass(width, p.K, p.out, a, s, &ctx->launches);
+      launch_tile_pass(in_bytes, out_bytes, p.K, p.out, a, s, &ctx->launches);
     }
     CUDA_TRY(cudaGetLastError());
     if (after_chunk) after_chunk(c);
@@ -454,7 +464,9 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   PrefixCounts cnt;  // natural-prefix counts per level
   if (tile_engine) {
     cnt = PrefixCounts::view(h_flat, L);
-    tile_passes = plan_tile_passes(cnt, L, kmax, tile_pass_elems(wx->width), want_tree, &regroup);
+    const uint32_t w = wx->width;
+    tile_passes = plan_tile_passes(
+        cnt, L, kmax, [&](uint32_t l) { return tile_pass_elems(tile_pass_key_bytes(w, L, l)); }, want_tree, &regroup);
     tabs = build_tables_tile(cnt, L, want_tree ? regroup : std::vector<uint32_t>{}, h_zeros);
   } else {
     plan = plan_passes(L, ctx->pass_levels);

@@ -389,6 +389,14 @@ __device__ __forceinline__ void write_key_run(unsigned char* dst, const unsigned
   if (uint32_t(lane) < len - done) dst[done + lane] = src[done + lane];
 }
 
+// One warp copies `len` keys from shared memory to global memory, each
+// narrowed to its low 8 * sizeof(KeyO) bits (the bits of the levels the
+// following passes still split on): a key per lane and step.
+template <typename KeyT, typename KeyO>
+__device__ __forceinline__ void write_key_run_narrow(KeyO* dst, const KeyT* src, uint32_t len) {
+  for (uint32_t i = threadIdx.x & 31; i < len; i += 32) dst[i] = KeyO(src[i]);
+}
+
 // Load `bytes` bytes from global `src` (any alignment) into the 16-byte
 // aligned shared buffer `dst`, 16 bytes per thread step.  Bytes past the end
 // of the tile are not read beyond the 16-byte block that holds the last one.
@@ -453,7 +461,9 @@ __device__ __forceinline__ void warp_exclusive_scan(const uint32_t* in, uint32_t
 // shrinking with it), the tile first waits until every tile of the text's
 // previous pass is done and afterwards counts itself done; otherwise
 // TileText's batch fields are ignored.
-template <typename KeyT, int K, bool OUT, int THREADS, int V, bool BATCH>
+// KeyO: the key type of S_{l+K} (KeyT, or narrower when the levels left
+// after this pass fit it).
+template <typename KeyT, int K, bool OUT, int THREADS, int V, bool BATCH, typename KeyO = KeyT>
 __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in) {
   using C = TileCfg<KeyT, K, OUT, THREADS, V>;
   constexpr int D = C::D, KPL = C::KPL, T = C::T, WARPS = C::WARPS, WSLICE = C::WSLICE, SBW = C::SBW;
@@ -476,15 +486,26 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
   __shared__ unsigned long long s_table[tile_table_size(K)];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) {
+  if (warp == 0) {
+    // the last segment with tile0 <= g, by a 32-way search of warp 0 (a
+    // batch has thousands of segments: three dependent loads, not twelve).
+    // Invariant: segs[lo].tile0 <= g < segs[hi].tile0 (hi = nsegs: none).
     const uint32_t g = g_in;
-    uint32_t lo = 0, hi = a.nsegs;  // last segment with tile0 <= g
+    uint32_t lo = 0, hi = a.nsegs;
     while (hi - lo > 1) {
-      const uint32_t mid = (lo + hi) >> 1;
-      if (a.segs[mid].tile0 <= g) lo = mid; else hi = mid;
+      const uint32_t span = hi - lo;
+      const uint32_t idx = span <= 32 ? lo + uint32_t(lane) : lo + uint32_t((uint64_t(span) * uint32_t(lane)) >> 5);
+      const bool le = idx < hi && (idx == lo || a.segs[idx].tile0 <= g);
+      const uint32_t m = __ballot_sync(0xFFFFFFFFu, le);
+      const int k = 31 - __clz(m);  // the last probe at or before the answer (lane 0 always is)
+      const uint32_t nxt = __shfl_sync(0xFFFFFFFFu, idx, k < 31 ? k + 1 : 31);
+      lo = __shfl_sync(0xFFFFFFFFu, idx, k);
+      if (k < 31) hi = min(hi, nxt);
     }
-    s_tile = g;
-    s_seg = lo;
+    if (lane == 0) {
+      s_tile = g;
+      s_seg = lo;
+    }
   }
   __syncthreads();
   const uint32_t g = s_tile;
@@ -869,8 +890,11 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
         if (lane == 0) atomicOr(a.status, kErrBounds);
         continue;
       }
-      write_key_run(reinterpret_cast<unsigned char*>(static_cast<KeyT*>(a.out) + dst),
-                    reinterpret_cast<const unsigned char*>(cb + rst[D][v]), len * uint32_t(KB));
+      if constexpr (sizeof(KeyO) == sizeof(KeyT))
+        write_key_run(reinterpret_cast<unsigned char*>(static_cast<KeyT*>(a.out) + dst),
+                      reinterpret_cast<const unsigned char*>(cb + rst[D][v]), len * uint32_t(KB));
+      else
+        write_key_run_narrow<KeyT, KeyO>(static_cast<KeyO*>(a.out) + dst, cb + rst[D][v], len);
     } else {
       const int e = (it - NOUT) % (NINNER > 0 ? NINNER : 1);
       const int st = (it - NOUT) / (NINNER > 0 ? NINNER : 1);
@@ -909,12 +933,12 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
 
 // A launch of one pass: each CTA takes the next tile from the launch's tile
 // counter.
-template <typename KeyT, int K, bool OUT, int THREADS, int V>
+template <typename KeyT, int K, bool OUT, int THREADS, int V, typename KeyO = KeyT>
 __global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / THREADS) tile_pass_kernel(TileArgs a) {
   __shared__ uint32_t s_g;
   if (threadIdx.x == 0) s_g = a.tile_base + atomicAdd(a.tile_counter, 1u);
   __syncthreads();
-  tile_pass_body<KeyT, K, OUT, THREADS, V, false>(a, s_g);
+  tile_pass_body<KeyT, K, OUT, THREADS, V, false, KeyO>(a, s_g);
 }
 
 }  // namespace pwmgpu

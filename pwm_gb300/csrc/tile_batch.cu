@@ -20,6 +20,39 @@ namespace {
 
 constexpr int kPlanThreads = 256;
 
+// The per-thread partial sums part[0..kPlanThreads) replaced by their
+// exclusive prefixes (warp 0, 8 per lane, one shuffle scan); returns the
+// total.  Called by every thread after part is written.
+__device__ unsigned long long scan_parts(unsigned long long* part) {
+  static_assert(kPlanThreads == 256, "8 partial sums per lane of one warp");
+  __shared__ unsigned long long total;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int lane = int(threadIdx.x);
+    unsigned long long v[8], sum = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      v[q] = part[8 * lane + q];
+      sum += v[q];
+    }
+    unsigned long long x = sum;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+      if (lane >= d) x += y;
+    }
+    unsigned long long run = x - sum;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      part[8 * lane + q] = run;
+      run += v[q];
+    }
+    if (lane == 31) total = x;
+  }
+  __syncthreads();
+  return total;
+}
+
 // Exclusive prefix sums of a[0..len) into out[0..len), the total into
 // out[len] (len <= 2^kTileBatchMaxLevels), by one CTA; `fetch(i)` gives
 // element i.  Each thread sums a run of consecutive elements.
@@ -31,17 +64,8 @@ __device__ void cta_exclusive_scan(uint64_t len, F fetch, uint64_t* out, unsigne
   unsigned long long sum = 0;
   for (uint64_t i = b; i < e; ++i) sum += fetch(i);
   part[tid] = sum;
-  __syncthreads();
-  if (tid == 0) {
-    unsigned long long run = 0;
-    for (int t = 0; t < kPlanThreads; ++t) {
-      const unsigned long long x = part[t];
-      part[t] = run;
-      run += x;
-    }
-    out[len] = run;
-  }
-  __syncthreads();
+  const unsigned long long total = scan_parts(part);
+  if (tid == 0) out[len] = total;
   unsigned long long run = part[tid];
   for (uint64_t i = b; i < e; ++i) {
     const unsigned long long x = fetch(i);
@@ -82,12 +106,8 @@ __global__ void __launch_bounds__(kPlanThreads) tile_batch_fold_kernel(const Til
     unsigned long long z = 0;
     for (uint64_t p = 2 * threadIdx.x; p < (uint64_t(2) << m); p += 2 * kPlanThreads) z += c[p];
     part[threadIdx.x] = z;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      unsigned long long s = 0;
-      for (int i = 0; i < kPlanThreads; ++i) s += part[i];
-      zeros[t.zeros_off + m] = s;
-    }
+    const unsigned long long total = scan_parts(part);
+    if (threadIdx.x == 0) zeros[t.zeros_off + m] = total;
     __syncthreads();
   }
   for (uint32_t m = 0; m <= L; ++m) {
@@ -143,12 +163,8 @@ __global__ void __launch_bounds__(kPlanThreads) tile_batch_segments_kernel(
       for (uint32_t v = 0; v < (1u << K); ++v) tb[tile_out_entry(int(K), int(v))] = t.key_begin + PK(l + K, (uint64_t(v) << l) | g);
   }
   part[threadIdx.x] = tiles;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned long long s = 0;
-    for (int i = 0; i < kPlanThreads; ++i) s += part[i];
-    need[p.slot] = unsigned(s);
-  }
+  const unsigned long long total = scan_parts(part);
+  if (threadIdx.x == 0) need[p.slot] = unsigned(total);
 }
 
 // Per group: the first tile of every segment (exclusive sums of the tile
@@ -185,6 +201,11 @@ __global__ void __launch_bounds__(256, 4) tile_batch_kernel(TileBatchQueue q) {
   __shared__ uint32_t s_base[kTileBatchMaxGroups + 1];
   __shared__ uint32_t s_item, s_gi;
   __shared__ __align__(16) TileArgs s_args;
+  // Thread 0 claims the next item as soon as it starts one, so the claim's
+  // round trip overlaps the tile.  (The earliest unfinished item is always
+  // running or about to run: a CTA's claimed item follows its current one in
+  // queue order, so the queue still drains.)
+  uint32_t next = 0;
   if (threadIdx.x == 0) {
     uint32_t run = 0;
     for (uint32_t k = 0; k < q.ngroups; ++k) {
@@ -192,25 +213,29 @@ __global__ void __launch_bounds__(256, 4) tile_batch_kernel(TileBatchQueue q) {
       run += q.group_tiles[k];
     }
     s_base[q.ngroups] = run;
+    next = atomicAdd(q.head, 1u);
   }
-  __syncthreads();
+  uint32_t have = ~0u;  // the group whose arguments s_args holds
   for (;;) {
+    __syncthreads();  // s_base is set; the previous item is done with shared memory
     if (threadIdx.x == 0) {
-      const uint32_t item = atomicAdd(q.head, 1u);
+      const uint32_t item = next;
       uint32_t k = 0;
       while (k < q.ngroups && item >= s_base[k + 1]) ++k;
       s_item = item;
       s_gi = k;
+      if (k < q.ngroups) next = atomicAdd(q.head, 1u);
     }
     __syncthreads();
     const uint32_t k = s_gi;
     if (k >= q.ngroups) break;
-    {
+    if (k != have) {
       const uint32_t* src = reinterpret_cast<const uint32_t*>(q.args + k);
       uint32_t* dst = reinterpret_cast<uint32_t*>(&s_args);
       for (uint32_t i = threadIdx.x; i < sizeof(TileArgs) / 4; i += blockDim.x) dst[i] = src[i];
+      have = k;
+      __syncthreads();
     }
-    __syncthreads();
     const uint32_t g = s_item - s_base[k];
     switch (q.variant[k]) {
       case kTileBatchK4Out: tile_pass_body<KeyT, 4, true, 256, 4, true>(s_args, g); break;
@@ -219,7 +244,6 @@ __global__ void __launch_bounds__(256, 4) tile_batch_kernel(TileBatchQueue q) {
       case kTileBatchK2: tile_pass_body<KeyT, 2, false, 256, 4, true>(s_args, g); break;
       default: tile_pass_body<KeyT, 1, false, 256, 4, true>(s_args, g); break;
     }
-    __syncthreads();  // shared memory is reused by the next item
   }
 }
 

@@ -9,10 +9,10 @@ namespace pwmgpu {
 constexpr int kTileThreads = 256;
 constexpr int kTileVectors = 4;  // 16-byte vectors per thread: 64 bytes of keys
 
-template <typename KeyT, int K, bool OUT>
+template <typename KeyT, int K, bool OUT, typename KeyO = KeyT>
 void launch_tile_one(const TileArgs& a, cudaStream_t s) {
   using C = TileCfg<KeyT, K, OUT, kTileThreads, kTileVectors>;
-  auto kern = tile_pass_kernel<KeyT, K, OUT, kTileThreads, kTileVectors>;
+  auto kern = tile_pass_kernel<KeyT, K, OUT, kTileThreads, kTileVectors, KeyO>;
   static bool configured = false;  // attribute set once per instantiation
   if (!configured) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(C::smem_bytes()));
