@@ -559,6 +559,100 @@ __global__ void symbol_hist_kernel(const T* text, uint64_t n, uint64_t nsym, uns
 // n words and a status word into host-mapped memory: small results the host
 // waits for, written by the SMs instead of a copy engine, so that they do not
 // queue behind bulk downloads.
+// Matrix-only builds of more than 8 levels need, per pass, only the counts
+// of its natural K-bit digit (the bits of its levels, the first most
+// significant), not a leaf histogram of 2^L bins.  Each thread counts into
+// its own column of (pass, digit) counters (counter (e, lane) at e * 32 +
+// lane: the lanes of an atomic never share a bank), a CTA adds its totals to
+// `digits` in global memory, and the last CTA to finish writes, into mapped
+// host memory, the natural prefix counts of levels 0..K0 (flat: level m at
+// 2^m - 1; the first pass's start table reads them), the zero bits of every
+// level, the status word and the digit counts.
+__global__ void __launch_bounds__(256) pass_digits_kernel(const unsigned char* __restrict__ text, uint64_t n,
+                                                          uint32_t width, PassDigitsArgs pd,
+                                                          unsigned long long* digits, unsigned int* done,
+                                                          uint32_t* status, uint64_t* out) {
+  extern __shared__ uint32_t dcnt[];  // [npasses * 16][32]
+  const uint32_t tid = threadIdx.x, lane = tid & 31;
+  const uint32_t ncnt = pd.npasses * 16;
+  for (uint32_t i = tid; i < ncnt * 32; i += blockDim.x) dcnt[i] = 0;
+  __syncthreads();
+  const uint32_t base = uint32_t(__cvta_generic_to_shared(dcnt)) + lane * 4;
+  bool bad = false;
+  auto count = [&](uint32_t x) {
+    if (pd.L < 32 && (x >> pd.L)) {
+      bad = true;
+      return;
+    }
+    for (uint32_t p = 0; p < pd.npasses; ++p) {
+      const uint32_t d = (x >> pd.lo[p]) & pd.mask[p];
+      asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(base + (p * 16 + d) * 128) : "memory");
+    }
+  };
+  // 16-byte vectors between the unaligned ends of the text
+  const uint32_t E = 16 / width;
+  const uint64_t head = min(n, uint64_t((16u - (reinterpret_cast<uintptr_t>(text) & 15u)) & 15u) / width);
+  const uint64_t nv = (n - head) / E;
+  auto sym = [&](uint64_t i) {
+    return width == 1 ? uint32_t(text[i]) : width == 2 ? uint32_t(reinterpret_cast<const uint16_t*>(text)[i])
+                                                       : reinterpret_cast<const uint32_t*>(text)[i];
+  };
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x, gid = uint64_t(blockIdx.x) * blockDim.x + tid;
+  if (gid < head) count(sym(gid));
+  const uint4* v = reinterpret_cast<const uint4*>(text + head * width);
+  for (uint64_t k = gid; k < nv; k += stride) {
+    const uint4 x = __ldcs(v + k);
+    const uint32_t w[4] = {x.x, x.y, x.z, x.w};
+    if (width == 1) {
+#pragma unroll
+      for (int e = 0; e < 16; ++e) count((w[e >> 2] >> (8 * (e & 3))) & 0xFFu);
+    } else if (width == 2) {
+#pragma unroll
+      for (int e = 0; e < 8; ++e) count((w[e >> 1] >> (16 * (e & 1))) & 0xFFFFu);
+    } else {
+#pragma unroll
+      for (int e = 0; e < 4; ++e) count(w[e]);
+    }
+  }
+  for (uint64_t i = head + nv * E + gid; i < n; i += stride) count(sym(i));
+  if (bad) atomicOr(status, kErrSymbol);
+  __syncthreads();
+  for (uint32_t e = tid; e < ncnt; e += blockDim.x) {
+    uint32_t sum = 0;
+    for (uint32_t l = 0; l < 32; ++l) sum += dcnt[e * 32 + ((l + e) & 31)];
+    if (sum) atomicAdd(&digits[e], (unsigned long long)sum);
+  }
+  __threadfence();
+  __syncthreads();
+  __shared__ bool last;
+  if (tid == 0) last = atomicAdd(done, 1u) + 1 == gridDim.x;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const volatile unsigned long long* dg = digits;
+  // flat natural prefix counts of levels 0..K0 (the first pass, from level 0)
+  const uint32_t K0 = pd.K[0];
+  uint64_t* flat = out;
+  for (uint32_t i = tid; i < (2u << K0) - 1; i += blockDim.x) {
+    const uint32_t m = 31 - __clz(i + 1), q = i + 1 - (1u << m);  // level m, prefix q
+    unsigned long long c = 0;
+    for (uint32_t d = 0; d < (1u << K0); ++d)
+      if ((d >> (K0 - m)) == q) c += dg[d];
+    flat[i] = c;
+  }
+  uint64_t* zeros = out + (2u << K0) - 1;
+  for (uint32_t p = 0; p < pd.npasses; ++p)
+    for (uint32_t j = tid; j < pd.K[p]; j += blockDim.x) {
+      unsigned long long z = 0;
+      for (uint32_t d = 0; d < (1u << pd.K[p]); ++d)
+        if (!((d >> (pd.K[p] - 1 - j)) & 1u)) z += dg[p * 16 + d];
+      zeros[pd.level[p] + j] = z;
+    }
+  uint64_t* rest = zeros + pd.L;
+  if (tid == 0) rest[0] = *static_cast<volatile uint32_t*>(status);
+  for (uint32_t e = tid; e < ncnt; e += blockDim.x) rest[1 + e] = dg[e];
+}
+
 __global__ void readback_kernel(const unsigned long long* src, uint64_t n, const uint32_t* status, uint64_t* dst) {
   for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
     dst[i] = src[i];
@@ -858,6 +952,26 @@ void launch_symbol_histogram(const void* text, uint64_t n, uint32_t width, uint6
     return;
   }
   symbol_hist_kernel<<<g, 256, 0, s>>>(static_cast<const uint32_t*>(text), n, nsym, hist, first);
+  ++*launches;
+}
+
+void launch_pass_digits(const void* text, uint64_t n, uint32_t width, const PassDigitsArgs& pd,
+                        unsigned long long* digits, unsigned int* done, uint32_t* status, uint64_t* out,
+                        cudaStream_t s, uint64_t* launches) {
+  const size_t smem = size_t(pd.npasses) * 16 * 32 * 4;
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(pass_digits_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(kPassDigitsMaxPasses * 16 * 32 * 4));
+    configured = true;
+  }
+  const uint64_t vecs = (n * width + 15) / 16;
+  const uint64_t want = (vecs + 255) / 256;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+  const uint64_t cap = uint64_t(sms > 0 ? sms : 1) * 4;
+  pass_digits_kernel<<<unsigned(std::max<uint64_t>(1, std::min(want, cap))), 256, smem, s>>>(
+      static_cast<const unsigned char*>(text), n, width, pd, digits, done, status, out);
   ++*launches;
 }
 

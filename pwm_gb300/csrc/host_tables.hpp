@@ -241,6 +241,28 @@ struct TilePassHost {
   std::vector<uint64_t> table;  // per segment: tile_table_size(K) entries
 };
 
+// Start table of a matrix-only pass over all of S_l (one segment) from the
+// counts of its natural K-bit digit (digit[d]: the symbols whose bits of
+// levels l..l+K-1, level l's most significant, read d): the starts of the
+// runs of key_j (the same bits, level l's least significant) in levels
+// l..l+K-1 and, with `out`, in S_{l+K}.
+inline void matrix_pass_table(const std::vector<uint64_t>& digit, int K, bool out, std::vector<uint64_t>& tab) {
+  std::vector<uint64_t> ck(size_t(1) << K, 0);  // by key_K
+  for (size_t r = 0; r < ck.size(); ++r) ck[rev_bits_host(r, uint32_t(K))] += digit[r];
+  for (int j = 0; j <= K; ++j) {
+    if (j < K || out) {
+      uint64_t run = 0;
+      for (int v = 0; v < (1 << j); ++v) {
+        uint64_t cv = 0;  // key_j == v: the low j bits of key_K
+        for (int h = 0; h < (1 << (K - j)); ++h) cv += ck[size_t(v + (h << j))];
+        if (j < K) tab[size_t(tile_wm_entry(j, v))] = run;
+        else tab[size_t(tile_out_entry(K, v))] = run;
+        run += cv;
+      }
+    }
+  }
+}
+
 // cnt: the folded prefix counts (fold_prefix_counts).  tile_keys(l): keys
 // per tile of the pass starting at level l (its key width may narrow as the
 // passes go on).  regroup: tree levels the passes leave to the regroup
@@ -298,29 +320,16 @@ inline std::vector<TilePassHost> plan_tile_passes(const PrefixCounts& cnt, uint3
         add_segment(prek[l][g], m, tab, g);
       }
     } else {
-      // counts of key_K (bits l..l+K-1, first least significant) over the
-      // whole text, from the natural prefixes of level l+K; key_j folds it
+      // counts of the pass's natural K-bit digit (bits of levels l..l+K-1,
+      // level l's most significant) over the whole text: the natural
+      // prefixes of level l+K summed by their last K bits
       const uint32_t top = l + uint32_t(K);
-      std::vector<uint64_t> ck(size_t(1) << K, 0);
       const CountSpan c = cnt[top];
-      // sums over the prefixes with the same last K bits, then reversed
       const size_t R = size_t(1) << K;
       std::vector<uint64_t> low(R, 0);
       for (size_t p = 0; p < c.size(); p += R)
         for (size_t r = 0; r < R; ++r) low[r] += c[p + r];
-      for (size_t r = 0; r < R; ++r) ck[rev_bits_host(r, uint32_t(K))] += low[r];
-      for (int j = 0; j <= K; ++j) {
-        if (j < K || ps.out) {
-          uint64_t run = 0;
-          for (int v = 0; v < (1 << j); ++v) {
-            uint64_t cv = 0;  // key_j == v: the low j bits of key_K
-            for (int h = 0; h < (1 << (K - j)); ++h) cv += ck[size_t(v + (h << j))];
-            if (j < K) tab[size_t(tile_wm_entry(j, v))] = run;
-            else tab[size_t(tile_out_entry(K, v))] = run;
-            run += cv;
-          }
-        }
-      }
+      matrix_pass_table(low, K, ps.out, tab);
       add_segment(0, n, tab, 0);
       if (want_tree && regroup)
         for (int j = 0; j < K; ++j)
@@ -330,6 +339,47 @@ inline std::vector<TilePassHost> plan_tile_passes(const PrefixCounts& cnt, uint3
     passes.push_back(std::move(ps));
   }
   return passes;
+}
+
+// Matrix-only passes (no tree) from the digit counts of each pass alone:
+// digits[16 p + d] counts the natural K-bit digit d of pass p (the passes of
+// plan_passes(L, kmax)); the same plan as plan_tile_passes without a tree.
+template <typename TileKeys>
+inline std::vector<TilePassHost> plan_matrix_passes(const uint64_t* digits, uint64_t n, uint32_t L, int kmax,
+                                                    TileKeys tile_keys) {
+  std::vector<TilePassHost> passes;
+  size_t pi = 0;
+  for (const auto& pp : plan_passes(L, kmax)) {
+    TilePassHost ps;
+    ps.level = pp.level;
+    ps.K = pp.K;
+    ps.out = pp.has_out;
+    std::vector<uint64_t> tab(size_t(tile_table_size(pp.K)), 0);
+    const std::vector<uint64_t> digit(digits + 16 * pi, digits + 16 * pi + (size_t(1) << pp.K));
+    matrix_pass_table(digit, pp.K, ps.out, tab);
+    if (n) {
+      ps.segs.push_back({0, n, 0, 0u, 0u, 0});
+      ps.table = tab;
+      ps.tiles = uint32_t((n + tile_keys(pp.level) - 1) / tile_keys(pp.level));
+    }
+    passes.push_back(std::move(ps));
+    ++pi;
+  }
+  return passes;
+}
+
+// Zero bits of every level from the same digit counts: level l+j of pass p
+// is bit K-1-j of its digit.
+inline std::vector<uint64_t> matrix_pass_zeros(const uint64_t* digits, uint32_t L, int kmax) {
+  std::vector<uint64_t> z(L, 0);
+  size_t pi = 0;
+  for (const auto& pp : plan_passes(L, kmax)) {
+    for (int j = 0; j < pp.K; ++j)
+      for (int d = 0; d < (1 << pp.K); ++d)
+        if (!((d >> (pp.K - 1 - j)) & 1)) z[pp.level + uint32_t(j)] += digits[16 * pi + size_t(d)];
+    ++pi;
+  }
+  return z;
 }
 
 // The same with T keys per tile in every pass.

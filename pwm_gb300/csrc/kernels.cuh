@@ -125,6 +125,23 @@ void launch_split_pass_batched(uint32_t key_bytes, int K, const SplitArgs* args,
 // Keys of one tile for a key width.
 uint32_t tile_pass_elems(uint32_t key_bytes);
 // One pass of K levels over a.tiles tiles; `out`: the pass writes S_{l+K}.
+// Digit counts of the passes of a matrix-only build (pass_digits_kernel):
+// pass p covers levels level[p]..level[p]+K[p]-1, its natural digit is
+// (symbol >> lo[p]) & mask[p].
+constexpr uint32_t kPassDigitsMaxPasses = 24;
+struct PassDigitsArgs {
+  uint32_t npasses, L;
+  uint32_t level[kPassDigitsMaxPasses], K[kPassDigitsMaxPasses], lo[kPassDigitsMaxPasses],
+      mask[kPassDigitsMaxPasses];
+};
+// digits: npasses * 16 zeroed counters; done: a zeroed counter; out (device
+// view of mapped host memory): flat prefix counts of levels 0..K[0]
+// (2^(K[0]+1) - 1 words), the zeros of every level (L words), the status
+// word, the digit counts (npasses * 16).
+void launch_pass_digits(const void* text, uint64_t n, uint32_t width, const PassDigitsArgs& pd,
+                        unsigned long long* digits, unsigned int* done, uint32_t* status, uint64_t* out,
+                        cudaStream_t s, uint64_t* launches);
+
 // The narrowest key width (1, 2 or 4 bytes) holding `bits` bits.
 uint32_t tile_key_bytes(uint32_t bits);
 // One tile pass over keys of key_bytes; a pass writing S_{l+K} (out) writes

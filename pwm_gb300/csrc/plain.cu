@@ -252,8 +252,6 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   if (io && io->text && !pinned_in) host_to_device(ctx, const_cast<void*>(d_text), io->text, n * wx->width, s);
   CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, 4, s));
   const uint64_t bins = uint64_t(1) << L;
-  auto* d_hist = static_cast<unsigned long long*>(ctx->grow("hist", bins * 8));
-  CUDA_TRY(cudaMemsetAsync(d_hist, 0, bins * 8, s));
   // Tile engine: level 0 is written in whole words (by the histogram kernel,
   // or by the first pass, whose tiles start at multiples of 64 bits); the
   // first pass's other levels are zeroed by the histogram kernel (levels <= 8)
@@ -273,6 +271,14 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   const int Kz = std::min<int>(kmax, int(L));
   const uint32_t D0 = uint32_t(Kz < int(L) ? Kz : Kz - 1);  // splits of the first pass
   const bool tile_hist = tile_engine && L <= 8 && D0 >= 1;
+  const bool want_tree = wx->wt.present;
+  // Matrix-only, more than 8 levels, no host streaming: the passes need only
+  // the counts of their own digits, not a leaf histogram of 2^L bins
+  // (plan_matrix_passes).
+  const bool digit_plan = tile_engine && !want_tree && L > 8 && !wx->keep_hist && !stream_out;
+  const auto digit_shape = digit_plan ? plan_passes(L, kmax) : std::vector<PassPlan>{};
+  auto* d_hist = digit_plan ? nullptr : static_cast<unsigned long long*>(ctx->grow("hist", bins * 8));
+  if (!digit_plan) CUDA_TRY(cudaMemsetAsync(d_hist, 0, bins * 8, s));
   if (tile_engine && !tile_hist && Kz > 1)
     for (Structure* st : {&wx->wm, &wx->wt})
       if (st->present)
@@ -287,13 +293,16 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   // (level m at 2^m - 1; level L is the leaf histogram), the zero bits of
   // every level and the status word; and (pinned) the block prefix rows at
   // the bounds of a chunked first pass
+  // (with digit_plan: the prefix counts of levels 0..Kz only, then the
+  // zero bits, the status word and every pass's digit counts)
   const uint64_t NB0 = uint64_t(1) << D0;
-  const uint64_t flat_words = (bins << 1) - 1;
-  uint64_t* h_flat = ctx->grow_mapped((flat_words + L + 1) * 8);
+  const uint64_t flat_words = digit_plan ? (uint64_t(2) << Kz) - 1 : (bins << 1) - 1;
+  uint64_t* h_flat = ctx->grow_mapped((flat_words + L + 1 + 16 * digit_shape.size()) * 8);
   uint64_t* d_flat_host = ctx->mapped_dev;
   uint64_t* h_hist = h_flat + bins - 1;
   const uint64_t* h_zeros = h_flat + flat_words;
   auto* h_status = reinterpret_cast<uint32_t*>(h_flat + flat_words + L);
+  const uint64_t* h_digits = h_flat + flat_words + L + 1;
   auto* d_level_zeros = static_cast<unsigned long long*>(ctx->grow("level_zeros", uint64_t(L) * 8));
   auto* h_rows = static_cast<uint64_t*>(
       ctx->grow_pinned(uint64_t(kMaxStreamChunks) * (uint64_t(1) << kTileGivenMaxLevels) * 8));
@@ -351,6 +360,23 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
       }
     }
     // (the block scan follows with the first pass's start table, below)
+  } else if (digit_plan) {
+    if (pinned_in) CUDA_TRY(cudaMemcpyAsync(const_cast<void*>(d_text), io->text, n * wx->width,
+                                            cudaMemcpyHostToDevice, s));
+    PassDigitsArgs pd{};
+    pd.npasses = uint32_t(digit_shape.size());
+    pd.L = L;
+    for (uint32_t p = 0; p < pd.npasses; ++p) {
+      pd.level[p] = digit_shape[p].level;
+      pd.K[p] = uint32_t(digit_shape[p].K);
+      pd.lo[p] = L - digit_shape[p].level - pd.K[p];
+      pd.mask[p] = (1u << pd.K[p]) - 1u;
+    }
+    auto* d_digits = static_cast<unsigned long long*>(ctx->grow("pass_digits", (16 * kPassDigitsMaxPasses + 2) * 8));
+    CUDA_TRY(cudaMemsetAsync(d_digits, 0, (16 * pd.npasses + 2) * 8, s));
+    ProfScope ps(ctx, "leaf_histogram", n * wx->width);
+    launch_pass_digits(d_text, n, wx->width, pd, d_digits, reinterpret_cast<unsigned int*>(d_digits + 16 * pd.npasses),
+                       ctx->d_status, d_flat_host, s, &ctx->launches);
   } else {
     if (pinned_in) CUDA_TRY(cudaMemcpyAsync(const_cast<void*>(d_text), io->text, n * wx->width,
                                             cudaMemcpyHostToDevice, s));
@@ -358,12 +384,13 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     launch_leaf_histogram(d_text, n, wx->width, L, d_hist, ctx->d_status, s, &ctx->launches);
   }
   CUDA_TRY(cudaGetLastError());
-  // prefix counts, zero bits and the status word to the host
-  CUDA_TRY(cudaMemsetAsync(d_level_zeros, 0, uint64_t(L) * 8, s));
-  launch_fold_levels(d_hist, L, d_flat_host, d_level_zeros, s, &ctx->launches);
-  launch_readback(d_level_zeros, L, ctx->d_status, d_flat_host + flat_words, s, &ctx->launches);
+  if (!digit_plan) {
+    // prefix counts, zero bits and the status word to the host
+    CUDA_TRY(cudaMemsetAsync(d_level_zeros, 0, uint64_t(L) * 8, s));
+    launch_fold_levels(d_hist, L, d_flat_host, d_level_zeros, s, &ctx->launches);
+    launch_readback(d_level_zeros, L, ctx->d_status, d_flat_host + flat_words, s, &ctx->launches);
+  }
   CUDA_TRY(cudaEventRecord(ctx->hist_event(), s));
-  const bool want_tree = wx->wt.present;
   // After the tile histogram the first pass needs nothing from the host but
   // its start table, which a one-CTA kernel derives from the histogram: the
   // pass runs while the host reads the histogram and plans the other passes
@@ -462,11 +489,17 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   std::vector<TilePassHost> tile_passes;
   std::vector<uint32_t> regroup;
   PrefixCounts cnt;  // natural-prefix counts per level
-  if (tile_engine) {
+  const uint32_t w = wx->width;
+  auto tile_keys = [&](uint32_t l) { return tile_pass_elems(tile_pass_key_bytes(w, L, l)); };
+  if (digit_plan) {
+    tile_passes = plan_matrix_passes(h_digits, n, L, kmax, tile_keys);
+    tabs.level_bits.assign(L, n);
+    tabs.zeros.assign(h_zeros, h_zeros + L);
+    tabs.seg_tree.resize(L);
+    tabs.seg_matrix.resize(L);
+  } else if (tile_engine) {
     cnt = PrefixCounts::view(h_flat, L);
-    const uint32_t w = wx->width;
-    tile_passes = plan_tile_passes(
-        cnt, L, kmax, [&](uint32_t l) { return tile_pass_elems(tile_pass_key_bytes(w, L, l)); }, want_tree, &regroup);
+    tile_passes = plan_tile_passes(cnt, L, kmax, tile_keys, want_tree, &regroup);
     tabs = build_tables_tile(cnt, L, want_tree ? regroup : std::vector<uint32_t>{}, h_zeros);
   } else {
     plan = plan_passes(L, ctx->pass_levels);

@@ -201,11 +201,9 @@ __global__ void __launch_bounds__(256, 4) tile_batch_kernel(TileBatchQueue q) {
   __shared__ uint32_t s_base[kTileBatchMaxGroups + 1];
   __shared__ uint32_t s_item, s_gi;
   __shared__ __align__(16) TileArgs s_args;
-  // Thread 0 claims the next item as soon as it starts one, so the claim's
-  // round trip overlaps the tile.  (The earliest unfinished item is always
-  // running or about to run: a CTA's claimed item follows its current one in
-  // queue order, so the queue still drains.)
-  uint32_t next = 0;
+  // (Claiming the next item while the current one runs was slower: a tile
+  // waiting for a text's previous pass then also waits for items that other
+  // CTAs hold unstarted.)
   if (threadIdx.x == 0) {
     uint32_t run = 0;
     for (uint32_t k = 0; k < q.ngroups; ++k) {
@@ -213,18 +211,16 @@ __global__ void __launch_bounds__(256, 4) tile_batch_kernel(TileBatchQueue q) {
       run += q.group_tiles[k];
     }
     s_base[q.ngroups] = run;
-    next = atomicAdd(q.head, 1u);
   }
   uint32_t have = ~0u;  // the group whose arguments s_args holds
   for (;;) {
     __syncthreads();  // s_base is set; the previous item is done with shared memory
     if (threadIdx.x == 0) {
-      const uint32_t item = next;
+      const uint32_t item = atomicAdd(q.head, 1u);
       uint32_t k = 0;
       while (k < q.ngroups && item >= s_base[k + 1]) ++k;
       s_item = item;
       s_gi = k;
-      if (k < q.ngroups) next = atomicAdd(q.head, 1u);
     }
     __syncthreads();
     const uint32_t k = s_gi;

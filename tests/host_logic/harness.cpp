@@ -116,6 +116,46 @@ static int plan(uint32_t L, bool tree, int kmax, uint32_t T) {
   return 0;
 }
 
+// Matrix-only plans two ways from one leaf histogram: from the folded
+// prefix counts of every level (plan_tile_passes) and from the digit counts
+// of each pass alone (plan_matrix_passes, what the device counts for deep
+// matrix-only builds); both plans and the zero counts must agree.
+static int digits(uint32_t L, int kmax, uint32_t T) {
+  std::vector<uint64_t> hist(size_t(1) << L);
+  for (auto& h : hist) {
+    unsigned long long v = 0;
+    if (scanf("%llu", &v) != 1) return 2;
+    h = v;
+  }
+  const PrefixCounts cnt = fold_prefix_counts(hist.data(), L);
+  std::vector<uint32_t> regroup;
+  const auto a = plan_tile_passes(cnt, L, kmax, T, false, &regroup);
+  const auto shape = plan_passes(L, kmax);
+  std::vector<uint64_t> dg(16 * shape.size(), 0);
+  for (size_t p = 0; p < shape.size(); ++p)
+    for (uint64_t x = 0; x < hist.size(); ++x)
+      dg[16 * p + ((x >> (L - shape[p].level - uint32_t(shape[p].K))) & ((1u << shape[p].K) - 1))] += hist[x];
+  const auto b = plan_matrix_passes(dg.data(), cnt[0][0], L, kmax, [T](uint32_t) { return T; });
+  if (a.size() != b.size() || !regroup.empty()) { printf("pass count\n"); return 1; }
+  for (size_t p = 0; p < a.size(); ++p) {
+    if (a[p].level != b[p].level || a[p].K != b[p].K || a[p].out != b[p].out || a[p].tiles != b[p].tiles ||
+        a[p].table != b[p].table || a[p].segs.size() != b[p].segs.size() || a[p].segmented || b[p].segmented) {
+      printf("pass %zu differs\n", p);
+      return 1;
+    }
+    for (size_t i = 0; i < a[p].segs.size(); ++i)
+      if (a[p].segs[i].in_begin != b[p].segs[i].in_begin || a[p].segs[i].m != b[p].segs[i].m ||
+          a[p].segs[i].table != b[p].segs[i].table || a[p].segs[i].tile0 != b[p].segs[i].tile0) {
+        printf("pass %zu segment %zu differs\n", p, i);
+        return 1;
+      }
+  }
+  const LevelTables t = build_tables_tile(cnt, L, {});
+  if (t.zeros != matrix_pass_zeros(dg.data(), L, kmax)) { printf("zeros differ\n"); return 1; }
+  printf("ok %zu\n", a.size());
+  return 0;
+}
+
 static int merge(uint32_t L, uint32_t shards, bool tree) {
   std::vector<PrefixCounts> cnt;
   std::vector<uint64_t> hist(size_t(1) << L);
@@ -164,6 +204,8 @@ static int copy(unsigned seed) {
 
 int main(int argc, char** argv) {
   if (argc >= 3 && !strcmp(argv[1], "copy")) return copy(unsigned(atoi(argv[2])));
+  if (argc >= 5 && !strcmp(argv[1], "digits"))
+    return digits(uint32_t(atoi(argv[2])), atoi(argv[3]), uint32_t(atoi(argv[4])));
   if (argc >= 5 && !strcmp(argv[1], "merge"))
     return merge(uint32_t(atoi(argv[2])), uint32_t(atoi(argv[3])), atoi(argv[4]) != 0);
   if (argc >= 6 && !strcmp(argv[1], "plan"))

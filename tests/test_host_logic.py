@@ -217,3 +217,20 @@ def test_merge_plan(harness, L, shards, tree):
 def test_staging_copy_pool(harness):
     r = subprocess.run([harness, "copy", "7"], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr
+
+
+@pytest.mark.parametrize("L,kmax,T,scale", [(9, 4, 4096, 50), (12, 4, 8192, 7), (16, 4, 16384, 3), (20, 4, 4096, 2),
+                                           (13, 3, 4096, 9), (10, 1, 16384, 30), (11, 2, 4096, 0)])
+def test_matrix_plan_from_digit_counts(harness, L, kmax, T, scale):
+    """Deep matrix-only builds plan from the digit counts of each pass (what
+    the device counts instead of a leaf histogram): same passes, tables and
+    zero counts as the plan from every level's prefix counts."""
+    rng = np.random.default_rng(L * 13 + kmax)
+    hist = rng.integers(0, scale + 1, 1 << L).astype(np.int64)
+    hist[rng.random(1 << L) < 0.3] = 0
+    if hist.sum() == 0:
+        hist[rng.integers(0, 1 << L)] = 5
+    inp = "".join("%d\n" % int(h) for h in hist)
+    r = subprocess.run([harness, "digits", str(L), str(kmax), str(T)], input=inp, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0 and r.stdout.startswith("ok"), r.stdout + r.stderr
