@@ -171,7 +171,7 @@ def cpu_baseline(n):
                       "leg); one warm-up and one timed step per leg"}
 
 
-def batched_vs_per_text(torch, pg, ctx, count=4096, seed=1, reps=5):
+def batched_vs_per_text(torch, pg, ctx, count=4096, seed=1, reps=5, per_text=True):
     """The batched workload: 4096 uint8 texts (log-normal lengths, 85%
     DNA-like with 3 levels, 15% Zipf bytes with 8 levels), matrix + tree of
     every text.  Batched: one CUDA graph per build whose persistent kernel
@@ -201,6 +201,10 @@ def batched_vs_per_text(torch, pg, ctx, count=4096, seed=1, reps=5):
     b.check()
     batched_ms = e0.elapsed_time(e1) / reps
     vpt = [b.tile_vectors(i) for i in range(count)]
+    if not per_text:  # (profiling runs: the batched builds only)
+        b.free()
+        return {"texts": count, "symbols": total, "batched_ms": batched_ms,
+                "batched_gbs": total / (batched_ms / 1e3) / 1e9}
     # per-text: a batch of one text each (graphs recorded up front, untimed)
     base = d.data_ptr()
     per = []
@@ -245,7 +249,7 @@ def batched_vs_per_text(torch, pg, ctx, count=4096, seed=1, reps=5):
             "identical_to_per_text": bool(same), "structures": ["matrix", "tree"]}
 
 
-def other_workloads(torch, pg, ctx, reps=3):
+def other_workloads(torch, pg, ctx, reps=3, only=None):
     """Build times of the other configured workloads (resident text, CUDA
     events on the library's stream; the drop-in Huffman builds host to host):
     2^26 DNA-like bytes with 2 levels (matrix + tree), 2^30 bytes uniform
@@ -259,6 +263,8 @@ def other_workloads(torch, pg, ctx, reps=3):
     stream = torch.cuda.current_stream()
 
     def timed(name, n, width, levels, dist, param, tree, rs, shards=0):
+        if only is not None and name not in only:
+            return None
         dtype = {1: torch.uint8, 2: torch.int16, 4: torch.int32}[width]
         t = torch.empty(n, dtype=dtype, device="cuda")
         pg.generate(dist, 3, n, width, param=param, device_ptr=t.data_ptr(), context=ctx)
@@ -295,6 +301,8 @@ def other_workloads(torch, pg, ctx, reps=3):
     timed("zipf_2p30_levels8_16_shards", 1 << 30, 1, 8, pg.GEN_ZIPF256, 0, True, False, shards=16)
     t16 = timed("mix16_2p28_levels16", 1 << 28, 2, 16, pg.GEN_MIX16, 0, True, False)
     timed("uniform20_2p26_levels20", 1 << 26, 4, 20, pg.GEN_UNIFORM, 1 << 20, False, True)
+    if only is not None:  # (profiling runs: the named builds only)
+        return out
     # pwm's reduce_alphabet on the device (the 2^28 16-bit text; histogram,
     # first occurrences, host ranking of the symbols, remap): wall time
     out16 = torch.empty_like(t16)
@@ -591,6 +599,10 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--engine", default="tile", choices=["tile", "warp"])
     ap.add_argument("--no-other", action="store_true")
+    # profiling runs: the batched builds without the per-text baseline, and
+    # only the named other workloads (comma-separated)
+    ap.add_argument("--no-per-text", action="store_true")
+    ap.add_argument("--other-only", default=None)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -722,11 +734,12 @@ def main():
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(n)
         if world == 1 and not args.no_batch:
-            line["batched"] = batched_vs_per_text(torch, pg, ctx)
+            line["batched"] = batched_vs_per_text(torch, pg, ctx, per_text=not args.no_per_text)
         if world == 1 and not args.no_serve:
             line["serving"] = serving_bench(pg)
         if world == 1 and not args.no_other:
-            line["other_workloads"] = other_workloads(torch, pg, ctx)
+            line["other_workloads"] = other_workloads(
+                torch, pg, ctx, only=args.other_only.split(",") if args.other_only else None)
         print(json.dumps(line))
     ds.free()
     if dist:

@@ -34,28 +34,41 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hist_kernel(const T* __re
   const uint32_t mine = threadIdx.x % copies;
   for (uint32_t i = threadIdx.x; i < bins * copies; i += kBatchThreads) h[i] = 0;
   __syncthreads();
-  bool bad = false;
-  auto count = [&](uint32_t s) {
-    if (s >= bins) bad = true;
-    else atomicAdd(&h[s * copies + mine], 1u);
-  };
+  // Branch-free: every symbol counts into bin (symbol mod 2^L), and `seen`
+  // collects the bits of all of them (of whole words: 2^L - 1 per symbol
+  // lane of a word is the allowed part), so one test at the end finds a
+  // symbol >= 2^L (the counts are then not used).
+  uint32_t seen = 0;
+  const uint32_t bmask = bins - 1;
+  // the allowed bits of one symbol lane of a word (2^L - 1, at most the lane)
+  const uint32_t lmask = sizeof(T) == 4 ? bmask : min(bmask, (1u << (8 * sizeof(T))) - 1u);
+  auto count = [&](uint32_t s) { atomicAdd(&h[(s & bmask) * copies + mine], 1u); };
   const T* p = texts + t.offset + c.start;
   const uint64_t head = min(c.len, uint64_t((16u - (reinterpret_cast<uintptr_t>(p) & 15u)) & 15u) / sizeof(T));
   const uint64_t nv = (c.len - head) / E;
-  if (threadIdx.x < head) count(uint32_t(p[threadIdx.x]));
+  if (threadIdx.x < head) {
+    seen |= uint32_t(p[threadIdx.x]);
+    count(uint32_t(p[threadIdx.x]));
+  }
   const uint4* v = reinterpret_cast<const uint4*>(p + head);
-  for (uint64_t k = threadIdx.x; k < nv; k += kBatchThreads) {
+  uint32_t seen_w = 0;  // the OR of whole vector words
+  for (uint32_t k = threadIdx.x; k < nv; k += kBatchThreads) {
     const uint4 x = __ldcs(v + k);
     const uint32_t w[4] = {x.x, x.y, x.z, x.w};
+    seen_w |= x.x | x.y | x.z | x.w;
 #pragma unroll
     for (uint32_t e = 0; e < E; ++e) {
-      if constexpr (sizeof(T) == 1) count((w[e >> 2] >> (8 * (e & 3))) & 0xFFu);
-      else if constexpr (sizeof(T) == 2) count((w[e >> 1] >> (16 * (e & 1))) & 0xFFFFu);
+      if constexpr (sizeof(T) == 1) count((w[e >> 2] >> (8 * (e & 3))) & lmask);
+      else if constexpr (sizeof(T) == 2) count((w[e >> 1] >> (16 * (e & 1))) & lmask);
       else count(w[e]);
     }
   }
-  for (uint64_t i = head + nv * E + threadIdx.x; i < c.len; i += kBatchThreads) count(uint32_t(p[i]));
-  if (bad) atomicOr(status, kErrSymbol);
+  for (uint64_t i = head + nv * E + threadIdx.x; i < c.len; i += kBatchThreads) {
+    seen |= uint32_t(p[i]);
+    count(uint32_t(p[i]));
+  }
+  const uint32_t lanes = sizeof(T) == 1 ? 0x01010101u : (sizeof(T) == 2 ? 0x00010001u : 1u);
+  if ((seen & ~bmask) || (seen_w & ~(lanes * lmask))) atomicOr(status, kErrSymbol);
   __syncthreads();
   unsigned long long* out = hist + t.hist_off;
   for (uint32_t s = threadIdx.x; s < bins; s += kBatchThreads) {

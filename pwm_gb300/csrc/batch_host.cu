@@ -16,6 +16,8 @@ namespace {
 
 constexpr uint32_t kBatchMaxLevels = 12;        // per-text tables live in shared memory
 constexpr uint64_t kBatchChunk = 65536;         // symbols per histogram CTA
+constexpr size_t kTuneMaxTexts = 4096;           // texts of a tuning sub-batch (at most)
+constexpr uint64_t kTuneSymbols = uint64_t(1) << 26;  // symbols of a tuning sub-batch (about)
 constexpr uint64_t kBatchRegroupWords = 1024;   // words per regroup CTA
 
 struct BatchPassGroup {
@@ -416,11 +418,15 @@ void tune_tile_sizes(pwmgpu_batch* b, const void* d_texts) {
   for (uint32_t t = 0; t < b->count; ++t) cls[tune_key(b->width, b->L[t], b->info[t].n)].push_back(t);
   for (const auto& kv : cls) {
     if (ctx->batch_tune.count(kv.first)) continue;
+    // The class's texts, repeated (the same input, separate outputs) until
+    // the sub-batch is about as large as a batch that fills the GPU many
+    // times over: timed alone, a sub-batch of a few waves of tiles favours
+    // small tiles through its tail, which a full batch does not have.
     std::vector<uint64_t> bg, ln;
     std::vector<uint32_t> lv;
     uint64_t sym = 0;
-    for (uint32_t t : kv.second) {
-      if (bg.size() >= 64 || (sym >= (uint64_t(1) << 24) && !bg.empty())) break;
+    for (size_t k = 0; bg.size() < kTuneMaxTexts && sym < kTuneSymbols; ++k) {
+      const uint32_t t = kv.second[k % kv.second.size()];
       bg.push_back(b->info[t].offset);
       ln.push_back(b->info[t].n);
       lv.push_back(b->L[t]);

@@ -53,69 +53,73 @@ __device__ unsigned long long scan_parts(unsigned long long* part) {
   return total;
 }
 
-// Exclusive prefix sums of a[0..len) into out[0..len), the total into
-// out[len] (len <= 2^kTileBatchMaxLevels), by one CTA; `fetch(i)` gives
-// element i.  Each thread sums a run of consecutive elements.
-template <typename F>
-__device__ void cta_exclusive_scan(uint64_t len, F fetch, uint64_t* out, unsigned long long* part) {
-  const uint32_t tid = threadIdx.x;
-  const uint64_t per = (len + kPlanThreads - 1) / kPlanThreads;
-  const uint64_t b = min(len, uint64_t(tid) * per), e = min(len, b + per);
-  unsigned long long sum = 0;
-  for (uint64_t i = b; i < e; ++i) sum += fetch(i);
-  part[tid] = sum;
-  const unsigned long long total = scan_parts(part);
-  if (tid == 0) out[len] = total;
-  unsigned long long run = part[tid];
-  for (uint64_t i = b; i < e; ++i) {
-    const unsigned long long x = fetch(i);
-    out[i] = run;
-    run += x;
-  }
-  __syncthreads();
-}
-
 __device__ __forceinline__ uint32_t rev_bits(uint32_t v, uint32_t bits) {
   return bits == 0 ? 0u : (__brev(v) >> (32 - bits));
 }
 
-// Per text: the natural prefix counts of every level folded from its leaf
-// histogram, the matrix zero counts, and the exclusive prefixes of every
-// level in natural (tree) and key (matrix: bit-reversed prefix) order.
-__global__ void __launch_bounds__(kPlanThreads) tile_batch_fold_kernel(const TileBatchText* __restrict__ texts,
-                                                                       const unsigned long long* __restrict__ hist,
-                                                                       uint64_t* pfx, uint64_t* zeros) {
-  __shared__ unsigned long long part[kPlanThreads];
-  const TileBatchText t = texts[blockIdx.x];
+// Exclusive prefix sums of a[0..len) into out[0..len), the total into
+// out[len], by one warp: lane i sums a run of consecutive elements, one
+// shuffle scan of the run sums, then each lane writes its run.
+template <typename F>
+__device__ void warp_exclusive_scan_u64(uint64_t len, F fetch, uint64_t* out, uint32_t lane) {
+  const uint64_t per = (len + 31) / 32;
+  const uint64_t b = min(len, uint64_t(lane) * per), e = min(len, b + per);
+  unsigned long long sum = 0;
+  for (uint64_t i = b; i < e; ++i) sum += fetch(i);
+  unsigned long long x = sum;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+    if (int(lane) >= d) x += y;
+  }
+  unsigned long long run = x - sum;
+  for (uint64_t i = b; i < e; ++i) {
+    const unsigned long long v = fetch(i);
+    out[i] = run;
+    run += v;
+  }
+  if (lane == 31) out[len] = x;
+}
+
+// Per text, one warp (at most 2^12 leaves, 128 per lane): the natural
+// prefix counts of every level folded from its leaf histogram, the matrix
+// zero counts, and the exclusive prefixes of every level in natural (tree)
+// and key (matrix: bit-reversed prefix) order.  A CTA of 256 threads per
+// text spent its time in barriers: most texts have a few dozen leaves.
+__global__ void __launch_bounds__(256) tile_batch_fold_kernel(const TileBatchText* __restrict__ texts, uint32_t ntexts,
+                                                              const unsigned long long* __restrict__ hist, uint64_t* pfx,
+                                                              uint64_t* zeros) {
+  const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= ntexts) return;
+  const TileBatchText t = texts[w];
   const uint32_t L = t.levels;
   uint64_t* cnt = pfx + t.pfx_off;  // level m at 2^m - 1
   uint64_t* pn = cnt + tile_batch_counts(L);
   uint64_t* pk = pn + tile_batch_prefixes(L);
   const unsigned long long* h = hist + t.hist_off;
-  for (uint64_t p = threadIdx.x; p < (uint64_t(1) << L); p += kPlanThreads) cnt[(uint64_t(1) << L) - 1 + p] = h[p];
-  __syncthreads();
+  for (uint64_t p = lane; p < (uint64_t(1) << L); p += 32) cnt[(uint64_t(1) << L) - 1 + p] = h[p];
+  __syncwarp();
   for (int m = int(L) - 1; m >= 0; --m) {
     const uint64_t* up = cnt + (uint64_t(2) << m) - 1;
     uint64_t* o = cnt + (uint64_t(1) << m) - 1;
-    for (uint64_t p = threadIdx.x; p < (uint64_t(1) << m); p += kPlanThreads) o[p] = up[2 * p] + up[2 * p + 1];
-    __syncthreads();
+    for (uint64_t p = lane; p < (uint64_t(1) << m); p += 32) o[p] = up[2 * p] + up[2 * p + 1];
+    __syncwarp();
   }
   // zeros of level m: the symbols whose (m+1)-bit prefix is even
   for (uint32_t m = 0; m < L; ++m) {
     const uint64_t* c = cnt + (uint64_t(2) << m) - 1;
     unsigned long long z = 0;
-    for (uint64_t p = 2 * threadIdx.x; p < (uint64_t(2) << m); p += 2 * kPlanThreads) z += c[p];
-    part[threadIdx.x] = z;
-    const unsigned long long total = scan_parts(part);
-    if (threadIdx.x == 0) zeros[t.zeros_off + m] = total;
-    __syncthreads();
+    for (uint64_t p = 2 * lane; p < (uint64_t(2) << m); p += 64) z += c[p];
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) z += __shfl_xor_sync(0xFFFFFFFFu, z, d);
+    if (lane == 0) zeros[t.zeros_off + m] = z;
   }
   for (uint32_t m = 0; m <= L; ++m) {
     const uint64_t* c = cnt + (uint64_t(1) << m) - 1;
     const uint64_t len = uint64_t(1) << m;
-    cta_exclusive_scan(len, [&](uint64_t i) { return c[i]; }, pn + tile_batch_level_at(m), part);
-    cta_exclusive_scan(len, [&](uint64_t i) { return c[rev_bits(uint32_t(i), m)]; }, pk + tile_batch_level_at(m),
-                       part);
+    warp_exclusive_scan_u64(len, [&](uint64_t i) { return c[i]; }, pn + tile_batch_level_at(m), lane);
+    warp_exclusive_scan_u64(len, [&](uint64_t i) { return c[rev_bits(uint32_t(i), m)]; }, pk + tile_batch_level_at(m),
+                            lane);
   }
 }
 
@@ -276,7 +280,7 @@ void launch_tile_batch_plan(const TileBatchText* texts, uint32_t ntexts, const T
                             const unsigned long long* hist, uint64_t* pfx, uint64_t* zeros, uint32_t key_bytes,
                             unsigned* need, unsigned* group_tiles, cudaStream_t s, uint64_t* launches) {
   if (ntexts == 0) return;
-  tile_batch_fold_kernel<<<ntexts, kPlanThreads, 0, s>>>(texts, hist, pfx, zeros);
+  tile_batch_fold_kernel<<<(ntexts + 7) / 8, 256, 0, s>>>(texts, ntexts, hist, pfx, zeros);
   tile_batch_segments_kernel<<<npasses, kPlanThreads, 0, s>>>(texts, passes, groups, pfx, key_bytes, need);
   tile_batch_scan_kernel<<<ngroups, 1024, 0, s>>>(groups, group_tiles);
   *launches += 3;
