@@ -19,20 +19,31 @@ __device__ __forceinline__ uint32_t rev_bits_dev(uint32_t v, uint32_t bits) {
 // per thread; bin s of copy c at s * copies + c, so the lanes of a warp hit
 // different banks), which spreads the atomics of texts with few levels over
 // the copies instead of piling them on a handful of words.  The chunk is
-// read in 16-byte vectors between its unaligned ends.
+// read in 16-byte vectors between its unaligned ends.  A chunk of a tile
+// batch also counts, per first-pass tile, the tile's finest runs (the
+// D-bit digit of the top symbol bits, counter = the digit bit-reversed), a
+// column per lane, for the pass's given prefixes.
+constexpr uint32_t kHistTileCounters = 16 * 16 * 32;  // tiles x counters x lanes
 template <typename T>
 __global__ void __launch_bounds__(kBatchThreads) batch_hist_kernel(const T* __restrict__ texts,
                                                                    const BatchChunk* __restrict__ chunks,
                                                                    const BatchText* __restrict__ info,
-                                                                   unsigned long long* hist, uint32_t* status) {
+                                                                   unsigned long long* hist, uint32_t* tilecnt,
+                                                                   uint32_t* relpre, unsigned long long* blocksum,
+                                                                   uint32_t* status) {
   constexpr uint32_t E = 16 / sizeof(T);  // symbols per vector
-  __shared__ uint32_t h[4096];
+  extern __shared__ uint32_t hsm[];
+  uint32_t* h = hsm;               // [4096]
+  uint32_t* tc = hsm + 4096;       // [16 tiles][16 counters][32 lanes]
   const BatchChunk c = chunks[blockIdx.x];
   const BatchText t = info[c.text];
   const uint32_t bins = 1u << t.levels;
   const uint32_t copies = min(uint32_t(kBatchThreads), 4096u >> t.levels);
-  const uint32_t mine = threadIdx.x % copies;
+  const uint32_t mine = threadIdx.x % copies, lane = threadIdx.x & 31;
+  const uint32_t D = c.D, dsh = t.levels - c.D;  // the digit: symbol bits [L-D, L)
+  const uint32_t ntiles = D ? uint32_t((c.len + (uint64_t(1) << c.log2T) - 1) >> c.log2T) : 0u;
   for (uint32_t i = threadIdx.x; i < bins * copies; i += kBatchThreads) h[i] = 0;
+  for (uint32_t i = threadIdx.x; i < ntiles * 16 * 32; i += kBatchThreads) tc[i] = 0;
   __syncthreads();
   // Branch-free: every symbol counts into bin (symbol mod 2^L), and `seen`
   // collects the bits of all of them (of whole words: 2^L - 1 per symbol
@@ -42,13 +53,20 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hist_kernel(const T* __re
   const uint32_t bmask = bins - 1;
   // the allowed bits of one symbol lane of a word (2^L - 1, at most the lane)
   const uint32_t lmask = sizeof(T) == 4 ? bmask : min(bmask, (1u << (8 * sizeof(T))) - 1u);
-  auto count = [&](uint32_t s) { atomicAdd(&h[(s & bmask) * copies + mine], 1u); };
+  const uint32_t tcb = uint32_t(__cvta_generic_to_shared(tc)) + lane * 4;
+  auto count = [&](uint32_t s, uint32_t i) {  // symbol s at chunk position i
+    atomicAdd(&h[(s & bmask) * copies + mine], 1u);
+    if (D) {
+      const uint32_t cn = __brev((s >> dsh) & ((1u << D) - 1u)) >> (32 - D);
+      asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(tcb + (((i >> c.log2T) * 16 + cn) << 7)) : "memory");
+    }
+  };
   const T* p = texts + t.offset + c.start;
   const uint64_t head = min(c.len, uint64_t((16u - (reinterpret_cast<uintptr_t>(p) & 15u)) & 15u) / sizeof(T));
   const uint64_t nv = (c.len - head) / E;
   if (threadIdx.x < head) {
     seen |= uint32_t(p[threadIdx.x]);
-    count(uint32_t(p[threadIdx.x]));
+    count(uint32_t(p[threadIdx.x]), threadIdx.x);
   }
   const uint4* v = reinterpret_cast<const uint4*>(p + head);
   uint32_t seen_w = 0;  // the OR of whole vector words
@@ -56,16 +74,17 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hist_kernel(const T* __re
     const uint4 x = __ldcs(v + k);
     const uint32_t w[4] = {x.x, x.y, x.z, x.w};
     seen_w |= x.x | x.y | x.z | x.w;
+    const uint32_t i0 = uint32_t(head) + k * E;
 #pragma unroll
     for (uint32_t e = 0; e < E; ++e) {
-      if constexpr (sizeof(T) == 1) count((w[e >> 2] >> (8 * (e & 3))) & lmask);
-      else if constexpr (sizeof(T) == 2) count((w[e >> 1] >> (16 * (e & 1))) & lmask);
-      else count(w[e]);
+      if constexpr (sizeof(T) == 1) count((w[e >> 2] >> (8 * (e & 3))) & lmask, i0 + e);
+      else if constexpr (sizeof(T) == 2) count((w[e >> 1] >> (16 * (e & 1))) & lmask, i0 + e);
+      else count(w[e], i0 + e);
     }
   }
   for (uint64_t i = head + nv * E + threadIdx.x; i < c.len; i += kBatchThreads) {
     seen |= uint32_t(p[i]);
-    count(uint32_t(p[i]));
+    count(uint32_t(p[i]), uint32_t(i));
   }
   const uint32_t lanes = sizeof(T) == 1 ? 0x01010101u : (sizeof(T) == 2 ? 0x00010001u : 1u);
   if ((seen & ~bmask) || (seen_w & ~(lanes * lmask))) atomicOr(status, kErrSymbol);
@@ -75,6 +94,27 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hist_kernel(const T* __re
     uint32_t sum = 0;
     for (uint32_t k = 0; k < copies; ++k) sum += h[s * copies + k];
     if (sum) atomicAdd(&out[s], (unsigned long long)sum);
+  }
+  // per tile and counter the lanes' sum (into lane column 0), then per
+  // counter the block's exclusive prefixes over its tiles and its total
+  const uint32_t nb = 1u << D;
+  for (uint32_t e = threadIdx.x; e < ntiles * nb; e += kBatchThreads) {
+    const uint32_t tile = e >> D, cn = e & (nb - 1);
+    uint32_t sum = 0;
+    for (uint32_t l = 0; l < 32; ++l) sum += tc[(tile * 16 + cn) * 32 + ((l + e) & 31)];
+    tilecnt[c.cnt_off + e] = sum;
+    tc[(tile * 16 + cn) * 32 + ((e + 1) & 31)] = sum;  // a lane this thread read last: no other thread reads it
+  }
+  __syncthreads();
+  if (threadIdx.x < nb && D) {
+    const uint32_t cn = threadIdx.x;
+    uint32_t run = 0;
+    for (uint32_t tile = 0; tile < ntiles; ++tile) {
+      const uint32_t e = tile * nb + cn;
+      relpre[c.cnt_off + e] = run;
+      run += tc[(tile * 16 + cn) * 32 + ((e + 1) & 31)];
+    }
+    blocksum[c.blk_off + cn] = run;
   }
 }
 
@@ -189,16 +229,27 @@ __global__ void __launch_bounds__(kBatchThreads) batch_regroup_kernel(const Batc
 
 }  // namespace
 
+template <typename T>
+void launch_hist_w(const void* texts, const BatchChunk* chunks, uint32_t nchunks, const BatchText* info,
+                   unsigned long long* hist, uint32_t* tilecnt, uint32_t* relpre, unsigned long long* blocksum,
+                   uint32_t* status, cudaStream_t s) {
+  constexpr size_t smem = (4096 + kHistTileCounters) * 4;
+  static bool configured = false;  // attribute set once per width
+  if (!configured) {
+    cudaFuncSetAttribute(batch_hist_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    configured = true;
+  }
+  batch_hist_kernel<T><<<nchunks, kBatchThreads, smem, s>>>(static_cast<const T*>(texts), chunks, info, hist, tilecnt,
+                                                            relpre, blocksum, status);
+}
+
 void launch_batch_hist(const void* texts, uint32_t width, const BatchChunk* chunks, uint32_t nchunks,
-                       const BatchText* info, unsigned long long* hist, uint32_t* status, cudaStream_t s,
-                       uint64_t* launches) {
+                       const BatchText* info, unsigned long long* hist, uint32_t* tilecnt, uint32_t* relpre,
+                       unsigned long long* blocksum, uint32_t* status, cudaStream_t s, uint64_t* launches) {
   if (nchunks == 0) return;
-  if (width == 1)
-    batch_hist_kernel<<<nchunks, kBatchThreads, 0, s>>>(static_cast<const uint8_t*>(texts), chunks, info, hist, status);
-  else if (width == 2)
-    batch_hist_kernel<<<nchunks, kBatchThreads, 0, s>>>(static_cast<const uint16_t*>(texts), chunks, info, hist, status);
-  else
-    batch_hist_kernel<<<nchunks, kBatchThreads, 0, s>>>(static_cast<const uint32_t*>(texts), chunks, info, hist, status);
+  if (width == 1) launch_hist_w<uint8_t>(texts, chunks, nchunks, info, hist, tilecnt, relpre, blocksum, status, s);
+  else if (width == 2) launch_hist_w<uint16_t>(texts, chunks, nchunks, info, hist, tilecnt, relpre, blocksum, status, s);
+  else launch_hist_w<uint32_t>(texts, chunks, nchunks, info, hist, tilecnt, relpre, blocksum, status, s);
   ++*launches;
 }
 

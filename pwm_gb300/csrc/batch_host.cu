@@ -18,6 +18,7 @@ constexpr uint32_t kBatchMaxLevels = 12;        // per-text tables live in share
 constexpr uint64_t kBatchChunk = 65536;         // symbols per histogram CTA
 constexpr size_t kTuneMaxTexts = 4096;           // texts of a tuning sub-batch (at most)
 constexpr uint64_t kTuneSymbols = uint64_t(1) << 26;  // symbols of a tuning sub-batch (about)
+constexpr uint32_t kGivenBlockTiles = 16;        // first-pass tiles per histogram block (a CTA's)
 constexpr uint64_t kBatchRegroupWords = 1024;   // words per regroup CTA
 
 struct BatchPassGroup {
@@ -65,6 +66,12 @@ struct pwmgpu_batch {
   TileBatchGroup* d_tb_groups = nullptr;
   uint64_t* d_pfx = nullptr;
   unsigned *d_done = nullptr, *d_need = nullptr, *d_group_tiles = nullptr, *d_head = nullptr;
+  // histogram chunks of whole first-pass tiles, and those tiles' finest-run
+  // counts and prefixes (the first pass's given prefixes)
+  std::vector<BatchChunk> tchunks;
+  BatchChunk* d_tchunks = nullptr;
+  uint32_t *d_tilecnt = nullptr, *d_relpre = nullptr;
+  unsigned long long *d_blocksum = nullptr, *d_blockpre = nullptr;
   std::vector<std::pair<void*, size_t>> lookback;  // per group
   const void* tile_text = nullptr;   // the text buffer the plan was made for
   cudaGraph_t graph = nullptr;
@@ -199,8 +206,8 @@ void batch_enqueue(pwmgpu_batch* b, const void* d_texts) {
   CUDA_TRY(cudaMemsetAsync(b->d_hist, 0, std::max<uint64_t>(b->hist_n, 1) * 8, s));
   CUDA_TRY(cudaMemsetAsync(b->d_wm, 0, std::max<uint64_t>(b->wm_words, 1) * 8, s));
   for (auto& g : b->groups) CUDA_TRY(cudaMemsetAsync(g.d_lookback, 0, g.lb_bytes, s));
-  launch_batch_hist(d_texts, b->width, b->d_chunks, uint32_t(b->chunks.size()), b->d_info, b->d_hist, ctx->d_status,
-                    s, &ctx->launches);
+  launch_batch_hist(d_texts, b->width, b->d_chunks, uint32_t(b->chunks.size()), b->d_info, b->d_hist, nullptr, nullptr,
+                    nullptr, ctx->d_status, s, &ctx->launches);
   launch_batch_tables(b->d_hist, b->d_info, b->count, b->maxL, b->kmax, b->d_zeros, b->d_starts, b->d_segs, s,
                       &ctx->launches);
   for (auto& g : b->groups) {
@@ -288,6 +295,16 @@ void tile_plan(pwmgpu_batch* b, const void* d_texts) {
   b->d_head = static_cast<unsigned*>(b->talloc(4));
   uint64_t tiles_all = 0;
   uint32_t gi = 0;
+  // first passes: each text's tiles get given prefixes (counted by the
+  // histogram kernel in chunks of whole tiles), at counter offsets of one
+  // array for all first-pass groups
+  uint64_t cnt_total = 0, blk_total = 0;
+  struct GivenGroup {
+    size_t arg;
+    uint64_t cnt_off, blk_off;
+  };
+  std::vector<GivenGroup> given_groups;
+  b->tchunks.clear();
   for (const auto& kv : by) {
     const auto& items = kv.second;
     const uint32_t K = items[0].K;
@@ -311,6 +328,10 @@ void tile_plan(pwmgpu_batch* b, const void* d_texts) {
     auto* d_tx = static_cast<TileText*>(b->talloc(items.size() * sizeof(TileText)));
     std::vector<TileText> tx(items.size());
     uint64_t seg_base = 0;
+    const uint32_t D = out ? K : K - 1;
+    const bool given = p == 0 && D >= 1;
+    const uint64_t group_cnt_off = cnt_total, group_blk_off = blk_total;
+    uint64_t group_tile = 0, group_blk = 0;  // tiles and blocks of the group's texts so far (device order)
     for (size_t i = 0; i < items.size(); ++i) {
       const Item& it = items[i];
       const uint32_t t = it.t;
@@ -335,9 +356,37 @@ void tile_plan(pwmgpu_batch* b, const void* d_texts) {
       P.table_base = seg_base * uint64_t(TS);
       passes.push_back(P);
       seg_base += uint64_t(1) << it.l;
+      if (given) {
+        // blocks of kGivenBlockTiles tiles, one histogram CTA each
+        const uint64_t TT = uint64_t(256) * b->vpt[t] * KPL, n = b->info[t].n, NB = uint64_t(1) << D;
+        const uint64_t nt = (n + TT - 1) / TT, nblk = (nt + kGivenBlockTiles - 1) / kGivenBlockTiles;
+        uint32_t log2T = 0;
+        while ((uint64_t(1) << log2T) < TT) ++log2T;
+        TileBatchText& x0 = texts[t];
+        x0.blk_off = group_blk_off + group_blk * NB;
+        x0.nblk0 = uint32_t(nblk);
+        x0.nb0 = uint32_t(NB);
+        tx[i].blk0 = uint32_t(group_blk);
+        for (uint64_t k = 0; k < nblk; ++k) {
+          BatchChunk ch{};
+          ch.text = t;
+          ch.start = k * kGivenBlockTiles * TT;
+          ch.len = std::min<uint64_t>(kGivenBlockTiles * TT, n - ch.start);
+          ch.cnt_off = group_cnt_off + (group_tile + k * kGivenBlockTiles) * NB;
+          ch.blk_off = x0.blk_off + k * NB;
+          ch.D = D;
+          ch.log2T = log2T;
+          b->tchunks.push_back(ch);
+        }
+        group_tile += nt;
+        group_blk += nblk;
+      }
+    }
+    if (given) {
+      cnt_total += group_tile * (uint64_t(1) << D);
+      blk_total += group_blk * (uint64_t(1) << D);
     }
     CUDA_TRY(cudaMemcpy(d_tx, tx.data(), tx.size() * sizeof(TileText), cudaMemcpyHostToDevice));
-    const uint32_t D = out ? K : K - 1;
     const size_t lb_bytes = (uint64_t(1) << D) * tiles_ub * 8;
     void* lb = b->talloc(lb_bytes);
     b->lookback.push_back({lb, lb_bytes});
@@ -356,11 +405,40 @@ void tile_plan(pwmgpu_batch* b, const void* d_texts) {
     a.spin_limit = ctx->spin_limit;
     a.done = b->d_done;
     a.need = b->d_need;
+    if (given) {
+      a.tiles_per_block = kGivenBlockTiles;
+      a.text_blocks = 1;
+      given_groups.push_back({args.size(), group_cnt_off, group_blk_off});  // arrays set below
+    }
     args.push_back(a);
     groups.push_back(g);
     q.variant[gi] = kv.first.second;
     tiles_all += tiles_ub;
     ++gi;
+  }
+  // texts whose first pass takes no given prefixes (D = 0), and the rest of
+  // the histogram chunks: whole texts in chunks of kBatchChunk symbols
+  for (uint32_t t = 0; t < b->count; ++t)
+    if (texts[t].nb0 == 0)
+      for (uint64_t c0 = 0; c0 < b->info[t].n; c0 += kBatchChunk) {
+        BatchChunk ch{};
+        ch.text = t;
+        ch.start = c0;
+        ch.len = std::min<uint64_t>(kBatchChunk, b->info[t].n - c0);
+        b->tchunks.push_back(ch);
+      }
+  b->d_tchunks = static_cast<BatchChunk*>(b->talloc(std::max<size_t>(b->tchunks.size(), 1) * sizeof(BatchChunk)));
+  if (!b->tchunks.empty())
+    CUDA_TRY(cudaMemcpy(b->d_tchunks, b->tchunks.data(), b->tchunks.size() * sizeof(BatchChunk),
+                        cudaMemcpyHostToDevice));
+  b->d_tilecnt = static_cast<uint32_t*>(b->talloc(std::max<uint64_t>(cnt_total, 1) * 4));
+  b->d_relpre = static_cast<uint32_t*>(b->talloc(std::max<uint64_t>(cnt_total, 1) * 4));
+  b->d_blocksum = static_cast<unsigned long long*>(b->talloc(std::max<uint64_t>(blk_total, 1) * 8));
+  b->d_blockpre = static_cast<unsigned long long*>(b->talloc(std::max<uint64_t>(blk_total, 1) * 8));
+  for (const auto& gg : given_groups) {
+    args[gg.arg].tilecnt = b->d_tilecnt + gg.cnt_off;
+    args[gg.arg].relpre = b->d_relpre + gg.cnt_off;
+    args[gg.arg].blockpre = b->d_blockpre + gg.blk_off;
   }
   b->d_tb_texts = static_cast<TileBatchText*>(b->talloc(std::max<size_t>(texts.size(), 1) * sizeof(TileBatchText)));
   b->d_tb_passes = static_cast<TileBatchPass*>(b->talloc(std::max<size_t>(passes.size(), 1) * sizeof(TileBatchPass)));
@@ -396,10 +474,11 @@ void tile_enqueue(pwmgpu_batch* b, const void* d_texts) {
   for (const auto& lb : b->lookback) CUDA_TRY(cudaMemsetAsync(lb.first, 0, lb.second, s));
   CUDA_TRY(cudaMemsetAsync(b->d_done, 0, std::max<uint32_t>(b->ntextpasses, 1) * 4, s));
   CUDA_TRY(cudaMemsetAsync(b->d_head, 0, 4, s));
-  launch_batch_hist(d_texts, b->width, b->d_chunks, uint32_t(b->chunks.size()), b->d_info, b->d_hist, ctx->d_status,
-                    s, &ctx->launches);
+  launch_batch_hist(d_texts, b->width, b->d_tchunks, uint32_t(b->tchunks.size()), b->d_info, b->d_hist, b->d_tilecnt,
+                    b->d_relpre, b->d_blocksum, ctx->d_status, s, &ctx->launches);
   launch_tile_batch_plan(b->d_tb_texts, b->count, b->d_tb_passes, b->ntextpasses, b->d_tb_groups, b->ngroups, b->d_hist,
-                         b->d_pfx, b->d_zeros, b->width, b->d_need, b->d_group_tiles, s, &ctx->launches);
+                         b->d_pfx, b->d_zeros, b->width, b->d_need, b->d_group_tiles, b->d_blocksum, b->d_blockpre, s,
+                         &ctx->launches);
   launch_tile_batch(b->width, b->queue, b->tile_ctas, s, &ctx->launches);
   CUDA_TRY(cudaGetLastError());
 }

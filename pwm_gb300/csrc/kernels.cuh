@@ -238,6 +238,13 @@ struct BatchChunk {
   uint32_t pad;
   uint64_t start;  // symbol offset inside the text
   uint64_t len;
+  // Tile batches: the chunk is a block of whole first-pass tiles of 2^log2T
+  // symbols (at most 16), whose counts of the pass's finest runs (2^D
+  // counters per tile; D = 0: none) go to tilecnt[cnt_off + tile * 2^D +
+  // counter], their exclusive prefixes within the block to relpre (same
+  // place) and the block's totals to blocksum[blk_off + counter].
+  uint64_t cnt_off, blk_off;
+  uint32_t D, log2T;
 };
 struct BatchRegroup {
   const uint64_t* matrix;
@@ -249,8 +256,8 @@ struct BatchRegroup {
   uint64_t word_begin, word_end;
 };
 void launch_batch_hist(const void* texts, uint32_t width, const BatchChunk* chunks, uint32_t nchunks,
-                       const BatchText* info, unsigned long long* hist, uint32_t* status, cudaStream_t s,
-                       uint64_t* launches);
+                       const BatchText* info, unsigned long long* hist, uint32_t* tilecnt, uint32_t* relpre,
+                       unsigned long long* blocksum, uint32_t* status, cudaStream_t s, uint64_t* launches);
 void launch_batch_tables(const unsigned long long* hist, const BatchText* info, uint32_t ntexts, uint32_t max_levels,
                          int kmax, uint64_t* zeros, uint64_t* starts, uint64_t* segs, cudaStream_t s,
                          uint64_t* launches);

@@ -62,7 +62,7 @@ struct TileText {
   uint32_t vpt;         // 16-byte vectors per thread of this text's tiles (1, 2 or 4)
   uint32_t wait_idx;    // ~0u, or a counter in TileArgs::done this pass waits for ...
   uint32_t signal_idx;  // ~0u, or a counter each of its tiles adds one to when done
-  uint32_t pad;
+  uint32_t blk0;        // with TileArgs::text_blocks: the text's first block of given prefixes
 };
 
 struct TileArgs {
@@ -87,6 +87,10 @@ struct TileArgs {
   const uint32_t* relpre;
   const uint32_t* tilecnt;
   uint32_t tiles_per_block;
+  // 0: tile g's block is g / tiles_per_block; 1 (the first pass of a
+  // batch's texts, blocks restarting at every text): TileText::blk0 + the
+  // tile's index in its segment / tiles_per_block.
+  uint32_t text_blocks;
   uint32_t first_level_written;  // level l is already written (by the histogram kernel)
   uint32_t clear_edges;          // the levels were not zeroed: shared words are cleared before they are set
   // Optional: words [0, zero_words) at zero_a (and zero_b) are zeroed, tile g
@@ -556,8 +560,9 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
   const bool given = a.blockpre != nullptr;  // prefixes from the histogram kernel
   if (D >= 1 && given) {
     if (tid < NLB) {
+      const uint64_t blk = a.text_blocks ? uint64_t(s_tx.blk0) + tl / a.tiles_per_block : g / a.tiles_per_block;
       s_cnt[tid] = a.tilecnt[uint64_t(g) * NLB + tid];
-      pre[tid] = a.blockpre[uint64_t(g / a.tiles_per_block) * NLB + tid] + a.relpre[uint64_t(g) * NLB + tid];
+      pre[tid] = a.blockpre[blk * NLB + tid] + a.relpre[uint64_t(g) * NLB + tid];
     }
   } else if constexpr (D >= 1 && D <= kTileMaxLevels) {
     __shared__ uint32_t s_wcnt[WARPS][NLB];

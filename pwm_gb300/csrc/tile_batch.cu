@@ -88,7 +88,9 @@ __device__ void warp_exclusive_scan_u64(uint64_t len, F fetch, uint64_t* out, ui
 // text spent its time in barriers: most texts have a few dozen leaves.
 __global__ void __launch_bounds__(256) tile_batch_fold_kernel(const TileBatchText* __restrict__ texts, uint32_t ntexts,
                                                               const unsigned long long* __restrict__ hist, uint64_t* pfx,
-                                                              uint64_t* zeros) {
+                                                              uint64_t* zeros,
+                                                              const unsigned long long* __restrict__ blocksum,
+                                                              unsigned long long* blockpre) {
   const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (w >= ntexts) return;
   const TileBatchText t = texts[w];
@@ -120,6 +122,27 @@ __global__ void __launch_bounds__(256) tile_batch_fold_kernel(const TileBatchTex
     warp_exclusive_scan_u64(len, [&](uint64_t i) { return c[i]; }, pn + tile_batch_level_at(m), lane);
     warp_exclusive_scan_u64(len, [&](uint64_t i) { return c[rev_bits(uint32_t(i), m)]; }, pk + tile_batch_level_at(m),
                             lane);
+  }
+  // the first pass's block prefixes: per counter, exclusive sums over the
+  // text's blocks of tiles (lane i takes a run of consecutive blocks)
+  const uint32_t nb = t.nb0, nt = t.nblk0;
+  for (uint32_t cn = 0; cn < nb; ++cn) {
+    const uint32_t per = (nt + 31) / 32, b = min(nt, lane * per), e = min(nt, b + per);
+    unsigned long long sum = 0;
+    for (uint32_t i = b; i < e; ++i) sum += blocksum[t.blk_off + uint64_t(i) * nb + cn];
+    unsigned long long x = sum;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+      if (int(lane) >= d) x += y;
+    }
+    unsigned long long run = x - sum;
+    for (uint32_t i = b; i < e; ++i) {
+      const uint64_t at = t.blk_off + uint64_t(i) * nb + cn;
+      const unsigned long long v = blocksum[at];
+      blockpre[at] = run;
+      run += v;
+    }
   }
 }
 
@@ -278,9 +301,10 @@ int batch_kernel_occupancy() {
 void launch_tile_batch_plan(const TileBatchText* texts, uint32_t ntexts, const TileBatchPass* passes,
                             uint32_t npasses, const TileBatchGroup* groups, uint32_t ngroups,
                             const unsigned long long* hist, uint64_t* pfx, uint64_t* zeros, uint32_t key_bytes,
-                            unsigned* need, unsigned* group_tiles, cudaStream_t s, uint64_t* launches) {
+                            unsigned* need, unsigned* group_tiles, const unsigned long long* blocksum,
+                            unsigned long long* blockpre, cudaStream_t s, uint64_t* launches) {
   if (ntexts == 0) return;
-  tile_batch_fold_kernel<<<(ntexts + 7) / 8, 256, 0, s>>>(texts, ntexts, hist, pfx, zeros);
+  tile_batch_fold_kernel<<<(ntexts + 7) / 8, 256, 0, s>>>(texts, ntexts, hist, pfx, zeros, blocksum, blockpre);
   tile_batch_segments_kernel<<<npasses, kPlanThreads, 0, s>>>(texts, passes, groups, pfx, key_bytes, need);
   tile_batch_scan_kernel<<<ngroups, 1024, 0, s>>>(groups, group_tiles);
   *launches += 3;

@@ -35,6 +35,12 @@ struct TileBatchText {
   uint64_t hist_off;   // its 2^levels leaf counts in the batch's histogram array
   uint64_t pfx_off;    // its planning scratch (tile_batch_scratch words)
   uint64_t zeros_off;  // its matrix zero counts
+  // its first pass's given prefixes: the histogram kernel's totals of its
+  // nblk0 blocks of tiles at blocksum[blk_off + block * nb0 + counter],
+  // their exclusive prefixes to the same place in blockpre (nb0 = 0: the
+  // first pass counts and looks back)
+  uint64_t blk_off;
+  uint32_t nblk0, nb0;
 };
 
 struct TileBatchPass {  // one pass of one text
@@ -72,7 +78,8 @@ struct TileBatchQueue {
 void launch_tile_batch_plan(const TileBatchText* texts, uint32_t ntexts, const TileBatchPass* passes,
                             uint32_t npasses, const TileBatchGroup* groups, uint32_t ngroups,
                             const unsigned long long* hist, uint64_t* pfx, uint64_t* zeros, uint32_t key_bytes,
-                            unsigned* need, unsigned* group_tiles, cudaStream_t s, uint64_t* launches);
+                            unsigned* need, unsigned* group_tiles, const unsigned long long* blocksum,
+                            unsigned long long* blockpre, cudaStream_t s, uint64_t* launches);
 // The persistent kernel on `ctas` CTAs.
 void launch_tile_batch(uint32_t key_bytes, const TileBatchQueue& q, uint32_t ctas, cudaStream_t s,
                        uint64_t* launches);
