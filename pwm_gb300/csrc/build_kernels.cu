@@ -568,6 +568,9 @@ __global__ void symbol_hist_kernel(const T* text, uint64_t n, uint64_t nsym, uns
 // host memory, the natural prefix counts of levels 0..K0 (flat: level m at
 // 2^m - 1; the first pass's start table reads them), the zero bits of every
 // level, the status word and the digit counts.
+// NP: the passes' count bound, so that the per-symbol loop over the passes
+// unrolls (6 covers every text up to 24 levels in passes of 4).
+template <int NP>
 __global__ void __launch_bounds__(256) pass_digits_kernel(const unsigned char* __restrict__ text, uint64_t n,
                                                           uint32_t width, PassDigitsArgs pd,
                                                           unsigned long long* digits, unsigned int* done,
@@ -578,16 +581,22 @@ __global__ void __launch_bounds__(256) pass_digits_kernel(const unsigned char* _
   for (uint32_t i = tid; i < ncnt * 32; i += blockDim.x) dcnt[i] = 0;
   __syncthreads();
   const uint32_t base = uint32_t(__cvta_generic_to_shared(dcnt)) + lane * 4;
-  bool bad = false;
+  // a symbol >= 2^L sets a bit of `seen` at or above L (its digits still
+  // count, into counters whose values the failed build never uses)
+  uint32_t seen = 0;
+  uint32_t lo[NP], mask[NP];
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    lo[p] = p < int(pd.npasses) ? pd.lo[p] : 0u;
+    mask[p] = p < int(pd.npasses) ? pd.mask[p] : 0u;
+  }
   auto count = [&](uint32_t x) {
-    if (pd.L < 32 && (x >> pd.L)) {
-      bad = true;
-      return;
-    }
-    for (uint32_t p = 0; p < pd.npasses; ++p) {
-      const uint32_t d = (x >> pd.lo[p]) & pd.mask[p];
-      asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(base + (p * 16 + d) * 128) : "memory");
-    }
+    seen |= x;
+#pragma unroll
+    for (int p = 0; p < NP; ++p)
+      if (p < int(pd.npasses))
+        asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(base + ((uint32_t(p) * 16 + ((x >> lo[p]) & mask[p])) << 7))
+                     : "memory");
   };
   // 16-byte vectors between the unaligned ends of the text
   const uint32_t E = 16 / width;
@@ -615,7 +624,7 @@ __global__ void __launch_bounds__(256) pass_digits_kernel(const unsigned char* _
     }
   }
   for (uint64_t i = head + nv * E + gid; i < n; i += stride) count(sym(i));
-  if (bad) atomicOr(status, kErrSymbol);
+  if (pd.L < 32 && (seen >> pd.L)) atomicOr(status, kErrSymbol);
   __syncthreads();
   for (uint32_t e = tid; e < ncnt; e += blockDim.x) {
     uint32_t sum = 0;
@@ -961,7 +970,7 @@ void launch_pass_digits(const void* text, uint64_t n, uint32_t width, const Pass
   const size_t smem = size_t(pd.npasses) * 16 * 32 * 4;
   static bool configured = false;
   if (!configured) {
-    cudaFuncSetAttribute(pass_digits_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(pass_digits_kernel<kPassDigitsMaxPasses>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          int(kPassDigitsMaxPasses * 16 * 32 * 4));
     configured = true;
   }
@@ -970,8 +979,13 @@ void launch_pass_digits(const void* text, uint64_t n, uint32_t width, const Pass
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
   const uint64_t cap = uint64_t(sms > 0 ? sms : 1) * 4;
-  pass_digits_kernel<<<unsigned(std::max<uint64_t>(1, std::min(want, cap))), 256, smem, s>>>(
-      static_cast<const unsigned char*>(text), n, width, pd, digits, done, status, out);
+  const unsigned grid = unsigned(std::max<uint64_t>(1, std::min(want, cap)));
+  if (pd.npasses <= 6)
+    pass_digits_kernel<6><<<grid, 256, smem, s>>>(static_cast<const unsigned char*>(text), n, width, pd, digits, done,
+                                                  status, out);
+  else
+    pass_digits_kernel<kPassDigitsMaxPasses><<<grid, 256, smem, s>>>(static_cast<const unsigned char*>(text), n, width,
+                                                                     pd, digits, done, status, out);
   ++*launches;
 }
 
