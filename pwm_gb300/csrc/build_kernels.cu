@@ -515,19 +515,21 @@ __global__ void regroup_kernel(const uint64_t* __restrict__ matrix_level, uint64
 // ---------------------------------------------------------------------------
 // Huffman code keys
 // ---------------------------------------------------------------------------
+// Key of symbol c with code (word, len), L the longest code: the code
+// followed by a stop bit, ((word << 1) | 1) << (L - len), in L + 1 <= 8 *
+// sizeof(K) bits (split.cuh HuffKeys).
 template <typename T, typename K>
 __global__ void huffman_keys_kernel(const T* text, uint64_t n, const uint64_t* code_len, const uint64_t* code_word,
-                                    uint64_t ncodes, K* keys, uint32_t* status) {
-  constexpr uint32_t kBits = sizeof(K) * 8 - 8;
+                                    uint64_t ncodes, uint32_t L, K* keys, uint32_t* status) {
   for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
     uint64_t c = uint64_t(text[i]);
     uint64_t len = c < ncodes ? code_len[c] : 0;
-    if (len == 0 || len > kBits) {
+    if (len == 0 || len > L) {
       atomicOr(status, kErrSymbol);
       keys[i] = K(0);
       continue;
     }
-    keys[i] = K(((uint64_t(code_word[c]) << (kBits - len)) << 8) | len);
+    keys[i] = K(((uint64_t(code_word[c]) << 1) | 1u) << (L - len));
   }
 }
 
@@ -929,20 +931,33 @@ void launch_regroup(const uint64_t* matrix_level, uint64_t* tree_level, uint64_t
   ++*launches;
 }
 
+template <typename T, typename K>
+void launch_hk(const void* text, uint64_t n, const uint64_t* code_len, const uint64_t* code_word, uint64_t ncodes,
+               uint32_t L, void* keys, uint32_t* status, cudaStream_t s) {
+  huffman_keys_kernel<T, K><<<grid_for(n, 256), 256, 0, s>>>(static_cast<const T*>(text), n, code_len, code_word,
+                                                             ncodes, L, static_cast<K*>(keys), status);
+}
+
+template <typename T>
+void launch_hk_width(uint32_t key_bytes, const void* text, uint64_t n, const uint64_t* code_len,
+                     const uint64_t* code_word, uint64_t ncodes, uint32_t L, void* keys, uint32_t* status,
+                     cudaStream_t s) {
+  switch (key_bytes) {
+    case 1: launch_hk<T, uint8_t>(text, n, code_len, code_word, ncodes, L, keys, status, s); break;
+    case 2: launch_hk<T, uint16_t>(text, n, code_len, code_word, ncodes, L, keys, status, s); break;
+    case 4: launch_hk<T, uint32_t>(text, n, code_len, code_word, ncodes, L, keys, status, s); break;
+    default: launch_hk<T, uint64_t>(text, n, code_len, code_word, ncodes, L, keys, status, s); break;
+  }
+}
+
 void launch_huffman_keys(const void* text, uint64_t n, uint32_t width, const uint64_t* code_len,
-                         const uint64_t* code_word, uint64_t ncodes, uint32_t key_bytes, void* keys,
+                         const uint64_t* code_word, uint64_t ncodes, uint32_t levels, uint32_t key_bytes, void* keys,
                          uint32_t* status, cudaStream_t s, uint64_t* launches) {
   if (n == 0) return;
-  const int g = grid_for(n, 256);
-#define PWMGPU_HK(T)                                                                                            \
-  if (key_bytes == 4)                                                                                           \
-    huffman_keys_kernel<T, uint32_t><<<g, 256, 0, s>>>(static_cast<const T*>(text), n, code_len, code_word,    \
-                                                       ncodes, static_cast<uint32_t*>(keys), status);          \
-  else                                                                                                          \
-    huffman_keys_kernel<T, uint64_t><<<g, 256, 0, s>>>(static_cast<const T*>(text), n, code_len, code_word,    \
-                                                       ncodes, static_cast<uint64_t*>(keys), status);
-  if (width == 1) { PWMGPU_HK(uint8_t) } else if (width == 2) { PWMGPU_HK(uint16_t) } else { PWMGPU_HK(uint32_t) }
-#undef PWMGPU_HK
+  if (width == 1) launch_hk_width<uint8_t>(key_bytes, text, n, code_len, code_word, ncodes, levels, keys, status, s);
+  else if (width == 2)
+    launch_hk_width<uint16_t>(key_bytes, text, n, code_len, code_word, ncodes, levels, keys, status, s);
+  else launch_hk_width<uint32_t>(key_bytes, text, n, code_len, code_word, ncodes, levels, keys, status, s);
   ++*launches;
 }
 

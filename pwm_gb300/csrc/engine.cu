@@ -192,7 +192,11 @@ void run_passes(pwmgpu_ctx* ctx, const void* keys, uint32_t key_bytes, uint32_t 
     }
 
   const uint64_t n0 = tabs.level_bits.empty() ? 0 : tabs.level_bits[0];
-  const uint32_t T = split_tile_elems(key_bytes);
+  // Huffman keys narrow as the passes go: the pass from level l reads keys
+  // of the L - l + 1 low bits (its levels, the later ones, the stop bit)
+  auto in_bytes = [&](uint32_t l) {
+    return (huff && l > 0) ? std::min(key_bytes, huff_key_bytes(L - l + 1)) : key_bytes;
+  };
   void* ping = ctx->grow("keys_a", std::max<uint64_t>(n0, 1) * key_bytes);
   void* pong = ctx->grow("keys_b", std::max<uint64_t>(n0, 1) * key_bytes);
   const void* in = keys;
@@ -200,6 +204,8 @@ void run_passes(pwmgpu_ctx* ctx, const void* keys, uint32_t key_bytes, uint32_t 
   for (size_t pi = 0; pi < plan.size(); ++pi) {
     const auto& p = plan[pi];
     const uint64_t m = tabs.level_bits[p.level];
+    const uint32_t kb = in_bytes(p.level), kbo = in_bytes(p.level + uint32_t(p.K));
+    const uint32_t T = split_tile_elems(kb);
     const uint32_t tiles = uint32_t((m + T - 1) / T);
     const int nlb = huff ? (2 << p.K) - 2 : (1 << p.K);
     auto* lb = static_cast<unsigned long long*>(ctx->grow("lookback", std::max<uint64_t>(tiles, 1) * nlb * 8 + 64));
@@ -228,7 +234,7 @@ void run_passes(pwmgpu_ctx* ctx, const void* keys, uint32_t key_bytes, uint32_t 
         bytes += mj * text_bytes + words_for(mj) * 8;
       }
       ProfScope ps(ctx, "split_pass", bytes);
-      launch_split_pass(key_bytes, huff, p.K, a, L, s, &ctx->launches);
+      launch_split_pass(kb, kbo, huff, p.K, a, L, s, &ctx->launches);
     }
     CUDA_TRY(cudaGetLastError());
     start_off += tabs.starts[pi].size();

@@ -424,6 +424,9 @@ struct HostIO {
 // host arrays; d_text is then the device copy to fill).
 void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostIO* io = nullptr);
 
+// Bytes of the narrowest Huffman key holding `bits` bits (1, 2, 4 or 8).
+inline uint32_t huff_key_bytes(uint32_t bits) { return bits <= 8 ? 1u : bits <= 16 ? 2u : bits <= 32 ? 4u : 8u; }
+
 // ---- host copies (staging.cu) -----------------------------------------------------
 bool host_pinned(const void* p);
 // Host to device on `s`; returns once `h_src` may be reused.  Pageable

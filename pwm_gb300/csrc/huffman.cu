@@ -75,7 +75,8 @@ void build_huffman(pwmgpu_ctx* ctx, const void* d_text, uint64_t n, uint32_t wid
   for (auto& c : wc) maxlen = std::max(maxlen, c.len);
   if (levels == 0) levels = maxlen;  // the longest code of a symbol that occurs
   if (maxlen != levels) throw Fail{PWMGPU_ERR_ARG, "levels must equal the longest code length"};
-  const uint32_t key_bytes = maxlen <= 24 ? 4 : 8;
+  // keys: the code and a stop bit, levels + 1 bits (split.cuh HuffKeys)
+  const uint32_t key_bytes = huff_key_bytes(levels + 1);
   const auto plan = plan_passes(levels, ctx->pass_levels);
   const LevelTables tabs = build_tables(wc, levels, plan, wt != nullptr);
   // layouts
@@ -89,7 +90,8 @@ void build_huffman(pwmgpu_ctx* ctx, const void* d_text, uint64_t n, uint32_t wid
   CUDA_TRY(cudaMemcpyAsync(d_len, code_len.data(), ncodes * 8, cudaMemcpyHostToDevice, s));
   CUDA_TRY(cudaMemcpyAsync(d_word, code_word.data(), ncodes * 8, cudaMemcpyHostToDevice, s));
   void* keys = ctx->grow("huff_keys", std::max<uint64_t>(n, 1) * key_bytes);
-  launch_huffman_keys(d_text, n, width, d_len, d_word, ncodes, key_bytes, keys, ctx->d_status, s, &ctx->launches);
+  launch_huffman_keys(d_text, n, width, d_len, d_word, ncodes, levels, key_bytes, keys, ctx->d_status, s,
+                      &ctx->launches);
   run_passes(ctx, keys, key_bytes, width, true, levels, plan, tabs, wm, wt);
   check_device_status(ctx);
   build_rank_select(ctx, !is_tree ? &wm : nullptr, wt);

@@ -113,7 +113,8 @@ void launch_merge_gather(const MergeSeg* segs, uint64_t nseg, uint64_t* dst, uin
 uint32_t split_tile_elems(uint32_t key_bytes);
 // Dynamic shared memory of one CTA.
 size_t split_smem_bytes(uint32_t key_bytes, int K);
-void launch_split_pass(uint32_t key_bytes, bool huffman, int K, const SplitArgs& a, uint32_t L, cudaStream_t s,
+void launch_split_pass(uint32_t key_bytes, uint32_t out_bytes, bool huffman, int K, const SplitArgs& a, uint32_t L,
+                       cudaStream_t s,
                        uint64_t* launches);
 // Plain keys of a batch of texts: args[t] describes text t's pass, its tiles
 // are [tile_base[t], tile_base[t+1]) of the launch; counter zeroed.
@@ -156,9 +157,10 @@ void launch_regroup(const uint64_t* matrix_level, uint64_t* tree_level, uint64_t
                     const uint64_t* seg_matrix, uint64_t nseg, uint32_t* status, cudaStream_t s, uint64_t* launches);
 
 // ---- Huffman keys -------------------------------------------------------------
-// key = (code << (keybits - 8 - len)) << 8 | len for every text symbol.
+// key = ((code << 1) | 1) << (levels - len) for every text symbol, in keys
+// of key_bytes >= (levels + 1) / 8 bytes.
 void launch_huffman_keys(const void* text, uint64_t n, uint32_t width, const uint64_t* code_len,
-                         const uint64_t* code_word, uint64_t ncodes, uint32_t key_bytes, void* keys,
+                         const uint64_t* code_word, uint64_t ncodes, uint32_t levels, uint32_t key_bytes, void* keys,
                          uint32_t* status, cudaStream_t s, uint64_t* launches);
 // Histogram of the symbols (u64 counts; 8- and 16-bit texts: all 2^8 / 2^16
 // values, so hist needs that many entries; 32-bit texts: symbols below nsym)

@@ -14,13 +14,14 @@ template <> struct SplitGeometry<2> { static constexpr int ITEMS = 64; using Key
 template <> struct SplitGeometry<4> { static constexpr int ITEMS = 32; using Key = uint32_t; };
 template <> struct SplitGeometry<8> { static constexpr int ITEMS = 16; using Key = uint64_t; };
 
-template <int KB, bool HUFF, int K>
+template <int KB, bool HUFF, int K, int KBO = KB>
 void launch_one(const SplitArgs& a, uint32_t L, cudaStream_t s) {
   using G = SplitGeometry<KB>;
   using Key = typename G::Key;
+  using KeyO = typename SplitGeometry<KBO>::Key;
   using Tr = typename std::conditional<HUFF, HuffKeys<Key>, PlainKeys<Key>>::type;
   using P = SplitPass<Key, Tr, K, kSplitThreads, G::ITEMS>;
-  auto kern = split_pass_kernel<Key, Tr, K, kSplitThreads, G::ITEMS>;
+  auto kern = split_pass_kernel<Key, Tr, K, kSplitThreads, G::ITEMS, KeyO>;
   static bool configured = false;  // one attribute call per instantiation and process
   const size_t smem = P::smem_bytes();
   if (!configured) {
@@ -48,13 +49,13 @@ void launch_batched_one(const SplitArgs* args, const uint32_t* tile_base, uint32
   kern<<<tiles, kSplitThreads, smem, s>>>(args, tile_base, ntexts, counter);
 }
 
-template <int KB, bool HUFF>
+template <int KB, bool HUFF, int KBO = KB>
 void launch_k(int K, const SplitArgs& a, uint32_t L, cudaStream_t s) {
   switch (K) {
-    case 1: launch_one<KB, HUFF, 1>(a, L, s); break;
-    case 2: launch_one<KB, HUFF, 2>(a, L, s); break;
-    case 3: launch_one<KB, HUFF, 3>(a, L, s); break;
-    default: launch_one<KB, HUFF, 4>(a, L, s); break;
+    case 1: launch_one<KB, HUFF, 1, KBO>(a, L, s); break;
+    case 2: launch_one<KB, HUFF, 2, KBO>(a, L, s); break;
+    case 3: launch_one<KB, HUFF, 3, KBO>(a, L, s); break;
+    default: launch_one<KB, HUFF, 4, KBO>(a, L, s); break;
   }
 }
 
@@ -94,11 +95,23 @@ size_t split_smem_bytes(uint32_t key_bytes, int K) {
   return 2 * T * key_bytes + size_t(K > 1 ? K - 1 : 1) * (T / 32 + 1) * 4;
 }
 
-void launch_split_pass(uint32_t key_bytes, bool huffman, int K, const SplitArgs& a, uint32_t L, cudaStream_t s,
-                       uint64_t* launches) {
+void launch_split_pass(uint32_t key_bytes, uint32_t out_bytes, bool huffman, int K, const SplitArgs& a, uint32_t L,
+                       cudaStream_t s, uint64_t* launches) {
   if (a.tiles == 0) return;
   if (huffman) {
-    if (key_bytes == 4) launch_k<4, true>(K, a, L, s); else launch_k<8, true>(K, a, L, s);
+    // a pass without S_{l+K} has no output keys: the input width alone
+    const uint32_t o = a.out ? std::min(out_bytes, key_bytes) : key_bytes;
+    if (key_bytes == 8) {
+      if (o == 8) launch_k<8, true>(K, a, L, s); else launch_k<8, true, 4>(K, a, L, s);
+    } else if (key_bytes == 4) {
+      if (o == 4) launch_k<4, true>(K, a, L, s);
+      else if (o == 2) launch_k<4, true, 2>(K, a, L, s);
+      else launch_k<4, true, 1>(K, a, L, s);
+    } else if (key_bytes == 2) {
+      if (o == 2) launch_k<2, true>(K, a, L, s); else launch_k<2, true, 1>(K, a, L, s);
+    } else {
+      launch_k<1, true>(K, a, L, s);
+    }
   } else {
     switch (key_bytes) {
       case 1: launch_k<1, false>(K, a, L, s); break;

@@ -44,17 +44,22 @@ struct PlainKeys {
   static constexpr bool kDrops = false;
 };
 
-// Huffman keys: code left-aligned in the top (bits-8) bits, code length in
-// the low 8 bits.  Level m tests code bit m; the element is alive at level m
-// while length > m.
+// Huffman keys with a stop bit: ((code << 1) | 1) << (L - length), L the
+// longest code.  Level m tests bit L - m; the element is alive at level m
+// while a bit below that one is set (the stop bit lies below every code
+// bit of the element and nothing lies below the stop bit).  A pass needs
+// only the bits of its levels and below, so it writes S_{l+K} in the
+// narrowest keys that hold the L - (l + K) + 1 low bits, and the bit a
+// level tests keeps its position.
 template <typename KeyT>
 struct HuffKeys {
-  uint32_t L;  // unused; keeps the layout of PlainKeys
-  static constexpr uint32_t kTop = sizeof(KeyT) * 8 - 1;
+  uint32_t L;
   __device__ __forceinline__ uint32_t bit(KeyT k, uint32_t level) const {
-    return uint32_t(uint64_t(k) >> (kTop - level)) & 1u;
+    return uint32_t(uint64_t(k) >> (L - level)) & 1u;
   }
-  __device__ __forceinline__ bool alive(KeyT k, uint32_t level) const { return uint32_t(k & 0xFFu) > level; }
+  __device__ __forceinline__ bool alive(KeyT k, uint32_t level) const {
+    return (uint64_t(k) & ((uint64_t(1) << (L - level)) - 1u)) != 0;
+  }
   static constexpr bool kDrops = true;
 };
 
@@ -224,16 +229,17 @@ __device__ __forceinline__ void copy_run_bytes(unsigned char* dst, const unsigne
   if (uint32_t(lane) < len - done) dst[done + lane] = src[done + lane];
 }
 
-template <typename KeyT, typename Traits, int K, int THREADS, int ITEMS>
+template <typename KeyT, typename Traits, int K, int THREADS, int ITEMS, typename KeyO = KeyT>
 __device__ __forceinline__ void split_pass_tile(const SplitArgs& a, const Traits& tr, uint32_t tile);
 
-// One text: tiles are taken in launch order from a.tile_counter.
-template <typename KeyT, typename Traits, int K, int THREADS, int ITEMS>
+// One text: tiles are taken in launch order from a.tile_counter.  KeyO: the
+// key type of S_{l+K} (KeyT, or narrower for Huffman keys, their low bits).
+template <typename KeyT, typename Traits, int K, int THREADS, int ITEMS, typename KeyO = KeyT>
 __global__ void __launch_bounds__(THREADS, K <= 2 ? 4 : 3) split_pass_kernel(SplitArgs a, Traits tr) {
   __shared__ uint32_t s_tile;
   if (threadIdx.x == 0) s_tile = atomicAdd(a.tile_counter, 1u);
   __syncthreads();
-  split_pass_tile<KeyT, Traits, K, THREADS, ITEMS>(a, tr, s_tile);
+  split_pass_tile<KeyT, Traits, K, THREADS, ITEMS, KeyO>(a, tr, s_tile);
 }
 
 // A batch of texts: global tile g belongs to the text whose range
@@ -263,7 +269,7 @@ __global__ void __launch_bounds__(THREADS, K <= 2 ? 4 : 3)
   split_pass_tile<KeyT, Traits, K, THREADS, ITEMS>(s_args, tr, s_tile);
 }
 
-template <typename KeyT, typename Traits, int K, int THREADS, int ITEMS>
+template <typename KeyT, typename Traits, int K, int THREADS, int ITEMS, typename KeyO>
 __device__ __forceinline__ void split_pass_tile(const SplitArgs& a, const Traits& tr, const uint32_t tile) {
   using P = SplitPass<KeyT, Traits, K, THREADS, ITEMS>;
   constexpr int T = P::T, C = P::C, WARPS = P::WARPS, SW = P::SW, KPL = P::KPL, ROUND = P::ROUND;
@@ -510,8 +516,13 @@ __device__ __forceinline__ void split_pass_tile(const SplitArgs& a, const Traits
         if (lane == 0) atomicOr(a.status, kErrBounds);
         continue;
       }
-      copy_run_bytes(reinterpret_cast<unsigned char*>(static_cast<KeyT*>(a.out) + g),
-                     reinterpret_cast<const unsigned char*>(cur + start), len * uint32_t(sizeof(KeyT)));
+      if constexpr (sizeof(KeyO) == sizeof(KeyT)) {
+        copy_run_bytes(reinterpret_cast<unsigned char*>(static_cast<KeyT*>(a.out) + g),
+                       reinterpret_cast<const unsigned char*>(cur + start), len * uint32_t(sizeof(KeyT)));
+      } else {
+        KeyO* dst = static_cast<KeyO*>(a.out) + g;
+        for (uint32_t i = uint32_t(lane); i < len; i += 32) dst[i] = KeyO(cur[start + i]);
+      }
     }
   }
 }
