@@ -340,6 +340,8 @@ pwmgpu_status guarded(pwmgpu_ctx* ctx, F&& f) {
     return fail(ctx, e.st, e.msg);
   } catch (const std::bad_alloc&) {
     return fail(ctx, PWMGPU_ERR_OOM, "host allocation failed");
+  } catch (const std::exception& e) {  // nothing else may cross the C ABI
+    return fail(ctx, PWMGPU_ERR_CUDA, std::string("host error: ") + e.what());
   }
 }
 

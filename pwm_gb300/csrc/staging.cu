@@ -18,7 +18,7 @@ unsigned copy_threads(const pwmgpu_ctx* ctx) {
 }
 
 char* stage_ring(pwmgpu_ctx* ctx, unsigned threads) {
-  if (!ctx->copy_pool || ctx->copy_pool->threads() != threads) {
+  if (!ctx->copy_pool || ctx->copy_pool->requested() != threads) {
     ctx->copy_pool.reset();
     ctx->copy_pool = std::make_unique<CopyPool>(threads);
   }

@@ -8,6 +8,7 @@
 #include <cstdint>
 #include <cstring>
 #include <mutex>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -15,9 +16,13 @@ namespace pwmgpu {
 
 class CopyPool {
  public:
-  // `threads` copiers in all, the calling thread included.
-  explicit CopyPool(unsigned threads) {
-    for (unsigned i = 1; i < std::max(1u, threads); ++i) workers_.emplace_back([this, i]() { run(i); });
+  // `threads` copiers in all, the calling thread included (fewer when the
+  // system cannot start more: the copies then take fewer parts).
+  explicit CopyPool(unsigned threads) : requested_(threads) {
+    try {
+      for (unsigned i = 1; i < std::max(1u, threads); ++i) workers_.emplace_back([this, i]() { run(i); });
+    } catch (const std::system_error&) {
+    }
   }
   ~CopyPool() {
     {
@@ -31,6 +36,7 @@ class CopyPool {
   CopyPool& operator=(const CopyPool&) = delete;
 
   unsigned threads() const { return unsigned(workers_.size()) + 1; }
+  unsigned requested() const { return requested_; }
 
   // dst[0, bytes) = src[0, bytes); returns when every part is copied.
   void copy(void* dst, const void* src, uint64_t bytes) {
@@ -74,6 +80,7 @@ class CopyPool {
     }
   }
 
+  unsigned requested_;
   std::vector<std::thread> workers_;
   std::mutex m_;
   std::condition_variable go_, done_;
