@@ -424,25 +424,32 @@ inline LevelTables build_tables(const std::vector<WeightedCode>& codes, uint32_t
   LevelTables t;
   t.zeros.assign(L, 0);
   t.level_bits.assign(L, 0);
+  // one walk over every (code, level): the level sizes and zeros, and per
+  // pass (l, K) the counts of its key_j values among the codes alive at l+j
+  // (key_j: code bits l..l+j-1, bit l least significant)
+  std::vector<uint32_t> pass_of(L, 0);
+  for (size_t pi = 0; pi < plan.size(); ++pi)
+    for (int j = 0; j < plan[pi].K && plan[pi].level + uint32_t(j) < L; ++j) pass_of[plan[pi].level + j] = uint32_t(pi);
+  std::vector<std::vector<uint64_t>> cnts(plan.size());
+  for (size_t pi = 0; pi < plan.size(); ++pi) cnts[pi].assign(size_t((2 << plan[pi].K) - 2), 0);
   for (const auto& c : codes) {
-    for (uint32_t m = 0; m < c.len && m < L; ++m) {
+    const uint32_t top = std::min<uint32_t>(c.len, L);
+    uint32_t key = 0;
+    for (uint32_t m = 0; m < top; ++m) {
+      const uint32_t b = code_bit(c, m);
       t.level_bits[m] += c.freq;
-      if (!code_bit(c, m)) t.zeros[m] += c.freq;
+      if (!b) t.zeros[m] += c.freq;
+      const PassPlan& p = plan[pass_of[m]];
+      const uint32_t j = m - p.level + 1;  // 1..K
+      key = (j == 1 ? 0u : key) | (b << (j - 1));
+      if (m + 1 < c.len) cnts[pass_of[m]][size_t((1u << j) - 2 + key)] += c.freq;  // alive at l+j
     }
   }
   t.starts.resize(plan.size());
   for (size_t pi = 0; pi < plan.size(); ++pi) {
     const auto& p = plan[pi];
     const int C = (2 << p.K) - 2;
-    std::vector<uint64_t> cnt(size_t(C), 0);
-    for (const auto& c : codes) {
-      uint32_t key = 0;
-      for (int j = 1; j <= p.K; ++j) {
-        if (p.level + j - 1 >= c.len) break;
-        key |= code_bit(c, p.level + j - 1) << (j - 1);
-        if (p.level + j < c.len) cnt[size_t((1 << j) - 2 + int(key))] += c.freq;  // alive at l+j
-      }
-    }
+    const std::vector<uint64_t>& cnt = cnts[pi];
     std::vector<uint64_t> st(size_t(C), 0);
     for (int j = 1; j <= p.K; ++j) {
       uint64_t run = 0;
@@ -458,19 +465,27 @@ inline LevelTables build_tables(const std::vector<WeightedCode>& codes, uint32_t
     t.seg_matrix.resize(L);
     // codes by their left-aligned code word: at every level the prefixes of
     // the longer codes then come in prefix order, so no level sorts them
-    std::vector<size_t> by_word;
+    std::vector<std::pair<uint64_t, size_t>> by_word;  // (left-aligned code word, code)
     by_word.reserve(codes.size());
     for (size_t i = 0; i < codes.size(); ++i)
-      if (codes[i].len > 1) by_word.push_back(i);
-    auto aligned = [&](size_t i) { return codes[i].word << (64 - codes[i].len); };
-    std::sort(by_word.begin(), by_word.end(), [&](size_t a, size_t b) { return aligned(a) < aligned(b); });
+      if (codes[i].len > 1) by_word.emplace_back(codes[i].word << (64 - codes[i].len), i);
+    std::sort(by_word.begin(), by_word.end());  // distinct prefix-free codes: the words differ
+    // (prefix, length, count) in that order, read sequentially by every level
+    struct Sorted {
+      uint64_t word;
+      uint64_t freq;
+      uint32_t len;
+    };
+    std::vector<Sorted> sorted;
+    sorted.reserve(by_word.size());
+    for (const auto& bw : by_word) sorted.push_back({codes[bw.second].word, codes[bw.second].freq, codes[bw.second].len});
     std::vector<std::pair<uint64_t, uint64_t>> g;     // (prefix, count) in natural prefix order
     std::vector<std::pair<uint64_t, size_t>> rorder;  // (bit-reversed prefix, group)
+    std::vector<uint64_t> by_rev;                     // counts by bit-reversed prefix
     for (uint32_t m = 1; m < L; ++m) {
       // prefix groups of level m among codes longer than m
       g.clear();
-      for (size_t i : by_word) {
-        const auto& c = codes[i];
+      for (const Sorted& c : sorted) {
         if (c.len <= m) continue;
         const uint64_t pfx = c.word >> (c.len - m);
         if (!g.empty() && g.back().first == pfx) g.back().second += c.freq;
@@ -479,11 +494,25 @@ inline LevelTables build_tables(const std::vector<WeightedCode>& codes, uint32_t
       std::vector<uint64_t> tree_start(g.size()), matrix_start(g.size());
       uint64_t run = 0;
       for (size_t i = 0; i < g.size(); ++i) { tree_start[i] = run; run += g[i].second; }
-      rorder.resize(g.size());
-      for (size_t i = 0; i < g.size(); ++i) rorder[i] = {rev_bits_host(g[i].first, m), i};
-      std::sort(rorder.begin(), rorder.end());
-      run = 0;
-      for (const auto& r : rorder) { matrix_start[r.second] = run; run += g[r.second].second; }
+      if (m <= 20) {
+        // the matrix orders the groups by bit-reversed prefix: counts
+        // scattered to their reversed prefixes, exclusive sums in that order
+        by_rev.assign(size_t(1) << m, 0);
+        for (const auto& x : g) by_rev[rev_bits_host(x.first, m)] = x.second;
+        run = 0;
+        for (auto& x : by_rev) {
+          const uint64_t v = x;
+          x = run;
+          run += v;
+        }
+        for (size_t i = 0; i < g.size(); ++i) matrix_start[i] = by_rev[rev_bits_host(g[i].first, m)];
+      } else {
+        rorder.resize(g.size());
+        for (size_t i = 0; i < g.size(); ++i) rorder[i] = {rev_bits_host(g[i].first, m), i};
+        std::sort(rorder.begin(), rorder.end());
+        run = 0;
+        for (const auto& r : rorder) { matrix_start[r.second] = run; run += g[r.second].second; }
+      }
       std::vector<uint64_t> st, sm;
       for (size_t i = 0; i < g.size(); ++i)
         if (g[i].second) { st.push_back(tree_start[i]); sm.push_back(matrix_start[i]); }

@@ -256,7 +256,12 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   // or by the first pass, whose tiles start at multiples of 64 bits); the
   // first pass's other levels are zeroed by the histogram kernel (levels <= 8)
   // or here; the padding is zero from allocation.
-  const bool tile_engine = ctx->engine == PWMGPU_ENGINE_TILE && L <= kTilePlanMaxLevels;
+  // Deeper than the tile planner's folded prefix counts reach: the tile
+  // engine still builds a matrix alone from every pass's digit counts
+  // (digit_plan below), the warp-pass engine the rest.
+  const bool tile_engine =
+      ctx->engine == PWMGPU_ENGINE_TILE &&
+      (L <= kTilePlanMaxLevels || (!wx->wt.present && !wx->keep_hist && !stream_out));
   // Pass width: by default a text of up to kSinglePassMaxLevels levels takes
   // one pass of all its levels (the histogram kernel gives that pass its
   // prefixes), deeper texts passes of kDefaultTileLevels; set_pass_levels(k)
@@ -299,7 +304,7 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   const uint64_t flat_words = digit_plan ? (uint64_t(2) << Kz) - 1 : (bins << 1) - 1;
   uint64_t* h_flat = ctx->grow_mapped((flat_words + L + 1 + 16 * digit_shape.size()) * 8);
   uint64_t* d_flat_host = ctx->mapped_dev;
-  uint64_t* h_hist = h_flat + bins - 1;
+  uint64_t* h_hist = digit_plan ? nullptr : h_flat + bins - 1;
   const uint64_t* h_zeros = h_flat + flat_words;
   auto* h_status = reinterpret_cast<uint32_t*>(h_flat + flat_words + L);
   const uint64_t* h_digits = h_flat + flat_words + L + 1;
