@@ -110,6 +110,27 @@ def test_long_codes_use_wide_keys(pg, orc):
             assert ws.zeros() == [int(z) for z in ref.zeros]
 
 
+def test_codes_longer_than_32_bits(pg, orc):
+    """A caller's prefix code with codes up to 47 bits: 64-bit keys (the
+    code and its stop bit), narrowed to 32 bits once the levels left fit."""
+    nsym = 48
+    ln = np.array([i + 1 for i in range(nsym - 1)] + [nsym - 1], np.uint64)  # i ones then a zero; all ones
+    wd = np.array([(1 << (i + 1)) - 2 for i in range(nsym - 1)] + [(1 << (nsym - 1)) - 1], np.uint64)
+    rng = np.random.default_rng(9)
+    text = rng.integers(0, nsym, 200_003).astype(np.uint8)
+    levels = int(ln.max())
+    counts = np.bincount(text, minlength=nsym)
+    sizes = np.array([int(counts[ln > l].sum()) for l in range(levels)], np.uint64)
+    for tree in (False, True):
+        ws = pg.wx_huff_ps(np.uint8, tree).compute(text, text.size, 0, codes=(ln, wd))
+        ref = orc.huff_build(text, tree, codes=(ln, wd, sizes, levels))
+        assert ws.levels() == levels == 47
+        for l in range(levels):
+            assert np.array_equal(np.asarray(ws.bvs()[l]), ref.level(l)), (tree, l)
+        if not tree:
+            assert ws.zeros() == [int(z) for z in ref.zeros]
+
+
 def test_single_symbol_text(pg, orc):
     text = np.full(1000, 7, np.uint8)
     for tree in (False, True):
