@@ -6,20 +6,24 @@ namespace pwmgpu {
 
 namespace {
 
-template <typename KeyT, bool OUT, typename KeyO = KeyT>
+template <typename KeyT, bool OUT, typename KeyO = KeyT, bool PLANES = false>
 void launch_k(int K, const TileArgs& a, cudaStream_t s) {
   switch (K) {
-    case 1: launch_tile_one<KeyT, 1, OUT, KeyO>(a, s); break;
-    case 2: launch_tile_one<KeyT, 2, OUT, KeyO>(a, s); break;
-    case 3: launch_tile_one<KeyT, 3, OUT, KeyO>(a, s); break;
-    default: launch_tile_one<KeyT, 4, OUT, KeyO>(a, s); break;
+    case 1: launch_tile_one<KeyT, 1, OUT, KeyO, PLANES>(a, s); break;
+    case 2: launch_tile_one<KeyT, 2, OUT, KeyO, PLANES>(a, s); break;
+    case 3: launch_tile_one<KeyT, 3, OUT, KeyO, PLANES>(a, s); break;
+    default: launch_tile_one<KeyT, 4, OUT, KeyO, PLANES>(a, s); break;
   }
 }
 
-// A pass writing S_{l+K} in keys of out_bytes (<= the input's key width).
+// A pass writing S_{l+K} in keys of out_bytes (<= the input's key width).  A
+// pass over 1-byte keys without S_{l+K} moves bit planes.
 template <typename KeyT>
 void launch_key(int K, bool out, uint32_t out_bytes, const TileArgs& a, cudaStream_t s) {
-  if (!out) launch_k<KeyT, false>(K, a, s);
+  if (!out) {
+    if constexpr (sizeof(KeyT) == 1) launch_k<KeyT, false, KeyT, true>(K, a, s);
+    else launch_k<KeyT, false>(K, a, s);
+  }
   else if (out_bytes >= sizeof(KeyT)) launch_k<KeyT, true>(K, a, s);
   else if constexpr (sizeof(KeyT) >= 2) {
     if (out_bytes == 1) launch_k<KeyT, true, uint8_t>(K, a, s);

@@ -36,6 +36,11 @@
 //   * writes every run of every level to the matrix and the tree at
 //     table start + look-back prefix in 64-bit words, and the runs of
 //     S_{l+K} to the next pass's input (one warp per run, round-robin).
+// A pass that writes no S_{l+K} over 1-byte keys (the last pass of every
+// text whose remaining levels fit a byte) runs the splits on bit planes
+// instead (tile_planes_splits): the K bits of every key as K planes of 32-key
+// words, each split a stable partition of the later planes' words; the
+// streams of the levels are then the planes themselves.
 #pragma once
 
 #include "common.cuh"
@@ -126,6 +131,9 @@ struct TileCfg {
   static constexpr size_t smem_bytes() {
     return size_t(2) * T * sizeof(KeyT) + size_t(K) * SBW * 4 + (D >= 2 ? size_t(NVEC) * 4 : 0);
   }
+  // the bit-plane form (tile_pass_body with PLANES): two sets of K planes, a
+  // zero count per plane word and the 256-entry compress table
+  static constexpr size_t plane_smem_bytes() { return size_t(2) * K * SBW * 4 + size_t(T / 32) * 4 + 256 * 4; }
 };
 
 // Split bits of the keys of one 16-byte vector, MSB first: bit KPL-1-i is the
@@ -401,6 +409,22 @@ __device__ __forceinline__ void write_key_run_narrow(KeyO* dst, const KeyT* src,
   for (uint32_t i = threadIdx.x & 31; i < len; i += 32) dst[i] = KeyO(src[i]);
 }
 
+// Bytes [off, off + 16) of the 32 bytes lo:hi (off < 16, the same for the
+// whole tile): a two-stage word shifter (by 2, then by 1 word) and one
+// funnel shift per output word.
+__device__ __forceinline__ uint4 realign16(const uint4& lo, const uint4& hi, uint32_t off) {
+  const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+  const bool s2 = (off & 8u) != 0, s1 = (off & 4u) != 0;
+  uint32_t g[6], f[5];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) g[i] = s2 ? w[i + 2] : w[i];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) f[i] = s1 ? g[i + 1] : g[i];
+  const uint32_t bsh = 8u * (off & 3u);
+  return make_uint4(__funnelshift_r(f[0], f[1], bsh), __funnelshift_r(f[1], f[2], bsh),
+                    __funnelshift_r(f[2], f[3], bsh), __funnelshift_r(f[3], f[4], bsh));
+}
+
 // Load `bytes` bytes from global `src` (any alignment) into the 16-byte
 // aligned shared buffer `dst`, 16 bytes per thread step.  Bytes past the end
 // of the tile are not read beyond the 16-byte block that holds the last one.
@@ -414,24 +438,90 @@ __device__ __forceinline__ void load_tile_bytes(uint4* dst, const unsigned char*
     for (uint32_t k = threadIdx.x; k < nv; k += THREADS) dst[k] = __ldcs(a + k);
     return;
   }
-  const uint32_t wsh = off >> 2, bsh = 8 * (off & 3);
   const uint32_t last_block = uint32_t((off + bytes - 1) >> 4);  // last aligned block holding tile bytes
   for (uint32_t k = threadIdx.x; k < nv; k += THREADS) {
     const uint4 lo = __ldcs(a + k);
     const uint4 hi = k + 1 <= last_block ? __ldcs(a + k + 1) : make_uint4(0, 0, 0, 0);
-    const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-    uint32_t o[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      uint32_t x0 = 0, x1 = 0;
-      // select words wsh+i and wsh+i+1 without dynamic register indexing
-#pragma unroll
-      for (int s = 0; s < 4; ++s)
-        if (uint32_t(s) == wsh) { x0 = w[s + i]; x1 = w[s + i + 1]; }
-      o[i] = __funnelshift_r(x0, x1, bsh);
-    }
-    dst[k] = make_uint4(o[0], o[1], o[2], o[3]);
+    dst[k] = realign16(lo, hi, off);
   }
+}
+
+// ---- bit planes (the last pass of 1-byte keys) -----------------------------
+// A plane holds one level's bit of every key of the tile, 32 keys per word,
+// the first key in bit 31.  A 1-bit split of the keys then becomes a stable
+// partition of each later plane's words by the split plane's word: its bits
+// under zeros packed to the top ("compress", Hacker's Delight 7-4, mirrored to
+// pack toward bit 31) and appended to the zero part of the new plane, the
+// bits under ones to the one part.  The compress runs inside each byte (three
+// rounds of moves by 1, 2 and 4 bits), then shifts the four byte pieces
+// together; the move masks of a byte depend on its mask byte only and come
+// from a 256-entry table, so a mask word costs four table reads and a byte
+// transpose, once per word and polarity, for every plane that moves.
+
+// Bit q of the 8 keys of w0 (keys 0-3, key k in byte k) and w1 (keys 4-7),
+// key 0 in bit 7 of the result (higher bits are not cleared).  The 8 bits are
+// spread to byte bit 0 (w1) and bit 4 (w0) and collected by one 32x32->64-bit
+// multiply by 2^4 + 2^13 + 2^22 + 2^31: the 32 partial products land on
+// distinct bit positions, so no carries disturb bits 28-35.
+__device__ __forceinline__ uint32_t key_bits8(uint32_t w0, uint32_t w1, int q) {
+  const uint32_t t0 = (w0 >> q) & 0x01010101u, t1 = (w1 >> q) & 0x01010101u;
+  return uint32_t((uint64_t(t0 * 16u + t1) * 0x80402010ull) >> 28);
+}
+
+// Table entry of mask byte b: the move masks of compress toward bit 7 inside
+// the byte (Hacker's Delight 7-4 with every shift mirrored: round i moves the
+// selected bits whose remaining distance has bit i set) in bytes 0-2, the
+// number of selected bits in byte 3.
+__device__ __forceinline__ uint32_t compress_lut_entry(uint32_t b) {
+  uint32_t m = b, mk = (~b & 0xFFu) >> 1, e = uint32_t(__popc(b)) << 24;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    uint32_t mp = mk ^ (mk >> 1);
+    mp ^= mp >> 2;
+    mp ^= mp >> 4;
+    const uint32_t v = mp & m;
+    m = ((m ^ v) | (v << (1 << i))) & 0xFFu;
+    e |= v << (8 * i);
+    mk &= ~mp;
+  }
+  return e;
+}
+// The byte move masks of mask word m (mv[0..2], byte k from the entry of mask
+// byte k: a 4x4 byte transpose of the four entries) and the shifts that join
+// the byte pieces (mv[3..5] for bytes 2, 1, 0: the bits not selected in the
+// bytes above, summed from the top by one multiply).
+__device__ __forceinline__ void compress_masks(const uint32_t* lut, uint32_t m, uint32_t (&mv)[6]) {
+  const uint32_t e0 = lut[m & 0xFFu], e1 = lut[(m >> 8) & 0xFFu], e2 = lut[(m >> 16) & 0xFFu], e3 = lut[m >> 24];
+  const uint32_t l01 = __byte_perm(e0, e1, 0x5140), l23 = __byte_perm(e2, e3, 0x5140);
+  const uint32_t h01 = __byte_perm(e0, e1, 0x7362), h23 = __byte_perm(e2, e3, 0x7362);
+  mv[0] = __byte_perm(l01, l23, 0x5410);
+  mv[1] = __byte_perm(l01, l23, 0x7632);
+  mv[2] = __byte_perm(h01, h23, 0x5410);
+  const uint32_t sh = __byte_perm(0x08080808u - __byte_perm(h01, h23, 0x7632), 0u, 0x0123) * 0x01010101u;
+  mv[3] = sh & 0xFFu;
+  mv[4] = (sh >> 8) & 0xFFu;
+  mv[5] = (sh >> 16) & 0xFFu;
+}
+
+// The bits of x under m, in order, packed to the top of the word (mv: the
+// masks of m).
+__device__ __forceinline__ uint32_t compress_apply(uint32_t x, uint32_t m, const uint32_t (&mv)[6]) {
+  x &= m;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const uint32_t t = x & mv[i];
+    x = (x ^ t) | (t << (1 << i));
+  }
+  return (x & 0xFF000000u) | ((x & 0x00FF0000u) << mv[3]) | ((x & 0x0000FF00u) << mv[4]) | ((x & 0xFFu) << mv[5]);
+}
+
+// OR the top `len` bits of v into a zeroed shared bit stream at bit `pos`
+// (other threads fill the rest of the words it touches).
+__device__ __forceinline__ void or_stream_bits(uint32_t* sb, uint32_t pos, uint32_t v, uint32_t len) {
+  if (len == 0) return;
+  const uint32_t i = pos >> 5, sh = pos & 31;
+  atomicOr(sb + i, v >> sh);
+  if (sh + len > 32) atomicOr(sb + i + 1, v << (32 - sh));
 }
 
 // Exclusive prefix of in[0..count) into out (count <= 128) by one warp, lane
@@ -459,6 +549,237 @@ __device__ __forceinline__ void warp_exclusive_scan(const uint32_t* in, uint32_t
   }
 }
 
+// The load and the splits of a tile in bit-plane form (tile_pass_body with
+// PLANES; 1-byte keys, no S_{l+K}).  Leaves the streams of levels l..l+K-1
+// (plane j of set j % 2), the run sizes and starts of key_1..key_D, and the
+// finest-run counts (counted and published for the look-back, or given).
+// Per split s the thread owning plane words [tid * WPT, (tid + 1) * WPT)
+// reads its words of plane s (the split bit, in S_{l+s} order) and of the
+// later planes, scans the zero counts over the CTA, and ORs the compressed
+// zero and one parts of each later plane into the other set at the word's
+// zero and one cursors; its own words of the read set are then cleared for
+// the split after next.  BATCH: the tile has VP <= V vectors per thread, so
+// NWt = THREADS * VP / 2 plane words, max(VP / 2, 1) per thread (VP = 1:
+// the first half of the threads own one word each); the words above NWt stay
+// zero.
+template <int K, int THREADS, int V, bool BATCH>
+__device__ __forceinline__ void tile_planes_splits(const TileArgs& a, const TileText& s_tx, const TileSeg& s_sg,
+                                                   uint32_t g, uint32_t tl, uint64_t tstart, uint32_t n, int VP,
+                                                   uint32_t shift, bool given, uint32_t* sbits, uint32_t* s_cnt,
+                                                   unsigned long long* pre, uint32_t* s_wz, uint32_t* s_ztot,
+                                                   uint32_t (*rsz)[1 << (K - 1)], uint32_t (*rst)[1 << (K - 1)]) {
+  using C = TileCfg<uint8_t, K, false, THREADS, V>;
+  constexpr int D = C::D, T = C::T, WARPS = C::WARPS, SBW = C::SBW, NLB = C::NLB;
+  constexpr int NW = T / 32;         // plane words of a tile of V vectors per thread
+  constexpr int WPT = NW / THREADS;  // plane words per thread in the splits
+  static_assert(K >= 1 && K <= kTileMaxLevels && WPT * THREADS == NW, "up to 4 levels; whole words per thread");
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t NWt = BATCH ? uint32_t(THREADS * VP / 2) : uint32_t(NW);  // plane words of this tile
+  const int wpt = BATCH ? (VP >= 2 ? VP / 2 : 1) : WPT;                     // of them per thread
+  uint32_t* zpos = sbits + 2 * K * SBW;  // zeros before each plane word, current split
+  uint32_t* s_clut = zpos + NW;          // compress table
+  for (int b = tid; b < 256; b += THREADS) s_clut[b] = compress_lut_entry(uint32_t(b));
+  const uint32_t nfull = n >> 5, nrem = n & 31;
+  auto word_valid = [&](uint32_t w) -> uint32_t {
+    return w < nfull ? ~0u : ((w == nfull && nrem) ? ~0u << (32 - nrem) : 0u);
+  };
+
+  // set 1 and the words of set 0 above the tile's start cleared
+  for (int i = tid; i < K * SBW; i += THREADS) sbits[K * SBW + i] = 0u;
+  if (BATCH && NWt < uint32_t(NW)) {
+    const uint32_t pad = uint32_t(SBW) - NWt;
+    for (uint32_t i = tid; i < K * pad; i += THREADS) sbits[(i / pad) * SBW + NWt + i % pad] = 0u;
+  } else if (tid < 2 * K) {
+    sbits[(tid >> 1) * SBW + NW + (tid & 1)] = 0u;
+  }
+  if (tid == 0) {
+    rsz[0][0] = n;
+    rst[0][0] = 0;
+  }
+
+  // ---- load; planes 0..K-1 in text order (set 0) ---------------------------
+  {
+    const uintptr_t sa = reinterpret_cast<uintptr_t>(static_cast<const unsigned char*>(a.in) + s_sg.in_begin + tstart);
+    const uint32_t off = uint32_t(sa & 15);
+    const uint4* av = reinterpret_cast<const uint4*>(sa - off);
+    const uint32_t nvec = (n + 15) >> 4;
+    const uint32_t last_block = uint32_t((uint64_t(off) + n + 15) >> 4) - 1;  // last aligned block holding tile bytes
+    const uint32_t lo = shift - uint32_t(K - 1);  // plane j is key bit lo + K-1-j
+#pragma unroll
+    for (int r = 0; r < V; ++r) {
+      if (BATCH && r >= VP) break;  // uniform over the CTA
+      const int gv = (warp * VP + r) * 32 + lane;
+      uint4 kv = make_uint4(0u, 0u, 0u, 0u);
+      if (uint32_t(gv) < nvec) {
+        const uint4 x0 = __ldcs(av + gv);
+        if (off == 0) {
+          kv = x0;
+        } else {
+          const uint4 x1 = uint32_t(gv) + 1 <= last_block ? __ldcs(av + gv + 1) : make_uint4(0u, 0u, 0u, 0u);
+          kv = realign16(x0, x1, off);
+        }
+      }
+      const int rem = int(n) - gv * 16;
+      const int nvv = rem >= 16 ? 16 : (rem > 0 ? rem : 0);
+      const uint32_t vm = 0xFFFFu & ~((1u << (16 - nvv)) - 1u);  // valid keys, key 0 in bit 15
+      const uint32_t w0 = kv.x >> lo, w1 = kv.y >> lo, w2 = kv.z >> lo, w3 = kv.w >> lo;
+      uint32_t b[K];
+#pragma unroll
+      for (int j = 0; j < K; ++j)
+        b[j] = __byte_perm(key_bits8(w2, w3, K - 1 - j), key_bits8(w0, w1, K - 1 - j), 0x0040) & vm;
+      // an even lane's vector is the upper half of the plane word, its odd
+      // neighbour's the lower half: one shuffle per two planes
+      const uint32_t pwi = uint32_t(gv) >> 1;
+#pragma unroll
+      for (int j = 0; j < K; j += 2) {
+        if (j + 1 < K) {
+          const uint32_t odd = __shfl_down_sync(0xFFFFFFFFu, b[j] | (b[j + 1] << 16), 1);
+          if (!(lane & 1)) {
+            sbits[j * SBW + pwi] = (b[j] << 16) | (odd & 0xFFFFu);
+            sbits[(j + 1) * SBW + pwi] = (b[j + 1] << 16) | (odd >> 16);
+          }
+        } else {
+          const uint32_t odd = __shfl_down_sync(0xFFFFFFFFu, b[j], 1);
+          if (!(lane & 1)) sbits[j * SBW + pwi] = (b[j] << 16) | odd;
+        }
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- counts of the finest runs (key_D: bit t of the digit is plane t) -----
+  if constexpr (D >= 1) {
+    if (given) {
+      if (tid < NLB) {
+        const uint64_t blk = a.text_blocks ? uint64_t(s_tx.blk0) + tl / a.tiles_per_block : g / a.tiles_per_block;
+        s_cnt[tid] = a.tilecnt[uint64_t(g) * NLB + tid];
+        pre[tid] = a.blockpre[blk * NLB + tid] + a.relpre[uint64_t(g) * NLB + tid];
+      }
+    } else {
+      // per-warp counts in the zero-count words (first written after split 0's barrier)
+      uint32_t (*s_wcnt)[NLB] = reinterpret_cast<uint32_t (*)[NLB]>(zpos);
+      static_assert(WARPS * NLB <= NW, "the counts fit the zero-count words");
+      uint32_t cnt[NLB];
+#pragma unroll
+      for (int c = 0; c < NLB; ++c) cnt[c] = 0;
+#pragma unroll
+      for (int k = 0; k < WPT; ++k) {
+        if (BATCH && k >= wpt) break;
+        const uint32_t w = uint32_t(tid) * wpt + k;
+        const uint32_t vmk = word_valid(w);  // 0 above the tile's words
+        uint32_t pl[D];
+#pragma unroll
+        for (int t = 0; t < D; ++t) pl[t] = sbits[t * SBW + w];
+#pragma unroll
+        for (int c = 0; c < NLB; ++c) {
+          uint32_t mt = vmk;
+#pragma unroll
+          for (int t = 0; t < D; ++t) mt &= ((c >> t) & 1) ? pl[t] : ~pl[t];
+          cnt[c] += __popc(mt);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < NLB; ++c) {
+        const uint32_t x = __reduce_add_sync(0xFFFFFFFFu, cnt[c]);
+        if (lane == 0) s_wcnt[warp][c] = x;
+      }
+      __syncthreads();
+      if (tid < NLB) {
+        uint32_t t = 0;
+#pragma unroll
+        for (int w = 0; w < WARPS; ++w) t += s_wcnt[w][tid];
+        s_cnt[tid] = t;
+        st_volatile(a.lookback + uint64_t(tid) * a.tiles + g, (g == s_sg.tile0 ? kFlagPrefix : kFlagAggregate) | t);
+      }
+    }
+  }
+
+  // ---- the splits -------------------------------------------------------------
+#pragma unroll
+  for (int s = 0; s < D; ++s) {
+    uint32_t* Pc = sbits + (s & 1) * K * SBW;        // planes in S_{l+s} order
+    uint32_t* Pn = sbits + ((s & 1) ^ 1) * K * SBW;  // planes s+1.. in S_{l+s+1} order
+    uint32_t m[WPT], vmk[WPT], zc[WPT], pw[K][WPT];
+    uint32_t tsum = 0;
+#pragma unroll
+    for (int k = 0; k < WPT; ++k) {
+      const uint32_t w = uint32_t(tid) * wpt + k;  // < NW: every word read is inside the planes
+      vmk[k] = (BATCH && k >= wpt) ? 0u : word_valid(w);
+      m[k] = (BATCH && k >= wpt) ? 0u : Pc[s * SBW + w];
+      zc[k] = __popc(~m[k] & vmk[k]);
+      tsum += zc[k];
+#pragma unroll
+      for (int p = s + 1; p < K; ++p) pw[p][k] = (BATCH && k >= wpt) ? 0u : Pc[p * SBW + w];
+    }
+    uint32_t x = tsum;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+      if (lane >= d) x += y;
+    }
+    if (lane == 31) s_wz[warp] = x;
+    __syncthreads();  // (A)
+    uint32_t ztot = 0, zpre = 0;
+#pragma unroll
+    for (int w = 0; w < WARPS; ++w) {
+      const uint32_t z = s_wz[w];
+      ztot += z;
+      zpre += w < warp ? z : 0u;
+    }
+    if (tid == 0) *s_ztot = ztot;
+    if (s >= 2 && tid == 0) {
+      uint32_t run = 0;
+      for (int v = 0; v < (1 << s); ++v) {
+        rst[s][v] = run;
+        run += rsz[s][v];
+      }
+    }
+    uint32_t zp = zpre + x - tsum;  // zeros before this thread's first word
+#pragma unroll
+    for (int k = 0; k < WPT; ++k) {
+      if (BATCH && k >= wpt) break;
+      const uint32_t w = uint32_t(tid) * wpt + k;
+      zpos[w] = zp;
+#pragma unroll
+      for (int p = s + 1; p < K; ++p) Pc[p * SBW + w] = 0u;  // read above; set again two splits on
+      if (s + 1 < K) {
+        const uint32_t mz = ~m[k] & vmk[k], mo = m[k];
+        const uint32_t nz = zc[k], no = __popc(mo);
+        const uint32_t opos = ztot + 32u * w - zp;  // every word before w is whole
+        uint32_t mvz[6], mvo[6];
+        compress_masks(s_clut, mz, mvz);
+        compress_masks(s_clut, mo, mvo);
+#pragma unroll
+        for (int p = s + 1; p < K; ++p) {
+          or_stream_bits(Pn + p * SBW, zp, compress_apply(pw[p][k], mz, mvz), nz);
+          or_stream_bits(Pn + p * SBW, opos, compress_apply(pw[p][k], mo, mvo), no);
+        }
+      }
+      zp += zc[k];
+    }
+    __syncthreads();  // (B)
+    // ---- run sizes of key_{s+1} -------------------------------------------
+    if (s == 0) {
+      if (tid == 0) {
+        rsz[1][0] = ztot;
+        rsz[1][1] = n - ztot;
+        rst[1][0] = 0;
+        rst[1][1] = ztot;
+      }
+    } else if (tid < (2 << s)) {
+      const int v = tid & ((1 << s) - 1);
+      const uint32_t st = rst[s][v], en = st + rsz[s][v];
+      auto zb = [&](uint32_t p) -> uint32_t {  // zeros of plane s before position p (S_{l+s} order)
+        if (p >= n) return *s_ztot;
+        const uint32_t w = p >> 5, k = p & 31;
+        return zpos[w] + k - (k ? __popc(Pc[s * SBW + w] >> (32 - k)) : 0u);
+      };
+      const uint32_t zin = zb(en) - zb(st);
+      rsz[s + 1][tid] = (tid >> s) ? rsz[s][v] - zin : zin;
+    }
+  }
+}
+
 // One tile of a pass: tile g of the launch's segments.  BATCH: a pass of a
 // batch of texts inside the persistent kernel (tile_batch.cu): the tile size
 // is the text's own (TileText::vpt vectors per thread, a warp's slice
@@ -466,8 +787,9 @@ __device__ __forceinline__ void warp_exclusive_scan(const uint32_t* in, uint32_t
 // previous pass is done and afterwards counts itself done; otherwise
 // TileText's batch fields are ignored.
 // KeyO: the key type of S_{l+K} (KeyT, or narrower when the levels left
-// after this pass fit it).
-template <typename KeyT, int K, bool OUT, int THREADS, int V, bool BATCH, typename KeyO = KeyT>
+// after this pass fit it).  PLANES (1-byte keys, a pass without S_{l+K}, up
+// to 4 levels): the splits move bit planes instead of keys.
+template <typename KeyT, int K, bool OUT, int THREADS, int V, bool BATCH, typename KeyO = KeyT, bool PLANES = false>
 __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in) {
   using C = TileCfg<KeyT, K, OUT, THREADS, V>;
   constexpr int D = C::D, KPL = C::KPL, T = C::T, WARPS = C::WARPS, WSLICE = C::WSLICE, SBW = C::SBW;
@@ -477,8 +799,11 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   KeyT* buf0 = reinterpret_cast<KeyT*>(smem_raw);
-  uint32_t* sbits = reinterpret_cast<uint32_t*>(smem_raw + size_t(2) * T * KB);  // K streams of SBW words
-  uint32_t* meta = sbits + K * SBW;                                               // D >= 2: per vector
+  // K streams of SBW words (PLANES: two sets of K planes, the stream of level
+  // l+j being plane j of set j % 2)
+  uint32_t* sbits = reinterpret_cast<uint32_t*>(smem_raw + (PLANES ? size_t(0) : size_t(2) * T * KB));
+  uint32_t* meta = sbits + K * SBW;  // D >= 2: per vector
+  auto stream = [&](int j) -> const uint32_t* { return sbits + ((PLANES ? (j & 1) * K : 0) + j) * SBW; };
 
   __shared__ uint32_t s_tile, s_seg;
   __shared__ TileSeg s_sg;
@@ -542,6 +867,15 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
   const uint32_t n = s_sg.m - tstart < uint64_t(TT) ? uint32_t(s_sg.m - tstart) : TT;
   for (int i = tid; i < tile_table_size(K); i += THREADS) s_table[i] = a.tables[s_sg.table + i];
 
+  const uint32_t shift = s_tx.shift;
+  __shared__ uint32_t s_cnt[NLB];
+  const bool given = a.blockpre != nullptr;  // prefixes from the histogram kernel
+  int cur = 0;
+  if constexpr (PLANES) {
+    static_assert(sizeof(KeyT) == 1 && !OUT, "bit planes: passes over 1-byte keys without S_{l+K}");
+    tile_planes_splits<K, THREADS, V, BATCH>(a, s_tx, s_sg, g, tl, tstart, n, VP, shift, given, sbits, s_cnt, pre,
+                                             s_wz, &s_ztot, rsz, rst);
+  } else {
   load_tile_bytes<THREADS>(reinterpret_cast<uint4*>(buf0),
                            static_cast<const unsigned char*>(a.in) + (s_sg.in_begin + tstart) * KB, n * KB);
   if (tid == 0) {
@@ -551,13 +885,10 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
   __syncthreads();
 
   const uint32_t smem_base = uint32_t(__cvta_generic_to_shared(smem_raw));
-  const uint32_t shift = s_tx.shift;
 
   // ---- counts of the finest runs (key_D), published before the splits -----
   // Every thread counts its keys into its own column of 2^D counters in the
   // second key buffer (free until the first split scatters into it).
-  __shared__ uint32_t s_cnt[NLB];
-  const bool given = a.blockpre != nullptr;  // prefixes from the histogram kernel
   if (D >= 1 && given) {
     if (tid < NLB) {
       const uint64_t blk = a.text_blocks ? uint64_t(s_tx.blk0) + tl / a.tiles_per_block : g / a.tiles_per_block;
@@ -567,6 +898,7 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
   } else if constexpr (D >= 1 && D <= kTileMaxLevels) {
     __shared__ uint32_t s_wcnt[WARPS][NLB];
     constexpr int NB = 1 << D;
+    static_assert(size_t(NB) * THREADS * 4 <= size_t(T) * KB, "the counters fit the second key buffer");
     uint32_t* cnt = reinterpret_cast<uint32_t*>(buf0 + T);
 #pragma unroll
     for (int b = 0; b < NB; ++b) cnt[b * THREADS + tid] = 0;
@@ -611,7 +943,6 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
   const uint32_t nw = n > wbeg ? min(n - wbeg, wslice) : 0u;
   const uint32_t vbefore = min(n, wbeg);
 
-  int cur = 0;
 #pragma unroll 1
   for (int s = 0; s < K; ++s) {
     const bool split = s < D;
@@ -719,6 +1050,7 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
     }
     cur ^= 1;
   }
+  }  // !PLANES
   __syncthreads();
   if constexpr (D >= 2) {
     if constexpr (K > kTileMaxLevels) {
@@ -734,10 +1066,11 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
   for (int st = 0; st < (a.first_level_written ? 0 : nstruct); ++st) {
     const uint64_t dst = s_table[st ? tile_wt_entry(K, 0, 0) : tile_wm_entry(0, 0)] + tstart;
     if (a.clear_edges)
-      write_bits64_clear(st ? s_tx.wt : s_tx.wm, s_tx.nbits, dst, sbits, 0, n, uint32_t(tid), uint32_t(THREADS),
+      write_bits64_clear(st ? s_tx.wt : s_tx.wm, s_tx.nbits, dst, stream(0), 0, n, uint32_t(tid), uint32_t(THREADS),
                          a.status);
     else
-      write_bits64(st ? s_tx.wt : s_tx.wm, s_tx.nbits, dst, sbits, 0, n, uint32_t(tid), uint32_t(THREADS), a.status);
+      write_bits64(st ? s_tx.wt : s_tx.wm, s_tx.nbits, dst, stream(0), 0, n, uint32_t(tid), uint32_t(THREADS),
+                   a.status);
   }
   if constexpr (D >= 1) {
     if (tid < NLB && s_cnt[tid] != rsz[D][tid]) atomicOr(a.status, kErrBounds);  // counts must agree
@@ -850,7 +1183,7 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
       const int v = e + 2 - (1 << j);
       uint64_t* level = (st ? s_tx.wt : s_tx.wm) + uint64_t(j) * s_tx.stride;
       const uint64_t dst = s_table[st ? tile_wt_entry(K, j, v) : tile_wm_entry(j, v)] + runpre[e];
-      write_bits64_clear(level, s_tx.nbits, dst, sbits + j * SBW, rst[j][v], rsz[j][v], uint32_t(lane), 32u, a.status);
+      write_bits64_clear(level, s_tx.nbits, dst, stream(j), rst[j][v], rsz[j][v], uint32_t(lane), 32u, a.status);
     }
     const uint32_t total = s_cw[NC];
     int c = 0;
@@ -869,7 +1202,7 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
       const uint4 r = rec[st * ((1 << K) - 2) + (1 << j) - 2 + lo];
       uint64_t* out = reinterpret_cast<uint64_t*>(uint64_t(r.x) | (uint64_t(r.y) << 32));
       const uint32_t base = r.z, ke = r.w & 0xFFFFu, lead = (r.w >> 16) & 0xFFu, tail = r.w >> 24;
-      const uint32_t* sb = sbits + j * SBW;
+      const uint32_t* sb = stream(j);
       const uint64_t tmask = (k == nw - 1 && tail) ? ~(~0ull >> tail) : ~0ull;  // bits of the last word
       if (k >= (lead ? 1u : 0u) && k < ke) {
         out[k] = stream64(sb, base + 64 * k) & tmask;
@@ -909,10 +1242,10 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
       uint64_t* level = (st ? s_tx.wt : s_tx.wm) + uint64_t(j) * s_tx.stride;
       const uint64_t dst = s_table[st ? tile_wt_entry(K, j, v) : tile_wm_entry(j, v)] + runpre[e];
       if (a.clear_edges)
-        write_bits64_clear(level, s_tx.nbits, dst, sbits + j * SBW, rst[j][v], rsz[j][v], uint32_t(lane), 32u,
+        write_bits64_clear(level, s_tx.nbits, dst, stream(j), rst[j][v], rsz[j][v], uint32_t(lane), 32u,
                            a.status);
       else
-        write_bits64(level, s_tx.nbits, dst, sbits + j * SBW, rst[j][v], rsz[j][v], uint32_t(lane), 32u, a.status);
+        write_bits64(level, s_tx.nbits, dst, stream(j), rst[j][v], rsz[j][v], uint32_t(lane), 32u, a.status);
     }
   }
   }
@@ -937,13 +1270,14 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
 }
 
 // A launch of one pass: each CTA takes the next tile from the launch's tile
-// counter.
-template <typename KeyT, int K, bool OUT, int THREADS, int V, typename KeyO = KeyT>
-__global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : 1024) / THREADS) tile_pass_kernel(TileArgs a) {
+// counter.  The bit-plane form holds few shared bytes, so six CTAs share an
+// SM (40 registers a thread) where the key form fits four.
+template <typename KeyT, int K, bool OUT, int THREADS, int V, typename KeyO = KeyT, bool PLANES = false>
+__global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : (PLANES ? 1536 : 1024)) / THREADS) tile_pass_kernel(TileArgs a) {
   __shared__ uint32_t s_g;
   if (threadIdx.x == 0) s_g = a.tile_base + atomicAdd(a.tile_counter, 1u);
   __syncthreads();
-  tile_pass_body<KeyT, K, OUT, THREADS, V, false, KeyO>(a, s_g);
+  tile_pass_body<KeyT, K, OUT, THREADS, V, false, KeyO, PLANES>(a, s_g);
 }
 
 }  // namespace pwmgpu

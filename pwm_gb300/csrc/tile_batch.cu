@@ -260,12 +260,14 @@ __global__ void __launch_bounds__(256, 4) tile_batch_kernel(TileBatchQueue q) {
       __syncthreads();
     }
     const uint32_t g = s_item - s_base[k];
+    // passes without S_{l+K} over 1-byte keys split bit planes
+    constexpr bool PL = sizeof(KeyT) == 1;
     switch (q.variant[k]) {
       case kTileBatchK4Out: tile_pass_body<KeyT, 4, true, 256, 4, true>(s_args, g); break;
-      case kTileBatchK4: tile_pass_body<KeyT, 4, false, 256, 4, true>(s_args, g); break;
-      case kTileBatchK3: tile_pass_body<KeyT, 3, false, 256, 4, true>(s_args, g); break;
-      case kTileBatchK2: tile_pass_body<KeyT, 2, false, 256, 4, true>(s_args, g); break;
-      default: tile_pass_body<KeyT, 1, false, 256, 4, true>(s_args, g); break;
+      case kTileBatchK4: tile_pass_body<KeyT, 4, false, 256, 4, true, KeyT, PL>(s_args, g); break;
+      case kTileBatchK3: tile_pass_body<KeyT, 3, false, 256, 4, true, KeyT, PL>(s_args, g); break;
+      case kTileBatchK2: tile_pass_body<KeyT, 2, false, 256, 4, true, KeyT, PL>(s_args, g); break;
+      default: tile_pass_body<KeyT, 1, false, 256, 4, true, KeyT, PL>(s_args, g); break;
     }
   }
 }
