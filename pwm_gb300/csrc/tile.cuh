@@ -129,7 +129,16 @@ struct TileCfg {
                 "1..4 levels per pass; up to 8 in a last pass with given prefixes");
   static_assert(V % 2 == 0, "vectors are scanned in pairs");
   static constexpr size_t smem_bytes() {
-    return size_t(2) * T * sizeof(KeyT) + size_t(K) * SBW * 4 + (D >= 2 ? size_t(NVEC) * 4 : 0);
+    return size_t(T) * sizeof(KeyT) + stream_area();
+  }
+  // One key buffer (a split reads all its keys into registers before its
+  // first barrier, then scatters into the same buffer), then the K streams
+  // and the per-vector zero prefixes; before the splits the same bytes hold
+  // the finest-run counters (16 bits per thread and run).
+  static constexpr size_t stream_area() {
+    const size_t s = size_t(K) * SBW * 4 + (D >= 2 ? size_t(NVEC) * 4 : 0);
+    const size_t c = size_t(1 << D) * THREADS * 2;
+    return s > c ? s : c;
   }
   // the bit-plane form (tile_pass_body with PLANES): two sets of K planes, a
   // zero count per plane word and the 256-entry compress table
@@ -801,7 +810,7 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
   KeyT* buf0 = reinterpret_cast<KeyT*>(smem_raw);
   // K streams of SBW words (PLANES: two sets of K planes, the stream of level
   // l+j being plane j of set j % 2)
-  uint32_t* sbits = reinterpret_cast<uint32_t*>(smem_raw + (PLANES ? size_t(0) : size_t(2) * T * KB));
+  uint32_t* sbits = reinterpret_cast<uint32_t*>(smem_raw + (PLANES ? size_t(0) : size_t(T) * KB));
   uint32_t* meta = sbits + K * SBW;  // D >= 2: per vector
   auto stream = [&](int j) -> const uint32_t* { return sbits + ((PLANES ? (j & 1) * K : 0) + j) * SBW; };
 
@@ -887,8 +896,8 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
   const uint32_t smem_base = uint32_t(__cvta_generic_to_shared(smem_raw));
 
   // ---- counts of the finest runs (key_D), published before the splits -----
-  // Every thread counts its keys into its own column of 2^D counters in the
-  // second key buffer (free until the first split scatters into it).
+  // Every thread counts its keys into its own 16-bit column of 2^D counters
+  // in the stream area (free until the first split emits a stream).
   if (D >= 1 && given) {
     if (tid < NLB) {
       const uint64_t blk = a.text_blocks ? uint64_t(s_tx.blk0) + tl / a.tiles_per_block : g / a.tiles_per_block;
@@ -898,13 +907,16 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
   } else if constexpr (D >= 1 && D <= kTileMaxLevels) {
     __shared__ uint32_t s_wcnt[WARPS][NLB];
     constexpr int NB = 1 << D;
-    static_assert(size_t(NB) * THREADS * 4 <= size_t(T) * KB, "the counters fit the second key buffer");
-    uint32_t* cnt = reinterpret_cast<uint32_t*>(buf0 + T);
+    // bin b of thread t: half (t & 1) of word b * THREADS/2 + t/2 (a thread
+    // counts at most 64 keys)
+    uint32_t* cnt = sbits;
 #pragma unroll
-    for (int b = 0; b < NB; ++b) cnt[b * THREADS + tid] = 0;
+    for (int b = 0; b < NB; b += 2) cnt[b * (THREADS / 2) + tid] = 0;
     const uint32_t lo = shift - uint32_t(D - 1);  // field bit D-1 is level l
     const uint32_t fmask = uint32_t(NB - 1) & (KB < 4 ? (0xFFFFFFFFu >> (32 - 8 * KB)) >> lo : 0xFFFFFFFFu);
-    const uint32_t cbase = smem_base + uint32_t(T * KB) + uint32_t(tid) * 4u;
+    const uint32_t cbase = smem_base + uint32_t(T * KB) + uint32_t(tid >> 1) * 4u;
+    const uint32_t one = 1u << (16 * (tid & 1));
+    __syncthreads();  // the counters are cleared by other threads
 #pragma unroll
     for (int r = 0; r < V; ++r) {
       if (BATCH && r >= VP) break;
@@ -916,12 +928,12 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
       vector_fields<KeyT>(kv, lo, fmask, f);
 #pragma unroll
       for (int i = 0; i < KPL; ++i)
-        if (i < nvv) asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(cbase + f[i] * uint32_t(THREADS * 4)) : "memory");
+        if (i < nvv) asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(cbase + f[i] * uint32_t(THREADS * 2)), "r"(one) : "memory");
     }
     __syncthreads();
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
-      const uint32_t x = __reduce_add_sync(0xFFFFFFFFu, cnt[b * THREADS + tid]);
+      const uint32_t x = __reduce_add_sync(0xFFFFFFFFu, (cnt[b * (THREADS / 2) + (tid >> 1)] >> (16 * (tid & 1))) & 0xFFFFu);
       if (lane == 0) s_wcnt[warp][b] = x;
     }
     __syncthreads();
@@ -1013,7 +1025,7 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
       for (int v = 0; v < (1 << s); ++v) { rst[s][v] = run; run += rsz[s][v]; }
     }
     const uint32_t opre = vbefore - zpre;
-    const uint32_t nb = smem_base + uint32_t((cur ^ 1) * T * KB);
+    const uint32_t nb = smem_base;  // the keys are in registers: scatter into the same buffer
 #pragma unroll
     for (int r = 0; r < V; ++r) {
       if (BATCH && r >= VP) break;
@@ -1048,7 +1060,6 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
       const uint32_t zin = zb(en) - zb(st);
       rsz[s + 1][tid] = (tid >> s) ? rsz[s][v] - zin : zin;
     }
-    cur ^= 1;
   }
   }  // !PLANES
   __syncthreads();
@@ -1116,7 +1127,7 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
     constexpr int MAXR = 1 << (K - 1);      // runs of the deepest level
     constexpr int RPL = (MAXR + 31) / 32;   // runs per lane in a scan
     constexpr int NREC = 2 * ((1 << K) - 2);
-    static_assert(size_t(NREC) * 16 + size_t(NC) * (MAXR + 1) * 4 <= size_t(2) * T * KB,
+    static_assert(size_t(NREC) * 16 + size_t(NC) * (MAXR + 1) * 4 <= size_t(T) * KB,
                   "run records and word prefixes fit the key buffers");
     uint4* rec = reinterpret_cast<uint4*>(smem_raw);                   // [NREC], the key buffers are free
     uint32_t* wp = reinterpret_cast<uint32_t*>(smem_raw + NREC * 16);  // [NC][MAXR + 1]
@@ -1270,10 +1281,13 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
 }
 
 // A launch of one pass: each CTA takes the next tile from the launch's tile
-// counter.  The bit-plane form holds few shared bytes, so six CTAs share an
-// SM (40 registers a thread) where the key form fits four.
+// counter.  CTAs per SM (registers a thread): the bit-plane form 6 (40), the
+// key form over 1-byte keys 5 (48), over wider keys 4 (64; at 48 they spill
+// more and measured slower).
 template <typename KeyT, int K, bool OUT, int THREADS, int V, typename KeyO = KeyT, bool PLANES = false>
-__global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768 : (PLANES ? 1536 : 1024)) / THREADS) tile_pass_kernel(TileArgs a) {
+__global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768
+                                                                 : (PLANES ? 1536 : (sizeof(KeyT) == 1 ? 1280 : 1024))) /
+                                               THREADS) tile_pass_kernel(TileArgs a) {
   __shared__ uint32_t s_g;
   if (threadIdx.x == 0) s_g = a.tile_base + atomicAdd(a.tile_counter, 1u);
   __syncthreads();

@@ -221,10 +221,11 @@ __global__ void __launch_bounds__(1024) tile_batch_scan_kernel(const TileBatchGr
   if (tid == 1023) group_tiles[blockIdx.x] = unsigned(part[1023]);
 }
 
-// The persistent kernel: a CTA per resident slot takes items until the queue
-// is drained.  Item i of group k is tile i - base(k) of that group's pass.
+// The persistent kernel: a CTA per resident slot (5 per SM, 48 registers a
+// thread) takes items until the queue is drained.  Item i of group k is tile
+// i - base(k) of that group's pass.
 template <typename KeyT>
-__global__ void __launch_bounds__(256, 4) tile_batch_kernel(TileBatchQueue q) {
+__global__ void __launch_bounds__(256, 5) tile_batch_kernel(TileBatchQueue q) {
   __shared__ uint32_t s_base[kTileBatchMaxGroups + 1];
   __shared__ uint32_t s_item, s_gi;
   __shared__ __align__(16) TileArgs s_args;
