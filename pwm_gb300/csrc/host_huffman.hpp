@@ -22,6 +22,38 @@ struct HuffCodes {
   uint32_t levels = 0;
 };
 
+// The merges of pwm's priority queue of items T (compare: "greater" by
+// occurrences only, as std::greater on pwm's items): child[2i], child[2i+1]
+// are the nodes merge i popped (leaves are nodes 0..leaves-1, merge i makes
+// node leaves + i).  Returns the number of merges.
+template <typename T, typename Cmp, typename Make, typename Occ, typename Node>
+inline uint32_t huffman_merges(const std::vector<std::pair<uint64_t, uint64_t>>& entries, std::vector<uint32_t>& child,
+                               Cmp comp, Make make, Occ occ, Node node) {
+  std::vector<T> heap;
+  heap.reserve(entries.size());
+  auto push = [&](T it) {
+    heap.push_back(it);
+    std::push_heap(heap.begin(), heap.end(), comp);
+  };
+  auto pop = [&]() {
+    std::pop_heap(heap.begin(), heap.end(), comp);
+    const T it = heap.back();
+    heap.pop_back();
+    return it;
+  };
+  for (size_t i = 0; i < entries.size(); ++i) push(make(entries[i].second, uint32_t(i)));
+  uint32_t merges = 0;
+  while (heap.size() > 1) {
+    const T a = pop();
+    const T b = pop();
+    child[2 * merges] = node(a);
+    child[2 * merges + 1] = node(b);
+    push(make(occ(a) + occ(b), uint32_t(entries.size() + merges)));
+    ++merges;
+  }
+  return merges;
+}
+
 // entries: (symbol, frequency) in pwm's histogram order.
 inline HuffCodes build_huffman_codes(const std::vector<std::pair<uint64_t, uint64_t>>& entries, uint64_t max_symbol,
                                      bool is_tree) {
@@ -35,40 +67,38 @@ inline HuffCodes build_huffman_codes(const std::vector<std::pair<uint64_t, uint6
   // lengthens the codes of all symbols of the merged item, so a code length
   // is the depth of the symbol's leaf in the tree of merges.  The same heap
   // operations (push: push_back + push_heap, pop: pop_heap + pop_back) on
-  // (occurrences, node) pairs break ties identically; the depths come from
-  // one pass over the merge tree, parents before children.
-  struct Item {
-    uint64_t occ;
-    uint32_t node;
-    bool operator>(const Item& o) const { return occ > o.occ; }
-  };
-  std::vector<Item> heap;
-  const std::greater<Item> comp;
-  auto push = [&](Item it) {
-    heap.push_back(it);
-    std::push_heap(heap.begin(), heap.end(), comp);
-  };
-  auto pop = [&]() {
-    std::pop_heap(heap.begin(), heap.end(), comp);
-    const Item it = heap.back();
-    heap.pop_back();
-    return it;
-  };
+  // (occurrences, node) items compared by occurrences only break ties
+  // identically; the depths come from one pass over the merge tree, parents
+  // before children.  Items are one 64-bit word (occurrences above the node
+  // bits) when the text's total fits beside them: half the bytes the heap
+  // moves, the same comparisons.
   h.len.assign(nsym, 0);
   h.word.assign(nsym, 0);
   const size_t leaves = entries.size();
   std::vector<uint32_t> child(2 * leaves, 0);  // node leaves + i: children of merge i at 2i, 2i + 1
-  heap.reserve(leaves);
-  for (size_t i = 0; i < leaves; ++i) push(Item{entries[i].second, uint32_t(i)});
-  if (heap.size() == 1) ++h.len[entries[0].first];
+  if (leaves == 1) ++h.len[entries[0].first];
+  uint64_t total = 0;
+  bool fits = true;
+  for (const auto& e : entries) fits = fits && !__builtin_add_overflow(total, e.second, &total);
+  uint32_t nb = 1;  // node bits
+  while ((uint64_t(1) << nb) < 2 * leaves) ++nb;
+  fits = fits && nb < 64 && total < (uint64_t(1) << (64 - nb));
   uint32_t merges = 0;
-  while (heap.size() > 1) {
-    const Item a = pop();
-    const Item b = pop();
-    child[2 * merges] = a.node;
-    child[2 * merges + 1] = b.node;
-    push(Item{a.occ + b.occ, uint32_t(leaves + merges)});
-    ++merges;
+  if (fits) {
+    const uint64_t nmask = (uint64_t(1) << nb) - 1;
+    merges = huffman_merges<uint64_t>(
+        entries, child, [nb](uint64_t a, uint64_t b) { return (a >> nb) > (b >> nb); },
+        [nb](uint64_t occ, uint32_t node) { return (occ << nb) | node; }, [nb](uint64_t a) { return a >> nb; },
+        [nmask](uint64_t a) { return uint32_t(a & nmask); });
+  } else {
+    struct Item {
+      uint64_t occ;
+      uint32_t node;
+    };
+    merges = huffman_merges<Item>(
+        entries, child, [](const Item& a, const Item& b) { return a.occ > b.occ; },
+        [](uint64_t occ, uint32_t node) { return Item{occ, node}; }, [](const Item& a) { return a.occ; },
+        [](const Item& a) { return a.node; });
   }
   if (merges) {
     std::vector<uint64_t> depth(leaves + merges, 0);

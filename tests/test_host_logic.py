@@ -30,15 +30,25 @@ def harness(tmp_path_factory):
     return exe
 
 
-def codes(harness, text, tree):
+def text_counts(text):
     t = np.asarray(text)
     nsym = 1 << (8 * t.dtype.itemsize)
     count = np.bincount(t.astype(np.int64), minlength=nsym)
     first = np.full(nsym, (1 << 64) - 1, dtype=np.uint64)
     syms, idx = np.unique(t, return_index=True)
     first[syms.astype(np.int64)] = idx
-    inp = "%d\n" % nsym + "".join("%d %d\n" % (int(c), int(f)) for c, f in zip(count, first))
-    r = subprocess.run([harness, "huff", str(int(tree)), str(t.dtype.itemsize)], input=inp, capture_output=True,
+    return count, first
+
+
+def codes(harness, text, tree, scale=1):
+    t = np.asarray(text)
+    count, first = text_counts(t)
+    return codes_from_counts(harness, [int(c) * scale for c in count], first, t.dtype.itemsize, tree)
+
+
+def codes_from_counts(harness, count, first, width, tree):
+    inp = "%d\n" % len(count) + "".join("%d %d\n" % (int(c), int(f)) for c, f in zip(count, first))
+    r = subprocess.run([harness, "huff", str(int(tree)), str(width)], input=inp, capture_output=True,
                        text=True)
     assert r.returncode == 0, r.stderr
     lines = r.stdout.split("\n")
@@ -73,6 +83,25 @@ def test_code_tables_match_pwm_seeded(pg, harness, golden_seeded, tree):
         assert sha_words(np.array(ln, np.uint64)) == g["code_len_sha256"], case["name"]
         assert sha_words(np.array(wd, np.uint64)) == g["code_word_sha256"], case["name"]
         assert sizes == g["level_bits"], case["name"]
+
+
+@pytest.mark.parametrize("tree", [False, True])
+def test_code_tables_tie_heavy(harness, orc, tree):
+    """2^16 symbols of 1..6 occurrences each: most counts, and most merged
+    sums, tie, so the tables depend on the exact heap order of pwm's
+    priority queue.  The builder's one-word heap items must give the oracle's
+    tables, and counts scaled by 2^40 (too large for one-word items: the
+    wide-item heap, the same comparisons) the same code lengths and words."""
+    rng = np.random.default_rng(11)
+    count = rng.integers(1, 7, size=1 << 16)
+    text = np.repeat(np.arange(1 << 16, dtype=np.uint16), count)
+    rng.shuffle(text)
+    levels, sizes, ln, wd = codes(harness, text, tree)
+    o_ln, o_wd, o_sizes, o_levels = orc.huff_codes(text, tree)
+    assert levels == o_levels and sizes == [int(x) for x in o_sizes]
+    assert ln == [int(x) for x in o_ln] and wd == [int(x) for x in o_wd]
+    levels2, _, ln2, wd2 = codes(harness, text, tree, scale=1 << 40)
+    assert levels2 == levels and ln2 == ln and wd2 == wd
 
 
 def test_stream_tracker(harness):
