@@ -140,10 +140,26 @@ struct TileCfg {
     const size_t c = size_t(1 << D) * THREADS * 2;
     return s > c ? s : c;
   }
+  // run records and word prefixes of the deep write path (K > 4)
+  static constexpr size_t deep_bytes() {
+    return K > kTileMaxLevels ? size_t(2 * ((1 << K) - 2)) * 16 + size_t(2 * (K - 4)) * ((1 << (K - 1)) + 1) * 4 : 0;
+  }
   // the bit-plane form (tile_pass_body with PLANES): two sets of K planes, a
-  // zero count per plane word and the 256-entry compress table
-  static constexpr size_t plane_smem_bytes() { return size_t(2) * K * SBW * 4 + size_t(T / 32) * 4 + 256 * 4; }
+  // zero count per plane word, the 256-entry compress table, then the deep
+  // records
+  static constexpr size_t plane_area() { return size_t(2) * K * SBW * 4 + size_t(T / 32) * 4 + 256 * 4; }
+  static constexpr size_t plane_smem_bytes() { return plane_area() + deep_bytes(); }
 };
+
+// Bit q of the 8 keys of w0 (keys 0-3, key k in byte k) and w1 (keys 4-7),
+// key 0 in bit 7 of the result (higher bits are not cleared).  The 8 bits are
+// spread to byte bit 0 (w1) and bit 4 (w0) and collected by one 32x32->64-bit
+// multiply by 2^4 + 2^13 + 2^22 + 2^31: the 32 partial products land on
+// distinct bit positions, so no carries disturb bits 28-35.
+__device__ __forceinline__ uint32_t key_bits8(uint32_t w0, uint32_t w1, int q) {
+  const uint32_t t0 = (w0 >> q) & 0x01010101u, t1 = (w1 >> q) & 0x01010101u;
+  return uint32_t((uint64_t(t0 * 16u + t1) * 0x80402010ull) >> 28);
+}
 
 // Split bits of the keys of one 16-byte vector, MSB first: bit KPL-1-i is the
 // bit of key i.
@@ -154,6 +170,8 @@ __device__ __forceinline__ uint32_t vector_bits(const uint4& v, uint32_t sh) {
   uint32_t m = 0;
   if constexpr (sizeof(KeyT) == 1) {
     // byte k of a word lands at bit 3-k: ((w >> sh) & 0x01010101) * 0x80402010 >> 28
+    // (one 32-bit multiply per word measured faster in this form than
+    // key_bits8's 64-bit multiply per two words)
 #pragma unroll
     for (int q = 0; q < 4; ++q) m |= ((((w[q] >> sh) & 0x01010101u) * 0x80402010u) >> 28) << (12 - 4 * q);
   } else if constexpr (sizeof(KeyT) == 2) {
@@ -467,16 +485,6 @@ __device__ __forceinline__ void load_tile_bytes(uint4* dst, const unsigned char*
 // from a 256-entry table, so a mask word costs four table reads and a byte
 // transpose, once per word and polarity, for every plane that moves.
 
-// Bit q of the 8 keys of w0 (keys 0-3, key k in byte k) and w1 (keys 4-7),
-// key 0 in bit 7 of the result (higher bits are not cleared).  The 8 bits are
-// spread to byte bit 0 (w1) and bit 4 (w0) and collected by one 32x32->64-bit
-// multiply by 2^4 + 2^13 + 2^22 + 2^31: the 32 partial products land on
-// distinct bit positions, so no carries disturb bits 28-35.
-__device__ __forceinline__ uint32_t key_bits8(uint32_t w0, uint32_t w1, int q) {
-  const uint32_t t0 = (w0 >> q) & 0x01010101u, t1 = (w1 >> q) & 0x01010101u;
-  return uint32_t((uint64_t(t0 * 16u + t1) * 0x80402010ull) >> 28);
-}
-
 // Table entry of mask byte b: the move masks of compress toward bit 7 inside
 // the byte (Hacker's Delight 7-4 with every shift mirrored: round i moves the
 // selected bits whose remaining distance has bit i set) in bytes 0-2, the
@@ -581,7 +589,7 @@ __device__ __forceinline__ void tile_planes_splits(const TileArgs& a, const Tile
   constexpr int D = C::D, T = C::T, WARPS = C::WARPS, SBW = C::SBW, NLB = C::NLB;
   constexpr int NW = T / 32;         // plane words of a tile of V vectors per thread
   constexpr int WPT = NW / THREADS;  // plane words per thread in the splits
-  static_assert(K >= 1 && K <= kTileMaxLevels && WPT * THREADS == NW, "up to 4 levels; whole words per thread");
+  static_assert(K >= 1 && K <= kTileGivenMaxLevels && WPT * THREADS == NW, "up to 8 levels; whole words per thread");
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t NWt = BATCH ? uint32_t(THREADS * VP / 2) : uint32_t(NW);  // plane words of this tile
   const int wpt = BATCH ? (VP >= 2 ? VP / 2 : 1) : WPT;                     // of them per thread
@@ -659,11 +667,14 @@ __device__ __forceinline__ void tile_planes_splits(const TileArgs& a, const Tile
   // ---- counts of the finest runs (key_D: bit t of the digit is plane t) -----
   if constexpr (D >= 1) {
     if (given) {
-      if (tid < NLB) {
+      for (int c = tid; c < NLB; c += THREADS) {
         const uint64_t blk = a.text_blocks ? uint64_t(s_tx.blk0) + tl / a.tiles_per_block : g / a.tiles_per_block;
-        s_cnt[tid] = a.tilecnt[uint64_t(g) * NLB + tid];
-        pre[tid] = a.blockpre[blk * NLB + tid] + a.relpre[uint64_t(g) * NLB + tid];
+        s_cnt[c] = a.tilecnt[uint64_t(g) * NLB + c];
+        pre[c] = a.blockpre[blk * NLB + c] + a.relpre[uint64_t(g) * NLB + c];
       }
+    } else if constexpr (K > kTileMaxLevels) {  // deeper passes need their prefixes given
+      if (tid == 0) atomicOr(a.status, kErrBounds);
+      for (int c = tid; c < NLB; c += THREADS) s_cnt[c] = 0, pre[c] = 0;
     } else {
       // per-warp counts in the zero-count words (first written after split 0's barrier)
       uint32_t (*s_wcnt)[NLB] = reinterpret_cast<uint32_t (*)[NLB]>(zpos);
@@ -736,7 +747,9 @@ __device__ __forceinline__ void tile_planes_splits(const TileArgs& a, const Tile
       zpre += w < warp ? z : 0u;
     }
     if (tid == 0) *s_ztot = ztot;
-    if (s >= 2 && tid == 0) {
+    if constexpr (K > kTileMaxLevels) {  // up to 64 runs: a warp scan
+      if (s >= 2 && warp == 0) warp_exclusive_scan(rsz[s], rst[s], 1 << s, lane);
+    } else if (s >= 2 && tid == 0) {
       uint32_t run = 0;
       for (int v = 0; v < (1 << s); ++v) {
         rst[s][v] = run;
@@ -882,6 +895,7 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
   int cur = 0;
   if constexpr (PLANES) {
     static_assert(sizeof(KeyT) == 1 && !OUT, "bit planes: passes over 1-byte keys without S_{l+K}");
+    static_assert(K <= kTileMaxLevels || !BATCH, "batched passes take at most 4 levels");
     tile_planes_splits<K, THREADS, V, BATCH>(a, s_tx, s_sg, g, tl, tstart, n, VP, shift, given, sbits, s_cnt, pre,
                                              s_wz, &s_ztot, rsz, rst);
   } else {
@@ -1127,10 +1141,13 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
     constexpr int MAXR = 1 << (K - 1);      // runs of the deepest level
     constexpr int RPL = (MAXR + 31) / 32;   // runs per lane in a scan
     constexpr int NREC = 2 * ((1 << K) - 2);
-    static_assert(size_t(NREC) * 16 + size_t(NC) * (MAXR + 1) * 4 <= size_t(T) * KB,
-                  "run records and word prefixes fit the key buffers");
-    uint4* rec = reinterpret_cast<uint4*>(smem_raw);                   // [NREC], the key buffers are free
-    uint32_t* wp = reinterpret_cast<uint32_t*>(smem_raw + NREC * 16);  // [NC][MAXR + 1]
+    static_assert(PLANES || size_t(NREC) * 16 + size_t(NC) * (MAXR + 1) * 4 <= size_t(T) * KB,
+                  "run records and word prefixes fit the key buffer");
+    static_assert(size_t(NREC) * 16 + size_t(NC) * (MAXR + 1) * 4 == C::deep_bytes(), "deep record layout");
+    // key form: in the key buffer (free after the splits); bit planes: after the planes
+    unsigned char* deep = smem_raw + (PLANES ? C::plane_area() : size_t(0));
+    uint4* rec = reinterpret_cast<uint4*>(deep);                   // [NREC]
+    uint32_t* wp = reinterpret_cast<uint32_t*>(deep + NREC * 16);  // [NC][MAXR + 1]
     __shared__ uint32_t s_cw[NC + 1];
     const uint64_t nbits = s_tx.nbits;
     for (int c = warp; c < NC; c += WARPS) {
@@ -1281,11 +1298,11 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
 }
 
 // A launch of one pass: each CTA takes the next tile from the launch's tile
-// counter.  CTAs per SM (registers a thread): the bit-plane form 6 (40), the
-// key form over 1-byte keys 5 (48), over wider keys 4 (64; at 48 they spill
-// more and measured slower).
+// counter.  CTAs per SM (registers a thread): the bit-plane form 6 (40), 4
+// (64) for 5-8 levels; the key form over 1-byte keys 5 (48), over wider keys
+// 4 (64; at 48 they spill more and measured slower), 3 for 5-8 levels.
 template <typename KeyT, int K, bool OUT, int THREADS, int V, typename KeyO = KeyT, bool PLANES = false>
-__global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? 768
+__global__ void __launch_bounds__(THREADS, (K > kTileMaxLevels ? (PLANES ? 1024 : 768)
                                                                  : (PLANES ? 1536 : (sizeof(KeyT) == 1 ? 1280 : 1024))) /
                                                THREADS) tile_pass_kernel(TileArgs a) {
   __shared__ uint32_t s_g;

@@ -7,13 +7,15 @@ namespace pwmgpu {
 
 namespace {
 
+// 1-byte keys in the bit-plane form
 template <typename KeyT>
 void launch_deep_key(int K, const TileArgs& a, cudaStream_t s) {
+  constexpr bool PL = sizeof(KeyT) == 1;
   switch (K) {
-    case 5: launch_tile_one<KeyT, 5, false>(a, s); break;
-    case 6: launch_tile_one<KeyT, 6, false>(a, s); break;
-    case 7: launch_tile_one<KeyT, 7, false>(a, s); break;
-    default: launch_tile_one<KeyT, 8, false>(a, s); break;
+    case 5: launch_tile_one<KeyT, 5, false, KeyT, PL>(a, s); break;
+    case 6: launch_tile_one<KeyT, 6, false, KeyT, PL>(a, s); break;
+    case 7: launch_tile_one<KeyT, 7, false, KeyT, PL>(a, s); break;
+    default: launch_tile_one<KeyT, 8, false, KeyT, PL>(a, s); break;
   }
 }
 
