@@ -3,6 +3,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cstddef>
 #include <cstdint>
 #include <functional>
 #include <numeric>
@@ -152,9 +153,44 @@ inline HuffCodes build_huffman_codes(const std::vector<std::pair<uint64_t, uint6
   return h;
 }
 
+// Allocator for pwm's histogram map: nodes come from one block that lives as
+// long as the map (allocation does not change a std::unordered_map's bucket
+// sequence, so the iteration order stays pwm's).
+struct NodeArena {
+  std::vector<std::max_align_t> block;
+  size_t used = 0;  // in units of max_align_t
+};
+template <typename T>
+struct ArenaAlloc {
+  using value_type = T;
+  NodeArena* arena;
+  explicit ArenaAlloc(NodeArena* a) : arena(a) {}
+  template <typename U>
+  ArenaAlloc(const ArenaAlloc<U>& o) : arena(o.arena) {}
+  T* allocate(size_t n) {
+    const size_t units = (n * sizeof(T) + sizeof(std::max_align_t) - 1) / sizeof(std::max_align_t);
+    if (alignof(T) <= alignof(std::max_align_t) && arena->used + units <= arena->block.size()) {
+      T* p = reinterpret_cast<T*>(arena->block.data() + arena->used);
+      arena->used += units;
+      return p;
+    }
+    return static_cast<T*>(::operator new(n * sizeof(T)));
+  }
+  void deallocate(T* p, size_t) {
+    const auto* b = reinterpret_cast<const std::max_align_t*>(p);
+    if (b < arena->block.data() || b >= arena->block.data() + arena->block.size()) ::operator delete(p);
+  }
+  template <typename U>
+  bool operator==(const ArenaAlloc<U>& o) const { return arena == o.arena; }
+  template <typename U>
+  bool operator!=(const ArenaAlloc<U>& o) const { return arena != o.arena; }
+};
+
 // pwm's histogram order (include/util/histogram.hpp:39-76): ascending symbols
 // for 8-bit texts; for wider texts the iteration order of a
-// std::unordered_map filled in order of first occurrence.
+// std::unordered_map filled in order of first occurrence (a default map, as
+// pwm's, so the same buckets and rehashes; first occurrences are distinct, so
+// a radix sort of (first, symbol) gives the one insert order).
 template <typename A>
 inline std::vector<std::pair<uint64_t, uint64_t>> histogram_order(const std::vector<uint64_t>& count,
                                                                   const std::vector<uint64_t>& first, uint32_t width) {
@@ -164,13 +200,32 @@ inline std::vector<std::pair<uint64_t, uint64_t>> histogram_order(const std::vec
       if (count[c]) out.emplace_back(c, count[c]);
     return out;
   }
-  std::vector<uint64_t> syms;
+  std::vector<std::pair<uint64_t, uint64_t>> fs, tmp;  // (first occurrence, symbol)
+  uint64_t top = 0;
   for (uint64_t c = 0; c < count.size(); ++c)
-    if (count[c]) syms.push_back(c);
-  std::sort(syms.begin(), syms.end(), [&](uint64_t a, uint64_t b) { return first[a] < first[b]; });
-  std::unordered_map<A, uint64_t> m;
-  for (uint64_t c : syms) m.emplace(A(c), count[c]);
-  for (const auto& e : m) out.emplace_back(uint64_t(e.first), e.second);
+    if (count[c]) {
+      fs.emplace_back(first[c], c);
+      top |= first[c];
+    }
+  tmp.resize(fs.size());
+  std::vector<uint32_t> cnt(65537);
+  for (int sh = 0; sh < 64 && (top >> sh); sh += 16) {  // LSD, 16-bit digits
+    std::fill(cnt.begin(), cnt.end(), 0u);
+    for (const auto& p : fs) ++cnt[((p.first >> sh) & 0xFFFF) + 1];
+    for (size_t i = 0; i < 65536; ++i) cnt[i + 1] += cnt[i];
+    for (const auto& p : fs) tmp[cnt[(p.first >> sh) & 0xFFFF]++] = p;
+    fs.swap(tmp);
+  }
+  using Node = std::pair<const A, uint64_t>;
+  NodeArena arena;
+  arena.block.resize(fs.size() * ((sizeof(Node) + 2 * sizeof(void*) + sizeof(std::max_align_t) - 1) /
+                                  sizeof(std::max_align_t)) + 64);
+  {
+    std::unordered_map<A, uint64_t, std::hash<A>, std::equal_to<A>, ArenaAlloc<Node>> m{ArenaAlloc<Node>(&arena)};
+    for (const auto& p : fs) m.emplace(A(p.second), count[p.second]);
+    out.reserve(m.size());
+    for (const auto& e : m) out.emplace_back(uint64_t(e.first), e.second);
+  }
   return out;
 }
 
