@@ -249,7 +249,7 @@ def batched_vs_per_text(torch, pg, ctx, count=4096, seed=1, reps=5, per_text=Tru
             "identical_to_per_text": bool(same), "structures": ["matrix", "tree"]}
 
 
-def other_workloads(torch, pg, ctx, reps=3, only=None):
+def other_workloads(torch, pg, ctx, reps=3, only=None, cap_n=0):
     """Build times of the other configured workloads (resident text, CUDA
     events on the library's stream; the drop-in Huffman builds host to host):
     2^26 DNA-like bytes with 2 levels (matrix + tree), 2^30 bytes uniform
@@ -265,6 +265,8 @@ def other_workloads(torch, pg, ctx, reps=3, only=None):
     def timed(name, n, width, levels, dist, param, tree, rs, shards=0):
         if only is not None and name not in only:
             return None
+        if cap_n:  # a smaller case of the same workload (profiling)
+            n = min(n, cap_n)
         dtype = {1: torch.uint8, 2: torch.int16, 4: torch.int32}[width]
         t = torch.empty(n, dtype=dtype, device="cuda")
         pg.generate(dist, 3, n, width, param=param, device_ptr=t.data_ptr(), context=ctx)
@@ -603,6 +605,7 @@ def main():
     # only the named other workloads (comma-separated)
     ap.add_argument("--no-per-text", action="store_true")
     ap.add_argument("--other-only", default=None)
+    ap.add_argument("--other-n", type=int, default=0, help="cap the other workloads' sizes (profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -739,7 +742,7 @@ def main():
             line["serving"] = serving_bench(pg)
         if world == 1 and not args.no_other:
             line["other_workloads"] = other_workloads(
-                torch, pg, ctx, only=args.other_only.split(",") if args.other_only else None)
+                torch, pg, ctx, only=args.other_only.split(",") if args.other_only else None, cap_n=args.other_n)
         print(json.dumps(line))
     ds.free()
     if dist:

@@ -424,26 +424,36 @@ inline LevelTables build_tables(const std::vector<WeightedCode>& codes, uint32_t
   LevelTables t;
   t.zeros.assign(L, 0);
   t.level_bits.assign(L, 0);
-  // one walk over every (code, level): the level sizes and zeros, and per
-  // pass (l, K) the counts of its key_j values among the codes alive at l+j
-  // (key_j: code bits l..l+j-1, bit l least significant)
-  std::vector<uint32_t> pass_of(L, 0);
-  for (size_t pi = 0; pi < plan.size(); ++pi)
-    for (int j = 0; j < plan[pi].K && plan[pi].level + uint32_t(j) < L; ++j) pass_of[plan[pi].level + j] = uint32_t(pi);
+  // One walk over the codes: per code its bits reversed (code bit m at bit m),
+  // its zero bits, and per pass (l, K) the counts of its key_j values among
+  // the codes alive at l+j (key_j: code bits l..l+j-1, bit l least
+  // significant); the level sizes from the counts by length.
+  std::vector<uint64_t> by_len(L + 1, 0);
   std::vector<std::vector<uint64_t>> cnts(plan.size());
   for (size_t pi = 0; pi < plan.size(); ++pi) cnts[pi].assign(size_t((2 << plan[pi].K) - 2), 0);
   for (const auto& c : codes) {
     const uint32_t top = std::min<uint32_t>(c.len, L);
-    uint32_t key = 0;
-    for (uint32_t m = 0; m < top; ++m) {
-      const uint32_t b = code_bit(c, m);
-      t.level_bits[m] += c.freq;
-      if (!b) t.zeros[m] += c.freq;
-      const PassPlan& p = plan[pass_of[m]];
-      const uint32_t j = m - p.level + 1;  // 1..K
-      key = (j == 1 ? 0u : key) | (b << (j - 1));
-      if (m + 1 < c.len) cnts[pass_of[m]][size_t((1u << j) - 2 + key)] += c.freq;  // alive at l+j
+    by_len[top] += c.freq;
+    uint64_t rw = 0;
+    for (uint32_t m = 0; m < top; ++m) rw |= uint64_t(code_bit(c, m)) << m;
+    for (uint64_t z = ~rw & (top >= 64 ? ~uint64_t(0) : (uint64_t(1) << top) - 1); z; z &= z - 1)
+      t.zeros[__builtin_ctzll(z)] += c.freq;
+    for (size_t pi = 0; pi < plan.size(); ++pi) {
+      const uint32_t l = plan[pi].level;
+      if (l >= top) break;
+      const uint32_t chunk = uint32_t(rw >> l);
+      std::vector<uint64_t>& cn = cnts[pi];
+      for (int j = 1; j <= plan[pi].K; ++j) {
+        const uint32_t m = l + uint32_t(j) - 1;
+        if (m >= top || m + 1 >= c.len) break;  // alive at l+j
+        cn[size_t((1u << j) - 2 + (chunk & ((1u << j) - 1)))] += c.freq;
+      }
     }
+  }
+  uint64_t run = 0;
+  for (uint32_t m = L; m-- > 0;) {
+    run += by_len[m + 1];
+    t.level_bits[m] = run;
   }
   t.starts.resize(plan.size());
   for (size_t pi = 0; pi < plan.size(); ++pi) {
@@ -452,10 +462,10 @@ inline LevelTables build_tables(const std::vector<WeightedCode>& codes, uint32_t
     const std::vector<uint64_t>& cnt = cnts[pi];
     std::vector<uint64_t> st(size_t(C), 0);
     for (int j = 1; j <= p.K; ++j) {
-      uint64_t run = 0;
+      uint64_t r = 0;
       for (int v = 0; v < (1 << j); ++v) {
-        st[size_t((1 << j) - 2 + v)] = run;
-        run += cnt[size_t((1 << j) - 2 + v)];
+        st[size_t((1 << j) - 2 + v)] = r;
+        r += cnt[size_t((1 << j) - 2 + v)];
       }
     }
     t.starts[pi] = std::move(st);
@@ -463,60 +473,87 @@ inline LevelTables build_tables(const std::vector<WeightedCode>& codes, uint32_t
   if (want_tree) {
     t.seg_tree.resize(L);
     t.seg_matrix.resize(L);
-    // codes by their left-aligned code word: at every level the prefixes of
-    // the longer codes then come in prefix order, so no level sorts them
-    std::vector<std::pair<uint64_t, size_t>> by_word;  // (left-aligned code word, code)
+    // codes longer than one bit by their left-aligned code word: at every
+    // level the prefixes of the longer codes then come in prefix order, so no
+    // level sorts them.  The words are distinct (the codes are prefix-free):
+    // an LSD radix sort on their top maxlen bits, 11 bits a pass.
+    uint32_t maxlen = 1;
+    for (const auto& c : codes) maxlen = std::max<uint32_t>(maxlen, std::min<uint32_t>(c.len, 64));
+    std::vector<std::pair<uint64_t, uint32_t>> by_word, tmpw;  // (left-aligned code word, code)
     by_word.reserve(codes.size());
     for (size_t i = 0; i < codes.size(); ++i)
-      if (codes[i].len > 1) by_word.emplace_back(codes[i].word << (64 - codes[i].len), i);
-    std::sort(by_word.begin(), by_word.end());  // distinct prefix-free codes: the words differ
-    // (prefix, length, count) in that order, read sequentially by every level
+      if (codes[i].len > 1) by_word.emplace_back(codes[i].word << (64 - codes[i].len), uint32_t(i));
+    tmpw.resize(by_word.size());
+    std::vector<uint32_t> rc(2049);
+    for (uint32_t lo = 0; lo < maxlen; lo += 11) {
+      const uint32_t sh = 64 - maxlen + lo;
+      std::fill(rc.begin(), rc.end(), 0u);
+      for (const auto& pw : by_word) ++rc[((pw.first >> sh) & 2047u) + 1];
+      for (size_t i = 0; i < 2048; ++i) rc[i + 1] += rc[i];
+      for (const auto& pw : by_word) tmpw[rc[(pw.first >> sh) & 2047u]++] = pw;
+      by_word.swap(tmpw);
+    }
+    // (prefix, length, count) in that order; each level keeps the codes
+    // still alive below it
     struct Sorted {
       uint64_t word;
       uint64_t freq;
       uint32_t len;
     };
-    std::vector<Sorted> sorted;
-    sorted.reserve(by_word.size());
-    for (const auto& bw : by_word) sorted.push_back({codes[bw.second].word, codes[bw.second].freq, codes[bw.second].len});
-    std::vector<std::pair<uint64_t, uint64_t>> g;     // (prefix, count) in natural prefix order
-    std::vector<std::pair<uint64_t, size_t>> rorder;  // (bit-reversed prefix, group)
-    std::vector<uint64_t> by_rev;                     // counts by bit-reversed prefix
+    std::vector<Sorted> alive, next;
+    alive.reserve(by_word.size());
+    for (const auto& bw : by_word) alive.push_back({codes[bw.second].word, codes[bw.second].freq, codes[bw.second].len});
+    std::vector<uint64_t> gp, gc, gr, by_rev;  // per group of a level: prefix, count, bit-reversed prefix
     for (uint32_t m = 1; m < L; ++m) {
-      // prefix groups of level m among codes longer than m
-      g.clear();
-      for (const Sorted& c : sorted) {
-        if (c.len <= m) continue;
+      // prefix groups of level m among the codes longer than m
+      gp.clear();
+      gc.clear();
+      next.clear();
+      for (const Sorted& c : alive) {
         const uint64_t pfx = c.word >> (c.len - m);
-        if (!g.empty() && g.back().first == pfx) g.back().second += c.freq;
-        else g.emplace_back(pfx, c.freq);
+        if (!gp.empty() && gp.back() == pfx) gc.back() += c.freq;
+        else {
+          gp.push_back(pfx);
+          gc.push_back(c.freq);
+        }
+        if (c.len > m + 1) next.push_back(c);
       }
-      std::vector<uint64_t> tree_start(g.size()), matrix_start(g.size());
-      uint64_t run = 0;
-      for (size_t i = 0; i < g.size(); ++i) { tree_start[i] = run; run += g[i].second; }
-      if (m <= 20) {
+      alive.swap(next);
+      const size_t G = gp.size();
+      std::vector<uint64_t> st(G), sm(G);
+      run = 0;
+      for (size_t i = 0; i < G; ++i) {
+        st[i] = run;
+        run += gc[i];
+      }
+      gr.resize(G);
+      for (size_t i = 0; i < G; ++i) gr[i] = rev_bits_host(gp[i], m);
+      if (m <= 20 && (size_t(1) << m) <= 16 * G) {
         // the matrix orders the groups by bit-reversed prefix: counts
         // scattered to their reversed prefixes, exclusive sums in that order
         by_rev.assign(size_t(1) << m, 0);
-        for (const auto& x : g) by_rev[rev_bits_host(x.first, m)] = x.second;
+        for (size_t i = 0; i < G; ++i) by_rev[gr[i]] = gc[i];
         run = 0;
         for (auto& x : by_rev) {
           const uint64_t v = x;
           x = run;
           run += v;
         }
-        for (size_t i = 0; i < g.size(); ++i) matrix_start[i] = by_rev[rev_bits_host(g[i].first, m)];
-      } else {
-        rorder.resize(g.size());
-        for (size_t i = 0; i < g.size(); ++i) rorder[i] = {rev_bits_host(g[i].first, m), i};
-        std::sort(rorder.begin(), rorder.end());
+        for (size_t i = 0; i < G; ++i) sm[i] = by_rev[gr[i]];
+      } else {  // few groups for the reversed-prefix range: sort them
+        std::vector<std::pair<uint64_t, size_t>> ro(G);
+        for (size_t i = 0; i < G; ++i) ro[i] = {gr[i], i};
+        std::sort(ro.begin(), ro.end());
         run = 0;
-        for (const auto& r : rorder) { matrix_start[r.second] = run; run += g[r.second].second; }
+        for (const auto& r : ro) {
+          sm[r.second] = run;
+          run += gc[r.second];
+        }
       }
-      std::vector<uint64_t> st, sm;
-      for (size_t i = 0; i < g.size(); ++i)
-        if (g[i].second) { st.push_back(tree_start[i]); sm.push_back(matrix_start[i]); }
-      if (st.empty()) { st.push_back(0); sm.push_back(0); }
+      if (G == 0) {
+        st.push_back(0);
+        sm.push_back(0);
+      }
       t.seg_tree[m] = std::move(st);
       t.seg_matrix[m] = std::move(sm);
     }
