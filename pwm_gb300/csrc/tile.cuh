@@ -129,7 +129,10 @@ struct TileCfg {
                 "1..4 levels per pass; up to 8 in a last pass with given prefixes");
   static_assert(V % 2 == 0, "vectors are scanned in pairs");
   static constexpr size_t smem_bytes() {
-    return size_t(T) * sizeof(KeyT) + stream_area();
+    return deep_offset() + (K > kTileMaxLevels ? 0 : deep_bytes());
+  }
+  // key form, K <= 4: the run records after the streams, 16-byte aligned
+  static constexpr size_t deep_offset() { return (size_t(T) * sizeof(KeyT) + stream_area() + 15) & ~size_t(15);
   }
   // One key buffer (a split reads all its keys into registers before its
   // first barrier, then scatters into the same buffer), then the K streams
@@ -140,9 +143,16 @@ struct TileCfg {
     const size_t c = size_t(1 << D) * THREADS * 2;
     return s > c ? s : c;
   }
-  // run records and word prefixes of the deep write path (K > 4)
+  // Levels 1..K-1 written word-parallel (tile_pass_body): passes of 5..8
+  // levels (levels 1..JW still a warp per run), and passes over 2- and
+  // 4-byte keys, whose smaller tiles give runs too short for a warp each
+  // (measured: 16-bit, 16 levels 4.48 -> 4.38 ms of passes; 32-bit, 20 levels
+  // 1.64 -> 1.58; slower over 1-byte keys: 4.71 -> 4.80 ms at 8 levels).
+  static constexpr bool WORD_PARALLEL = K > kTileMaxLevels || (K > 1 && sizeof(KeyT) > 1);
+  static constexpr int JW = K > kTileMaxLevels ? 3 : 0;
+  // run records and word prefixes of the word-parallel writes
   static constexpr size_t deep_bytes() {
-    return K > kTileMaxLevels ? size_t(2 * ((1 << K) - 2)) * 16 + size_t(2 * (K - 4)) * ((1 << (K - 1)) + 1) * 4 : 0;
+    return WORD_PARALLEL ? size_t(2 * ((1 << K) - 2)) * 16 + size_t(2 * (K - 1 - JW)) * ((1 << (K - 1)) + 1) * 4 : 0;
   }
   // the bit-plane form (tile_pass_body with PLANES): two sets of K planes, a
   // zero count per plane word, the 256-entry compress table, then the deep
@@ -1122,30 +1132,32 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
     runpre[tid] = p;
   }
   __syncthreads();
-  if constexpr (K > kTileMaxLevels) {
+  if constexpr (C::WORD_PARALLEL) {
     // Levels 1..K-1 of both structures, word-parallel: a deep level has up to
-    // 2^(K-1) runs, most of them a few words long, so instead of a warp per
-    // run every thread takes destination words of the concatenated runs.
-    // Per (structure, level) list one warp scans the runs' word counts and
-    // stores a 16-byte record per run (first destination word, stream bit
-    // of that word, last whole word, lead and tail bits); a thread then
-    // finds its word's run by binary search.  The levels are not zeroed
-    // before this pass: a word shared with other runs is cleared in this
-    // run's bits, then set (writers of one word touch disjoint bits, so the
-    // atomics commute, and the runs of a level cover all of its bits).
-    // Levels 1..JW (runs of 32 words and more on average) go a warp per
-    // run, the deeper levels word-parallel.
-    constexpr int JW = 3;
+    // 2^(K-1) runs, most of them a few words long (and the tiles of 2- and
+    // 4-byte keys are short), so instead of a warp per run every thread
+    // takes destination words of the concatenated runs.  Per (structure,
+    // level) list one warp scans the runs' word counts and stores a 16-byte
+    // record per run (first destination word, stream bit of that word, last
+    // whole word, lead and tail bits); a thread then finds its word's run by
+    // binary search.  A word shared with other runs is cleared in this run's
+    // bits, then set, whether or not the level was zeroed (writers of one
+    // word touch disjoint bits, so the atomics commute, and the runs of a
+    // level cover all of its bits).  In passes of 5..8 levels, levels 1..JW
+    // (runs of 32 words and more on average) go a warp per run.
+    constexpr int JW = C::JW;
     constexpr int NCJ = K - 1 - JW;         // word-parallel levels per structure
     constexpr int NC = 2 * NCJ;             // lists
     constexpr int MAXR = 1 << (K - 1);      // runs of the deepest level
     constexpr int RPL = (MAXR + 31) / 32;   // runs per lane in a scan
     constexpr int NREC = 2 * ((1 << K) - 2);
-    static_assert(PLANES || size_t(NREC) * 16 + size_t(NC) * (MAXR + 1) * 4 <= size_t(T) * KB,
+    static_assert(PLANES || K <= kTileMaxLevels || size_t(NREC) * 16 + size_t(NC) * (MAXR + 1) * 4 <= size_t(T) * KB,
                   "run records and word prefixes fit the key buffer");
     static_assert(size_t(NREC) * 16 + size_t(NC) * (MAXR + 1) * 4 == C::deep_bytes(), "deep record layout");
-    // key form: in the key buffer (free after the splits); bit planes: after the planes
-    unsigned char* deep = smem_raw + (PLANES ? C::plane_area() : size_t(0));
+    // bit planes: after the planes; key form: 5..8 levels in the key buffer
+    // (free after the splits), up to 4 after the streams
+    unsigned char* deep = smem_raw + (PLANES ? C::plane_area() : (K > kTileMaxLevels ? size_t(0) : C::deep_offset()));
+    static_assert(C::plane_area() % 16 == 0 && C::deep_offset() % 16 == 0, "16-byte records");
     uint4* rec = reinterpret_cast<uint4*>(deep);                   // [NREC]
     uint32_t* wp = reinterpret_cast<uint32_t*>(deep + NREC * 16);  // [NC][MAXR + 1]
     __shared__ uint32_t s_cw[NC + 1];
@@ -1239,6 +1251,24 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
         const uint64_t mask = (k ? ~0ull : (~0ull >> lead)) & tmask;
         atomicAnd(reinterpret_cast<unsigned long long*>(out + k), (unsigned long long)~mask);
         atomicOr(reinterpret_cast<unsigned long long*>(out + k), (unsigned long long)(val & mask));
+      }
+    }
+    if constexpr (OUT) {
+      const KeyT* cb = buf0 + cur * T;
+#pragma unroll 1
+      for (int v = warp; v < (1 << K); v += WARPS) {
+        const uint32_t len = rsz[D][v];
+        if (len == 0) continue;
+        const uint64_t dst = s_table[tile_out_entry(K, v)] + pre[v];
+        if (dst + len > a.out_size) {
+          if (lane == 0) atomicOr(a.status, kErrBounds);
+          continue;
+        }
+        if constexpr (sizeof(KeyO) == sizeof(KeyT))
+          write_key_run(reinterpret_cast<unsigned char*>(static_cast<KeyT*>(a.out) + dst),
+                        reinterpret_cast<const unsigned char*>(cb + rst[D][v]), len * uint32_t(KB));
+        else
+          write_key_run_narrow<KeyT, KeyO>(static_cast<KeyO*>(a.out) + dst, cb + rst[D][v], len);
       }
     }
   } else {
