@@ -493,32 +493,36 @@ inline LevelTables build_tables(const std::vector<WeightedCode>& codes, uint32_t
       for (const auto& pw : by_word) tmpw[rc[(pw.first >> sh) & 2047u]++] = pw;
       by_word.swap(tmpw);
     }
-    // (prefix, length, count) in that order; each level keeps the codes
-    // still alive below it
-    struct Sorted {
-      uint64_t word;
-      uint64_t freq;
-      uint32_t len;
-    };
-    std::vector<Sorted> alive, next;
-    alive.reserve(by_word.size());
-    for (const auto& bw : by_word) alive.push_back({codes[bw.second].word, codes[bw.second].freq, codes[bw.second].len});
-    std::vector<uint64_t> gp, gc, gr, by_rev;  // per group of a level: prefix, count, bit-reversed prefix
-    for (uint32_t m = 1; m < L; ++m) {
-      // prefix groups of level m among the codes longer than m
-      gp.clear();
-      gc.clear();
-      next.clear();
-      for (const Sorted& c : alive) {
-        const uint64_t pfx = c.word >> (c.len - m);
-        if (!gp.empty() && gp.back() == pfx) gc.back() += c.freq;
-        else {
-          gp.push_back(pfx);
-          gc.push_back(c.freq);
+    // The prefix groups of every level in one walk: with the codes in that
+    // order, code i (longer than m) starts a new group at level m exactly
+    // when m > b_i = min(common prefix with code i-1, length of code i-1 - 1)
+    // -- a code between two codes sharing m bits would share them too and,
+    // being no longer than m, be a prefix of them (the codes are prefix-free).
+    std::vector<std::vector<uint64_t>> gpl(L), gcl(L);  // per level: group prefixes and counts
+    {
+      uint64_t prev_lw = 0;
+      uint32_t prev_len = 0;
+      for (size_t q = 0; q < by_word.size(); ++q) {
+        const WeightedCode& c = codes[by_word[q].second];
+        const uint64_t lw = by_word[q].first;
+        const uint32_t b = q == 0 ? 0u : std::min<uint32_t>(uint32_t(__builtin_clzll(prev_lw ^ lw)), prev_len - 1);
+        const uint32_t top = std::min<uint32_t>(c.len, L);  // levels 1..top-1 hold the code
+        for (uint32_t m = 1; m < top; ++m) {
+          if (m > b) {
+            gpl[m].push_back(lw >> (64 - m));
+            gcl[m].push_back(c.freq);
+          } else {
+            gcl[m].back() += c.freq;
+          }
         }
-        if (c.len > m + 1) next.push_back(c);
+        prev_lw = lw;
+        prev_len = c.len;
       }
-      alive.swap(next);
+    }
+    std::vector<uint64_t> gr, by_rev;  // per group of a level: bit-reversed prefix
+    for (uint32_t m = 1; m < L; ++m) {
+      const std::vector<uint64_t>& gp = gpl[m];
+      const std::vector<uint64_t>& gc = gcl[m];
       const size_t G = gp.size();
       std::vector<uint64_t> st(G), sm(G);
       run = 0;
