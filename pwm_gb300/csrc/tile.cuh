@@ -483,6 +483,46 @@ __device__ __forceinline__ void load_tile_bytes(uint4* dst, const unsigned char*
   }
 }
 
+// A contiguous tile by one TMA bulk copy (cp.async.bulk) into shared memory:
+// thread 0 arms the mbarrier with the byte count and issues the copy, every
+// thread waits for the barrier's first phase.  Both addresses must be
+// 16-byte aligned and `bytes` a multiple of 16 (the caller checks).  The
+// wait is bounded: after `spin_limit` polls kErrTimeout is recorded and the
+// thread waits once more (bounded) for the copy in flight before it goes on.
+__device__ __forceinline__ void bulk_load_tile(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                               uint32_t spin_limit, uint32_t* status) {
+  const uint32_t b = uint32_t(__cvta_generic_to_shared(bar));
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     uint32_t(__cvta_generic_to_shared(dst))),
+                 "l"(src), "r"(bytes), "r"(b)
+                 : "memory");
+  }
+  auto done = [&]() {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(b)
+        : "memory");
+    return ok != 0;
+  };
+  uint32_t spins = 0;
+  while (!done()) {
+    if (++spins >= spin_limit) {
+      atomicOr(status, kErrTimeout);
+      for (uint32_t k = 0; k < spin_limit && !done(); ++k) __nanosleep(256);
+      break;
+    }
+  }
+}
+
 // ---- bit planes (the last pass of 1-byte keys) -----------------------------
 // A plane holds one level's bit of every key of the tile, 32 keys per word,
 // the first key in bit 31.  A 1-bit split of the keys then becomes a stable
@@ -909,8 +949,18 @@ __device__ __forceinline__ void tile_pass_body(const TileArgs& a, uint32_t g_in)
     tile_planes_splits<K, THREADS, V, BATCH>(a, s_tx, s_sg, g, tl, tstart, n, VP, shift, given, sbits, s_cnt, pre,
                                              s_wz, &s_ztot, rsz, rst);
   } else {
-  load_tile_bytes<THREADS>(reinterpret_cast<uint4*>(buf0),
-                           static_cast<const unsigned char*>(a.in) + (s_sg.in_begin + tstart) * KB, n * KB);
+  {
+    const unsigned char* src = static_cast<const unsigned char*>(a.in) + (s_sg.in_begin + tstart) * KB;
+    const uint32_t bytes = n * uint32_t(KB);
+    // a 16-byte aligned tile of whole 16-byte blocks (every tile of a first
+    // pass but the text's last): one TMA bulk copy; otherwise vector loads
+    if (!BATCH && (reinterpret_cast<uintptr_t>(src) & 15) == 0 && (bytes & 15) == 0 && bytes) {
+      __shared__ __align__(8) uint64_t s_bar;
+      bulk_load_tile(buf0, src, bytes, &s_bar, a.spin_limit, a.status);
+    } else {
+      load_tile_bytes<THREADS>(reinterpret_cast<uint4*>(buf0), src, bytes);
+    }
+  }
   if (tid == 0) {
     rsz[0][0] = n;
     rst[0][0] = 0;
