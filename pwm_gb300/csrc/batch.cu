@@ -42,7 +42,13 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hist_kernel(const T* __re
   const uint32_t mine = threadIdx.x % copies, lane = threadIdx.x & 31;
   const uint32_t D = c.D, dsh = t.levels - c.D;  // the digit: symbol bits [L-D, L)
   const uint32_t ntiles = D ? uint32_t((c.len + (uint64_t(1) << c.log2T) - 1) >> c.log2T) : 0u;
-  for (uint32_t i = threadIdx.x; i < bins * copies; i += kBatchThreads) h[i] = 0;
+  // Up to 16 bins: one counter per (tile, bin, lane) serves both the text's
+  // histogram and the tiles' finest-run counts (each a sum over bins), one
+  // shared atomic per symbol; else a text histogram (per-thread copies) and
+  // the tiles' digit counters.
+  const bool by_tile = D && bins <= 16;
+  if (!by_tile)
+    for (uint32_t i = threadIdx.x; i < bins * copies; i += kBatchThreads) h[i] = 0;
   for (uint32_t i = threadIdx.x; i < ntiles * 16 * 32; i += kBatchThreads) tc[i] = 0;
   __syncthreads();
   // Branch-free: every symbol counts into bin (symbol mod 2^L), and `seen`
@@ -55,6 +61,10 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hist_kernel(const T* __re
   const uint32_t lmask = sizeof(T) == 4 ? bmask : min(bmask, (1u << (8 * sizeof(T))) - 1u);
   const uint32_t tcb = uint32_t(__cvta_generic_to_shared(tc)) + lane * 4;
   auto count = [&](uint32_t s, uint32_t i) {  // symbol s at chunk position i
+    if (by_tile) {
+      asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(tcb + (((i >> c.log2T) * 16 + (s & bmask)) << 7)) : "memory");
+      return;
+    }
     atomicAdd(&h[(s & bmask) * copies + mine], 1u);
     if (D) {
       const uint32_t cn = __brev((s >> dsh) & ((1u << D) - 1u)) >> (32 - D);
@@ -90,6 +100,43 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hist_kernel(const T* __re
   if ((seen & ~bmask) || (seen_w & ~(lanes * lmask))) atomicOr(status, kErrSymbol);
   __syncthreads();
   unsigned long long* out = hist + t.hist_off;
+  if (by_tile) {
+    // per (tile, bin) the lanes' sum into lane column 0, then the text's
+    // histogram over the tiles and each tile's counters over the bins of
+    // each digit (the slots of unused tiles and bins are zero)
+    for (uint32_t e = threadIdx.x; e < ntiles * 16; e += kBatchThreads) {
+      uint32_t sum = 0;
+      for (uint32_t l = 0; l < 32; ++l) sum += tc[e * 32 + l];
+      h[e] = sum;  // h (free in this mode): [tile][bin]
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < bins; b += kBatchThreads) {
+      uint32_t sum = 0;
+      for (uint32_t tile = 0; tile < ntiles; ++tile) sum += h[tile * 16 + b];
+      if (sum) atomicAdd(&out[b], (unsigned long long)sum);
+    }
+    const uint32_t nb = 1u << D;
+    for (uint32_t e = threadIdx.x; e < ntiles * nb; e += kBatchThreads) {
+      const uint32_t tile = e >> D, cn = e & (nb - 1);
+      uint32_t sum = 0;
+      for (uint32_t b = 0; b < bins; ++b)
+        if ((__brev((b >> dsh) & (nb - 1u)) >> (32 - D)) == cn) sum += h[tile * 16 + b];
+      tilecnt[c.cnt_off + e] = sum;
+      tc[(tile * 16 + cn) * 32 + ((e + 1) & 31)] = sum;  // read back below by the prefix loop
+    }
+    __syncthreads();
+    if (threadIdx.x < nb) {
+      const uint32_t cn = threadIdx.x;
+      uint32_t run = 0;
+      for (uint32_t tile = 0; tile < ntiles; ++tile) {
+        const uint32_t e = tile * nb + cn;
+        relpre[c.cnt_off + e] = run;
+        run += tc[(tile * 16 + cn) * 32 + ((e + 1) & 31)];
+      }
+      blocksum[c.blk_off + cn] = run;
+    }
+    return;
+  }
   for (uint32_t s = threadIdx.x; s < bins; s += kBatchThreads) {
     uint32_t sum = 0;
     for (uint32_t k = 0; k < copies; ++k) sum += h[s * copies + k];
