@@ -17,8 +17,9 @@
 // one l-bit prefix group of S_l, whose elements share key_l and therefore
 // land in every later level at group-specific run starts of both structures.
 // Per tile the kernel
-//   * loads the tile into shared memory (16-byte vectors; misaligned
-//     segments are realigned with funnel shifts);
+//   * loads the tile into shared memory (one TMA bulk copy when the tile is
+//     16-byte aligned whole blocks, else 16-byte vectors, misaligned segments
+//     realigned with funnel shifts);
 //   * runs D = K (or K-1 in the last pass) CTA-wide stable 1-bit splits in
 //     LSD order.  Each thread keeps V 16-byte vectors of keys in registers in
 //     a striped layout (conflict-free 128-bit shared loads), extracts the
@@ -35,7 +36,9 @@
 //     coalesced load per counter, 256 predecessors per round trip);
 //   * writes every run of every level to the matrix and the tree at
 //     table start + look-back prefix in 64-bit words, and the runs of
-//     S_{l+K} to the next pass's input (one warp per run, round-robin).
+//     S_{l+K} to the next pass's input (one warp per run, round-robin; the
+//     level words word-parallel in passes of 5-8 levels and over 2- and
+//     4-byte keys).
 // A pass that writes no S_{l+K} over 1-byte keys (the last pass of every
 // text whose remaining levels fit a byte) runs the splits on bit planes
 // instead (tile_planes_splits): the K bits of every key as K planes of 32-key
