@@ -490,8 +490,10 @@ __device__ __forceinline__ void load_tile_bytes(uint4* dst, const unsigned char*
 // thread 0 arms the mbarrier with the byte count and issues the copy, every
 // thread waits for the barrier's first phase.  Both addresses must be
 // 16-byte aligned and `bytes` a multiple of 16 (the caller checks).  The
-// wait is bounded: after `spin_limit` polls kErrTimeout is recorded and the
-// thread waits once more (bounded) for the copy in flight before it goes on.
+// wait is bounded (the context's limit, at least 2^16 polls): on expiry
+// kErrTimeout is recorded and the thread waits once more (bounded, ~1 s) for
+// the copy in flight, so that no copy outlives the tile; the tile then goes
+// on (its results are void, the status says so) and publishes its prefixes.
 __device__ __forceinline__ void bulk_load_tile(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
                                                uint32_t spin_limit, uint32_t* status) {
   const uint32_t b = uint32_t(__cvta_generic_to_shared(bar));
@@ -516,12 +518,12 @@ __device__ __forceinline__ void bulk_load_tile(void* dst, const void* src, uint3
         : "memory");
     return ok != 0;
   };
-  uint32_t spins = 0;
-  while (!done()) {
-    if (++spins >= spin_limit) {
+  const uint32_t limit = spin_limit > (1u << 16) ? spin_limit : (1u << 16);
+  for (uint32_t spins = 0; !done();) {
+    if (++spins >= limit) {
       atomicOr(status, kErrTimeout);
-      for (uint32_t k = 0; k < spin_limit && !done(); ++k) __nanosleep(256);
-      break;
+      for (uint32_t k = 0; k < (1u << 20) && !done(); ++k) __nanosleep(1000);
+      return;
     }
   }
 }
