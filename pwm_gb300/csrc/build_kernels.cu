@@ -493,9 +493,22 @@ __global__ void regroup_kernel(const uint64_t* __restrict__ matrix_level, uint64
     const uint64_t wp = w << 6, end = min(wp + 64, nbits);
     uint64_t pos = wp, acc = 0;
     while (pos < end) {
-      while (pos >= seg_end) {  // advance to the segment holding pos (empty ones are skipped)
-        ++seg;
-        seg_start = seg_end;
+      if (pos >= seg_end) {
+        // the last segment starting at or before pos, searched from the next
+        // one by galloping (runs of empty segments cost their logarithm)
+        uint64_t a = seg + 1, b = a + 1, step = 1;  // seg_tree[a] == seg_end <= pos
+        while (b < nseg && seg_tree[b] <= pos) {
+          a = b;
+          step <<= 1;
+          b = a + step;
+        }
+        b = min(b, nseg);
+        while (b - a > 1) {
+          const uint64_t mid = (a + b) >> 1;
+          if (seg_tree[mid] <= pos) a = mid; else b = mid;
+        }
+        seg = a;
+        seg_start = seg_tree[seg];
         seg_end = seg + 1 < nseg ? seg_tree[seg + 1] : nbits;
       }
       const uint64_t stop = min(end, seg_end);
@@ -509,6 +522,173 @@ __global__ void regroup_kernel(const uint64_t* __restrict__ matrix_level, uint64
       pos = stop;
     }
     tree_level[w] = acc;
+  }
+}
+
+// The same for levels of many small (or empty) segments: one thread per tree
+// bit, each searching its segment on its own, so that no thread walks a long
+// chain of segments.  A warp covers 32 consecutive bits (one half of a word,
+// written as the word's upper or lower 32 bits); the grid covers every word.
+__global__ void __launch_bounds__(256) regroup_bits_kernel(const uint64_t* __restrict__ matrix_level,
+                                                           uint32_t* __restrict__ tree_halves, uint64_t nbits,
+                                                           const uint64_t* __restrict__ seg_tree,
+                                                           const uint64_t* __restrict__ seg_matrix, uint64_t nseg,
+                                                           uint32_t* status) {
+  const uint64_t pos = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  bool bit = false;
+  if (pos < nbits) {
+    uint64_t lo = 0, hi = nseg;
+    while (hi - lo > 1) {
+      const uint64_t mid = (lo + hi) >> 1;
+      if (seg_tree[mid] <= pos) lo = mid; else hi = mid;
+    }
+    const uint64_t src = seg_matrix[lo] + (pos - seg_tree[lo]);
+    if (src >= nbits) atomicOr(status, kErrBounds);  // inconsistent segments: never read out of range
+    else bit = (matrix_level[src >> 6] >> (63 - (src & 63))) & 1u;
+  }
+  const uint32_t m = __ballot_sync(0xFFFFFFFFu, bit);
+  // bits pos..pos+31 of a word are its upper half when pos % 64 < 32
+  // (the first bit of a word is its most significant)
+  if ((threadIdx.x & 31) == 0) tree_halves[2 * (pos >> 6) + ((pos & 32) ? 0 : 1)] = __brev(m);
+}
+
+// ---- the regroup's segments, on the device -------------------------------------
+// Level m of the tree holds the groups of the m-bit natural prefixes in
+// natural order; the matrix level holds the same groups in key order (the
+// prefix bit-reversed, as pwm's matrix orders level m by the bit of level m-1
+// first); both keep text order inside a group.  So group p starts in the tree
+// at the exclusive prefix of the level's counts in natural order, and in the
+// matrix at the exclusive prefix, in key order, at rev_m(p).  Blocks take
+// chunks of kSegChunk groups of every listed level: chunk sums, then each
+// level's chunk offsets, then the starts.
+constexpr uint32_t kSegThreads = 256, kSegPer = 8, kSegChunk = kSegThreads * kSegPer;
+constexpr uint32_t kSegMaxLevels = 32;
+
+struct RegroupSegPlan {
+  uint32_t count;
+  uint32_t m[kSegMaxLevels];
+  uint32_t chunk0[kSegMaxLevels + 1];  // first block of each level; chunk0[count]: all blocks
+  uint64_t out[kSegMaxLevels];         // tree starts at out[i], matrix starts at out[i] + 2^m
+};
+
+__device__ __forceinline__ uint32_t seg_rev(uint32_t x, uint32_t m) { return __brev(x) >> (32 - m); }
+
+__device__ __forceinline__ uint32_t seg_level_of(const RegroupSegPlan& p, uint32_t b) {
+  uint32_t i = 0;
+  while (i + 1 < p.count && p.chunk0[i + 1] <= b) ++i;
+  return i;
+}
+
+// Exclusive scan of the pairs (a, b) over the block, in place; ta, tb: totals.
+__device__ __forceinline__ void seg_block_scan(uint64_t& a, uint64_t& b, uint64_t& ta, uint64_t& tb) {
+  __shared__ uint64_t wa[kSegThreads / 32], wb[kSegThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint64_t ia = a, ib = b;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint64_t ya = __shfl_up_sync(0xFFFFFFFFu, ia, o), yb = __shfl_up_sync(0xFFFFFFFFu, ib, o);
+    if (lane >= o) {
+      ia += ya;
+      ib += yb;
+    }
+  }
+  if (lane == 31) {
+    wa[warp] = ia;
+    wb[warp] = ib;
+  }
+  __syncthreads();
+  uint64_t oa = 0, ob = 0;
+  ta = tb = 0;
+#pragma unroll
+  for (int w = 0; w < int(kSegThreads / 32); ++w) {
+    if (w < warp) {
+      oa += wa[w];
+      ob += wb[w];
+    }
+    ta += wa[w];
+    tb += wb[w];
+  }
+  a = oa + ia - a;
+  b = ob + ib - b;
+  __syncthreads();  // wa, wb free for the next call
+}
+
+__global__ void __launch_bounds__(kSegThreads) regroup_seg_sums_kernel(const uint64_t* __restrict__ flat,
+                                                                       RegroupSegPlan p, uint64_t* __restrict__ sums) {
+  const uint32_t i = seg_level_of(p, blockIdx.x);
+  const uint32_t m = p.m[i];
+  const uint64_t ng = 1ull << m;
+  const uint64_t* c = flat + (ng - 1);
+  const uint64_t x0 = uint64_t(blockIdx.x - p.chunk0[i]) * kSegChunk + threadIdx.x * kSegPer;
+  uint64_t a = 0, b = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < kSegPer; ++k) {
+    const uint64_t x = x0 + k;
+    if (x < ng) {
+      a += c[x];
+      b += c[seg_rev(uint32_t(x), m)];
+    }
+  }
+  uint64_t ta, tb;
+  seg_block_scan(a, b, ta, tb);
+  if (threadIdx.x == 0) {
+    sums[2 * uint64_t(blockIdx.x)] = ta;
+    sums[2 * uint64_t(blockIdx.x) + 1] = tb;
+  }
+}
+
+// One block per level: its chunk sums become exclusive chunk offsets.
+__global__ void __launch_bounds__(kSegThreads) regroup_seg_offsets_kernel(RegroupSegPlan p,
+                                                                          uint64_t* __restrict__ sums) {
+  const uint32_t c0 = p.chunk0[blockIdx.x], c1 = p.chunk0[blockIdx.x + 1];
+  uint64_t carry_a = 0, carry_b = 0;
+  for (uint32_t base = c0; base < c1; base += kSegThreads) {
+    const uint32_t k = base + threadIdx.x;
+    uint64_t a = k < c1 ? sums[2 * uint64_t(k)] : 0, b = k < c1 ? sums[2 * uint64_t(k) + 1] : 0;
+    uint64_t ta, tb;
+    seg_block_scan(a, b, ta, tb);
+    if (k < c1) {
+      sums[2 * uint64_t(k)] = carry_a + a;
+      sums[2 * uint64_t(k) + 1] = carry_b + b;
+    }
+    carry_a += ta;
+    carry_b += tb;
+  }
+}
+
+__global__ void __launch_bounds__(kSegThreads) regroup_seg_write_kernel(const uint64_t* __restrict__ flat,
+                                                                        RegroupSegPlan p,
+                                                                        const uint64_t* __restrict__ sums,
+                                                                        uint64_t* __restrict__ out) {
+  const uint32_t i = seg_level_of(p, blockIdx.x);
+  const uint32_t m = p.m[i];
+  const uint64_t ng = 1ull << m;
+  const uint64_t* c = flat + (ng - 1);
+  uint64_t* st = out + p.out[i];
+  uint64_t* sm = st + ng;
+  const uint64_t x0 = uint64_t(blockIdx.x - p.chunk0[i]) * kSegChunk + threadIdx.x * kSegPer;
+  uint64_t va[kSegPer], vb[kSegPer], a = 0, b = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < kSegPer; ++k) {
+    const uint64_t x = x0 + k;
+    va[k] = x < ng ? c[x] : 0;
+    vb[k] = x < ng ? c[seg_rev(uint32_t(x), m)] : 0;
+    a += va[k];
+    b += vb[k];
+  }
+  uint64_t ta, tb;
+  seg_block_scan(a, b, ta, tb);
+  a += sums[2 * uint64_t(blockIdx.x)];
+  b += sums[2 * uint64_t(blockIdx.x) + 1];
+#pragma unroll
+  for (uint32_t k = 0; k < kSegPer; ++k) {
+    const uint64_t x = x0 + k;
+    if (x < ng) {
+      st[x] = a;                         // group x (natural) in the tree
+      sm[seg_rev(uint32_t(x), m)] = b;  // group rev(x), key position x, in the matrix
+    }
+    a += va[k];
+    b += vb[k];
   }
 }
 
@@ -677,17 +857,21 @@ __global__ void readback_kernel(const unsigned long long* src, uint64_t n, const
 // or from the flat array) `down` <= 10 levels down; a block takes 1024
 // entries of level top, halves them `down` times in shared memory and adds
 // its even entries of each level into zeros with one atomic per level.
-__global__ void __launch_bounds__(256) fold_levels_kernel(uint64_t* flat, const unsigned long long* leaves,
-                                                          uint32_t top, uint32_t down, unsigned long long* zeros) {
+__global__ void __launch_bounds__(256) fold_levels_kernel(uint64_t* flat, uint64_t* flat_dev,
+                                                          const unsigned long long* leaves, uint32_t top,
+                                                          uint32_t down, unsigned long long* zeros) {
   __shared__ uint64_t v[1024];
   __shared__ unsigned long long s_even;
   const uint64_t n_top = 1ull << top;
   const uint64_t base = uint64_t(blockIdx.x) * 1024;
-  const uint64_t* src = leaves ? reinterpret_cast<const uint64_t*>(leaves) : flat + (n_top - 1);
+  const uint64_t* src = leaves ? reinterpret_cast<const uint64_t*>(leaves) : (flat_dev ? flat_dev : flat) + (n_top - 1);
   for (int i = threadIdx.x; i < 1024; i += 256) {
     const uint64_t x = base + i < n_top ? src[base + i] : 0;
     v[i] = x;
-    if (leaves && base + i < n_top) flat[n_top - 1 + base + i] = x;
+    if (leaves && base + i < n_top) {
+      flat[n_top - 1 + base + i] = x;
+      if (flat_dev) flat_dev[n_top - 1 + base + i] = x;
+    }
   }
   __syncthreads();
   for (uint32_t d = 1; d <= down; ++d) {
@@ -712,7 +896,10 @@ __global__ void __launch_bounds__(256) fold_levels_kernel(uint64_t* flat, const 
       const uint32_t i = threadIdx.x + 256u * r;
       if (i < k) {
         v[i] = sums[r];
-        if (b_m + i < n_m) flat[n_m - 1 + b_m + i] = sums[r];
+        if (b_m + i < n_m) {
+          flat[n_m - 1 + b_m + i] = sums[r];
+          if (flat_dev) flat_dev[n_m - 1 + b_m + i] = sums[r];
+        }
       }
     }
     if (threadIdx.x == 0 && s_even) atomicAdd(&zeros[m], s_even);
@@ -925,10 +1112,55 @@ void launch_regroup(const uint64_t* matrix_level, uint64_t* tree_level, uint64_t
                     const uint64_t* seg_matrix, uint64_t nseg, uint32_t* status, cudaStream_t s, uint64_t* launches) {
   const uint64_t nwords = (nbits + 63) >> 6;
   if (nwords == 0) return;
+  if (nseg * 64 > nbits && nbits <= (uint64_t(1) << 22)) {  // groups of under 64 bits on average
+    regroup_bits_kernel<<<unsigned((nwords * 64 + 255) / 256), 256, 0, s>>>(
+        matrix_level, reinterpret_cast<uint32_t*>(tree_level), nbits, seg_tree, seg_matrix, nseg, status);
+    ++*launches;
+    return;
+  }
   const uint64_t threads = (nwords + kRegroupWords - 1) / kRegroupWords;
   regroup_kernel<<<unsigned((threads + 255) / 256), 256, 0, s>>>(matrix_level, tree_level, nbits, seg_tree, seg_matrix,
                                                                  nseg, status);
   ++*launches;
+}
+
+static uint64_t regroup_seg_chunks(uint32_t m) { return ((uint64_t(1) << m) + kSegChunk - 1) / kSegChunk; }
+
+uint64_t regroup_segs_offset(const uint32_t* levels, uint32_t i) {
+  uint64_t o = 0;
+  for (uint32_t k = 0; k < i; ++k) o += uint64_t(2) << levels[k];
+  return o;
+}
+
+uint64_t regroup_segs_words(const uint32_t* levels, uint32_t count) { return regroup_segs_offset(levels, count); }
+
+uint64_t regroup_segs_scratch_words(const uint32_t* levels, uint32_t count) {
+  uint64_t c = 0;
+  for (uint32_t k = 0; k < count; ++k) c += regroup_seg_chunks(levels[k]);
+  return 2 * c;
+}
+
+bool launch_regroup_segs(const uint64_t* flat, const uint32_t* levels, uint32_t count, uint64_t* out,
+                         uint64_t* scratch, cudaStream_t s, uint64_t* launches) {
+  if (count == 0) return true;
+  if (count > kSegMaxLevels) return false;
+  RegroupSegPlan p{};
+  p.count = count;
+  uint64_t blocks = 0;
+  for (uint32_t k = 0; k < count; ++k) {
+    if (levels[k] < 1 || levels[k] > 31) return false;
+    p.m[k] = levels[k];
+    p.chunk0[k] = uint32_t(blocks);
+    p.out[k] = regroup_segs_offset(levels, k);
+    blocks += regroup_seg_chunks(levels[k]);
+  }
+  if (blocks >= (uint64_t(1) << 31)) return false;
+  p.chunk0[count] = uint32_t(blocks);
+  regroup_seg_sums_kernel<<<unsigned(blocks), kSegThreads, 0, s>>>(flat, p, scratch);
+  regroup_seg_offsets_kernel<<<count, kSegThreads, 0, s>>>(p, scratch);
+  regroup_seg_write_kernel<<<unsigned(blocks), kSegThreads, 0, s>>>(flat, p, scratch, out);
+  *launches += 3;
+  return true;
 }
 
 template <typename T, typename K>
@@ -1018,13 +1250,13 @@ void launch_widen40(const void* in, uint64_t n, uint32_t* out, cudaStream_t s, u
 }
 
 void launch_fold_levels(const unsigned long long* hist, uint32_t levels, uint64_t* flat, unsigned long long* zeros,
-                        cudaStream_t s, uint64_t* launches) {
+                        cudaStream_t s, uint64_t* launches, uint64_t* flat_dev) {
   uint32_t top = levels;
   bool first = true;
   for (;;) {
     const uint32_t down = top < 10u ? top : 10u;
     const uint64_t blocks = ((1ull << top) + 1023) / 1024;
-    fold_levels_kernel<<<unsigned(blocks), 256, 0, s>>>(flat, first ? hist : nullptr, top, down, zeros);
+    fold_levels_kernel<<<unsigned(blocks), 256, 0, s>>>(flat, flat_dev, first ? hist : nullptr, top, down, zeros);
     ++*launches;
     first = false;
     if (down == top) break;  // level 0 written

@@ -30,10 +30,11 @@ uint32_t tile_hist_tiles_per_block();
 // 2^32 and more become 0xFFFFFFFF).
 void launch_widen40(const void* in, uint64_t n, uint32_t* out, cudaStream_t s, uint64_t* launches);
 // Prefix counts of levels 0..levels from the leaf histogram into `flat`
-// (level m at offset 2^m - 1; host-mapped memory allowed), the zero bits of
-// each level added into zeros[0..levels) (zeroed by the caller).
+// (level m at offset 2^m - 1; host-mapped memory allowed) and, when given,
+// the same into device memory `flat_dev`; the zero bits of each level added
+// into zeros[0..levels) (zeroed by the caller).
 void launch_fold_levels(const unsigned long long* hist, uint32_t levels, uint64_t* flat, unsigned long long* zeros,
-                        cudaStream_t s, uint64_t* launches);
+                        cudaStream_t s, uint64_t* launches, uint64_t* flat_dev = nullptr);
 // dst[0..n) = src[0..n), dst[n] = *status (dst: host-mapped memory).
 void launch_readback(const unsigned long long* src, uint64_t n, const uint32_t* status, uint64_t* dst,
                      cudaStream_t s, uint64_t* launches);
@@ -155,6 +156,19 @@ void launch_tile_pass(uint32_t key_bytes, uint32_t out_bytes, int K, bool out, c
 // seg_tree/seg_matrix: nseg (>=1) group starts sorted by seg_tree, seg_tree[0] == 0.
 void launch_regroup(const uint64_t* matrix_level, uint64_t* tree_level, uint64_t nbits, const uint64_t* seg_tree,
                     const uint64_t* seg_matrix, uint64_t nseg, uint32_t* status, cudaStream_t s, uint64_t* launches);
+// The segments of the regroup of levels[0..count) (each 1..23, ascending not
+// required) from the device prefix counts `flat` (level m at 2^m - 1, as
+// launch_fold_levels writes them): at out + regroup_segs_offset(levels, i),
+// level m = levels[i] gets 2^m group starts in the tree level (natural
+// prefix order) followed by the 2^m starts of the same groups in the matrix
+// level (key order: the bit-reversed prefix), empty groups included.
+// scratch: regroup_segs_scratch_words(levels, count) words.  False (nothing
+// launched) for more than 32 levels or a level outside 1..31.
+uint64_t regroup_segs_words(const uint32_t* levels, uint32_t count);
+uint64_t regroup_segs_offset(const uint32_t* levels, uint32_t i);
+uint64_t regroup_segs_scratch_words(const uint32_t* levels, uint32_t count);
+bool launch_regroup_segs(const uint64_t* flat, const uint32_t* levels, uint32_t count, uint64_t* out,
+                         uint64_t* scratch, cudaStream_t s, uint64_t* launches);
 
 // ---- Huffman keys -------------------------------------------------------------
 // key = ((code << 1) | 1) << (levels - len) for every text symbol, in keys

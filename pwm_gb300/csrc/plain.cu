@@ -163,7 +163,8 @@ struct PassChunks {
 // is enqueued, and after_pass(passes.size()) once the regroup is.
 void run_tile_passes(pwmgpu_ctx* ctx, const void* in, uint32_t width, uint32_t L,
                      const std::vector<TilePassHost>& passes, const std::vector<uint32_t>& regroup,
-                     const LevelTables& tabs, Structure& wm, Structure* wt, const TileFirstPass* first = nullptr,
+                     const uint64_t* d_segs, const LevelTables& tabs, Structure& wm, Structure* wt,
+                     const TileFirstPass* first = nullptr,
                      const std::function<void(size_t)>& after_pass = {}, size_t from = 0,
                      const PassChunks* chunks = nullptr) {
   cudaStream_t s = ctx->stream;
@@ -180,24 +181,15 @@ void run_tile_passes(pwmgpu_ctx* ctx, const void* in, uint32_t width, uint32_t L
     if (after_pass) after_pass(pi);
   }
 
-  if (wt && !regroup.empty()) {
-    size_t seg_words = 0;
-    for (uint32_t m : regroup) seg_words += 2 * tabs.seg_tree[m].size();
-    std::vector<uint64_t> segs;
-    segs.reserve(seg_words);
-    for (uint32_t m : regroup) {
-      segs.insert(segs.end(), tabs.seg_tree[m].begin(), tabs.seg_tree[m].end());
-      segs.insert(segs.end(), tabs.seg_matrix[m].begin(), tabs.seg_matrix[m].end());
-    }
-    uint64_t* d_segs = static_cast<uint64_t*>(ctx->grow("segs", std::max<size_t>(seg_words, 1) * 8));
-    CUDA_TRY(cudaMemcpyAsync(d_segs, segs.data(), seg_words * 8, cudaMemcpyHostToDevice, s));
-    size_t off = 0;
-    for (uint32_t m : regroup) {
-      const uint64_t ns = tabs.seg_tree[m].size();
+  if (wt && !regroup.empty()) {  // d_segs: every group of each level (launch_regroup_segs)
+    if (!d_segs) throw Fail{PWMGPU_ERR_CUDA, "internal: the regroup has no segments"};
+    for (uint32_t i = 0; i < uint32_t(regroup.size()); ++i) {
+      const uint32_t m = regroup[i];
+      const uint64_t ns = uint64_t(1) << m;
+      const uint64_t* seg = d_segs + regroup_segs_offset(regroup.data(), i);
       ProfScope ps(ctx, "regroup", 2 * words_for(wm.bits[m]) * 8);
-      launch_regroup(wm.d_words + wm.offs[m], wt->d_words + wt->offs[m], wm.bits[m], d_segs + off, d_segs + off + ns,
-                     ns, ctx->d_status, s, &ctx->launches);
-      off += 2 * ns;
+      launch_regroup(wm.d_words + wm.offs[m], wt->d_words + wt->offs[m], wm.bits[m], seg, seg + ns, ns,
+                     ctx->d_status, s, &ctx->launches);
     }
     CUDA_TRY(cudaGetLastError());
   }
@@ -309,6 +301,11 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   auto* h_status = reinterpret_cast<uint32_t*>(h_flat + flat_words + L);
   const uint64_t* h_digits = h_flat + flat_words + L + 1;
   auto* d_level_zeros = static_cast<unsigned long long*>(ctx->grow("level_zeros", uint64_t(L) * 8));
+  // a tree's prefix counts also in device memory: the regroup's segments
+  // (every group of a level, in both orders) are derived from them there
+  uint64_t* d_flat = tile_engine && want_tree && !digit_plan
+                         ? static_cast<uint64_t*>(ctx->grow("flat_dev", flat_words * 8))
+                         : nullptr;
   auto* h_rows = static_cast<uint64_t*>(
       ctx->grow_pinned(uint64_t(kMaxStreamChunks) * (uint64_t(1) << kTileGivenMaxLevels) * 8));
   // words of each structure already streamed to the host (a prefix of level 0)
@@ -392,7 +389,7 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   if (!digit_plan) {
     // prefix counts, zero bits and the status word to the host
     CUDA_TRY(cudaMemsetAsync(d_level_zeros, 0, uint64_t(L) * 8, s));
-    launch_fold_levels(d_hist, L, d_flat_host, d_level_zeros, s, &ctx->launches);
+    launch_fold_levels(d_hist, L, d_flat_host, d_level_zeros, s, &ctx->launches, d_flat);
     launch_readback(d_level_zeros, L, ctx->d_status, d_flat_host + flat_words, s, &ctx->launches);
   }
   CUDA_TRY(cudaEventRecord(ctx->hist_event(), s));
@@ -493,6 +490,7 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   std::vector<PassPlan> plan;
   std::vector<TilePassHost> tile_passes;
   std::vector<uint32_t> regroup;
+  uint64_t* d_segs = nullptr;  // the regroup's segments (device)
   PrefixCounts cnt;  // natural-prefix counts per level
   const uint32_t w = wx->width;
   auto tile_keys = [&](uint32_t l) { return tile_pass_elems(tile_pass_key_bytes(w, L, l)); };
@@ -505,7 +503,15 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   } else if (tile_engine) {
     cnt = PrefixCounts::view(h_flat, L);
     tile_passes = plan_tile_passes(cnt, L, kmax, tile_keys, want_tree, &regroup);
-    tabs = build_tables_tile(cnt, L, want_tree ? regroup : std::vector<uint32_t>{}, h_zeros);
+    tabs = build_tables_tile(cnt, L, {}, h_zeros);
+    if (want_tree && !regroup.empty()) {
+      const auto nr = uint32_t(regroup.size());
+      const uint64_t words = regroup_segs_words(regroup.data(), nr);
+      d_segs = static_cast<uint64_t*>(
+          ctx->grow("regroup_segs", (words + regroup_segs_scratch_words(regroup.data(), nr)) * 8));
+      if (!d_flat || !launch_regroup_segs(d_flat, regroup.data(), nr, d_segs, d_segs + words, s, &ctx->launches))
+        throw Fail{PWMGPU_ERR_CUDA, "internal: regroup segments"};
+    }
   } else {
     plan = plan_passes(L, ctx->pass_levels);
     tabs = build_tables_plain(std::vector<uint64_t>(h_hist, h_hist + bins), L, plan, want_tree);
@@ -690,7 +696,7 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   };
   if (tile_engine) {
     if (from == 1) hook(0);
-    run_tile_passes(ctx, next_in, wx->width, L, tile_passes, regroup, tabs, wx->wm, want_tree ? &wx->wt : nullptr,
+    run_tile_passes(ctx, next_in, wx->width, L, tile_passes, regroup, d_segs, tabs, wx->wm, want_tree ? &wx->wt : nullptr,
                     first.blockpre ? &first : nullptr, std::function<void(size_t)>(hook), from,
                     chunk_stream ? &chunks : nullptr);
   }

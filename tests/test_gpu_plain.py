@@ -102,6 +102,18 @@ def test_all_level_counts(pg, orc):
             assert_same(ws, orc.build(text, L, tree, "ps"), L, tree)
 
 
+def test_deep_trees_of_tiny_texts(pg, orc):
+    # nearly every prefix group of the regrouped tree levels is empty: the
+    # device derives the segments of all 2^m groups of each level
+    rng = np.random.default_rng(17)
+    for L in (17, 20, 24):
+        for n in (1, 2, 63, 64, 65, 1000):
+            text = rng.integers(0, 1 << L, n).astype(np.uint32)
+            for tree in (False, True):
+                ws = pg.wx_ps(np.uint32, tree).compute(text, n, L)
+                assert_same(ws, orc.build(text, L, tree, "ps"), L, tree)
+
+
 def test_skewed_and_constant_texts(pg, orc):
     texts = [np.zeros(50_000, np.uint8), np.full(40_000, 255, np.uint8),
              np.repeat(np.arange(256, dtype=np.uint8), 300), np.tile(np.array([0, 255], np.uint8), 30_000)]
