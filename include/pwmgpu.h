@@ -244,6 +244,12 @@ PWMGPU_API pwmgpu_status pwmgpu_wx_query(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, i
  * returns when out[] holds the answers. */
 PWMGPU_API pwmgpu_status pwmgpu_wx_query_host(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which, int op,
                                               const uint64_t* a, const uint64_t* b, uint64_t count, uint64_t* out);
+/* A mixed batch on host arrays: query i is of kind ops[i] (PWMGPU_Q_*) with
+ * operands a[i], b[i] (b may be NULL when every query is an ACCESS); one
+ * upload, one launch, one download.  Plain (not Huffman-shaped) structures. */
+PWMGPU_API pwmgpu_status pwmgpu_wx_query_batch_host(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which,
+                                                    const uint8_t* ops, const uint64_t* a, const uint64_t* b,
+                                                    uint64_t count, uint64_t* out);
 /* pwm's reduce_alphabet (include/util/alphabet_util.hpp:18-45) on the
  * device: the symbols of d_text renumbered 0, 1, ... in order of first
  * occurrence into d_out (same width; d_out == d_text allowed); *max_char

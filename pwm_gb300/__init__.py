@@ -528,6 +528,18 @@ class DeviceStructure:
                                                     ctypes.c_void_p(int(d_b)) if d_b is not None else None,
                                                     int(count), ctypes.c_void_p(int(d_out))))
 
+    def query_batch_host(self, which, ops, a, b=None):
+        """A mixed batch of queries on host arrays (pwmgpu_wx_query_batch_host):
+        query i is of kind ops[i] with operands a[i], b[i]; returns the answers."""
+        ops = np.ascontiguousarray(ops, dtype=np.uint8)
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        b = np.ascontiguousarray(b, dtype=np.uint64) if b is not None else None
+        out = np.zeros(max(a.size, 1), dtype=np.uint64)
+        self.ctx.check(self.ctx.lib.pwmgpu_wx_query_batch_host(self.ctx.h, self.h, int(which), ops.ctypes.data,
+                                                               a.ctypes.data, b.ctypes.data if b is not None else None,
+                                                               a.size, out.ctypes.data))
+        return out[:a.size]
+
     def free(self):
         if getattr(self, "h", None):
             self.ctx.lib.pwmgpu_wx_free(self.h)

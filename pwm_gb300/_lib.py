@@ -85,6 +85,7 @@ SIGNATURES = {
     "pwmgpu_wx_query": (i32, [vp, vp, i32, i32, vp, vp, u64, vp]),
     "pwmgpu_wx_free": (None, [vp]),
     "pwmgpu_wx_query_host": (i32, [vp, vp, i32, i32, vp, vp, u64, vp]),
+    "pwmgpu_wx_query_batch_host": (i32, [vp, vp, i32, vp, vp, vp, u64, vp]),
     "pwmgpu_ctx_set_stream_ordered_alloc": (i32, [vp, i32]),
     "pwmgpu_server_create": (i32, [i32, u64, u32, ctypes.POINTER(vp)]),
     "pwmgpu_server_submit": (i32, [vp, ctypes.POINTER(Request), u64p]),

@@ -408,6 +408,36 @@ pwmgpu_status pwmgpu_wx_query_host(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int whi
   });
 }
 
+pwmgpu_status pwmgpu_wx_query_batch_host(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, int which, const uint8_t* ops,
+                                         const uint64_t* a, const uint64_t* b, uint64_t count, uint64_t* out) {
+  if (!ctx || !wx || (count && (!ops || !a || !out))) return PWMGPU_ERR_ARG;
+  if (count == 0) return PWMGPU_OK;
+  for (uint64_t i = 0; i < count; ++i)
+    if (ops[i] > PWMGPU_Q_SELECT || (ops[i] != PWMGPU_Q_ACCESS && !b)) return PWMGPU_ERR_ARG;
+  const Structure& s = which ? wx->wt : wx->wm;
+  if (!s.present || !s.rs || (which == 0 && wx->wm_internal))
+    return fail(ctx, PWMGPU_ERR_ARG, "queries need a structure with rank/select");
+  if (s.huffman) return fail(ctx, PWMGPU_ERR_ARG, "mixed query batches need a plain structure");
+  return guarded(ctx, [&]() {
+    // a, b, the answers, then the kinds
+    auto* d = static_cast<uint64_t*>(ctx->grow("query_io", count * 3 * 8 + count));
+    auto* d_ops = reinterpret_cast<uint8_t*>(d + 3 * count);
+    cudaStream_t st = ctx->stream;
+    CUDA_TRY(cudaMemcpyAsync(d, a, count * 8, cudaMemcpyHostToDevice, st));
+    if (b) CUDA_TRY(cudaMemcpyAsync(d + count, b, count * 8, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_ops, ops, count, cudaMemcpyHostToDevice, st));
+    QueryStructure q{s.levels, s.is_tree ? 1u : 0u, s.n, s.d_q_levels, s.d_zeros};
+    {
+      ProfScope ps(ctx, "queries", count * 25);
+      launch_queries(q, 0, d, d + count, count, d + 2 * count, st, &ctx->launches, d_ops);
+    }
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(out, d + 2 * count, count * 8, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return PWMGPU_OK;
+  });
+}
+
 pwmgpu_status pwmgpu_reduce_alphabet(pwmgpu_ctx* ctx, const void* d_text, uint64_t size, uint32_t word_width,
                                      void* d_out, uint64_t* max_char) {
   if (!ctx || !max_char || (size && (!d_text || !d_out))) return PWMGPU_ERR_ARG;

@@ -216,8 +216,9 @@ struct QueryStructure {
   const QueryLevel* lv;        // device array of `levels`
   const uint64_t* zeros;       // device array of `levels` (matrix)
 };
+// ops: each query's kind (a mixed batch), or null for `op` throughout.
 void launch_queries(const QueryStructure& q, int op, const uint64_t* a, const uint64_t* b, uint64_t count,
-                    uint64_t* out, cudaStream_t s, uint64_t* launches);
+                    uint64_t* out, cudaStream_t s, uint64_t* launches, const uint8_t* ops = nullptr);
 
 // Code table of a Huffman-shaped structure, as its queries read it.
 struct HuffQueryTables {

@@ -313,10 +313,13 @@ __device__ uint64_t q_select(const QueryLevel& L, int value, uint64_t occ) {
 
 __device__ __forceinline__ bool bit_at(const uint64_t* d, uint64_t i) { return (d[i >> 6] >> (63 - (i & 63))) & 1; }
 
-__global__ void query_kernel(QueryStructure q, int op, const uint64_t* __restrict__ a, const uint64_t* __restrict__ b,
-                             uint64_t count, uint64_t* __restrict__ out) {
+// ops: the kind of each query (a mixed batch), or null for `op` throughout.
+__global__ void query_kernel(QueryStructure q, int op0, const uint8_t* __restrict__ ops,
+                             const uint64_t* __restrict__ a, const uint64_t* __restrict__ b, uint64_t count,
+                             uint64_t* __restrict__ out) {
   const uint32_t Lv = q.levels;
   for (uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < count; t += uint64_t(gridDim.x) * blockDim.x) {
+    const int op = ops ? int(ops[t]) : op0;
     uint64_t result = 0;
     if (op == 0 && a[t] >= q.n) {  // access past the text
       result = ~0ull;
@@ -614,11 +617,11 @@ void launch_rank_select(const RankSelectLevel* host_levels, uint32_t count, Rank
 }
 
 void launch_queries(const QueryStructure& q, int op, const uint64_t* a, const uint64_t* b, uint64_t count,
-                    uint64_t* out, cudaStream_t s, uint64_t* launches) {
+                    uint64_t* out, cudaStream_t s, uint64_t* launches, const uint8_t* ops) {
   if (count == 0) return;
   uint64_t blocks = (count + 127) / 128;
   if (blocks > 65535) blocks = 65535;
-  query_kernel<<<unsigned(blocks), 128, 0, s>>>(q, op, a, b, count, out);
+  query_kernel<<<unsigned(blocks), 128, 0, s>>>(q, op, ops, a, b, count, out);
   ++*launches;
 }
 

@@ -99,31 +99,16 @@ struct pwmgpu_server {
 namespace {
 
 // Answers a batch of queries against a resident structure on one context:
-// grouped by kind (one launch each), answers scattered back to request order.
+// the mixed batch in one launch, answers in request order.
 void answer(pwmgpu_ctx* ctx, pwmgpu_wx* wx, uint32_t which, uint64_t count, const uint8_t* ops, const uint64_t* qa,
             const uint64_t* qb, uint64_t* results) {
   if (count == 0) return;
-  std::vector<uint64_t> idx[3];
   for (uint64_t i = 0; i < count; ++i) {
     if (ops[i] > PWMGPU_Q_SELECT) throw std::runtime_error("unknown query kind");
-    idx[ops[i]].push_back(i);
+    if (ops[i] != PWMGPU_Q_ACCESS && !qb) throw std::runtime_error("rank and select queries need query_b");
   }
-  std::vector<uint64_t> ha, hb, ho;
-  for (int op = 0; op < 3; ++op) {
-    const uint64_t c = idx[op].size();
-    if (!c) continue;
-    if (op > 0 && !qb) throw std::runtime_error("rank and select queries need query_b");
-    ha.resize(c);
-    hb.resize(c);
-    ho.resize(c);
-    for (uint64_t k = 0; k < c; ++k) {
-      ha[k] = qa[idx[op][k]];
-      hb[k] = qb ? qb[idx[op][k]] : 0;
-    }
-    if (pwmgpu_wx_query_host(ctx, wx, int(which), op, ha.data(), hb.data(), c, ho.data()) != PWMGPU_OK)
-      throw std::runtime_error(pwmgpu_ctx_last_error(ctx));
-    for (uint64_t k = 0; k < c; ++k) results[idx[op][k]] = ho[k];
-  }
+  if (pwmgpu_wx_query_batch_host(ctx, wx, int(which), ops, qa, qb, count, results) != PWMGPU_OK)
+    throw std::runtime_error(pwmgpu_ctx_last_error(ctx));
 }
 
 }  // namespace
