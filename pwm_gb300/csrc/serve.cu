@@ -66,10 +66,12 @@ uint64_t structure_bytes(uint64_t n, uint32_t levels, uint32_t flags) {
 }
 
 // Transient device bytes of a build: the text, the key sequences of the split
-// passes, histograms and tables, queries and answers.
+// passes, histograms and tables (per symbol value 8 bytes of leaf histogram,
+// 16 of prefix counts of every level and up to 16 of a tree's regroup
+// segments, rounded up to 48), queries and answers.
 uint64_t build_scratch_bytes(uint64_t n, uint32_t width, uint32_t levels, uint64_t nq) {
-  return 3 * n * width + (uint64_t(8) << std::min<uint32_t>(levels, 24)) * 4 + (n / 1024 + 64) * 256 +
-         nq * 24 + (uint64_t(16) << 20);
+  return 3 * n * width + (uint64_t(8) << std::min<uint32_t>(levels, 24)) * 6 + (n / 1024 + 64) * 256 +
+         nq * 25 + (uint64_t(16) << 20);
 }
 
 }  // namespace
