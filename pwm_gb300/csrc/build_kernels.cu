@@ -552,6 +552,45 @@ __global__ void __launch_bounds__(256) regroup_bits_kernel(const uint64_t* __res
   if ((threadIdx.x & 31) == 0) tree_halves[2 * (pos >> 6) + ((pos & 32) ? 0 : 1)] = __brev(m);
 }
 
+// ---- every pass's digit counts from the prefix counts ---------------------------
+// digits[16 p + r]: the symbols whose bits of levels l..l+K-1 of pass p
+// (level l's most significant) read r: the natural prefix counts of level
+// l+K summed by their last K bits.  Blocks take chunks of kDigitChunk counts
+// of one pass; a thread's counts share one residue (the stride is a multiple
+// of 16), lanes 16 apart share it too.
+constexpr uint32_t kDigitThreads = 256, kDigitChunk = kDigitThreads * 16;
+
+struct FlatDigitPlan {
+  uint32_t count;
+  uint32_t top[kPassDigitsMaxPasses];  // level l+K of each pass
+  uint32_t K[kPassDigitsMaxPasses];
+  uint32_t chunk0[kPassDigitsMaxPasses + 1];
+};
+
+__global__ void __launch_bounds__(kDigitThreads) flat_digits_kernel(const uint64_t* __restrict__ flat,
+                                                                    FlatDigitPlan p,
+                                                                    unsigned long long* __restrict__ digits) {
+  __shared__ unsigned long long s_d[16];
+  uint32_t i = 0;
+  while (i + 1 < p.count && p.chunk0[i + 1] <= blockIdx.x) ++i;
+  if (threadIdx.x < 16) s_d[threadIdx.x] = 0;
+  __syncthreads();
+  const uint64_t ne = 1ull << p.top[i];
+  const uint64_t* c = flat + (ne - 1);
+  const uint64_t x0 = uint64_t(blockIdx.x - p.chunk0[i]) * kDigitChunk + threadIdx.x;
+  uint64_t v = 0;
+#pragma unroll 4
+  for (uint32_t k = 0; k < kDigitChunk / kDigitThreads; ++k) {
+    const uint64_t x = x0 + uint64_t(k) * kDigitThreads;
+    if (x < ne) v += c[x];
+  }
+  v += __shfl_xor_sync(0xFFFFFFFFu, v, 16);
+  const uint32_t mask = (1u << p.K[i]) - 1u;
+  if ((threadIdx.x & 31) < 16 && v) atomicAdd(&s_d[threadIdx.x & mask], (unsigned long long)v);
+  __syncthreads();
+  if (threadIdx.x <= mask && s_d[threadIdx.x]) atomicAdd(&digits[16 * i + threadIdx.x], s_d[threadIdx.x]);
+}
+
 // ---- the regroup's segments, on the device -------------------------------------
 // Level m of the tree holds the groups of the m-bit natural prefixes in
 // natural order; the matrix level holds the same groups in key order (the
@@ -1122,6 +1161,27 @@ void launch_regroup(const uint64_t* matrix_level, uint64_t* tree_level, uint64_t
   regroup_kernel<<<unsigned((threads + 255) / 256), 256, 0, s>>>(matrix_level, tree_level, nbits, seg_tree, seg_matrix,
                                                                  nseg, status);
   ++*launches;
+}
+
+bool launch_flat_digits(const uint64_t* flat, uint32_t L, const uint32_t* level, const uint32_t* K, uint32_t count,
+                        unsigned long long* digits, cudaStream_t s, uint64_t* launches) {
+  if (count == 0) return true;
+  if (count > kPassDigitsMaxPasses) return false;
+  FlatDigitPlan p{};
+  p.count = count;
+  uint64_t blocks = 0;
+  for (uint32_t i = 0; i < count; ++i) {
+    if (K[i] < 1 || K[i] > 4 || level[i] + K[i] > L || L > 31) return false;
+    p.top[i] = level[i] + K[i];
+    p.K[i] = K[i];
+    p.chunk0[i] = uint32_t(blocks);
+    blocks += ((uint64_t(1) << p.top[i]) + kDigitChunk - 1) / kDigitChunk;
+  }
+  p.chunk0[count] = uint32_t(blocks);
+  if (cudaMemsetAsync(digits, 0, size_t(count) * 16 * 8, s) != cudaSuccess) return false;
+  flat_digits_kernel<<<unsigned(blocks), kDigitThreads, 0, s>>>(flat, p, digits);
+  ++*launches;
+  return true;
 }
 
 static uint64_t regroup_seg_chunks(uint32_t m) { return ((uint64_t(1) << m) + kSegChunk - 1) / kSegChunk; }

@@ -269,11 +269,13 @@ inline void matrix_pass_table(const std::vector<uint64_t>& digit, int K, bool ou
 // (empty without a tree).  Exclusive prefixes over all 2^m groups of a level
 // are built only for the levels of segmented passes (few groups); a
 // matrix-only pass needs only the counts of its own K bits, folded from one
-// level.
+// level, or given: digits[16 p + r] for pass p of plan_passes(L, kmax)
+// (launch_flat_digits; passes of at most 4 levels).
 template <typename TileKeys>
 inline std::vector<TilePassHost> plan_tile_passes(const PrefixCounts& cnt, uint32_t L, int kmax,
                                                   TileKeys tile_keys, bool want_tree,
-                                                  std::vector<uint32_t>* regroup) {
+                                                  std::vector<uint32_t>* regroup,
+                                                  const uint64_t* digits = nullptr) {
   const uint64_t n = cnt[0][0];
   std::vector<std::vector<uint64_t>> pren(L + 1), prek(L + 1);
   auto prefixes = [&](uint32_t m) {  // natural order (tree) and key order (matrix: reversed prefix)
@@ -285,6 +287,7 @@ inline std::vector<TilePassHost> plan_tile_passes(const PrefixCounts& cnt, uint3
     for (size_t x = 0; x < sz; ++x) prek[m][x + 1] = prek[m][x] + cnt[m][rev_bits_host(x, m)];
   };
   std::vector<TilePassHost> passes;
+  size_t pi = 0;
   for (const auto& pp : plan_passes(L, kmax)) {
     TilePassHost ps;
     ps.level = pp.level;
@@ -293,6 +296,7 @@ inline std::vector<TilePassHost> plan_tile_passes(const PrefixCounts& cnt, uint3
     const uint32_t l = pp.level;
     const int K = pp.K;
     const uint64_t groups = uint64_t(1) << l;
+    const size_t pass_index = pi++;
     const uint32_t T = tile_keys(l);
     ps.segmented = want_tree && (l == 0 || (groups <= 65536 && n >= groups * 4 * uint64_t(T)));
     const int TS = tile_table_size(K);
@@ -324,11 +328,15 @@ inline std::vector<TilePassHost> plan_tile_passes(const PrefixCounts& cnt, uint3
       // level l's most significant) over the whole text: the natural
       // prefixes of level l+K summed by their last K bits
       const uint32_t top = l + uint32_t(K);
-      const CountSpan c = cnt[top];
       const size_t R = size_t(1) << K;
       std::vector<uint64_t> low(R, 0);
-      for (size_t p = 0; p < c.size(); p += R)
-        for (size_t r = 0; r < R; ++r) low[r] += c[p + r];
+      if (digits && K <= 4) {  // (16 counts per pass)
+        for (size_t r = 0; r < R; ++r) low[r] = digits[16 * pass_index + r];
+      } else {
+        const CountSpan c = cnt[top];
+        for (size_t p = 0; p < c.size(); p += R)
+          for (size_t r = 0; r < R; ++r) low[r] += c[p + r];
+      }
       matrix_pass_table(low, K, ps.out, tab);
       add_segment(0, n, tab, 0);
       if (want_tree && regroup)
@@ -384,8 +392,9 @@ inline std::vector<uint64_t> matrix_pass_zeros(const uint64_t* digits, uint32_t 
 
 // The same with T keys per tile in every pass.
 inline std::vector<TilePassHost> plan_tile_passes(const PrefixCounts& cnt, uint32_t L, int kmax, uint32_t T,
-                                                  bool want_tree, std::vector<uint32_t>* regroup) {
-  return plan_tile_passes(cnt, L, kmax, [T](uint32_t) { return T; }, want_tree, regroup);
+                                                  bool want_tree, std::vector<uint32_t>* regroup,
+                                                  const uint64_t* digits = nullptr) {
+  return plan_tile_passes(cnt, L, kmax, [T](uint32_t) { return T; }, want_tree, regroup, digits);
 }
 
 // One run of a merge of shards (pwm's merge_bit_vectors, include/

@@ -144,6 +144,14 @@ void launch_pass_digits(const void* text, uint64_t n, uint32_t width, const Pass
                         unsigned long long* digits, unsigned int* done, uint32_t* status, uint64_t* out,
                         cudaStream_t s, uint64_t* launches);
 
+// Every pass's digit counts (16 per pass, pass i at 16 i: the symbols whose
+// bits of levels level[i]..level[i]+K[i]-1 read r, level[i]'s most
+// significant) from the device prefix counts `flat` of an L-level text
+// (level m at 2^m - 1).  digits is zeroed here.  False (nothing launched) for
+// more than kPassDigitsMaxPasses passes or K outside 1..4.
+bool launch_flat_digits(const uint64_t* flat, uint32_t L, const uint32_t* level, const uint32_t* K, uint32_t count,
+                        unsigned long long* digits, cudaStream_t s, uint64_t* launches);
+
 // The narrowest key width (1, 2 or 4 bytes) holding `bits` bits.
 uint32_t tile_key_bytes(uint32_t bits);
 // One tile pass over keys of key_bytes; a pass writing S_{l+K} (out) writes

@@ -273,7 +273,11 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   // the counts of their own digits, not a leaf histogram of 2^L bins
   // (plan_matrix_passes).
   const bool digit_plan = tile_engine && !want_tree && L > 8 && !wx->keep_hist && !stream_out;
-  const auto digit_shape = digit_plan ? plan_passes(L, kmax) : std::vector<PassPlan>{};
+  // A tree of more than 8 levels: the device also sums every pass's digit
+  // counts from the prefix counts (the planner's matrix-only passes would
+  // otherwise sum up to 2^L counts on the host: ~0.5 ms at 20 levels).
+  const bool tree_digits = tile_engine && want_tree && !digit_plan && L > 8;
+  const auto digit_shape = digit_plan || tree_digits ? plan_passes(L, kmax) : std::vector<PassPlan>{};
   auto* d_hist = digit_plan ? nullptr : static_cast<unsigned long long*>(ctx->grow("hist", bins * 8));
   if (!digit_plan) CUDA_TRY(cudaMemsetAsync(d_hist, 0, bins * 8, s));
   if (tile_engine && !tile_hist && Kz > 1)
@@ -294,7 +298,7 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   // zero bits, the status word and every pass's digit counts)
   const uint64_t NB0 = uint64_t(1) << D0;
   const uint64_t flat_words = digit_plan ? (uint64_t(2) << Kz) - 1 : (bins << 1) - 1;
-  uint64_t* h_flat = ctx->grow_mapped((flat_words + L + 1 + 16 * digit_shape.size()) * 8);
+  uint64_t* h_flat = ctx->grow_mapped((flat_words + L + 1 + 16 * digit_shape.size() + 1) * 8);
   uint64_t* d_flat_host = ctx->mapped_dev;
   uint64_t* h_hist = digit_plan ? nullptr : h_flat + bins - 1;
   const uint64_t* h_zeros = h_flat + flat_words;
@@ -303,6 +307,7 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
   auto* d_level_zeros = static_cast<unsigned long long*>(ctx->grow("level_zeros", uint64_t(L) * 8));
   // a tree's prefix counts also in device memory: the regroup's segments
   // (every group of a level, in both orders) are derived from them there
+  bool tree_digits_ok = false;  // h_digits holds every pass's digit counts of a tree
   uint64_t* d_flat = tile_engine && want_tree && !digit_plan
                          ? static_cast<uint64_t*>(ctx->grow("flat_dev", flat_words * 8))
                          : nullptr;
@@ -391,6 +396,19 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     CUDA_TRY(cudaMemsetAsync(d_level_zeros, 0, uint64_t(L) * 8, s));
     launch_fold_levels(d_hist, L, d_flat_host, d_level_zeros, s, &ctx->launches, d_flat);
     launch_readback(d_level_zeros, L, ctx->d_status, d_flat_host + flat_words, s, &ctx->launches);
+    if (tree_digits) {
+      std::vector<uint32_t> lv, kk;
+      for (const auto& ps : digit_shape) {
+        lv.push_back(ps.level);
+        kk.push_back(uint32_t(ps.K));
+      }
+      const uint64_t nd = 16 * lv.size();
+      auto* d_dg = static_cast<unsigned long long*>(ctx->grow("tree_digits", nd * 8));
+      tree_digits_ok = launch_flat_digits(d_flat, L, lv.data(), kk.data(), uint32_t(lv.size()), d_dg, s,
+                                          &ctx->launches);
+      if (tree_digits_ok)
+        launch_readback(d_dg, nd, ctx->d_status, d_flat_host + flat_words + L + 1, s, &ctx->launches);
+    }
   }
   CUDA_TRY(cudaEventRecord(ctx->hist_event(), s));
   // After the tile histogram the first pass needs nothing from the host but
@@ -502,7 +520,7 @@ void build_plain(pwmgpu_ctx* ctx, pwmgpu_wx* wx, const void* d_text, const HostI
     tabs.seg_matrix.resize(L);
   } else if (tile_engine) {
     cnt = PrefixCounts::view(h_flat, L);
-    tile_passes = plan_tile_passes(cnt, L, kmax, tile_keys, want_tree, &regroup);
+    tile_passes = plan_tile_passes(cnt, L, kmax, tile_keys, want_tree, &regroup, tree_digits_ok ? h_digits : nullptr);
     tabs = build_tables_tile(cnt, L, {}, h_zeros);
     if (want_tree && !regroup.empty()) {
       const auto nr = uint32_t(regroup.size());

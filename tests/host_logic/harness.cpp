@@ -98,6 +98,27 @@ static int plan(uint32_t L, bool tree, int kmax, uint32_t T) {
   const PrefixCounts cnt = fold_prefix_counts(hist.data(), L);
   std::vector<uint32_t> regroup;
   const auto passes = plan_tile_passes(cnt, L, kmax, T, tree, &regroup);
+  // the same plan from every pass's digit counts, summed from the leaves
+  // (what launch_flat_digits derives from the prefix counts on the device)
+  {
+    const auto shape = plan_passes(L, kmax);
+    std::vector<uint64_t> digits(16 * shape.size(), 0);
+    for (size_t s = 0; s < hist.size(); ++s)
+      for (size_t p = 0; p < shape.size(); ++p)
+        if (shape[p].K <= 4)
+          digits[16 * p + ((s >> (L - shape[p].level - uint32_t(shape[p].K))) & ((size_t(1) << shape[p].K) - 1))] +=
+              hist[s];
+    std::vector<uint32_t> regroup2;
+    const auto passes2 = plan_tile_passes(cnt, L, kmax, T, tree, &regroup2, digits.data());
+    bool same = regroup2 == regroup && passes2.size() == passes.size();
+    for (size_t p = 0; same && p < passes.size(); ++p)
+      same = passes2[p].table == passes[p].table && passes2[p].segs.size() == passes[p].segs.size() &&
+             passes2[p].tiles == passes[p].tiles;
+    if (!same) {
+      fprintf(stderr, "plan from digit counts differs\n");
+      return 3;
+    }
+  }
   const LevelTables t = build_tables_tile(cnt, L, tree ? regroup : std::vector<uint32_t>{});
   printf("zeros");
   for (uint64_t z : t.zeros) printf(" %llu", (unsigned long long)z);
