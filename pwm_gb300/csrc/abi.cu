@@ -3,6 +3,7 @@
 // builder, queries and alphabet reduction.  The build work itself lives in
 // plain.cu, huffman.cu and shards.cu; batches and generators in
 // batch_host.cu.
+#include <cstring>
 #include "engine.hpp"
 
 using namespace pwmgpu;
@@ -419,21 +420,27 @@ pwmgpu_status pwmgpu_wx_query_batch_host(pwmgpu_ctx* ctx, const pwmgpu_wx* wx, i
     return fail(ctx, PWMGPU_ERR_ARG, "queries need a structure with rank/select");
   if (s.huffman) return fail(ctx, PWMGPU_ERR_ARG, "mixed query batches need a plain structure");
   return guarded(ctx, [&]() {
-    // a, b, the answers, then the kinds
-    auto* d = static_cast<uint64_t*>(ctx->grow("query_io", count * 3 * 8 + count));
-    auto* d_ops = reinterpret_cast<uint8_t*>(d + 3 * count);
+    // a, b and the kinds staged in pinned memory and uploaded in one copy;
+    // on the device the answers follow them (8-byte aligned)
+    const uint64_t in_bytes = count * 16 + count, out_off = count * 2 + (count + 7) / 8;
+    auto* h = static_cast<unsigned char*>(ctx->grow_pinned_named("query_io", std::max(in_bytes, count * 8)));
+    std::memcpy(h, a, count * 8);
+    if (b) std::memcpy(h + count * 8, b, count * 8);
+    else std::memset(h + count * 8, 0, count * 8);
+    std::memcpy(h + count * 16, ops, count);
+    auto* d = static_cast<uint64_t*>(ctx->grow("query_io", (out_off + count) * 8));
     cudaStream_t st = ctx->stream;
-    CUDA_TRY(cudaMemcpyAsync(d, a, count * 8, cudaMemcpyHostToDevice, st));
-    if (b) CUDA_TRY(cudaMemcpyAsync(d + count, b, count * 8, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(d_ops, ops, count, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d, h, in_bytes, cudaMemcpyHostToDevice, st));
     QueryStructure q{s.levels, s.is_tree ? 1u : 0u, s.n, s.d_q_levels, s.d_zeros};
     {
       ProfScope ps(ctx, "queries", count * 25);
-      launch_queries(q, 0, d, d + count, count, d + 2 * count, st, &ctx->launches, d_ops);
+      launch_queries(q, 0, d, d + count, count, d + out_off, st, &ctx->launches,
+                     reinterpret_cast<const uint8_t*>(d + 2 * count));
     }
     CUDA_TRY(cudaGetLastError());
-    CUDA_TRY(cudaMemcpyAsync(out, d + 2 * count, count * 8, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(h, d + out_off, count * 8, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
+    std::memcpy(out, h, count * 8);
     return PWMGPU_OK;
   });
 }
